@@ -1,0 +1,1257 @@
+// CPU oracle for the fluid simulation step (test infrastructure only).
+//
+// This file restates, in C++17, the simulation step of the Go package
+// pkg/fluid (TheFellow/fluid).  It is the checker for the CUDA path: only the
+// test-suite, the smoke entry and the CPU-baseline leg of the benchmark load
+// it, and nothing in the product links against it.
+//
+// Two kinds of restatement live here, selected per instance:
+//   * the reference scheme (Scheme::LexSOR): the exact operation order of
+//     pkg/fluid/fluid.go, including the serial lexicographic SOR pressure loop
+//     with its relaxation schedule and early exit (fluid.go:157-234), the
+//     stage order of Simulate (fluid.go:79-109) and the hidden newU/newV/newM
+//     staging state (fluid.go:291-434, walls.go:26-47);
+//   * the GPU scheme (Scheme::Jacobi / Scheme::RedBlack): the same step with
+//     the pressure loop replaced by the parallel relaxation the CUDA kernels
+//     run, with the identical per-cell operation order, so the FP32 GPU
+//     result can be compared bit for bit.
+// The template parameter T is float (FP32-faithful: Go's float32 arithmetic,
+// math.* evaluated in double and rounded back) or double (the FP64 oracle).
+//
+// Build with -O2 -ffp-contract=off and without -ffast-math: every float op is
+// a separately rounded IEEE op, which is what Go's compiler emits on amd64.
+//
+// Parity pin: the reference's own known-answer and threshold tests
+// (pkg/fluid/fluid_test.go, confinement_test.go) are ported under tests/ and
+// run against this oracle.  There is no Go toolchain to produce golden field
+// dumps, so bit-level agreement with the Go binary itself is unpinned.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <condition_variable>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <type_traits>
+#include <vector>
+
+namespace orc {
+
+enum Scheme { LexSOR = 0, Jacobi = 1, RedBlack = 2 };
+
+// ---------------------------------------------------------------------------
+// Thread pool standing in for parallelRange (pkg/fluid/parallel.go:10-39):
+// static contiguous chunks of [start,end) over the worker count.
+// ---------------------------------------------------------------------------
+class Pool {
+ public:
+  explicit Pool(int n) : n_(std::max(1, n)) {
+    for (int w = 1; w < n_; ++w) threads_.emplace_back([this, w] { loop(w); });
+  }
+  ~Pool() {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : threads_) t.join();
+  }
+  int size() const { return n_; }
+  void range(int start, int end, const std::function<void(int)>& fn) {
+    int total = end - start;
+    if (total <= 0) return;
+    int workers = std::min(n_, total);
+    if (workers == 1) {
+      for (int i = start; i < end; ++i) fn(i);
+      return;
+    }
+    int chunk = (total + workers - 1) / workers;
+    {
+      std::lock_guard<std::mutex> g(m_);
+      fn_ = &fn;
+      start_ = start;
+      end_ = end;
+      chunk_ = chunk;
+      workers_ = workers;
+      pending_ = workers - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    run_chunk(0);
+    std::unique_lock<std::mutex> lk(m_);
+    done_cv_.wait(lk, [this] { return pending_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  void run_chunk(int w) {
+    int s = start_ + w * chunk_;
+    int e = std::min(s + chunk_, end_);
+    for (int i = s; i < e; ++i) (*fn_)(i);
+  }
+  void loop(int w) {
+    uint64_t seen = 0;
+    for (;;) {
+      std::unique_lock<std::mutex> lk(m_);
+      cv_.wait(lk, [&] { return gen_ != seen; });
+      seen = gen_;
+      if (stop_) return;
+      bool mine = w < workers_;
+      lk.unlock();
+      if (mine) {
+        run_chunk(w);
+        std::lock_guard<std::mutex> g(m_);
+        if (--pending_ == 0) done_cv_.notify_all();
+      }
+    }
+  }
+  int n_;
+  std::vector<std::thread> threads_;
+  std::mutex m_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)>* fn_ = nullptr;
+  int start_ = 0, end_ = 0, chunk_ = 0, workers_ = 0, pending_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+// ---------------------------------------------------------------------------
+// Go semantics helpers.
+// ---------------------------------------------------------------------------
+// Go's builtin min/max on floats: NaN wins, and -0 < +0.
+template <typename T>
+inline T go_min(T a, T b) {
+  if (std::isnan(a) || std::isnan(b)) return std::numeric_limits<T>::quiet_NaN();
+  if (a == b) return std::signbit(a) ? a : b;
+  return a < b ? a : b;
+}
+template <typename T>
+inline T go_max(T a, T b) {
+  if (std::isnan(a) || std::isnan(b)) return std::numeric_limits<T>::quiet_NaN();
+  if (a == b) return std::signbit(a) ? b : a;
+  return a > b ? a : b;
+}
+// float32(math.Sqrt(float64(x))) / math.Sqrt for T=double.
+template <typename T>
+inline T go_sqrt(T x) { return (T)std::sqrt((double)x); }
+template <typename T>
+inline T go_abs(T x) { return (T)std::fabs((double)x); }
+
+struct Stats {
+  double div_l2_post = 0, div_max_post = 0, div_count_post = 0;
+  double resid_l2 = 0, resid_max = 0;
+  double smoke_mass = 0;
+  int sweeps = 0;
+  double last_maxdiv = 0;
+};
+
+template <typename T>
+struct Fluid {
+  T density, h;
+  int NX, NY, N;
+  std::vector<T> U, V, newU, newV, p, S, M, newM;
+  T Confinement = 0, ViscosityDiffusion = 0, PressureDamping = 1,
+    TurbulenceStrength = (T)0.02, SmokeAdvection = 1;
+  bool UseMultigrid = false;
+  int MultigridLevels = 2;
+  bool UseBFECC = false;
+  T Relaxation = (T)1.9;  // package var Relaxation (fluid.go:7-9)
+
+  // Extensions shared with the CUDA path.
+  int num_iters = 8;        // numIters, hard-coded to 8 in Simulate (fluid.go:81)
+  T tolerance = (T)1e-5;    // fluid.go:159
+  bool early_exit = true;
+  int scheme = LexSOR;
+  T jacobi_omega = 1;       // relaxation of the parallel schemes
+  int check_every = 1;      // early-exit check interval (sweeps) of the parallel schemes
+  int refine_sweeps = 0;    // FP64-residual outer correction sweeps (0 = off)
+
+  // Parallel-scheme work arrays.
+  std::vector<T> phi, phi2, rhs, err, err2;
+  std::vector<uint8_t> cnt;  // neighbour fluid count of active cells, 0 = inactive
+  Stats st;
+  Pool* pool;
+
+  Fluid(T density_, int width, int height, T h_, Pool* pool_)
+      : density(density_), h(h_), NX(width + 2), NY(height + 2),
+        N((width + 2) * (height + 2)), pool(pool_) {
+    U.assign(N, 0); V.assign(N, 0); newU.assign(N, 0); newV.assign(N, 0);
+    p.assign(N, 0); S.assign(N, 0); M.assign(N, 0); newM.assign(N, 0);
+  }
+  inline int ix(int i, int j) const { return i * NY + j; }
+  void par(int s, int e, const std::function<void(int)>& fn) { pool->range(s, e, fn); }
+
+  // ---------------------------------------------------------------- Simulate
+  // fluid.go:79-109
+  void simulate(T dt) {
+    int numIters = num_iters;
+    std::fill(p.begin(), p.end(), (T)0);
+    if (ViscosityDiffusion > 0) applyViscosity(dt);
+    makeIncompressible(numIters, dt);
+    if (Confinement != 0) applyVorticityConfinement(dt);
+    if (TurbulenceStrength > 0) addTurbulence(dt);
+    handleBorders();
+    if (UseBFECC) {
+      advectVelocityBFECC(dt);
+      advectSmokeBFECC(dt);
+    } else {
+      advectVelocity(dt);
+      advectSmoke(dt);
+    }
+    st.smoke_mass = smokeMass();
+  }
+
+  // fluid.go:112-142
+  void applyViscosity(T dt) {
+    if (ViscosityDiffusion <= 0) return;
+    int n = NY;
+    T visc = ViscosityDiffusion * dt;
+    newU = U;
+    newV = V;
+    par(1, NX - 1, [&](int i) {
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] > 0) {
+          T uLap = U[(i - 1) * n + j] + U[(i + 1) * n + j] + U[i * n + j - 1] +
+                   U[i * n + j + 1] - (T)4 * U[i * n + j];
+          newU[i * n + j] = U[i * n + j] + visc * uLap;
+          T vLap = V[(i - 1) * n + j] + V[(i + 1) * n + j] + V[i * n + j - 1] +
+                   V[i * n + j + 1] - (T)4 * V[i * n + j];
+          newV[i * n + j] = V[i * n + j] + visc * vLap;
+        }
+      }
+    });
+    U = newU;
+    V = newV;
+  }
+
+  // fluid.go:144-155
+  void makeIncompressible(int numIters, T dt) {
+    copyBorder(newU, U);
+    copyBorder(newV, V);
+    if (UseMultigrid && MultigridLevels > 1) {
+      solveMultigridVCycle(numIters, dt);
+    } else if (scheme == LexSOR) {
+      solveSingleGrid(numIters, dt);
+    } else {
+      solveParallel(numIters, dt);
+    }
+    postProjectionStats();
+  }
+
+  // fluid.go:157-186
+  void solveSingleGrid(int numIters, T dt) {
+    T cp = density * h / dt;
+    T tol = tolerance;
+    T initialRelaxation = Relaxation;
+    T minRelaxation = (T)1.2;
+    st.sweeps = 0;
+    for (int iter = 0; iter < numIters; ++iter) {
+      T iterProgress = (T)(unsigned)iter / (T)(unsigned)numIters;
+      T currentRelaxation =
+          initialRelaxation - (initialRelaxation - minRelaxation) * iterProgress;
+      T maxDiv = pressureJacobiIteration(currentRelaxation, cp);
+      st.sweeps = iter + 1;
+      st.last_maxdiv = maxDiv;
+      if (early_exit && maxDiv < tol) break;
+    }
+  }
+
+  // fluid.go:188-234 (serial, in place, lexicographic i-major then j)
+  T pressureJacobiIteration(T relaxation, T cp) {
+    int n = NY;
+    T maxDiv = 0;
+    for (int i = 1; i < NX - 1; ++i) {
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] == 0) continue;
+        T sx0 = S[(i - 1) * n + j];
+        T sx1 = S[(i + 1) * n + j];
+        T sy0 = S[i * n + j - 1];
+        T sy1 = S[i * n + j + 1];
+        T s = sx0 + sx1 + sy0 + sy1;
+        if (s == 0) continue;
+        T div = U[(i + 1) * n + j] - U[i * n + j] + V[i * n + j + 1] - V[i * n + j];
+        T absDiv = go_abs(div);
+        if (absDiv > maxDiv) maxDiv = absDiv;
+        T pp = -div / s;
+        pp *= relaxation;
+        pp *= PressureDamping;
+        p[i * n + j] += cp * pp;
+        U[i * n + j] -= sx0 * pp;
+        U[(i + 1) * n + j] += sx1 * pp;
+        V[i * n + j] -= sy0 * pp;
+        V[i * n + j + 1] += sy1 * pp;
+      }
+    }
+    return maxDiv;
+  }
+
+  // ---------------------------------------------------- parallel GPU schemes
+  // The masked Poisson system the SOR loop above relaxes, written for the
+  // cell potential phi (the accumulated per-cell velocity correction):
+  //   s_c phi_c - sum_{n} phi_n = b_c = -div_c,
+  // with phi = 0 on inactive cells (solid, border ring, no fluid neighbour),
+  // followed by U_face += S_R phi_L - S_L phi_R (and the same for V) and
+  // p = cp phi.  Jacobi and red-black relaxations of it run on the GPU.
+  void setupSystem() {
+    int n = NY;
+    phi.assign(N, 0); phi2.assign(N, 0); rhs.assign(N, 0); cnt.assign(N, 0);
+    par(1, NX - 1, [&](int i) {
+      for (int j = 1; j < NY - 1; ++j) {
+        int c = i * n + j;
+        if (S[c] == 0) continue;
+        T s = S[(i - 1) * n + j] + S[(i + 1) * n + j] + S[i * n + j - 1] + S[i * n + j + 1];
+        if (s == 0) continue;
+        T div = U[(i + 1) * n + j] - U[c] + V[c + 1] - V[c];
+        rhs[c] = -div;
+        cnt[c] = (uint8_t)s;
+      }
+    });
+  }
+  T omegaTable(int s) const {
+    T om = jacobi_omega * PressureDamping;
+    return om / (T)s;
+  }
+  // One relaxation sweep over cells of the given colour (-1 = all cells, a
+  // Jacobi sweep from src into dst; 0/1 = red-black half sweep in place with
+  // src == dst).  Returns the max |r| seen over the updated cells.
+  T sweep(const std::vector<T>& b, const std::vector<T>& src, std::vector<T>& dst,
+          int colour, T omega_scale) {
+    int n = NY;
+    T w[5];
+    for (int s = 1; s <= 4; ++s) w[s] = (omega_scale * PressureDamping) / (T)s;
+    std::vector<T> rowmax(NX, 0);
+    par(1, NX - 1, [&](int i) {
+      T mx = 0;
+      for (int j = 1; j < NY - 1; ++j) {
+        int c = i * n + j;
+        if (colour >= 0 && ((i + j) & 1) != colour) {
+          continue;
+        }
+        int s = cnt[c];
+        if (s == 0) {
+          dst[c] = 0;
+          continue;
+        }
+        T nb = src[c - n] + src[c + n] + src[c - 1] + src[c + 1];
+        T t1 = b[c] + nb;
+        T r = std::fma(-(T)s, src[c], t1);
+        T a = go_abs(r);
+        if (a > mx) mx = a;
+        dst[c] = std::fma(w[s], r, src[c]);
+      }
+      rowmax[i] = mx;
+    });
+    T mx = 0;
+    for (int i = 1; i < NX - 1; ++i)
+      if (rowmax[i] > mx) mx = rowmax[i];
+    return mx;
+  }
+  // Runs `iters` sweeps on x (ping-pong with tmp); early exit checked after
+  // sweeps whose count is a multiple of check_every.  Returns sweeps done.
+  int relax(const std::vector<T>& b, std::vector<T>& x, std::vector<T>& tmp, int iters,
+            bool allow_exit) {
+    int done = 0;
+    for (int t = 0; t < iters; ++t) {
+      T mx;
+      if (scheme == RedBlack) {
+        // Red-black SOR with the reference's relaxation schedule.
+        T prog = (T)(unsigned)t / (T)(unsigned)iters;
+        T om = Relaxation - (Relaxation - (T)1.2) * prog;
+        T m0 = sweep(b, x, x, 0, om);
+        T m1 = sweep(b, x, x, 1, om);
+        mx = m0 > m1 ? m0 : m1;
+      } else {
+        mx = sweep(b, x, tmp, -1, jacobi_omega);
+        std::swap(x, tmp);
+      }
+      done = t + 1;
+      st.last_maxdiv = mx;
+      if (allow_exit && early_exit && ((t + 1) % check_every) == 0 && mx < tolerance) break;
+    }
+    return done;
+  }
+  void solveParallel(int numIters, T dt) {
+    int n = NY;
+    T cp = density * h / dt;
+    setupSystem();
+    st.sweeps = relax(rhs, phi, phi2, numIters, true);
+    residualFP64();
+    if (refine_sweeps > 0) {
+      // Outer correction: FP64 residual of the FP32 iterate, a correction
+      // solve A e = r by the same relaxation, then phi += e.
+      std::vector<T> r(N, 0);
+      for (int c = 0; c < N; ++c)
+        if (cnt[c]) r[c] = (T)resid64_[c];
+      err.assign(N, 0); err2.assign(N, 0);
+      relax(r, err, err2, refine_sweeps, false);
+      for (int c = 0; c < N; ++c)
+        if (cnt[c]) phi[c] = phi[c] + err[c];
+      residualFP64();
+    }
+    // Gradient subtract + pressure.
+    par(1, NX, [&](int i) {
+      for (int j = 1; j < NY - 1; ++j) {
+        int c = i * n + j;
+        int cl = c - n;
+        if (cnt[cl] || (i < NX - 1 && cnt[c])) {
+          T d = S[c] * phi[cl] - S[cl] * phi[c];
+          U[c] = U[c] + d;
+        }
+      }
+    });
+    par(1, NX - 1, [&](int i) {
+      for (int j = 1; j < NY; ++j) {
+        int c = i * n + j;
+        int cb = c - 1;
+        if (cnt[cb] || (j < NY - 1 && cnt[c])) {
+          T d = S[c] * phi[cb] - S[cb] * phi[c];
+          V[c] = V[c] + d;
+        }
+      }
+    });
+    for (int c = 0; c < N; ++c) p[c] = cnt[c] ? cp * phi[c] : (T)0;
+  }
+  std::vector<double> resid64_;
+  void residualFP64() {
+    int n = NY;
+    resid64_.assign(N, 0.0);
+    double l2 = 0, mx = 0;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        int c = i * n + j;
+        if (!cnt[c]) continue;
+        double nb = (double)phi[c - n] + (double)phi[c + n] + (double)phi[c - 1] +
+                    (double)phi[c + 1];
+        double r = ((double)rhs[c] + nb) - (double)cnt[c] * (double)phi[c];
+        resid64_[c] = r;
+        l2 += r * r;
+        if (std::fabs(r) > mx) mx = std::fabs(r);
+      }
+    st.resid_l2 = std::sqrt(l2);
+    st.resid_max = mx;
+  }
+  void postProjectionStats() {
+    int n = NY;
+    double l2 = 0, mx = 0, cntc = 0;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        int c = i * n + j;
+        if (S[c] == 0) continue;
+        T div = U[c + n] - U[c] + V[c + 1] - V[c];
+        double d = (double)div;
+        l2 += d * d;
+        if (std::fabs(d) > mx) mx = std::fabs(d);
+        cntc += 1;
+      }
+    st.div_l2_post = std::sqrt(l2);
+    st.div_max_post = mx;
+    st.div_count_post = cntc;
+  }
+  double smokeMass() const {
+    double m = 0;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) m += (double)M[i * NY + j];
+    return m;
+  }
+
+  // fluid.go:236-289
+  void handleBorders() {
+    int n = NY;
+    par(0, NX, [&](int i) {
+      if (S[i * n + 0] == 0 || S[i * n + 1] == 0) {
+        U[i * n + 0] = 0;
+      } else {
+        if (i > 0 && i < NX - 1 && S[i * n + 2] > 0)
+          U[i * n + 0] = (T)2 * U[i * n + 1] - U[i * n + 2];
+        else
+          U[i * n + 0] = U[i * n + 1];
+      }
+      if (S[i * n + NY - 1] == 0 || S[i * n + NY - 2] == 0) {
+        U[i * n + NY - 1] = 0;
+      } else {
+        if (i > 0 && i < NX - 1 && S[i * n + NY - 3] > 0)
+          U[i * n + NY - 1] = (T)2 * U[i * n + NY - 2] - U[i * n + NY - 3];
+        else
+          U[i * n + NY - 1] = U[i * n + NY - 2];
+      }
+    });
+    par(0, NY, [&](int j) {
+      if (S[0 * n + j] == 0 || S[1 * n + j] == 0) {
+        V[0 * n + j] = 0;
+      } else {
+        if (j > 0 && j < NY - 1 && S[2 * n + j] > 0)
+          V[0 * n + j] = (T)2 * V[1 * n + j] - V[2 * n + j];
+        else
+          V[0 * n + j] = V[1 * n + j];
+      }
+      if (S[(NX - 1) * n + j] == 0 || S[(NX - 2) * n + j] == 0) {
+        V[(NX - 1) * n + j] = 0;
+      } else {
+        if (j > 0 && j < NY - 1 && S[(NX - 3) * n + j] > 0)
+          V[(NX - 1) * n + j] = (T)2 * V[(NX - 2) * n + j] - V[(NX - 3) * n + j];
+        else
+          V[(NX - 1) * n + j] = V[(NX - 2) * n + j];
+      }
+    });
+  }
+
+  // fluid.go:436-446
+  void copyBorder(std::vector<T>& dst, const std::vector<T>& src) {
+    int n = NY;
+    for (int i = 0; i < NX; ++i) {
+      dst[i * n + 0] = src[i * n + 0];
+      dst[i * n + NY - 1] = src[i * n + NY - 1];
+    }
+    for (int j = 0; j < NY; ++j) {
+      dst[0 * n + j] = src[0 * n + j];
+      dst[(NX - 1) * n + j] = src[(NX - 1) * n + j];
+    }
+  }
+
+  // fluid.go:335-347
+  inline T avgU(const std::vector<T>& Uf, int i, int j) const {
+    int n = NY;
+    return (Uf[i * n + j - 1] + Uf[i * n + j] + Uf[(i + 1) * n + j - 1] + Uf[(i + 1) * n + j]) *
+           (T)0.25;
+  }
+  inline T avgV(const std::vector<T>& Vf, int i, int j) const {
+    int n = NY;
+    return (Vf[(i - 1) * n + j] + Vf[i * n + j] + Vf[(i - 1) * n + j + 1] + Vf[i * n + j + 1]) *
+           (T)0.25;
+  }
+
+  // fluid.go:357-398 and fluid.go:1055-1091; fld: 0 = U, 1 = V, 2 = M
+  T sampleFrom(T x, T y, const std::vector<T>& data, int fld) const {
+    int n = NY;
+    T h1 = (T)1.0 / h;
+    T h2 = (T)0.5 * h;
+    x = go_max(go_min(x, (T)NX * h), h);
+    y = go_max(go_min(y, (T)NY * h), h);
+    T dx = 0, dy = 0;
+    if (fld == 0) dy = h2;
+    else if (fld == 1) dx = h2;
+    else { dx = h2; dy = h2; }
+    int x0 = std::min((int)std::floor((double)((x - dx) * h1)), NX - 1);
+    T tx = ((x - dx) - (T)x0 * h) * h1;
+    int x1 = std::min(x0 + 1, NX - 1);
+    int y0 = std::min((int)std::floor((double)((y - dy) * h1)), NY - 1);
+    T ty = ((y - dy) - (T)y0 * h) * h1;
+    int y1 = std::min(y0 + 1, NY - 1);
+    T sx = (T)1.0 - tx;
+    T sy = (T)1.0 - ty;
+    return sx * sy * data[x0 * n + y0] + tx * sy * data[x1 * n + y0] +
+           tx * ty * data[x1 * n + y1] + sx * ty * data[x0 * n + y1];
+  }
+
+  // fluid.go:291-333
+  void advectVelocity(T dt) {
+    copyBorder(newU, U);
+    copyBorder(newV, V);
+    int n = NY;
+    T hh = h;
+    T h2 = hh / (T)2;
+    par(1, NX, [&](int i) {
+      for (int j = 1; j < NY; ++j) {
+        if (S[i * n + j] != 0 && S[(i - 1) * n + j] != 0 && j < NY - 1) {
+          T x = (T)i * hh;
+          T y = (T)j * hh + h2;
+          T u = U[i * n + j];
+          T v = avgV(V, i, j);
+          x = x - dt * u;
+          y = y - dt * v;
+          newU[i * n + j] = sampleFrom(x, y, U, 0);
+        }
+        if (S[i * n + j] != 0 && S[i * n + j - 1] != 0 && i < NX - 1) {
+          T x = (T)i * hh + h2;
+          T y = (T)j * hh;
+          T u = avgU(U, i, j);
+          T v = V[i * n + j];
+          x = x - dt * u;
+          y = y - dt * v;
+          newV[i * n + j] = sampleFrom(x, y, V, 1);
+        }
+      }
+    });
+    U = newU;
+    V = newV;
+  }
+
+  // fluid.go:400-434
+  void advectSmoke(T dt) {
+    copyBorder(newM, M);
+    int n = NY;
+    T hh = h;
+    T h2 = (T)0.5 * hh;
+    par(1, NX - 1, [&](int i) {
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] != 0) {
+          T u = (U[i * n + j] + U[(i + 1) * n + j]) * (T)0.5 * SmokeAdvection;
+          T v = (V[i * n + j] + V[i * n + j + 1]) * (T)0.5 * SmokeAdvection;
+          T x = (T)i * hh + h2 - dt * u;
+          T y = (T)j * hh + h2 - dt * v;
+          T smokeValue = sampleFrom(x, y, M, 2);
+          if (ViscosityDiffusion > 0) {
+            T smokeDiffusion = ViscosityDiffusion * (T)0.3 * dt;
+            T neighbors = M[(i - 1) * n + j] + M[(i + 1) * n + j] + M[i * n + j - 1] +
+                          M[i * n + j + 1] - (T)4 * M[i * n + j];
+            smokeValue += smokeDiffusion * neighbors;
+          }
+          newM[i * n + j] = go_max(smokeValue, (T)0.0);
+        }
+      }
+    });
+    M = newM;
+  }
+
+  // fluid.go:449-493 (two serial passes; curl is a fresh zeroed array)
+  void applyVorticityConfinement(T dt) {
+    int n = NY;
+    T hh = h;
+    std::vector<T> curl(N, 0);
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] == 0) continue;
+        T dvdx = (V[(i + 1) * n + j] - V[(i - 1) * n + j]) * (T)0.5 / hh;
+        T dudy = (U[i * n + j + 1] - U[i * n + j - 1]) * (T)0.5 / hh;
+        curl[i * n + j] = dvdx - dudy;
+      }
+    T eps = (T)1e-5;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] == 0) continue;
+        T gx = (go_abs(curl[(i + 1) * n + j]) - go_abs(curl[(i - 1) * n + j])) * (T)0.5 / hh;
+        T gy = (go_abs(curl[i * n + j + 1]) - go_abs(curl[i * n + j - 1])) * (T)0.5 / hh;
+        T mag = go_sqrt(gx * gx + gy * gy) + eps;
+        gx /= mag;
+        gy /= mag;
+        T vort = curl[i * n + j];
+        T localVel = go_sqrt(U[i * n + j] * U[i * n + j] + V[i * n + j] * V[i * n + j]);
+        T adaptiveStrength = Confinement * ((T)1.0 + localVel * (T)0.1);
+        U[i * n + j] += adaptiveStrength * gy * vort * dt;
+        V[i * n + j] -= adaptiveStrength * gx * vort * dt;
+      }
+  }
+
+  // fluid.go:496-526
+  void addTurbulence(T dt) {
+    if (TurbulenceStrength <= 0) return;
+    int n = NY;
+    T turbStrength = TurbulenceStrength * dt;
+    par(1, NX - 1, [&](int i) {
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] > 0) {
+          T seedU = (T)(i * 137 + j * 241) * (T)0.01;
+          T seedV = (T)(i * 157 + j * 263) * (T)0.01;
+          T noiseU = (T)std::sin((double)seedU) * turbStrength;
+          T noiseV = (T)std::sin((double)seedV) * turbStrength;
+          T localVel = go_sqrt(U[i * n + j] * U[i * n + j] + V[i * n + j] * V[i * n + j]);
+          if (localVel > (T)0.1) {
+            T turbulenceFactor = go_min(localVel * (T)0.5, (T)1.0);
+            U[i * n + j] += noiseU * turbulenceFactor;
+            V[i * n + j] += noiseV * turbulenceFactor;
+          }
+        }
+      }
+    });
+  }
+
+  // fluid.go:529-557
+  T getAdaptiveTimeStep(T basedt) const {
+    T maxVel = 0;
+    int n = NY;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j)
+        if (S[i * n + j] > 0) {
+          T vel = go_abs(U[i * n + j]) + go_abs(V[i * n + j]);
+          if (vel > maxVel) maxVel = vel;
+        }
+    if (maxVel == 0) return basedt;
+    T cflFactor = (T)0.8;
+    T adaptivedt = cflFactor * h / maxVel;
+    adaptivedt = go_max(go_min(adaptivedt, basedt * (T)2.0), basedt * (T)0.1);
+    return adaptivedt;
+  }
+
+  // ------------------------------------------------ multigrid (fluid.go:559-758, 1122-1149)
+  void solveMultigridVCycle(int numIters, T dt) {
+    T cp = density * h / dt;
+    T tol = tolerance;
+    st.sweeps = 0;
+    for (int iter = 0; iter < numIters; ++iter) {
+      T maxDiv = 0;
+      for (int sm = 0; sm < 3; ++sm) maxDiv = pressureJacobiIteration((T)1.5, cp);
+      st.sweeps += 3;
+      if (maxDiv < tol) break;
+      std::vector<T> residual = computePressureResidual();
+      std::vector<T> coarseRHS = restrictResidual(residual);
+      std::vector<T> coarse = solveCoarseGrid(coarseRHS);
+      std::vector<T> corr = prolongateCorrection(coarse);
+      applyPressureCorrection(corr, cp);
+      for (int sm = 0; sm < 3; ++sm) pressureJacobiIteration((T)1.2, cp);
+      st.sweeps += 3;
+    }
+  }
+  std::vector<T> computePressureResidual() {
+    int n = NY;
+    std::vector<T> r(N, 0);
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] == 0) continue;
+        T div = U[(i + 1) * n + j] - U[i * n + j] + V[i * n + j + 1] - V[i * n + j];
+        T sx0 = S[(i - 1) * n + j], sx1 = S[(i + 1) * n + j];
+        T sy0 = S[i * n + j - 1], sy1 = S[i * n + j + 1];
+        T lap = sx0 * (p[(i - 1) * n + j] - p[i * n + j]) +
+                sx1 * (p[(i + 1) * n + j] - p[i * n + j]) +
+                sy0 * (p[i * n + j - 1] - p[i * n + j]) +
+                sy1 * (p[i * n + j + 1] - p[i * n + j]);
+        r[i * n + j] = -div - lap;
+      }
+    return r;
+  }
+  std::vector<T> restrictResidual(const std::vector<T>& fr) {
+    int cNX = (NX + 1) / 2, cNY = (NY + 1) / 2;
+    std::vector<T> c(cNX * cNY, 0);
+    for (int i = 1; i < cNX - 1; ++i)
+      for (int j = 1; j < cNY - 1; ++j) {
+        int fi = i * 2, fj = j * 2;
+        if (fi < NX - 1 && fj < NY - 1) {
+          T center = fr[fi * NY + fj] * (T)0.25;
+          T nbr = (fr[(fi - 1) * NY + fj] + fr[(fi + 1) * NY + fj] + fr[fi * NY + fj - 1] +
+                   fr[fi * NY + fj + 1]) * (T)0.125;
+          T crn = (fr[(fi - 1) * NY + fj - 1] + fr[(fi + 1) * NY + fj - 1] +
+                   fr[(fi - 1) * NY + fj + 1] + fr[(fi + 1) * NY + fj + 1]) * (T)0.0625;
+          c[i * cNY + j] = center + nbr + crn;
+        }
+      }
+    return c;
+  }
+  std::vector<T> solveCoarseGrid(const std::vector<T>& rhsc) {
+    int cNX = (NX + 1) / 2, cNY = (NY + 1) / 2;
+    std::vector<T> cP(cNX * cNY, 0), cS(cNX * cNY, 0);
+    for (int i = 0; i < cNX; ++i)
+      for (int j = 0; j < cNY; ++j) {
+        int fi = i * 2, fj = j * 2;
+        cS[i * cNY + j] = (fi < NX && fj < NY) ? S[fi * NY + fj] : (T)0;
+      }
+    T relaxation = (T)1.6;
+    for (int it = 0; it < 40; ++it)
+      for (int i = 1; i < cNX - 1; ++i)
+        for (int j = 1; j < cNY - 1; ++j) {
+          if (cS[i * cNY + j] == 0) continue;
+          T sx0 = cS[(i - 1) * cNY + j], sx1 = cS[(i + 1) * cNY + j];
+          T sy0 = cS[i * cNY + j - 1], sy1 = cS[i * cNY + j + 1];
+          T s = sx0 + sx1 + sy0 + sy1;
+          if (s == 0) continue;
+          T lap = sx0 * (cP[(i - 1) * cNY + j] - cP[i * cNY + j]) +
+                  sx1 * (cP[(i + 1) * cNY + j] - cP[i * cNY + j]) +
+                  sy0 * (cP[i * cNY + j - 1] - cP[i * cNY + j]) +
+                  sy1 * (cP[i * cNY + j + 1] - cP[i * cNY + j]);
+          T residual = rhsc[i * cNY + j] - lap;
+          T correction = -residual / s * relaxation;
+          cP[i * cNY + j] += correction;
+        }
+    return cP;
+  }
+  std::vector<T> prolongateCorrection(const std::vector<T>& cc) {
+    std::vector<T> corr(N, 0);
+    int cNY = (NY + 1) / 2, cNX = (NX + 1) / 2;
+    for (int i = 0; i < NX; ++i)
+      for (int j = 0; j < NY; ++j) {
+        int ci = i / 2, cj = j / 2;
+        if (ci >= cNX - 1 || cj >= cNY - 1) continue;
+        T fI = (T)(i % 2) * (T)0.5, fJ = (T)(j % 2) * (T)0.5;
+        corr[i * NY + j] = ((T)1 - fI) * ((T)1 - fJ) * cc[ci * cNY + cj] +
+                           fI * ((T)1 - fJ) * cc[(ci + 1) * cNY + cj] +
+                           ((T)1 - fI) * fJ * cc[ci * cNY + cj + 1] +
+                           fI * fJ * cc[(ci + 1) * cNY + cj + 1];
+      }
+    return corr;
+  }
+  void applyPressureCorrection(const std::vector<T>& corr, T cp) {
+    int n = NY;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] == 0) continue;
+        p[i * n + j] += corr[i * n + j] * cp;
+        T sx0 = S[(i - 1) * n + j], sx1 = S[(i + 1) * n + j];
+        T sy0 = S[i * n + j - 1], sy1 = S[i * n + j + 1];
+        T pc = corr[i * n + j];
+        U[i * n + j] -= sx0 * pc;
+        U[(i + 1) * n + j] += sx1 * pc;
+        V[i * n + j] -= sy0 * pc;
+        V[i * n + j + 1] += sy1 * pc;
+      }
+  }
+
+  // ------------------------------------------------ tools (walls.go, fluid.go:760-907)
+  // Return 0 on success, -1 on an index the reference would panic on.
+  int setSolid(int i, int j, bool value) {
+    if (i < 0 || i >= NX || j < 0 || j >= NY) return -1;
+    int cell = i * NY + j;
+    S[cell] = value ? (T)0 : (T)1;
+    if (value) {
+      int n = NY;
+      U[i * n + j] = 0;
+      if (i + 1 < NX) U[(i + 1) * n + j] = 0;
+      V[i * n + j] = 0;
+      if (j + 1 < NY) V[i * n + j + 1] = 0;
+      newU[i * n + j] = 0;
+      if (i + 1 < NX) newU[(i + 1) * n + j] = 0;
+      newV[i * n + j] = 0;
+      if (j + 1 < NY) newV[i * n + j + 1] = 0;
+    }
+    return 0;
+  }
+  int isSolid(int i, int j) const {
+    if (i < 0 || i >= NX || j < 0 || j >= NY) return -1;
+    return S[i * NY + j] == 0 ? 1 : 0;
+  }
+  int setVelocity(int i, int j, T u, T v) {
+    if (i < 0 || i >= NX || j < 0 || j >= NY) return -1;
+    U[i * NY + j] = u;
+    V[i * NY + j] = v;
+    return 0;
+  }
+  int addSmoke(int i, int j, T s) {
+    if (i < 0 || i >= NX || j < 0 || j >= NY) return -1;
+    M[i * NY + j] += s;
+    return 0;
+  }
+  void reset() {
+    std::fill(U.begin(), U.end(), (T)0); std::fill(V.begin(), V.end(), (T)0);
+    std::fill(newU.begin(), newU.end(), (T)0); std::fill(newV.begin(), newV.end(), (T)0);
+    std::fill(p.begin(), p.end(), (T)0); std::fill(M.begin(), M.end(), (T)0);
+    std::fill(newM.begin(), newM.end(), (T)0);
+  }
+  void applyForce(int i, int j, T fx, T fy) {
+    if (i < 1 || i >= NX - 1 || j < 1 || j >= NY - 1) return;
+    if (S[i * NY + j] == 0) return;
+    U[i * NY + j] += fx;
+    V[i * NY + j] += fy;
+  }
+  void applyForceRadius(int cx, int cy, T fx, T fy, int radius) {
+    if (radius <= 0) { applyForce(cx, cy, fx, fy); return; }
+    T r2 = (T)(radius * radius);
+    for (int i = cx - radius; i <= cx + radius; ++i)
+      for (int j = cy - radius; j <= cy + radius; ++j) {
+        if (i < 1 || i >= NX - 1 || j < 1 || j >= NY - 1) continue;
+        T dx = (T)(i - cx), dy = (T)(j - cy);
+        T dist2 = dx * dx + dy * dy;
+        if (dist2 > r2) continue;
+        T weight = (T)std::exp((double)((T)-3.0 * dist2 / r2));
+        applyForce(i, j, fx * weight, fy * weight);
+      }
+  }
+  void setCircularObstacle(int cx, int cy, int radius) {
+    for (int i = cx - radius; i <= cx + radius; ++i)
+      for (int j = cy - radius; j <= cy + radius; ++j) {
+        if (i < 0 || i >= NX || j < 0 || j >= NY) continue;
+        T dx = (T)(i - cx), dy = (T)(j - cy);
+        if (dx * dx + dy * dy <= (T)(radius * radius)) setSolid(i, j, true);
+      }
+  }
+
+  // ------------------------------------------------ views (fluid.go:798-891)
+  T maxDivergence() const {
+    int n = NY;
+    T maxDiv = 0;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] == 0) continue;
+        T div = U[(i + 1) * n + j] - U[i * n + j] + V[i * n + j + 1] - V[i * n + j];
+        T a = go_abs(div);
+        if (a > maxDiv) maxDiv = a;
+      }
+    return maxDiv;
+  }
+  void vorticity(T* out, T* mn, T* mx) const {
+    int n = NY;
+    T minVal = std::numeric_limits<T>::max(), maxVal = -(std::numeric_limits<T>::max() - 1);
+    std::fill(out, out + N, (T)0);
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] == 0) continue;
+        T dvdx = (V[(i + 1) * n + j] - V[(i - 1) * n + j]) * (T)0.5 / h;
+        T dudy = (U[i * n + j + 1] - U[i * n + j - 1]) * (T)0.5 / h;
+        T c = dvdx - dudy;
+        out[i * n + j] = c;
+        if (c < minVal) minVal = c;
+        if (c > maxVal) maxVal = c;
+      }
+    *mn = minVal;
+    *mx = maxVal;
+  }
+  void velocityMagnitude(T* out, T* mn, T* mx) const {
+    int n = NY;
+    T minVal = std::numeric_limits<T>::max(), maxVal = -(std::numeric_limits<T>::max() - 1);
+    std::fill(out, out + N, (T)0);
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] == 0) continue;
+        T u = (U[i * n + j] + U[(i + 1) * n + j]) * (T)0.5;
+        T v = (V[i * n + j] + V[i * n + j + 1]) * (T)0.5;
+        T mag = go_sqrt(u * u + v * v);
+        out[i * n + j] = mag;
+        if (mag < minVal) minVal = mag;
+        if (mag > maxVal) maxVal = mag;
+      }
+    *mn = minVal;
+    *mx = maxVal;
+  }
+
+  // ------------------------------------------------ BFECC (fluid.go:909-1120)
+  T clampToNeighbors(T val, const std::vector<T>& src, int i, int j) const {
+    int n = NY;
+    T lo = src[i * n + j], hi = src[i * n + j];
+    for (int di = -1; di <= 1; ++di)
+      for (int dj = -1; dj <= 1; ++dj) {
+        int ni = i + di, nj = j + dj;
+        if (ni >= 0 && ni < NX && nj >= 0 && nj < NY) {
+          T v = src[ni * n + nj];
+          if (v < lo) lo = v;
+          if (v > hi) hi = v;
+        }
+      }
+    if (val < lo) return lo;
+    if (val > hi) return hi;
+    return val;
+  }
+  void advectVelocityBFECC(T dt) {
+    int n = NY;
+    T hh = h, h2 = hh / (T)2;
+    std::vector<T> origU = U, origV = V;
+    advectVelocity(dt);
+    std::vector<T> fwdU = U, fwdV = V;
+    U = origU;
+    V = origV;
+    std::vector<T> bwdU(N, 0), bwdV(N, 0);
+    copyBorder(bwdU, fwdU);
+    copyBorder(bwdV, fwdV);
+    par(1, NX, [&](int i) {
+      for (int j = 1; j < NY; ++j) {
+        if (S[i * n + j] != 0 && S[(i - 1) * n + j] != 0 && j < NY - 1) {
+          T x = (T)i * hh, y = (T)j * hh + h2;
+          T u = U[i * n + j], v = avgV(V, i, j);
+          x = x + dt * u;
+          y = y + dt * v;
+          bwdU[i * n + j] = sampleFrom(x, y, fwdU, 0);
+        }
+        if (S[i * n + j] != 0 && S[i * n + j - 1] != 0 && i < NX - 1) {
+          T x = (T)i * hh + h2, y = (T)j * hh;
+          T u = avgU(U, i, j), v = V[i * n + j];
+          x = x + dt * u;
+          y = y + dt * v;
+          bwdV[i * n + j] = sampleFrom(x, y, fwdV, 1);
+        }
+      }
+    });
+    std::vector<T> corrU = origU, corrV = origV;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        corrU[i * n + j] = origU[i * n + j] - (bwdU[i * n + j] - origU[i * n + j]) * (T)0.5;
+        corrV[i * n + j] = origV[i * n + j] - (bwdV[i * n + j] - origV[i * n + j]) * (T)0.5;
+      }
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        corrU[i * n + j] = clampToNeighbors(corrU[i * n + j], origU, i, j);
+        corrV[i * n + j] = clampToNeighbors(corrV[i * n + j], origV, i, j);
+      }
+    U = corrU;
+    V = corrV;
+    advectVelocity(dt);
+  }
+  void advectSmokeBFECC(T dt) {
+    int n = NY;
+    T hh = h, h2 = (T)0.5 * hh;
+    std::vector<T> origM = M;
+    advectSmoke(dt);
+    std::vector<T> fwdM = M;
+    std::vector<T> bwdM(N, 0);
+    copyBorder(bwdM, fwdM);
+    par(1, NX - 1, [&](int i) {
+      for (int j = 1; j < NY - 1; ++j) {
+        if (S[i * n + j] != 0) {
+          T u = (U[i * n + j] + U[(i + 1) * n + j]) * (T)0.5 * SmokeAdvection;
+          T v = (V[i * n + j] + V[i * n + j + 1]) * (T)0.5 * SmokeAdvection;
+          T x = (T)i * hh + h2 + dt * u;
+          T y = (T)j * hh + h2 + dt * v;
+          bwdM[i * n + j] = sampleFrom(x, y, fwdM, 2);
+        }
+      }
+    });
+    std::vector<T> corrM = origM;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j)
+        corrM[i * n + j] = origM[i * n + j] - (bwdM[i * n + j] - origM[i * n + j]) * (T)0.5;
+    for (int i = 1; i < NX - 1; ++i)
+      for (int j = 1; j < NY - 1; ++j) {
+        corrM[i * n + j] = clampToNeighbors(corrM[i * n + j], origM, i, j);
+        if (corrM[i * n + j] < 0) corrM[i * n + j] = 0;
+      }
+    M = corrM;
+    advectSmoke(dt);
+  }
+};
+
+}  // namespace orc
+
+// ===========================================================================
+// C ABI (loaded with ctypes by the tests and the benchmark's CPU leg).
+// Fields: 0 U, 1 V, 2 newU, 3 newV, 4 p, 5 S, 6 M, 7 newM.
+// ===========================================================================
+namespace {
+struct Handle {
+  int prec;
+  orc::Pool* pool;
+  orc::Fluid<float>* f32;
+  orc::Fluid<double>* f64;
+};
+template <typename F>
+auto with(Handle* h, F&& fn) {
+  if (h->prec == 32) return fn(*h->f32);
+  return fn(*h->f64);
+}
+template <typename T>
+std::vector<T>* field_of(orc::Fluid<T>& f, int k) {
+  switch (k) {
+    case 0: return &f.U;
+    case 1: return &f.V;
+    case 2: return &f.newU;
+    case 3: return &f.newV;
+    case 4: return &f.p;
+    case 5: return &f.S;
+    case 6: return &f.M;
+    case 7: return &f.newM;
+    case 8: return &f.phi;
+    case 9: return &f.rhs;
+  }
+  return nullptr;
+}
+}  // namespace
+
+extern "C" {
+
+void* orc_create(int prec, int width, int height, double density, double h, int threads) {
+  if ((prec != 32 && prec != 64) || width < 1 || height < 1) return nullptr;
+  Handle* hd = new Handle{prec, new orc::Pool(threads), nullptr, nullptr};
+  if (prec == 32)
+    hd->f32 = new orc::Fluid<float>((float)density, width, height, (float)h, hd->pool);
+  else
+    hd->f64 = new orc::Fluid<double>(density, width, height, h, hd->pool);
+  return hd;
+}
+
+void orc_destroy(void* p) {
+  Handle* h = (Handle*)p;
+  if (!h) return;
+  delete h->f32;
+  delete h->f64;
+  delete h->pool;
+  delete h;
+}
+
+int orc_dims(void* p, int* nx, int* ny) {
+  return with((Handle*)p, [&](auto& f) { *nx = f.NX; *ny = f.NY; return 0; });
+}
+
+void* orc_field(void* p, int k) {
+  return with((Handle*)p, [&](auto& f) -> void* {
+    auto* v = field_of(f, k);
+    if (!v || v->empty()) return nullptr;
+    return (void*)v->data();
+  });
+}
+
+int orc_set_param(void* p, const char* name, double value) {
+  std::string k(name);
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    if (k == "Confinement") f.Confinement = (T)value;
+    else if (k == "ViscosityDiffusion") f.ViscosityDiffusion = (T)value;
+    else if (k == "PressureDamping") f.PressureDamping = (T)value;
+    else if (k == "TurbulenceStrength") f.TurbulenceStrength = (T)value;
+    else if (k == "SmokeAdvection") f.SmokeAdvection = (T)value;
+    else if (k == "UseMultigrid") f.UseMultigrid = value != 0;
+    else if (k == "MultigridLevels") f.MultigridLevels = (int)value;
+    else if (k == "UseBFECC") f.UseBFECC = value != 0;
+    else if (k == "Relaxation") f.Relaxation = (T)value;
+    else if (k == "num_iters") f.num_iters = (int)value;
+    else if (k == "tolerance") f.tolerance = (T)value;
+    else if (k == "early_exit") f.early_exit = value != 0;
+    else if (k == "scheme") f.scheme = (int)value;
+    else if (k == "jacobi_omega") f.jacobi_omega = (T)value;
+    else if (k == "check_every") f.check_every = std::max(1, (int)value);
+    else if (k == "refine_sweeps") f.refine_sweeps = (int)value;
+    else return -1;
+    return 0;
+  });
+}
+
+double orc_get_param(void* p, const char* name) {
+  std::string k(name);
+  return with((Handle*)p, [&](auto& f) -> double {
+    if (k == "Confinement") return f.Confinement;
+    if (k == "ViscosityDiffusion") return f.ViscosityDiffusion;
+    if (k == "PressureDamping") return f.PressureDamping;
+    if (k == "TurbulenceStrength") return f.TurbulenceStrength;
+    if (k == "SmokeAdvection") return f.SmokeAdvection;
+    if (k == "UseMultigrid") return f.UseMultigrid;
+    if (k == "MultigridLevels") return f.MultigridLevels;
+    if (k == "UseBFECC") return f.UseBFECC;
+    if (k == "Relaxation") return f.Relaxation;
+    if (k == "num_iters") return f.num_iters;
+    if (k == "tolerance") return f.tolerance;
+    if (k == "early_exit") return f.early_exit;
+    if (k == "scheme") return f.scheme;
+    if (k == "jacobi_omega") return f.jacobi_omega;
+    if (k == "check_every") return f.check_every;
+    if (k == "refine_sweeps") return f.refine_sweeps;
+    if (k == "h") return f.h;
+    if (k == "density") return f.density;
+    return std::nan("");
+  });
+}
+
+void orc_simulate(void* p, double dt) {
+  with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    f.simulate((T)dt);
+    return 0;
+  });
+}
+
+// Stage entry points (the white-box tests of the reference call these).
+// stage: 0 makeIncompressible(iters, dt) 1 advectVelocity 2 advectSmoke
+// 3 handleBorders 4 applyVorticityConfinement 5 applyViscosity
+// 6 addTurbulence 7 advectVelocityBFECC 8 advectSmokeBFECC
+// 9 fill(p, 0)
+int orc_stage(void* p, int stage, int iters, double dt) {
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    T d = (T)dt;
+    switch (stage) {
+      case 0: f.makeIncompressible(iters, d); break;
+      case 1: f.advectVelocity(d); break;
+      case 2: f.advectSmoke(d); break;
+      case 3: f.handleBorders(); break;
+      case 4: f.applyVorticityConfinement(d); break;
+      case 5: f.applyViscosity(d); break;
+      case 6: f.addTurbulence(d); break;
+      case 7: f.advectVelocityBFECC(d); break;
+      case 8: f.advectSmokeBFECC(d); break;
+      case 9: std::fill(f.p.begin(), f.p.end(), (T)0); break;
+      default: return -1;
+    }
+    return 0;
+  });
+}
+
+// copyBorder(dst, src) on two caller buffers of NX*NY elements of the
+// instance's precision.
+int orc_copy_border(void* p, void* dst, const void* src) {
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    std::vector<T> d((T*)dst, (T*)dst + f.N), s((const T*)src, (const T*)src + f.N);
+    f.copyBorder(d, s);
+    std::memcpy(dst, d.data(), sizeof(T) * f.N);
+    return 0;
+  });
+}
+
+int orc_set_solid(void* p, int i, int j, int v) {
+  return with((Handle*)p, [&](auto& f) { return f.setSolid(i, j, v != 0); });
+}
+int orc_is_solid(void* p, int i, int j) {
+  return with((Handle*)p, [&](auto& f) { return f.isSolid(i, j); });
+}
+int orc_set_velocity(void* p, int i, int j, double u, double v) {
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    return f.setVelocity(i, j, (T)u, (T)v);
+  });
+}
+int orc_add_smoke(void* p, int i, int j, double s) {
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    return f.addSmoke(i, j, (T)s);
+  });
+}
+void orc_reset(void* p) { with((Handle*)p, [&](auto& f) { f.reset(); return 0; }); }
+void orc_apply_force(void* p, int i, int j, double fx, double fy) {
+  with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    f.applyForce(i, j, (T)fx, (T)fy);
+    return 0;
+  });
+}
+void orc_apply_force_radius(void* p, int cx, int cy, double fx, double fy, int r) {
+  with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    f.applyForceRadius(cx, cy, (T)fx, (T)fy, r);
+    return 0;
+  });
+}
+void orc_set_circular_obstacle(void* p, int cx, int cy, int r) {
+  with((Handle*)p, [&](auto& f) { f.setCircularObstacle(cx, cy, r); return 0; });
+}
+double orc_max_divergence(void* p) {
+  return with((Handle*)p, [&](auto& f) -> double { return f.maxDivergence(); });
+}
+double orc_adaptive_dt(void* p, double basedt) {
+  return with((Handle*)p, [&](auto& f) -> double {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    return f.getAdaptiveTimeStep((T)basedt);
+  });
+}
+// out: NX*NY elements of the instance precision; mnmx[2] (double)
+int orc_vorticity(void* p, void* out, double* mnmx) {
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    T mn, mx;
+    f.vorticity((T*)out, &mn, &mx);
+    mnmx[0] = mn;
+    mnmx[1] = mx;
+    return 0;
+  });
+}
+int orc_velocity_magnitude(void* p, void* out, double* mnmx) {
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    T mn, mx;
+    f.velocityMagnitude((T*)out, &mn, &mx);
+    mnmx[0] = mn;
+    mnmx[1] = mx;
+    return 0;
+  });
+}
+int orc_sample_velocity(void* p, double x, double y, double* uv) {
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    uv[0] = f.sampleFrom((T)x, (T)y, f.U, 0);
+    uv[1] = f.sampleFrom((T)x, (T)y, f.V, 1);
+    return 0;
+  });
+}
+// stats: div_l2_post, div_max_post, div_count_post, resid_l2, resid_max,
+// smoke_mass, sweeps, last_maxdiv
+int orc_stats(void* p, double* out) {
+  return with((Handle*)p, [&](auto& f) {
+    out[0] = f.st.div_l2_post;
+    out[1] = f.st.div_max_post;
+    out[2] = f.st.div_count_post;
+    out[3] = f.st.resid_l2;
+    out[4] = f.st.resid_max;
+    out[5] = f.st.smoke_mass;
+    out[6] = f.st.sweeps;
+    out[7] = f.st.last_maxdiv;
+    return 0;
+  });
+}
+int orc_threads(void* p) { return ((Handle*)p)->pool->size(); }
+
+}  // extern "C"
