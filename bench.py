@@ -1,0 +1,377 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 simulation step (pkg/fluid Simulate) on the
+2048x2048 lid-driven cavity.
+
+Workload (one "step" = one Simulate call): 2048x2048 interior cells, density
+1, h = 1, dt = 0.1, closed box, lid source row U = 1.0 under the top wall
+(the app's cavity preset, without its smoke), BFECC advection on, the
+New() default turbulence 0.02, 200 Jacobi pressure sweeps per step run in
+temporal blocks of 8 sweeps per launch, FP64 residual reduction and one FP64
+outer correction of 8 sweeps, fixed sweep count (no early exit).  Fields are
+FP32; inputs are synthetic (zero initial state, seeded scene).
+
+Arms:
+  (default)          the CUDA path.  `value` is device-timed with CUDA events
+                     on the library's stream, the lid held by device-resident
+                     sources; `e2e` drives the same workload through the C ABI
+                     from the host: per step the lid edits are uploaded, the
+                     step runs and the smoke field is read back.
+  --impl reference   the reference's CPU algorithm (serial lexicographic SOR
+                     pressure, FP32) restated in C++, on the host cores.
+
+Metric: Mcell-steps/s = 2048 * 2048 * steps / seconds / 1e6.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s fwd at 2048^2 (lid-driven cavity, BFECC, 200 Jacobi sweeps)"
+W = H = 2048
+DT = 0.1
+ITERS = 200
+TB = 8
+REFINE = 8
+# Algorithmic bytes per cell per Jacobi sweep (phi read + write, rhs, 1-byte mask).
+JACOBI_BYTES_PER_CELL_SWEEP = 13
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_config(extra=None):
+    cfg = {
+        "workload": "lid-driven cavity 2048x2048, BFECC, turbulence 0.02, 200 Jacobi sweeps "
+                    "(temporal blocks of 8), FP64 residual + 8-sweep FP64 outer correction",
+        "grid": [W, H],
+        "dt": DT,
+        "pressure_sweeps": ITERS,
+        "tb_depth": TB,
+        "refine_sweeps": REFINE,
+        "l2": "per-step working set ~250 MB of fields > 129 MB L2; no flush between steps",
+    }
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ---------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per Jacobi launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "jacobi_tb_traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def build_cavity(fluid_gb300, auto_sync=False):
+    f = fluid_gb300.Fluid(1.0, W, H, 1.0, auto_sync=auto_sync, scheme=fluid_gb300.SCHEME_JACOBI,
+                          num_iters=ITERS, tb_depth=TB, refine_sweeps=REFINE, UseBFECC=True,
+                          early_exit=False)
+    S = f.S.reshape(f.NumX, f.NumY)
+    S[:] = 1.0
+    S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
+    f.mark_dirty(1 << fluid_gb300.FIELDS["S"])
+    return f
+
+
+def lid_cells(f):
+    import numpy as np
+
+    i = np.arange(2, f.NumX - 2, dtype=np.int32)
+    j = np.full_like(i, f.NumY - 2)
+    return i, j
+
+
+# ---------------------------------------------------------------- CPU legs
+def cpu_reference_steps(steps, threads, budget_s=None):
+    """Times the reference algorithm (FP32, serial SOR pressure, parallelRange
+    stages on `threads` host threads) on the cavity workload."""
+    from oracle.pyoracle import LEXSOR, OracleFluid
+
+    o = OracleFluid(1.0, W, H, 1.0, prec=32, threads=threads, scheme=LEXSOR, num_iters=ITERS,
+                    UseBFECC=True, early_exit=False)
+    S = o.S.reshape(o.NumX, o.NumY)
+    S[:] = 1.0
+    S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
+    times = []
+    for k in range(steps):
+        for i in range(2, o.NumX - 2):
+            o.SetVelocity(i, o.NumY - 2, 1.0, 0.0)
+        t0 = time.perf_counter()
+        o.Simulate(DT)
+        times.append(time.perf_counter() - t0)
+        if budget_s is not None and sum(times) > budget_s:
+            break
+    return times
+
+
+# ---------------------------------------------------------------- arms
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # Each step is one full 2048^2 step of the reference algorithm (~seconds
+    # on the host); the count is bounded so the whole run ends in minutes.
+    warm = cpu_reference_steps(1, threads)
+    per = warm[0]
+    n = max(1, min(args.steps, int(90.0 / max(per, 1e-3))))
+    times = cpu_reference_steps(n, threads)
+    sec = sum(times)
+    value = W * H * len(times) / sec / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mcell-steps/s",
+        "n_gpus": args.gpus, "steps": len(times), "warmup": 1,
+        "ms_per_step": 1e3 * sec / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config({"scheme": "reference serial lexicographic SOR (fluid.go:157-234)"}),
+        "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d full 2048x2048 steps after 1 warm-up step; pressure loop "
+                                   "serial as in the reference, other stages on %d threads"
+                                   % (len(times), threads)},
+        "e2e": {"value": value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import fluid_gb300
+
+    fluid_gb300.build()
+    f = build_cavity(fluid_gb300)
+    li, lj = lid_cells(f)
+    f.set_sources(li, lj, u=1.0, v=0.0, mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY)
+    stream = torch.cuda.ExternalStream(f.stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        f.Simulate(DT)
+    f.synchronize()
+
+    # ------------------------------------------------------------ timed region
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0] or 0) \
+        if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local
+    sampler = ClockSampler(gpu_index)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with sampler:
+        barrier()
+        torch.cuda.synchronize()
+        f.synchronize()
+        launches0 = f.launch_count()
+        t_host = time.perf_counter()
+        e0.record(stream)
+        for _ in range(args.steps):
+            f.Simulate(DT)
+        e1.record(stream)
+        f.synchronize()
+        torch.cuda.synchronize()
+        t_host = time.perf_counter() - t_host
+        barrier()
+    launches = f.launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    t_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * W * H * args.steps / (t_max / 1e3) / 1e6
+    st = f.stats()
+
+    # ------------------------------------------------------------ dominant kernel
+    f.profile(True)
+    spans = []
+    for _ in range(min(args.steps, 5)):
+        f.Simulate(DT)
+        span, nl = f.jacobi_span()
+        spans.append(span / nl)
+    f.profile(False)
+    launch_ms = statistics.median(spans)
+    n_cells = f.NumX * f.NumY
+    alg_bytes = JACOBI_BYTES_PER_CELL_SWEEP * TB * n_cells
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_hbm()
+    tr = committed_traffic()
+    roofline = {
+        "kernel": "k_jacobi_tb (8 Jacobi sweeps per launch)",
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_kind + " MEASURED_PEAKS.json hbm_gbs"
+        if peak_kind == "measured" else "fallback 6.8 TB/s",
+        "bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
+        "traffic": tr.get("dram_bytes_per_launch_full") if tr else None,
+        "traffic_source": tr.get("source") if tr else None,
+    }
+
+    # ------------------------------------------------------------ e2e through the C ABI
+    e2e = None
+    if rank == 0:
+        g = build_cavity(fluid_gb300)
+        mbit = 1 << fluid_gb300.FIELDS["M"]
+        u = np.ones(li.size, np.float32)
+        v = np.zeros(li.size, np.float32)
+        for _ in range(args.warmup):
+            g.SetVelocityMany(li, lj, u, v)
+            g.Simulate(DT)
+            g.download(mbit)
+        g.synchronize()
+        b0 = g.edit_bytes()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            g.SetVelocityMany(li, lj, u, v)
+            g.Simulate(DT)
+            g.download(mbit)
+        t_e2e = time.perf_counter() - t0
+        h2d = (g.edit_bytes() - b0) / args.steps
+        e2e = {"value": W * H * args.steps / t_e2e / 1e6, "unit": "Mcell-steps/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4 * g.NumX * g.NumY,
+               "path": "fg_set_velocity_many (lid) + fg_simulate + fg_download(M) per step"}
+        del g
+
+    # ------------------------------------------------------------ CPU baseline
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        times = cpu_reference_steps(args.cpu_steps, threads)
+        cpu = {"value": W * H * len(times) / sum(times) / 1e6, "unit": "Mcell-steps/s",
+               "cores": threads, "kind": "port",
+               "sample": "%d full 2048x2048 step(s) of the reference algorithm (serial SOR "
+                         "pressure, FP32), stages on %d host threads" % (len(times), threads)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": workload_config({"parallelism": "replicas%d" % world if world > 1 else "single"}),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": sampler.summary(),
+            "host_ms_per_step": 1e3 * t_host / args.steps,
+            "step_stats": {"div_l2_post": st["div_l2_post"], "resid_l2": st["resid_l2"],
+                           "smoke_mass": st["smoke_mass"], "sweeps": st["sweeps"]},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,25 @@
+"""GB300-native simulation step of pkg/fluid (TheFellow/fluid).
+
+The CUDA kernels sit behind the C ABI declared in include/fluidgpu.h
+(libfluidgpu.so, built in-tree by fluid_gb300._build).  ``Fluid`` is the
+Python mirror of the Go type ``fluid.Fluid`` over that ABI.
+"""
+from . import fluid as _fluid_mod
+from ._build import build
+from .fluid import (ALL_FIELDS, FIELDS, SCHEME_JACOBI, SCHEME_LEXSOR, Fluid, FluidError,
+                    ScalarField, VectorField)
+
+
+def __getattr__(name):
+    if name == "Relaxation":
+        return _fluid_mod.Relaxation
+    raise AttributeError(name)
+
+
+def set_relaxation(value: float) -> None:
+    """Sets the package variable fluid.Relaxation (fluid.go:7-9)."""
+    _fluid_mod.Relaxation = float(value)
+
+
+__all__ = ["Fluid", "FluidError", "ScalarField", "VectorField", "build", "set_relaxation",
+           "FIELDS", "ALL_FIELDS", "SCHEME_LEXSOR", "SCHEME_JACOBI"]

@@ -1,0 +1,944 @@
+// C ABI of libfluidgpu: handle lifetime, host mirrors, tool edits, the step
+// driver and the views.  The kernels live in k_*.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "fg_internal.cuh"
+
+namespace fg {
+size_t pctl_bytes(int n_slots);
+int jacobi_launches(const fg_fluid* f, int iters);
+}  // namespace fg
+
+using namespace fg;
+
+namespace {
+
+constexpr int kSlots = 4096;
+
+int fail(fg_fluid* f, int code, const char* what, cudaError_t e = cudaSuccess) {
+  if (f) {
+    char buf[512];
+    if (e != cudaSuccess)
+      snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+    else
+      snprintf(buf, sizeof buf, "%s", what);
+    f->last_error = buf;
+  }
+  return code;
+}
+
+#define CK(f, call, what)                                  \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return fail(f, FG_ERR_CUDA, what, e_); \
+  } while (0)
+
+float host_go_min(float a, float b) {
+  if (std::isnan(a) || std::isnan(b)) return std::nanf("");
+  if (a == b) return std::signbit(a) ? a : b;
+  return a < b ? a : b;
+}
+float host_go_max(float a, float b) {
+  if (std::isnan(a) || std::isnan(b)) return std::nanf("");
+  if (a == b) return std::signbit(a) ? b : a;
+  return a > b ? a : b;
+}
+
+bool in_grid(const fg_fluid* f, int i, int j) { return i >= 0 && i < f->NX && j >= 0 && j < f->NY; }
+
+int bind(fg_fluid* f) {
+  cudaError_t e = cudaSetDevice(f->device);
+  if (e != cudaSuccess) return fail(f, FG_ERR_CUDA, "cudaSetDevice", e);
+  return FG_OK;
+}
+
+size_t field_bytes(const fg_fluid* f) { return sizeof(float) * (size_t)f->NX * f->P; }
+
+int alloc_dev(fg_fluid* f, float** p) {
+  cudaError_t e = cudaMalloc((void**)p, field_bytes(f));
+  if (e != cudaSuccess) return fail(f, FG_ERR_NOMEM, "cudaMalloc", e);
+  e = cudaMemsetAsync(*p, 0, field_bytes(f), f->stream);
+  if (e != cudaSuccess) return fail(f, FG_ERR_CUDA, "cudaMemsetAsync", e);
+  return FG_OK;
+}
+
+int upload_field(fg_fluid* f, int k) {
+  CK(f, cudaMemcpy2DAsync(f->d[k], sizeof(float) * f->P, f->hm[k], sizeof(float) * f->NY,
+                          sizeof(float) * f->NY, f->NX, cudaMemcpyHostToDevice, f->stream),
+     "upload");
+  return FG_OK;
+}
+
+int download_field(fg_fluid* f, int k) {
+  CK(f, cudaMemcpy2DAsync(f->hm[k], sizeof(float) * f->NY, f->d[k], sizeof(float) * f->P,
+                          sizeof(float) * f->NY, f->NX, cudaMemcpyDeviceToHost, f->stream),
+     "download");
+  return FG_OK;
+}
+
+int check_mask(fg_fluid* f) {
+  const float* S = f->hm[FG_S];
+  size_t n = (size_t)f->NX * f->NY;
+  for (size_t k = 0; k < n; ++k)
+    if (!(S[k] == 0.0f || S[k] == 1.0f)) {
+      char buf[160];
+      snprintf(buf, sizeof buf, "S[%zu] = %g: the GPU step supports S values 0 and 1 only", k,
+               (double)S[k]);
+      return fail(f, FG_ERR_MASK, buf);
+    }
+  return FG_OK;
+}
+
+// Applies pending mirror uploads and queued tool edits, rebuilds the flag
+// bytes if S changed.  Called at the start of every device operation.
+int flush(fg_fluid* f) {
+  int rc = bind(f);
+  if (rc) return rc;
+  unsigned up = f->dirty;
+  if (up & FG_FIELD_BIT(FG_S)) {
+    if ((rc = check_mask(f))) {
+      f->dirty &= ~FG_FIELD_BIT(FG_S);
+      return rc;
+    }
+    f->masks_stale = true;
+  }
+  for (int k = 0; k < FG_NUM_FIELDS; ++k)
+    if (up & FG_FIELD_BIT(k))
+      if ((rc = upload_field(f, k))) return rc;
+  if (up) {
+    // The caller may write the mirrors again as soon as we return.
+    CK(f, cudaStreamSynchronize(f->stream), "upload sync");
+  }
+  f->dirty = 0;
+  if (!f->edits.empty()) {
+    std::vector<EditRec> ed;
+    ed.reserve(f->edits.size());
+    for (const EditRec& r : f->edits)
+      if (!(up & FG_FIELD_BIT(r.field))) ed.push_back(r);
+    f->edits.clear();
+    if (!ed.empty()) {
+      std::stable_sort(ed.begin(), ed.end(), [](const EditRec& a, const EditRec& b) {
+        return a.field != b.field ? a.field < b.field : a.cell < b.cell;
+      });
+      std::vector<uint32_t> off;
+      off.push_back(0);
+      for (size_t k = 1; k < ed.size(); ++k)
+        if (ed[k].field != ed[k - 1].field || ed[k].cell != ed[k - 1].cell) off.push_back((uint32_t)k);
+      off.push_back((uint32_t)ed.size());
+      size_t ng = off.size() - 1;
+      int sl = f->edit_slot;
+      f->edit_slot ^= 1;
+      // The slot's previous upload must have left its pinned buffers.
+      CK(f, cudaEventSynchronize(f->edit_ev[sl]), "edit slot wait");
+      if (ed.size() > f->edit_cap[sl] || off.size() > f->edit_cap[sl] + 1) {
+        cudaFreeHost(f->edit_pinned[sl]);
+        cudaFreeHost(f->edit_off_pinned[sl]);
+        cudaFree(f->edit_dev[sl]);
+        cudaFree(f->edit_off_dev[sl]);
+        size_t cap = std::max<size_t>(ed.size(), off.size()) * 2;
+        CK(f, cudaMallocHost((void**)&f->edit_pinned[sl], cap * sizeof(EditRec)), "edit alloc");
+        CK(f, cudaMallocHost((void**)&f->edit_off_pinned[sl], (cap + 1) * sizeof(uint32_t)),
+           "edit alloc");
+        CK(f, cudaMalloc((void**)&f->edit_dev[sl], cap * sizeof(EditRec)), "edit alloc");
+        CK(f, cudaMalloc((void**)&f->edit_off_dev[sl], (cap + 1) * sizeof(uint32_t)), "edit alloc");
+        f->edit_cap[sl] = cap;
+      }
+      memcpy(f->edit_pinned[sl], ed.data(), ed.size() * sizeof(EditRec));
+      memcpy(f->edit_off_pinned[sl], off.data(), off.size() * sizeof(uint32_t));
+      CK(f, cudaMemcpyAsync(f->edit_dev[sl], f->edit_pinned[sl], ed.size() * sizeof(EditRec),
+                            cudaMemcpyHostToDevice, f->stream), "edit upload");
+      CK(f, cudaMemcpyAsync(f->edit_off_dev[sl], f->edit_off_pinned[sl],
+                            off.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, f->stream),
+         "edit upload");
+      CK(f, cudaEventRecord(f->edit_ev[sl], f->stream), "edit event");
+      f->edit_bytes += ed.size() * sizeof(EditRec) + off.size() * sizeof(uint32_t);
+      CK(f, launch_apply_edits(f, (int)ng, sl), "apply edits");
+    }
+  }
+  if (f->masks_stale) {
+    CK(f, launch_build_flags(f), "build flags");
+    f->masks_stale = false;
+  }
+  return FG_OK;
+}
+
+void invalidate(fg_fluid* f, unsigned mask) {
+  for (int k = 0; k < FG_NUM_FIELDS; ++k)
+    if ((mask & FG_FIELD_BIT(k)) && k != FG_S) f->host_valid[k] = false;
+}
+
+constexpr unsigned kStepFields = FG_ALL_FIELDS & ~FG_FIELD_BIT(FG_S);
+
+// Records a tool edit of `field` at host index `cell`: applied to a current
+// mirror at once, and queued for the device unless the mirror is scheduled
+// for upload anyway.
+void edit(fg_fluid* f, int field, int cell, int op, float value) {
+  if (f->host_valid[field]) {
+    float& m = f->hm[field][cell];
+    m = op == 0 ? value : m + value;
+  }
+  if (!(f->dirty & FG_FIELD_BIT(field))) f->edits.push_back(EditRec{(uint32_t)field, (uint32_t)cell, (uint32_t)op, value});
+}
+
+int check_params(fg_fluid* f, const fg_params* p) {
+  if (p->num_iters < 0) return fail(f, FG_ERR_INVALID, "num_iters < 0");
+  if (p->scheme != FG_SCHEME_LEXSOR && p->scheme != FG_SCHEME_JACOBI)
+    return fail(f, FG_ERR_INVALID, "unknown pressure scheme");
+  if (p->refine_sweeps < 0) return fail(f, FG_ERR_INVALID, "refine_sweeps < 0");
+  return FG_OK;
+}
+
+void clear_graphs(fg_fluid* f) {
+  for (auto& g : f->graphs) cudaGraphExecDestroy(g.exec);
+  f->graphs.clear();
+}
+
+int check_iters(fg_fluid* f, int iters) {
+  if (iters < 0) return fail(f, FG_ERR_INVALID, "num_iters < 0");
+  if (f->prm.scheme == FG_SCHEME_JACOBI) {
+    int need = std::max(jacobi_launches(f, iters), jacobi_launches(f, f->prm.refine_sweeps)) + 1;
+    if (need > f->n_slots) {
+      CK(f, cudaStreamSynchronize(f->stream), "sync");
+      cudaFree(f->pctl);
+      cudaFree(f->ectl);
+      f->n_slots = need * 2;
+      CK(f, cudaMalloc(&f->pctl, pctl_bytes(f->n_slots)), "pctl alloc");
+      CK(f, cudaMalloc(&f->ectl, pctl_bytes(f->n_slots)), "pctl alloc");
+      CK(f, cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream), "pctl");
+      CK(f, cudaMemsetAsync(f->ectl, 0, pctl_bytes(f->n_slots), f->stream), "pctl");
+      clear_graphs(f);
+    }
+  }
+  return FG_OK;
+}
+
+// Enqueues makeIncompressible's solve with the statistics of the projected
+// field.
+int enqueue_pressure(fg_fluid* f, int iters, float dt) {
+  if (f->prm.use_multigrid && f->prm.multigrid_levels > 1)
+    return fail(f, FG_ERR_UNSUPPORTED, "UseMultigrid is not built for the GPU step");
+  CK(f, launch_pressure(f, iters, dt), "pressure");
+  CK(f, launch_div_stats(f), "div stats");
+  return FG_OK;
+}
+
+// One Simulate(dt) (fluid.go:79-109) as a kernel sequence; swaps the state
+// pointers as the out-of-place stages run.
+int enqueue_step(fg_fluid* f, float dt) {
+  const fg_params& p = f->prm;
+  CK(f, launch_apply_sources(f), "sources");
+  CK(f, launch_clear_stats(f), "clear stats");
+  if (p.scheme == FG_SCHEME_LEXSOR)
+    CK(f, cudaMemsetAsync(f->d[FG_P], 0, field_bytes(f), f->stream), "fill p");
+  if (p.viscosity_diffusion > 0.0f) CK(f, launch_viscosity(f, dt), "viscosity");
+  int rc = enqueue_pressure(f, p.num_iters, dt);
+  if (rc) return rc;
+  CK(f, launch_confinement_turbulence(f, dt, p.confinement != 0.0f, p.turbulence_strength > 0.0f),
+     "confinement/turbulence");
+  CK(f, launch_borders(f), "borders");
+  if (p.use_bfecc) {
+    CK(f, launch_advect_velocity_bfecc(f, dt), "advect velocity");
+    CK(f, launch_advect_smoke_bfecc(f, dt), "advect smoke");
+  } else {
+    CK(f, launch_advect_velocity(f, dt), "advect velocity");
+    CK(f, launch_advect_smoke(f, dt), "advect smoke");
+  }
+  CK(f, launch_smoke_mass(f), "smoke mass");
+  return FG_OK;
+}
+
+void state_key(const fg_fluid* f, float* key[8]) {
+  key[0] = f->d[FG_U];
+  key[1] = f->d[FG_V];
+  key[2] = f->d[FG_M];
+  key[3] = f->partner[FG_U];
+  key[4] = f->partner[FG_V];
+  key[5] = f->partner[FG_M];
+  key[6] = nullptr;
+  key[7] = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_params_default(fg_params* out) {
+  if (!out) return FG_ERR_INVALID;
+  memset(out, 0, sizeof *out);
+  out->confinement = 0.0f;
+  out->viscosity_diffusion = 0.0f;
+  out->pressure_damping = 1.0f;
+  out->turbulence_strength = 0.02f;
+  out->smoke_advection = 1.0f;
+  out->use_multigrid = 0;
+  out->multigrid_levels = 2;
+  out->use_bfecc = 0;
+  out->relaxation = 1.9f;
+  out->num_iters = 8;
+  out->tolerance = 1e-5f;
+  out->early_exit = 1;
+  out->scheme = FG_SCHEME_LEXSOR;
+  out->jacobi_omega = 1.0f;
+  out->tb_depth = 8;
+  out->refine_sweeps = 0;
+  out->use_graphs = 1;
+  return FG_OK;
+}
+
+int fg_create(int width, int height, float density, float h, const fg_params* params,
+              fg_fluid** out) {
+  if (!out || width < 1 || height < 1 || !(h > 0.0f)) return FG_ERR_INVALID;
+  if ((long long)(width + 2) * (height + 2) > (1ll << 30)) return FG_ERR_INVALID;
+  *out = nullptr;
+  fg_fluid* f = new fg_fluid();
+  fg_params_default(&f->prm);
+  if (params) {
+    if (check_params(f, params)) {
+      delete f;
+      return FG_ERR_INVALID;
+    }
+    f->prm = *params;
+  }
+  f->NX = width + 2;
+  f->NY = height + 2;
+  f->P = (f->NY + 31) / 32 * 32;
+  f->density = density;
+  f->h = h;
+  f->g = make_grid(f->NX, f->NY, f->P, h);
+  int rc = FG_OK;
+  auto bail = [&](int code) {
+    fg_destroy(f);
+    return code;
+  };
+  if (cudaGetDevice(&f->device) != cudaSuccess) return bail(FG_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(FG_ERR_CUDA);
+  for (int k = 0; k < 2; ++k) {
+    if (cudaEventCreateWithFlags(&f->edit_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return bail(FG_ERR_CUDA);
+    if (cudaEventCreate(&f->prof_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
+  }
+  for (int k = 0; k < FG_NUM_FIELDS; ++k)
+    if ((rc = alloc_dev(f, &f->d[k]))) return bail(rc);
+  for (int k : {FG_U, FG_V, FG_M})
+    if ((rc = alloc_dev(f, &f->partner[k]))) return bail(rc);
+  float** scratch[] = {&f->fwdU, &f->fwdV, &f->fwdM, &f->corrU, &f->corrV, &f->corrM,
+                       &f->phi,  &f->phi2, &f->rhs,  &f->err,   &f->err2,  &f->rhs_e,
+                       &f->curl, &f->view};
+  for (float** s : scratch)
+    if ((rc = alloc_dev(f, s))) return bail(rc);
+  size_t cells = (size_t)f->NX * f->P;
+  if (cudaMalloc((void**)&f->noise, cells * sizeof(float2)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  if (cudaMalloc((void**)&f->flags, cells) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  int nb = ((f->NY + 31) / 32) * ((f->NX + 7) / 8);
+  f->n_partials = 4 * nb + 64;
+  if (cudaMalloc((void**)&f->partials, sizeof(double) * f->n_partials) != cudaSuccess)
+    return bail(FG_ERR_NOMEM);
+  if (cudaMalloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  f->n_slots = kSlots;
+  if (cudaMalloc(&f->pctl, pctl_bytes(f->n_slots)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  if (cudaMalloc(&f->ectl, pctl_bytes(f->n_slots)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream);
+  cudaMemsetAsync(f->ectl, 0, pctl_bytes(f->n_slots), f->stream);
+  cudaMemsetAsync(f->dstats, 0, sizeof(DevStats), f->stream);
+  cudaMemsetAsync(f->flags, 0, cells, f->stream);
+  size_t hbytes = sizeof(float) * (size_t)f->NX * f->NY;
+  for (int k = 0; k < FG_NUM_FIELDS; ++k) {
+    if (cudaMallocHost((void**)&f->hm[k], hbytes) != cudaSuccess) return bail(FG_ERR_NOMEM);
+    memset(f->hm[k], 0, hbytes);
+    f->host_valid[k] = true;
+  }
+  if (cudaMallocHost((void**)&f->scalar_pinned, 64 * sizeof(float)) != cudaSuccess)
+    return bail(FG_ERR_NOMEM);
+  if (cudaMallocHost((void**)&f->stats_pinned, sizeof(DevStats)) != cudaSuccess)
+    return bail(FG_ERR_NOMEM);
+  if (launch_noise_table(f) != cudaSuccess) return bail(FG_ERR_CUDA);
+  f->masks_stale = true;
+  if (flush(f) || cudaStreamSynchronize(f->stream) != cudaSuccess) return bail(FG_ERR_CUDA);
+  *out = f;
+  return FG_OK;
+}
+
+int fg_destroy(fg_fluid* f) {
+  if (!f) return FG_ERR_INVALID;
+  cudaSetDevice(f->device);
+  if (f->stream) cudaStreamSynchronize(f->stream);
+  clear_graphs(f);
+  for (int k = 0; k < FG_NUM_FIELDS; ++k) {
+    cudaFree(f->d[k]);
+    cudaFree(f->partner[k]);
+    cudaFreeHost(f->hm[k]);
+  }
+  float* scratch[] = {f->fwdU, f->fwdV, f->fwdM, f->corrU, f->corrV, f->corrM, f->phi,
+                      f->phi2, f->rhs,  f->err,  f->err2,  f->rhs_e, f->curl,  f->view,
+                      f->copy_tmp};
+  for (float* s : scratch) cudaFree(s);
+  cudaFree(f->noise);
+  cudaFree(f->flags);
+  cudaFree(f->src_dev);
+  cudaFree(f->src_off_dev);
+  cudaFree(f->partials);
+  cudaFree(f->dstats);
+  cudaFree(f->pctl);
+  cudaFree(f->ectl);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(f->edit_dev[k]);
+    cudaFree(f->edit_off_dev[k]);
+    cudaFreeHost(f->edit_pinned[k]);
+    cudaFreeHost(f->edit_off_pinned[k]);
+    if (f->edit_ev[k]) cudaEventDestroy(f->edit_ev[k]);
+    if (f->prof_ev[k]) cudaEventDestroy(f->prof_ev[k]);
+  }
+  cudaFreeHost(f->scalar_pinned);
+  cudaFreeHost(f->stats_pinned);
+  if (f->stream) cudaStreamDestroy(f->stream);
+  delete f;
+  return FG_OK;
+}
+
+int fg_dims(const fg_fluid* f, int* nx, int* ny) {
+  if (!f || !nx || !ny) return FG_ERR_INVALID;
+  *nx = f->NX;
+  *ny = f->NY;
+  return FG_OK;
+}
+
+float fg_h(const fg_fluid* f) { return f ? f->h : 0.0f; }
+
+int fg_get_params(const fg_fluid* f, fg_params* out) {
+  if (!f || !out) return FG_ERR_INVALID;
+  *out = f->prm;
+  return FG_OK;
+}
+
+int fg_set_params(fg_fluid* f, const fg_params* p) {
+  if (!f || !p) return FG_ERR_INVALID;
+  int rc = check_params(f, p);
+  if (rc) return rc;
+  if (memcmp(&f->prm, p, sizeof *p) != 0) {
+    f->prm = *p;
+    f->params_version++;
+  }
+  return FG_OK;
+}
+
+int fg_field(fg_fluid* f, int field, float** host_ptr) {
+  if (!f || !host_ptr || field < 0 || field >= FG_NUM_FIELDS) return FG_ERR_INVALID;
+  *host_ptr = f->hm[field];
+  return FG_OK;
+}
+
+int fg_mark_dirty(fg_fluid* f, unsigned mask) {
+  if (!f) return FG_ERR_INVALID;
+  for (int k = 0; k < FG_NUM_FIELDS; ++k)
+    if ((mask & FG_FIELD_BIT(k)) && !f->host_valid[k])
+      return fail(f, FG_ERR_INVALID, "mirror is not current: fg_download it before writing");
+  f->dirty |= mask & FG_ALL_FIELDS;
+  return FG_OK;
+}
+
+int fg_download(fg_fluid* f, unsigned mask) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = flush(f);
+  if (rc) return rc;
+  for (int k = 0; k < FG_NUM_FIELDS; ++k)
+    if ((mask & FG_FIELD_BIT(k)) && !f->host_valid[k])
+      if ((rc = download_field(f, k))) return rc;
+  CK(f, cudaStreamSynchronize(f->stream), "download sync");
+  for (int k = 0; k < FG_NUM_FIELDS; ++k)
+    if (mask & FG_FIELD_BIT(k)) f->host_valid[k] = true;
+  return FG_OK;
+}
+
+int fg_synchronize(fg_fluid* f) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  CK(f, cudaStreamSynchronize(f->stream), "synchronize");
+  return FG_OK;
+}
+
+void* fg_stream(fg_fluid* f) { return f ? (void*)f->stream : nullptr; }
+
+int fg_simulate(fg_fluid* f, float dt) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = flush(f);
+  if (rc) return rc;
+  if ((rc = check_iters(f, f->prm.num_iters))) return rc;
+  if (f->prm.use_multigrid && f->prm.multigrid_levels > 1)
+    return fail(f, FG_ERR_UNSUPPORTED, "UseMultigrid is not built for the GPU step");
+  invalidate(f, kStepFields);
+  if (!f->prm.use_graphs) return enqueue_step(f, dt);
+  float* key[8];
+  state_key(f, key);
+  uint32_t dtb;
+  memcpy(&dtb, &dt, 4);
+  for (auto& g : f->graphs) {
+    if (g.dt_bits == dtb && g.version == f->params_version && memcmp(g.key, key, sizeof key) == 0) {
+      CK(f, cudaGraphLaunch(g.exec, f->stream), "graph launch");
+      f->launches += g.launches;
+      // Apply the pointer rotation the captured step performed.
+      f->d[FG_U] = g.post[0];
+      f->d[FG_V] = g.post[1];
+      f->d[FG_M] = g.post[2];
+      f->partner[FG_U] = g.post[3];
+      f->partner[FG_V] = g.post[4];
+      f->partner[FG_M] = g.post[5];
+      return FG_OK;
+    }
+  }
+  // Capture this configuration (at most two entries per configuration: the
+  // rotation alternates between two pointer states).
+  if (f->graphs.size() >= 8) clear_graphs(f);
+  fg_fluid::GraphEntry ent;
+  memcpy(ent.key, key, sizeof key);
+  ent.dt_bits = dtb;
+  ent.version = f->params_version;
+  CK(f, cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  unsigned long long before = f->launches;
+  rc = enqueue_step(f, dt);
+  ent.launches = f->launches - before;
+  f->launches = before;
+  cudaGraph_t graph = nullptr;
+  cudaError_t ec = cudaStreamEndCapture(f->stream, &graph);
+  if (rc || ec != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    // Restore the pre-step pointers; nothing was executed.
+    f->d[FG_U] = key[0];
+    f->d[FG_V] = key[1];
+    f->d[FG_M] = key[2];
+    f->partner[FG_U] = key[3];
+    f->partner[FG_V] = key[4];
+    f->partner[FG_M] = key[5];
+    return rc ? rc : fail(f, FG_ERR_CUDA, "end capture", ec);
+  }
+  ent.post[0] = f->d[FG_U];
+  ent.post[1] = f->d[FG_V];
+  ent.post[2] = f->d[FG_M];
+  ent.post[3] = f->partner[FG_U];
+  ent.post[4] = f->partner[FG_V];
+  ent.post[5] = f->partner[FG_M];
+  ec = cudaGraphInstantiate(&ent.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ec != cudaSuccess) return fail(f, FG_ERR_CUDA, "graph instantiate", ec);
+  f->graphs.push_back(ent);
+  CK(f, cudaGraphLaunch(ent.exec, f->stream), "graph launch");
+  f->launches += ent.launches;
+  return FG_OK;
+}
+
+int fg_get_stats(fg_fluid* f, fg_stats* out) {
+  if (!f || !out) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  CK(f, cudaMemcpyAsync(f->stats_pinned, f->dstats, sizeof(DevStats), cudaMemcpyDeviceToHost,
+                        f->stream), "stats");
+  CK(f, cudaStreamSynchronize(f->stream), "stats sync");
+  const DevStats& s = *f->stats_pinned;
+  memset(out, 0, sizeof *out);
+  out->div_l2_post = std::sqrt(s.div_l2_sq);
+  out->div_max_post = s.div_max;
+  out->div_count_post = s.div_count;
+  out->resid_l2 = std::sqrt(s.resid_l2_sq);
+  out->resid_max = s.resid_max;
+  out->smoke_mass = s.smoke_mass;
+  out->last_maxdiv = s.last_maxdiv;
+  out->sweeps = s.sweeps;
+  return FG_OK;
+}
+
+// ------------------------------------------------------------------ stages
+#define STAGE_PROLOGUE(f)       \
+  if (!(f)) return FG_ERR_INVALID; \
+  int rc = flush(f);            \
+  if (rc) return rc;
+
+int fg_make_incompressible(fg_fluid* f, int num_iters, float dt) {
+  STAGE_PROLOGUE(f);
+  if ((rc = check_iters(f, num_iters))) return rc;
+  invalidate(f, kStepFields);
+  CK(f, launch_clear_stats(f), "clear stats");
+  // copyBorder(newU, U), copyBorder(newV, V) (fluid.go:145-146).
+  CK(f, launch_copy_border(f, f->d[FG_NEWU], f->d[FG_U]), "copy border");
+  CK(f, launch_copy_border(f, f->d[FG_NEWV], f->d[FG_V]), "copy border");
+  return enqueue_pressure(f, num_iters, dt);
+}
+
+int fg_advect_velocity(fg_fluid* f, float dt) {
+  STAGE_PROLOGUE(f);
+  invalidate(f, kStepFields);
+  CK(f, launch_advect_velocity(f, dt), "advect velocity");
+  return FG_OK;
+}
+
+int fg_advect_smoke(fg_fluid* f, float dt) {
+  STAGE_PROLOGUE(f);
+  invalidate(f, kStepFields);
+  CK(f, launch_advect_smoke(f, dt), "advect smoke");
+  return FG_OK;
+}
+
+int fg_advect_velocity_bfecc(fg_fluid* f, float dt) {
+  STAGE_PROLOGUE(f);
+  invalidate(f, kStepFields);
+  CK(f, launch_advect_velocity_bfecc(f, dt), "advect velocity bfecc");
+  return FG_OK;
+}
+
+int fg_advect_smoke_bfecc(fg_fluid* f, float dt) {
+  STAGE_PROLOGUE(f);
+  invalidate(f, kStepFields);
+  CK(f, launch_advect_smoke_bfecc(f, dt), "advect smoke bfecc");
+  return FG_OK;
+}
+
+int fg_handle_borders(fg_fluid* f) {
+  STAGE_PROLOGUE(f);
+  invalidate(f, kStepFields);
+  CK(f, launch_borders(f), "borders");
+  return FG_OK;
+}
+
+int fg_apply_vorticity_confinement(fg_fluid* f, float dt) {
+  STAGE_PROLOGUE(f);
+  invalidate(f, kStepFields);
+  CK(f, launch_confinement_turbulence(f, dt, true, false), "confinement");
+  return FG_OK;
+}
+
+int fg_apply_viscosity(fg_fluid* f, float dt) {
+  STAGE_PROLOGUE(f);
+  if (!(f->prm.viscosity_diffusion > 0.0f)) return FG_OK;  // fluid.go:113-115
+  invalidate(f, kStepFields);
+  CK(f, launch_viscosity(f, dt), "viscosity");
+  return FG_OK;
+}
+
+int fg_add_turbulence(fg_fluid* f, float dt) {
+  STAGE_PROLOGUE(f);
+  if (!(f->prm.turbulence_strength > 0.0f)) return FG_OK;  // fluid.go:497-499
+  invalidate(f, kStepFields);
+  CK(f, launch_confinement_turbulence(f, dt, false, true), "turbulence");
+  return FG_OK;
+}
+
+int fg_clear_pressure(fg_fluid* f) {
+  STAGE_PROLOGUE(f);
+  invalidate(f, FG_FIELD_BIT(FG_P));
+  CK(f, cudaMemsetAsync(f->d[FG_P], 0, field_bytes(f), f->stream), "fill p");
+  return FG_OK;
+}
+
+int fg_copy_border(fg_fluid* f, float* dst, const float* src) {
+  STAGE_PROLOGUE(f);
+  if (!dst || !src) return fail(f, FG_ERR_INVALID, "null buffer");
+  if (!f->copy_tmp)
+    CK(f, cudaMalloc((void**)&f->copy_tmp, 2 * field_bytes(f)), "copy_border alloc");
+  float* dd = f->copy_tmp;
+  float* ds = f->copy_tmp + (size_t)f->NX * f->P;
+  size_t hp = sizeof(float) * f->NY, dp = sizeof(float) * f->P;
+  CK(f, cudaMemcpy2DAsync(dd, dp, dst, hp, hp, f->NX, cudaMemcpyHostToDevice, f->stream), "copy");
+  CK(f, cudaMemcpy2DAsync(ds, dp, src, hp, hp, f->NX, cudaMemcpyHostToDevice, f->stream), "copy");
+  CK(f, launch_copy_border(f, dd, ds), "copy border");
+  CK(f, cudaMemcpy2DAsync(dst, hp, dd, dp, hp, f->NX, cudaMemcpyDeviceToHost, f->stream), "copy");
+  CK(f, cudaStreamSynchronize(f->stream), "copy sync");
+  return FG_OK;
+}
+
+// ------------------------------------------------------------------ tools
+int fg_set_solid(fg_fluid* f, int i, int j, int value) {
+  if (!f) return FG_ERR_INVALID;
+  if (!in_grid(f, i, j)) return fail(f, FG_ERR_INDEX, i < 0 || i >= f->NX ? "invalid x-index" : "invalid y-index");
+  int n = f->NY;
+  int cell = i * n + j;
+  f->hm[FG_S][cell] = value ? 0.0f : 1.0f;
+  f->dirty |= FG_FIELD_BIT(FG_S);
+  if (value) {
+    for (int fld : {FG_U, FG_NEWU}) {
+      edit(f, fld, cell, 0, 0.0f);
+      if (i + 1 < f->NX) edit(f, fld, (i + 1) * n + j, 0, 0.0f);
+    }
+    for (int fld : {FG_V, FG_NEWV}) {
+      edit(f, fld, cell, 0, 0.0f);
+      if (j + 1 < f->NY) edit(f, fld, cell + 1, 0, 0.0f);
+    }
+  }
+  return FG_OK;
+}
+
+int fg_is_solid(const fg_fluid* f, int i, int j, int* out) {
+  if (!f || !out) return FG_ERR_INVALID;
+  if (!in_grid(f, i, j)) return FG_ERR_INDEX;
+  *out = f->hm[FG_S][i * f->NY + j] == 0.0f ? 1 : 0;
+  return FG_OK;
+}
+
+int fg_set_velocity(fg_fluid* f, int i, int j, float u, float v) {
+  if (!f) return FG_ERR_INVALID;
+  if (!in_grid(f, i, j)) return fail(f, FG_ERR_INDEX, i < 0 || i >= f->NX ? "invalid x-index" : "invalid y-index");
+  int cell = i * f->NY + j;
+  edit(f, FG_U, cell, 0, u);
+  edit(f, FG_V, cell, 0, v);
+  return FG_OK;
+}
+
+int fg_add_smoke(fg_fluid* f, int i, int j, float smoke) {
+  if (!f) return FG_ERR_INVALID;
+  if (!in_grid(f, i, j)) return fail(f, FG_ERR_INDEX, i < 0 || i >= f->NX ? "invalid x-index" : "invalid y-index");
+  edit(f, FG_M, i * f->NY + j, 1, smoke);
+  return FG_OK;
+}
+
+int fg_set_velocity_many(fg_fluid* f, int n, const int* is, const int* js, const float* us,
+                         const float* vs) {
+  if (!f || n < 0 || (n && (!is || !js || !us || !vs))) return FG_ERR_INVALID;
+  for (int k = 0; k < n; ++k)
+    if (!in_grid(f, is[k], js[k])) return fail(f, FG_ERR_INDEX, "invalid index");
+  for (int k = 0; k < n; ++k) {
+    int cell = is[k] * f->NY + js[k];
+    edit(f, FG_U, cell, 0, us[k]);
+    edit(f, FG_V, cell, 0, vs[k]);
+  }
+  return FG_OK;
+}
+
+int fg_add_smoke_many(fg_fluid* f, int n, const int* is, const int* js, const float* ss) {
+  if (!f || n < 0 || (n && (!is || !js || !ss))) return FG_ERR_INVALID;
+  for (int k = 0; k < n; ++k)
+    if (!in_grid(f, is[k], js[k])) return fail(f, FG_ERR_INDEX, "invalid index");
+  for (int k = 0; k < n; ++k) edit(f, FG_M, is[k] * f->NY + js[k], 1, ss[k]);
+  return FG_OK;
+}
+
+int fg_set_sources(fg_fluid* f, int n, const int* is, const int* js, const float* us,
+                   const float* vs, const float* smoke, const int* mode) {
+  if (!f || n < 0 || (n && (!is || !js || !mode))) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  std::vector<SourceRec> recs;
+  for (int k = 0; k < n; ++k) {
+    if (!in_grid(f, is[k], js[k])) return fail(f, FG_ERR_INDEX, "invalid source index");
+    SourceRec r;
+    r.cell = (uint32_t)(is[k] * f->NY + js[k]);
+    r.mode = (uint32_t)mode[k];
+    r.u = us ? us[k] : 0.0f;
+    r.v = vs ? vs[k] : 0.0f;
+    r.smoke = smoke ? smoke[k] : 0.0f;
+    recs.push_back(r);
+  }
+  std::stable_sort(recs.begin(), recs.end(),
+                   [](const SourceRec& a, const SourceRec& b) { return a.cell < b.cell; });
+  std::vector<uint32_t> off;
+  if (!recs.empty()) {
+    off.push_back(0);
+    for (size_t k = 1; k < recs.size(); ++k)
+      if (recs[k].cell != recs[k - 1].cell) off.push_back((uint32_t)k);
+    off.push_back((uint32_t)recs.size());
+  }
+  CK(f, cudaStreamSynchronize(f->stream), "sources sync");
+  cudaFree(f->src_dev);
+  cudaFree(f->src_off_dev);
+  f->src_dev = nullptr;
+  f->src_off_dev = nullptr;
+  f->n_src_groups = 0;
+  if (!recs.empty()) {
+    CK(f, cudaMalloc((void**)&f->src_dev, recs.size() * sizeof(SourceRec)), "sources alloc");
+    CK(f, cudaMalloc((void**)&f->src_off_dev, off.size() * sizeof(uint32_t)), "sources alloc");
+    CK(f, cudaMemcpy(f->src_dev, recs.data(), recs.size() * sizeof(SourceRec),
+                     cudaMemcpyHostToDevice), "sources upload");
+    CK(f, cudaMemcpy(f->src_off_dev, off.data(), off.size() * sizeof(uint32_t),
+                     cudaMemcpyHostToDevice), "sources upload");
+    f->n_src_groups = (int)off.size() - 1;
+  }
+  f->params_version++;  // the step graph embeds the source list
+  return FG_OK;
+}
+
+int fg_reset(fg_fluid* f) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  const int fields[] = {FG_U, FG_V, FG_NEWU, FG_NEWV, FG_P, FG_M, FG_NEWM};
+  unsigned mask = 0;
+  for (int k : fields) mask |= FG_FIELD_BIT(k);
+  std::vector<EditRec> keep;
+  for (const EditRec& r : f->edits)
+    if (!(mask & FG_FIELD_BIT(r.field))) keep.push_back(r);
+  f->edits.swap(keep);
+  f->dirty &= ~mask;
+  size_t hbytes = sizeof(float) * (size_t)f->NX * f->NY;
+  for (int k : fields) {
+    CK(f, cudaMemsetAsync(f->d[k], 0, field_bytes(f), f->stream), "reset");
+    memset(f->hm[k], 0, hbytes);
+    f->host_valid[k] = true;
+  }
+  return FG_OK;
+}
+
+int fg_apply_force(fg_fluid* f, int i, int j, float fx, float fy) {
+  if (!f) return FG_ERR_INVALID;
+  if (i < 1 || i >= f->NX - 1 || j < 1 || j >= f->NY - 1) return FG_OK;  // fluid.go:762-764
+  int cell = i * f->NY + j;
+  if (f->hm[FG_S][cell] == 0.0f) return FG_OK;
+  edit(f, FG_U, cell, 1, fx);
+  edit(f, FG_V, cell, 1, fy);
+  return FG_OK;
+}
+
+int fg_apply_force_radius(fg_fluid* f, int cx, int cy, float fx, float fy, int radius) {
+  if (!f) return FG_ERR_INVALID;
+  if (radius <= 0) return fg_apply_force(f, cx, cy, fx, fy);
+  float r2 = (float)(radius * radius);
+  for (int i = cx - radius; i <= cx + radius; ++i)
+    for (int j = cy - radius; j <= cy + radius; ++j) {
+      if (i < 1 || i >= f->NX - 1 || j < 1 || j >= f->NY - 1) continue;
+      float dx = (float)(i - cx), dy = (float)(j - cy);
+      float dist2 = dx * dx + dy * dy;
+      if (dist2 > r2) continue;
+      float weight = (float)std::exp((double)(-3.0f * dist2 / r2));  // fluid.go:792
+      fg_apply_force(f, i, j, fx * weight, fy * weight);
+    }
+  return FG_OK;
+}
+
+int fg_set_circular_obstacle(fg_fluid* f, int cx, int cy, int radius) {
+  if (!f) return FG_ERR_INVALID;
+  for (int i = cx - radius; i <= cx + radius; ++i)
+    for (int j = cy - radius; j <= cy + radius; ++j) {
+      if (i < 0 || i >= f->NX || j < 0 || j >= f->NY) continue;
+      float dx = (float)(i - cx), dy = (float)(j - cy);
+      if (dx * dx + dy * dy <= (float)(radius * radius)) fg_set_solid(f, i, j, 1);
+    }
+  return FG_OK;
+}
+
+// ------------------------------------------------------------------ views
+static int read_scalars(fg_fluid* f, int n) {
+  CK(f, cudaStreamSynchronize(f->stream), "view sync");
+  (void)n;
+  return FG_OK;
+}
+
+static float* dev_scalar_slot(fg_fluid* f) {
+  // The last 8 floats of the partials buffer hold small device results; the
+  // reductions never use them (they need at most 4*nb + 4 doubles).
+  return (float*)f->partials + 2 * (size_t)f->n_partials - 8;
+}
+
+int fg_max_divergence(fg_fluid* f, float* out) {
+  STAGE_PROLOGUE(f);
+  if (!out) return FG_ERR_INVALID;
+  float* slot = dev_scalar_slot(f);
+  CK(f, launch_max_divergence(f, slot), "maxdiv");
+  CK(f, cudaMemcpyAsync(f->scalar_pinned, slot, sizeof(float), cudaMemcpyDeviceToHost, f->stream),
+     "maxdiv");
+  if ((rc = read_scalars(f, 1))) return rc;
+  *out = f->scalar_pinned[0];
+  return FG_OK;
+}
+
+static int view_common(fg_fluid* f, int kind, float* out_host, float* mn, float* mx) {
+  float* slot = dev_scalar_slot(f);
+  CK(f, launch_view(f, kind, slot), "view");
+  CK(f, cudaMemcpyAsync(f->scalar_pinned, slot, 2 * sizeof(float), cudaMemcpyDeviceToHost,
+                        f->stream), "view");
+  if (out_host) {
+    size_t hp = sizeof(float) * f->NY, dp = sizeof(float) * f->P;
+    CK(f, cudaMemcpy2DAsync(out_host, hp, f->view, dp, hp, f->NX, cudaMemcpyDeviceToHost,
+                            f->stream), "view");
+  }
+  int rc = read_scalars(f, 2);
+  if (rc) return rc;
+  if (mn) *mn = f->scalar_pinned[0];
+  if (mx) *mx = f->scalar_pinned[1];
+  return FG_OK;
+}
+
+int fg_vorticity(fg_fluid* f, float* out_host, float* mn, float* mx) {
+  STAGE_PROLOGUE(f);
+  return view_common(f, 0, out_host, mn, mx);
+}
+
+int fg_velocity_magnitude(fg_fluid* f, float* out_host, float* mn, float* mx) {
+  STAGE_PROLOGUE(f);
+  return view_common(f, 1, out_host, mn, mx);
+}
+
+int fg_field_min_max(fg_fluid* f, int field, float* mn, float* mx) {
+  STAGE_PROLOGUE(f);
+  if (field < 0 || field >= FG_NUM_FIELDS) return fail(f, FG_ERR_INVALID, "bad field");
+  float* slot = dev_scalar_slot(f);
+  CK(f, launch_field_minmax(f, field, slot), "minmax");
+  CK(f, cudaMemcpyAsync(f->scalar_pinned, slot, 2 * sizeof(float), cudaMemcpyDeviceToHost,
+                        f->stream), "minmax");
+  if ((rc = read_scalars(f, 2))) return rc;
+  if (mn) *mn = f->scalar_pinned[0];
+  if (mx) *mx = f->scalar_pinned[1];
+  return FG_OK;
+}
+
+int fg_sample_velocity(fg_fluid* f, float x, float y, float* u, float* v) {
+  STAGE_PROLOGUE(f);
+  float* slot = dev_scalar_slot(f);
+  CK(f, launch_sample_velocity(f, x, y, slot), "sample");
+  CK(f, cudaMemcpyAsync(f->scalar_pinned, slot, 2 * sizeof(float), cudaMemcpyDeviceToHost,
+                        f->stream), "sample");
+  if ((rc = read_scalars(f, 2))) return rc;
+  if (u) *u = f->scalar_pinned[0];
+  if (v) *v = f->scalar_pinned[1];
+  return FG_OK;
+}
+
+int fg_adaptive_time_step(fg_fluid* f, float basedt, float* out) {
+  STAGE_PROLOGUE(f);
+  if (!out) return FG_ERR_INVALID;
+  float* slot = dev_scalar_slot(f);
+  CK(f, launch_max_speed(f, slot), "max speed");
+  CK(f, cudaMemcpyAsync(f->scalar_pinned, slot, sizeof(float), cudaMemcpyDeviceToHost, f->stream),
+     "max speed");
+  if ((rc = read_scalars(f, 1))) return rc;
+  float maxVel = f->scalar_pinned[0];
+  if (maxVel == 0.0f) {
+    *out = basedt;
+    return FG_OK;
+  }
+  // fluid.go:550-556 in float32 arithmetic with Go's min / max.
+  float cflFactor = 0.8f;
+  float adaptivedt = cflFactor * f->h / maxVel;
+  *out = host_go_max(host_go_min(adaptivedt, basedt * 2.0f), basedt * 0.1f);
+  return FG_OK;
+}
+
+int fg_profile_enable(fg_fluid* f, int on) {
+  if (!f) return FG_ERR_INVALID;
+  if (f->profile != (on != 0)) {
+    f->profile = on != 0;
+    f->params_version++;  // recapture with or without the event nodes
+  }
+  return FG_OK;
+}
+
+int fg_profile_jacobi(fg_fluid* f, float* ms, int* launches) {
+  if (!f || !ms || !launches) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  CK(f, cudaStreamSynchronize(f->stream), "profile sync");
+  if (!f->profile || f->prof_launches == 0) return fail(f, FG_ERR_INVALID, "no profiled solve");
+  CK(f, cudaEventElapsedTime(ms, f->prof_ev[0], f->prof_ev[1]), "profile elapsed");
+  *launches = f->prof_launches;
+  return FG_OK;
+}
+
+unsigned long long fg_launch_count(const fg_fluid* f) { return f ? f->launches : 0ull; }
+
+unsigned long long fg_edit_bytes(const fg_fluid* f) { return f ? f->edit_bytes : 0ull; }
+
+const char* fg_last_error(const fg_fluid* f) {
+  if (!f) return "invalid handle";
+  return f->last_error.c_str();
+}
+
+}  // extern "C"

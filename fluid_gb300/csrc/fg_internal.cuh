@@ -1,0 +1,239 @@
+// Internal declarations shared by the CUDA translation units of libfluidgpu.
+//
+// Device layout: every field is an array of NX rows of `pitch` floats
+// (pitch = NY rounded up to 32, so rows start on 128-byte boundaries);
+// cell (i, j) sits at i*pitch + j.  Padding cells (j >= NY) are never read
+// by a kernel.  Arithmetic on the simulated fields is FP32 with every
+// operation separately rounded (the library is compiled with -fmad=false;
+// fused multiply-adds appear only as explicit __fmaf_rn calls in the
+// parallel pressure schemes), so a step reproduces the CPU restatement of
+// pkg/fluid bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/fluidgpu.h"
+
+namespace fg {
+
+// Per-cell flag byte (built from S when S changes).
+enum : uint8_t {
+  F_W = 1,          // S[i-1, j] != 0
+  F_E = 2,          // S[i+1, j] != 0
+  F_S = 4,          // S[i, j-1] != 0
+  F_N = 8,          // S[i, j+1] != 0
+  F_FLUID = 16,     // S[i, j] != 0
+  F_INTERIOR = 32,  // 1 <= i <= NX-2 and 1 <= j <= NY-2
+};
+__host__ __device__ inline int flag_count(uint8_t f) {
+  return (f & 1) + ((f >> 1) & 1) + ((f >> 2) & 1) + ((f >> 3) & 1);
+}
+// A cell the pressure relaxation updates: interior, fluid, >= 1 fluid neighbour.
+__host__ __device__ inline bool flag_active(uint8_t f) {
+  return (f & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR) && (f & 15) != 0;
+}
+
+struct Grid {
+  int NX, NY, P;   // NumX, NumY, device pitch (floats)
+  float h;         // grid spacing
+  float h1;        // float32(1.0 / h)           fluid.go:360
+  float hh;        // 0.5 * h  (== h / 2)        fluid.go:298, 361, 406
+  float NXh, NYh;  // float32(NumX) * h, float32(NumY) * h   fluid.go:363-364
+};
+
+inline Grid make_grid(int NX, int NY, int P, float h) {
+  Grid g;
+  g.NX = NX;
+  g.NY = NY;
+  g.P = P;
+  g.h = h;
+  g.h1 = 1.0f / h;
+  g.hh = 0.5f * h;
+  g.NXh = (float)NX * h;
+  g.NYh = (float)NY * h;
+  return g;
+}
+
+// ---------------------------------------------------------------- device helpers
+#ifdef __CUDACC__
+__device__ __forceinline__ float canon_nan() { return __int_as_float(0x7fc00000); }
+// Go's builtin min / max on float32: a NaN argument gives NaN, -0 < +0.
+__device__ __forceinline__ float go_min(float a, float b) {
+  if (isnan(a) || isnan(b)) return canon_nan();
+  if (a == b) return signbit(a) ? a : b;
+  return a < b ? a : b;
+}
+__device__ __forceinline__ float go_max(float a, float b) {
+  if (isnan(a) || isnan(b)) return canon_nan();
+  if (a == b) return signbit(a) ? b : a;
+  return a > b ? a : b;
+}
+__device__ __forceinline__ float fbit(uint8_t f, uint8_t bit) { return (f & bit) ? 1.0f : 0.0f; }
+
+// sampleField / sampleFieldFrom (fluid.go:357-398, 1055-1091).  dx, dy are
+// the staggering offsets of the sampled field (U: 0,h/2; V: h/2,0; M: h/2,h/2).
+__device__ __forceinline__ float sample_field(const float* __restrict__ d, float x, float y,
+                                              float dx, float dy, const Grid& g) {
+  x = go_max(go_min(x, g.NXh), g.h);
+  y = go_max(go_min(y, g.NYh), g.h);
+  float xs = x - dx;
+  float ys = y - dy;
+  int x0 = min((int)floorf(xs * g.h1), g.NX - 1);
+  float tx = (xs - (float)x0 * g.h) * g.h1;
+  int x1 = min(x0 + 1, g.NX - 1);
+  int y0 = min((int)floorf(ys * g.h1), g.NY - 1);
+  float ty = (ys - (float)y0 * g.h) * g.h1;
+  int y1 = min(y0 + 1, g.NY - 1);
+  // Finite inputs keep x0, y0 >= 0; a NaN coordinate converts to 0.
+  x0 = max(x0, 0);
+  y0 = max(y0, 0);
+  x1 = max(x1, 0);
+  y1 = max(y1, 0);
+  float sx = 1.0f - tx;
+  float sy = 1.0f - ty;
+  return sx * sy * d[x0 * g.P + y0] + tx * sy * d[x1 * g.P + y0] + tx * ty * d[x1 * g.P + y1] +
+         sx * ty * d[x0 * g.P + y1];
+}
+#endif
+
+// ---------------------------------------------------------------- handle
+struct EditRec {  // one queued tool edit
+  uint32_t field;
+  uint32_t cell;  // host index i*NY + j
+  uint32_t op;    // 0 = set, 1 = add
+  float value;
+};
+
+struct SourceRec {  // one persistent per-step source (applied at the start of a step)
+  uint32_t cell;      // host index i*NY + j
+  uint32_t mode;      // bit 0: skip if the cell is solid, bit 1: set U,V, bit 2: add smoke
+  float u, v, smoke;
+};
+
+struct DevStats {  // device-side accumulation target (finalised per step)
+  double div_l2_sq, div_max, div_count;
+  double resid_l2_sq, resid_max;
+  double smoke_mass;
+  double last_maxdiv;
+  int sweeps;
+  int pad;
+};
+
+}  // namespace fg
+
+struct fg_fluid {
+  int device = 0;
+  int NX = 0, NY = 0, P = 0;
+  float density = 0, h = 0;
+  fg_params prm;
+  fg::Grid g;
+  cudaStream_t stream = nullptr;
+
+  // State fields on the device (indexed by FG_*), plus one rotation partner
+  // for U, V and M (out-of-place stages swap state and partner).
+  float* d[FG_NUM_FIELDS] = {};
+  float* partner[FG_NUM_FIELDS] = {};
+  // Scratch.
+  float *fwdU = nullptr, *fwdV = nullptr, *fwdM = nullptr;
+  float *corrU = nullptr, *corrV = nullptr, *corrM = nullptr;
+  float *phi = nullptr, *phi2 = nullptr, *rhs = nullptr;
+  float *err = nullptr, *err2 = nullptr, *rhs_e = nullptr;
+  float* curl = nullptr;
+  float* view = nullptr;       // output of the vorticity / magnitude views
+  float2* noise = nullptr;     // per-cell float32(sin(seed)) pairs for addTurbulence
+  uint8_t* flags = nullptr;    // per-cell flag byte
+  double* partials = nullptr;  // block partials of the reductions
+  int n_partials = 0;
+  fg::DevStats* dstats = nullptr;
+  void* pctl = nullptr;   // control block of the main Jacobi solve (k_pressure.cu PCtl)
+  void* ectl = nullptr;   // control block of the FP64-residual correction solve
+  int n_slots = 0;        // launch slots per control block
+  float* copy_tmp = nullptr;        // fg_copy_border staging (2 fields)
+
+  // Host mirrors (pinned) and bookkeeping.
+  float* hm[FG_NUM_FIELDS] = {};  // pinned host mirrors (NX*NY, Go slice layout)
+  bool host_valid[FG_NUM_FIELDS] = {};
+  unsigned dirty = 0;
+  bool masks_stale = true;
+  std::vector<fg::EditRec> edits;
+  // Two staging slots for queued edits, used alternately; a slot is reused
+  // once the event recorded after its upload has completed.
+  fg::EditRec* edit_pinned[2] = {};
+  fg::EditRec* edit_dev[2] = {};
+  uint32_t* edit_off_pinned[2] = {};
+  uint32_t* edit_off_dev[2] = {};
+  cudaEvent_t edit_ev[2] = {};
+  size_t edit_cap[2] = {};
+  int edit_slot = 0;
+  unsigned long long edit_bytes = 0;  // bytes of queued edits uploaded so far
+  // Persistent sources, grouped by cell on the host (offsets into src_dev).
+  fg::SourceRec* src_dev = nullptr;
+  uint32_t* src_off_dev = nullptr;
+  int n_src_groups = 0;
+  // Kernel launches enqueued so far (graph replays add the captured count).
+  unsigned long long launches = 0;
+  // Optional CUDA-event bracket around the main Jacobi launches of a solve.
+  bool profile = false;
+  cudaEvent_t prof_ev[2] = {};
+  int prof_launches = 0;
+  float* scalar_pinned = nullptr;  // small D2H results
+  fg::DevStats* stats_pinned = nullptr;
+  std::string last_error;
+
+  // CUDA graphs of the step, keyed by the state pointers and dt.
+  struct GraphEntry {
+    float* key[8];   // state pointers before the step
+    float* post[6];  // state pointers after it
+    unsigned long long launches;  // kernels in the graph
+    uint32_t dt_bits;
+    uint64_t version;
+    cudaGraphExec_t exec;
+  };
+  std::vector<GraphEntry> graphs;
+  uint64_t params_version = 1;
+};
+
+namespace fg {
+
+// Launchers implemented in the kernel translation units.  All enqueue on
+// f->stream and return cudaGetLastError().
+// k_forces.cu
+cudaError_t launch_build_flags(fg_fluid* f);
+cudaError_t launch_apply_edits(fg_fluid* f, int n_groups, int slot);
+cudaError_t launch_apply_sources(fg_fluid* f);
+cudaError_t launch_viscosity(fg_fluid* f, float dt);  // U,V -> partner, newU/newV = result; swaps
+cudaError_t launch_confinement_turbulence(fg_fluid* f, float dt, bool conf, bool turb);
+cudaError_t launch_borders(fg_fluid* f);
+cudaError_t launch_copy_border(fg_fluid* f, float* dst, const float* src);
+cudaError_t launch_noise_table(fg_fluid* f);
+// k_advect.cu
+cudaError_t launch_advect_velocity(fg_fluid* f, float dt);
+cudaError_t launch_advect_smoke(fg_fluid* f, float dt);
+cudaError_t launch_advect_velocity_bfecc(fg_fluid* f, float dt);
+cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt);
+// k_pressure.cu
+cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt);
+// k_diag.cu
+cudaError_t launch_div_stats(fg_fluid* f);
+cudaError_t launch_smoke_mass(fg_fluid* f);
+cudaError_t launch_clear_stats(fg_fluid* f);
+cudaError_t launch_max_divergence(fg_fluid* f, float* dev_out);
+cudaError_t launch_view(fg_fluid* f, int kind, float* dev_minmax);  // 0 vorticity, 1 magnitude
+cudaError_t launch_field_minmax(fg_fluid* f, int field, float* dev_minmax);
+cudaError_t launch_sample_velocity(fg_fluid* f, float x, float y, float* dev_uv);
+cudaError_t launch_max_speed(fg_fluid* f, float* dev_out);
+
+// Counts one kernel launch on the handle (for the benchmark's launch tally).
+inline void count(fg_fluid* f, int n = 1) { f->launches += (unsigned long long)n; }
+
+inline void swap_state(fg_fluid* f, int field) {
+  float* t = f->d[field];
+  f->d[field] = f->partner[field];
+  f->partner[field] = t;
+}
+
+}  // namespace fg

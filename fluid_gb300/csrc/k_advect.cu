@@ -1,0 +1,310 @@
+// Semi-Lagrangian and BFECC advection of the staggered velocity and the
+// cell-centred smoke (pkg/fluid/fluid.go:291-434 and 909-1120).
+//
+// The reference stages results in the persistent newU/newV/newM buffers and
+// copies them back (fluid.go:331-332, 433); faces or cells it does not
+// advect keep whatever that buffer held ("stale" values, e.g. faces next to
+// a solid).  The kernels reproduce that: a face takes the advected value if
+// it is advected, else the border value of the field being advected if it
+// lies on the ghost ring (copyBorder, fluid.go:293-294), else the stale
+// staging value.  The result is written to the rotation partner of the state
+// field and to the staging buffer, after which state and partner swap.
+#include "fg_internal.cuh"
+
+namespace fg {
+namespace {
+
+constexpr int BX = 32, BY = 8;
+
+inline dim3 cell_grid(const fg_fluid* f) {
+  return dim3((f->NY + BX - 1) / BX, (f->NX + BY - 1) / BY);
+}
+
+__device__ __forceinline__ bool on_ring(int i, int j, const Grid& g) {
+  return i == 0 || j == 0 || i == g.NX - 1 || j == g.NY - 1;
+}
+
+// U face (i, j) is advected iff 1 <= i <= NX-1, 1 <= j <= NY-2, and both
+// adjacent cells are fluid (fluid.go:304).
+__device__ __forceinline__ bool u_advected(uint8_t fl, int i, int j, const Grid& g) {
+  return i >= 1 && j >= 1 && j <= g.NY - 2 && (fl & F_FLUID) && (fl & F_W);
+}
+// V face (i, j): 1 <= i <= NX-2, 1 <= j <= NY-1, both cells fluid (fluid.go:317).
+__device__ __forceinline__ bool v_advected(uint8_t fl, int i, int j, const Grid& g) {
+  return i >= 1 && i <= g.NX - 2 && j >= 1 && (fl & F_FLUID) && (fl & F_S);
+}
+
+// Backtrace of the U face (i, j) through the velocity (Ut, Vt); sdt = dt
+// traces backward in time (x - dt*u), sdt = -dt forward (x + dt*u, BFECC's
+// reverse pass fluid.go:951-952).
+__device__ __forceinline__ float trace_sample_u(const float* __restrict__ Ut,
+                                                const float* __restrict__ Vt,
+                                                const float* __restrict__ Fs, int i, int j,
+                                                float sdt, const Grid& g) {
+  int c = i * g.P + j;
+  float x = (float)i * g.h;
+  float y = (float)j * g.h + g.hh;
+  float u = Ut[c];
+  float v = (Vt[c - g.P] + Vt[c] + Vt[c - g.P + 1] + Vt[c + 1]) * 0.25f;  // avgV fluid.go:342-347
+  x = x - sdt * u;
+  y = y - sdt * v;
+  return sample_field(Fs, x, y, 0.0f, g.hh, g);
+}
+__device__ __forceinline__ float trace_sample_v(const float* __restrict__ Ut,
+                                                const float* __restrict__ Vt,
+                                                const float* __restrict__ Fs, int i, int j,
+                                                float sdt, const Grid& g) {
+  int c = i * g.P + j;
+  float x = (float)i * g.h + g.hh;
+  float y = (float)j * g.h;
+  float u = (Ut[c - 1] + Ut[c] + Ut[c + g.P - 1] + Ut[c + g.P]) * 0.25f;  // avgU fluid.go:335-340
+  float v = Vt[c];
+  x = x - sdt * u;
+  y = y - sdt * v;
+  return sample_field(Fs, x, y, g.hh, 0.0f, g);
+}
+
+// advectVelocity (fluid.go:291-333) with trace field = sampled field =
+// border field = (Ui, Vi); stale values from the staging buffers nU, nV;
+// result to (Uo, Vo) and back into (nU, nV).
+__global__ void k_sl_velocity(const float* __restrict__ Ui, const float* __restrict__ Vi,
+                              float* __restrict__ Uo, float* __restrict__ Vo, float* nU,
+                              float* nV, const uint8_t* __restrict__ flags, float dt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  uint8_t fl = flags[c];
+  bool ring = on_ring(i, j, g);
+  float u, v;
+  if (u_advected(fl, i, j, g))
+    u = trace_sample_u(Ui, Vi, Ui, i, j, dt, g);
+  else
+    u = ring ? Ui[c] : nU[c];
+  if (v_advected(fl, i, j, g))
+    v = trace_sample_v(Ui, Vi, Vi, i, j, dt, g);
+  else
+    v = ring ? Vi[c] : nV[c];
+  Uo[c] = u;
+  Vo[c] = v;
+  nU[c] = u;
+  nV[c] = v;
+}
+
+// BFECC pass 1 (fluid.go:923): forward advection of the original field into
+// (Fu, Fv).  The staging buffers are not written: the final pass reads the
+// same stale values from them (newU = fwdU on the faces that are stale).
+__global__ void k_bfecc_vel_fwd(const float* __restrict__ Ui, const float* __restrict__ Vi,
+                                const float* __restrict__ nU, const float* __restrict__ nV,
+                                float* __restrict__ Fu, float* __restrict__ Fv,
+                                const uint8_t* __restrict__ flags, float dt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  uint8_t fl = flags[c];
+  bool ring = on_ring(i, j, g);
+  Fu[c] = u_advected(fl, i, j, g) ? trace_sample_u(Ui, Vi, Ui, i, j, dt, g) : (ring ? Ui[c] : nU[c]);
+  Fv[c] = v_advected(fl, i, j, g) ? trace_sample_v(Ui, Vi, Vi, i, j, dt, g) : (ring ? Vi[c] : nV[c]);
+}
+
+// clampToNeighbors (fluid.go:1094-1120) for an interior cell (all 3x3
+// neighbours in range).
+__device__ __forceinline__ float clamp3x3(float val, const float* __restrict__ src, int c,
+                                          int P) {
+  float lo = src[c], hi = src[c];
+#pragma unroll
+  for (int di = -1; di <= 1; ++di)
+#pragma unroll
+    for (int dj = -1; dj <= 1; ++dj) {
+      float v = src[c + di * P + dj];
+      if (v < lo) lo = v;
+      if (v > hi) hi = v;
+    }
+  if (val < lo) return lo;
+  if (val > hi) return hi;
+  return val;
+}
+
+// BFECC passes 2-3 (fluid.go:931-987): reverse advection of the forward
+// result traced with the original velocity, error compensation on every
+// interior face (non-advected faces see bwd = 0), clamp to the original
+// field's 3x3 range.  Ring faces keep the original value.
+__global__ void k_bfecc_vel_correct(const float* __restrict__ Ui, const float* __restrict__ Vi,
+                                    const float* __restrict__ Fu, const float* __restrict__ Fv,
+                                    float* __restrict__ Cu, float* __restrict__ Cv,
+                                    const uint8_t* __restrict__ flags, float dt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  if (on_ring(i, j, g)) {
+    Cu[c] = Ui[c];
+    Cv[c] = Vi[c];
+    return;
+  }
+  uint8_t fl = flags[c];
+  float bu = u_advected(fl, i, j, g) ? trace_sample_u(Ui, Vi, Fu, i, j, -dt, g) : 0.0f;
+  float bv = v_advected(fl, i, j, g) ? trace_sample_v(Ui, Vi, Fv, i, j, -dt, g) : 0.0f;
+  float ou = Ui[c], ov = Vi[c];
+  float cu = ou - (bu - ou) * 0.5f;
+  float cv = ov - (bv - ov) * 0.5f;
+  Cu[c] = clamp3x3(cu, Ui, c, g.P);
+  Cv[c] = clamp3x3(cv, Vi, c, g.P);
+}
+
+// advectSmoke (fluid.go:400-434).  Trace velocity (Ut, Vt); sampled field Ms
+// (which also feeds the optional diffusion term); ring cells from Ms; stale
+// cells from nM.  Result to Mo and back into nM.
+__device__ __forceinline__ float smoke_value(const float* __restrict__ Ut,
+                                             const float* __restrict__ Vt,
+                                             const float* __restrict__ Ms, int i, int j,
+                                             float sdt, float smokeAdv, const Grid& g) {
+  int c = i * g.P + j;
+  float u = (Ut[c] + Ut[c + g.P]) * 0.5f * smokeAdv;
+  float v = (Vt[c] + Vt[c + 1]) * 0.5f * smokeAdv;
+  float x = (float)i * g.h + g.hh - sdt * u;
+  float y = (float)j * g.h + g.hh - sdt * v;
+  return sample_field(Ms, x, y, g.hh, g.hh, g);
+}
+
+__global__ void k_sl_smoke(const float* __restrict__ Ut, const float* __restrict__ Vt,
+                           const float* __restrict__ Ms, float* __restrict__ Mo, float* nM,
+                           const uint8_t* __restrict__ flags, float dt, float smokeAdv,
+                           int diffuse, float smokeDiffusion, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  uint8_t fl = flags[c];
+  float m;
+  if ((fl & (F_INTERIOR | F_FLUID)) == (F_INTERIOR | F_FLUID)) {
+    float s = smoke_value(Ut, Vt, Ms, i, j, dt, smokeAdv, g);
+    if (diffuse) {
+      float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
+      s += smokeDiffusion * neighbors;
+    }
+    m = go_max(s, 0.0f);
+  } else {
+    m = on_ring(i, j, g) ? Ms[c] : nM[c];
+  }
+  Mo[c] = m;
+  nM[c] = m;
+}
+
+// BFECC smoke pass 1 (fluid.go:1007): forward advection into Fm without
+// touching the staging buffer.
+__global__ void k_bfecc_smoke_fwd(const float* __restrict__ Ut, const float* __restrict__ Vt,
+                                  const float* __restrict__ Ms, const float* __restrict__ nM,
+                                  float* __restrict__ Fm, const uint8_t* __restrict__ flags,
+                                  float dt, float smokeAdv, int diffuse, float smokeDiffusion,
+                                  Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  uint8_t fl = flags[c];
+  float m;
+  if ((fl & (F_INTERIOR | F_FLUID)) == (F_INTERIOR | F_FLUID)) {
+    float s = smoke_value(Ut, Vt, Ms, i, j, dt, smokeAdv, g);
+    if (diffuse) {
+      float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
+      s += smokeDiffusion * neighbors;
+    }
+    m = go_max(s, 0.0f);
+  } else {
+    m = on_ring(i, j, g) ? Ms[c] : nM[c];
+  }
+  Fm[c] = m;
+}
+
+// BFECC smoke passes 2-3 (fluid.go:1013-1046): reverse advection of the
+// forward result, compensation on every interior cell (non-fluid cells see
+// bwd = 0), clamp to the original 3x3 range, then to >= 0.
+__global__ void k_bfecc_smoke_correct(const float* __restrict__ Ut, const float* __restrict__ Vt,
+                                      const float* __restrict__ Mi, const float* __restrict__ Fm,
+                                      float* __restrict__ Cm, const uint8_t* __restrict__ flags,
+                                      float dt, float smokeAdv, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  if (on_ring(i, j, g)) {
+    Cm[c] = Mi[c];
+    return;
+  }
+  uint8_t fl = flags[c];
+  float b = (fl & F_FLUID) ? smoke_value(Ut, Vt, Fm, i, j, -dt, smokeAdv, g) : 0.0f;
+  float o = Mi[c];
+  float cm = o - (b - o) * 0.5f;
+  cm = clamp3x3(cm, Mi, c, g.P);
+  if (cm < 0.0f) cm = 0.0f;
+  Cm[c] = cm;
+}
+
+}  // namespace
+
+cudaError_t launch_advect_velocity(fg_fluid* f, float dt) {
+  count(f);
+  k_sl_velocity<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(
+      f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV],
+      f->flags, dt, f->g);
+  swap_state(f, FG_U);
+  swap_state(f, FG_V);
+  return cudaGetLastError();
+}
+
+static float smoke_diffusion(const fg_fluid* f, float dt, int* diffuse) {
+  *diffuse = f->prm.viscosity_diffusion > 0.0f ? 1 : 0;
+  return f->prm.viscosity_diffusion * 0.3f * dt;  // fluid.go:422
+}
+
+cudaError_t launch_advect_smoke(fg_fluid* f, float dt) {
+  int diffuse;
+  float sd = smoke_diffusion(f, dt, &diffuse);
+  count(f);
+  k_sl_smoke<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(
+      f->d[FG_U], f->d[FG_V], f->d[FG_M], f->partner[FG_M], f->d[FG_NEWM], f->flags, dt,
+      f->prm.smoke_advection, diffuse, sd, f->g);
+  swap_state(f, FG_M);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_advect_velocity_bfecc(fg_fluid* f, float dt) {
+  dim3 gr = cell_grid(f), bl(BX, BY);
+  count(f);
+  k_bfecc_vel_fwd<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_NEWU],
+                                            f->d[FG_NEWV], f->fwdU, f->fwdV, f->flags, dt, f->g);
+  count(f);
+  k_bfecc_vel_correct<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->fwdU, f->fwdV,
+                                                f->corrU, f->corrV, f->flags, dt, f->g);
+  // Pass 4 (fluid.go:991-993): advect the corrected field with itself.
+  count(f);
+  k_sl_velocity<<<gr, bl, 0, f->stream>>>(f->corrU, f->corrV, f->partner[FG_U],
+                                          f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV],
+                                          f->flags, dt, f->g);
+  swap_state(f, FG_U);
+  swap_state(f, FG_V);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt) {
+  dim3 gr = cell_grid(f), bl(BX, BY);
+  int diffuse;
+  float sd = smoke_diffusion(f, dt, &diffuse);
+  float sa = f->prm.smoke_advection;
+  count(f);
+  k_bfecc_smoke_fwd<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_M],
+                                              f->d[FG_NEWM], f->fwdM, f->flags, dt, sa, diffuse,
+                                              sd, f->g);
+  count(f);
+  k_bfecc_smoke_correct<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_M], f->fwdM,
+                                                  f->corrM, f->flags, dt, sa, f->g);
+  count(f);
+  k_sl_smoke<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->corrM, f->partner[FG_M],
+                                       f->d[FG_NEWM], f->flags, dt, sa, diffuse, sd, f->g);
+  swap_state(f, FG_M);
+  return cudaGetLastError();
+}
+
+}  // namespace fg

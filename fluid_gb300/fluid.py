@@ -1,0 +1,391 @@
+"""Python front end of libfluidgpu with the surface of the Go type fluid.Fluid.
+
+``Fluid`` mirrors pkg/fluid (fluid.go:11-68 for the state and tuning fields,
+walls.go for the tools, the view files for ScalarField/VectorField) over the
+C ABI of include/fluidgpu.h.  Its exported slices U, V, S, M are numpy views
+of the library's pinned host mirrors, laid out like the Go slices (index
+i*NumY + j).
+
+With ``auto_sync=True`` (the default) every call behaves like the Go
+methods: before a device call all mirrors are uploaded, after it they are
+downloaded, so code may read and write the arrays freely between calls.
+With ``auto_sync=False`` the device copy is authoritative: use the tool
+methods for edits and ``download()`` before reading arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+Relaxation = 1.9  # package var fluid.Relaxation (fluid.go:7-9)
+
+FIELDS = {"U": 0, "V": 1, "newU": 2, "newV": 3, "p": 4, "S": 5, "M": 6, "newM": 7}
+ALL_FIELDS = 0xFF
+SCHEME_LEXSOR, SCHEME_JACOBI = 0, 1
+
+# Python attribute -> fg_params member.
+_PARAMS = {
+    "Confinement": "confinement",
+    "ViscosityDiffusion": "viscosity_diffusion",
+    "PressureDamping": "pressure_damping",
+    "TurbulenceStrength": "turbulence_strength",
+    "SmokeAdvection": "smoke_advection",
+    "UseMultigrid": "use_multigrid",
+    "MultigridLevels": "multigrid_levels",
+    "UseBFECC": "use_bfecc",
+    "num_iters": "num_iters",
+    "tolerance": "tolerance",
+    "early_exit": "early_exit",
+    "scheme": "scheme",
+    "jacobi_omega": "jacobi_omega",
+    "tb_depth": "tb_depth",
+    "check_every": "tb_depth",
+    "refine_sweeps": "refine_sweeps",
+    "use_graphs": "use_graphs",
+}
+_BOOL = {"UseMultigrid", "UseBFECC", "early_exit", "use_graphs"}
+
+
+class FluidError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (code %d)" % (msg, code))
+        self.code = code
+
+
+class ScalarField:
+    """pkg/fluid/scalar_field.go:7-22."""
+
+    def __init__(self, nx, ny, values, mn, mx):
+        self.NumX, self.NumY = nx, ny
+        self.values = values
+        self.MinValue, self.MaxValue = mn, mx
+
+    def Value(self, i, j):
+        if i < 0 or i >= self.NumX:
+            return 0.0, "x index (%d) out of range, must be between 0 and %d" % (i, self.NumX - 1)
+        if j < 0 or j >= self.NumY:
+            return 0.0, "y index (%d) out of range, must be between 0 and %d" % (j, self.NumY - 1)
+        return float(self.values[i * self.NumY + j]), None
+
+
+class VectorField:
+    """pkg/fluid/vector_field.go:5-19."""
+
+    def __init__(self, nx, ny, u, v):
+        self.NumX, self.NumY = nx, ny
+        self.valuesU, self.valuesV = u, v
+
+    def Value(self, i, j):
+        if i < 0 or i >= self.NumX:
+            return 0.0, 0.0, "x index out of range, must be between 0 and %d" % (self.NumX - 1)
+        if j < 0 or j >= self.NumY:
+            return 0.0, 0.0, "y index out of range, must be between 0 and %d" % (self.NumY - 1)
+        k = i * self.NumY + j
+        return float(self.valuesU[k]), float(self.valuesV[k]), None
+
+
+class Fluid:
+    """fluid.New(density, width, height, h) on the GPU."""
+
+    dtype = np.float32
+
+    def __init__(self, density, width, height, h, auto_sync=True, **params):
+        L = _lib.lib()
+        object.__setattr__(self, "_L", L)
+        object.__setattr__(self, "_h", ctypes.c_void_p())
+        object.__setattr__(self, "auto_sync", auto_sync)
+        prm = _lib.Params()
+        L.fg_params_default(ctypes.byref(prm))
+        object.__setattr__(self, "_prm", prm)
+        rc = L.fg_create(int(width), int(height), float(density), float(h), ctypes.byref(prm),
+                         ctypes.byref(self._h))
+        if rc != 0:
+            raise FluidError(rc, "fg_create failed")
+        nx, ny = ctypes.c_int(), ctypes.c_int()
+        L.fg_dims(self._h, ctypes.byref(nx), ctypes.byref(ny))
+        object.__setattr__(self, "NumX", nx.value)
+        object.__setattr__(self, "NumY", ny.value)
+        object.__setattr__(self, "numCells", nx.value * ny.value)
+        object.__setattr__(self, "_density", float(np.float32(density)))
+        views = {}
+        for name, k in FIELDS.items():
+            ptr = ctypes.POINTER(ctypes.c_float)()
+            L.fg_field(self._h, k, ctypes.byref(ptr))
+            views[name] = np.ctypeslib.as_array(ptr, shape=(self.numCells,))
+        object.__setattr__(self, "_views", views)
+        for k, v in params.items():
+            setattr(self, k, v)
+
+    def __del__(self):
+        h = self.__dict__.get("_h")
+        if h:
+            self._L.fg_destroy(h)
+            object.__setattr__(self, "_h", None)
+
+    # ------------------------------------------------------------ plumbing
+    def _check(self, rc, what="call"):
+        if rc != 0:
+            msg = self._L.fg_last_error(self._h)
+            raise FluidError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def _push_params(self):
+        self._prm.relaxation = float(Relaxation)
+        self._check(self._L.fg_set_params(self._h, ctypes.byref(self._prm)), "fg_set_params")
+
+    def _before(self):
+        self._push_params()
+        if self.auto_sync:
+            self._check(self._L.fg_mark_dirty(self._h, ALL_FIELDS), "fg_mark_dirty")
+
+    def _after(self):
+        if self.auto_sync:
+            self._check(self._L.fg_download(self._h, ALL_FIELDS), "fg_download")
+
+    def _device(self, fn, *args, what=None):
+        self._before()
+        self._check(fn(self._h, *args), what or fn.__name__)
+        self._after()
+
+    def download(self, mask=ALL_FIELDS):
+        self._check(self._L.fg_download(self._h, mask), "fg_download")
+
+    def mark_dirty(self, mask=ALL_FIELDS):
+        self._check(self._L.fg_mark_dirty(self._h, mask), "fg_mark_dirty")
+
+    def synchronize(self):
+        self._check(self._L.fg_synchronize(self._h), "fg_synchronize")
+
+    @property
+    def stream(self):
+        return self._L.fg_stream(self._h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ------------------------------------------------------------ fields / params
+    U = property(lambda self: self._views["U"])
+    V = property(lambda self: self._views["V"])
+    S = property(lambda self: self._views["S"])
+    M = property(lambda self: self._views["M"])
+    p = property(lambda self: self._views["p"])
+    newU = property(lambda self: self._views["newU"])
+    newV = property(lambda self: self._views["newV"])
+    newM = property(lambda self: self._views["newM"])
+
+    @property
+    def density(self):
+        return self._density
+
+    def H(self):
+        return self._L.fg_h(self._h)
+
+    def __getattr__(self, name):
+        if name in _PARAMS:
+            v = getattr(self.__dict__["_prm"], _PARAMS[name])
+            return bool(v) if name in _BOOL else v
+        raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        if name in _PARAMS:
+            field = _PARAMS[name]
+            ctype = dict(_lib.Params._fields_)[field]
+            setattr(self._prm, field, int(value) if ctype is ctypes.c_int else float(value))
+            self._push_params()
+        else:
+            object.__setattr__(self, name, value)
+
+    # ------------------------------------------------------------ step + stages
+    def Simulate(self, dt):
+        """(*Fluid).Simulate fluid.go:79-109."""
+        self._device(self._L.fg_simulate, ctypes.c_float(dt), what="Simulate")
+
+    def stats(self):
+        st = _lib.Stats()
+        self._check(self._L.fg_get_stats(self._h, ctypes.byref(st)), "fg_get_stats")
+        return {k: getattr(st, k) for k, _ in _lib.Stats._fields_ if k != "reserved"}
+
+    def makeIncompressible(self, numIters, dt):
+        self._device(self._L.fg_make_incompressible, int(numIters), ctypes.c_float(dt))
+
+    def advectVelocity(self, dt):
+        self._device(self._L.fg_advect_velocity, ctypes.c_float(dt))
+
+    def advectSmoke(self, dt):
+        self._device(self._L.fg_advect_smoke, ctypes.c_float(dt))
+
+    def advectVelocityBFECC(self, dt):
+        self._device(self._L.fg_advect_velocity_bfecc, ctypes.c_float(dt))
+
+    def advectSmokeBFECC(self, dt):
+        self._device(self._L.fg_advect_smoke_bfecc, ctypes.c_float(dt))
+
+    def handleBorders(self):
+        self._device(self._L.fg_handle_borders)
+
+    def applyVorticityConfinement(self, dt):
+        self._device(self._L.fg_apply_vorticity_confinement, ctypes.c_float(dt))
+
+    def applyViscosity(self, dt):
+        self._device(self._L.fg_apply_viscosity, ctypes.c_float(dt))
+
+    def addTurbulence(self, dt):
+        self._device(self._L.fg_add_turbulence, ctypes.c_float(dt))
+
+    def clearPressure(self):
+        self._device(self._L.fg_clear_pressure)
+
+    def copyBorder(self, dst, src):
+        assert dst.dtype == np.float32 and src.dtype == np.float32
+        assert dst.size == self.numCells and src.size == self.numCells
+        self._before()
+        self._check(self._L.fg_copy_border(self._h, dst.ctypes.data, src.ctypes.data), "copyBorder")
+        self._after()
+
+    # ------------------------------------------------------------ tools
+    def _index(self, rc, i, j):
+        if rc == _lib.FG_ERR_INDEX:
+            if i < 0 or i >= self.NumX:
+                raise IndexError("invalid x-index: %d" % i)
+            raise IndexError("invalid y-index: %d" % j)
+        self._check(rc)
+
+    def SetSolid(self, i, j, value):
+        self._index(self._L.fg_set_solid(self._h, i, j, int(bool(value))), i, j)
+
+    def IsSolid(self, i, j):
+        out = ctypes.c_int()
+        self._index(self._L.fg_is_solid(self._h, i, j, ctypes.byref(out)), i, j)
+        return bool(out.value)
+
+    def SetVelocity(self, i, j, u, v):
+        self._index(self._L.fg_set_velocity(self._h, i, j, ctypes.c_float(u), ctypes.c_float(v)), i, j)
+
+    def AddSmoke(self, i, j, s):
+        self._index(self._L.fg_add_smoke(self._h, i, j, ctypes.c_float(s)), i, j)
+
+    def SetVelocityMany(self, i, j, u, v):
+        """n SetVelocity calls in order (one C call)."""
+        i, j = np.ascontiguousarray(i, np.int32), np.ascontiguousarray(j, np.int32)
+        u = np.ascontiguousarray(np.broadcast_to(u, i.shape), np.float32)
+        v = np.ascontiguousarray(np.broadcast_to(v, i.shape), np.float32)
+        rc = self._L.fg_set_velocity_many(self._h, i.size, i.ctypes.data, j.ctypes.data,
+                                          u.ctypes.data, v.ctypes.data)
+        if rc == _lib.FG_ERR_INDEX:
+            raise IndexError("invalid index")
+        self._check(rc, "SetVelocityMany")
+
+    def AddSmokeMany(self, i, j, s):
+        i, j = np.ascontiguousarray(i, np.int32), np.ascontiguousarray(j, np.int32)
+        s = np.ascontiguousarray(np.broadcast_to(s, i.shape), np.float32)
+        rc = self._L.fg_add_smoke_many(self._h, i.size, i.ctypes.data, j.ctypes.data, s.ctypes.data)
+        if rc == _lib.FG_ERR_INDEX:
+            raise IndexError("invalid index")
+        self._check(rc, "AddSmokeMany")
+
+    SRC_SKIP_SOLID, SRC_SET_VELOCITY, SRC_ADD_SMOKE = 1, 2, 4
+
+    def set_sources(self, i, j, u=None, v=None, smoke=None, mode=None):
+        """Persistent per-step sources applied on the device before every step."""
+        i = np.ascontiguousarray(i, np.int32)
+        j = np.ascontiguousarray(j, np.int32)
+        n = i.size
+
+        def arr(x, dt, default):
+            return np.ascontiguousarray(np.broadcast_to(default if x is None else x, (n,)), dt)
+
+        u, v, sm = arr(u, np.float32, 0.0), arr(v, np.float32, 0.0), arr(smoke, np.float32, 0.0)
+        md = arr(mode, np.int32, self.SRC_SET_VELOCITY)
+        rc = self._L.fg_set_sources(self._h, n, i.ctypes.data, j.ctypes.data, u.ctypes.data,
+                                    v.ctypes.data, sm.ctypes.data, md.ctypes.data)
+        if rc == _lib.FG_ERR_INDEX:
+            raise IndexError("invalid source index")
+        self._check(rc, "set_sources")
+
+    def launch_count(self):
+        return int(self._L.fg_launch_count(self._h))
+
+    def edit_bytes(self):
+        return int(self._L.fg_edit_bytes(self._h))
+
+    def profile(self, on=True):
+        self._check(self._L.fg_profile_enable(self._h, int(bool(on))), "fg_profile_enable")
+
+    def jacobi_span(self):
+        """(milliseconds, launches) of the main Jacobi launches of the last solve."""
+        ms, n = ctypes.c_float(), ctypes.c_int()
+        self._check(self._L.fg_profile_jacobi(self._h, ctypes.byref(ms), ctypes.byref(n)),
+                    "fg_profile_jacobi")
+        return ms.value, n.value
+
+    def Reset(self):
+        self._check(self._L.fg_reset(self._h), "Reset")
+
+    def ApplyForce(self, i, j, fx, fy):
+        self._check(self._L.fg_apply_force(self._h, i, j, ctypes.c_float(fx), ctypes.c_float(fy)))
+
+    def ApplyForceRadius(self, cx, cy, fx, fy, radius):
+        self._check(self._L.fg_apply_force_radius(self._h, cx, cy, ctypes.c_float(fx),
+                                                  ctypes.c_float(fy), radius))
+
+    def SetCircularObstacle(self, cx, cy, radius):
+        self._check(self._L.fg_set_circular_obstacle(self._h, cx, cy, radius))
+
+    # ------------------------------------------------------------ views
+    def _scalar(self, fn, *args):
+        self._before()
+        outs = [ctypes.c_float() for _ in range(2)]
+        self._check(fn(self._h, *args, *[ctypes.byref(o) for o in outs]))
+        self._after()
+        return [o.value for o in outs]
+
+    def MaxDivergence(self):
+        self._before()
+        out = ctypes.c_float()
+        self._check(self._L.fg_max_divergence(self._h, ctypes.byref(out)), "MaxDivergence")
+        self._after()
+        return out.value
+
+    def GetAdaptiveTimeStep(self, basedt):
+        self._before()
+        out = ctypes.c_float()
+        self._check(self._L.fg_adaptive_time_step(self._h, ctypes.c_float(basedt), ctypes.byref(out)))
+        self._after()
+        return out.value
+
+    def SampleVelocity(self, x, y):
+        return tuple(self._scalar(self._L.fg_sample_velocity, ctypes.c_float(x), ctypes.c_float(y)))
+
+    def _view(self, fn):
+        self._before()
+        out = np.zeros(self.numCells, dtype=np.float32)
+        mn, mx = ctypes.c_float(), ctypes.c_float()
+        self._check(fn(self._h, out.ctypes.data, ctypes.byref(mn), ctypes.byref(mx)))
+        self._after()
+        return ScalarField(self.NumX, self.NumY, out, mn.value, mx.value)
+
+    def Vorticity(self):
+        return self._view(self._L.fg_vorticity)
+
+    def VelocityMagnitude(self):
+        return self._view(self._L.fg_velocity_magnitude)
+
+    def _minmax_view(self, field):
+        mn, mx = self._scalar(self._L.fg_field_min_max, FIELDS[field])
+        if not self.auto_sync:
+            self.download(1 << FIELDS[field])
+        return ScalarField(self.NumX, self.NumY, self._views[field], mn, mx)
+
+    def Pressure(self):
+        return self._minmax_view("p")
+
+    def Smoke(self):
+        return self._minmax_view("M")
+
+    def Velocity(self):
+        if not self.auto_sync:
+            self.download((1 << FIELDS["U"]) | (1 << FIELDS["V"]))
+        return VectorField(self.NumX, self.NumY, self.U, self.V)

@@ -1,0 +1,206 @@
+/*
+ * fluidgpu.h -- C ABI of the GB300 simulation step for pkg/fluid.
+ *
+ * One `fg_fluid` handle stands in for one Go `*fluid.Fluid`.  Every entry
+ * point below replaces one method (or one exported field access) of the Go
+ * package pkg/fluid of TheFellow/fluid; the replaced symbol is cited as
+ * file:line inside that package.  The signatures use plain C types only, so a
+ * cgo, ctypes or JNI binding can call them directly.
+ *
+ * Memory model.  The fields live in device memory (HBM), pitched, x-major
+ * like the reference (cell (i, j) at i*pitch + j, j contiguous).  Each field
+ * also has a pinned host mirror of NumX*NumY floats laid out exactly like the
+ * Go slices (index i*NumY + j), returned by fg_field().  The device copy is
+ * authoritative: fg_download() refreshes a mirror, fg_mark_dirty() schedules
+ * a mirror for upload before the next device operation.  The tool calls
+ * (fg_set_solid, fg_set_velocity, ...) update a mirror that is current and
+ * queue the same edit for the device, so they need no transfer of whole
+ * fields.
+ *
+ * Threading.  A handle is not safe for concurrent use (neither is the Go
+ * type).  Calls may come from different OS threads (cgo moves goroutines):
+ * each call binds the handle's device first.
+ *
+ * Errors.  Every call returns FG_OK (0) or a negative FG_ERR_* code;
+ * fg_last_error() gives the text of the last failure on the handle.  Index
+ * errors (FG_ERR_INDEX) are the cases where the Go methods panic.
+ */
+#ifndef FLUIDGPU_H
+#define FLUIDGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FG_OK 0
+#define FG_ERR_INVALID (-1)     /* bad argument: dimensions, pointer, parameter range   */
+#define FG_ERR_INDEX (-2)       /* cell index out of range (the Go API panics)          */
+#define FG_ERR_CUDA (-3)        /* a CUDA runtime call failed                            */
+#define FG_ERR_UNSUPPORTED (-4) /* option not built for the GPU (UseMultigrid)          */
+#define FG_ERR_MASK (-5)        /* S holds a value other than 0 or 1                     */
+#define FG_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up                    */
+#define FG_ERR_NOMEM (-7)       /* device or pinned allocation failed                    */
+
+/* Field identifiers (Fluid.U, .V, .newU, .newV, .p, .S, .M, .newM). */
+enum {
+  FG_U = 0,
+  FG_V = 1,
+  FG_NEWU = 2,
+  FG_NEWV = 3,
+  FG_P = 4,
+  FG_S = 5,
+  FG_M = 6,
+  FG_NEWM = 7,
+  FG_NUM_FIELDS = 8
+};
+#define FG_FIELD_BIT(f) (1u << (f))
+#define FG_ALL_FIELDS 0xFFu
+
+/* Pressure schemes.  LEXSOR is the reference's serial lexicographic SOR
+ * (fluid.go:157-234) reproduced exactly by a wavefront kernel; JACOBI is the
+ * parallel weighted-Jacobi relaxation of the same masked Poisson system with
+ * temporal blocking. */
+enum { FG_SCHEME_LEXSOR = 0, FG_SCHEME_JACOBI = 1 };
+
+typedef struct fg_params {
+  /* Exported tuning fields of fluid.Fluid (fluid.go:25-39). */
+  float confinement;          /* Confinement                                  */
+  float viscosity_diffusion;  /* ViscosityDiffusion                           */
+  float pressure_damping;     /* PressureDamping                              */
+  float turbulence_strength;  /* TurbulenceStrength                           */
+  float smoke_advection;      /* SmokeAdvection                               */
+  int use_multigrid;          /* UseMultigrid (GPU: FG_ERR_UNSUPPORTED if set) */
+  int multigrid_levels;       /* MultigridLevels                              */
+  int use_bfecc;              /* UseBFECC                                     */
+  float relaxation;           /* package var fluid.Relaxation (fluid.go:7-9)  */
+  /* Constants the reference hard-codes in Simulate / solveSingleGrid. */
+  int num_iters;              /* numIters = 8 (fluid.go:81)                   */
+  float tolerance;            /* early-exit tolerance 1e-5 (fluid.go:159)     */
+  int early_exit;             /* 1 = stop when max|div| < tolerance           */
+  /* GPU scheme selection. */
+  int scheme;                 /* FG_SCHEME_*                                  */
+  float jacobi_omega;         /* Jacobi relaxation weight (times damping)     */
+  int tb_depth;               /* Jacobi sweeps per launch; also the early-exit check interval */
+  int refine_sweeps;          /* FP64-residual outer correction sweeps (0 = off) */
+  int use_graphs;             /* capture each step in a CUDA graph            */
+  int reserved[7];
+} fg_params;
+
+/* Per-step diagnostics, accumulated in FP64 on the device. */
+typedef struct fg_stats {
+  double div_l2_post;    /* sqrt(sum div^2) over fluid interior cells after the projection */
+  double div_max_post;   /* max |div| after the projection                               */
+  double div_count_post; /* number of fluid interior cells                               */
+  double resid_l2;       /* FP64 L2 norm of the pressure residual (parallel schemes)      */
+  double resid_max;      /* FP64 max |residual|                                           */
+  double smoke_mass;     /* sum of M over interior cells after the step                   */
+  double last_maxdiv;    /* max |div| seen by the last pressure sweep                     */
+  int sweeps;            /* pressure sweeps executed (early exit included)                */
+  int reserved[7];
+} fg_stats;
+
+typedef struct fg_fluid fg_fluid;
+
+/* Defaults of fluid.New (fluid.go:42-68) plus numIters = 8, LEXSOR. */
+int fg_params_default(fg_params* out);
+
+/* fluid.New(density, width, height, h) -- fluid.go:42-68.  Allocates the
+ * NumX = width+2 by NumY = height+2 grid on the current device. */
+int fg_create(int width, int height, float density, float h, const fg_params* params,
+              fg_fluid** out);
+/* Releases the handle (no counterpart: Go frees by GC). */
+int fg_destroy(fg_fluid* f);
+int fg_dims(const fg_fluid* f, int* num_x, int* num_y);
+/* Fluid.H() -- fluid.go:71. */
+float fg_h(const fg_fluid* f);
+/* Reads / writes the exported tuning fields (fluid.go:25-39). */
+int fg_get_params(const fg_fluid* f, fg_params* out);
+int fg_set_params(fg_fluid* f, const fg_params* params);
+
+/* Host mirror of a field (the Go slices Fluid.U/.V/.S/.M and the private
+ * p/newU/newV/newM the white-box tests read). */
+int fg_field(fg_fluid* f, int field, float** host_ptr);
+/* Schedules the mirrors in `mask` for upload before the next device call. */
+int fg_mark_dirty(fg_fluid* f, unsigned mask);
+/* Copies the device fields in `mask` into their mirrors (waits). */
+int fg_download(fg_fluid* f, unsigned mask);
+/* Waits for all queued work on the handle's stream. */
+int fg_synchronize(fg_fluid* f);
+/* The handle's CUDA stream (cudaStream_t), for callers that time it. */
+void* fg_stream(fg_fluid* f);
+
+/* (*Fluid).Simulate(dt) -- fluid.go:79-109.  Enqueues one step; returns when
+ * it is queued.  Results are read with fg_download / fg_get_stats. */
+int fg_simulate(fg_fluid* f, float dt);
+/* Statistics of the last step or stage (waits). */
+int fg_get_stats(fg_fluid* f, fg_stats* out);
+
+/* Stage entry points (the unexported methods the reference tests call). */
+int fg_make_incompressible(fg_fluid* f, int num_iters, float dt); /* fluid.go:144-155 */
+int fg_advect_velocity(fg_fluid* f, float dt);                    /* fluid.go:291-333 */
+int fg_advect_smoke(fg_fluid* f, float dt);                       /* fluid.go:400-434 */
+int fg_advect_velocity_bfecc(fg_fluid* f, float dt);              /* fluid.go:911-994 */
+int fg_advect_smoke_bfecc(fg_fluid* f, float dt);                 /* fluid.go:997-1051 */
+int fg_handle_borders(fg_fluid* f);                               /* fluid.go:236-289 */
+int fg_apply_vorticity_confinement(fg_fluid* f, float dt);        /* fluid.go:449-493 */
+int fg_apply_viscosity(fg_fluid* f, float dt);                    /* fluid.go:112-142 */
+int fg_add_turbulence(fg_fluid* f, float dt);                     /* fluid.go:496-526 */
+int fg_clear_pressure(fg_fluid* f);                               /* fill(f.p, 0) fluid.go:83 */
+/* copyBorder(dst, src) -- fluid.go:436-446, on two host arrays of
+ * NumX*NumY floats (run through the device kernel). */
+int fg_copy_border(fg_fluid* f, float* dst, const float* src);
+
+/* Tools (walls.go:5-93, fluid.go:760-796, 893-907). */
+int fg_set_solid(fg_fluid* f, int i, int j, int value);          /* walls.go:5-49   */
+int fg_is_solid(const fg_fluid* f, int i, int j, int* out);      /* walls.go:51-60  */
+int fg_set_velocity(fg_fluid* f, int i, int j, float u, float v);/* walls.go:62-72  */
+int fg_add_smoke(fg_fluid* f, int i, int j, float smoke);        /* walls.go:74-83  */
+int fg_reset(fg_fluid* f);                                       /* walls.go:85-93  */
+int fg_apply_force(fg_fluid* f, int i, int j, float fx, float fy);                 /* fluid.go:761-771 */
+int fg_apply_force_radius(fg_fluid* f, int cx, int cy, float fx, float fy, int r); /* fluid.go:774-796 */
+int fg_set_circular_obstacle(fg_fluid* f, int cx, int cy, int radius);             /* fluid.go:894-907 */
+
+/* Batched forms of SetVelocity / AddSmoke: the same as n calls in order. */
+int fg_set_velocity_many(fg_fluid* f, int n, const int* i, const int* j, const float* u,
+                         const float* v);
+int fg_add_smoke_many(fg_fluid* f, int n, const int* i, const int* j, const float* smoke);
+
+/* Persistent sources, applied on the device at the start of every
+ * fg_simulate, in list order: the per-frame SetVelocity / AddSmoke calls the
+ * reference app makes before Simulate for its jet and its sources
+ * (main/main.go:236-241, 474-486).  mode bit 0: skip the source while its
+ * cell is solid (applySources' IsSolid check); bit 1: set U and V to u, v;
+ * bit 2: add `smoke` to M.  n = 0 clears the list. */
+#define FG_SRC_SKIP_SOLID 1
+#define FG_SRC_SET_VELOCITY 2
+#define FG_SRC_ADD_SMOKE 4
+int fg_set_sources(fg_fluid* f, int n, const int* i, const int* j, const float* u,
+                   const float* v, const float* smoke, const int* mode);
+
+/* Views and diagnostics (fluid.go:798-891, 529-557; pressure.go, smoke.go). */
+int fg_max_divergence(fg_fluid* f, float* out);                                  /* fluid.go:876-891 */
+int fg_vorticity(fg_fluid* f, float* out_host, float* min_val, float* max_val);  /* fluid.go:806-838 */
+int fg_velocity_magnitude(fg_fluid* f, float* out_host, float* min_val, float* max_val); /* fluid.go:841-873 */
+int fg_field_min_max(fg_fluid* f, int field, float* min_val, float* max_val);    /* pressure.go:5-24, smoke.go:5-24 */
+int fg_sample_velocity(fg_fluid* f, float x, float y, float* u, float* v);       /* fluid.go:799-803 */
+int fg_adaptive_time_step(fg_fluid* f, float basedt, float* out);                /* fluid.go:529-557 */
+
+/* Measurement hooks (no counterpart in the reference).  With profiling on,
+ * CUDA events bracket the main Jacobi launches of each pressure solve;
+ * fg_profile_jacobi waits and returns that span and its launch count.
+ * fg_launch_count is the number of kernels the handle has enqueued;
+ * fg_edit_bytes the bytes of queued tool edits uploaded so far. */
+int fg_profile_enable(fg_fluid* f, int on);
+int fg_profile_jacobi(fg_fluid* f, float* ms, int* launches);
+unsigned long long fg_launch_count(const fg_fluid* f);
+unsigned long long fg_edit_bytes(const fg_fluid* f);
+
+/* Text of the last error on the handle ("" if none); static text for a
+ * NULL handle. */
+const char* fg_last_error(const fg_fluid* f);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUIDGPU_H */

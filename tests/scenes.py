@@ -1,0 +1,85 @@
+"""Seeded synthetic scenes shared by the parity tests and the benchmark.
+
+Walls and sources follow the reference app's presets (main/main.go:761-793,
+840-849); every scene only calls the Go API surface, so it runs unchanged on
+the CPU oracle and on the CUDA path.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def apply_walls(f, top=True, bottom=True, left=True, right=False):
+    """applyWallSettings (main/main.go:840-849) after clearing every cell."""
+    for i in range(f.NumX):
+        for j in range(f.NumY):
+            f.SetSolid(i, j, False)
+    for i in range(f.NumX):
+        f.SetSolid(i, 0, bottom)
+        f.SetSolid(i, f.NumY - 1, top)
+    for j in range(f.NumY):
+        f.SetSolid(0, j, left)
+        f.SetSolid(f.NumX - 1, j, right)
+
+
+def fast_walls(f, top=True, bottom=True, left=True, right=False):
+    """Same mask as apply_walls, written directly into S (for large grids)."""
+    S = f.S.reshape(f.NumX, f.NumY)
+    S[:] = 1.0
+    S[:, 0] = 0.0 if bottom else 1.0
+    S[:, -1] = 0.0 if top else 1.0
+    S[0, :] = 0.0 if left else 1.0
+    S[-1, :] = 0.0 if right else 1.0
+
+
+def jet_rows(f, half=4):
+    return range(f.NumY // 2 - half, f.NumY // 2 + half)
+
+
+def jet_inject(f, speed=2.0, smoke=1.0, half=4):
+    """Jet inlet on the left wall: U = speed, M = smoke on 2*half rows at i = 1."""
+    n = f.NumY
+    for j in jet_rows(f, half):
+        f.SetVelocity(1, j, speed, 0.0)
+        f.M[1 * n + j] = smoke
+
+
+def jet_scene(f):
+    apply_walls(f, top=True, bottom=True, left=True, right=False)
+
+
+def karman_scene(f, radius=24, seed=2, noise=1e-3):
+    """Inflow left, outflow right, slip walls top/bottom, disc at (W/4, H/2)."""
+    apply_walls(f, top=True, bottom=True, left=False, right=False)
+    cx, cy = (f.NumX - 2) // 4, (f.NumY - 2) // 2
+    f.SetCircularObstacle(cx, cy, radius)
+    rng = np.random.default_rng(seed)
+    U = f.U.reshape(f.NumX, f.NumY)
+    S = f.S.reshape(f.NumX, f.NumY)
+    U[1:-1, 1:-1] = (1.0 + rng.uniform(-noise, noise, (f.NumX - 2, f.NumY - 2))) * (S[1:-1, 1:-1] != 0)
+
+
+def karman_inflow(f, speed=1.0):
+    n = f.NumY
+    for j in range(1, f.NumY - 1):
+        if f.S[1 * n + j] != 0:
+            f.SetVelocity(1, j, speed, 0.0)
+
+
+def cavity_scene(f):
+    apply_walls(f, top=True, bottom=True, left=True, right=True)
+
+
+def cavity_lid(f, speed=1.0):
+    """Source row under the top wall (main/main.go:774-779), without smoke."""
+    j = f.NumY - 2
+    for i in range(2, f.NumX - 2):
+        f.SetVelocity(i, j, speed, 0.0)
+
+
+def random_state(f, seed=0, amp=1.0, smoke=True):
+    rng = np.random.default_rng(seed)
+    f.U[:] = rng.uniform(-amp, amp, f.numCells).astype(f.dtype)
+    f.V[:] = rng.uniform(-amp, amp, f.numCells).astype(f.dtype)
+    if smoke:
+        f.M[:] = rng.uniform(0, 1, f.numCells).astype(f.dtype)

@@ -1,0 +1,264 @@
+"""Parity of the CUDA step (through the C ABI) with the CPU oracle.
+
+* Reference scheme (LEXSOR, the default): the GPU step must equal the
+  FP32-faithful restatement of pkg/fluid bit for bit, field by field,
+  including the hidden staging buffers newU/newV/newM.
+* Parallel scheme (JACOBI): bit-identical to the oracle's FP32 Jacobi
+  variant for every temporal-blocking depth, and within the stated
+  tolerances of the FP64 oracle: velocity max-abs error <= 1e-4 relative to
+  the field's max, post-projection divergence L2 within 1e-5.
+"""
+import numpy as np
+import pytest
+
+import reference_cases as rc
+import scenes
+from oracle.pyoracle import OracleFluid
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("U", "V", "M", "p", "S", "newU", "newV", "newM")
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import fluid_gb300
+
+    fluid_gb300.build()
+    return fluid_gb300
+
+
+def both(gpu, width, height, density=1.0, h=1.0, **params):
+    g = gpu.Fluid(density, width, height, h, **params)
+    oparams = dict(params)
+    oparams.pop("use_graphs", None)
+    if "tb_depth" in oparams:
+        oparams["check_every"] = oparams.pop("tb_depth")
+    elif oparams.get("scheme", 0) == 1:
+        oparams["check_every"] = 8
+    o = OracleFluid(density, width, height, h, prec=32, **oparams)
+    return g, o
+
+
+def assert_bitwise(g, o, fields=FIELDS, where=""):
+    for k in fields:
+        a, b = getattr(g, k), getattr(o, k)
+        if not np.array_equal(a.view(np.uint32), b.view(np.uint32)):
+            bad = np.flatnonzero(a.view(np.uint32) != b.view(np.uint32))
+            c = bad[0]
+            raise AssertionError("%s %s differs at %d cells; first (i=%d, j=%d): gpu %r oracle %r"
+                                 % (where, k, bad.size, c // g.NumY, c % g.NumY, a[c], b[c]))
+
+
+# ------------------------------------------------------------------ reference tests on the GPU
+@pytest.mark.parametrize("case", rc.ALL_CASES, ids=lambda c: c.__name__)
+def test_reference_case_on_gpu(gpu, case):
+    case(lambda d, w, h, hh: gpu.Fluid(d, w, h, hh))
+
+
+# ------------------------------------------------------------------ bitwise parity, reference scheme
+@pytest.mark.parametrize("bfecc", [False, True])
+def test_jet_128_bitwise_lexsor(gpu, bfecc):
+    """Config 1 shape: 128x128 jet, 40 iterations, 60 steps, every field."""
+    g, o = both(gpu, 128, 128, num_iters=40, UseBFECC=bfecc)
+    for f in (g, o):
+        scenes.jet_scene(f)
+    for step in range(60):
+        for f in (g, o):
+            scenes.jet_inject(f)
+            f.Simulate(0.1)
+        if step % 20 == 19:
+            assert_bitwise(g, o, where="step %d" % step)
+    assert g.stats()["sweeps"] == o.stats()["sweeps"]
+
+
+def test_all_stages_bitwise_lexsor(gpu):
+    """Viscosity, confinement, turbulence, BFECC, an obstacle, odd sizes."""
+    g, o = both(gpu, 37, 29, density=1000.0, h=0.01, ViscosityDiffusion=0.1, Confinement=0.3,
+                PressureDamping=0.95, SmokeAdvection=1.2, UseBFECC=True, num_iters=20)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        f.SetCircularObstacle(15, 14, 4)
+    for step in range(25):
+        for f in (g, o):
+            scenes.jet_inject(f, speed=4.0)
+            if step % 7 == 0:
+                f.ApplyForceRadius(20, 10, 3.0, -2.0, 3)
+                f.AddSmoke(10, 20, 0.5)
+            f.Simulate(1.0 / 120.0)
+    assert_bitwise(g, o)
+
+
+def test_early_exit_matches(gpu):
+    g, o = both(gpu, 30, 20, num_iters=40)
+    for f in (g, o):
+        f.S[:] = 1.0
+        f.ApplyForceRadius(10, 10, 0.01, 0.0, 3)
+        f.Simulate(0.1)
+    assert g.stats()["sweeps"] == o.stats()["sweeps"] < 40
+    assert_bitwise(g, o)
+
+
+def test_zero_field_exits_after_one_sweep(gpu):
+    g, o = both(gpu, 40, 30)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        f.Simulate(1 / 120)
+    assert g.stats()["sweeps"] == o.stats()["sweeps"] == 1
+    assert_bitwise(g, o)
+
+
+# ------------------------------------------------------------------ bitwise parity, Jacobi scheme
+@pytest.mark.parametrize("tb", [1, 3, 8])
+def test_jacobi_bitwise(gpu, tb):
+    g, o = both(gpu, 70, 45, scheme=1, num_iters=30, tb_depth=tb, UseBFECC=True, Confinement=0.2)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        f.SetCircularObstacle(30, 22, 6)
+    for _ in range(15):
+        for f in (g, o):
+            scenes.jet_inject(f, speed=3.0)
+            f.Simulate(0.1)
+    assert_bitwise(g, o)
+    sg, so = g.stats(), o.stats()
+    assert sg["sweeps"] == so["sweeps"]
+    assert sg["resid_l2"] == pytest.approx(so["resid_l2"], rel=1e-9, abs=1e-12)
+
+
+def test_jacobi_early_exit_bitwise(gpu):
+    g, o = both(gpu, 33, 33, scheme=1, num_iters=200, tb_depth=4, tolerance=1e-3)
+    for f in (g, o):
+        f.S[:] = 1.0
+        f.S[: f.NumY] = 0.0
+        scenes.random_state(f, seed=3, amp=0.01)
+        f.makeIncompressible(200, 0.1)
+    assert g.stats()["sweeps"] == o.stats()["sweeps"] < 200
+    assert_bitwise(g, o, fields=("U", "V", "p"))
+
+
+def test_jacobi_refinement_bitwise(gpu):
+    g, o = both(gpu, 50, 40, scheme=1, num_iters=40, tb_depth=8, refine_sweeps=16, early_exit=False)
+    for f in (g, o):
+        scenes.cavity_scene(f)
+        scenes.random_state(f, seed=5)
+        f.makeIncompressible(40, 0.1)
+    assert_bitwise(g, o, fields=("U", "V", "p"))
+    sg, so = g.stats(), o.stats()
+    assert sg["resid_l2"] == pytest.approx(so["resid_l2"], rel=1e-9)
+
+
+def test_jacobi_against_fp64_oracle(gpu):
+    """Per-step error of the FP32 GPU step against the FP64 oracle."""
+    g = gpu.Fluid(1.0, 96, 64, 1.0, scheme=1, num_iters=100, tb_depth=8, UseBFECC=True,
+                  Confinement=0.3)
+    o = OracleFluid(1.0, 96, 64, 1.0, prec=64, scheme=1, num_iters=100, check_every=8,
+                    UseBFECC=True, Confinement=0.3)
+    for f in (g, o):
+        scenes.karman_scene(f, radius=8)
+    for _ in range(5):
+        for f in (g, o):
+            scenes.karman_inflow(f)
+            f.Simulate(0.1)
+    scale = float(np.abs(o.U).max())
+    err = max(float(np.abs(g.U.astype(np.float64) - o.U).max()),
+              float(np.abs(g.V.astype(np.float64) - o.V).max())) / scale
+    assert err <= 1e-4, err
+    assert abs(g.stats()["div_l2_post"] - o.stats()["div_l2_post"]) <= 1e-5
+
+
+# ------------------------------------------------------------------ API behaviour
+def test_graphs_do_not_change_results(gpu):
+    a = gpu.Fluid(1.0, 40, 30, 1.0, use_graphs=True, UseBFECC=True, num_iters=20)
+    b = gpu.Fluid(1.0, 40, 30, 1.0, use_graphs=False, UseBFECC=True, num_iters=20)
+    for f in (a, b):
+        scenes.jet_scene(f)
+    for _ in range(12):
+        for f in (a, b):
+            scenes.jet_inject(f)
+            f.Simulate(0.1)
+    for k in FIELDS:
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+
+
+def test_explicit_sync_mode_matches_auto(gpu):
+    """auto_sync=False: tool calls only, device authoritative, one download."""
+    a = gpu.Fluid(1.0, 48, 40, 1.0, num_iters=20)
+    b = gpu.Fluid(1.0, 48, 40, 1.0, num_iters=20, auto_sync=False)
+    for f in (a, b):
+        scenes.apply_walls(f)
+    for step in range(10):
+        for f in (a, b):
+            for j in scenes.jet_rows(f):
+                f.SetVelocity(1, j, 2.0, 0.0)
+                f.AddSmoke(1, j, 1.0)
+            f.Simulate(0.1)
+    b.download()
+    for k in FIELDS:
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+
+
+def test_views_match_oracle(gpu):
+    g, o = both(gpu, 30, 25, num_iters=10)
+    for f in (g, o):
+        scenes.jet_scene(f)
+    for _ in range(10):
+        for f in (g, o):
+            scenes.jet_inject(f, speed=5.0)
+            f.Simulate(0.05)
+    assert g.MaxDivergence() == np.float32(o.MaxDivergence())
+    for name in ("Vorticity", "VelocityMagnitude"):
+        vg, vo = getattr(g, name)(), getattr(o, name)()
+        assert np.array_equal(vg.values, vo.values), name
+        assert vg.MinValue == np.float32(vo.MinValue) and vg.MaxValue == np.float32(vo.MaxValue)
+    for x, y in ((3.3, 7.1), (0.0, 0.0), (100.0, 100.0), (12.5, 12.5)):
+        ug, vg_ = g.SampleVelocity(x, y)
+        uo, vo_ = o.SampleVelocity(x, y)
+        assert (ug, vg_) == (np.float32(uo), np.float32(vo_))
+    assert g.GetAdaptiveTimeStep(0.08) == np.float32(o.GetAdaptiveTimeStep(0.08))
+    sm = g.Smoke()
+    assert sm.MinValue == float(o.M.min()) and sm.MaxValue == float(o.M.max())
+
+
+def test_stage_entry_points_bitwise(gpu):
+    g, o = both(gpu, 21, 17, ViscosityDiffusion=0.2, Confinement=1.0)
+    for f in (g, o):
+        f.S[:] = 1.0
+        f.S[5 * f.NumY + 5] = 0.0
+        scenes.random_state(f, seed=7)
+    for name, args in (("applyViscosity", (0.1,)), ("makeIncompressible", (12, 0.1)),
+                       ("applyVorticityConfinement", (0.1,)), ("addTurbulence", (0.1,)),
+                       ("handleBorders", ()), ("advectVelocity", (0.1,)), ("advectSmoke", (0.1,)),
+                       ("advectVelocityBFECC", (0.1,)), ("advectSmokeBFECC", (0.1,))):
+        for f in (g, o):
+            getattr(f, name)(*args)
+        assert_bitwise(g, o, where=name)
+
+
+def test_invalid_mask_fails_loudly(gpu):
+    f = gpu.Fluid(1.0, 8, 8, 1.0)
+    f.S[:] = 0.5
+    with pytest.raises(gpu.FluidError) as e:
+        f.Simulate(0.1)
+    assert e.value.code == -5
+
+
+def test_multigrid_reports_unsupported(gpu):
+    f = gpu.Fluid(1.0, 8, 8, 1.0, UseMultigrid=True)
+    f.S[:] = 1.0
+    with pytest.raises(gpu.FluidError) as e:
+        f.Simulate(0.1)
+    assert e.value.code == -4
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (1, 7), (9, 1), (2, 3), (65, 33)])
+def test_small_and_ragged_grids_bitwise(gpu, w, h):
+    for scheme in (0, 1):
+        g, o = both(gpu, w, h, scheme=scheme, num_iters=6, tb_depth=2, UseBFECC=True)
+        for f in (g, o):
+            f.S[:] = 1.0
+            f.S[: f.NumY] = 0.0
+            scenes.random_state(f, seed=w * 100 + h)
+        for _ in range(3):
+            for f in (g, o):
+                f.Simulate(0.05)
+        assert_bitwise(g, o, where="%dx%d scheme %d" % (w, h, scheme))
