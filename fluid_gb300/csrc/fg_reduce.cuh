@@ -3,6 +3,8 @@
 // result does not depend on scheduling or on atomics.
 #pragma once
 
+#include <cfloat>
+
 #include "fg_internal.cuh"
 
 namespace fg {
@@ -24,7 +26,7 @@ __device__ __forceinline__ double block_reduce(double v, double* sh) {
   if ((tid & 31) == 0) sh[tid >> 5] = v;
   __syncthreads();
   if (tid < 32) {
-    v = tid < (nt >> 5) ? sh[tid] : 0.0;
+    v = tid < (nt >> 5) ? sh[tid] : (MAX ? -DBL_MAX : 0.0);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       double w = __shfl_down_sync(0xffffffffu, v, o);
