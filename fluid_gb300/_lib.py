@@ -18,6 +18,8 @@ FG_ERR_UNSUPPORTED = -4
 FG_ERR_MASK = -5
 FG_ERR_TIMEOUT = -6
 FG_ERR_NOMEM = -7
+FG_ERR_TOO_LARGE = -8
+NOALLOC_MAX_CELLS = 1 << 20
 
 _c_i, _c_f, _c_d = ctypes.c_int, ctypes.c_float, ctypes.c_double
 
@@ -90,6 +92,8 @@ SIGNATURES = {
     "fg_profile_jacobi": (_c_i, [_vp, _fp, ctypes.POINTER(_c_i)]),
     "fg_launch_count": (ctypes.c_ulonglong, [_vp]),
     "fg_edit_bytes": (ctypes.c_ulonglong, [_vp]),
+    "fg_project_noalloc": (_c_i, [_vp, _vp, _vp, _vp, _c_i, _c_i, _c_i, _c_f, _c_f, _c_f, _c_i,
+                                  _c_f, _c_f, _c_i, _c_i, _c_f, _vp]),
     "fg_last_error": (ctypes.c_char_p, [_vp]),
 }
 

@@ -20,6 +20,8 @@
 //    there, so HBM sees one read and one write of phi per launch.  Optional
 //    outer correction: an FP64 residual of the FP32 iterate, a correction
 //    solve on it, phi += e.
+#include <mutex>
+
 #include "fg_internal.cuh"
 #include "fg_reduce.cuh"
 
@@ -476,3 +478,114 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt) {
 }
 
 }  // namespace fg
+
+// ===========================================================================
+// Projection without allocation.
+//
+// Some callers cannot allocate device memory at the moment they need a
+// projection: an embedding engine whose allocator owns all of the device
+// memory, a real-time loop that forbids cudaMalloc (it may synchronise the
+// device), or code running where allocation is not allowed at all.  For them
+// fg_project_noalloc runs the Jacobi projection on caller-owned fields using
+// the scratch array below instead of the handle's buffers.  The array is a
+// fixed part of the library image, so every GPU that loads the library holds
+// it (about 13 MiB) until the process exits.
+// ===========================================================================
+namespace fg {
+namespace {
+
+constexpr size_t kNoAllocMaxCells = (size_t)FG_NOALLOC_MAX_CELLS;  // num_x * pitch
+constexpr int kNoAllocSlots = 4096;                                  // Jacobi launches per call
+constexpr size_t kNoAllocCtlBytes = 256 + sizeof(unsigned) * kNoAllocSlots;
+constexpr size_t kNoAllocBytes = 13 * kNoAllocMaxCells + kNoAllocCtlBytes;
+
+// Scratch shared by every call on a device: phi, phi2, rhs (floats), the
+// flag bytes and the control block, carved at fixed offsets.  It keeps the
+// previous call's contents; each call rewrites or clears what it reads.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Flag bytes from a caller-owned S (nonzero = fluid).
+__global__ void k_noalloc_flags(const float* __restrict__ S, uint8_t* __restrict__ flags, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  uint8_t fl = 0;
+  if (S[c] != 0.0f) fl |= F_FLUID;
+  if (i > 0 && S[c - g.P] != 0.0f) fl |= F_W;
+  if (i < g.NX - 1 && S[c + g.P] != 0.0f) fl |= F_E;
+  if (j > 0 && S[c - 1] != 0.0f) fl |= F_S;
+  if (j < g.NY - 1 && S[c + 1] != 0.0f) fl |= F_N;
+  if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2) fl |= F_INTERIOR;
+  flags[c] = fl;
+}
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[256] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the first call on each device does it).
+cudaError_t noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace fg
+
+extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x,
+                                  int num_y, int pitch, float density, float h, float dt,
+                                  int num_iters, float jacobi_omega, float pressure_damping,
+                                  int tb_depth, int early_exit, float tolerance, void* stream) {
+  using namespace fg;
+  if (!u || !v || !p || !s || num_x < 3 || num_y < 3 || pitch < num_y || num_iters < 0 ||
+      !(h > 0.0f) || dt == 0.0f)
+    return FG_ERR_INVALID;
+  if ((size_t)num_x * (size_t)pitch > kNoAllocMaxCells) return FG_ERR_TOO_LARGE;
+  int T = tb_depth < 1 ? 1 : (tb_depth > TMAX ? TMAX : tb_depth);
+  int nlaunch = (num_iters + T - 1) / T;
+  if (nlaunch > kNoAllocSlots) return FG_ERR_TOO_LARGE;
+  void* base = nullptr;
+  if (noalloc_scratch(&base) != cudaSuccess) return FG_ERR_CUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned char* b = (unsigned char*)base;
+  float* phi = (float*)b;
+  float* phi2 = (float*)(b + 4 * kNoAllocMaxCells);
+  float* rhs = (float*)(b + 8 * kNoAllocMaxCells);
+  uint8_t* flags = b + 12 * kNoAllocMaxCells;
+  PCtl* ctl = (PCtl*)(b + 13 * kNoAllocMaxCells);
+  Grid g = make_grid(num_x, num_y, pitch, h);
+  WTab w;
+  float om = jacobi_omega * pressure_damping;
+  w.w[0] = 0.0f;
+  for (int k = 1; k <= 4; ++k) w.w[k] = om / (float)k;
+  float cp = density * h / dt;
+  dim3 gr((num_y + BX - 1) / BX, (num_x + BY - 1) / BY), bl(BX, BY);
+  // The control words start at zero (sel = 0 until a launch runs).
+  if (cudaMemsetAsync(ctl, 0, pctl_bytes(nlaunch), st) != cudaSuccess) return FG_ERR_CUDA;
+  k_noalloc_flags<<<gr, bl, 0, st>>>(s, flags, g);
+  k_setup_system<<<gr, bl, 0, st>>>(u, v, phi, phi2, rhs, flags, g);
+  dim3 tg((num_y + TJ - 1) / TJ, (num_x + TI - 1) / TI);
+  int check = early_exit ? 1 : 0;
+  for (int k = 0; k < nlaunch; ++k) {
+    int t0 = k * T;
+    int ns = num_iters - t0 < T ? num_iters - t0 : T;
+    const float* src = (k & 1) ? phi2 : phi;
+    float* dst = (k & 1) ? phi : phi2;
+    k_jacobi_tb<<<tg, TB_THREADS, 0, st>>>(src, dst, rhs, flags, w, ctl, k, t0, ns, check,
+                                           tolerance, (k & 1) ? 0 : 1, g);
+  }
+  k_grad<<<gr, bl, 0, st>>>(u, v, p, phi, phi2, ctl, flags, cp, g);
+  return cudaGetLastError() == cudaSuccess ? FG_OK : FG_ERR_CUDA;
+}

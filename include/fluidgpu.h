@@ -40,6 +40,7 @@ extern "C" {
 #define FG_ERR_MASK (-5)        /* S holds a value other than 0 or 1                     */
 #define FG_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up                    */
 #define FG_ERR_NOMEM (-7)       /* device or pinned allocation failed                    */
+#define FG_ERR_TOO_LARGE (-8)   /* grid beyond the fixed scratch of fg_project_noalloc    */
 
 /* Field identifiers (Fluid.U, .V, .newU, .newV, .p, .S, .M, .newM). */
 enum {
@@ -194,6 +195,31 @@ int fg_profile_enable(fg_fluid* f, int on);
 int fg_profile_jacobi(fg_fluid* f, float* ms, int* launches);
 unsigned long long fg_launch_count(const fg_fluid* f);
 unsigned long long fg_edit_bytes(const fg_fluid* f);
+
+/* Pressure projection that allocates nothing (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc when they project: an
+ * engine whose own allocator owns the device memory, a frame loop that must
+ * not risk the device-wide synchronisation an allocation can cause, or code
+ * where allocation is forbidden.  It runs the JACOBI projection of
+ * fg_make_incompressible (same kernels, same results) on caller-owned device
+ * fields: u, v (in/out, staggered faces), p (out) and s (in, 0 = solid,
+ * 1 = fluid; any nonzero value counts as fluid), each num_x rows of `pitch`
+ * floats (pitch >= num_y), cell (i, j) at i*pitch + j.  Its scratch is a
+ * fixed array inside the library of FG_NOALLOC_MAX_CELLS cells (about
+ * 13 MiB, held on every GPU that loads the library until the process exits):
+ * num_x * pitch above FG_NOALLOC_MAX_CELLS, or more than 4096 Jacobi
+ * launches (num_iters / tb_depth), returns FG_ERR_TOO_LARGE.  The work is
+ * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream)
+ * and the call returns without waiting.  The first call on a device looks up
+ * the scratch array's device address; make that first call before any stream
+ * capture.  All calls on a device share the one scratch array, so calls
+ * whose work can overlap on the GPU (other streams, other host threads) race
+ * and must be ordered by the caller. */
+#define FG_NOALLOC_MAX_CELLS (1 << 20)
+int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x, int num_y,
+                       int pitch, float density, float h, float dt, int num_iters,
+                       float jacobi_omega, float pressure_damping, int tb_depth, int early_exit,
+                       float tolerance, void* stream);
 
 /* Text of the last error on the handle ("" if none); static text for a
  * NULL handle. */
