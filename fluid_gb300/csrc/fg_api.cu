@@ -327,7 +327,7 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
     if ((rc = alloc_dev(f, &f->partner[k]))) return bail(rc);
   float** scratch[] = {&f->fwdU, &f->fwdV, &f->fwdM, &f->corrU, &f->corrV, &f->corrM,
                        &f->phi,  &f->phi2, &f->rhs,  &f->err,   &f->err2,  &f->rhs_e,
-                       &f->curl, &f->view};
+                       &f->curl, &f->view, &f->wgt,  &f->bw,    &f->bwe};
   for (float** s : scratch)
     if ((rc = alloc_dev(f, s))) return bail(rc);
   size_t cells = (size_t)f->NX * f->P;
@@ -374,7 +374,7 @@ int fg_destroy(fg_fluid* f) {
   }
   float* scratch[] = {f->fwdU, f->fwdV, f->fwdM, f->corrU, f->corrV, f->corrM, f->phi,
                       f->phi2, f->rhs,  f->err,  f->err2,  f->rhs_e, f->curl,  f->view,
-                      f->copy_tmp};
+                      f->wgt,  f->bw,   f->bwe,  f->copy_tmp};
   for (float* s : scratch) cudaFree(s);
   cudaFree(f->noise);
   cudaFree(f->flags);

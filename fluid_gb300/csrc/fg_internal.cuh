@@ -142,6 +142,7 @@ struct fg_fluid {
   float *corrU = nullptr, *corrV = nullptr, *corrM = nullptr;
   float *phi = nullptr, *phi2 = nullptr, *rhs = nullptr;
   float *err = nullptr, *err2 = nullptr, *rhs_e = nullptr;
+  float *wgt = nullptr, *bw = nullptr, *bwe = nullptr;  // Jacobi w = om/s, w*b, w*b_e
   float* curl = nullptr;
   float* view = nullptr;       // output of the vorticity / magnitude views
   float2* noise = nullptr;     // per-cell float32(sin(seed)) pairs for addTurbulence

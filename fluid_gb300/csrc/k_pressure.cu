@@ -161,50 +161,61 @@ struct WTab {
   float w[5];  // w[s] = (omega * damping) / s
 };
 
-// b = -div on active cells, phi = 0 everywhere (ring included).
+// Per cell: b = -div, w = om / s and bw = w * b on active cells, all 0
+// elsewhere (ring included); phi = 0 when `zero_phi` (a solve with no sweeps
+// reads it directly).
+// U, V use the grid pitch g.P, the solver arrays the pitch Ps.
 __global__ void k_setup_system(const float* __restrict__ U, const float* __restrict__ V,
-                               float* __restrict__ phi, float* __restrict__ phi2,
-                               float* __restrict__ rhs, const uint8_t* __restrict__ flags,
-                               Grid g) {
+                               float* __restrict__ phi, float* __restrict__ rhs,
+                               float* __restrict__ W, float* __restrict__ BW,
+                               const uint8_t* __restrict__ flags, float om, int zero_phi, Grid g,
+                               int Ps) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
-  int c = i * g.P + j;
-  float b = 0.0f;
-  if (flag_active(flags[c])) {
-    float div = U[c + g.P] - U[c] + V[c + 1] - V[c];
+  int u = i * g.P + j;
+  int c = i * Ps + j;
+  float b = 0.0f, w = 0.0f, bw = 0.0f;
+  uint8_t fl = flags[c];
+  if (flag_active(fl)) {
+    float div = U[u + g.P] - U[u] + V[u + 1] - V[u];
     b = -div;
+    w = om / (float)flag_count(fl);
+    bw = w * b;
   }
   rhs[c] = b;
-  phi[c] = 0.0f;
-  phi2[c] = 0.0f;
+  W[c] = w;
+  BW[c] = bw;
+  if (zero_phi) phi[c] = 0.0f;
 }
 
-__device__ __forceinline__ float jacobi_cell(float x, float nb, float b, int s, const WTab& w,
-                                             float* r_out) {
-  float t1 = b + nb;
-  float r = __fmaf_rn(-(float)s, x, t1);
-  *r_out = r;
-  return __fmaf_rn(w.w[s], r, x);
-}
+// Register-blocked, temporally blocked Jacobi.  A CTA of 8 warps holds a
+// 64 x 128 region (rows i x columns j) in registers: each thread a block of
+// RT = 8 rows by JT = 4 consecutive columns.  Vertical neighbours come from
+// the thread's own rows, or through shared memory from the warp above/below
+// at its first/last row; horizontal neighbours from the thread's own columns
+// or a warp shuffle.  `ns` <= H sweeps run per launch; the region carries a
+// halo of H = 8 cells on each side, so the CTA owns the inner 48 x 112 cells
+// and writes only those.  Cells outside the grid or inactive have w = bw = 0
+// and stay 0.  Launch k first decides whether the solve already stopped
+// (thread 0 of every CTA reads the same control words, so all CTAs agree);
+// a running launch records the max |r| of its last sweep over the active
+// cells it owns, r = fma(-s, phi, b + nb), in slots[k].
+constexpr int JT = 4, RT = 8, NWARP = 8, TMAX = 8;
+constexpr int RJ = 32 * JT;        // 128 region columns
+constexpr int RI = NWARP * RT;     // 64 region rows
+constexpr int OJ = RJ - 2 * TMAX;  // 112 owned columns
+constexpr int OI = RI - 2 * TMAX;  // 48 owned rows
+constexpr int TB_THREADS = 32 * NWARP;
 
-// Temporally blocked Jacobi: `ns` sweeps of a TI x TJ tile with a halo of
-// TMAX cells (ns <= TMAX) in shared memory.  Launch k of a solve first
-// decides whether the solve already stopped (thread 0 of every CTA reads the
-// same control words, so all CTAs agree); a running launch records the max
-// |r| of its last sweep over the cells it owns in slots[k].
-constexpr int TI = 32, TJ = 48, TMAX = 8;
-constexpr int RI = TI + 2 * TMAX, RJ = TJ + 2 * TMAX;
-constexpr int TB_THREADS = 256;
-
-__global__ void __launch_bounds__(TB_THREADS)
-    k_jacobi_tb(const float* __restrict__ src, float* __restrict__ dst,
-                const float* __restrict__ rhs, const uint8_t* __restrict__ flags, WTab w,
+template <bool OMEGA1, bool ZERO_INIT>
+__global__ void __launch_bounds__(TB_THREADS, 2)
+    k_jacobi_rb(const float* __restrict__ src, float* __restrict__ dst,
+                const float* __restrict__ W, const float* __restrict__ BW,
+                const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float om1,
                 PCtl* ctl, int k, int t0, int ns, int check, float tol, int out_sel, Grid g) {
-  __shared__ float ph[2][RI * RJ];
-  __shared__ float rh[RI * RJ];
-  __shared__ uint8_t sc[RI * RJ];
-  __shared__ double red[32];
+  __shared__ float4 xch[2][2][NWARP][32];
+  __shared__ float red[NWARP];
   __shared__ int skip;
   if (threadIdx.x == 0) {
     int sk = ctl->stop;
@@ -216,60 +227,121 @@ __global__ void __launch_bounds__(TB_THREADS)
   }
   __syncthreads();
   if (skip) return;
-  const int i0 = blockIdx.y * TI - TMAX, j0 = blockIdx.x * TJ - TMAX;
-  for (int q = threadIdx.x; q < RI * RJ; q += TB_THREADS) {
-    int ri = q / RJ, rj = q - (q / RJ) * RJ;
-    int gi = i0 + ri, gj = j0 + rj;
-    float x = 0.0f, b = 0.0f;
-    uint8_t s = 0;
-    if (gi >= 0 && gi < g.NX && gj >= 0 && gj < g.NY) {
-      int c = gi * g.P + gj;
-      uint8_t fl = flags[c];
-      x = src[c];
-      if (flag_active(fl)) {
-        s = (uint8_t)flag_count(fl);
-        b = rhs[c];
-      }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gi0 = blockIdx.y * OI - TMAX + warp * RT;
+  const int gj = blockIdx.x * OJ - TMAX + lane * JT;
+  // gj is a multiple of 4 and the pitch a multiple of 32: a 4-column group is
+  // either wholly left of the grid or a 16-byte aligned read inside the row.
+  const bool colok = gj >= 0 && gj < g.P;
+  float x[RT][JT], w[RT][JT], bw[RT][JT];
+#pragma unroll
+  for (int r = 0; r < RT; ++r) {
+    int gi = gi0 + r;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), ww = a, bb = a;
+    if (colok && gi >= 0 && gi < g.NX) {
+      size_t c = (size_t)gi * g.P + gj;
+      if (!ZERO_INIT) a = *reinterpret_cast<const float4*>(src + c);
+      ww = *reinterpret_cast<const float4*>(W + c);
+      bb = *reinterpret_cast<const float4*>(BW + c);
     }
-    ph[0][q] = x;
-    rh[q] = b;
-    sc[q] = s;
+    x[r][0] = a.x; x[r][1] = a.y; x[r][2] = a.z; x[r][3] = a.w;
+    w[r][0] = ww.x; w[r][1] = ww.y; w[r][2] = ww.z; w[r][3] = ww.w;
+    bw[r][0] = bb.x; bw[r][1] = bb.y; bw[r][2] = bb.z; bw[r][3] = bb.w;
+#pragma unroll
+    for (int q = 0; q < JT; ++q)
+      if (gj + q >= g.NY) {
+        x[r][q] = 0.0f;
+        w[r][q] = 0.0f;
+        bw[r][q] = 0.0f;
+      }
   }
-  __syncthreads();
+  const bool own_col = lane * JT >= TMAX && lane * JT < RJ - TMAX;
   float mx = 0.0f;
-  int cur = 0;
-  for (int sw = 1; sw <= ns; ++sw) {
-    const float* a = ph[cur];
-    float* o = ph[cur ^ 1];
-    const bool last = sw == ns;
-    for (int q = threadIdx.x; q < RI * RJ; q += TB_THREADS) {
-      int ri = q / RJ, rj = q - (q / RJ) * RJ;
-      if (ri < sw || ri >= RI - sw || rj < sw || rj >= RJ - sw) continue;
-      int s = sc[q];
-      float y = 0.0f;
-      if (s) {
-        float nb = a[q - RJ] + a[q + RJ] + a[q - 1] + a[q + 1];
-        float r;
-        y = jacobi_cell(a[q], nb, rh[q], s, w, &r);
-        if (last && ri >= TMAX && ri < TMAX + TI && rj >= TMAX && rj < TMAX + TJ) {
-          float ar = fabsf(r);
-          if (ar > mx) mx = ar;
+  for (int sw = 0; sw < ns; ++sw) {
+    const int buf = sw & 1;
+    xch[buf][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
+    xch[buf][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
+    __syncthreads();
+    float4 u4 = warp > 0 ? xch[buf][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 d4 = warp < NWARP - 1 ? xch[buf][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool last = sw == ns - 1;
+    float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
+#pragma unroll
+    for (int r = 0; r < RT; ++r) {
+      float lf = __shfl_up_sync(0xffffffffu, x[r][JT - 1], 1);
+      float rt = __shfl_down_sync(0xffffffffu, x[r][0], 1);
+      float nxt[JT];
+      if (r < RT - 1) {
+#pragma unroll
+        for (int q = 0; q < JT; ++q) nxt[q] = x[r + 1][q];
+      } else {
+        nxt[0] = d4.x; nxt[1] = d4.y; nxt[2] = d4.z; nxt[3] = d4.w;
+      }
+      float nw[JT];
+      float nbv[JT];
+#pragma unroll
+      for (int q = 0; q < JT; ++q) {
+        float left = q == 0 ? lf : x[r][q - 1];
+        float right = q == JT - 1 ? rt : x[r][q + 1];
+        float nb = prev[q] + nxt[q] + left + right;  // (i-1) + (i+1) + (j-1) + (j+1)
+        nbv[q] = nb;
+        float y = __fmaf_rn(w[r][q], nb, bw[r][q]);
+        if (!OMEGA1) y = __fmaf_rn(om1, x[r][q], y);
+        nw[q] = y;
+      }
+      if (last) {
+        const int ri = warp * RT + r;
+        const int gi = gi0 + r;
+        if (own_col && ri >= TMAX && ri < RI - TMAX && gi < g.NX) {
+          size_t c = (size_t)gi * g.P + gj;
+          if (gj < g.NY) {
+            float4 b4 = *reinterpret_cast<const float4*>(rhs + c);
+            uint32_t f4 = *reinterpret_cast<const uint32_t*>(flags + c);
+            float bq[JT] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+            for (int q = 0; q < JT; ++q) {
+              uint8_t fl = (uint8_t)(f4 >> (8 * q));
+              if (gj + q < g.NY && flag_active(fl)) {
+                float rr = __fmaf_rn(-(float)flag_count(fl), x[r][q], bq[q] + nbv[q]);
+                float ar = fabsf(rr);
+                if (ar > mx) mx = ar;
+              }
+            }
+          }
         }
       }
-      o[q] = y;
+#pragma unroll
+      for (int q = 0; q < JT; ++q) {
+        prev[q] = x[r][q];
+        x[r][q] = nw[q];
+      }
     }
-    __syncthreads();
-    cur ^= 1;
   }
-  // Write the owned cells.
-  for (int q = threadIdx.x; q < TI * TJ; q += TB_THREADS) {
-    int oi = q / TJ, oj = q - (q / TJ) * TJ;
-    int gi = i0 + TMAX + oi, gj = j0 + TMAX + oj;
-    if (gi < g.NX && gj < g.NY) dst[gi * g.P + gj] = ph[cur][(oi + TMAX) * RJ + oj + TMAX];
+  // Owned cells: rows TMAX..RI-TMAX-1 (warps 1..6), columns TMAX..RJ-TMAX-1.
+  if (own_col && warp >= TMAX / RT && warp < NWARP - TMAX / RT) {
+#pragma unroll
+    for (int r = 0; r < RT; ++r) {
+      int gi = gi0 + r;
+      if (gi >= g.NX || gj >= g.NY) continue;
+      size_t c = (size_t)gi * g.P + gj;
+      if (gj + JT <= g.NY) {
+        *reinterpret_cast<float4*>(dst + c) = make_float4(x[r][0], x[r][1], x[r][2], x[r][3]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < JT; ++q)
+          if (gj + q < g.NY) dst[c + q] = x[r][q];
+      }
+    }
   }
-  double m = block_reduce<true>((double)mx, red);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if (lane == 0) red[warp] = mx;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    if (m > 0.0) atomicMax(&ctl->slots[k], __float_as_uint((float)m));
+    float m = 0.0f;
+#pragma unroll
+    for (int q = 0; q < NWARP; ++q) m = fmaxf(m, red[q]);
+    if (m > 0.0f) atomicMax(&ctl->slots[k], __float_as_uint(m));
     if (blockIdx.x == 0 && blockIdx.y == 0) {
       ctl->sweeps = t0 + ns;
       ctl->last_launch = k;
@@ -278,13 +350,13 @@ __global__ void __launch_bounds__(TB_THREADS)
   }
 }
 
-// FP64 residual r = b - A phi of the current iterate: writes r (rounded to
-// float) as the correction right-hand side and the block partials
-// (sum r^2, max |r|).
+// FP64 residual r = b - A phi of the current iterate, with the block
+// partials (sum r^2, max |r|).  When `rhs_e` is given it also writes the
+// correction right-hand side b_e = (float) r and bw_e = w * b_e.
 __global__ void k_resid64(const float* __restrict__ phi0, const float* __restrict__ phi1,
                           const PCtl* __restrict__ ctl, const float* __restrict__ rhs,
-                          const uint8_t* __restrict__ flags, float* __restrict__ rhs_e,
-                          float* __restrict__ err, float* __restrict__ err2,
+                          const float* __restrict__ W, const uint8_t* __restrict__ flags,
+                          float* __restrict__ rhs_e, float* __restrict__ bwe,
                           double* __restrict__ partials, Grid g) {
   __shared__ double red[32];
   const float* phi = ctl->sel ? phi1 : phi0;
@@ -305,8 +377,7 @@ __global__ void k_resid64(const float* __restrict__ phi0, const float* __restric
     }
     if (rhs_e) {
       rhs_e[c] = re;
-      err[c] = 0.0f;
-      err2[c] = 0.0f;
+      bwe[c] = W[c] * re;
     }
   }
   double s = block_reduce<false>(r2, red);
@@ -335,32 +406,34 @@ __global__ void k_add_correction(float* __restrict__ phi0, float* __restrict__ p
 // Gradient subtract and pressure: U_face += S_R phi_L - S_L phi_R on faces
 // with an active neighbour, V likewise, p = cp * phi on active cells, 0
 // elsewhere (fill(f.p, 0) fluid.go:83 plus p += cp * delta fluid.go:224).
+// U, V, p use the grid pitch g.P; phi and the flags the pitch Ps.
 __global__ void k_grad(float* __restrict__ U, float* __restrict__ V, float* __restrict__ p,
                        const float* __restrict__ phi0, const float* __restrict__ phi1,
                        const PCtl* __restrict__ ctl, const uint8_t* __restrict__ flags, float cp,
-                       Grid g) {
+                       Grid g, int Ps) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
   const float* phi = ctl->sel ? phi1 : phi0;
-  int c = i * g.P + j;
+  int c = i * Ps + j;
+  int u = i * g.P + j;
   uint8_t fl = flags[c];
   bool act = flag_active(fl);
   if (i >= 1 && j >= 1 && j <= g.NY - 2) {
-    bool actL = flag_active(flags[c - g.P]);
+    bool actL = flag_active(flags[c - Ps]);
     if (act || actL) {
-      float d = fbit(fl, F_FLUID) * phi[c - g.P] - fbit(fl, F_W) * phi[c];
-      U[c] = U[c] + d;
+      float d = fbit(fl, F_FLUID) * phi[c - Ps] - fbit(fl, F_W) * phi[c];
+      U[u] = U[u] + d;
     }
   }
   if (j >= 1 && i >= 1 && i <= g.NX - 2) {
     bool actB = flag_active(flags[c - 1]);
     if (act || actB) {
       float d = fbit(fl, F_FLUID) * phi[c - 1] - fbit(fl, F_S) * phi[c];
-      V[c] = V[c] + d;
+      V[u] = V[u] + d;
     }
   }
-  p[c] = act ? cp * phi[c] : 0.0f;
+  p[u] = act ? cp * phi[c] : 0.0f;
 }
 
 __global__ void k_finish_parallel(const PCtl* __restrict__ ctl, DevStats* st) {
@@ -380,8 +453,8 @@ static cudaError_t resid_stats(fg_fluid* f, bool write_rhs_e) {
   int nb = gr.x * gr.y;
   count(f);
   k_resid64<<<gr, dim3(BX, BY), 0, f->stream>>>(
-      f->phi, f->phi2, (PCtl*)f->pctl, f->rhs, f->flags, write_rhs_e ? f->rhs_e : nullptr,
-      f->err, f->err2, f->partials, f->g);
+      f->phi, f->phi2, (PCtl*)f->pctl, f->rhs, f->wgt, f->flags,
+      write_rhs_e ? f->rhs_e : nullptr, f->bwe, f->partials, f->g);
   double* out = f->partials + 2 * (size_t)nb;
   count(f);
   k_combine<2><<<1, 1024, 0, f->stream>>>(f->partials, nb, 2u, out);
@@ -392,19 +465,53 @@ static cudaError_t resid_stats(fg_fluid* f, bool write_rhs_e) {
 
 size_t pctl_bytes(int n_slots) { return sizeof(PCtl) + sizeof(unsigned) * (size_t)n_slots; }
 
-// Runs `iters` Jacobi sweeps of A x = b in launches of tb_depth sweeps; x
-// ping-pongs between x0 and x1 and ctl->sel names the buffer holding the
-// result.
-static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, float* x0, float* x1,
-                                int iters, bool allow_exit) {
-  WTab w;
-  float om = f->prm.jacobi_omega * f->prm.pressure_damping;
-  w.w[0] = 0.0f;
-  for (int s = 1; s <= 4; ++s) w.w[s] = om / (float)s;
-  int T = f->prm.tb_depth;
-  if (T < 1) T = 1;
-  if (T > TMAX) T = TMAX;
-  dim3 gr((f->NY + TJ - 1) / TJ, (f->NX + TI - 1) / TI);
+inline int clamp_tb(int t) { return t < 1 ? 1 : (t > TMAX ? TMAX : t); }
+
+int jacobi_launches(const fg_fluid* f, int iters) {
+  int T = clamp_tb(f->prm.tb_depth);
+  return (iters + T - 1) / T;
+}
+
+// Enqueues `iters` Jacobi sweeps of A x = b from x = 0 in launches of T
+// sweeps; x ping-pongs between x0 and x1 and ctl->sel names the buffer that
+// holds the result.  The grid g's pitch is the solver arrays' pitch.
+static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, const float* b,
+                                  const float* bw, const float* W, const uint8_t* flags, float* x0,
+                                  float* x1, int iters, int T, float om, int check, float tol,
+                                  int* n_launched) {
+  float om1 = 1.0f - om;
+  bool o1 = om1 == 0.0f;
+  dim3 gr((g.NY + OJ - 1) / OJ, (g.NX + OI - 1) / OI);
+  int nlaunch = (iters + T - 1) / T;
+  for (int k = 0; k < nlaunch; ++k) {
+    int t0 = k * T;
+    int ns = iters - t0 < T ? iters - t0 : T;
+    const float* src = (k & 1) ? x1 : x0;
+    float* dst = (k & 1) ? x0 : x1;
+    int sel = (k & 1) ? 0 : 1;
+    if (k == 0) {
+      if (o1)
+        k_jacobi_rb<true, true><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl, k,
+                                                           t0, ns, check, tol, sel, g);
+      else
+        k_jacobi_rb<false, true><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl, k,
+                                                            t0, ns, check, tol, sel, g);
+    } else {
+      if (o1)
+        k_jacobi_rb<true, false><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl, k,
+                                                            t0, ns, check, tol, sel, g);
+      else
+        k_jacobi_rb<false, false><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl,
+                                                             k, t0, ns, check, tol, sel, g);
+    }
+  }
+  *n_launched = nlaunch;
+  return cudaGetLastError();
+}
+
+static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const float* bw, float* x0,
+                                float* x1, int iters, bool allow_exit) {
+  int T = clamp_tb(f->prm.tb_depth);
   int nlaunch = (iters + T - 1) / T;
   if (nlaunch > f->n_slots) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(ctl, 0, pctl_bytes(nlaunch), f->stream);
@@ -412,27 +519,16 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, float* x
   int check = allow_exit && f->prm.early_exit ? 1 : 0;
   const bool prof = f->profile && allow_exit;
   if (prof && (e = cudaEventRecord(f->prof_ev[0], f->stream)) != cudaSuccess) return e;
-  for (int k = 0; k < nlaunch; ++k) {
-    int t0 = k * T;
-    int ns = iters - t0 < T ? iters - t0 : T;
-    const float* src = (k & 1) ? x1 : x0;
-    float* dst = (k & 1) ? x0 : x1;
-    count(f);
-    k_jacobi_tb<<<gr, TB_THREADS, 0, f->stream>>>(src, dst, b, f->flags, w, ctl, k, t0, ns, check,
-                                                  f->prm.tolerance, (k & 1) ? 0 : 1, f->g);
-  }
+  int n = 0;
+  e = enqueue_jacobi(f->stream, f->g, ctl, b, bw, f->wgt, f->flags, x0, x1, iters, T,
+                     f->prm.jacobi_omega * f->prm.pressure_damping, check, f->prm.tolerance, &n);
+  count(f, n);
+  if (e != cudaSuccess) return e;
   if (prof) {
     if ((e = cudaEventRecord(f->prof_ev[1], f->stream)) != cudaSuccess) return e;
     f->prof_launches = nlaunch;
   }
   return cudaGetLastError();
-}
-
-int jacobi_launches(const fg_fluid* f, int iters) {
-  int T = f->prm.tb_depth;
-  if (T < 1) T = 1;
-  if (T > TMAX) T = TMAX;
-  return (iters + T - 1) / T;
 }
 
 cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt) {
@@ -449,13 +545,14 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt) {
   PCtl* ctl = (PCtl*)f->pctl;
   PCtl* ectl = (PCtl*)f->ectl;
   dim3 gr = cell_grid(f), bl(BX, BY);
+  float om = f->prm.jacobi_omega * f->prm.pressure_damping;
   // sel = 0 (phi) until a launch runs.
   if ((e = cudaMemsetAsync(ctl, 0, sizeof(PCtl), f->stream)) != cudaSuccess) return e;
   count(f);
-  k_setup_system<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->phi, f->phi2, f->rhs,
-                                           f->flags, f->g);
+  k_setup_system<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->phi, f->rhs, f->wgt, f->bw,
+                                           f->flags, om, num_iters == 0 ? 1 : 0, f->g, f->P);
   if (num_iters > 0) {
-    if ((e = jacobi_solve(f, ctl, f->rhs, f->phi, f->phi2, num_iters, true)) != cudaSuccess)
+    if ((e = jacobi_solve(f, ctl, f->rhs, f->bw, f->phi, f->phi2, num_iters, true)) != cudaSuccess)
       return e;
     count(f);
     k_finish_parallel<<<1, 1, 0, f->stream>>>(ctl, f->dstats);
@@ -463,17 +560,16 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt) {
   bool refine = f->prm.refine_sweeps > 0;
   if ((e = resid_stats(f, refine)) != cudaSuccess) return e;
   if (refine) {
-    if ((e = jacobi_solve(f, ectl, f->rhs_e, f->err, f->err2, f->prm.refine_sweeps, false)) !=
-        cudaSuccess)
+    if ((e = jacobi_solve(f, ectl, f->rhs_e, f->bwe, f->err, f->err2, f->prm.refine_sweeps,
+                          false)) != cudaSuccess)
       return e;
     count(f);
     k_add_correction<<<gr, bl, 0, f->stream>>>(f->phi, f->phi2, f->err, f->err2, ctl, ectl,
                                                f->flags, f->g);
-    if ((e = resid_stats(f, false)) != cudaSuccess) return e;
   }
   count(f);
   k_grad<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
-                                   f->flags, cp, f->g);
+                                   f->flags, cp, f->g, f->P);
   return cudaGetLastError();
 }
 
@@ -489,23 +585,25 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt) {
 // fg_project_noalloc runs the Jacobi projection on caller-owned fields using
 // the scratch array below instead of the handle's buffers.  The array is a
 // fixed part of the library image, so every GPU that loads the library holds
-// it (about 13 MiB) until the process exits.
+// it (about 21 MiB) until the process exits.
 // ===========================================================================
 namespace fg {
 namespace {
 
-constexpr size_t kNoAllocMaxCells = (size_t)FG_NOALLOC_MAX_CELLS;  // num_x * pitch
+constexpr size_t kNoAllocMaxCells = (size_t)FG_NOALLOC_MAX_CELLS;  // num_x * padded num_y
 constexpr int kNoAllocSlots = 4096;                                  // Jacobi launches per call
 constexpr size_t kNoAllocCtlBytes = 256 + sizeof(unsigned) * kNoAllocSlots;
-constexpr size_t kNoAllocBytes = 13 * kNoAllocMaxCells + kNoAllocCtlBytes;
+constexpr size_t kNoAllocBytes = 21 * kNoAllocMaxCells + kNoAllocCtlBytes;
 
-// Scratch shared by every call on a device: phi, phi2, rhs (floats), the
-// flag bytes and the control block, carved at fixed offsets.  It keeps the
-// previous call's contents; each call rewrites or clears what it reads.
+// Scratch shared by every call on a device: phi, phi2, rhs, w, bw (floats),
+// the flag bytes and the control block, carved at fixed offsets with the
+// solver's own pitch (num_y rounded up to 32).  It keeps the previous call's
+// contents; each call rewrites or clears what it reads.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 // Flag bytes from a caller-owned S (nonzero = fluid).
-__global__ void k_noalloc_flags(const float* __restrict__ S, uint8_t* __restrict__ flags, Grid g) {
+__global__ void k_noalloc_flags(const float* __restrict__ S, uint8_t* __restrict__ flags, Grid g,
+                                int Ps) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
@@ -517,7 +615,7 @@ __global__ void k_noalloc_flags(const float* __restrict__ S, uint8_t* __restrict
   if (j > 0 && S[c - 1] != 0.0f) fl |= F_S;
   if (j < g.NY - 1 && S[c + 1] != 0.0f) fl |= F_N;
   if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2) fl |= F_INTERIOR;
-  flags[c] = fl;
+  flags[i * Ps + j] = fl;
 }
 
 std::mutex g_noalloc_mu;
@@ -552,8 +650,9 @@ extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, 
   if (!u || !v || !p || !s || num_x < 3 || num_y < 3 || pitch < num_y || num_iters < 0 ||
       !(h > 0.0f) || dt == 0.0f)
     return FG_ERR_INVALID;
-  if ((size_t)num_x * (size_t)pitch > kNoAllocMaxCells) return FG_ERR_TOO_LARGE;
-  int T = tb_depth < 1 ? 1 : (tb_depth > TMAX ? TMAX : tb_depth);
+  const int Ps = (num_y + 31) / 32 * 32;  // solver pitch inside the scratch
+  if ((size_t)num_x * (size_t)Ps > kNoAllocMaxCells) return FG_ERR_TOO_LARGE;
+  int T = clamp_tb(tb_depth);
   int nlaunch = (num_iters + T - 1) / T;
   if (nlaunch > kNoAllocSlots) return FG_ERR_TOO_LARGE;
   void* base = nullptr;
@@ -563,29 +662,25 @@ extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, 
   float* phi = (float*)b;
   float* phi2 = (float*)(b + 4 * kNoAllocMaxCells);
   float* rhs = (float*)(b + 8 * kNoAllocMaxCells);
-  uint8_t* flags = b + 12 * kNoAllocMaxCells;
-  PCtl* ctl = (PCtl*)(b + 13 * kNoAllocMaxCells);
-  Grid g = make_grid(num_x, num_y, pitch, h);
-  WTab w;
+  float* W = (float*)(b + 12 * kNoAllocMaxCells);
+  float* BW = (float*)(b + 16 * kNoAllocMaxCells);
+  uint8_t* flags = b + 20 * kNoAllocMaxCells;
+  PCtl* ctl = (PCtl*)(b + 21 * kNoAllocMaxCells);
+  Grid g = make_grid(num_x, num_y, pitch, h);   // caller fields
+  Grid gs = make_grid(num_x, num_y, Ps, h);     // solver arrays
   float om = jacobi_omega * pressure_damping;
-  w.w[0] = 0.0f;
-  for (int k = 1; k <= 4; ++k) w.w[k] = om / (float)k;
   float cp = density * h / dt;
   dim3 gr((num_y + BX - 1) / BX, (num_x + BY - 1) / BY), bl(BX, BY);
   // The control words start at zero (sel = 0 until a launch runs).
   if (cudaMemsetAsync(ctl, 0, pctl_bytes(nlaunch), st) != cudaSuccess) return FG_ERR_CUDA;
-  k_noalloc_flags<<<gr, bl, 0, st>>>(s, flags, g);
-  k_setup_system<<<gr, bl, 0, st>>>(u, v, phi, phi2, rhs, flags, g);
-  dim3 tg((num_y + TJ - 1) / TJ, (num_x + TI - 1) / TI);
-  int check = early_exit ? 1 : 0;
-  for (int k = 0; k < nlaunch; ++k) {
-    int t0 = k * T;
-    int ns = num_iters - t0 < T ? num_iters - t0 : T;
-    const float* src = (k & 1) ? phi2 : phi;
-    float* dst = (k & 1) ? phi : phi2;
-    k_jacobi_tb<<<tg, TB_THREADS, 0, st>>>(src, dst, rhs, flags, w, ctl, k, t0, ns, check,
-                                           tolerance, (k & 1) ? 0 : 1, g);
-  }
-  k_grad<<<gr, bl, 0, st>>>(u, v, p, phi, phi2, ctl, flags, cp, g);
+  k_noalloc_flags<<<gr, bl, 0, st>>>(s, flags, g, Ps);
+  k_setup_system<<<gr, bl, 0, st>>>(u, v, phi, rhs, W, BW, flags, om, num_iters == 0 ? 1 : 0, g,
+                                    Ps);
+  int n = 0;
+  if (num_iters > 0 &&
+      enqueue_jacobi(st, gs, ctl, rhs, BW, W, flags, phi, phi2, num_iters, T, om,
+                     early_exit ? 1 : 0, tolerance, &n) != cudaSuccess)
+    return FG_ERR_CUDA;
+  k_grad<<<gr, bl, 0, st>>>(u, v, p, phi, phi2, ctl, flags, cp, g, Ps);
   return cudaGetLastError() == cudaSuccess ? FG_OK : FG_ERR_CUDA;
 }

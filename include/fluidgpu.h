@@ -206,9 +206,9 @@ unsigned long long fg_edit_bytes(const fg_fluid* f);
  * 1 = fluid; any nonzero value counts as fluid), each num_x rows of `pitch`
  * floats (pitch >= num_y), cell (i, j) at i*pitch + j.  Its scratch is a
  * fixed array inside the library of FG_NOALLOC_MAX_CELLS cells (about
- * 13 MiB, held on every GPU that loads the library until the process exits):
- * num_x * pitch above FG_NOALLOC_MAX_CELLS, or more than 4096 Jacobi
- * launches (num_iters / tb_depth), returns FG_ERR_TOO_LARGE.  The work is
+ * 21 MiB, held on every GPU that loads the library until the process exits):
+ * num_x * (num_y rounded up to 32) above FG_NOALLOC_MAX_CELLS, or more than
+ * 4096 Jacobi launches (num_iters / tb_depth), returns FG_ERR_TOO_LARGE.  The work is
  * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream)
  * and the call returns without waiting.  The first call on a device looks up
  * the scratch array's device address; make that first call before any stream

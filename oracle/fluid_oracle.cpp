@@ -297,9 +297,15 @@ struct Fluid {
   // with phi = 0 on inactive cells (solid, border ring, no fluid neighbour),
   // followed by U_face += S_R phi_L - S_L phi_R (and the same for V) and
   // p = cp phi.  Jacobi and red-black relaxations of it run on the GPU.
+  // Per active cell c with s_c fluid neighbours, the Jacobi update is
+  //   phi' = (1 - om) phi + w_c (nb + b_c),   w_c = om / s_c,  om = omega * damping,
+  // evaluated as fma(w_c, nb, bw_c) with bw_c = w_c * b_c precomputed (and an
+  // outer fma with 1 - om when om != 1); W = BW = 0 off the active cells.
   void setupSystem() {
     int n = NY;
     phi.assign(N, 0); phi2.assign(N, 0); rhs.assign(N, 0); cnt.assign(N, 0);
+    Wc.assign(N, 0); BWc.assign(N, 0);
+    T om = jacobi_omega * PressureDamping;
     par(1, NX - 1, [&](int i) {
       for (int j = 1; j < NY - 1; ++j) {
         int c = i * n + j;
@@ -309,18 +315,43 @@ struct Fluid {
         T div = U[(i + 1) * n + j] - U[c] + V[c + 1] - V[c];
         rhs[c] = -div;
         cnt[c] = (uint8_t)s;
+        Wc[c] = om / s;
+        BWc[c] = Wc[c] * rhs[c];
       }
     });
   }
-  T omegaTable(int s) const {
-    T om = jacobi_omega * PressureDamping;
-    return om / (T)s;
+  std::vector<T> Wc, BWc, BWe;
+  // One Jacobi sweep src -> dst; returns max |r| over the active cells, with
+  // r = fma(-s, phi, b + nb) the residual of the input iterate.
+  T sweepJacobi(const std::vector<T>& b, const std::vector<T>& bw, const std::vector<T>& src,
+                std::vector<T>& dst) {
+    int n = NY;
+    T om1 = (T)1 - jacobi_omega * PressureDamping;
+    std::vector<T> rowmax(NX, 0);
+    par(1, NX - 1, [&](int i) {
+      T mx = 0;
+      for (int j = 1; j < NY - 1; ++j) {
+        int c = i * n + j;
+        T nb = src[c - n] + src[c + n] + src[c - 1] + src[c + 1];
+        T y = std::fma(Wc[c], nb, bw[c]);
+        if (om1 != 0) y = std::fma(om1, src[c], y);
+        int s = cnt[c];
+        if (s) {
+          T r = std::fma(-(T)s, src[c], b[c] + nb);
+          T a = go_abs(r);
+          if (a > mx) mx = a;
+        }
+        dst[c] = y;
+      }
+      rowmax[i] = mx;
+    });
+    T mx = 0;
+    for (int i = 1; i < NX - 1; ++i)
+      if (rowmax[i] > mx) mx = rowmax[i];
+    return mx;
   }
-  // One relaxation sweep over cells of the given colour (-1 = all cells, a
-  // Jacobi sweep from src into dst; 0/1 = red-black half sweep in place with
-  // src == dst).  Returns the max |r| seen over the updated cells.
-  T sweep(const std::vector<T>& b, const std::vector<T>& src, std::vector<T>& dst,
-          int colour, T omega_scale) {
+  // Red-black SOR half sweep (CPU-only variant), in place.
+  T sweepRB(const std::vector<T>& b, std::vector<T>& x, int colour, T omega_scale) {
     int n = NY;
     T w[5];
     for (int s = 1; s <= 4; ++s) w[s] = (omega_scale * PressureDamping) / (T)s;
@@ -329,20 +360,14 @@ struct Fluid {
       T mx = 0;
       for (int j = 1; j < NY - 1; ++j) {
         int c = i * n + j;
-        if (colour >= 0 && ((i + j) & 1) != colour) {
-          continue;
-        }
+        if (((i + j) & 1) != colour) continue;
         int s = cnt[c];
-        if (s == 0) {
-          dst[c] = 0;
-          continue;
-        }
-        T nb = src[c - n] + src[c + n] + src[c - 1] + src[c + 1];
-        T t1 = b[c] + nb;
-        T r = std::fma(-(T)s, src[c], t1);
+        if (s == 0) continue;
+        T nb = x[c - n] + x[c + n] + x[c - 1] + x[c + 1];
+        T r = std::fma(-(T)s, x[c], b[c] + nb);
         T a = go_abs(r);
         if (a > mx) mx = a;
-        dst[c] = std::fma(w[s], r, src[c]);
+        x[c] = std::fma(w[s], r, x[c]);
       }
       rowmax[i] = mx;
     });
@@ -353,8 +378,8 @@ struct Fluid {
   }
   // Runs `iters` sweeps on x (ping-pong with tmp); early exit checked after
   // sweeps whose count is a multiple of check_every.  Returns sweeps done.
-  int relax(const std::vector<T>& b, std::vector<T>& x, std::vector<T>& tmp, int iters,
-            bool allow_exit) {
+  int relax(const std::vector<T>& b, const std::vector<T>& bw, std::vector<T>& x,
+            std::vector<T>& tmp, int iters, bool allow_exit) {
     int done = 0;
     for (int t = 0; t < iters; ++t) {
       T mx;
@@ -362,11 +387,11 @@ struct Fluid {
         // Red-black SOR with the reference's relaxation schedule.
         T prog = (T)(unsigned)t / (T)(unsigned)iters;
         T om = Relaxation - (Relaxation - (T)1.2) * prog;
-        T m0 = sweep(b, x, x, 0, om);
-        T m1 = sweep(b, x, x, 1, om);
+        T m0 = sweepRB(b, x, 0, om);
+        T m1 = sweepRB(b, x, 1, om);
         mx = m0 > m1 ? m0 : m1;
       } else {
-        mx = sweep(b, x, tmp, -1, jacobi_omega);
+        mx = sweepJacobi(b, bw, x, tmp);
         std::swap(x, tmp);
       }
       done = t + 1;
@@ -379,19 +404,24 @@ struct Fluid {
     int n = NY;
     T cp = density * h / dt;
     setupSystem();
-    st.sweeps = relax(rhs, phi, phi2, numIters, true);
+    st.sweeps = relax(rhs, BWc, phi, phi2, numIters, true);
     residualFP64();
     if (refine_sweeps > 0) {
       // Outer correction: FP64 residual of the FP32 iterate, a correction
       // solve A e = r by the same relaxation, then phi += e.
       std::vector<T> r(N, 0);
+      BWe.assign(N, 0);
       for (int c = 0; c < N; ++c)
-        if (cnt[c]) r[c] = (T)resid64_[c];
+        if (cnt[c]) {
+          r[c] = (T)resid64_[c];
+          BWe[c] = Wc[c] * r[c];
+        }
       err.assign(N, 0); err2.assign(N, 0);
-      relax(r, err, err2, refine_sweeps, false);
+      T keep = st.last_maxdiv;
+      relax(r, BWe, err, err2, refine_sweeps, false);
+      st.last_maxdiv = keep;
       for (int c = 0; c < N; ++c)
         if (cnt[c]) phi[c] = phi[c] + err[c];
-      residualFP64();
     }
     // Gradient subtract + pressure.
     par(1, NX, [&](int i) {
