@@ -56,3 +56,98 @@ __global__ void k_combine(const double* __restrict__ partials, int n, unsigned m
 
 }  // namespace
 }  // namespace fg
+
+// ---------------------------------------------------------------------------
+// Double-float ("float-float") accumulation.  This part's FP64 rate is about
+// 1/64 of its FP32 rate, so the per-cell and intra-block work of the FP64
+// reductions uses error-free FP32 transformations (Knuth's TwoSum, the exact
+// product error by fma), which carry about 48 significant bits; block totals
+// are converted exactly to double and combined across blocks in IEEE FP64.
+// ---------------------------------------------------------------------------
+namespace fg {
+namespace {
+
+struct FF {
+  float hi, lo;
+};
+
+// Knuth's TwoSum: s + e == a + b exactly.
+__host__ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__host__ __device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e = e + (a.lo + b.lo);
+  float h, l;
+  two_sum(s, e, h, l);
+  return FF{h, l};
+}
+
+// x*x as an unevaluated float pair (exact).
+__device__ __forceinline__ FF ff_sq(float x) {
+  float p = x * x;
+  return FF{p, __fmaf_rn(x, x, -p)};
+}
+
+// Residual b + (pw + pe + ps + pn) - s*x of FP32 inputs as a normalised float
+// pair (hi = the residual rounded to float): the product s*x is split
+// exactly by fma and the seven terms are summed with a TwoSum cascade.
+__host__ __device__ __forceinline__ FF resid_ff(float b, float pw, float pe, float ps, float pn,
+                                                float s, float x) {
+  float p = s * x;
+#ifdef __CUDA_ARCH__
+  float pl = __fmaf_rn(s, x, -p);
+#else
+  float pl = fmaf(s, x, -p);
+#endif
+  float hi = b, lo = 0.0f, t, e;
+  two_sum(hi, pw, t, e); hi = t; lo = lo + e;
+  two_sum(hi, pe, t, e); hi = t; lo = lo + e;
+  two_sum(hi, ps, t, e); hi = t; lo = lo + e;
+  two_sum(hi, pn, t, e); hi = t; lo = lo + e;
+  two_sum(hi, -p, t, e); hi = t; lo = lo + e;
+  lo = lo - pl;
+  two_sum(hi, lo, t, e);
+  return FF{t, e};
+}
+
+// Sum of a float pair per thread over the block, as a double in thread 0.
+// Warp level in float-float, block level in double.  sh: 32 doubles.
+__device__ __forceinline__ double block_sum_ff(FF v, double* sh) {
+  int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  int nt = blockDim.x * blockDim.y;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    FF w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+    v = ff_add(v, w);
+  }
+  __syncthreads();
+  if ((tid & 31) == 0) sh[tid >> 5] = (double)v.hi + (double)v.lo;
+  __syncthreads();
+  double r = 0.0;
+  if (tid == 0)
+    for (int k = 0; k < (nt >> 5); ++k) r += sh[k];
+  return r;
+}
+
+// Max of a non-negative float per thread over the block (thread 0).
+__device__ __forceinline__ float block_max_f(float v, float* sh) {
+  int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  int nt = blockDim.x * blockDim.y;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((tid & 31) == 0) sh[tid >> 5] = v;
+  __syncthreads();
+  float r = 0.0f;
+  if (tid == 0)
+    for (int k = 0; k < (nt >> 5); ++k) r = fmaxf(r, sh[k]);
+  return r;
+}
+
+}  // namespace
+}  // namespace fg

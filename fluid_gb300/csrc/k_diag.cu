@@ -18,32 +18,35 @@ __device__ __forceinline__ bool fluid_interior(uint8_t fl) {
   return (fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR);
 }
 
-// sum div^2, max |div|, count over fluid interior cells.
+// sum div^2 (float pairs in the block, FP64 across blocks), max |div| and
+// the count of fluid interior cells.
 __global__ void k_div_partials(const float* __restrict__ U, const float* __restrict__ V,
                                const uint8_t* __restrict__ flags, double* __restrict__ part,
                                Grid g) {
   __shared__ double red[32];
+  __shared__ float redf[32];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
-  double s2 = 0.0, mx = 0.0, n = 0.0;
+  FF s2{0.0f, 0.0f};
+  float mx = 0.0f;
+  bool in = false;
   if (i < g.NX && j < g.NY) {
     int c = i * g.P + j;
     if (fluid_interior(flags[c])) {
       float div = U[c + g.P] - U[c] + V[c + 1] - V[c];
-      double d = (double)div;
-      s2 = d * d;
-      mx = fabs(d);
-      n = 1.0;
+      s2 = ff_sq(div);
+      mx = fabsf(div);
+      in = true;
     }
   }
-  double a = block_reduce<false>(s2, red);
-  double b = block_reduce<true>(mx, red);
-  double cn = block_reduce<false>(n, red);
+  int cnt = __syncthreads_count(in);
+  double a = block_sum_ff(s2, red);
+  float b = block_max_f(mx, redf);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     double* o = part + 3 * (size_t)block_id();
     o[0] = a;
-    o[1] = b;
-    o[2] = cn;
+    o[1] = (double)b;
+    o[2] = (double)cnt;
   }
 }
 
@@ -53,14 +56,14 @@ __global__ void k_store_div(const double* __restrict__ r, DevStats* st) {
   st->div_count = r[2];
 }
 
-// sum of M over interior cells.
+// sum of M over interior cells (float pairs in the block, FP64 across blocks).
 __global__ void k_mass_partials(const float* __restrict__ M, double* __restrict__ part, Grid g) {
   __shared__ double red[32];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
-  double m = 0.0;
-  if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2) m = (double)M[i * g.P + j];
-  double a = block_reduce<false>(m, red);
+  FF m{0.0f, 0.0f};
+  if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2) m.hi = M[i * g.P + j];
+  double a = block_sum_ff(m, red);
   if (threadIdx.x == 0 && threadIdx.y == 0) part[block_id()] = a;
 }
 

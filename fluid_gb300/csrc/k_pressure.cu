@@ -350,90 +350,94 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   }
 }
 
-// FP64 residual r = b - A phi of the current iterate, with the block
-// partials (sum r^2, max |r|).  When `rhs_e` is given it also writes the
-// correction right-hand side b_e = (float) r and bw_e = w * b_e.
+// Residual r = b - A phi of the current iterate, per cell as an exact-to-
+// ~48-bit float pair (resid_ff), with block partials (sum r^2 accumulated in
+// float pairs within the block and in FP64 across blocks, max |r|).  When
+// `rhs_e` is given it also writes the correction right-hand side
+// b_e = (float) r and bw_e = w * b_e.
 __global__ void k_resid64(const float* __restrict__ phi0, const float* __restrict__ phi1,
                           const PCtl* __restrict__ ctl, const float* __restrict__ rhs,
                           const float* __restrict__ W, const uint8_t* __restrict__ flags,
                           float* __restrict__ rhs_e, float* __restrict__ bwe,
                           double* __restrict__ partials, Grid g) {
   __shared__ double red[32];
+  __shared__ float redf[32];
   const float* phi = ctl->sel ? phi1 : phi0;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
-  double r2 = 0.0, ra = 0.0;
+  FF sq{0.0f, 0.0f};
+  float ra = 0.0f;
   if (i < g.NX && j < g.NY) {
     int c = i * g.P + j;
     uint8_t fl = flags[c];
     float re = 0.0f;
     if (flag_active(fl)) {
-      double nb = (double)phi[c - g.P] + (double)phi[c + g.P] + (double)phi[c - 1] +
-                  (double)phi[c + 1];
-      double r = ((double)rhs[c] + nb) - (double)flag_count(fl) * (double)phi[c];
-      re = (float)r;
-      r2 = r * r;
-      ra = fabs(r);
+      FF r = resid_ff(rhs[c], phi[c - g.P], phi[c + g.P], phi[c - 1], phi[c + 1],
+                      (float)flag_count(fl), phi[c]);
+      re = r.hi;
+      sq = ff_sq(r.hi);
+      sq.lo = sq.lo + 2.0f * r.hi * r.lo;
+      ra = fabsf(r.hi);
     }
     if (rhs_e) {
       rhs_e[c] = re;
       bwe[c] = W[c] * re;
     }
   }
-  double s = block_reduce<false>(r2, red);
-  double m = block_reduce<true>(ra, red);
+  double s = block_sum_ff(sq, red);
+  float m = block_max_f(ra, redf);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     int b = blockIdx.y * gridDim.x + blockIdx.x;
     partials[2 * b] = s;
-    partials[2 * b + 1] = m;
+    partials[2 * b + 1] = (double)m;
   }
 }
 
-__global__ void k_add_correction(float* __restrict__ phi0, float* __restrict__ phi1,
-                                 const float* __restrict__ e0, const float* __restrict__ e1,
-                                 const PCtl* __restrict__ ctl, const PCtl* __restrict__ ectl,
-                                 const uint8_t* __restrict__ flags, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
-  int c = i * g.P + j;
-  if (!flag_active(flags[c])) return;
-  float* phi = ctl->sel ? phi1 : phi0;
-  const float* e = ectl->sel ? e1 : e0;
-  phi[c] = phi[c] + e[c];
+// Final potential at cell c: the main iterate, plus the outer correction on
+// active cells when one ran (phi = phi + e, fluid.go's p accumulation aside).
+__device__ __forceinline__ float phi_final(const float* __restrict__ phi,
+                                           const float* __restrict__ e, int c, bool act) {
+  float x = phi[c];
+  if (e && act) x = x + e[c];
+  return x;
 }
 
 // Gradient subtract and pressure: U_face += S_R phi_L - S_L phi_R on faces
 // with an active neighbour, V likewise, p = cp * phi on active cells, 0
 // elsewhere (fill(f.p, 0) fluid.go:83 plus p += cp * delta fluid.go:224).
-// U, V, p use the grid pitch g.P; phi and the flags the pitch Ps.
+// U, V, p use the grid pitch g.P; phi, e and the flags the pitch Ps.
 __global__ void k_grad(float* __restrict__ U, float* __restrict__ V, float* __restrict__ p,
                        const float* __restrict__ phi0, const float* __restrict__ phi1,
-                       const PCtl* __restrict__ ctl, const uint8_t* __restrict__ flags, float cp,
-                       Grid g, int Ps) {
+                       const PCtl* __restrict__ ctl, const float* __restrict__ e0,
+                       const float* __restrict__ e1, const PCtl* __restrict__ ectl,
+                       const uint8_t* __restrict__ flags, float cp, Grid g, int Ps) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
   const float* phi = ctl->sel ? phi1 : phi0;
+  const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
   int c = i * Ps + j;
   int u = i * g.P + j;
   uint8_t fl = flags[c];
   bool act = flag_active(fl);
+  float pc = phi_final(phi, e, c, act);
   if (i >= 1 && j >= 1 && j <= g.NY - 2) {
-    bool actL = flag_active(flags[c - Ps]);
+    uint8_t fL = flags[c - Ps];
+    bool actL = flag_active(fL);
     if (act || actL) {
-      float d = fbit(fl, F_FLUID) * phi[c - Ps] - fbit(fl, F_W) * phi[c];
+      float d = fbit(fl, F_FLUID) * phi_final(phi, e, c - Ps, actL) - fbit(fl, F_W) * pc;
       U[u] = U[u] + d;
     }
   }
   if (j >= 1 && i >= 1 && i <= g.NX - 2) {
-    bool actB = flag_active(flags[c - 1]);
+    uint8_t fB = flags[c - 1];
+    bool actB = flag_active(fB);
     if (act || actB) {
-      float d = fbit(fl, F_FLUID) * phi[c - 1] - fbit(fl, F_S) * phi[c];
+      float d = fbit(fl, F_FLUID) * phi_final(phi, e, c - 1, actB) - fbit(fl, F_S) * pc;
       V[u] = V[u] + d;
     }
   }
-  p[u] = act ? cp * phi[c] : 0.0f;
+  p[u] = act ? cp * pc : 0.0f;
 }
 
 __global__ void k_finish_parallel(const PCtl* __restrict__ ctl, DevStats* st) {
@@ -563,13 +567,11 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt) {
     if ((e = jacobi_solve(f, ectl, f->rhs_e, f->bwe, f->err, f->err2, f->prm.refine_sweeps,
                           false)) != cudaSuccess)
       return e;
-    count(f);
-    k_add_correction<<<gr, bl, 0, f->stream>>>(f->phi, f->phi2, f->err, f->err2, ctl, ectl,
-                                               f->flags, f->g);
   }
   count(f);
   k_grad<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
-                                   f->flags, cp, f->g, f->P);
+                                   f->err, f->err2, refine ? ectl : nullptr, f->flags, cp, f->g,
+                                   f->P);
   return cudaGetLastError();
 }
 
@@ -681,6 +683,6 @@ extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, 
       enqueue_jacobi(st, gs, ctl, rhs, BW, W, flags, phi, phi2, num_iters, T, om,
                      early_exit ? 1 : 0, tolerance, &n) != cudaSuccess)
     return FG_ERR_CUDA;
-  k_grad<<<gr, bl, 0, st>>>(u, v, p, phi, phi2, ctl, flags, cp, g, Ps);
+  k_grad<<<gr, bl, 0, st>>>(u, v, p, phi, phi2, ctl, nullptr, nullptr, nullptr, flags, cp, g, Ps);
   return cudaGetLastError() == cudaSuccess ? FG_OK : FG_ERR_CUDA;
 }

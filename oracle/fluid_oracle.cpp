@@ -447,6 +447,31 @@ struct Fluid {
     for (int c = 0; c < N; ++c) p[c] = cnt[c] ? cp * phi[c] : (T)0;
   }
   std::vector<double> resid64_;
+  // Knuth's TwoSum: s + e == a + b exactly.
+  static void twoSum(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+  }
+  // Residual b + (pw + pe + ps + pn) - s*x of float inputs as a normalised
+  // float pair: the product split exactly by fma, the terms summed by a
+  // TwoSum cascade (the GPU scheme's residual, bit for bit).
+  static void residFF(float b, float pw, float pe, float ps, float pn, float s, float x,
+                      float& rhi, float& rlo) {
+    float p = s * x;
+    float pl = std::fma(s, x, -p);
+    float hi = b, lo = 0.0f, t, e;
+    twoSum(hi, pw, t, e); hi = t; lo = lo + e;
+    twoSum(hi, pe, t, e); hi = t; lo = lo + e;
+    twoSum(hi, ps, t, e); hi = t; lo = lo + e;
+    twoSum(hi, pn, t, e); hi = t; lo = lo + e;
+    twoSum(hi, -p, t, e); hi = t; lo = lo + e;
+    lo = lo - pl;
+    twoSum(hi, lo, rhi, rlo);
+  }
+  // Residual r = b - A phi of the current iterate in ~FP64 accuracy: float
+  // pairs per cell for the FP32 oracle, doubles for the FP64 one; its
+  // L2 norm and max accumulate in double.
   void residualFP64() {
     int n = NY;
     resid64_.assign(N, 0.0);
@@ -455,12 +480,22 @@ struct Fluid {
       for (int j = 1; j < NY - 1; ++j) {
         int c = i * n + j;
         if (!cnt[c]) continue;
-        double nb = (double)phi[c - n] + (double)phi[c + n] + (double)phi[c - 1] +
-                    (double)phi[c + 1];
-        double r = ((double)rhs[c] + nb) - (double)cnt[c] * (double)phi[c];
+        double r, a;
+        if constexpr (std::is_same<T, float>::value) {
+          float hi, lo;
+          residFF(rhs[c], phi[c - n], phi[c + n], phi[c - 1], phi[c + 1], (float)cnt[c], phi[c],
+                  hi, lo);
+          r = (double)hi + (double)lo;
+          a = std::fabs((double)hi);
+        } else {
+          double nb = (double)phi[c - n] + (double)phi[c + n] + (double)phi[c - 1] +
+                      (double)phi[c + 1];
+          r = ((double)rhs[c] + nb) - (double)cnt[c] * (double)phi[c];
+          a = std::fabs(r);
+        }
         resid64_[c] = r;
         l2 += r * r;
-        if (std::fabs(r) > mx) mx = std::fabs(r);
+        if (a > mx) mx = a;
       }
     st.resid_l2 = std::sqrt(l2);
     st.resid_max = mx;
