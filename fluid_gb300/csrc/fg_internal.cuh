@@ -228,6 +228,18 @@ cudaError_t launch_field_minmax(fg_fluid* f, int field, float* dev_minmax);
 cudaError_t launch_sample_velocity(fg_fluid* f, float x, float y, float* dev_uv);
 cudaError_t launch_max_speed(fg_fluid* f, float* dev_out);
 
+// Grid of the reduction kernels: 32 x 8 threads per block over (j, i), at
+// most about 600 blocks; each block strides down the rows, so the single-
+// block combine of the block partials stays short.
+inline dim3 reduce_grid(const fg_fluid* f) {
+  int gx = (f->NY + 31) / 32;
+  int gy = (f->NX + 7) / 8;
+  int cap = 608 / gx;
+  if (cap < 1) cap = 1;
+  if (gy > cap) gy = cap;
+  return dim3(gx, gy);
+}
+
 // Counts one kernel launch on the handle (for the benchmark's launch tally).
 inline void count(fg_fluid* f, int n = 1) { f->launches += (unsigned long long)n; }
 

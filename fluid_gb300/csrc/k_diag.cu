@@ -26,27 +26,29 @@ __global__ void k_div_partials(const float* __restrict__ U, const float* __restr
   __shared__ double red[32];
   __shared__ float redf[32];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
   FF s2{0.0f, 0.0f};
   float mx = 0.0f;
-  bool in = false;
-  if (i < g.NX && j < g.NY) {
-    int c = i * g.P + j;
-    if (fluid_interior(flags[c])) {
-      float div = U[c + g.P] - U[c] + V[c + 1] - V[c];
-      s2 = ff_sq(div);
-      mx = fabsf(div);
-      in = true;
+  int n = 0;
+  if (j < g.NY) {
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < g.NX; i += gridDim.y * blockDim.y) {
+      int c = i * g.P + j;
+      if (fluid_interior(flags[c])) {
+        float div = U[c + g.P] - U[c] + V[c + 1] - V[c];
+        s2 = ff_add(s2, ff_sq(div));
+        float a = fabsf(div);
+        if (a > mx) mx = a;
+        ++n;
+      }
     }
   }
-  int cnt = __syncthreads_count(in);
   double a = block_sum_ff(s2, red);
   float b = block_max_f(mx, redf);
+  double cn = block_sum_ff(FF{(float)n, 0.0f}, red);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     double* o = part + 3 * (size_t)block_id();
     o[0] = a;
     o[1] = (double)b;
-    o[2] = (double)cnt;
+    o[2] = cn;
   }
 }
 
@@ -60,9 +62,11 @@ __global__ void k_store_div(const double* __restrict__ r, DevStats* st) {
 __global__ void k_mass_partials(const float* __restrict__ M, double* __restrict__ part, Grid g) {
   __shared__ double red[32];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
   FF m{0.0f, 0.0f};
-  if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2) m.hi = M[i * g.P + j];
+  if (j >= 1 && j <= g.NY - 2) {
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < g.NX; i += gridDim.y * blockDim.y)
+      if (i >= 1 && i <= g.NX - 2) m = ff_add(m, FF{M[i * g.P + j], 0.0f});
+  }
   double a = block_sum_ff(m, red);
   if (threadIdx.x == 0 && threadIdx.y == 0) part[block_id()] = a;
 }
@@ -205,7 +209,7 @@ cudaError_t launch_clear_stats(fg_fluid* f) {
 }
 
 cudaError_t launch_div_stats(fg_fluid* f) {
-  dim3 gr = cell_grid(f);
+  dim3 gr = reduce_grid(f);
   int nb = gr.x * gr.y;
   count(f);
   k_div_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags,
@@ -219,7 +223,7 @@ cudaError_t launch_div_stats(fg_fluid* f) {
 }
 
 cudaError_t launch_smoke_mass(fg_fluid* f) {
-  dim3 gr = cell_grid(f);
+  dim3 gr = reduce_grid(f);
   int nb = gr.x * gr.y;
   count(f);
   k_mass_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_M], f->partials, f->g);

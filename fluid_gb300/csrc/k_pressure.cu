@@ -208,18 +208,18 @@ constexpr int OJ = RJ - 2 * TMAX;  // 112 owned columns
 constexpr int OI = RI - 2 * TMAX;  // 48 owned rows
 constexpr int TB_THREADS = 32 * NWARP;
 
-template <bool OMEGA1, bool ZERO_INIT>
+template <bool OMEGA1, bool FULL, bool CHECK>
 __global__ void __launch_bounds__(TB_THREADS, 2)
     k_jacobi_rb(const float* __restrict__ src, float* __restrict__ dst,
                 const float* __restrict__ W, const float* __restrict__ BW,
                 const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float om1,
-                PCtl* ctl, int k, int t0, int ns, int check, float tol, int out_sel, Grid g) {
+                PCtl* ctl, int k, int t0, int ns, float tol, int out_sel, int zero_init, Grid g) {
   __shared__ float4 xch[2][2][NWARP][32];
   __shared__ float red[NWARP];
   __shared__ int skip;
   if (threadIdx.x == 0) {
     int sk = ctl->stop;
-    if (!sk && check && k > 0 && __uint_as_float(ctl->slots[k - 1]) < tol) {
+    if (!sk && CHECK && k > 0 && __uint_as_float(ctl->slots[k - 1]) < tol) {
       sk = 1;
       ctl->stop = 1;
     }
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gi0 = blockIdx.y * OI - TMAX + warp * RT;
   const int gj = blockIdx.x * OJ - TMAX + lane * JT;
-  // gj is a multiple of 4 and the pitch a multiple of 32: a 4-column group is
+  // gj is a multiple of 4 and the pitch a multiple of 4: a 4-column group is
   // either wholly left of the grid or a 16-byte aligned read inside the row.
   const bool colok = gj >= 0 && gj < g.P;
   float x[RT][JT], w[RT][JT], bw[RT][JT];
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), ww = a, bb = a;
     if (colok && gi >= 0 && gi < g.NX) {
       size_t c = (size_t)gi * g.P + gj;
-      if (!ZERO_INIT) a = *reinterpret_cast<const float4*>(src + c);
+      if (!zero_init) a = *reinterpret_cast<const float4*>(src + c);
       ww = *reinterpret_cast<const float4*>(W + c);
       bb = *reinterpret_cast<const float4*>(BW + c);
     }
@@ -257,14 +257,13 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   }
   const bool own_col = lane * JT >= TMAX && lane * JT < RJ - TMAX;
   float mx = 0.0f;
-  for (int sw = 0; sw < ns; ++sw) {
+  auto sweep = [&](int sw, bool last) {
     const int buf = sw & 1;
     xch[buf][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
     xch[buf][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
     __syncthreads();
     float4 u4 = warp > 0 ? xch[buf][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 d4 = warp < NWARP - 1 ? xch[buf][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const bool last = sw == ns - 1;
     float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
 #pragma unroll
     for (int r = 0; r < RT; ++r) {
@@ -289,23 +288,21 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
         if (!OMEGA1) y = __fmaf_rn(om1, x[r][q], y);
         nw[q] = y;
       }
-      if (last) {
+      if (CHECK && last) {
         const int ri = warp * RT + r;
         const int gi = gi0 + r;
-        if (own_col && ri >= TMAX && ri < RI - TMAX && gi < g.NX) {
+        if (own_col && ri >= TMAX && ri < RI - TMAX && gi < g.NX && gj < g.NY) {
           size_t c = (size_t)gi * g.P + gj;
-          if (gj < g.NY) {
-            float4 b4 = *reinterpret_cast<const float4*>(rhs + c);
-            uint32_t f4 = *reinterpret_cast<const uint32_t*>(flags + c);
-            float bq[JT] = {b4.x, b4.y, b4.z, b4.w};
+          float4 b4 = *reinterpret_cast<const float4*>(rhs + c);
+          uint32_t f4 = *reinterpret_cast<const uint32_t*>(flags + c);
+          float bq[JT] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-            for (int q = 0; q < JT; ++q) {
-              uint8_t fl = (uint8_t)(f4 >> (8 * q));
-              if (gj + q < g.NY && flag_active(fl)) {
-                float rr = __fmaf_rn(-(float)flag_count(fl), x[r][q], bq[q] + nbv[q]);
-                float ar = fabsf(rr);
-                if (ar > mx) mx = ar;
-              }
+          for (int q = 0; q < JT; ++q) {
+            uint8_t fl = (uint8_t)(f4 >> (8 * q));
+            if (gj + q < g.NY && flag_active(fl)) {
+              float rr = __fmaf_rn(-(float)flag_count(fl), x[r][q], bq[q] + nbv[q]);
+              float ar = fabsf(rr);
+              if (ar > mx) mx = ar;
             }
           }
         }
@@ -316,8 +313,14 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
         x[r][q] = nw[q];
       }
     }
+  };
+  if (FULL) {
+#pragma unroll
+    for (int sw = 0; sw < TMAX; ++sw) sweep(sw, sw == TMAX - 1);
+  } else {
+    for (int sw = 0; sw < ns; ++sw) sweep(sw, sw == ns - 1);
   }
-  // Owned cells: rows TMAX..RI-TMAX-1 (warps 1..6), columns TMAX..RJ-TMAX-1.
+  // Owned cells: rows TMAX..RI-TMAX-1, columns TMAX..RJ-TMAX-1.
   if (own_col && warp >= TMAX / RT && warp < NWARP - TMAX / RT) {
 #pragma unroll
     for (int r = 0; r < RT; ++r) {
@@ -333,15 +336,19 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
       }
     }
   }
+  if (CHECK) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
-  if (lane == 0) red[warp] = mx;
-  __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if (lane == 0) red[warp] = mx;
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
-    float m = 0.0f;
+    if (CHECK) {
+      float m = 0.0f;
 #pragma unroll
-    for (int q = 0; q < NWARP; ++q) m = fmaxf(m, red[q]);
-    if (m > 0.0f) atomicMax(&ctl->slots[k], __float_as_uint(m));
+      for (int q = 0; q < NWARP; ++q) m = fmaxf(m, red[q]);
+      if (m > 0.0f) atomicMax(&ctl->slots[k], __float_as_uint(m));
+    }
     if (blockIdx.x == 0 && blockIdx.y == 0) {
       ctl->sweeps = t0 + ns;
       ctl->last_launch = k;
@@ -364,24 +371,27 @@ __global__ void k_resid64(const float* __restrict__ phi0, const float* __restric
   __shared__ float redf[32];
   const float* phi = ctl->sel ? phi1 : phi0;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
   FF sq{0.0f, 0.0f};
   float ra = 0.0f;
-  if (i < g.NX && j < g.NY) {
-    int c = i * g.P + j;
-    uint8_t fl = flags[c];
-    float re = 0.0f;
-    if (flag_active(fl)) {
-      FF r = resid_ff(rhs[c], phi[c - g.P], phi[c + g.P], phi[c - 1], phi[c + 1],
-                      (float)flag_count(fl), phi[c]);
-      re = r.hi;
-      sq = ff_sq(r.hi);
-      sq.lo = sq.lo + 2.0f * r.hi * r.lo;
-      ra = fabsf(r.hi);
-    }
-    if (rhs_e) {
-      rhs_e[c] = re;
-      bwe[c] = W[c] * re;
+  if (j < g.NY) {
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < g.NX; i += gridDim.y * blockDim.y) {
+      int c = i * g.P + j;
+      uint8_t fl = flags[c];
+      float re = 0.0f;
+      if (flag_active(fl)) {
+        FF r = resid_ff(rhs[c], phi[c - g.P], phi[c + g.P], phi[c - 1], phi[c + 1],
+                        (float)flag_count(fl), phi[c]);
+        re = r.hi;
+        FF q = ff_sq(r.hi);
+        q.lo = q.lo + 2.0f * r.hi * r.lo;
+        sq = ff_add(sq, q);
+        float ar = fabsf(r.hi);
+        if (ar > ra) ra = ar;
+      }
+      if (rhs_e) {
+        rhs_e[c] = re;
+        bwe[c] = W[c] * re;
+      }
     }
   }
   double s = block_sum_ff(sq, red);
@@ -453,7 +463,7 @@ __global__ void k_store_resid(const double* __restrict__ r, DevStats* st) {
 }  // namespace
 
 static cudaError_t resid_stats(fg_fluid* f, bool write_rhs_e) {
-  dim3 gr = cell_grid(f);
+  dim3 gr = reduce_grid(f);
   int nb = gr.x * gr.y;
   count(f);
   k_resid64<<<gr, dim3(BX, BY), 0, f->stream>>>(
@@ -493,21 +503,19 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
     const float* src = (k & 1) ? x1 : x0;
     float* dst = (k & 1) ? x0 : x1;
     int sel = (k & 1) ? 0 : 1;
-    if (k == 0) {
-      if (o1)
-        k_jacobi_rb<true, true><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl, k,
-                                                           t0, ns, check, tol, sel, g);
-      else
-        k_jacobi_rb<false, true><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl, k,
-                                                            t0, ns, check, tol, sel, g);
+    int zi = k == 0 ? 1 : 0;
+    bool full = ns == TMAX;
+#define FG_JAC(O, F, C)                                                                        \
+  k_jacobi_rb<O, F, C><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl, k, t0, ns, \
+                                                  tol, sel, zi, g)
+    if (o1) {
+      if (full) { if (check) FG_JAC(true, true, true); else FG_JAC(true, true, false); }
+      else { if (check) FG_JAC(true, false, true); else FG_JAC(true, false, false); }
     } else {
-      if (o1)
-        k_jacobi_rb<true, false><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl, k,
-                                                            t0, ns, check, tol, sel, g);
-      else
-        k_jacobi_rb<false, false><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl,
-                                                             k, t0, ns, check, tol, sel, g);
+      if (full) { if (check) FG_JAC(false, true, true); else FG_JAC(false, true, false); }
+      else { if (check) FG_JAC(false, false, true); else FG_JAC(false, false, false); }
     }
+#undef FG_JAC
   }
   *n_launched = nlaunch;
   return cudaGetLastError();

@@ -395,7 +395,8 @@ struct Fluid {
         std::swap(x, tmp);
       }
       done = t + 1;
-      st.last_maxdiv = mx;
+      // The GPU scheme measures |r| only when it checks the early exit.
+      st.last_maxdiv = (allow_exit && early_exit) || scheme == RedBlack ? mx : (T)0;
       if (allow_exit && early_exit && ((t + 1) % check_every) == 0 && mx < tolerance) break;
     }
     return done;
