@@ -217,11 +217,12 @@ int check_iters(fg_fluid* f, int iters) {
 
 // Enqueues makeIncompressible's solve with the statistics of the projected
 // field.
-int enqueue_pressure(fg_fluid* f, int iters, float dt) {
+// fuse_turb: run addTurbulence inside the parallel scheme's gradient kernel.
+int enqueue_pressure(fg_fluid* f, int iters, float dt, bool fuse_turb) {
   if (f->prm.use_multigrid && f->prm.multigrid_levels > 1)
     return fail(f, FG_ERR_UNSUPPORTED, "UseMultigrid is not built for the GPU step");
-  CK(f, launch_pressure(f, iters, dt), "pressure");
-  CK(f, launch_div_stats(f), "div stats");
+  CK(f, launch_pressure(f, iters, dt, fuse_turb), "pressure");
+  if (f->prm.scheme == FG_SCHEME_LEXSOR) CK(f, launch_div_stats(f), "div stats");
   return FG_OK;
 }
 
@@ -234,10 +235,11 @@ int enqueue_step(fg_fluid* f, float dt) {
   if (p.scheme == FG_SCHEME_LEXSOR)
     CK(f, cudaMemsetAsync(f->d[FG_P], 0, field_bytes(f), f->stream), "fill p");
   if (p.viscosity_diffusion > 0.0f) CK(f, launch_viscosity(f, dt), "viscosity");
-  int rc = enqueue_pressure(f, p.num_iters, dt);
+  const bool conf = p.confinement != 0.0f, turb = p.turbulence_strength > 0.0f;
+  const bool fuse_turb = p.scheme == FG_SCHEME_JACOBI && !conf && turb;
+  int rc = enqueue_pressure(f, p.num_iters, dt, fuse_turb);
   if (rc) return rc;
-  CK(f, launch_confinement_turbulence(f, dt, p.confinement != 0.0f, p.turbulence_strength > 0.0f),
-     "confinement/turbulence");
+  if (!fuse_turb) CK(f, launch_confinement_turbulence(f, dt, conf, turb), "confinement/turbulence");
   CK(f, launch_borders(f), "borders");
   if (p.use_bfecc) {
     CK(f, launch_advect_velocity_bfecc(f, dt), "advect velocity");
@@ -566,7 +568,7 @@ int fg_make_incompressible(fg_fluid* f, int num_iters, float dt) {
   // copyBorder(newU, U), copyBorder(newV, V) (fluid.go:145-146).
   CK(f, launch_copy_border(f, f->d[FG_NEWU], f->d[FG_U]), "copy border");
   CK(f, launch_copy_border(f, f->d[FG_NEWV], f->d[FG_V]), "copy border");
-  return enqueue_pressure(f, num_iters, dt);
+  return enqueue_pressure(f, num_iters, dt, false);
 }
 
 int fg_advect_velocity(fg_fluid* f, float dt) {

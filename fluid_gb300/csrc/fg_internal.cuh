@@ -217,7 +217,9 @@ cudaError_t launch_advect_smoke(fg_fluid* f, float dt);
 cudaError_t launch_advect_velocity_bfecc(fg_fluid* f, float dt);
 cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt);
 // k_pressure.cu
-cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt);
+// Pressure solve + gradient subtract + post-projection divergence statistics;
+// with fuse_turb (parallel scheme only) also addTurbulence.
+cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb);
 // k_diag.cu
 cudaError_t launch_div_stats(fg_fluid* f);
 cudaError_t launch_smoke_mass(fg_fluid* f);
@@ -229,12 +231,12 @@ cudaError_t launch_sample_velocity(fg_fluid* f, float x, float y, float* dev_uv)
 cudaError_t launch_max_speed(fg_fluid* f, float* dev_out);
 
 // Grid of the reduction kernels: 32 x 8 threads per block over (j, i), at
-// most about 600 blocks; each block strides down the rows, so the single-
+// most about 1200 blocks; each block strides down the rows, so the single-
 // block combine of the block partials stays short.
 inline dim3 reduce_grid(const fg_fluid* f) {
   int gx = (f->NY + 31) / 32;
   int gy = (f->NX + 7) / 8;
-  int cap = 608 / gx;
+  int cap = 1216 / gx;
   if (cap < 1) cap = 1;
   if (gy > cap) gy = cap;
   return dim3(gx, gy);

@@ -450,6 +450,95 @@ __global__ void k_grad(float* __restrict__ U, float* __restrict__ V, float* __re
   p[u] = act ? cp * pc : 0.0f;
 }
 
+// Gradient subtract for the parallel scheme, fused with what follows it in
+// the step: the post-projection divergence statistics (sum div^2 in float
+// pairs within the block and FP64 across blocks, max |div|, fluid cell
+// count) and, when confinement is off, addTurbulence (fluid.go:496-526),
+// which only touches a cell's own U, V.  Reads U, V and writes the rotated
+// buffers Uo, Vo, so the divergence can recompute a neighbour's projected
+// face from its original value.  One thread strides down the rows of its
+// column (reduce_grid).
+__global__ void k_grad_fused(const float* __restrict__ U, const float* __restrict__ V,
+                             float* __restrict__ Uo, float* __restrict__ Vo, float* __restrict__ p,
+                             const float* __restrict__ phi0, const float* __restrict__ phi1,
+                             const PCtl* __restrict__ ctl, const float* __restrict__ e0,
+                             const float* __restrict__ e1, const PCtl* __restrict__ ectl,
+                             const uint8_t* __restrict__ flags, float cp,
+                             const float2* __restrict__ noise, float turbStrength, int do_turb,
+                             double* __restrict__ part, Grid g) {
+  __shared__ double red[32];
+  __shared__ float redf[32];
+  const float* phi = ctl->sel ? phi1 : phi0;
+  const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
+  const int P = g.P;
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  FF s2{0.0f, 0.0f};
+  float mx = 0.0f;
+  int n = 0;
+  if (j < g.NY) {
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < g.NX; i += gridDim.y * blockDim.y) {
+      int c = i * P + j;
+      uint8_t fl = flags[c];
+      bool act = flag_active(fl);
+      float pc = phi_final(phi, e, c, act);
+      float u = U[c], v = V[c];
+      if (i >= 1 && j >= 1 && j <= g.NY - 2) {
+        bool actL = flag_active(flags[c - P]);
+        if (act || actL) u = u + (fbit(fl, F_FLUID) * phi_final(phi, e, c - P, actL) - fbit(fl, F_W) * pc);
+      }
+      if (j >= 1 && i >= 1 && i <= g.NX - 2) {
+        bool actB = flag_active(flags[c - 1]);
+        if (act || actB) v = v + (fbit(fl, F_FLUID) * phi_final(phi, e, c - 1, actB) - fbit(fl, F_S) * pc);
+      }
+      p[c] = act ? cp * pc : 0.0f;
+      if ((fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR)) {
+        // Projected faces (i+1, j) and (i, j+1), as their own threads compute them.
+        uint8_t fR = flags[c + P];
+        bool actR = flag_active(fR);
+        float uR = U[c + P];
+        if (act || actR) uR = uR + (fbit(fR, F_FLUID) * pc - fbit(fR, F_W) * phi_final(phi, e, c + P, actR));
+        uint8_t fT = flags[c + 1];
+        bool actT = flag_active(fT);
+        float vT = V[c + 1];
+        if (act || actT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * phi_final(phi, e, c + 1, actT));
+        float div = uR - u + vT - v;
+        s2 = ff_add(s2, ff_sq(div));
+        float a = fabsf(div);
+        if (a > mx) mx = a;
+        ++n;
+        if (do_turb) {
+          float2 nz = noise[c];
+          float noiseU = nz.x * turbStrength;
+          float noiseV = nz.y * turbStrength;
+          float localVel = sqrtf(u * u + v * v);
+          if (localVel > 0.1f) {
+            float turbulenceFactor = go_min(localVel * 0.5f, 1.0f);
+            u += noiseU * turbulenceFactor;
+            v += noiseV * turbulenceFactor;
+          }
+        }
+      }
+      Uo[c] = u;
+      Vo[c] = v;
+    }
+  }
+  double a = block_sum_ff(s2, red);
+  float b = block_max_f(mx, redf);
+  double cn = block_sum_ff(FF{(float)n, 0.0f}, red);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    double* o = part + 3 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x);
+    o[0] = a;
+    o[1] = (double)b;
+    o[2] = cn;
+  }
+}
+
+__global__ void k_store_div_p(const double* __restrict__ r, DevStats* st) {
+  st->div_l2_sq = r[0];
+  st->div_max = r[1];
+  st->div_count = r[2];
+}
+
 __global__ void k_finish_parallel(const PCtl* __restrict__ ctl, DevStats* st) {
   st->sweeps = ctl->sweeps;
   st->last_maxdiv = (double)__uint_as_float(ctl->slots[ctl->last_launch]);
@@ -543,7 +632,7 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
   return cudaGetLastError();
 }
 
-cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt) {
+cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb) {
   float cp = f->density * f->h / dt;  // fluid.go:158
   cudaError_t e;
   if (f->prm.scheme == FG_SCHEME_LEXSOR) {
@@ -576,10 +665,18 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt) {
                           false)) != cudaSuccess)
       return e;
   }
-  count(f);
-  k_grad<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
-                                   f->err, f->err2, refine ? ectl : nullptr, f->flags, cp, f->g,
-                                   f->P);
+  dim3 rg = reduce_grid(f);
+  int nb = rg.x * rg.y;
+  count(f, 3);
+  k_grad_fused<<<rg, bl, 0, f->stream>>>(
+      f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
+      f->err, f->err2, refine ? ectl : nullptr, f->flags, cp, f->noise,
+      f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g);
+  swap_state(f, FG_U);
+  swap_state(f, FG_V);
+  double* out = f->partials + 3 * (size_t)nb;
+  k_combine<3><<<1, 1024, 0, f->stream>>>(f->partials, nb, 2u, out);
+  k_store_div_p<<<1, 1, 0, f->stream>>>(out, f->dstats);
   return cudaGetLastError();
 }
 
