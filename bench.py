@@ -282,12 +282,16 @@ def run_ours(args):
     # ------------------------------------------------------------ dominant kernel
     f.profile(True)
     spans = []
+    stages = {}
     for _ in range(min(args.steps, 5)):
         f.Simulate(DT)
         span, nl = f.jacobi_span()
         spans.append(span / nl)
+        for name, ms_ in f.stage_times():
+            stages.setdefault(name, []).append(ms_)
     f.profile(False)
     launch_ms = statistics.median(spans)
+    stage_ms = {k: round(statistics.median(v), 4) for k, v in stages.items()}
     n_cells = f.NumX * f.NumY
     alg_bytes = JACOBI_BYTES_PER_CELL_SWEEP * TB * n_cells
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
@@ -348,6 +352,7 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": sampler.summary(),
             "host_ms_per_step": 1e3 * t_host / args.steps,
+            "stage_ms": stage_ms,
             "step_stats": {"div_l2_post": st["div_l2_post"], "resid_l2": st["resid_l2"],
                            "smoke_mass": st["smoke_mass"], "sweeps": st["sweeps"]},
         }

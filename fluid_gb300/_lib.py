@@ -90,6 +90,7 @@ SIGNATURES = {
     "fg_adaptive_time_step": (_c_i, [_vp, _c_f, _fp]),
     "fg_profile_enable": (_c_i, [_vp, _c_i]),
     "fg_profile_jacobi": (_c_i, [_vp, _fp, ctypes.POINTER(_c_i)]),
+    "fg_profile_stages": (_c_i, [_vp, _c_i, _fp, ctypes.POINTER(ctypes.c_char_p)]),
     "fg_launch_count": (ctypes.c_ulonglong, [_vp]),
     "fg_edit_bytes": (ctypes.c_ulonglong, [_vp]),
     "fg_project_noalloc": (_c_i, [_vp, _vp, _vp, _vp, _c_i, _c_i, _c_i, _c_f, _c_f, _c_f, _c_i,

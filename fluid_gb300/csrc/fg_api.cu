@@ -230,25 +230,34 @@ int enqueue_pressure(fg_fluid* f, int iters, float dt, bool fuse_turb) {
 // pointers as the out-of-place stages run.
 int enqueue_step(fg_fluid* f, float dt) {
   const fg_params& p = f->prm;
+  f->n_marks = 0;
+  mark(f, "start");
   CK(f, launch_apply_sources(f), "sources");
   CK(f, launch_clear_stats(f), "clear stats");
   if (p.scheme == FG_SCHEME_LEXSOR)
     CK(f, cudaMemsetAsync(f->d[FG_P], 0, field_bytes(f), f->stream), "fill p");
   if (p.viscosity_diffusion > 0.0f) CK(f, launch_viscosity(f, dt), "viscosity");
+  mark(f, "sources+viscosity");
   const bool conf = p.confinement != 0.0f, turb = p.turbulence_strength > 0.0f;
   const bool fuse_turb = p.scheme == FG_SCHEME_JACOBI && !conf && turb;
   int rc = enqueue_pressure(f, p.num_iters, dt, fuse_turb);
   if (rc) return rc;
+  mark(f, "gradient+div stats");
   if (!fuse_turb) CK(f, launch_confinement_turbulence(f, dt, conf, turb), "confinement/turbulence");
   CK(f, launch_borders(f), "borders");
+  mark(f, "confinement/turbulence+borders");
   if (p.use_bfecc) {
     CK(f, launch_advect_velocity_bfecc(f, dt), "advect velocity");
+    mark(f, "advect velocity");
     CK(f, launch_advect_smoke_bfecc(f, dt), "advect smoke");
   } else {
     CK(f, launch_advect_velocity(f, dt), "advect velocity");
+    mark(f, "advect velocity");
     CK(f, launch_advect_smoke(f, dt), "advect smoke");
   }
+  mark(f, "advect smoke");
   CK(f, launch_smoke_mass(f), "smoke mass");
+  mark(f, "smoke mass");
   return FG_OK;
 }
 
@@ -323,6 +332,8 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
       return bail(FG_ERR_CUDA);
     if (cudaEventCreate(&f->prof_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
   }
+  for (int k = 0; k < fg_fluid::kMaxMarks; ++k)
+    if (cudaEventCreate(&f->mark_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
   for (int k = 0; k < FG_NUM_FIELDS; ++k)
     if ((rc = alloc_dev(f, &f->d[k]))) return bail(rc);
   for (int k : {FG_U, FG_V, FG_M})
@@ -394,6 +405,8 @@ int fg_destroy(fg_fluid* f) {
     if (f->edit_ev[k]) cudaEventDestroy(f->edit_ev[k]);
     if (f->prof_ev[k]) cudaEventDestroy(f->prof_ev[k]);
   }
+  for (int k = 0; k < fg_fluid::kMaxMarks; ++k)
+    if (f->mark_ev[k]) cudaEventDestroy(f->mark_ev[k]);
   cudaFreeHost(f->scalar_pinned);
   cudaFreeHost(f->stats_pinned);
   if (f->stream) cudaStreamDestroy(f->stream);
@@ -934,6 +947,19 @@ int fg_profile_jacobi(fg_fluid* f, float* ms, int* launches) {
   CK(f, cudaEventElapsedTime(ms, f->prof_ev[0], f->prof_ev[1]), "profile elapsed");
   *launches = f->prof_launches;
   return FG_OK;
+}
+
+int fg_profile_stages(fg_fluid* f, int max, float* ms, const char** names) {
+  if (!f || max < 0 || (max && (!ms || !names))) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  CK(f, cudaStreamSynchronize(f->stream), "profile sync");
+  int n = 0;
+  for (int k = 1; k < f->n_marks && n < max; ++k, ++n) {
+    CK(f, cudaEventElapsedTime(&ms[n], f->mark_ev[k - 1], f->mark_ev[k]), "profile elapsed");
+    names[n] = f->mark_name[k];
+  }
+  return n;
 }
 
 unsigned long long fg_launch_count(const fg_fluid* f) { return f ? f->launches : 0ull; }

@@ -181,6 +181,11 @@ struct fg_fluid {
   bool profile = false;
   cudaEvent_t prof_ev[2] = {};
   int prof_launches = 0;
+  // With profiling on, events at the stage boundaries of each step.
+  static constexpr int kMaxMarks = 16;
+  cudaEvent_t mark_ev[kMaxMarks] = {};
+  const char* mark_name[kMaxMarks] = {};
+  int n_marks = 0;
   float* scalar_pinned = nullptr;  // small D2H results
   fg::DevStats* stats_pinned = nullptr;
   std::string last_error;
@@ -240,6 +245,14 @@ inline dim3 reduce_grid(const fg_fluid* f) {
   if (cap < 1) cap = 1;
   if (gy > cap) gy = cap;
   return dim3(gx, gy);
+}
+
+// Records a stage-boundary event named `name` (profiling only).
+inline void mark(fg_fluid* f, const char* name) {
+  if (!f->profile || f->n_marks >= fg_fluid::kMaxMarks) return;
+  cudaEventRecord(f->mark_ev[f->n_marks], f->stream);
+  f->mark_name[f->n_marks] = name;
+  f->n_marks++;
 }
 
 // Counts one kernel launch on the handle (for the benchmark's launch tally).

@@ -652,18 +652,22 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   count(f);
   k_setup_system<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->phi, f->rhs, f->wgt, f->bw,
                                            f->flags, om, num_iters == 0 ? 1 : 0, f->g, f->P);
+  mark(f, "pressure setup");
   if (num_iters > 0) {
     if ((e = jacobi_solve(f, ctl, f->rhs, f->bw, f->phi, f->phi2, num_iters, true)) != cudaSuccess)
       return e;
     count(f);
     k_finish_parallel<<<1, 1, 0, f->stream>>>(ctl, f->dstats);
   }
+  mark(f, "jacobi sweeps");
   bool refine = f->prm.refine_sweeps > 0;
   if ((e = resid_stats(f, refine)) != cudaSuccess) return e;
+  mark(f, "fp64 residual");
   if (refine) {
     if ((e = jacobi_solve(f, ectl, f->rhs_e, f->bwe, f->err, f->err2, f->prm.refine_sweeps,
                           false)) != cudaSuccess)
       return e;
+    mark(f, "outer correction");
   }
   dim3 rg = reduce_grid(f);
   int nb = rg.x * rg.y;

@@ -321,6 +321,15 @@ class Fluid:
                     "fg_profile_jacobi")
         return ms.value, n.value
 
+    def stage_times(self):
+        """[(stage, ms)] of the last step run with profiling on."""
+        ms = (ctypes.c_float * 16)()
+        names = (ctypes.c_char_p * 16)()
+        n = self._L.fg_profile_stages(self._h, 16, ms, names)
+        if n < 0:
+            self._check(n, "fg_profile_stages")
+        return [(names[k].decode(), ms[k]) for k in range(n)]
+
     def Reset(self):
         self._check(self._L.fg_reset(self._h), "Reset")
 

@@ -193,6 +193,9 @@ int fg_adaptive_time_step(fg_fluid* f, float basedt, float* out);               
  * fg_edit_bytes the bytes of queued tool edits uploaded so far. */
 int fg_profile_enable(fg_fluid* f, int on);
 int fg_profile_jacobi(fg_fluid* f, float* ms, int* launches);
+/* Per-stage times (ms) of the last profiled step; returns the number of
+ * stages written (<= max), names[k] naming the stage that ended at mark k. */
+int fg_profile_stages(fg_fluid* f, int max, float* ms, const char** names);
 unsigned long long fg_launch_count(const fg_fluid* f);
 unsigned long long fg_edit_bytes(const fg_fluid* f);
 
