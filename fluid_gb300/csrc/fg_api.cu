@@ -255,9 +255,7 @@ int enqueue_step(fg_fluid* f, float dt) {
     mark(f, "advect velocity");
     CK(f, launch_advect_smoke(f, dt), "advect smoke");
   }
-  mark(f, "advect smoke");
-  CK(f, launch_smoke_mass(f), "smoke mass");
-  mark(f, "smoke mass");
+  mark(f, "advect smoke+mass");
   return FG_OK;
 }
 

@@ -76,10 +76,14 @@ __device__ __forceinline__ float fbit(uint8_t f, uint8_t bit) { return (f & bit)
 
 // sampleField / sampleFieldFrom (fluid.go:357-398, 1055-1091).  dx, dy are
 // the staggering offsets of the sampled field (U: 0,h/2; V: h/2,0; M: h/2,h/2).
+// The clamp of the coordinates uses fminf/fmaxf: for any non-NaN coordinate
+// they equal Go's min/max here (the bounds are positive, so no signed-zero
+// ties); a NaN coordinate, where the reference's int conversion of the floor
+// gives an out-of-range index and panics, clamps to the upper bound.
 __device__ __forceinline__ float sample_field(const float* __restrict__ d, float x, float y,
                                               float dx, float dy, const Grid& g) {
-  x = go_max(go_min(x, g.NXh), g.h);
-  y = go_max(go_min(y, g.NYh), g.h);
+  x = fmaxf(fminf(x, g.NXh), g.h);
+  y = fmaxf(fminf(y, g.NYh), g.h);
   float xs = x - dx;
   float ys = y - dy;
   int x0 = min((int)floorf(xs * g.h1), g.NX - 1);
@@ -88,11 +92,6 @@ __device__ __forceinline__ float sample_field(const float* __restrict__ d, float
   int y0 = min((int)floorf(ys * g.h1), g.NY - 1);
   float ty = (ys - (float)y0 * g.h) * g.h1;
   int y1 = min(y0 + 1, g.NY - 1);
-  // Finite inputs keep x0, y0 >= 0; a NaN coordinate converts to 0.
-  x0 = max(x0, 0);
-  y0 = max(y0, 0);
-  x1 = max(x1, 0);
-  y1 = max(y1, 0);
   float sx = 1.0f - tx;
   float sy = 1.0f - ty;
   return sx * sy * d[x0 * g.P + y0] + tx * sy * d[x1 * g.P + y0] + tx * ty * d[x1 * g.P + y1] +
@@ -228,6 +227,8 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
 // k_diag.cu
 cudaError_t launch_div_stats(fg_fluid* f);
 cudaError_t launch_smoke_mass(fg_fluid* f);
+// Combines the smoke-mass block partials the final smoke pass wrote.
+cudaError_t launch_store_mass(fg_fluid* f, int nb);
 cudaError_t launch_clear_stats(fg_fluid* f);
 cudaError_t launch_max_divergence(fg_fluid* f, float* dev_out);
 cudaError_t launch_view(fg_fluid* f, int kind, float* dev_minmax);  // 0 vorticity, 1 magnitude

@@ -36,22 +36,46 @@ __device__ __forceinline__ double block_reduce(double v, double* sh) {
   return v;
 }
 
-// Combines n rows of NS partials (partials[k*NS + s]); bit s of max_mask
-// selects max instead of sum for slot s.  One block of 1024 threads.
+// Combines rows [b*per, min(n, (b+1)*per)) of NS partials (partials[k*NS +
+// s]) into out[b*NS + s], one block b of 1024 threads per output row; bit s
+// of max_mask selects max instead of sum for slot s.
 template <int NS>
-__global__ void k_combine(const double* __restrict__ partials, int n, unsigned max_mask,
+__global__ void k_combine(const double* __restrict__ partials, int n, int per, unsigned max_mask,
                           double* __restrict__ out) {
   __shared__ double sh[32];
+  int k0 = blockIdx.x * per;
+  int k1 = min(n, k0 + per);
   for (int s = 0; s < NS; ++s) {
     bool mx = (max_mask >> s) & 1u;
     double v = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
       double w = partials[(size_t)k * NS + s];
       v = mx ? fmax(v, w) : v + w;
     }
     v = mx ? block_reduce<true>(v, sh) : block_reduce<false>(v, sh);
-    if (threadIdx.x == 0) out[s] = v;
+    if (threadIdx.x == 0) out[(size_t)blockIdx.x * NS + s] = v;
   }
+}
+
+// Deterministic two-level combine of n rows of NS partials starting at
+// `part`; the result (NS doubles) is written at *out_ptr, which points past
+// the level-one rows inside the same buffer.  Returns the number of kernels.
+template <int NS>
+inline int combine_partials(cudaStream_t st, double* part, int n, unsigned max_mask,
+                            double** out_ptr) {
+  double* lvl = part + (size_t)NS * n;
+  const int per = 2048;
+  if (n <= per) {
+    k_combine<NS><<<1, 1024, 0, st>>>(part, n, n, max_mask, lvl);
+    *out_ptr = lvl;
+    return 1;
+  }
+  int g = (n + per - 1) / per;
+  k_combine<NS><<<g, 1024, 0, st>>>(part, n, per, max_mask, lvl);
+  double* out = lvl + (size_t)NS * g;
+  k_combine<NS><<<1, 1024, 0, st>>>(lvl, g, g, max_mask, out);
+  *out_ptr = out;
+  return 2;
 }
 
 }  // namespace

@@ -10,6 +10,7 @@
 // staging value.  The result is written to the rotation partner of the state
 // field and to the staging buffer, after which state and partner swap.
 #include "fg_internal.cuh"
+#include "fg_reduce.cuh"
 
 namespace fg {
 namespace {
@@ -171,25 +172,36 @@ __device__ __forceinline__ float smoke_value(const float* __restrict__ Ut,
 __global__ void k_sl_smoke(const float* __restrict__ Ut, const float* __restrict__ Vt,
                            const float* __restrict__ Ms, float* __restrict__ Mo, float* nM,
                            const uint8_t* __restrict__ flags, float dt, float smokeAdv,
-                           int diffuse, float smokeDiffusion, Grid g) {
+                           int diffuse, float smokeDiffusion, double* __restrict__ mass_part,
+                           Grid g) {
+  __shared__ double red[32];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
-  int c = i * g.P + j;
-  uint8_t fl = flags[c];
-  float m;
-  if ((fl & (F_INTERIOR | F_FLUID)) == (F_INTERIOR | F_FLUID)) {
-    float s = smoke_value(Ut, Vt, Ms, i, j, dt, smokeAdv, g);
-    if (diffuse) {
-      float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
-      s += smokeDiffusion * neighbors;
+  FF mass{0.0f, 0.0f};
+  if (i < g.NX && j < g.NY) {
+    int c = i * g.P + j;
+    uint8_t fl = flags[c];
+    float m;
+    if ((fl & (F_INTERIOR | F_FLUID)) == (F_INTERIOR | F_FLUID)) {
+      float s = smoke_value(Ut, Vt, Ms, i, j, dt, smokeAdv, g);
+      if (diffuse) {
+        float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
+        s += smokeDiffusion * neighbors;
+      }
+      m = go_max(s, 0.0f);
+    } else {
+      m = on_ring(i, j, g) ? Ms[c] : nM[c];
     }
-    m = go_max(s, 0.0f);
-  } else {
-    m = on_ring(i, j, g) ? Ms[c] : nM[c];
+    Mo[c] = m;
+    nM[c] = m;
+    if (!on_ring(i, j, g)) mass.hi = m;
   }
-  Mo[c] = m;
-  nM[c] = m;
+  // Smoke mass of the result over interior cells (float pairs within the
+  // block, FP64 across blocks).
+  if (mass_part) {
+    double a = block_sum_ff(mass, red);
+    if (threadIdx.x == 0 && threadIdx.y == 0) mass_part[blockIdx.y * gridDim.x + blockIdx.x] = a;
+  }
 }
 
 // BFECC smoke pass 1 (fluid.go:1007): forward advection into Fm without
@@ -263,11 +275,12 @@ cudaError_t launch_advect_smoke(fg_fluid* f, float dt) {
   int diffuse;
   float sd = smoke_diffusion(f, dt, &diffuse);
   count(f);
-  k_sl_smoke<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(
+  dim3 gr = cell_grid(f);
+  k_sl_smoke<<<gr, dim3(BX, BY), 0, f->stream>>>(
       f->d[FG_U], f->d[FG_V], f->d[FG_M], f->partner[FG_M], f->d[FG_NEWM], f->flags, dt,
-      f->prm.smoke_advection, diffuse, sd, f->g);
+      f->prm.smoke_advection, diffuse, sd, f->partials, f->g);
   swap_state(f, FG_M);
-  return cudaGetLastError();
+  return launch_store_mass(f, gr.x * gr.y);
 }
 
 cudaError_t launch_advect_velocity_bfecc(fg_fluid* f, float dt) {
@@ -302,9 +315,10 @@ cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt) {
                                                   f->corrM, f->flags, dt, sa, f->g);
   count(f);
   k_sl_smoke<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->corrM, f->partner[FG_M],
-                                       f->d[FG_NEWM], f->flags, dt, sa, diffuse, sd, f->g);
+                                       f->d[FG_NEWM], f->flags, dt, sa, diffuse, sd, f->partials,
+                                       f->g);
   swap_state(f, FG_M);
-  return cudaGetLastError();
+  return launch_store_mass(f, gr.x * gr.y);
 }
 
 }  // namespace fg

@@ -26,19 +26,17 @@ __global__ void k_div_partials(const float* __restrict__ U, const float* __restr
   __shared__ double red[32];
   __shared__ float redf[32];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
   FF s2{0.0f, 0.0f};
   float mx = 0.0f;
   int n = 0;
-  if (j < g.NY) {
-    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < g.NX; i += gridDim.y * blockDim.y) {
-      int c = i * g.P + j;
-      if (fluid_interior(flags[c])) {
-        float div = U[c + g.P] - U[c] + V[c + 1] - V[c];
-        s2 = ff_add(s2, ff_sq(div));
-        float a = fabsf(div);
-        if (a > mx) mx = a;
-        ++n;
-      }
+  if (j < g.NY && i < g.NX) {
+    int c = i * g.P + j;
+    if (fluid_interior(flags[c])) {
+      float div = U[c + g.P] - U[c] + V[c + 1] - V[c];
+      s2 = ff_sq(div);
+      mx = fabsf(div);
+      n = 1;
     }
   }
   double a = block_sum_ff(s2, red);
@@ -209,14 +207,13 @@ cudaError_t launch_clear_stats(fg_fluid* f) {
 }
 
 cudaError_t launch_div_stats(fg_fluid* f) {
-  dim3 gr = reduce_grid(f);
+  dim3 gr = cell_grid(f);
   int nb = gr.x * gr.y;
   count(f);
   k_div_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags,
                                                      f->partials, f->g);
-  double* out = f->partials + 3 * (size_t)nb;
-  count(f);
-  k_combine<3><<<1, 1024, 0, f->stream>>>(f->partials, nb, 2u, out);
+  double* out = nullptr;
+  count(f, combine_partials<3>(f->stream, f->partials, nb, 2u, &out));
   count(f);
   k_store_div<<<1, 1, 0, f->stream>>>(out, f->dstats);
   return cudaGetLastError();
@@ -227,9 +224,16 @@ cudaError_t launch_smoke_mass(fg_fluid* f) {
   int nb = gr.x * gr.y;
   count(f);
   k_mass_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_M], f->partials, f->g);
-  double* out = f->partials + (size_t)nb;
+  double* out = nullptr;
+  count(f, combine_partials<1>(f->stream, f->partials, nb, 0u, &out));
   count(f);
-  k_combine<1><<<1, 1024, 0, f->stream>>>(f->partials, nb, 0u, out);
+  k_store_mass<<<1, 1, 0, f->stream>>>(out, f->dstats);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_store_mass(fg_fluid* f, int nb) {
+  double* out = nullptr;
+  count(f, combine_partials<1>(f->stream, f->partials, nb, 0u, &out));
   count(f);
   k_store_mass<<<1, 1, 0, f->stream>>>(out, f->dstats);
   return cudaGetLastError();
@@ -241,9 +245,8 @@ cudaError_t launch_max_divergence(fg_fluid* f, float* dev_out) {
   count(f);
   k_maxdiv_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags,
                                                         f->partials, f->g);
-  double* out = f->partials + (size_t)nb;
-  count(f);
-  k_combine<1><<<1, 1024, 0, f->stream>>>(f->partials, nb, 1u, out);
+  double* out = nullptr;
+  count(f, combine_partials<1>(f->stream, f->partials, nb, 1u, &out));
   count(f);
   k_store_float<<<1, 1, 0, f->stream>>>(out, dev_out);
   return cudaGetLastError();
@@ -255,9 +258,8 @@ cudaError_t launch_max_speed(fg_fluid* f, float* dev_out) {
   count(f);
   k_speed_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags,
                                                        f->partials, f->g);
-  double* out = f->partials + (size_t)nb;
-  count(f);
-  k_combine<1><<<1, 1024, 0, f->stream>>>(f->partials, nb, 1u, out);
+  double* out = nullptr;
+  count(f, combine_partials<1>(f->stream, f->partials, nb, 1u, &out));
   count(f);
   k_store_float<<<1, 1, 0, f->stream>>>(out, dev_out);
   return cudaGetLastError();

@@ -373,25 +373,22 @@ __global__ void k_resid64(const float* __restrict__ phi0, const float* __restric
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   FF sq{0.0f, 0.0f};
   float ra = 0.0f;
-  if (j < g.NY) {
-    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < g.NX; i += gridDim.y * blockDim.y) {
-      int c = i * g.P + j;
-      uint8_t fl = flags[c];
-      float re = 0.0f;
-      if (flag_active(fl)) {
-        FF r = resid_ff(rhs[c], phi[c - g.P], phi[c + g.P], phi[c - 1], phi[c + 1],
-                        (float)flag_count(fl), phi[c]);
-        re = r.hi;
-        FF q = ff_sq(r.hi);
-        q.lo = q.lo + 2.0f * r.hi * r.lo;
-        sq = ff_add(sq, q);
-        float ar = fabsf(r.hi);
-        if (ar > ra) ra = ar;
-      }
-      if (rhs_e) {
-        rhs_e[c] = re;
-        bwe[c] = W[c] * re;
-      }
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j < g.NY && i < g.NX) {
+    int c = i * g.P + j;
+    uint8_t fl = flags[c];
+    float re = 0.0f;
+    if (flag_active(fl)) {
+      FF r = resid_ff(rhs[c], phi[c - g.P], phi[c + g.P], phi[c - 1], phi[c + 1],
+                      (float)flag_count(fl), phi[c]);
+      re = r.hi;
+      sq = ff_sq(r.hi);
+      sq.lo = sq.lo + 2.0f * r.hi * r.lo;
+      ra = fabsf(r.hi);
+    }
+    if (rhs_e) {
+      rhs_e[c] = re;
+      bwe[c] = W[c] * re;
     }
   }
   double s = block_sum_ff(sq, red);
@@ -475,8 +472,9 @@ __global__ void k_grad_fused(const float* __restrict__ U, const float* __restric
   FF s2{0.0f, 0.0f};
   float mx = 0.0f;
   int n = 0;
-  if (j < g.NY) {
-    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < g.NX; i += gridDim.y * blockDim.y) {
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j < g.NY && i < g.NX) {
+    {
       int c = i * P + j;
       uint8_t fl = flags[c];
       bool act = flag_active(fl);
@@ -502,10 +500,9 @@ __global__ void k_grad_fused(const float* __restrict__ U, const float* __restric
         float vT = V[c + 1];
         if (act || actT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * phi_final(phi, e, c + 1, actT));
         float div = uR - u + vT - v;
-        s2 = ff_add(s2, ff_sq(div));
-        float a = fabsf(div);
-        if (a > mx) mx = a;
-        ++n;
+        s2 = ff_sq(div);
+        mx = fabsf(div);
+        n = 1;
         if (do_turb) {
           float2 nz = noise[c];
           float noiseU = nz.x * turbStrength;
@@ -552,15 +549,14 @@ __global__ void k_store_resid(const double* __restrict__ r, DevStats* st) {
 }  // namespace
 
 static cudaError_t resid_stats(fg_fluid* f, bool write_rhs_e) {
-  dim3 gr = reduce_grid(f);
+  dim3 gr = cell_grid(f);
   int nb = gr.x * gr.y;
   count(f);
   k_resid64<<<gr, dim3(BX, BY), 0, f->stream>>>(
       f->phi, f->phi2, (PCtl*)f->pctl, f->rhs, f->wgt, f->flags,
       write_rhs_e ? f->rhs_e : nullptr, f->bwe, f->partials, f->g);
-  double* out = f->partials + 2 * (size_t)nb;
-  count(f);
-  k_combine<2><<<1, 1024, 0, f->stream>>>(f->partials, nb, 2u, out);
+  double* out = nullptr;
+  count(f, combine_partials<2>(f->stream, f->partials, nb, 2u, &out));
   count(f);
   k_store_resid<<<1, 1, 0, f->stream>>>(out, f->dstats);
   return cudaGetLastError();
@@ -669,17 +665,17 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
       return e;
     mark(f, "outer correction");
   }
-  dim3 rg = reduce_grid(f);
+  dim3 rg = cell_grid(f);
   int nb = rg.x * rg.y;
-  count(f, 3);
+  count(f, 2);
   k_grad_fused<<<rg, bl, 0, f->stream>>>(
       f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
       f->err, f->err2, refine ? ectl : nullptr, f->flags, cp, f->noise,
       f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
-  double* out = f->partials + 3 * (size_t)nb;
-  k_combine<3><<<1, 1024, 0, f->stream>>>(f->partials, nb, 2u, out);
+  double* out = nullptr;
+  count(f, combine_partials<3>(f->stream, f->partials, nb, 2u, &out));
   k_store_div_p<<<1, 1, 0, f->stream>>>(out, f->dstats);
   return cudaGetLastError();
 }

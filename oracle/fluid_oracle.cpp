@@ -596,8 +596,11 @@ struct Fluid {
     int n = NY;
     T h1 = (T)1.0 / h;
     T h2 = (T)0.5 * h;
-    x = go_max(go_min(x, (T)NX * h), h);
-    y = go_max(go_min(y, (T)NY * h), h);
+    // fmin/fmax equal Go's min/max for every non-NaN coordinate here (the
+    // bounds are positive); a NaN coordinate, which makes the reference
+    // panic on its index, clamps to the upper bound as on the GPU.
+    x = std::fmax(std::fmin(x, (T)NX * h), h);
+    y = std::fmax(std::fmin(y, (T)NY * h), h);
     T dx = 0, dy = 0;
     if (fld == 0) dy = h2;
     else if (fld == 1) dx = h2;
