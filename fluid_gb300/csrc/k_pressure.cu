@@ -208,12 +208,22 @@ constexpr int OJ = RJ - 2 * TMAX;  // 112 owned columns
 constexpr int OI = RI - 2 * TMAX;  // 48 owned rows
 constexpr int TB_THREADS = 32 * NWARP;
 
-template <bool OMEGA1, bool FULL, bool CHECK>
+// RINIT (first launch of the outer correction): instead of loading bw, the
+// kernel loads the main potential phi (from the buffer the main solve's
+// control block names), b and the flags, forms the correction right-hand
+// side b_e = r(phi) = resid_ff(...) rounded to float on every region cell
+// (garbage only on the region's outermost ring, which the halo absorbs),
+// sets bw = w * b_e, starts the correction from 0 and, when more launches
+// follow, writes b_e and bw_e of the owned cells to rhs_e / bwe.
+template <bool OMEGA1, bool FULL, bool CHECK, bool RINIT>
 __global__ void __launch_bounds__(TB_THREADS, 2)
     k_jacobi_rb(const float* __restrict__ src, float* __restrict__ dst,
                 const float* __restrict__ W, const float* __restrict__ BW,
                 const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float om1,
-                PCtl* ctl, int k, int t0, int ns, float tol, int out_sel, int zero_init, Grid g) {
+                PCtl* ctl, int k, int t0, int ns, float tol, int out_sel, int zero_init, Grid g,
+                const float* __restrict__ mphi0, const float* __restrict__ mphi1,
+                const PCtl* __restrict__ mctl, float* __restrict__ rhs_e,
+                float* __restrict__ bwe) {
   __shared__ float4 xch[2][2][NWARP][32];
   __shared__ float red[NWARP];
   __shared__ int skip;
@@ -234,28 +244,94 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   // either wholly left of the grid or a 16-byte aligned read inside the row.
   const bool colok = gj >= 0 && gj < g.P;
   float x[RT][JT], w[RT][JT], bw[RT][JT];
+  uint32_t fr[RINIT ? RT : 1];
+  const float* ph = RINIT ? (mctl->sel ? mphi1 : mphi0) : src;
 #pragma unroll
   for (int r = 0; r < RT; ++r) {
     int gi = gi0 + r;
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), ww = a, bb = a;
+    uint32_t f4 = 0;
     if (colok && gi >= 0 && gi < g.NX) {
       size_t c = (size_t)gi * g.P + gj;
-      if (!zero_init) a = *reinterpret_cast<const float4*>(src + c);
+      if (RINIT || !zero_init) a = *reinterpret_cast<const float4*>(ph + c);
       ww = *reinterpret_cast<const float4*>(W + c);
-      bb = *reinterpret_cast<const float4*>(BW + c);
+      bb = *reinterpret_cast<const float4*>((RINIT ? rhs : BW) + c);
+      if (RINIT) f4 = *reinterpret_cast<const uint32_t*>(flags + c);
     }
     x[r][0] = a.x; x[r][1] = a.y; x[r][2] = a.z; x[r][3] = a.w;
     w[r][0] = ww.x; w[r][1] = ww.y; w[r][2] = ww.z; w[r][3] = ww.w;
     bw[r][0] = bb.x; bw[r][1] = bb.y; bw[r][2] = bb.z; bw[r][3] = bb.w;
+    if (RINIT) fr[r] = f4;
 #pragma unroll
     for (int q = 0; q < JT; ++q)
       if (gj + q >= g.NY) {
         x[r][q] = 0.0f;
         w[r][q] = 0.0f;
         bw[r][q] = 0.0f;
+        if (RINIT) fr[r] &= ~(0xffu << (8 * q));
       }
   }
   const bool own_col = lane * JT >= TMAX && lane * JT < RJ - TMAX;
+  if (RINIT) {
+    // Residual of the main potential held in x, with b in bw.
+    xch[1][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
+    xch[1][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
+    __syncthreads();
+    float4 u4 = warp > 0 ? xch[1][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 d4 = warp < NWARP - 1 ? xch[1][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
+    const bool own_row_warp = warp >= TMAX / RT && warp < NWARP - TMAX / RT;
+#pragma unroll
+    for (int r = 0; r < RT; ++r) {
+      float lf = __shfl_up_sync(0xffffffffu, x[r][JT - 1], 1);
+      float rt = __shfl_down_sync(0xffffffffu, x[r][0], 1);
+      float nxt[JT];
+      if (r < RT - 1) {
+#pragma unroll
+        for (int q = 0; q < JT; ++q) nxt[q] = x[r + 1][q];
+      } else {
+        nxt[0] = d4.x; nxt[1] = d4.y; nxt[2] = d4.z; nxt[3] = d4.w;
+      }
+      float be[JT];
+#pragma unroll
+      for (int q = 0; q < JT; ++q) {
+        uint8_t fl = (uint8_t)(fr[r] >> (8 * q));
+        float left = q == 0 ? lf : x[r][q - 1];
+        float right = q == JT - 1 ? rt : x[r][q + 1];
+        be[q] = 0.0f;
+        if (flag_active(fl))
+          be[q] = resid_ff(bw[r][q], prev[q], nxt[q], left, right, (float)flag_count(fl), x[r][q]).hi;
+      }
+#pragma unroll
+      for (int q = 0; q < JT; ++q) {
+        prev[q] = x[r][q];
+        bw[r][q] = w[r][q] * be[q];
+      }
+      if (rhs_e && own_col && own_row_warp) {
+        int gi = gi0 + r;
+        if (gi < g.NX && gj < g.NY) {
+          size_t c = (size_t)gi * g.P + gj;
+          if (gj + JT <= g.NY) {
+            *reinterpret_cast<float4*>(rhs_e + c) = make_float4(be[0], be[1], be[2], be[3]);
+            *reinterpret_cast<float4*>(bwe + c) =
+                make_float4(bw[r][0], bw[r][1], bw[r][2], bw[r][3]);
+          } else {
+#pragma unroll
+            for (int q = 0; q < JT; ++q)
+              if (gj + q < g.NY) {
+                rhs_e[c + q] = be[q];
+                bwe[c + q] = bw[r][q];
+              }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RT; ++r)
+#pragma unroll
+      for (int q = 0; q < JT; ++q) x[r][q] = 0.0f;
+    __syncthreads();  // xch[1] is read above and written again by the second sweep
+  }
   float mx = 0.0f;
   auto sweep = [&](int sw, bool last) {
     const int buf = sw & 1;
@@ -450,83 +526,101 @@ __global__ void k_grad(float* __restrict__ U, float* __restrict__ V, float* __re
 // Gradient subtract for the parallel scheme, fused with what follows it in
 // the step: the post-projection divergence statistics (sum div^2 in float
 // pairs within the block and FP64 across blocks, max |div|, fluid cell
-// count) and, when confinement is off, addTurbulence (fluid.go:496-526),
-// which only touches a cell's own U, V.  Reads U, V and writes the rotated
-// buffers Uo, Vo, so the divergence can recompute a neighbour's projected
-// face from its original value.  One thread strides down the rows of its
-// column (reduce_grid).
-__global__ void k_grad_fused(const float* __restrict__ U, const float* __restrict__ V,
-                             float* __restrict__ Uo, float* __restrict__ Vo, float* __restrict__ p,
-                             const float* __restrict__ phi0, const float* __restrict__ phi1,
-                             const PCtl* __restrict__ ctl, const float* __restrict__ e0,
-                             const float* __restrict__ e1, const PCtl* __restrict__ ectl,
-                             const uint8_t* __restrict__ flags, float cp,
-                             const float2* __restrict__ noise, float turbStrength, int do_turb,
-                             double* __restrict__ part, Grid g) {
+// count), the residual statistics of the final potential (resid_ff per
+// cell, sum r^2 and max |r| likewise) and, when confinement is off,
+// addTurbulence (fluid.go:496-526), which only touches a cell's own U, V.
+// Reads U, V and writes the rotated buffers Uo, Vo, so the divergence can
+// recompute a neighbour's projected face from its original value.  A thread
+// handles GR rows of one column (rows i, i+8, ...).
+constexpr int GR = 4;
+__global__ void __launch_bounds__(256)
+    k_grad_fused(const float* __restrict__ U, const float* __restrict__ V,
+                 float* __restrict__ Uo, float* __restrict__ Vo, float* __restrict__ p,
+                 const float* __restrict__ phi0, const float* __restrict__ phi1,
+                 const PCtl* __restrict__ ctl, const float* __restrict__ e0,
+                 const float* __restrict__ e1, const PCtl* __restrict__ ectl,
+                 const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float cp,
+                 const float2* __restrict__ noise, float turbStrength, int do_turb,
+                 double* __restrict__ part, Grid g) {
   __shared__ double red[32];
   __shared__ float redf[32];
   const float* phi = ctl->sel ? phi1 : phi0;
   const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
   const int P = g.P;
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  FF s2{0.0f, 0.0f};
-  float mx = 0.0f;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  FF s2{0.0f, 0.0f}, r2{0.0f, 0.0f};
+  float dmx = 0.0f, rmx = 0.0f;
   int n = 0;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j < g.NY && i < g.NX) {
-    {
-      int c = i * P + j;
-      uint8_t fl = flags[c];
-      bool act = flag_active(fl);
-      float pc = phi_final(phi, e, c, act);
-      float u = U[c], v = V[c];
-      if (i >= 1 && j >= 1 && j <= g.NY - 2) {
-        bool actL = flag_active(flags[c - P]);
-        if (act || actL) u = u + (fbit(fl, F_FLUID) * phi_final(phi, e, c - P, actL) - fbit(fl, F_W) * pc);
-      }
-      if (j >= 1 && i >= 1 && i <= g.NX - 2) {
-        bool actB = flag_active(flags[c - 1]);
-        if (act || actB) v = v + (fbit(fl, F_FLUID) * phi_final(phi, e, c - 1, actB) - fbit(fl, F_S) * pc);
-      }
-      p[c] = act ? cp * pc : 0.0f;
-      if ((fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR)) {
-        // Projected faces (i+1, j) and (i, j+1), as their own threads compute them.
-        uint8_t fR = flags[c + P];
-        bool actR = flag_active(fR);
-        float uR = U[c + P];
-        if (act || actR) uR = uR + (fbit(fR, F_FLUID) * pc - fbit(fR, F_W) * phi_final(phi, e, c + P, actR));
-        uint8_t fT = flags[c + 1];
-        bool actT = flag_active(fT);
-        float vT = V[c + 1];
-        if (act || actT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * phi_final(phi, e, c + 1, actT));
-        float div = uR - u + vT - v;
-        s2 = ff_sq(div);
-        mx = fabsf(div);
-        n = 1;
-        if (do_turb) {
-          float2 nz = noise[c];
-          float noiseU = nz.x * turbStrength;
-          float noiseV = nz.y * turbStrength;
-          float localVel = sqrtf(u * u + v * v);
-          if (localVel > 0.1f) {
-            float turbulenceFactor = go_min(localVel * 0.5f, 1.0f);
-            u += noiseU * turbulenceFactor;
-            v += noiseV * turbulenceFactor;
-          }
+#pragma unroll
+  for (int k = 0; k < GR; ++k) {
+    const int i = (blockIdx.y * GR + k) * blockDim.y + threadIdx.y;
+    if (j >= g.NY || i >= g.NX) continue;
+    const int c = i * P + j;
+    const uint8_t fl = flags[c];
+    const bool act = flag_active(fl);
+    const float pc = phi_final(phi, e, c, act);
+    float u = U[c], v = V[c];
+    if (i >= 1 && j >= 1 && j <= g.NY - 2) {
+      bool actL = flag_active(flags[c - P]);
+      if (act || actL) u = u + (fbit(fl, F_FLUID) * phi_final(phi, e, c - P, actL) - fbit(fl, F_W) * pc);
+    }
+    if (j >= 1 && i >= 1 && i <= g.NX - 2) {
+      bool actB = flag_active(flags[c - 1]);
+      if (act || actB) v = v + (fbit(fl, F_FLUID) * phi_final(phi, e, c - 1, actB) - fbit(fl, F_S) * pc);
+    }
+    p[c] = act ? cp * pc : 0.0f;
+    if (act) {
+      float pw = phi_final(phi, e, c - P, flag_active(flags[c - P]));
+      float pe = phi_final(phi, e, c + P, flag_active(flags[c + P]));
+      float ps = phi_final(phi, e, c - 1, flag_active(flags[c - 1]));
+      float pn = phi_final(phi, e, c + 1, flag_active(flags[c + 1]));
+      FF r = resid_ff(rhs[c], pw, pe, ps, pn, (float)flag_count(fl), pc);
+      FF q = ff_sq(r.hi);
+      q.lo = q.lo + 2.0f * r.hi * r.lo;
+      r2 = ff_add(r2, q);
+      rmx = fmaxf(rmx, fabsf(r.hi));
+    }
+    if ((fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR)) {
+      // Projected faces (i+1, j) and (i, j+1), as their own threads compute them.
+      uint8_t fR = flags[c + P];
+      bool actR = flag_active(fR);
+      float uR = U[c + P];
+      if (act || actR) uR = uR + (fbit(fR, F_FLUID) * pc - fbit(fR, F_W) * phi_final(phi, e, c + P, actR));
+      uint8_t fT = flags[c + 1];
+      bool actT = flag_active(fT);
+      float vT = V[c + 1];
+      if (act || actT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * phi_final(phi, e, c + 1, actT));
+      float div = uR - u + vT - v;
+      s2 = ff_add(s2, ff_sq(div));
+      dmx = fmaxf(dmx, fabsf(div));
+      ++n;
+      if (do_turb) {
+        float2 nz = noise[c];
+        float noiseU = nz.x * turbStrength;
+        float noiseV = nz.y * turbStrength;
+        float localVel = sqrtf(u * u + v * v);
+        if (localVel > 0.1f) {
+          float turbulenceFactor = go_min(localVel * 0.5f, 1.0f);
+          u += noiseU * turbulenceFactor;
+          v += noiseV * turbulenceFactor;
         }
       }
-      Uo[c] = u;
-      Vo[c] = v;
     }
+    Uo[c] = u;
+    Vo[c] = v;
   }
   double a = block_sum_ff(s2, red);
-  float b = block_max_f(mx, redf);
+  float b = block_max_f(dmx, redf);
   double cn = block_sum_ff(FF{(float)n, 0.0f}, red);
+  double ra = block_sum_ff(r2, red);
+  float rb = block_max_f(rmx, redf);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    double* o = part + 3 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x);
+    double* o = part + 5 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x);
     o[0] = a;
     o[1] = (double)b;
     o[2] = cn;
+    o[3] = ra;
+    o[4] = (double)rb;
   }
 }
 
@@ -534,6 +628,8 @@ __global__ void k_store_div_p(const double* __restrict__ r, DevStats* st) {
   st->div_l2_sq = r[0];
   st->div_max = r[1];
   st->div_count = r[2];
+  st->resid_l2_sq = r[3];
+  st->resid_max = r[4];
 }
 
 __global__ void k_finish_parallel(const PCtl* __restrict__ ctl, DevStats* st) {
@@ -574,10 +670,15 @@ int jacobi_launches(const fg_fluid* f, int iters) {
 // Enqueues `iters` Jacobi sweeps of A x = b from x = 0 in launches of T
 // sweeps; x ping-pongs between x0 and x1 and ctl->sel names the buffer that
 // holds the result.  The grid g's pitch is the solver arrays' pitch.
+// With `mphi0` set, the first launch forms the right-hand side from the main
+// potential (RINIT): b is then the main right-hand side, and b_e / bw_e are
+// written to rhs_e / bwe when more launches follow (which then read them).
 static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, const float* b,
                                   const float* bw, const float* W, const uint8_t* flags, float* x0,
                                   float* x1, int iters, int T, float om, int check, float tol,
-                                  int* n_launched) {
+                                  int* n_launched, const float* mphi0 = nullptr,
+                                  const float* mphi1 = nullptr, const PCtl* mctl = nullptr,
+                                  float* rhs_e = nullptr, float* bwe = nullptr) {
   float om1 = 1.0f - om;
   bool o1 = om1 == 0.0f;
   dim3 gr((g.NY + OJ - 1) / OJ, (g.NX + OI - 1) / OI);
@@ -590,15 +691,23 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
     int sel = (k & 1) ? 0 : 1;
     int zi = k == 0 ? 1 : 0;
     bool full = ns == TMAX;
-#define FG_JAC(O, F, C)                                                                        \
-  k_jacobi_rb<O, F, C><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bw, b, flags, om1, ctl, k, t0, ns, \
-                                                  tol, sel, zi, g)
-    if (o1) {
-      if (full) { if (check) FG_JAC(true, true, true); else FG_JAC(true, true, false); }
-      else { if (check) FG_JAC(true, false, true); else FG_JAC(true, false, false); }
+    bool rinit = k == 0 && mphi0 != nullptr;
+    const float* bk = rinit ? b : (mphi0 ? rhs_e : b);
+    const float* bwk = mphi0 && k > 0 ? bwe : bw;
+    float* re = rinit && nlaunch > 1 ? rhs_e : nullptr;
+#define FG_JAC(O, F, C, R)                                                                      \
+  k_jacobi_rb<O, F, C, R><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bwk, bk, flags, om1, ctl, k, t0, \
+                                                     ns, tol, sel, zi, g, mphi0, mphi1, mctl, re, \
+                                                     bwe)
+    if (rinit) {
+      if (o1) { if (full) FG_JAC(true, true, false, true); else FG_JAC(true, false, false, true); }
+      else { if (full) FG_JAC(false, true, false, true); else FG_JAC(false, false, false, true); }
+    } else if (o1) {
+      if (full) { if (check) FG_JAC(true, true, true, false); else FG_JAC(true, true, false, false); }
+      else { if (check) FG_JAC(true, false, true, false); else FG_JAC(true, false, false, false); }
     } else {
-      if (full) { if (check) FG_JAC(false, true, true); else FG_JAC(false, true, false); }
-      else { if (check) FG_JAC(false, false, true); else FG_JAC(false, false, false); }
+      if (full) { if (check) FG_JAC(false, true, true, false); else FG_JAC(false, true, false, false); }
+      else { if (check) FG_JAC(false, false, true, false); else FG_JAC(false, false, false, false); }
     }
 #undef FG_JAC
   }
@@ -607,7 +716,7 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
 }
 
 static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const float* bw, float* x0,
-                                float* x1, int iters, bool allow_exit) {
+                                float* x1, int iters, bool allow_exit, bool rinit = false) {
   int T = clamp_tb(f->prm.tb_depth);
   int nlaunch = (iters + T - 1) / T;
   if (nlaunch > f->n_slots) return cudaErrorInvalidValue;
@@ -617,8 +726,13 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
   const bool prof = f->profile && allow_exit;
   if (prof && (e = cudaEventRecord(f->prof_ev[0], f->stream)) != cudaSuccess) return e;
   int n = 0;
-  e = enqueue_jacobi(f->stream, f->g, ctl, b, bw, f->wgt, f->flags, x0, x1, iters, T,
-                     f->prm.jacobi_omega * f->prm.pressure_damping, check, f->prm.tolerance, &n);
+  if (rinit)
+    e = enqueue_jacobi(f->stream, f->g, ctl, b, bw, f->wgt, f->flags, x0, x1, iters, T,
+                       f->prm.jacobi_omega * f->prm.pressure_damping, 0, f->prm.tolerance, &n,
+                       f->phi, f->phi2, (const PCtl*)f->pctl, f->rhs_e, f->bwe);
+  else
+    e = enqueue_jacobi(f->stream, f->g, ctl, b, bw, f->wgt, f->flags, x0, x1, iters, T,
+                       f->prm.jacobi_omega * f->prm.pressure_damping, check, f->prm.tolerance, &n);
   count(f, n);
   if (e != cudaSuccess) return e;
   if (prof) {
@@ -657,25 +771,23 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   }
   mark(f, "jacobi sweeps");
   bool refine = f->prm.refine_sweeps > 0;
-  if ((e = resid_stats(f, refine)) != cudaSuccess) return e;
-  mark(f, "fp64 residual");
   if (refine) {
-    if ((e = jacobi_solve(f, ectl, f->rhs_e, f->bwe, f->err, f->err2, f->prm.refine_sweeps,
-                          false)) != cudaSuccess)
+    if ((e = jacobi_solve(f, ectl, f->rhs, f->bw, f->err, f->err2, f->prm.refine_sweeps, false,
+                          true)) != cudaSuccess)
       return e;
     mark(f, "outer correction");
   }
-  dim3 rg = cell_grid(f);
+  dim3 rg((f->NY + BX - 1) / BX, (f->NX + BY * GR - 1) / (BY * GR));
   int nb = rg.x * rg.y;
   count(f, 2);
   k_grad_fused<<<rg, bl, 0, f->stream>>>(
       f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
-      f->err, f->err2, refine ? ectl : nullptr, f->flags, cp, f->noise,
+      f->err, f->err2, refine ? ectl : nullptr, f->rhs, f->flags, cp, f->noise,
       f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   double* out = nullptr;
-  count(f, combine_partials<3>(f->stream, f->partials, nb, 2u, &out));
+  count(f, combine_partials<5>(f->stream, f->partials, nb, 0x12u, &out));
   k_store_div_p<<<1, 1, 0, f->stream>>>(out, f->dstats);
   return cudaGetLastError();
 }

@@ -423,6 +423,8 @@ struct Fluid {
       st.last_maxdiv = keep;
       for (int c = 0; c < N; ++c)
         if (cnt[c]) phi[c] = phi[c] + err[c];
+      // Statistics: the residual of the final potential.
+      residualFP64();
     }
     // Gradient subtract + pressure.
     par(1, NX, [&](int i) {

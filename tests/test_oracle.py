@@ -94,7 +94,7 @@ def test_refinement_reduces_fp64_residual():
         rng = np.random.default_rng(1)
         f.U[:] = rng.uniform(-1, 1, f.numCells).astype(np.float32)
         f.makeIncompressible(50, 0.1)
-    # Same main solve, so the same FP64 residual before the correction; the
-    # correction lowers the divergence of the projected field.
-    assert b.stats()["resid_l2"] == a.stats()["resid_l2"]
+    # The statistics are those of the final potential: the correction lowers
+    # its residual and the divergence of the projected field.
+    assert b.stats()["resid_l2"] < a.stats()["resid_l2"]
     assert b.stats()["div_l2_post"] < a.stats()["div_l2_post"]
