@@ -139,6 +139,48 @@ __host__ __device__ __forceinline__ FF resid_ff(float b, float pw, float pe, flo
   return FF{t, e};
 }
 
+// Warp-level reduction of NS float-pair sums, NM float maxima and a count
+// of predicates, then one block-level combine in double: the block's totals
+// land in out[0..NS+NM] (sums, maxima, count) written by thread 0.  The tree
+// adds pairs with one TwoSum per level and renormalises at the end.  sh
+// holds 8 * (NS + NM + 1) doubles (blocks of up to 256 threads).
+template <int NS, int NM>
+__device__ __forceinline__ void block_stats(FF (&s)[NS], float (&m)[NM], bool pred, double* sh,
+                                            double* out) {
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = (blockDim.x * blockDim.y) >> 5;
+  const int cnt = __popc(__ballot_sync(0xffffffffu, pred));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      float bh = __shfl_down_sync(0xffffffffu, s[k].hi, o);
+      float bl = __shfl_down_sync(0xffffffffu, s[k].lo, o);
+      float t, e;
+      two_sum(s[k].hi, bh, t, e);
+      s[k].hi = t;
+      s[k].lo = (s[k].lo + bl) + e;
+    }
+#pragma unroll
+    for (int k = 0; k < NM; ++k) m[k] = fmaxf(m[k], __shfl_down_sync(0xffffffffu, m[k], o));
+  }
+  constexpr int R = NS + NM + 1;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) sh[wid * R + k] = (double)s[k].hi + (double)s[k].lo;
+#pragma unroll
+    for (int k = 0; k < NM; ++k) sh[wid * R + NS + k] = (double)m[k];
+    sh[wid * R + NS + NM] = (double)cnt;
+  }
+  __syncthreads();
+  if (tid < R) {
+    double v = 0.0;
+    bool mx = tid >= NS && tid < NS + NM;
+    for (int w = 0; w < nw; ++w) v = mx ? fmax(v, sh[w * R + tid]) : v + sh[w * R + tid];
+    out[tid] = v;
+  }
+}
+
 // Sum of a float pair per thread over the block, as a double in thread 0.
 // Warp level in float-float, block level in double.  sh: 32 doubles.
 __device__ __forceinline__ double block_sum_ff(FF v, double* sh) {

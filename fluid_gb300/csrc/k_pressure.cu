@@ -530,9 +530,8 @@ __global__ void k_grad(float* __restrict__ U, float* __restrict__ V, float* __re
 // cell, sum r^2 and max |r| likewise) and, when confinement is off,
 // addTurbulence (fluid.go:496-526), which only touches a cell's own U, V.
 // Reads U, V and writes the rotated buffers Uo, Vo, so the divergence can
-// recompute a neighbour's projected face from its original value.  A thread
-// handles GR rows of one column (rows i, i+8, ...).
-constexpr int GR = 4;
+// recompute a neighbour's projected face from its original value.  One cell
+// per thread; every neighbour value is loaded once.
 __global__ void __launch_bounds__(256)
     k_grad_fused(const float* __restrict__ U, const float* __restrict__ V,
                  float* __restrict__ Uo, float* __restrict__ Vo, float* __restrict__ p,
@@ -542,58 +541,50 @@ __global__ void __launch_bounds__(256)
                  const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float cp,
                  const float2* __restrict__ noise, float turbStrength, int do_turb,
                  double* __restrict__ part, Grid g) {
-  __shared__ double red[32];
-  __shared__ float redf[32];
+  __shared__ double sh[8 * 5];
   const float* phi = ctl->sel ? phi1 : phi0;
   const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
   const int P = g.P;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  FF s2{0.0f, 0.0f}, r2{0.0f, 0.0f};
-  float dmx = 0.0f, rmx = 0.0f;
-  int n = 0;
-#pragma unroll
-  for (int k = 0; k < GR; ++k) {
-    const int i = (blockIdx.y * GR + k) * blockDim.y + threadIdx.y;
-    if (j >= g.NY || i >= g.NX) continue;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  FF sums[2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};  // div^2, r^2
+  float maxs[2] = {0.0f, 0.0f};                // |div|, |r|
+  bool fi = false;
+  if (j < g.NY && i < g.NX) {
     const int c = i * P + j;
+    const bool hasL = i >= 1, hasR = i <= g.NX - 2, hasB = j >= 1, hasT = j <= g.NY - 2;
     const uint8_t fl = flags[c];
-    const bool act = flag_active(fl);
+    const uint8_t fL = hasL ? flags[c - P] : 0, fR = hasR ? flags[c + P] : 0;
+    const uint8_t fB = hasB ? flags[c - 1] : 0, fT = hasT ? flags[c + 1] : 0;
+    const bool act = flag_active(fl), aL = flag_active(fL), aR = flag_active(fR);
+    const bool aB = flag_active(fB), aT = flag_active(fT);
+    // phi is 0 off the active cells; the correction is added on active ones.
     const float pc = phi_final(phi, e, c, act);
+    const float pL = hasL ? phi_final(phi, e, c - P, aL) : 0.0f;
+    const float pR = hasR ? phi_final(phi, e, c + P, aR) : 0.0f;
+    const float pB = hasB ? phi_final(phi, e, c - 1, aB) : 0.0f;
+    const float pT = hasT ? phi_final(phi, e, c + 1, aT) : 0.0f;
     float u = U[c], v = V[c];
-    if (i >= 1 && j >= 1 && j <= g.NY - 2) {
-      bool actL = flag_active(flags[c - P]);
-      if (act || actL) u = u + (fbit(fl, F_FLUID) * phi_final(phi, e, c - P, actL) - fbit(fl, F_W) * pc);
-    }
-    if (j >= 1 && i >= 1 && i <= g.NX - 2) {
-      bool actB = flag_active(flags[c - 1]);
-      if (act || actB) v = v + (fbit(fl, F_FLUID) * phi_final(phi, e, c - 1, actB) - fbit(fl, F_S) * pc);
-    }
+    if (hasL && hasB && hasT && (act || aL)) u = u + (fbit(fl, F_FLUID) * pL - fbit(fl, F_W) * pc);
+    if (hasB && hasL && hasR && (act || aB)) v = v + (fbit(fl, F_FLUID) * pB - fbit(fl, F_S) * pc);
     p[c] = act ? cp * pc : 0.0f;
     if (act) {
-      float pw = phi_final(phi, e, c - P, flag_active(flags[c - P]));
-      float pe = phi_final(phi, e, c + P, flag_active(flags[c + P]));
-      float ps = phi_final(phi, e, c - 1, flag_active(flags[c - 1]));
-      float pn = phi_final(phi, e, c + 1, flag_active(flags[c + 1]));
-      FF r = resid_ff(rhs[c], pw, pe, ps, pn, (float)flag_count(fl), pc);
+      FF r = resid_ff(rhs[c], pL, pR, pB, pT, (float)flag_count(fl), pc);
       FF q = ff_sq(r.hi);
       q.lo = q.lo + 2.0f * r.hi * r.lo;
-      r2 = ff_add(r2, q);
-      rmx = fmaxf(rmx, fabsf(r.hi));
+      sums[1] = q;
+      maxs[1] = fabsf(r.hi);
     }
     if ((fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR)) {
       // Projected faces (i+1, j) and (i, j+1), as their own threads compute them.
-      uint8_t fR = flags[c + P];
-      bool actR = flag_active(fR);
       float uR = U[c + P];
-      if (act || actR) uR = uR + (fbit(fR, F_FLUID) * pc - fbit(fR, F_W) * phi_final(phi, e, c + P, actR));
-      uint8_t fT = flags[c + 1];
-      bool actT = flag_active(fT);
+      if (act || aR) uR = uR + (fbit(fR, F_FLUID) * pc - fbit(fR, F_W) * pR);
       float vT = V[c + 1];
-      if (act || actT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * phi_final(phi, e, c + 1, actT));
+      if (act || aT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * pT);
       float div = uR - u + vT - v;
-      s2 = ff_add(s2, ff_sq(div));
-      dmx = fmaxf(dmx, fabsf(div));
-      ++n;
+      sums[0] = ff_sq(div);
+      maxs[0] = fabsf(div);
+      fi = true;
       if (do_turb) {
         float2 nz = noise[c];
         float noiseU = nz.x * turbStrength;
@@ -609,18 +600,19 @@ __global__ void __launch_bounds__(256)
     Uo[c] = u;
     Vo[c] = v;
   }
-  double a = block_sum_ff(s2, red);
-  float b = block_max_f(dmx, redf);
-  double cn = block_sum_ff(FF{(float)n, 0.0f}, red);
-  double ra = block_sum_ff(r2, red);
-  float rb = block_max_f(rmx, redf);
+  double tot[5];
+  __shared__ double out5[5];
+  block_stats<2, 2>(sums, maxs, fi, sh, out5);
+  __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
+    // slots: div^2, r^2, max|div|, max|r|, count
     double* o = part + 5 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x);
-    o[0] = a;
-    o[1] = (double)b;
-    o[2] = cn;
-    o[3] = ra;
-    o[4] = (double)rb;
+    for (int k = 0; k < 5; ++k) tot[k] = out5[k];
+    o[0] = tot[0];
+    o[1] = tot[2];
+    o[2] = tot[4];
+    o[3] = tot[1];
+    o[4] = tot[3];
   }
 }
 
@@ -777,7 +769,7 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
       return e;
     mark(f, "outer correction");
   }
-  dim3 rg((f->NY + BX - 1) / BX, (f->NX + BY * GR - 1) / (BY * GR));
+  dim3 rg = cell_grid(f);
   int nb = rg.x * rg.y;
   count(f, 2);
   k_grad_fused<<<rg, bl, 0, f->stream>>>(
