@@ -345,7 +345,8 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
   if (cudaMalloc((void**)&f->noise, cells * sizeof(float2)) != cudaSuccess) return bail(FG_ERR_NOMEM);
   if (cudaMalloc((void**)&f->flags, cells) != cudaSuccess) return bail(FG_ERR_NOMEM);
   int nb = ((f->NY + 31) / 32) * ((f->NX + 7) / 8);
-  f->n_partials = 4 * nb + 64;
+  // Up to 5 partials per block, the combine levels and the scalar slots.
+  f->n_partials = 8 * nb + 256;
   if (cudaMalloc((void**)&f->partials, sizeof(double) * f->n_partials) != cudaSuccess)
     return bail(FG_ERR_NOMEM);
   if (cudaMalloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess) return bail(FG_ERR_NOMEM);

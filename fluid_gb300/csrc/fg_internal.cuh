@@ -248,6 +248,14 @@ inline dim3 reduce_grid(const fg_fluid* f) {
   return dim3(gx, gy);
 }
 
+// True when a reduction with `ns` partials per block over `nb` blocks, plus
+// its two-level combine, fits the partials buffer without reaching the
+// scalar result slots at its end.
+inline bool partials_fit(const fg_fluid* f, int ns, int nb) {
+  size_t need = (size_t)ns * nb + (size_t)ns * ((nb + 2047) / 2048) + (size_t)ns;
+  return need + 8 <= (size_t)f->n_partials;
+}
+
 // Records a stage-boundary event named `name` (profiling only).
 inline void mark(fg_fluid* f, const char* name) {
   if (!f->profile || f->n_marks >= fg_fluid::kMaxMarks) return;

@@ -276,6 +276,7 @@ cudaError_t launch_advect_smoke(fg_fluid* f, float dt) {
   float sd = smoke_diffusion(f, dt, &diffuse);
   count(f);
   dim3 gr = cell_grid(f);
+  if (!partials_fit(f, 1, gr.x * gr.y)) return cudaErrorInvalidValue;
   k_sl_smoke<<<gr, dim3(BX, BY), 0, f->stream>>>(
       f->d[FG_U], f->d[FG_V], f->d[FG_M], f->partner[FG_M], f->d[FG_NEWM], f->flags, dt,
       f->prm.smoke_advection, diffuse, sd, f->partials, f->g);
@@ -303,6 +304,7 @@ cudaError_t launch_advect_velocity_bfecc(fg_fluid* f, float dt) {
 
 cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt) {
   dim3 gr = cell_grid(f), bl(BX, BY);
+  if (!partials_fit(f, 1, gr.x * gr.y)) return cudaErrorInvalidValue;
   int diffuse;
   float sd = smoke_diffusion(f, dt, &diffuse);
   float sa = f->prm.smoke_advection;

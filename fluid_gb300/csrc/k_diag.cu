@@ -209,6 +209,7 @@ cudaError_t launch_clear_stats(fg_fluid* f) {
 cudaError_t launch_div_stats(fg_fluid* f) {
   dim3 gr = cell_grid(f);
   int nb = gr.x * gr.y;
+  if (!partials_fit(f, 3, nb)) return cudaErrorInvalidValue;
   count(f);
   k_div_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags,
                                                      f->partials, f->g);
@@ -222,6 +223,7 @@ cudaError_t launch_div_stats(fg_fluid* f) {
 cudaError_t launch_smoke_mass(fg_fluid* f) {
   dim3 gr = reduce_grid(f);
   int nb = gr.x * gr.y;
+  if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
   count(f);
   k_mass_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_M], f->partials, f->g);
   double* out = nullptr;
@@ -232,6 +234,7 @@ cudaError_t launch_smoke_mass(fg_fluid* f) {
 }
 
 cudaError_t launch_store_mass(fg_fluid* f, int nb) {
+  if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
   double* out = nullptr;
   count(f, combine_partials<1>(f->stream, f->partials, nb, 0u, &out));
   count(f);
@@ -242,6 +245,7 @@ cudaError_t launch_store_mass(fg_fluid* f, int nb) {
 cudaError_t launch_max_divergence(fg_fluid* f, float* dev_out) {
   dim3 gr = cell_grid(f);
   int nb = gr.x * gr.y;
+  if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
   count(f);
   k_maxdiv_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags,
                                                         f->partials, f->g);
@@ -255,6 +259,7 @@ cudaError_t launch_max_divergence(fg_fluid* f, float* dev_out) {
 cudaError_t launch_max_speed(fg_fluid* f, float* dev_out) {
   dim3 gr = cell_grid(f);
   int nb = gr.x * gr.y;
+  if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
   count(f);
   k_speed_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags,
                                                        f->partials, f->g);
@@ -268,6 +273,7 @@ cudaError_t launch_max_speed(fg_fluid* f, float* dev_out) {
 cudaError_t launch_view(fg_fluid* f, int kind, float* dev_minmax) {
   dim3 gr = cell_grid(f);
   int nb = gr.x * gr.y;
+  if (!partials_fit(f, 2, nb)) return cudaErrorInvalidValue;
   count(f);
   k_view<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags, f->view, kind,
                                              f->partials, f->g);
@@ -282,6 +288,7 @@ cudaError_t launch_view(fg_fluid* f, int kind, float* dev_minmax) {
 cudaError_t launch_field_minmax(fg_fluid* f, int field, float* dev_minmax) {
   dim3 gr = cell_grid(f);
   int nb = gr.x * gr.y;
+  if (!partials_fit(f, 2, nb)) return cudaErrorInvalidValue;
   count(f);
   k_minmax_partials<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[field], f->partials, f->g);
   double* out = f->partials + 2 * (size_t)nb;

@@ -639,6 +639,7 @@ __global__ void k_store_resid(const double* __restrict__ r, DevStats* st) {
 static cudaError_t resid_stats(fg_fluid* f, bool write_rhs_e) {
   dim3 gr = cell_grid(f);
   int nb = gr.x * gr.y;
+  if (!partials_fit(f, 2, nb)) return cudaErrorInvalidValue;
   count(f);
   k_resid64<<<gr, dim3(BX, BY), 0, f->stream>>>(
       f->phi, f->phi2, (PCtl*)f->pctl, f->rhs, f->wgt, f->flags,
@@ -771,6 +772,7 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   }
   dim3 rg = cell_grid(f);
   int nb = rg.x * rg.y;
+  if (!partials_fit(f, 5, nb)) return cudaErrorInvalidValue;
   count(f, 2);
   k_grad_fused<<<rg, bl, 0, f->stream>>>(
       f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,

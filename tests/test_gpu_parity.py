@@ -166,6 +166,34 @@ def test_jacobi_against_fp64_oracle(gpu):
     assert abs(g.stats()["div_l2_post"] - o.stats()["div_l2_post"]) <= 1e-5
 
 
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_app_size_bitwise(gpu, scheme):
+    """The reference app's grid (300 x 251, main/main.go:22-23) with BFECC,
+    the outer correction (parallel scheme) and the app's jet; large enough
+    for the multi-block reductions and several Jacobi tiles."""
+    params = dict(scheme=scheme, num_iters=24, UseBFECC=True, early_exit=scheme == 0)
+    if scheme == 1:
+        params.update(tb_depth=8, refine_sweeps=8)
+    g, o = both(gpu, 300, 251, density=1000.0, h=0.01, **params)
+    for f in (g, o):
+        scenes.apply_walls(f, top=True, bottom=True, left=True, right=False)
+    for _ in range(4):
+        for f in (g, o):
+            n = f.NumY
+            for j in range(f.NumY // 2 - 50, f.NumY // 2 + 50):
+                f.SetVelocity(1, j, 4.0, 0.0)
+                f.AddSmoke(1, j, 1.0)
+            f.Simulate(1.0 / 120.0)
+    assert_bitwise(g, o)
+    sg, so = g.stats(), o.stats()
+    for k in ("div_l2_post", "div_max_post", "smoke_mass"):
+        assert sg[k] == pytest.approx(so[k], rel=1e-9, abs=1e-12), k
+    assert sg["div_count_post"] == so["div_count_post"]
+    if scheme == 1:
+        assert sg["resid_l2"] == pytest.approx(so["resid_l2"], rel=1e-9, abs=1e-12)
+        assert sg["resid_max"] == pytest.approx(so["resid_max"], rel=1e-9, abs=1e-12)
+
+
 # ------------------------------------------------------------------ API behaviour
 def test_graphs_do_not_change_results(gpu):
     a = gpu.Fluid(1.0, 40, 30, 1.0, use_graphs=True, UseBFECC=True, num_iters=20)
