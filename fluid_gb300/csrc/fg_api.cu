@@ -345,9 +345,10 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
   if (cudaMalloc((void**)&f->noise, cells * sizeof(float2)) != cudaSuccess) return bail(FG_ERR_NOMEM);
   if (cudaMalloc((void**)&f->flags, cells) != cudaSuccess) return bail(FG_ERR_NOMEM);
   int nb = ((f->NY + 31) / 32) * ((f->NX + 7) / 8);
-  // Up to 5 partials per block, the combine levels and the scalar slots.
-  f->n_partials = 8 * nb + 256;
-  if (cudaMalloc((void**)&f->partials, sizeof(double) * f->n_partials) != cudaSuccess)
+  // Rows of up to 5 float-pair slots per block, the combine levels and the
+  // scalar result slots at the end.
+  f->n_partials = 16 * nb + 512;
+  if (cudaMalloc((void**)&f->partials, sizeof(float) * f->n_partials) != cudaSuccess)
     return bail(FG_ERR_NOMEM);
   if (cudaMalloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess) return bail(FG_ERR_NOMEM);
   f->n_slots = kSlots;
@@ -840,8 +841,8 @@ static int read_scalars(fg_fluid* f, int n) {
 
 static float* dev_scalar_slot(fg_fluid* f) {
   // The last 8 floats of the partials buffer hold small device results; the
-  // reductions never use them (they need at most 4*nb + 4 doubles).
-  return (float*)f->partials + 2 * (size_t)f->n_partials - 8;
+  // reductions never reach them (partials_fit).
+  return f->partials + (size_t)f->n_partials - 8;
 }
 
 int fg_max_divergence(fg_fluid* f, float* out) {

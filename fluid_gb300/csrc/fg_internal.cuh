@@ -146,8 +146,8 @@ struct fg_fluid {
   float* view = nullptr;       // output of the vorticity / magnitude views
   float2* noise = nullptr;     // per-cell float32(sin(seed)) pairs for addTurbulence
   uint8_t* flags = nullptr;    // per-cell flag byte
-  double* partials = nullptr;  // block partials of the reductions
-  int n_partials = 0;
+  float* partials = nullptr;   // block partial rows of the reductions (float pairs)
+  int n_partials = 0;          // floats
   fg::DevStats* dstats = nullptr;
   void* pctl = nullptr;   // control block of the main Jacobi solve (k_pressure.cu PCtl)
   void* ectl = nullptr;   // control block of the FP64-residual correction solve
@@ -252,8 +252,8 @@ inline dim3 reduce_grid(const fg_fluid* f) {
 // its two-level combine, fits the partials buffer without reaching the
 // scalar result slots at its end.
 inline bool partials_fit(const fg_fluid* f, int ns, int nb) {
-  size_t need = (size_t)ns * nb + (size_t)ns * ((nb + 2047) / 2048) + (size_t)ns;
-  return need + 8 <= (size_t)f->n_partials;
+  size_t rows = (size_t)nb + (size_t)((nb + 2047) / 2048) + 1;
+  return 2 * (size_t)ns * rows + 8 <= (size_t)f->n_partials;
 }
 
 // Records a stage-boundary event named `name` (profiling only).

@@ -1,93 +1,23 @@
-// Deterministic block reductions: every block writes its partials to fixed
-// slots; a single-block pass combines the slots in a fixed tree order, so the
-// result does not depend on scheduling or on atomics.
+// Deterministic reductions in double-float arithmetic.
+//
+// This part retires only two FP64 operations per cycle per SM (1/64 of its
+// FP32 rate), so a single double operation per warp per block already
+// dominates a bandwidth-bound reduction pass.  The statistics are therefore
+// accumulated as unevaluated pairs of floats ("double-float", about 48
+// significant bits) with error-free transformations -- Knuth's TwoSum and
+// the exact product error by fma -- at every level: per thread, warp, block
+// and across blocks.  Only the final totals are converted to IEEE FP64.
+// Every block writes its partial row to a fixed slot and the rows are
+// combined in a fixed tree order, so results do not depend on scheduling.
+//
+// A partial row holds NS slots of two floats.  A slot is either a sum (hi,
+// lo) or a maximum (hi; lo unused), chosen by bit s of `max_mask`.
 #pragma once
 
-#include <cfloat>
+#include <math.h>
 
 #include "fg_internal.cuh"
 
-namespace fg {
-namespace {
-
-// Sum (MAX = false) or max (MAX = true) of one double per thread over the
-// block; the result is valid in thread 0.  The block size must be a
-// multiple of 32 and at most 1024; sh holds 32 doubles.
-template <bool MAX>
-__device__ __forceinline__ double block_reduce(double v, double* sh) {
-  int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  int nt = blockDim.x * blockDim.y;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    double w = __shfl_down_sync(0xffffffffu, v, o);
-    v = MAX ? fmax(v, w) : v + w;
-  }
-  __syncthreads();  // sh may still be read by a previous reduction
-  if ((tid & 31) == 0) sh[tid >> 5] = v;
-  __syncthreads();
-  if (tid < 32) {
-    v = tid < (nt >> 5) ? sh[tid] : (MAX ? -DBL_MAX : 0.0);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      double w = __shfl_down_sync(0xffffffffu, v, o);
-      v = MAX ? fmax(v, w) : v + w;
-    }
-  }
-  return v;
-}
-
-// Combines rows [b*per, min(n, (b+1)*per)) of NS partials (partials[k*NS +
-// s]) into out[b*NS + s], one block b of 1024 threads per output row; bit s
-// of max_mask selects max instead of sum for slot s.
-template <int NS>
-__global__ void k_combine(const double* __restrict__ partials, int n, int per, unsigned max_mask,
-                          double* __restrict__ out) {
-  __shared__ double sh[32];
-  int k0 = blockIdx.x * per;
-  int k1 = min(n, k0 + per);
-  for (int s = 0; s < NS; ++s) {
-    bool mx = (max_mask >> s) & 1u;
-    double v = 0.0;
-    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-      double w = partials[(size_t)k * NS + s];
-      v = mx ? fmax(v, w) : v + w;
-    }
-    v = mx ? block_reduce<true>(v, sh) : block_reduce<false>(v, sh);
-    if (threadIdx.x == 0) out[(size_t)blockIdx.x * NS + s] = v;
-  }
-}
-
-// Deterministic two-level combine of n rows of NS partials starting at
-// `part`; the result (NS doubles) is written at *out_ptr, which points past
-// the level-one rows inside the same buffer.  Returns the number of kernels.
-template <int NS>
-inline int combine_partials(cudaStream_t st, double* part, int n, unsigned max_mask,
-                            double** out_ptr) {
-  double* lvl = part + (size_t)NS * n;
-  const int per = 2048;
-  if (n <= per) {
-    k_combine<NS><<<1, 1024, 0, st>>>(part, n, n, max_mask, lvl);
-    *out_ptr = lvl;
-    return 1;
-  }
-  int g = (n + per - 1) / per;
-  k_combine<NS><<<g, 1024, 0, st>>>(part, n, per, max_mask, lvl);
-  double* out = lvl + (size_t)NS * g;
-  k_combine<NS><<<1, 1024, 0, st>>>(lvl, g, g, max_mask, out);
-  *out_ptr = out;
-  return 2;
-}
-
-}  // namespace
-}  // namespace fg
-
-// ---------------------------------------------------------------------------
-// Double-float ("float-float") accumulation.  This part's FP64 rate is about
-// 1/64 of its FP32 rate, so the per-cell and intra-block work of the FP64
-// reductions uses error-free FP32 transformations (Knuth's TwoSum, the exact
-// product error by fma), which carry about 48 significant bits; block totals
-// are converted exactly to double and combined across blocks in IEEE FP64.
-// ---------------------------------------------------------------------------
 namespace fg {
 namespace {
 
@@ -111,11 +41,13 @@ __host__ __device__ __forceinline__ FF ff_add(FF a, FF b) {
   return FF{h, l};
 }
 
+#ifdef __CUDACC__
 // x*x as an unevaluated float pair (exact).
 __device__ __forceinline__ FF ff_sq(float x) {
   float p = x * x;
   return FF{p, __fmaf_rn(x, x, -p)};
 }
+#endif
 
 // Residual b + (pw + pe + ps + pn) - s*x of FP32 inputs as a normalised float
 // pair (hi = the residual rounded to float): the product s*x is split
@@ -139,81 +71,124 @@ __host__ __device__ __forceinline__ FF resid_ff(float b, float pw, float pe, flo
   return FF{t, e};
 }
 
-// Warp-level reduction of NS float-pair sums, NM float maxima and a count
-// of predicates, then one block-level combine in double: the block's totals
-// land in out[0..NS+NM] (sums, maxima, count) written by thread 0.  The tree
-// adds pairs with one TwoSum per level and renormalises at the end.  sh
-// holds 8 * (NS + NM + 1) doubles (blocks of up to 256 threads).
-template <int NS, int NM>
-__device__ __forceinline__ void block_stats(FF (&s)[NS], float (&m)[NM], bool pred, double* sh,
-                                            double* out) {
-  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  const int lane = tid & 31, wid = tid >> 5, nw = (blockDim.x * blockDim.y) >> 5;
-  const int cnt = __popc(__ballot_sync(0xffffffffu, pred));
+#ifdef __CUDACC__
+// Combines slot values of two threads / rows.
+template <int NS>
+__device__ __forceinline__ void slots_merge(FF (&a)[NS], const FF (&b)[NS], unsigned max_mask) {
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    if ((max_mask >> s) & 1u) {
+      a[s].hi = fmaxf(a[s].hi, b[s].hi);
+    } else {
+      float t, e;
+      two_sum(a[s].hi, b[s].hi, t, e);
+      a[s].hi = t;
+      a[s].lo = (a[s].lo + b[s].lo) + e;
+    }
+  }
+}
+
+template <int NS>
+__device__ __forceinline__ void slots_identity(FF (&a)[NS], unsigned max_mask) {
+#pragma unroll
+  for (int s = 0; s < NS; ++s) a[s] = FF{((max_mask >> s) & 1u) ? -INFINITY : 0.0f, 0.0f};
+}
+
+template <int NS>
+__device__ __forceinline__ void warp_merge(FF (&v)[NS], unsigned max_mask) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
+    FF w[NS];
 #pragma unroll
-    for (int k = 0; k < NS; ++k) {
-      float bh = __shfl_down_sync(0xffffffffu, s[k].hi, o);
-      float bl = __shfl_down_sync(0xffffffffu, s[k].lo, o);
-      float t, e;
-      two_sum(s[k].hi, bh, t, e);
-      s[k].hi = t;
-      s[k].lo = (s[k].lo + bl) + e;
+    for (int s = 0; s < NS; ++s) {
+      w[s].hi = __shfl_down_sync(0xffffffffu, v[s].hi, o);
+      w[s].lo = __shfl_down_sync(0xffffffffu, v[s].lo, o);
     }
-#pragma unroll
-    for (int k = 0; k < NM; ++k) m[k] = fmaxf(m[k], __shfl_down_sync(0xffffffffu, m[k], o));
+    slots_merge<NS>(v, w, max_mask);
   }
-  constexpr int R = NS + NM + 1;
+}
+
+// Reduces the per-thread slot values over the block (at most 32 warps) and
+// writes the block's row (NS x {hi, lo}) from thread 0.  sh holds 64 * NS
+// floats.  Every thread of the block must call it.
+template <int NS>
+__device__ __forceinline__ void block_row(FF (&v)[NS], unsigned max_mask, float* sh, float* row) {
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = (blockDim.x * blockDim.y + 31) >> 5;
+  warp_merge<NS>(v, max_mask);
   if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < NS; ++k) sh[wid * R + k] = (double)s[k].hi + (double)s[k].lo;
-#pragma unroll
-    for (int k = 0; k < NM; ++k) sh[wid * R + NS + k] = (double)m[k];
-    sh[wid * R + NS + NM] = (double)cnt;
+    for (int s = 0; s < NS; ++s) {
+      sh[(wid * NS + s) * 2] = v[s].hi;
+      sh[(wid * NS + s) * 2 + 1] = v[s].lo;
+    }
   }
   __syncthreads();
-  if (tid < R) {
-    double v = 0.0;
-    bool mx = tid >= NS && tid < NS + NM;
-    for (int w = 0; w < nw; ++w) v = mx ? fmax(v, sh[w * R + tid]) : v + sh[w * R + tid];
-    out[tid] = v;
+  if (wid == 0) {
+    FF u[NS];
+    if (lane < nw) {
+#pragma unroll
+      for (int s = 0; s < NS; ++s) u[s] = FF{sh[(lane * NS + s) * 2], sh[(lane * NS + s) * 2 + 1]};
+    } else {
+      slots_identity<NS>(u, max_mask);
+    }
+    warp_merge<NS>(u, max_mask);
+    if (lane == 0) {
+#pragma unroll
+      for (int s = 0; s < NS; ++s) {
+        float h = u[s].hi, l = u[s].lo;
+        if (!((max_mask >> s) & 1u)) two_sum(u[s].hi, u[s].lo, h, l);
+        row[2 * s] = h;
+        row[2 * s + 1] = l;
+      }
+    }
   }
 }
 
-// Sum of a float pair per thread over the block, as a double in thread 0.
-// Warp level in float-float, block level in double.  sh: 32 doubles.
-__device__ __forceinline__ double block_sum_ff(FF v, double* sh) {
-  int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  int nt = blockDim.x * blockDim.y;
+// Combines rows [b*per, min(n, (b+1)*per)) of `in` into row b of `out`.
+template <int NS>
+__global__ void __launch_bounds__(1024)
+    k_combine_rows(const float* __restrict__ in, int n, int per, unsigned max_mask,
+                   float* __restrict__ out) {
+  __shared__ float sh[64 * NS];
+  FF v[NS];
+  slots_identity<NS>(v, max_mask);
+  int k1 = min(n, (int)blockIdx.x * per + per);
+  for (int k = blockIdx.x * per + threadIdx.x; k < k1; k += blockDim.x) {
+    FF w[NS];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    FF w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
-    v = ff_add(v, w);
+    for (int s = 0; s < NS; ++s)
+      w[s] = FF{in[(size_t)k * 2 * NS + 2 * s], in[(size_t)k * 2 * NS + 2 * s + 1]};
+    slots_merge<NS>(v, w, max_mask);
   }
-  __syncthreads();
-  if ((tid & 31) == 0) sh[tid >> 5] = (double)v.hi + (double)v.lo;
-  __syncthreads();
-  double r = 0.0;
-  if (tid == 0)
-    for (int k = 0; k < (nt >> 5); ++k) r += sh[k];
-  return r;
+  block_row<NS>(v, max_mask, sh, out + (size_t)blockIdx.x * 2 * NS);
 }
 
-// Max of a non-negative float per thread over the block (thread 0).
-__device__ __forceinline__ float block_max_f(float v, float* sh) {
-  int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  int nt = blockDim.x * blockDim.y;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
-  __syncthreads();
-  if ((tid & 31) == 0) sh[tid >> 5] = v;
-  __syncthreads();
-  float r = 0.0f;
-  if (tid == 0)
-    for (int k = 0; k < (nt >> 5); ++k) r = fmaxf(r, sh[k]);
-  return r;
+// Two-level combine of n rows at `part`; the final row is written past the
+// level-one rows in the same buffer and returned in *out_row.  Returns the
+// number of kernels launched.
+template <int NS>
+inline int combine_rows(cudaStream_t st, float* part, int n, unsigned max_mask, float** out_row) {
+  float* lvl = part + (size_t)2 * NS * n;
+  const int per = 2048;
+  if (n <= per) {
+    k_combine_rows<NS><<<1, 1024, 0, st>>>(part, n, n, max_mask, lvl);
+    *out_row = lvl;
+    return 1;
+  }
+  int g = (n + per - 1) / per;
+  k_combine_rows<NS><<<g, 1024, 0, st>>>(part, n, per, max_mask, lvl);
+  float* out = lvl + (size_t)2 * NS * g;
+  k_combine_rows<NS><<<1, 1024, 0, st>>>(lvl, g, g, max_mask, out);
+  *out_row = out;
+  return 2;
 }
+
+// Total of a sum slot of a final row, in FP64.
+__device__ __forceinline__ double row_sum(const float* row, int s) {
+  return (double)row[2 * s] + (double)row[2 * s + 1];
+}
+#endif
 
 }  // namespace
 }  // namespace fg

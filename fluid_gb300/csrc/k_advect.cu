@@ -172,9 +172,9 @@ __device__ __forceinline__ float smoke_value(const float* __restrict__ Ut,
 __global__ void k_sl_smoke(const float* __restrict__ Ut, const float* __restrict__ Vt,
                            const float* __restrict__ Ms, float* __restrict__ Mo, float* nM,
                            const uint8_t* __restrict__ flags, float dt, float smokeAdv,
-                           int diffuse, float smokeDiffusion, double* __restrict__ mass_part,
+                           int diffuse, float smokeDiffusion, float* __restrict__ mass_part,
                            Grid g) {
-  __shared__ double red[32];
+  __shared__ float sh[64];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   FF mass{0.0f, 0.0f};
@@ -199,8 +199,8 @@ __global__ void k_sl_smoke(const float* __restrict__ Ut, const float* __restrict
   // Smoke mass of the result over interior cells (float pairs within the
   // block, FP64 across blocks).
   if (mass_part) {
-    double a = block_sum_ff(mass, red);
-    if (threadIdx.x == 0 && threadIdx.y == 0) mass_part[blockIdx.y * gridDim.x + blockIdx.x] = a;
+    FF v[1] = {mass};
+    block_row<1>(v, 0u, sh, mass_part + 2 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x));
   }
 }
 

@@ -433,49 +433,6 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   }
 }
 
-// Residual r = b - A phi of the current iterate, per cell as an exact-to-
-// ~48-bit float pair (resid_ff), with block partials (sum r^2 accumulated in
-// float pairs within the block and in FP64 across blocks, max |r|).  When
-// `rhs_e` is given it also writes the correction right-hand side
-// b_e = (float) r and bw_e = w * b_e.
-__global__ void k_resid64(const float* __restrict__ phi0, const float* __restrict__ phi1,
-                          const PCtl* __restrict__ ctl, const float* __restrict__ rhs,
-                          const float* __restrict__ W, const uint8_t* __restrict__ flags,
-                          float* __restrict__ rhs_e, float* __restrict__ bwe,
-                          double* __restrict__ partials, Grid g) {
-  __shared__ double red[32];
-  __shared__ float redf[32];
-  const float* phi = ctl->sel ? phi1 : phi0;
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  FF sq{0.0f, 0.0f};
-  float ra = 0.0f;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (j < g.NY && i < g.NX) {
-    int c = i * g.P + j;
-    uint8_t fl = flags[c];
-    float re = 0.0f;
-    if (flag_active(fl)) {
-      FF r = resid_ff(rhs[c], phi[c - g.P], phi[c + g.P], phi[c - 1], phi[c + 1],
-                      (float)flag_count(fl), phi[c]);
-      re = r.hi;
-      sq = ff_sq(r.hi);
-      sq.lo = sq.lo + 2.0f * r.hi * r.lo;
-      ra = fabsf(r.hi);
-    }
-    if (rhs_e) {
-      rhs_e[c] = re;
-      bwe[c] = W[c] * re;
-    }
-  }
-  double s = block_sum_ff(sq, red);
-  float m = block_max_f(ra, redf);
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    int b = blockIdx.y * gridDim.x + blockIdx.x;
-    partials[2 * b] = s;
-    partials[2 * b + 1] = (double)m;
-  }
-}
-
 // Final potential at cell c: the main iterate, plus the outer correction on
 // active cells when one ran (phi = phi + e, fluid.go's p accumulation aside).
 __device__ __forceinline__ float phi_final(const float* __restrict__ phi,
@@ -540,8 +497,7 @@ __global__ void __launch_bounds__(256)
                  const float* __restrict__ e1, const PCtl* __restrict__ ectl,
                  const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float cp,
                  const float2* __restrict__ noise, float turbStrength, int do_turb,
-                 double* __restrict__ part, Grid g) {
-  __shared__ double sh[8 * 5];
+                 float* __restrict__ part, Grid g) {
   const float* phi = ctl->sel ? phi1 : phi0;
   const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
   const int P = g.P;
@@ -600,28 +556,18 @@ __global__ void __launch_bounds__(256)
     Uo[c] = u;
     Vo[c] = v;
   }
-  double tot[5];
-  __shared__ double out5[5];
-  block_stats<2, 2>(sums, maxs, fi, sh, out5);
-  __syncthreads();
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    // slots: div^2, r^2, max|div|, max|r|, count
-    double* o = part + 5 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x);
-    for (int k = 0; k < 5; ++k) tot[k] = out5[k];
-    o[0] = tot[0];
-    o[1] = tot[2];
-    o[2] = tot[4];
-    o[3] = tot[1];
-    o[4] = tot[3];
-  }
+  // Row slots: sum div^2, max |div|, fluid cells, sum r^2, max |r|.
+  __shared__ float shr[64 * 5];
+  FF row[5] = {sums[0], {maxs[0], 0.0f}, {fi ? 1.0f : 0.0f, 0.0f}, sums[1], {maxs[1], 0.0f}};
+  block_row<5>(row, 0x12u, shr, part + 10 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x));
 }
 
-__global__ void k_store_div_p(const double* __restrict__ r, DevStats* st) {
-  st->div_l2_sq = r[0];
-  st->div_max = r[1];
-  st->div_count = r[2];
-  st->resid_l2_sq = r[3];
-  st->resid_max = r[4];
+__global__ void k_store_div_p(const float* __restrict__ r, DevStats* st) {
+  st->div_l2_sq = row_sum(r, 0);
+  st->div_max = (double)r[2];
+  st->div_count = row_sum(r, 2);
+  st->resid_l2_sq = row_sum(r, 3);
+  st->resid_max = (double)r[8];
 }
 
 __global__ void k_finish_parallel(const PCtl* __restrict__ ctl, DevStats* st) {
@@ -629,27 +575,8 @@ __global__ void k_finish_parallel(const PCtl* __restrict__ ctl, DevStats* st) {
   st->last_maxdiv = (double)__uint_as_float(ctl->slots[ctl->last_launch]);
 }
 
-__global__ void k_store_resid(const double* __restrict__ r, DevStats* st) {
-  st->resid_l2_sq = r[0];
-  st->resid_max = r[1];
-}
 
 }  // namespace
-
-static cudaError_t resid_stats(fg_fluid* f, bool write_rhs_e) {
-  dim3 gr = cell_grid(f);
-  int nb = gr.x * gr.y;
-  if (!partials_fit(f, 2, nb)) return cudaErrorInvalidValue;
-  count(f);
-  k_resid64<<<gr, dim3(BX, BY), 0, f->stream>>>(
-      f->phi, f->phi2, (PCtl*)f->pctl, f->rhs, f->wgt, f->flags,
-      write_rhs_e ? f->rhs_e : nullptr, f->bwe, f->partials, f->g);
-  double* out = nullptr;
-  count(f, combine_partials<2>(f->stream, f->partials, nb, 2u, &out));
-  count(f);
-  k_store_resid<<<1, 1, 0, f->stream>>>(out, f->dstats);
-  return cudaGetLastError();
-}
 
 size_t pctl_bytes(int n_slots) { return sizeof(PCtl) + sizeof(unsigned) * (size_t)n_slots; }
 
@@ -780,8 +707,8 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
       f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
-  double* out = nullptr;
-  count(f, combine_partials<5>(f->stream, f->partials, nb, 0x12u, &out));
+  float* out = nullptr;
+  count(f, combine_rows<5>(f->stream, f->partials, nb, 0x12u, &out));
   k_store_div_p<<<1, 1, 0, f->stream>>>(out, f->dstats);
   return cudaGetLastError();
 }
