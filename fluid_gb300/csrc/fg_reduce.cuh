@@ -11,7 +11,9 @@
 // combined in a fixed tree order, so results do not depend on scheduling.
 //
 // A partial row holds NS slots of two floats.  A slot is either a sum (hi,
-// lo) or a maximum (hi; lo unused), chosen by bit s of `max_mask`.
+// lo) or a maximum (hi; lo unused), chosen by bit s of `max_mask`; a sum
+// whose bit is set in `exact_mask` holds small integers (cell counts) that
+// float addition sums exactly, so it skips the error term.
 #pragma once
 
 #include <math.h>
@@ -73,12 +75,14 @@ __host__ __device__ __forceinline__ FF resid_ff(float b, float pw, float pe, flo
 
 #ifdef __CUDACC__
 // Combines slot values of two threads / rows.
-template <int NS>
+template <int NS, unsigned EXACT = 0u>
 __device__ __forceinline__ void slots_merge(FF (&a)[NS], const FF (&b)[NS], unsigned max_mask) {
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
     if ((max_mask >> s) & 1u) {
       a[s].hi = fmaxf(a[s].hi, b[s].hi);
+    } else if ((EXACT >> s) & 1u) {
+      a[s].hi = a[s].hi + b[s].hi;
     } else {
       float t, e;
       two_sum(a[s].hi, b[s].hi, t, e);
@@ -94,7 +98,7 @@ __device__ __forceinline__ void slots_identity(FF (&a)[NS], unsigned max_mask) {
   for (int s = 0; s < NS; ++s) a[s] = FF{((max_mask >> s) & 1u) ? -INFINITY : 0.0f, 0.0f};
 }
 
-template <int NS>
+template <int NS, unsigned EXACT = 0u>
 __device__ __forceinline__ void warp_merge(FF (&v)[NS], unsigned max_mask) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -102,20 +106,21 @@ __device__ __forceinline__ void warp_merge(FF (&v)[NS], unsigned max_mask) {
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
       w[s].hi = __shfl_down_sync(0xffffffffu, v[s].hi, o);
-      w[s].lo = __shfl_down_sync(0xffffffffu, v[s].lo, o);
+      // Maxima and exact sums carry no error term.
+      w[s].lo = ((max_mask | EXACT) >> s) & 1u ? 0.0f : __shfl_down_sync(0xffffffffu, v[s].lo, o);
     }
-    slots_merge<NS>(v, w, max_mask);
+    slots_merge<NS, EXACT>(v, w, max_mask);
   }
 }
 
 // Reduces the per-thread slot values over the block (at most 32 warps) and
 // writes the block's row (NS x {hi, lo}) from thread 0.  sh holds 64 * NS
 // floats.  Every thread of the block must call it.
-template <int NS>
+template <int NS, unsigned EXACT = 0u>
 __device__ __forceinline__ void block_row(FF (&v)[NS], unsigned max_mask, float* sh, float* row) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
   const int lane = tid & 31, wid = tid >> 5, nw = (blockDim.x * blockDim.y + 31) >> 5;
-  warp_merge<NS>(v, max_mask);
+  warp_merge<NS, EXACT>(v, max_mask);
   if (lane == 0) {
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
@@ -132,7 +137,7 @@ __device__ __forceinline__ void block_row(FF (&v)[NS], unsigned max_mask, float*
     } else {
       slots_identity<NS>(u, max_mask);
     }
-    warp_merge<NS>(u, max_mask);
+    warp_merge<NS, EXACT>(u, max_mask);
     if (lane == 0) {
 #pragma unroll
       for (int s = 0; s < NS; ++s) {

@@ -482,13 +482,79 @@ __global__ void k_grad(float* __restrict__ U, float* __restrict__ V, float* __re
 
 // Gradient subtract for the parallel scheme, fused with what follows it in
 // the step: the post-projection divergence statistics (sum div^2 in float
-// pairs within the block and FP64 across blocks, max |div|, fluid cell
-// count), the residual statistics of the final potential (resid_ff per
-// cell, sum r^2 and max |r| likewise) and, when confinement is off,
-// addTurbulence (fluid.go:496-526), which only touches a cell's own U, V.
-// Reads U, V and writes the rotated buffers Uo, Vo, so the divergence can
-// recompute a neighbour's projected face from its original value.  One cell
-// per thread; every neighbour value is loaded once.
+// pairs, max |div|, fluid cell count), the residual statistics of the final
+// potential (resid_ff per cell, sum r^2 and max |r|) and, when confinement
+// is off, addTurbulence (fluid.go:496-526), which only touches a cell's own
+// U, V.  Reads U, V and writes the rotated buffers Uo, Vo, so the divergence
+// can recompute a neighbour's projected face from its original value.  A
+// thread handles GR cells of one column (rows i, i+8, ...); every neighbour
+// value is loaded once per cell.
+constexpr int GR = 4;
+struct GradAcc {
+  FF d2, r2;
+  float dmax, rmax, n;
+};
+
+__device__ __forceinline__ void grad_cell(int i, int j, const float* __restrict__ U,
+                                          const float* __restrict__ V, float* __restrict__ Uo,
+                                          float* __restrict__ Vo, float* __restrict__ p,
+                                          const float* __restrict__ phi,
+                                          const float* __restrict__ e,
+                                          const float* __restrict__ rhs,
+                                          const uint8_t* __restrict__ flags, float cp,
+                                          const float2* __restrict__ noise, float turbStrength,
+                                          int do_turb, const Grid& g, GradAcc& acc) {
+  const int P = g.P;
+  const int c = i * P + j;
+  const bool hasL = i >= 1, hasR = i <= g.NX - 2, hasB = j >= 1, hasT = j <= g.NY - 2;
+  const uint8_t fl = flags[c];
+  const uint8_t fL = hasL ? flags[c - P] : 0, fR = hasR ? flags[c + P] : 0;
+  const uint8_t fB = hasB ? flags[c - 1] : 0, fT = hasT ? flags[c + 1] : 0;
+  const bool act = flag_active(fl), aL = flag_active(fL), aR = flag_active(fR);
+  const bool aB = flag_active(fB), aT = flag_active(fT);
+  // phi is 0 off the active cells; the correction is added on active ones.
+  const float pc = phi_final(phi, e, c, act);
+  const float pL = hasL ? phi_final(phi, e, c - P, aL) : 0.0f;
+  const float pR = hasR ? phi_final(phi, e, c + P, aR) : 0.0f;
+  const float pB = hasB ? phi_final(phi, e, c - 1, aB) : 0.0f;
+  const float pT = hasT ? phi_final(phi, e, c + 1, aT) : 0.0f;
+  float u = U[c], v = V[c];
+  if (hasL && hasB && hasT && (act || aL)) u = u + (fbit(fl, F_FLUID) * pL - fbit(fl, F_W) * pc);
+  if (hasB && hasL && hasR && (act || aB)) v = v + (fbit(fl, F_FLUID) * pB - fbit(fl, F_S) * pc);
+  p[c] = act ? cp * pc : 0.0f;
+  if (act) {
+    FF r = resid_ff(rhs[c], pL, pR, pB, pT, (float)flag_count(fl), pc);
+    FF q = ff_sq(r.hi);
+    q.lo = q.lo + 2.0f * r.hi * r.lo;
+    acc.r2 = ff_add(acc.r2, q);
+    acc.rmax = fmaxf(acc.rmax, fabsf(r.hi));
+  }
+  if ((fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR)) {
+    // Projected faces (i+1, j) and (i, j+1), as their own threads compute them.
+    float uR = U[c + P];
+    if (act || aR) uR = uR + (fbit(fR, F_FLUID) * pc - fbit(fR, F_W) * pR);
+    float vT = V[c + 1];
+    if (act || aT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * pT);
+    float div = uR - u + vT - v;
+    acc.d2 = ff_add(acc.d2, ff_sq(div));
+    acc.dmax = fmaxf(acc.dmax, fabsf(div));
+    acc.n = acc.n + 1.0f;
+    if (do_turb) {
+      float2 nz = noise[c];
+      float noiseU = nz.x * turbStrength;
+      float noiseV = nz.y * turbStrength;
+      float localVel = sqrtf(u * u + v * v);
+      if (localVel > 0.1f) {
+        float turbulenceFactor = go_min(localVel * 0.5f, 1.0f);
+        u += noiseU * turbulenceFactor;
+        v += noiseV * turbulenceFactor;
+      }
+    }
+  }
+  Uo[c] = u;
+  Vo[c] = v;
+}
+
 __global__ void __launch_bounds__(256)
     k_grad_fused(const float* __restrict__ U, const float* __restrict__ V,
                  float* __restrict__ Uo, float* __restrict__ Vo, float* __restrict__ p,
@@ -498,68 +564,23 @@ __global__ void __launch_bounds__(256)
                  const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float cp,
                  const float2* __restrict__ noise, float turbStrength, int do_turb,
                  float* __restrict__ part, Grid g) {
+  __shared__ float shr[64 * 5];
   const float* phi = ctl->sel ? phi1 : phi0;
   const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
-  const int P = g.P;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  FF sums[2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};  // div^2, r^2
-  float maxs[2] = {0.0f, 0.0f};                // |div|, |r|
-  bool fi = false;
-  if (j < g.NY && i < g.NX) {
-    const int c = i * P + j;
-    const bool hasL = i >= 1, hasR = i <= g.NX - 2, hasB = j >= 1, hasT = j <= g.NY - 2;
-    const uint8_t fl = flags[c];
-    const uint8_t fL = hasL ? flags[c - P] : 0, fR = hasR ? flags[c + P] : 0;
-    const uint8_t fB = hasB ? flags[c - 1] : 0, fT = hasT ? flags[c + 1] : 0;
-    const bool act = flag_active(fl), aL = flag_active(fL), aR = flag_active(fR);
-    const bool aB = flag_active(fB), aT = flag_active(fT);
-    // phi is 0 off the active cells; the correction is added on active ones.
-    const float pc = phi_final(phi, e, c, act);
-    const float pL = hasL ? phi_final(phi, e, c - P, aL) : 0.0f;
-    const float pR = hasR ? phi_final(phi, e, c + P, aR) : 0.0f;
-    const float pB = hasB ? phi_final(phi, e, c - 1, aB) : 0.0f;
-    const float pT = hasT ? phi_final(phi, e, c + 1, aT) : 0.0f;
-    float u = U[c], v = V[c];
-    if (hasL && hasB && hasT && (act || aL)) u = u + (fbit(fl, F_FLUID) * pL - fbit(fl, F_W) * pc);
-    if (hasB && hasL && hasR && (act || aB)) v = v + (fbit(fl, F_FLUID) * pB - fbit(fl, F_S) * pc);
-    p[c] = act ? cp * pc : 0.0f;
-    if (act) {
-      FF r = resid_ff(rhs[c], pL, pR, pB, pT, (float)flag_count(fl), pc);
-      FF q = ff_sq(r.hi);
-      q.lo = q.lo + 2.0f * r.hi * r.lo;
-      sums[1] = q;
-      maxs[1] = fabsf(r.hi);
+  GradAcc acc{{0.0f, 0.0f}, {0.0f, 0.0f}, 0.0f, 0.0f, 0.0f};
+  if (j < g.NY) {
+#pragma unroll
+    for (int k = 0; k < GR; ++k) {
+      const int i = (blockIdx.y * GR + k) * blockDim.y + threadIdx.y;
+      if (i < g.NX)
+        grad_cell(i, j, U, V, Uo, Vo, p, phi, e, rhs, flags, cp, noise, turbStrength, do_turb, g,
+                  acc);
     }
-    if ((fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR)) {
-      // Projected faces (i+1, j) and (i, j+1), as their own threads compute them.
-      float uR = U[c + P];
-      if (act || aR) uR = uR + (fbit(fR, F_FLUID) * pc - fbit(fR, F_W) * pR);
-      float vT = V[c + 1];
-      if (act || aT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * pT);
-      float div = uR - u + vT - v;
-      sums[0] = ff_sq(div);
-      maxs[0] = fabsf(div);
-      fi = true;
-      if (do_turb) {
-        float2 nz = noise[c];
-        float noiseU = nz.x * turbStrength;
-        float noiseV = nz.y * turbStrength;
-        float localVel = sqrtf(u * u + v * v);
-        if (localVel > 0.1f) {
-          float turbulenceFactor = go_min(localVel * 0.5f, 1.0f);
-          u += noiseU * turbulenceFactor;
-          v += noiseV * turbulenceFactor;
-        }
-      }
-    }
-    Uo[c] = u;
-    Vo[c] = v;
   }
-  // Row slots: sum div^2, max |div|, fluid cells, sum r^2, max |r|.
-  __shared__ float shr[64 * 5];
-  FF row[5] = {sums[0], {maxs[0], 0.0f}, {fi ? 1.0f : 0.0f, 0.0f}, sums[1], {maxs[1], 0.0f}};
-  block_row<5>(row, 0x12u, shr, part + 10 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x));
+  // Row slots: sum div^2, max |div|, fluid cells (exact), sum r^2, max |r|.
+  FF row[5] = {acc.d2, {acc.dmax, 0.0f}, {acc.n, 0.0f}, acc.r2, {acc.rmax, 0.0f}};
+  block_row<5, 0x4u>(row, 0x12u, shr, part + 10 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x));
 }
 
 __global__ void k_store_div_p(const float* __restrict__ r, DevStats* st) {
@@ -697,7 +718,7 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
       return e;
     mark(f, "outer correction");
   }
-  dim3 rg = cell_grid(f);
+  dim3 rg((f->NY + BX - 1) / BX, (f->NX + BY * GR - 1) / (BY * GR));
   int nb = rg.x * rg.y;
   if (!partials_fit(f, 5, nb)) return cudaErrorInvalidValue;
   count(f, 2);
