@@ -507,23 +507,37 @@ __device__ __forceinline__ void grad_cell(int i, int j, const float* __restrict_
   const int P = g.P;
   const int c = i * P + j;
   const bool hasL = i >= 1, hasR = i <= g.NX - 2, hasB = j >= 1, hasT = j <= g.NY - 2;
+  // Neighbour indices clamped to the cell at the domain edge, so every load
+  // below is issued at once and valid; the edge values are masked after.
+  const int cL = hasL ? c - P : c, cR = hasR ? c + P : c;
+  const int cB = hasB ? c - 1 : c, cT = hasT ? c + 1 : c;
   const uint8_t fl = flags[c];
-  const uint8_t fL = hasL ? flags[c - P] : 0, fR = hasR ? flags[c + P] : 0;
-  const uint8_t fB = hasB ? flags[c - 1] : 0, fT = hasT ? flags[c + 1] : 0;
+  const uint8_t fL = hasL ? flags[cL] : 0, fR = hasR ? flags[cR] : 0;
+  const uint8_t fB = hasB ? flags[cB] : 0, fT = hasT ? flags[cT] : 0;
   const bool act = flag_active(fl), aL = flag_active(fL), aR = flag_active(fR);
   const bool aB = flag_active(fB), aT = flag_active(fT);
-  // phi is 0 off the active cells; the correction is added on active ones.
-  const float pc = phi_final(phi, e, c, act);
-  const float pL = hasL ? phi_final(phi, e, c - P, aL) : 0.0f;
-  const float pR = hasR ? phi_final(phi, e, c + P, aR) : 0.0f;
-  const float pB = hasB ? phi_final(phi, e, c - 1, aB) : 0.0f;
-  const float pT = hasT ? phi_final(phi, e, c + 1, aT) : 0.0f;
+  // phi and the correction are both exactly 0 off the active cells, so the
+  // final potential phi + e needs no activity test.
+  float pc = phi[c], pL = phi[cL], pR = phi[cR], pB = phi[cB], pT = phi[cT];
+  if (e) {
+    pc = pc + e[c];
+    pL = pL + e[cL];
+    pR = pR + e[cR];
+    pB = pB + e[cB];
+    pT = pT + e[cT];
+  }
+  if (!hasL) pL = 0.0f;
+  if (!hasR) pR = 0.0f;
+  if (!hasB) pB = 0.0f;
+  if (!hasT) pT = 0.0f;
   float u = U[c], v = V[c];
+  const float uR0 = U[cR], vT0 = V[cT], bc = rhs[c];
+  const float2 nz = do_turb ? noise[c] : make_float2(0.0f, 0.0f);
   if (hasL && hasB && hasT && (act || aL)) u = u + (fbit(fl, F_FLUID) * pL - fbit(fl, F_W) * pc);
   if (hasB && hasL && hasR && (act || aB)) v = v + (fbit(fl, F_FLUID) * pB - fbit(fl, F_S) * pc);
   p[c] = act ? cp * pc : 0.0f;
   if (act) {
-    FF r = resid_ff(rhs[c], pL, pR, pB, pT, (float)flag_count(fl), pc);
+    FF r = resid_ff(bc, pL, pR, pB, pT, (float)flag_count(fl), pc);
     FF q = ff_sq(r.hi);
     q.lo = q.lo + 2.0f * r.hi * r.lo;
     acc.r2 = ff_add(acc.r2, q);
@@ -531,16 +545,15 @@ __device__ __forceinline__ void grad_cell(int i, int j, const float* __restrict_
   }
   if ((fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR)) {
     // Projected faces (i+1, j) and (i, j+1), as their own threads compute them.
-    float uR = U[c + P];
+    float uR = uR0;
     if (act || aR) uR = uR + (fbit(fR, F_FLUID) * pc - fbit(fR, F_W) * pR);
-    float vT = V[c + 1];
+    float vT = vT0;
     if (act || aT) vT = vT + (fbit(fT, F_FLUID) * pc - fbit(fT, F_S) * pT);
     float div = uR - u + vT - v;
     acc.d2 = ff_add(acc.d2, ff_sq(div));
     acc.dmax = fmaxf(acc.dmax, fabsf(div));
     acc.n = acc.n + 1.0f;
     if (do_turb) {
-      float2 nz = noise[c];
       float noiseU = nz.x * turbStrength;
       float noiseV = nz.y * turbStrength;
       float localVel = sqrtf(u * u + v * v);
