@@ -142,6 +142,22 @@ def committed_traffic():
         return None
 
 
+def max_over_ranks(ms, device):
+    """Max of a per-rank time over the process group (the slowest replica
+    sets the job time)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, steps, t_max_ms, cells=W * H):
+    """Whole-job Mcell-steps/s of `world` replicas of `steps` steps each."""
+    return world * cells * steps / (t_max_ms / 1e3) / 1e6
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -271,12 +287,8 @@ def run_ours(args):
         barrier()
     launches = f.launch_count() - launches0
     ms = e0.elapsed_time(e1)
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * W * H * args.steps / (t_max / 1e3) / 1e6
+    t_max = max_over_ranks(ms, "cuda") if world > 1 else ms
+    value = replica_value(world, args.steps, t_max)
     st = f.stats()
 
     # ------------------------------------------------------------ dominant kernel
