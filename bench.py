@@ -184,6 +184,84 @@ def lid_cells(f):
     return i, j
 
 
+def fwd_adjoint(fluid_gb300, args):
+    """Forward + adjoint rollout on the cavity (refine_sweeps 0, the recorded
+    rollouts' form): ROLL steps with a device-resident per-step force field,
+    checkpoint every 8 steps, loss ||M_T - target||_2, gradients w.r.t. the
+    initial state and every step's forces.  Returns per-step times of the
+    rollout (forward + recompute + adjoint) and of plain forward steps of the
+    same configuration, both device-timed with CUDA events."""
+    import numpy as np
+    import torch
+
+    roll, every = 16, 8
+    f = build_cavity(fluid_gb300)
+    f.refine_sweeps = 0
+    li, lj = lid_cells(f)
+    f.set_sources(li, lj, u=1.0, v=0.0, smoke=1.0,
+                  mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY | f.SRC_ADD_SMOKE)
+    stream = torch.cuda.ExternalStream(f.stream)
+    n = f.numCells
+    gen = torch.Generator(device="cuda").manual_seed(4)
+    forces = (torch.rand((roll, 2, n), device="cuda", generator=gen) - 0.5) * 0.01
+    ii = torch.arange(f.NumX, device="cuda", dtype=torch.float32)[:, None]
+    jj = torch.arange(f.NumY, device="cuda", dtype=torch.float32)[None, :]
+    target = torch.zeros((f.NumX, f.NumY), device="cuda")
+    rng = np.random.default_rng(4)
+    for _ in range(4):
+        s, a = rng.uniform(10, 30), rng.uniform(0.5, 1.0)
+        ci, cj = rng.uniform(1, f.NumX - 1), rng.uniform(1, f.NumY - 1)
+        target += a * torch.exp(-((ii - ci) ** 2 + (jj - cj) ** 2) / (2 * s * s))
+    target = target.reshape(-1).contiguous()
+    gfu = torch.empty((roll, n), device="cuda")
+    gfv = torch.empty((roll, n), device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(8):  # spin up the flow so the rollout starts from a moving state
+        f.Simulate(DT)
+    f.synchronize()
+
+    def rollout():
+        f.tape_begin(roll, every)
+        for t in range(roll):
+            f.step_forward(DT, forces[t, 0], forces[t, 1])
+        loss = f.tape_seed_smoke_l2(target)
+        for t in reversed(range(roll)):
+            f.step_adjoint(gfu[t], gfv[t])
+        f.tape_end()
+        return loss
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    rollout()
+    f.synchronize()
+    reps = max(1, min(3, args.steps // 8))
+    e0.record(stream)
+    for _ in range(reps):
+        loss = rollout()
+    e1.record(stream)
+    f.synchronize()
+    ms_roll = e0.elapsed_time(e1) / (reps * roll)
+    l0 = f.launch_count()
+    e0.record(stream)
+    for _ in range(roll):
+        f.Simulate(DT)
+    e1.record(stream)
+    f.synchronize()
+    ms_fwd = e0.elapsed_time(e1) / roll
+    return {
+        "metric": "Mcell-steps/s fwd+adjoint at 2048^2",
+        "value": W * H / ms_roll / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms_roll,
+        "fwd_ms_per_step": ms_fwd, "ratio_to_fwd": ms_roll / ms_fwd,
+        "rollout_steps": roll, "checkpoint_every": every, "loss": loss,
+        "config": "cavity 2048x2048 as above with refine_sweeps 0 and +1 smoke on the lid row; "
+                  "per-step 2-channel force field on the device; one rollout = %d recorded "
+                  "steps + seed + %d adjoint steps (the first %d steps recomputed from their "
+                  "checkpoint); gradients w.r.t. the initial state and all forces"
+                  % (roll, roll, roll - every),
+        "fwd_launches_per_step": (f.launch_count() - l0) / roll,
+    }
+
+
 # ---------------------------------------------------------------- CPU legs
 def cpu_reference_steps(steps, threads, budget_s=None):
     """Times the reference algorithm (FP32, serial SOR pressure, parallelRange
@@ -344,6 +422,8 @@ def run_ours(args):
                "path": "fg_set_velocity_many (lid) + fg_simulate + fg_download(M) per step"}
         del g
 
+    adj = fwd_adjoint(fluid_gb300, args) if rank == 0 and not args.no_adjoint else None
+
     # ------------------------------------------------------------ CPU baseline
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -362,6 +442,7 @@ def run_ours(args):
             "data": "synthetic",
             "config": workload_config({"parallelism": "replicas%d" % world if world > 1 else "single"}),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "fwd_adjoint": adj,
             "clocks": sampler.summary(),
             "host_ms_per_step": 1e3 * t_host / args.steps,
             "stage_ms": stage_ms,
@@ -381,6 +462,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

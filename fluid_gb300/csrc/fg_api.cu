@@ -18,6 +18,8 @@ namespace {
 
 constexpr int kSlots = 4096;
 
+void tape_free(fg_fluid* f);  // differentiable rollouts, at the end of the file
+
 int fail(fg_fluid* f, int code, const char* what, cudaError_t e = cudaSuccess) {
   if (f) {
     char buf[512];
@@ -380,6 +382,8 @@ int fg_destroy(fg_fluid* f) {
   cudaSetDevice(f->device);
   if (f->stream) cudaStreamSynchronize(f->stream);
   clear_graphs(f);
+  tape_free(f);
+  for (int k = 0; k < fg_fluid::A_COUNT; ++k) cudaFree(f->adj[k]);
   for (int k = 0; k < FG_NUM_FIELDS; ++k) {
     cudaFree(f->d[k]);
     cudaFree(f->partner[k]);
@@ -969,6 +973,354 @@ unsigned long long fg_edit_bytes(const fg_fluid* f) { return f ? f->edit_bytes :
 const char* fg_last_error(const fg_fluid* f) {
   if (!f) return "invalid handle";
   return f->last_error.c_str();
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Differentiable rollouts: the Step / StepAdjoint pair.
+//
+// fg_tape_begin saves the current state as checkpoint 0; each
+// fg_step_forward runs one step with an optional force field and saves a
+// checkpoint every `every` steps; fg_tape_seed / fg_tape_seed_smoke_l2 set the
+// adjoint of the final state; each fg_step_adjoint reverses the latest step
+// not yet reversed.  Reversing a step needs the intermediates of its forward
+// pass: the steps of one checkpoint interval are recomputed from their
+// checkpoint, recording them (the last interval is recorded during the
+// forward pass itself), so memory is one interval of records plus the
+// checkpoints.  When the last step has been reversed, the handle's state is
+// restored to the end of the forward pass.
+// ===========================================================================
+struct Tape {
+  int max_steps = 0, every = 0;
+  int n_fwd = 0, n_rev = 0;
+  int n_ckpt = 0;
+  int seg_loaded = -1;  // interval whose steps' records fill the record slots
+  bool seeded = false;
+  bool final_saved = false;
+  uint64_t version = 0;
+  std::vector<float> dts;
+  std::vector<char> has_force;
+  float* forces = nullptr;  // max_steps x {Fu, Fv}
+  float* ckpt = nullptr;    // (n_ckpt + 1) x {U, V, M, newU, newV, newM}; the last is the final state
+  float* rec = nullptr;     // every x kTapeFields
+  float* aux = nullptr;     // loss target
+};
+
+namespace {
+
+constexpr int kStateFields[6] = {FG_U, FG_V, FG_M, FG_NEWU, FG_NEWV, FG_NEWM};
+
+size_t field_elems(const fg_fluid* f) { return (size_t)f->NX * f->P; }
+
+void tape_free(fg_fluid* f) {
+  if (!f->tape) return;
+  cudaStreamSynchronize(f->stream);
+  cudaFree(f->tape->forces);
+  cudaFree(f->tape->ckpt);
+  cudaFree(f->tape->rec);
+  cudaFree(f->tape->aux);
+  delete f->tape;
+  f->tape = nullptr;
+}
+
+int tape_supported(fg_fluid* f) {
+  const fg_params& p = f->prm;
+  if (p.scheme != FG_SCHEME_JACOBI)
+    return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts need the parallel (Jacobi) scheme");
+  if (p.early_exit)
+    return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts need a fixed sweep count (early_exit 0)");
+  if (p.refine_sweeps > 0)
+    return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support refine_sweeps");
+  if (p.viscosity_diffusion > 0.0f)
+    return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support viscosity");
+  if (p.confinement != 0.0f)
+    return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support confinement");
+  if (p.use_multigrid && p.multigrid_levels > 1)
+    return fail(f, FG_ERR_UNSUPPORTED, "UseMultigrid is not built for the GPU step");
+  return FG_OK;
+}
+
+int copy_field(fg_fluid* f, float* dst, const float* src) {
+  CK(f, cudaMemcpyAsync(dst, src, field_bytes(f), cudaMemcpyDeviceToDevice, f->stream), "copy");
+  return FG_OK;
+}
+
+int save_state(fg_fluid* f, float* dst) {
+  for (int k = 0; k < 6; ++k) {
+    int rc = copy_field(f, dst + k * field_elems(f), f->d[kStateFields[k]]);
+    if (rc) return rc;
+  }
+  return FG_OK;
+}
+
+int load_state(fg_fluid* f, const float* src) {
+  for (int k = 0; k < 6; ++k) {
+    int rc = copy_field(f, f->d[kStateFields[k]], src + k * field_elems(f));
+    if (rc) return rc;
+  }
+  return FG_OK;
+}
+
+// Copies a field in the Go slice layout (host or device memory) to a
+// pitched device field, or back.
+int put_field(fg_fluid* f, float* dev, const float* src) {
+  size_t hp = sizeof(float) * f->NY, dp = sizeof(float) * f->P;
+  CK(f, cudaMemcpy2DAsync(dev, dp, src, hp, hp, f->NX, cudaMemcpyDefault, f->stream), "upload");
+  return FG_OK;
+}
+int get_field(fg_fluid* f, float* dst, const float* dev) {
+  size_t hp = sizeof(float) * f->NY, dp = sizeof(float) * f->P;
+  CK(f, cudaMemcpy2DAsync(dst, hp, dev, dp, hp, f->NX, cudaMemcpyDefault, f->stream), "download");
+  return FG_OK;
+}
+
+// One recorded step: Simulate (fluid.go:79-109) with the force field added
+// to U, V before the sources, turbulence run as its own pass, and the
+// intermediates the adjoint reads written to `rec` (kTapeFields fields:
+// U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM corrM).  The BFECC
+// intermediates are produced in place: the scratch pointers are redirected
+// to the record for the step.
+int enqueue_step_record(fg_fluid* f, float dt, const float* fu, const float* fv, float* rec) {
+  const fg_params& p = f->prm;
+  const size_t n = field_elems(f);
+  auto R = [&](int k) { return rec + (size_t)k * n; };
+  int rc;
+  if (fu) CK(f, launch_add_forces(f, fu, fv), "forces");
+  CK(f, launch_apply_sources(f), "sources");
+  CK(f, launch_clear_stats(f), "clear stats");
+  if ((rc = enqueue_pressure(f, p.num_iters, dt, false))) return rc;
+  if (p.turbulence_strength > 0.0f) {
+    if ((rc = copy_field(f, R(0), f->d[FG_U])) || (rc = copy_field(f, R(1), f->d[FG_V]))) return rc;
+    CK(f, launch_confinement_turbulence(f, dt, false, true), "turbulence");
+  }
+  CK(f, launch_borders(f), "borders");
+  if ((rc = copy_field(f, R(2), f->d[FG_U])) || (rc = copy_field(f, R(3), f->d[FG_V]))) return rc;
+  float* keep[6] = {f->fwdU, f->fwdV, f->corrU, f->corrV, f->fwdM, f->corrM};
+  f->fwdU = R(4);
+  f->fwdV = R(5);
+  f->corrU = R(6);
+  f->corrV = R(7);
+  f->fwdM = R(11);
+  f->corrM = R(12);
+  cudaError_t e = p.use_bfecc ? launch_advect_velocity_bfecc(f, dt) : launch_advect_velocity(f, dt);
+  if (e == cudaSuccess) {
+    if ((rc = copy_field(f, R(8), f->d[FG_U])) || (rc = copy_field(f, R(9), f->d[FG_V])) ||
+        (rc = copy_field(f, R(10), f->d[FG_M]))) {
+      e = cudaErrorUnknown;
+    } else {
+      e = p.use_bfecc ? launch_advect_smoke_bfecc(f, dt) : launch_advect_smoke(f, dt);
+    }
+  }
+  f->fwdU = keep[0];
+  f->fwdV = keep[1];
+  f->corrU = keep[2];
+  f->corrV = keep[3];
+  f->fwdM = keep[4];
+  f->corrM = keep[5];
+  if (e != cudaSuccess) return fail(f, FG_ERR_CUDA, "advection", e);
+  return FG_OK;
+}
+
+int tape_usable(fg_fluid* f) {
+  Tape* t = f->tape;
+  if (!t) return fail(f, FG_ERR_INVALID, "no recorded rollout (fg_tape_begin)");
+  if (t->version != f->params_version)
+    return fail(f, FG_ERR_INVALID, "parameters or sources changed during a recorded rollout");
+  if (!f->edits.empty() || f->dirty || f->masks_stale)
+    return fail(f, FG_ERR_INVALID, "the state was edited during a recorded rollout");
+  return bind(f);
+}
+
+float* ckpt_at(fg_fluid* f, int k) { return f->tape->ckpt + (size_t)k * 6 * field_elems(f); }
+float* rec_at(fg_fluid* f, int k) { return f->tape->rec + (size_t)k * kTapeFields * field_elems(f); }
+float* force_at(fg_fluid* f, int t, int c) {
+  return f->tape->forces + ((size_t)t * 2 + c) * field_elems(f);
+}
+
+// Recomputes the steps of interval s from its checkpoint, recording them.
+int tape_load_interval(fg_fluid* f, int s) {
+  Tape* t = f->tape;
+  int rc = load_state(f, ckpt_at(f, s));
+  if (rc) return rc;
+  int t1 = std::min((s + 1) * t->every, t->n_fwd);
+  for (int k = s * t->every; k < t1; ++k) {
+    bool hf = t->has_force[k] != 0;
+    rc = enqueue_step_record(f, t->dts[k], hf ? force_at(f, k, 0) : nullptr,
+                             hf ? force_at(f, k, 1) : nullptr, rec_at(f, k - s * t->every));
+    if (rc) return rc;
+  }
+  t->seg_loaded = s;
+  return FG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_tape_begin(fg_fluid* f, int max_steps, int every) {
+  if (!f || max_steps < 1 || every < 1) return FG_ERR_INVALID;
+  int rc = flush(f);
+  if (rc) return rc;
+  if ((rc = tape_supported(f))) return rc;
+  if ((rc = check_iters(f, f->prm.num_iters))) return rc;
+  tape_free(f);
+  for (int k = 0; k < fg_fluid::A_COUNT; ++k)
+    if (!f->adj[k] && (rc = alloc_dev(f, &f->adj[k]))) return rc;
+  Tape* t = new Tape();
+  f->tape = t;
+  t->max_steps = max_steps;
+  t->every = std::min(every, max_steps);
+  t->n_ckpt = (max_steps + t->every - 1) / t->every;
+  t->version = f->params_version;
+  t->dts.assign(max_steps, 0.0f);
+  t->has_force.assign(max_steps, 0);
+  size_t fb = field_bytes(f);
+  cudaError_t e;
+  if ((e = cudaMalloc((void**)&t->forces, fb * 2 * max_steps)) != cudaSuccess ||
+      (e = cudaMalloc((void**)&t->ckpt, fb * 6 * (t->n_ckpt + 1))) != cudaSuccess ||
+      (e = cudaMalloc((void**)&t->rec, fb * kTapeFields * t->every)) != cudaSuccess ||
+      (e = cudaMalloc((void**)&t->aux, fb)) != cudaSuccess) {
+    tape_free(f);
+    return fail(f, FG_ERR_NOMEM, "tape allocation", e);
+  }
+  // Record fields a step leaves unwritten (U2, V2 without turbulence) and
+  // the padding columns stay zero.
+  CK(f, cudaMemsetAsync(t->rec, 0, fb * kTapeFields * t->every, f->stream), "tape");
+  CK(f, cudaMemsetAsync(t->forces, 0, fb * 2 * max_steps, f->stream), "tape");
+  CK(f, cudaMemsetAsync(t->aux, 0, fb, f->stream), "tape");
+  return save_state(f, ckpt_at(f, 0));
+}
+
+int fg_tape_end(fg_fluid* f) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  Tape* t = f->tape;
+  if (t && t->final_saved && t->n_rev < t->n_fwd) {
+    // Abandoned mid-reverse: put the end-of-rollout state back.
+    if ((rc = load_state(f, ckpt_at(f, t->n_ckpt)))) return rc;
+    invalidate(f, kStepFields);
+  }
+  tape_free(f);
+  return FG_OK;
+}
+
+int fg_step_forward(fg_fluid* f, float dt, const float* force_u, const float* force_v) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = tape_usable(f);
+  if (rc) return rc;
+  Tape* t = f->tape;
+  if (t->n_rev > 0 || t->seeded)
+    return fail(f, FG_ERR_INVALID, "the rollout is being reversed: no further forward steps");
+  if (t->n_fwd >= t->max_steps) return fail(f, FG_ERR_INVALID, "rollout longer than max_steps");
+  if ((force_u == nullptr) != (force_v == nullptr))
+    return fail(f, FG_ERR_INVALID, "give both force components or neither");
+  int k = t->n_fwd;
+  if (k > 0 && k % t->every == 0 && (rc = save_state(f, ckpt_at(f, k / t->every)))) return rc;
+  if (force_u) {
+    if ((rc = put_field(f, force_at(f, k, 0), force_u)) ||
+        (rc = put_field(f, force_at(f, k, 1), force_v)))
+      return rc;
+  }
+  invalidate(f, kStepFields);
+  rc = enqueue_step_record(f, dt, force_u ? force_at(f, k, 0) : nullptr,
+                           force_u ? force_at(f, k, 1) : nullptr, rec_at(f, k % t->every));
+  if (rc) return rc;
+  t->dts[k] = dt;
+  t->has_force[k] = force_u ? 1 : 0;
+  t->seg_loaded = k / t->every;
+  t->n_fwd = k + 1;
+  return FG_OK;
+}
+
+int fg_tape_seed(fg_fluid* f, const float* dU, const float* dV, const float* dM) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = tape_usable(f);
+  if (rc) return rc;
+  Tape* t = f->tape;
+  if (t->n_fwd == 0 || t->n_rev > 0)
+    return fail(f, FG_ERR_INVALID, "seed the adjoint after the forward steps, before reversing");
+  const float* src[3] = {dU, dV, dM};
+  const int dst[3] = {fg_fluid::A_U, fg_fluid::A_V, fg_fluid::A_M};
+  for (int k = 0; k < 3; ++k) {
+    CK(f, cudaMemsetAsync(f->adj[dst[k]], 0, field_bytes(f), f->stream), "seed");
+    if (src[k] && (rc = put_field(f, f->adj[dst[k]], src[k]))) return rc;
+  }
+  for (int k : {fg_fluid::A_NU, fg_fluid::A_NV, fg_fluid::A_NM})
+    CK(f, cudaMemsetAsync(f->adj[k], 0, field_bytes(f), f->stream), "seed");
+  t->seeded = true;
+  return FG_OK;
+}
+
+int fg_tape_seed_smoke_l2(fg_fluid* f, const float* target, float* loss) {
+  if (!f || !target) return FG_ERR_INVALID;
+  int rc = tape_usable(f);
+  if (rc) return rc;
+  Tape* t = f->tape;
+  if (t->n_fwd == 0 || t->n_rev > 0)
+    return fail(f, FG_ERR_INVALID, "seed the adjoint after the forward steps, before reversing");
+  if ((rc = put_field(f, t->aux, target))) return rc;
+  float* slot = dev_scalar_slot(f);
+  CK(f, launch_loss_seed(f, t->aux, slot), "loss");
+  t->seeded = true;
+  if (loss) {
+    CK(f, cudaMemcpyAsync(f->scalar_pinned, slot, sizeof(float), cudaMemcpyDeviceToHost, f->stream),
+       "loss");
+    CK(f, cudaStreamSynchronize(f->stream), "loss sync");
+    *loss = f->scalar_pinned[0];
+  }
+  return FG_OK;
+}
+
+int fg_step_adjoint(fg_fluid* f, float* grad_force_u, float* grad_force_v) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = tape_usable(f);
+  if (rc) return rc;
+  Tape* t = f->tape;
+  if (!t->seeded) return fail(f, FG_ERR_INVALID, "seed the adjoint first (fg_tape_seed)");
+  if (t->n_rev >= t->n_fwd) return fail(f, FG_ERR_INVALID, "every recorded step is reversed");
+  if (!t->final_saved) {
+    if ((rc = save_state(f, ckpt_at(f, t->n_ckpt)))) return rc;
+    t->final_saved = true;
+  }
+  int k = t->n_fwd - 1 - t->n_rev;
+  int s = k / t->every;
+  if (t->seg_loaded != s && (rc = tape_load_interval(f, s))) return rc;
+  float* rec[kTapeFields];
+  for (int q = 0; q < kTapeFields; ++q)
+    rec[q] = rec_at(f, k - s * t->every) + (size_t)q * field_elems(f);
+  CK(f, launch_step_adjoint(f, t->dts[k], rec), "step adjoint");
+  if (grad_force_u && (rc = get_field(f, grad_force_u, f->adj[fg_fluid::A_U]))) return rc;
+  if (grad_force_v && (rc = get_field(f, grad_force_v, f->adj[fg_fluid::A_V]))) return rc;
+  t->n_rev++;
+  if (t->n_rev == t->n_fwd) {
+    if ((rc = load_state(f, ckpt_at(f, t->n_ckpt)))) return rc;
+    t->seg_loaded = -1;
+  }
+  invalidate(f, kStepFields);
+  return FG_OK;
+}
+
+int fg_tape_grad(fg_fluid* f, float* dU, float* dV, float* dM, float* dNU, float* dNV, float* dNM) {
+  if (!f) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  if (!f->tape || !f->tape->seeded) return fail(f, FG_ERR_INVALID, "no seeded rollout");
+  float* out[6] = {dU, dV, dM, dNU, dNV, dNM};
+  const int src[6] = {fg_fluid::A_U, fg_fluid::A_V, fg_fluid::A_M,
+                      fg_fluid::A_NU, fg_fluid::A_NV, fg_fluid::A_NM};
+  for (int k = 0; k < 6; ++k)
+    if (out[k] && (rc = get_field(f, out[k], f->adj[src[k]]))) return rc;
+  CK(f, cudaStreamSynchronize(f->stream), "grad sync");
+  return FG_OK;
+}
+
+int fg_tape_steps(const fg_fluid* f, int* forward, int* reversed) {
+  if (!f || !forward || !reversed) return FG_ERR_INVALID;
+  *forward = f->tape ? f->tape->n_fwd : 0;
+  *reversed = f->tape ? f->tape->n_rev : 0;
+  return FG_OK;
 }
 
 }  // extern "C"

@@ -174,6 +174,13 @@ struct fg_fluid {
   fg::SourceRec* src_dev = nullptr;
   uint32_t* src_off_dev = nullptr;
   int n_src_groups = 0;
+  // Differentiable rollouts: the adjoint of the state (U, V, M and the
+  // staging fields) and the adjoint work fields, allocated by the first
+  // recorded rollout; the rollout's tape (fg_api.cu).
+  enum { A_U, A_V, A_M, A_NU, A_NV, A_NM, A_CU, A_CV, A_FU, A_FV, A_BU, A_BV, A_CM, A_FM, A_BM,
+         A_COUNT };
+  float* adj[A_COUNT] = {};
+  struct Tape* tape = nullptr;
   // Kernel launches enqueued so far (graph replays add the captured count).
   unsigned long long launches = 0;
   // Optional CUDA-event bracket around the main Jacobi launches of a solve.
@@ -224,6 +231,18 @@ cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt);
 // Pressure solve + gradient subtract + post-projection divergence statistics;
 // with fuse_turb (parallel scheme only) also addTurbulence.
 cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb);
+// K Jacobi sweeps of A x = b from x = 0 (no early exit); ctl->sel names the
+// buffer holding x.
+cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const float* bw, float* x0,
+                                float* x1, int iters);
+// k_adjoint.cu
+constexpr int kTapeFields = 13;  // U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM corrM
+cudaError_t launch_add_forces(fg_fluid* f, const float* fu, const float* fv);
+// Adjoint of one recorded step: adj[A_U..A_NM] go from the adjoint of the
+// state after the step to that of the state before it; adj[A_U], adj[A_V]
+// then also hold the adjoint of the step's force field.
+cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape);
+cudaError_t launch_loss_seed(fg_fluid* f, const float* target, float* dev_loss);
 // k_diag.cu
 cudaError_t launch_div_stats(fg_fluid* f);
 cudaError_t launch_smoke_mass(fg_fluid* f);

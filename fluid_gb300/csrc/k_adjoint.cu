@@ -1,0 +1,700 @@
+// Adjoint (reverse-mode derivative) of the simulation step for the parallel
+// pressure scheme.
+//
+// The forward step of a differentiable rollout is Simulate (fluid.go:79-109)
+// with two additions: an optional force field added to U and V before the
+// sources, and the pressure scheme fixed to Jacobi without early exit.  The
+// stages and their adjoints:
+//   forces       U += Fu, V += Fv            -> dFu = dU, dFv = dV
+//   sources      U, V set / M added          -> dU, dV zeroed on set cells
+//   projection   U2 = U1 + G P_K (-div U1)    -> dU1 = dU2 - div^T P_K G^T dU2
+//                (K Jacobi sweeps from 0 apply P_K = sum_k M^k W with M W =
+//                W M^T, so P_K is symmetric: its adjoint is the same solve)
+//   turbulence   pointwise, gated on |u| > 0.1 (fluid.go:496-526)
+//   borders      linear rules on the ghost rows (fluid.go:236-289)
+//   advection    bilinear gathers: transposed as scatters with atomics, plus
+//                the derivative of the backtrace position through the
+//                velocity that traced it; BFECC composes three of them with
+//                the compensation and the 3x3 clamp (fluid.go:909-1120)
+// Subgradient conventions at non-smooth points: a coordinate clamped to the
+// domain contributes no position derivative; the bilinear cell choice
+// (floor) is locally constant; a clamped BFECC value takes the derivative of
+// the neighbour that bounded it (the first in the reference's scan order);
+// max(x, 0) passes the derivative for x >= 0; min(0.5|u|, 1) has derivative
+// 0.5 below the kink and 0 at or above it; the turbulence gate passes the
+// noise term only for |u| > 0.1.
+//
+// The scatters use FP32 atomic adds, so an adjoint run is reproducible to
+// about 1e-7 relative, not bit for bit.
+#include <utility>
+
+#include "fg_internal.cuh"
+#include "fg_reduce.cuh"
+
+namespace fg {
+namespace {
+
+constexpr int BX = 32, BY = 8;
+inline dim3 cell_grid(const fg_fluid* f) {
+  return dim3((f->NY + BX - 1) / BX, (f->NX + BY - 1) / BY);
+}
+__device__ __forceinline__ bool on_ring(int i, int j, const Grid& g) {
+  return i == 0 || j == 0 || i == g.NX - 1 || j == g.NY - 1;
+}
+__device__ __forceinline__ bool u_advected(uint8_t fl, int i, int j, const Grid& g) {
+  return i >= 1 && j >= 1 && j <= g.NY - 2 && (fl & F_FLUID) && (fl & F_W);
+}
+__device__ __forceinline__ bool v_advected(uint8_t fl, int i, int j, const Grid& g) {
+  return i >= 1 && i <= g.NX - 2 && j >= 1 && (fl & F_FLUID) && (fl & F_S);
+}
+__device__ __forceinline__ bool fluid_interior(uint8_t fl) {
+  return (fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR);
+}
+
+// Forward: U += Fu, V += Fv on every cell.
+__global__ void k_add_forces(float* __restrict__ U, float* __restrict__ V,
+                             const float* __restrict__ Fu, const float* __restrict__ Fv, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  U[c] = U[c] + Fu[c];
+  V[c] = V[c] + Fv[c];
+}
+
+// Adjoint of a bilinear sample of field F at (x, y) (sampleField): scatters
+// lam * weights into dF and returns d value / d x, d value / d y (0 along a
+// clamped coordinate).
+__device__ __forceinline__ void sample_adjoint(const float* __restrict__ F, float* dF, float x,
+                                               float y, float dx, float dy, float lam,
+                                               const Grid& g, float* dvdx, float* dvdy) {
+  float xc = fmaxf(fminf(x, g.NXh), g.h);
+  float yc = fmaxf(fminf(y, g.NYh), g.h);
+  float xs = xc - dx, ys = yc - dy;
+  int x0 = min((int)floorf(xs * g.h1), g.NX - 1);
+  float tx = (xs - (float)x0 * g.h) * g.h1;
+  int x1 = min(x0 + 1, g.NX - 1);
+  int y0 = min((int)floorf(ys * g.h1), g.NY - 1);
+  float ty = (ys - (float)y0 * g.h) * g.h1;
+  int y1 = min(y0 + 1, g.NY - 1);
+  float sx = 1.0f - tx, sy = 1.0f - ty;
+  const int P = g.P;
+  float f00 = F[x0 * P + y0], f10 = F[x1 * P + y0], f11 = F[x1 * P + y1], f01 = F[x0 * P + y1];
+  if (lam != 0.0f) {
+    atomicAdd(&dF[x0 * P + y0], sx * sy * lam);
+    atomicAdd(&dF[x1 * P + y0], tx * sy * lam);
+    atomicAdd(&dF[x1 * P + y1], tx * ty * lam);
+    atomicAdd(&dF[x0 * P + y1], sx * ty * lam);
+  }
+  *dvdx = xc == x ? g.h1 * (sy * (f10 - f00) + ty * (f11 - f01)) : 0.0f;
+  *dvdy = yc == y ? g.h1 * (sx * (f01 - f00) + tx * (f11 - f10)) : 0.0f;
+}
+
+// Adjoint of a semi-Lagrangian velocity pass (advectVelocity fluid.go:291-333
+// and BFECC's passes): out = advected ? sample(Fs; trace with (Ut, Vt), sdt)
+// : ring ? R : stale.  lamU/lamV hold the output adjoint.  Accumulates into
+// dFu/dFv (sampled field), dUt/dVt (tracing velocity), dRu/dRv (ring source,
+// may be null: no ring term) and dNu/dNv (stale source, may be null).
+__global__ void k_adj_sl_velocity(const float* __restrict__ lamU, const float* __restrict__ lamV,
+                                  const float* __restrict__ Ut, const float* __restrict__ Vt,
+                                  const float* __restrict__ Fu, const float* __restrict__ Fv,
+                                  float* dUt, float* dVt, float* dFu, float* dFv, float* dRu,
+                                  float* dRv, float* dNu, float* dNv,
+                                  const uint8_t* __restrict__ flags, float sdt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  uint8_t fl = flags[c];
+  bool ring = on_ring(i, j, g);
+  float lu = lamU[c], lv = lamV[c];
+  if (u_advected(fl, i, j, g)) {
+    float x = (float)i * g.h, y = (float)j * g.h + g.hh;
+    float u = Ut[c];
+    float v = (Vt[c - P] + Vt[c] + Vt[c - P + 1] + Vt[c + 1]) * 0.25f;
+    x = x - sdt * u;
+    y = y - sdt * v;
+    float gx, gy;
+    sample_adjoint(Fu, dFu, x, y, 0.0f, g.hh, lu, g, &gx, &gy);
+    float du = -sdt * gx * lu, dv = -sdt * gy * lu;
+    if (du != 0.0f) atomicAdd(&dUt[c], du);
+    if (dv != 0.0f) {
+      float q = 0.25f * dv;
+      atomicAdd(&dVt[c - P], q);
+      atomicAdd(&dVt[c], q);
+      atomicAdd(&dVt[c - P + 1], q);
+      atomicAdd(&dVt[c + 1], q);
+    }
+  } else if (ring) {
+    if (dRu && lu != 0.0f) atomicAdd(&dRu[c], lu);
+  } else if (dNu) {
+    dNu[c] += lu;
+  }
+  if (v_advected(fl, i, j, g)) {
+    float x = (float)i * g.h + g.hh, y = (float)j * g.h;
+    float u = (Ut[c - 1] + Ut[c] + Ut[c + P - 1] + Ut[c + P]) * 0.25f;
+    float v = Vt[c];
+    x = x - sdt * u;
+    y = y - sdt * v;
+    float gx, gy;
+    sample_adjoint(Fv, dFv, x, y, g.hh, 0.0f, lv, g, &gx, &gy);
+    float du = -sdt * gx * lv, dv = -sdt * gy * lv;
+    if (dv != 0.0f) atomicAdd(&dVt[c], dv);
+    if (du != 0.0f) {
+      float q = 0.25f * du;
+      atomicAdd(&dUt[c - 1], q);
+      atomicAdd(&dUt[c], q);
+      atomicAdd(&dUt[c + P - 1], q);
+      atomicAdd(&dUt[c + P], q);
+    }
+  } else if (ring) {
+    if (dRv && lv != 0.0f) atomicAdd(&dRv[c], lv);
+  } else if (dNv) {
+    dNv[c] += lv;
+  }
+}
+
+// clampToNeighbors (fluid.go:1094-1120) on an interior cell: returns the
+// offset (in elements) of the neighbour whose value bounded `val`, or -1 if
+// val was inside the range.  Ties keep the first value in scan order, as the
+// strict comparisons of the reference do.
+__device__ __forceinline__ int clamp_source(float val, const float* __restrict__ src, int c, int P) {
+  float lo = src[c], hi = src[c];
+  int klo = 0, khi = 0;
+#pragma unroll
+  for (int di = -1; di <= 1; ++di)
+#pragma unroll
+    for (int dj = -1; dj <= 1; ++dj) {
+      int k = di * P + dj;
+      float v = src[c + k];
+      if (v < lo) {
+        lo = v;
+        klo = k;
+      }
+      if (v > hi) {
+        hi = v;
+        khi = k;
+      }
+    }
+  if (val < lo) return klo + 0x40000000;  // tagged: a neighbour offset
+  if (val > hi) return khi + 0x40000000;
+  return -1;
+}
+
+// Adjoint of BFECC's compensation + clamp for velocity (fluid.go:968-987):
+// corr = clamp(o - (bwd - o) * 0.5) on interior faces, corr = o on the ring.
+// Reads lamC (adjoint of corr); writes lamB (adjoint of bwd, 0 where bwd is
+// the constant 0 of a non-advected face) and accumulates into dO.
+__global__ void k_adj_bfecc_vel_correct(const float* __restrict__ lamCu,
+                                        const float* __restrict__ lamCv,
+                                        const float* __restrict__ Ou, const float* __restrict__ Ov,
+                                        const float* __restrict__ Fu, const float* __restrict__ Fv,
+                                        float* __restrict__ lamBu, float* __restrict__ lamBv,
+                                        float* dOu, float* dOv, const uint8_t* __restrict__ flags,
+                                        float dt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  float lu = lamCu[c], lv = lamCv[c];
+  if (on_ring(i, j, g)) {
+    lamBu[c] = 0.0f;
+    lamBv[c] = 0.0f;
+    if (lu != 0.0f) atomicAdd(&dOu[c], lu);
+    if (lv != 0.0f) atomicAdd(&dOv[c], lv);
+    return;
+  }
+  uint8_t fl = flags[c];
+  // Recompute bwd and the raw compensated value (as k_bfecc_vel_correct).
+  for (int comp = 0; comp < 2; ++comp) {
+    const float* O = comp == 0 ? Ou : Ov;
+    const float* F = comp == 0 ? Fu : Fv;
+    float lam = comp == 0 ? lu : lv;
+    bool adv = comp == 0 ? u_advected(fl, i, j, g) : v_advected(fl, i, j, g);
+    float b = 0.0f;
+    if (adv) {
+      float x, y, dx, dy;
+      if (comp == 0) {
+        x = (float)i * g.h;
+        y = (float)j * g.h + g.hh;
+        float u = Ou[c];
+        float v = (Ov[c - P] + Ov[c] + Ov[c - P + 1] + Ov[c + 1]) * 0.25f;
+        x = x + dt * u;
+        y = y + dt * v;
+        dx = 0.0f;
+        dy = g.hh;
+      } else {
+        x = (float)i * g.h + g.hh;
+        y = (float)j * g.h;
+        float u = (Ou[c - 1] + Ou[c] + Ou[c + P - 1] + Ou[c + P]) * 0.25f;
+        float v = Ov[c];
+        x = x + dt * u;
+        y = y + dt * v;
+        dx = g.hh;
+        dy = 0.0f;
+      }
+      b = sample_field(F, x, y, dx, dy, g);
+    }
+    float o = O[c];
+    float raw = o - (b - o) * 0.5f;
+    int src = clamp_source(raw, O, c, P);
+    float* dO = comp == 0 ? dOu : dOv;
+    float* lamB = comp == 0 ? lamBu : lamBv;
+    if (src >= 0) {
+      if (lam != 0.0f) atomicAdd(&dO[c + (src - 0x40000000)], lam);
+      lamB[c] = 0.0f;
+    } else {
+      if (lam != 0.0f) atomicAdd(&dO[c], 1.5f * lam);
+      lamB[c] = adv ? -0.5f * lam : 0.0f;
+    }
+  }
+}
+
+// Adjoint of a semi-Lagrangian smoke pass (advectSmoke fluid.go:400-434,
+// without the diffusion term): out = fluid interior ? max(sample(Ms), 0) :
+// ring ? Ms : stale.  With bwd = 1 the pass is BFECC's reverse sample (no
+// max, non-fluid cells constant 0, no ring / stale terms).  The trace
+// velocity is ((U[c] + U[c+P]) / 2 * SA, (V[c] + V[c+1]) / 2 * SA).
+__global__ void k_adj_sl_smoke(const float* __restrict__ lamM, const float* __restrict__ U,
+                               const float* __restrict__ V, const float* __restrict__ Ms,
+                               float* dU, float* dV, float* dMs, float* dN,
+                               const uint8_t* __restrict__ flags, float sdt, float smokeAdv,
+                               int bwd, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  uint8_t fl = flags[c];
+  float lam = lamM[c];
+  bool interior = !on_ring(i, j, g);
+  bool advected = bwd ? (interior && (fl & F_FLUID)) : fluid_interior(fl);
+  if (advected) {
+    float u = (U[c] + U[c + P]) * 0.5f * smokeAdv;
+    float v = (V[c] + V[c + 1]) * 0.5f * smokeAdv;
+    float x = (float)i * g.h + g.hh - sdt * u;
+    float y = (float)j * g.h + g.hh - sdt * v;
+    if (!bwd) {
+      float s = sample_field(Ms, x, y, g.hh, g.hh, g);
+      if (!(s >= 0.0f)) lam = 0.0f;  // max(s, 0) clamped
+    }
+    float gx, gy;
+    sample_adjoint(Ms, dMs, x, y, g.hh, g.hh, lam, g, &gx, &gy);
+    float du = -sdt * gx * lam * 0.5f * smokeAdv, dv = -sdt * gy * lam * 0.5f * smokeAdv;
+    if (du != 0.0f) {
+      atomicAdd(&dU[c], du);
+      atomicAdd(&dU[c + P], du);
+    }
+    if (dv != 0.0f) {
+      atomicAdd(&dV[c], dv);
+      atomicAdd(&dV[c + 1], dv);
+    }
+  } else if (!bwd) {
+    if (!interior) {
+      if (lam != 0.0f) atomicAdd(&dMs[c], lam);
+    } else if (dN) {
+      dN[c] += lam;
+    }
+  }
+}
+
+// Adjoint of BFECC's smoke compensation (fluid.go:1029-1046): corr =
+// clamp(o - (bwd - o) * 0.5), then max(corr, 0), on interior cells; o on the
+// ring.  Writes lamB, accumulates into dO.
+__global__ void k_adj_bfecc_smoke_correct(const float* __restrict__ lamC,
+                                          const float* __restrict__ U, const float* __restrict__ V,
+                                          const float* __restrict__ Mo, const float* __restrict__ Fm,
+                                          float* __restrict__ lamB, float* dO,
+                                          const uint8_t* __restrict__ flags, float dt,
+                                          float smokeAdv, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  float lam = lamC[c];
+  if (on_ring(i, j, g)) {
+    lamB[c] = 0.0f;
+    if (lam != 0.0f) atomicAdd(&dO[c], lam);
+    return;
+  }
+  uint8_t fl = flags[c];
+  float b = 0.0f;
+  bool adv = (fl & F_FLUID) != 0;
+  if (adv) {
+    float u = (U[c] + U[c + P]) * 0.5f * smokeAdv;
+    float v = (V[c] + V[c + 1]) * 0.5f * smokeAdv;
+    float x = (float)i * g.h + g.hh + dt * u;
+    float y = (float)j * g.h + g.hh + dt * v;
+    b = sample_field(Fm, x, y, g.hh, g.hh, g);
+  }
+  float o = Mo[c];
+  float raw = o - (b - o) * 0.5f;
+  int src = clamp_source(raw, Mo, c, P);
+  float cm = raw;
+  if (src >= 0) cm = Mo[c + (src - 0x40000000)];
+  if (cm < 0.0f) lam = 0.0f;  // the final max(., 0)
+  if (src >= 0) {
+    if (lam != 0.0f) atomicAdd(&dO[c + (src - 0x40000000)], lam);
+    lamB[c] = 0.0f;
+  } else {
+    if (lam != 0.0f) atomicAdd(&dO[c], 1.5f * lam);
+    lamB[c] = adv ? -0.5f * lam : 0.0f;
+  }
+}
+
+// Adjoint of handleBorders (fluid.go:236-289), in place on (dU, dV): each
+// ghost value was written from interior values or 0.  Thread t reverses the
+// U rows of column i = t (bottom row first: it was written last) and the V
+// columns of row j = t.
+__global__ void k_adj_borders(float* __restrict__ dU, float* __restrict__ dV,
+                              const uint8_t* __restrict__ flags, Grid g) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int P = g.P, NX = g.NX, NY = g.NY;
+  auto fluid = [&](int i, int j) { return (flags[i * P + j] & F_FLUID) != 0; };
+  if (t < NX) {
+    int i = t;
+    float* d = dU + (size_t)i * P;
+    float l = d[NY - 1];
+    d[NY - 1] = 0.0f;
+    if (fluid(i, NY - 1) && fluid(i, NY - 2)) {
+      if (i > 0 && i < NX - 1 && fluid(i, NY - 3)) {
+        d[NY - 2] += 2.0f * l;
+        d[NY - 3] -= l;
+      } else {
+        d[NY - 2] += l;
+      }
+    }
+    l = d[0];
+    d[0] = 0.0f;
+    if (fluid(i, 0) && fluid(i, 1)) {
+      if (i > 0 && i < NX - 1 && fluid(i, 2)) {
+        d[1] += 2.0f * l;
+        d[2] -= l;
+      } else {
+        d[1] += l;
+      }
+    }
+  }
+  if (t < NY) {
+    int j = t;
+    int a = (NX - 1) * P + j, b = (NX - 2) * P + j, cc = (NX - 3) * P + j;
+    float l = dV[a];
+    dV[a] = 0.0f;
+    if (fluid(NX - 1, j) && fluid(NX - 2, j)) {
+      if (j > 0 && j < NY - 1 && fluid(NX - 3, j)) {
+        dV[b] += 2.0f * l;
+        dV[cc] -= l;
+      } else {
+        dV[b] += l;
+      }
+    }
+    l = dV[j];
+    dV[j] = 0.0f;
+    if (fluid(0, j) && fluid(1, j)) {
+      if (j > 0 && j < NY - 1 && fluid(2, j)) {
+        dV[P + j] += 2.0f * l;
+        dV[2 * P + j] -= l;
+      } else {
+        dV[P + j] += l;
+      }
+    }
+  }
+}
+
+// Adjoint of addTurbulence (fluid.go:496-526) at the pre-turbulence field
+// (U2, V2), in place on (dU, dV).
+__global__ void k_adj_turbulence(float* __restrict__ dU, float* __restrict__ dV,
+                                 const float* __restrict__ U2, const float* __restrict__ V2,
+                                 const float2* __restrict__ noise,
+                                 const uint8_t* __restrict__ flags, float turbStrength, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  if (!fluid_interior(flags[c])) return;
+  float u = U2[c], v = V2[c];
+  float r = sqrtf(u * u + v * v);
+  if (!(r > 0.1f)) return;
+  float fp = 0.5f * r < 1.0f ? 0.5f : 0.0f;  // d min(0.5 r, 1) / d r
+  if (fp == 0.0f) return;
+  float2 nz = noise[c];
+  float nu = nz.x * turbStrength, nv = nz.y * turbStrength;
+  float au = u / r, av = v / r;  // d r / d u, d r / d v
+  float lu = dU[c], lv = dV[c];
+  float s = (lu * nu + lv * nv) * fp;
+  dU[c] = lu + s * au;
+  dV[c] = lv + s * av;
+}
+
+// G^T: the adjoint of the gradient subtract with respect to phi, as the
+// Jacobi right-hand side of the adjoint solve: rhs = G^T (dU, dV) on active
+// cells, and bw = w * rhs.
+__global__ void k_adj_grad_t(const float* __restrict__ dU, const float* __restrict__ dV,
+                             const float* __restrict__ W, float* __restrict__ rhs,
+                             float* __restrict__ BW, const uint8_t* __restrict__ flags, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  uint8_t fl = flags[c];
+  float r = 0.0f;
+  if (flag_active(fl)) {
+    r = fbit(fl, F_E) * dU[c + P] - fbit(fl, F_W) * dU[c] + fbit(fl, F_N) * dV[c + 1] -
+        fbit(fl, F_S) * dV[c];
+  }
+  rhs[c] = r;
+  BW[c] = W[c] * r;
+}
+
+// div^T: with b = -div on active cells, d(face) += db(cell on its high side)
+// - db(cell on its low side), db = the adjoint solve's result (0 off active).
+__global__ void k_adj_div_t(float* __restrict__ dU, float* __restrict__ dV,
+                            const float* __restrict__ x0, const float* __restrict__ x1,
+                            const void* __restrict__ ctl_sel, const uint8_t* __restrict__ flags,
+                            Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  const float* db = (*(const int*)ctl_sel) ? x1 : x0;
+  int c = i * P + j;
+  bool act = flag_active(flags[c]);
+  float bc = act ? db[c] : 0.0f;
+  if (i >= 1) {
+    float bl = flag_active(flags[c - P]) ? db[c - P] : 0.0f;
+    dU[c] = dU[c] + (bc - bl);
+  }
+  if (j >= 1) {
+    float bb = flag_active(flags[c - 1]) ? db[c - 1] : 0.0f;
+    dV[c] = dV[c] + (bc - bb);
+  }
+}
+
+// Sources that set U, V (fluid SetVelocity) cut the derivative there.
+__global__ void k_adj_sources(float* __restrict__ dU, float* __restrict__ dV,
+                              const SourceRec* __restrict__ recs, const uint32_t* __restrict__ off,
+                              int n_groups, const uint8_t* __restrict__ flags, Grid g) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_groups) return;
+  uint32_t b = off[k], e = off[k + 1];
+  uint32_t cell = recs[b].cell;
+  int i = (int)(cell / (uint32_t)g.NY), j = (int)(cell % (uint32_t)g.NY);
+  int c = i * g.P + j;
+  bool fluid = (flags[c] & F_FLUID) != 0;
+  bool set = false;
+  for (uint32_t q = b; q < e; ++q) {
+    SourceRec r = recs[q];
+    if ((r.mode & 1u) && !fluid) continue;
+    if (r.mode & 2u) set = true;
+  }
+  if (set) {
+    dU[c] = 0.0f;
+    dV[c] = 0.0f;
+  }
+}
+
+// Loss L = ||M - target||_2 over interior cells: float-pair block rows of
+// sum (M - target)^2, combined later.
+__global__ void k_loss_partials(const float* __restrict__ M, const float* __restrict__ T,
+                                float* __restrict__ part, Grid g) {
+  __shared__ float sh[64];
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  FF v[1] = {{0.0f, 0.0f}};
+  if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2) {
+    int c = i * g.P + j;
+    v[0] = ff_sq(M[c] - T[c]);
+  }
+  block_row<1>(v, 0u, sh, part + 2 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x));
+}
+
+// Seeds the adjoint state with dL/dM = (M - target) / L on interior cells,
+// zero elsewhere and for every other field; stores L.
+__global__ void k_loss_seed(const float* __restrict__ M, const float* __restrict__ T,
+                            const float* __restrict__ row, float* __restrict__ lamM,
+                            float* __restrict__ loss, Grid g) {
+  double L = sqrt((double)row[0] + (double)row[1]);
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i == 0 && j == 0) loss[0] = (float)L;
+  if (i >= g.NX || j >= g.NY) return;
+  int c = i * g.P + j;
+  float v = 0.0f;
+  if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2 && L > 0.0)
+    v = (float)((double)(M[c] - T[c]) / L);
+  lamM[c] = v;
+}
+
+// Start of a step's adjoint: the state after the step holds U5, V5 and M2
+// twice (state and staging copy), so their adjoints add; the staging
+// adjoints restart at zero (they collect the stale reads of the step), as
+// do the work fields that accumulate.
+__global__ void k_adj_begin(float* __restrict__ aU, float* __restrict__ aV, float* __restrict__ aM,
+                            float* __restrict__ aNU, float* __restrict__ aNV,
+                            float* __restrict__ aNM, float* __restrict__ w0,
+                            float* __restrict__ w1, float* __restrict__ w2,
+                            float* __restrict__ w3, float* __restrict__ w4,
+                            float* __restrict__ w5, int n) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  aU[k] = aU[k] + aNU[k];
+  aV[k] = aV[k] + aNV[k];
+  aM[k] = aM[k] + aNM[k];
+  aNU[k] = 0.0f;
+  aNV[k] = 0.0f;
+  aNM[k] = 0.0f;
+  w0[k] = 0.0f;
+  w1[k] = 0.0f;
+  w2[k] = 0.0f;
+  w3[k] = 0.0f;
+  w4[k] = 0.0f;
+  w5[k] = 0.0f;
+}
+
+}  // namespace
+
+cudaError_t launch_loss_seed(fg_fluid* f, const float* target, float* dev_loss) {
+  dim3 gr = cell_grid(f), bl(BX, BY);
+  int nb = gr.x * gr.y;
+  if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
+  count(f);
+  k_loss_partials<<<gr, bl, 0, f->stream>>>(f->d[FG_M], target, f->partials, f->g);
+  float* row = nullptr;
+  count(f, combine_rows<1>(f->stream, f->partials, nb, 0u, &row));
+  count(f);
+  k_loss_seed<<<gr, bl, 0, f->stream>>>(f->d[FG_M], target, row, f->adj[fg_fluid::A_M], dev_loss,
+                                        f->g);
+  size_t bytes = sizeof(float) * (size_t)f->NX * f->P;
+  for (int k : {fg_fluid::A_U, fg_fluid::A_V, fg_fluid::A_NU, fg_fluid::A_NV, fg_fluid::A_NM}) {
+    cudaError_t e = cudaMemsetAsync(f->adj[k], 0, bytes, f->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
+// Adjoint of one recorded step (see the file comment).  On entry adj[A_U..
+// A_NM] hold the adjoint of the state after the step; on exit the adjoint of
+// the state before it, and adj[A_FORCE_U/V] the adjoint of the step's force
+// fields.  tape: the kTapeFields fields recorded by the forward step.
+cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
+  const fg_params& p = f->prm;
+  const Grid& g = f->g;
+  dim3 gr = cell_grid(f), bl(BX, BY);
+  size_t bytes = sizeof(float) * (size_t)f->NX * f->P;
+  float** A = f->adj;
+  using F = fg_fluid;
+  float *U2 = tape[0], *V2 = tape[1], *U4 = tape[2], *V4 = tape[3], *fwdU = tape[4],
+        *fwdV = tape[5], *corrU = tape[6], *corrV = tape[7], *U5 = tape[8], *V5 = tape[9],
+        *M1 = tape[10], *fwdM = tape[11], *corrM = tape[12];
+  cudaStream_t st = f->stream;
+  cudaError_t e;
+  const int n = f->NX * f->P;
+  count(f);
+  k_adj_begin<<<(n + 255) / 256, 256, 0, st>>>(A[F::A_U], A[F::A_V], A[F::A_M], A[F::A_NU],
+                                               A[F::A_NV], A[F::A_NM], A[F::A_CU], A[F::A_CV],
+                                               A[F::A_FU], A[F::A_FV], A[F::A_CM], A[F::A_FM], n);
+  float sa = p.smoke_advection;
+  // ---- smoke (the trace velocity is the final U5, V5)
+  // dU5, dV5 accumulate into A_U, A_V (already holding dU5 from the state).
+  if (p.use_bfecc) {
+    // pass 4: final SL of corrM
+    count(f);
+    k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_M], U5, V5, corrM, A[F::A_U], A[F::A_V], A[F::A_CM],
+                                      A[F::A_NM], f->flags, dt, sa, 0, g);
+    // compensation + clamp: dM1 (orig) and dbwd
+    if ((e = cudaMemsetAsync(A[F::A_M], 0, bytes, st)) != cudaSuccess) return e;
+    count(f);
+    k_adj_bfecc_smoke_correct<<<gr, bl, 0, st>>>(A[F::A_CM], U5, V5, M1, fwdM, A[F::A_BM],
+                                                 A[F::A_M], f->flags, dt, sa, g);
+    // reverse sample of fwdM traced with U5, V5 at +dt
+    count(f);
+    k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_BM], U5, V5, fwdM, A[F::A_U], A[F::A_V], A[F::A_FM],
+                                      nullptr, f->flags, -dt, sa, 1, g);
+    // pass 1: forward SL of M1
+    count(f);
+    k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_FM], U5, V5, M1, A[F::A_U], A[F::A_V], A[F::A_M],
+                                      A[F::A_NM], f->flags, dt, sa, 0, g);
+  } else {
+    // single SL pass of M1: dM2 moves to the zeroed work field, dM1
+    // accumulates in the other
+    std::swap(A[F::A_M], A[F::A_CM]);
+    count(f);
+    k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_CM], U5, V5, M1, A[F::A_U], A[F::A_V], A[F::A_M],
+                                      A[F::A_NM], f->flags, dt, sa, 0, g);
+  }
+  // ---- velocity advection: A_U/A_V hold dU5/dV5; produce dU4 in A_CU..
+  if (p.use_bfecc) {
+    // pass 4: final SL of corr traced with corr: d -> dcorr (A_CU/A_CV)
+    count(f);
+    k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], corrU, corrV, corrU, corrV,
+                                         A[F::A_CU], A[F::A_CV], A[F::A_CU], A[F::A_CV],
+                                         A[F::A_CU], A[F::A_CV], A[F::A_NU], A[F::A_NV], f->flags,
+                                         dt, g);
+    // dU4 accumulates into A_U/A_V (reset first)
+    if ((e = cudaMemsetAsync(A[F::A_U], 0, bytes, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(A[F::A_V], 0, bytes, st)) != cudaSuccess) return e;
+    count(f);
+    k_adj_bfecc_vel_correct<<<gr, bl, 0, st>>>(A[F::A_CU], A[F::A_CV], U4, V4, fwdU, fwdV,
+                                               A[F::A_BU], A[F::A_BV], A[F::A_U], A[F::A_V],
+                                               f->flags, dt, g);
+    // reverse sample of fwd traced with U4 at +dt: dfwd (A_FU/A_FV), dU4
+    count(f);
+    k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_BU], A[F::A_BV], U4, V4, fwdU, fwdV, A[F::A_U],
+                                         A[F::A_V], A[F::A_FU], A[F::A_FV], nullptr, nullptr,
+                                         nullptr, nullptr, f->flags, -dt, g);
+    // pass 1: forward SL of U4 traced with U4
+    count(f);
+    k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_FU], A[F::A_FV], U4, V4, U4, V4, A[F::A_U],
+                                         A[F::A_V], A[F::A_U], A[F::A_V], A[F::A_U], A[F::A_V],
+                                         A[F::A_NU], A[F::A_NV], f->flags, dt, g);
+  } else {
+    std::swap(A[F::A_U], A[F::A_CU]);
+    std::swap(A[F::A_V], A[F::A_CV]);
+    count(f);
+    k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_CU], A[F::A_CV], U4, V4, U4, V4, A[F::A_U],
+                                         A[F::A_V], A[F::A_U], A[F::A_V], A[F::A_U], A[F::A_V],
+                                         A[F::A_NU], A[F::A_NV], f->flags, dt, g);
+  }
+  // ---- borders, turbulence (A_U/A_V: dU4 -> dU3 -> dU2)
+  int nbd = f->NX > f->NY ? f->NX : f->NY;
+  count(f);
+  k_adj_borders<<<(nbd + 127) / 128, 128, 0, st>>>(A[F::A_U], A[F::A_V], f->flags, g);
+  if (p.turbulence_strength > 0.0f) {
+    count(f);
+    k_adj_turbulence<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], U2, V2, f->noise, f->flags,
+                                        p.turbulence_strength * dt, g);
+  }
+  // ---- projection: dU1 = dU2 + div^T P_K G^T dU2
+  count(f);
+  k_adj_grad_t<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], f->wgt, f->rhs, f->bw, f->flags, g);
+  if (p.num_iters > 0) {
+    if ((e = launch_jacobi_solve(f, f->ectl, f->rhs, f->bw, f->phi, f->phi2, p.num_iters)) !=
+        cudaSuccess)
+      return e;
+  } else {
+    if ((e = cudaMemsetAsync(f->phi, 0, bytes, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(f->ectl, 0, sizeof(int) * 8, st)) != cudaSuccess) return e;
+  }
+  count(f);
+  k_adj_div_t<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], f->phi, f->phi2,
+                                 (const int*)f->ectl + 1, f->flags, g);
+  // ---- sources (the forces' adjoint is then the state's)
+  if (f->n_src_groups > 0) {
+    count(f);
+    k_adj_sources<<<(f->n_src_groups + 255) / 256, 256, 0, st>>>(
+        A[F::A_U], A[F::A_V], f->src_dev, f->src_off_dev, f->n_src_groups, f->flags, g);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add_forces(fg_fluid* f, const float* fu, const float* fv) {
+  count(f);
+  k_add_forces<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], fu, fv, f->g);
+  return cudaGetLastError();
+}
+
+}  // namespace fg

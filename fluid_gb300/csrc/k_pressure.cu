@@ -696,6 +696,11 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
   return cudaGetLastError();
 }
 
+cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const float* bw, float* x0,
+                                float* x1, int iters) {
+  return jacobi_solve(f, (PCtl*)ctl, b, bw, x0, x1, iters, false);
+}
+
 cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb) {
   float cp = f->density * f->h / dt;  // fluid.go:158
   cudaError_t e;

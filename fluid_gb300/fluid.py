@@ -330,6 +330,91 @@ class Fluid:
             self._check(n, "fg_profile_stages")
         return [(names[k].decode(), ms[k]) for k in range(n)]
 
+    # ------------------------------------------------------------ differentiable rollouts
+    # The Step / StepAdjoint pair of include/fluidgpu.h.  Fields (forces,
+    # seeds, targets, gradients) are numpy float32 arrays of numCells values
+    # in the mirrors' layout, or float32 torch tensors of that size (host or
+    # device memory).  During a recorded rollout the mirrors are not kept in
+    # sync: call download() to read the state.
+    def _field_ptr(self, x, writable=False):
+        if x is None:
+            return None
+        if isinstance(x, np.ndarray):
+            if x.dtype != np.float32 or x.size != self.numCells or not x.flags.c_contiguous:
+                raise ValueError("expected a contiguous float32 array of %d values" % self.numCells)
+            if writable and not x.flags.writeable:
+                raise ValueError("output array is read-only")
+            return x.ctypes.data
+        if hasattr(x, "data_ptr"):
+            import torch
+
+            if x.dtype != torch.float32 or x.numel() != self.numCells or not x.is_contiguous():
+                raise ValueError("expected a contiguous float32 tensor of %d values" % self.numCells)
+            return x.data_ptr()
+        raise TypeError("expected a numpy array or a torch tensor")
+
+    def tape_begin(self, max_steps, every=8):
+        """Starts a recorded rollout from the current state (fg_tape_begin)."""
+        self._before()
+        self._check(self._L.fg_tape_begin(self._h, int(max_steps), int(every)), "fg_tape_begin")
+
+    def step_forward(self, dt, force_u=None, force_v=None):
+        """One recorded step with an optional force field (fg_step_forward)."""
+        self._check(self._L.fg_step_forward(self._h, ctypes.c_float(dt), self._field_ptr(force_u),
+                                            self._field_ptr(force_v)), "fg_step_forward")
+
+    def tape_seed(self, dU=None, dV=None, dM=None):
+        self._check(self._L.fg_tape_seed(self._h, self._field_ptr(dU), self._field_ptr(dV),
+                                         self._field_ptr(dM)), "fg_tape_seed")
+
+    def tape_seed_smoke_l2(self, target):
+        """Seeds dL/dM for L = ||M - target||_2 over the interior; returns L."""
+        loss = ctypes.c_float()
+        self._check(self._L.fg_tape_seed_smoke_l2(self._h, self._field_ptr(target),
+                                                  ctypes.byref(loss)), "fg_tape_seed_smoke_l2")
+        return loss.value
+
+    def step_adjoint(self, grad_force_u=None, grad_force_v=None):
+        """Reverses the latest step; writes that step's force gradient if given."""
+        self._check(self._L.fg_step_adjoint(self._h, self._field_ptr(grad_force_u, True),
+                                            self._field_ptr(grad_force_v, True)), "fg_step_adjoint")
+
+    def tape_grad(self):
+        """dL/d(initial U, V, M, newU, newV, newM) as numpy arrays."""
+        out = [np.zeros(self.numCells, np.float32) for _ in range(6)]
+        self._check(self._L.fg_tape_grad(self._h, *[o.ctypes.data for o in out]), "fg_tape_grad")
+        return dict(zip(("U", "V", "M", "newU", "newV", "newM"), out))
+
+    def tape_steps(self):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self._check(self._L.fg_tape_steps(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def tape_end(self):
+        self._check(self._L.fg_tape_end(self._h), "fg_tape_end")
+
+    def rollout_grad(self, dt, steps, target, forces=None, every=8):
+        """Loss L = ||M_T - target||_2 after `steps` steps from the current
+        state with per-step forces (a list of (force_u, force_v) or None), and
+        its gradients: {"loss", "U", "V", "M", "newU", "newV", "newM",
+        "force_u": [steps arrays], "force_v": [...]}.  The state ends where
+        the forward pass ended."""
+        self.tape_begin(steps, every)
+        try:
+            for t in range(steps):
+                fu, fv = forces[t] if forces is not None else (None, None)
+                self.step_forward(dt, fu, fv)
+            loss = self.tape_seed_smoke_l2(target)
+            gfu = [np.zeros(self.numCells, np.float32) for _ in range(steps)]
+            gfv = [np.zeros(self.numCells, np.float32) for _ in range(steps)]
+            for t in reversed(range(steps)):
+                self.step_adjoint(gfu[t], gfv[t])
+            out = self.tape_grad()
+        finally:
+            self.tape_end()
+        out.update(loss=loss, force_u=gfu, force_v=gfv)
+        return out
+
     def Reset(self):
         self._check(self._L.fg_reset(self._h), "Reset")
 

@@ -224,6 +224,45 @@ int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x, 
                        float jacobi_omega, float pressure_damping, int tb_depth, int early_exit,
                        float tolerance, void* stream);
 
+/* Differentiable rollouts: a Step / StepAdjoint pair standing in for an
+ * autograd Function (no counterpart in the reference, which has no
+ * derivatives; the forward step is fg_simulate's, fluid.go:79-109).
+ *
+ * fg_tape_begin(f, max_steps, every) starts a recorded rollout from the
+ * current state and saves it as the first checkpoint.  It needs the JACOBI
+ * scheme with early_exit 0, refine_sweeps 0, viscosity_diffusion 0 and
+ * confinement 0 (else FG_ERR_UNSUPPORTED); the parameters, the sources and
+ * the state must not change until fg_tape_end (else FG_ERR_INVALID).
+ *
+ * fg_step_forward(f, dt, force_u, force_v) runs one step with the force
+ * field (force_u, force_v) added to U, V before the sources (both NULL: no
+ * force).  Every `every` steps the state is checkpointed on the device.
+ *
+ * fg_tape_seed sets the adjoint of the final state (dL/dU, dL/dV, dL/dM;
+ * NULL = zero); fg_tape_seed_smoke_l2 sets it for L = ||M - target||_2 over
+ * the interior cells and returns L.
+ *
+ * fg_step_adjoint reverses the latest step not yet reversed: the adjoint
+ * becomes that of the state before the step, and dL/d(force_u, force_v) of
+ * that step is written to grad_force_u / grad_force_v (NULL: skipped).  The
+ * steps of a checkpoint interval are recomputed from its checkpoint when the
+ * interval is first reversed.  After the last step is reversed the handle's
+ * state is back at the end of the forward pass, and fg_tape_grad returns
+ * dL/d(initial U, V, M, newU, newV, newM).
+ *
+ * All fields (forces, seeds, target, gradients) use the mirrors' layout
+ * (NumX * NumY floats, index i*NumY + j) in host or device memory.  Adjoint
+ * advection scatters with FP32 atomics: gradients reproduce to about 1e-6
+ * relative, not bit for bit. */
+int fg_tape_begin(fg_fluid* f, int max_steps, int every);
+int fg_step_forward(fg_fluid* f, float dt, const float* force_u, const float* force_v);
+int fg_tape_seed(fg_fluid* f, const float* dU, const float* dV, const float* dM);
+int fg_tape_seed_smoke_l2(fg_fluid* f, const float* target, float* loss);
+int fg_step_adjoint(fg_fluid* f, float* grad_force_u, float* grad_force_v);
+int fg_tape_grad(fg_fluid* f, float* dU, float* dV, float* dM, float* dNU, float* dNV, float* dNM);
+int fg_tape_steps(const fg_fluid* f, int* forward, int* reversed);
+int fg_tape_end(fg_fluid* f);
+
 /* Text of the last error on the handle ("" if none); static text for a
  * NULL handle. */
 const char* fg_last_error(const fg_fluid* f);
