@@ -987,11 +987,16 @@ const char* fg_last_error(const fg_fluid* f) {
 // not yet reversed.  Reversing a step needs the intermediates of its forward
 // pass: the steps of one checkpoint interval are recomputed from their
 // checkpoint, recording them (the last interval is recorded during the
-// forward pass itself), so memory is one interval of records plus the
-// checkpoints.  When the last step has been reversed, the handle's state is
-// restored to the end of the forward pass.
+// forward pass itself).  The forward pass also keeps each step's pressure
+// potential (one field per step), so a recomputed step replays the gradient
+// subtract instead of repeating the Jacobi solve.  Memory: one interval of
+// records, the checkpoints, the potentials and the forces; the buffers are
+// kept for the next rollout until the handle is destroyed.  When the last
+// step has been reversed, the handle's state is restored to the end of the
+// forward pass.
 // ===========================================================================
 struct Tape {
+  bool active = false;
   int max_steps = 0, every = 0;
   int n_fwd = 0, n_rev = 0;
   int n_ckpt = 0;
@@ -1001,9 +1006,12 @@ struct Tape {
   uint64_t version = 0;
   std::vector<float> dts;
   std::vector<char> has_force;
-  float* forces = nullptr;  // max_steps x {Fu, Fv}
-  float* ckpt = nullptr;    // (n_ckpt + 1) x {U, V, M, newU, newV, newM}; the last is the final state
-  float* rec = nullptr;     // every x kTapeFields
+  // Capacity of the buffers (steps, record slots, checkpoint slots).
+  int cap_steps = 0, cap_every = 0, cap_ckpt = 0;
+  float* forces = nullptr;  // cap_steps x {Fu, Fv}
+  float* phis = nullptr;    // cap_steps potentials
+  float* ckpt = nullptr;    // cap_ckpt x {U, V, M, newU, newV, newM}; slot n_ckpt: the final state
+  float* rec = nullptr;     // cap_every x kTapeFields
   float* aux = nullptr;     // loss target
 };
 
@@ -1017,6 +1025,7 @@ void tape_free(fg_fluid* f) {
   if (!f->tape) return;
   cudaStreamSynchronize(f->stream);
   cudaFree(f->tape->forces);
+  cudaFree(f->tape->phis);
   cudaFree(f->tape->ckpt);
   cudaFree(f->tape->rec);
   cudaFree(f->tape->aux);
@@ -1080,16 +1089,24 @@ int get_field(fg_fluid* f, float* dst, const float* dev) {
 // intermediates the adjoint reads written to `rec` (kTapeFields fields:
 // U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM corrM).  The BFECC
 // intermediates are produced in place: the scratch pointers are redirected
-// to the record for the step.
-int enqueue_step_record(fg_fluid* f, float dt, const float* fu, const float* fv, float* rec) {
+// to the record for the step.  The pressure potential is stored to `phi`
+// (replay = false) or, on a replay of a step already run, read from it in
+// place of the solve; both give the same bits.
+int enqueue_step_record(fg_fluid* f, float dt, const float* fu, const float* fv, float* rec,
+                        float* phi, bool replay) {
   const fg_params& p = f->prm;
   const size_t n = field_elems(f);
   auto R = [&](int k) { return rec + (size_t)k * n; };
   int rc;
   if (fu) CK(f, launch_add_forces(f, fu, fv), "forces");
   CK(f, launch_apply_sources(f), "sources");
-  CK(f, launch_clear_stats(f), "clear stats");
-  if ((rc = enqueue_pressure(f, p.num_iters, dt, false))) return rc;
+  if (replay) {
+    CK(f, launch_grad_replay(f, dt, phi), "gradient replay");
+  } else {
+    CK(f, launch_clear_stats(f), "clear stats");
+    if ((rc = enqueue_pressure(f, p.num_iters, dt, false))) return rc;
+    CK(f, launch_store_phi(f, phi), "store potential");
+  }
   if (p.turbulence_strength > 0.0f) {
     if ((rc = copy_field(f, R(0), f->d[FG_U])) || (rc = copy_field(f, R(1), f->d[FG_V]))) return rc;
     CK(f, launch_confinement_turbulence(f, dt, false, true), "turbulence");
@@ -1124,7 +1141,7 @@ int enqueue_step_record(fg_fluid* f, float dt, const float* fu, const float* fv,
 
 int tape_usable(fg_fluid* f) {
   Tape* t = f->tape;
-  if (!t) return fail(f, FG_ERR_INVALID, "no recorded rollout (fg_tape_begin)");
+  if (!t || !t->active) return fail(f, FG_ERR_INVALID, "no recorded rollout (fg_tape_begin)");
   if (t->version != f->params_version)
     return fail(f, FG_ERR_INVALID, "parameters or sources changed during a recorded rollout");
   if (!f->edits.empty() || f->dirty || f->masks_stale)
@@ -1137,6 +1154,7 @@ float* rec_at(fg_fluid* f, int k) { return f->tape->rec + (size_t)k * kTapeField
 float* force_at(fg_fluid* f, int t, int c) {
   return f->tape->forces + ((size_t)t * 2 + c) * field_elems(f);
 }
+float* phi_at(fg_fluid* f, int t) { return f->tape->phis + (size_t)t * field_elems(f); }
 
 // Recomputes the steps of interval s from its checkpoint, recording them.
 int tape_load_interval(fg_fluid* f, int s) {
@@ -1147,7 +1165,8 @@ int tape_load_interval(fg_fluid* f, int s) {
   for (int k = s * t->every; k < t1; ++k) {
     bool hf = t->has_force[k] != 0;
     rc = enqueue_step_record(f, t->dts[k], hf ? force_at(f, k, 0) : nullptr,
-                             hf ? force_at(f, k, 1) : nullptr, rec_at(f, k - s * t->every));
+                             hf ? force_at(f, k, 1) : nullptr, rec_at(f, k - s * t->every),
+                             phi_at(f, k), true);
     if (rc) return rc;
   }
   t->seg_loaded = s;
@@ -1164,31 +1183,46 @@ int fg_tape_begin(fg_fluid* f, int max_steps, int every) {
   if (rc) return rc;
   if ((rc = tape_supported(f))) return rc;
   if ((rc = check_iters(f, f->prm.num_iters))) return rc;
-  tape_free(f);
   for (int k = 0; k < fg_fluid::A_COUNT; ++k)
     if (!f->adj[k] && (rc = alloc_dev(f, &f->adj[k]))) return rc;
-  Tape* t = new Tape();
-  f->tape = t;
+  every = std::min(every, max_steps);
+  int n_ckpt = (max_steps + every - 1) / every;
+  Tape* t = f->tape;
+  if (t && (t->cap_steps < max_steps || t->cap_every < every || t->cap_ckpt < n_ckpt + 1)) {
+    tape_free(f);
+    t = nullptr;
+  }
+  if (!t) {
+    t = new Tape();
+    f->tape = t;
+    t->cap_steps = max_steps;
+    t->cap_every = every;
+    t->cap_ckpt = n_ckpt + 1;
+    size_t fb = field_bytes(f);
+    cudaError_t e;
+    if ((e = cudaMalloc((void**)&t->forces, fb * 2 * max_steps)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&t->phis, fb * max_steps)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&t->ckpt, fb * 6 * t->cap_ckpt)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&t->rec, fb * kTapeFields * every)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&t->aux, fb)) != cudaSuccess) {
+      tape_free(f);
+      return fail(f, FG_ERR_NOMEM, "tape allocation", e);
+    }
+    // Record fields a step leaves unwritten (U2, V2 without turbulence) and
+    // the padding columns stay zero.
+    CK(f, cudaMemsetAsync(t->rec, 0, fb * kTapeFields * every, f->stream), "tape");
+    CK(f, cudaMemsetAsync(t->aux, 0, fb, f->stream), "tape");
+  }
+  t->active = true;
   t->max_steps = max_steps;
-  t->every = std::min(every, max_steps);
-  t->n_ckpt = (max_steps + t->every - 1) / t->every;
+  t->every = every;
+  t->n_ckpt = n_ckpt;
+  t->n_fwd = t->n_rev = 0;
+  t->seg_loaded = -1;
+  t->seeded = t->final_saved = false;
   t->version = f->params_version;
   t->dts.assign(max_steps, 0.0f);
   t->has_force.assign(max_steps, 0);
-  size_t fb = field_bytes(f);
-  cudaError_t e;
-  if ((e = cudaMalloc((void**)&t->forces, fb * 2 * max_steps)) != cudaSuccess ||
-      (e = cudaMalloc((void**)&t->ckpt, fb * 6 * (t->n_ckpt + 1))) != cudaSuccess ||
-      (e = cudaMalloc((void**)&t->rec, fb * kTapeFields * t->every)) != cudaSuccess ||
-      (e = cudaMalloc((void**)&t->aux, fb)) != cudaSuccess) {
-    tape_free(f);
-    return fail(f, FG_ERR_NOMEM, "tape allocation", e);
-  }
-  // Record fields a step leaves unwritten (U2, V2 without turbulence) and
-  // the padding columns stay zero.
-  CK(f, cudaMemsetAsync(t->rec, 0, fb * kTapeFields * t->every, f->stream), "tape");
-  CK(f, cudaMemsetAsync(t->forces, 0, fb * 2 * max_steps, f->stream), "tape");
-  CK(f, cudaMemsetAsync(t->aux, 0, fb, f->stream), "tape");
   return save_state(f, ckpt_at(f, 0));
 }
 
@@ -1197,12 +1231,13 @@ int fg_tape_end(fg_fluid* f) {
   int rc = bind(f);
   if (rc) return rc;
   Tape* t = f->tape;
-  if (t && t->final_saved && t->n_rev < t->n_fwd) {
+  if (!t || !t->active) return FG_OK;
+  if (t->final_saved && t->n_rev < t->n_fwd) {
     // Abandoned mid-reverse: put the end-of-rollout state back.
     if ((rc = load_state(f, ckpt_at(f, t->n_ckpt)))) return rc;
     invalidate(f, kStepFields);
   }
-  tape_free(f);
+  t->active = false;
   return FG_OK;
 }
 
@@ -1225,7 +1260,8 @@ int fg_step_forward(fg_fluid* f, float dt, const float* force_u, const float* fo
   }
   invalidate(f, kStepFields);
   rc = enqueue_step_record(f, dt, force_u ? force_at(f, k, 0) : nullptr,
-                           force_u ? force_at(f, k, 1) : nullptr, rec_at(f, k % t->every));
+                           force_u ? force_at(f, k, 1) : nullptr, rec_at(f, k % t->every),
+                           phi_at(f, k), false);
   if (rc) return rc;
   t->dts[k] = dt;
   t->has_force[k] = force_u ? 1 : 0;
@@ -1306,7 +1342,8 @@ int fg_tape_grad(fg_fluid* f, float* dU, float* dV, float* dM, float* dNU, float
   if (!f) return FG_ERR_INVALID;
   int rc = bind(f);
   if (rc) return rc;
-  if (!f->tape || !f->tape->seeded) return fail(f, FG_ERR_INVALID, "no seeded rollout");
+  if (!f->tape || !f->tape->active || !f->tape->seeded)
+    return fail(f, FG_ERR_INVALID, "no seeded rollout");
   float* out[6] = {dU, dV, dM, dNU, dNV, dNM};
   const int src[6] = {fg_fluid::A_U, fg_fluid::A_V, fg_fluid::A_M,
                       fg_fluid::A_NU, fg_fluid::A_NV, fg_fluid::A_NM};
@@ -1318,8 +1355,9 @@ int fg_tape_grad(fg_fluid* f, float* dU, float* dV, float* dM, float* dNU, float
 
 int fg_tape_steps(const fg_fluid* f, int* forward, int* reversed) {
   if (!f || !forward || !reversed) return FG_ERR_INVALID;
-  *forward = f->tape ? f->tape->n_fwd : 0;
-  *reversed = f->tape ? f->tape->n_rev : 0;
+  bool on = f->tape && f->tape->active;
+  *forward = on ? f->tape->n_fwd : 0;
+  *reversed = on ? f->tape->n_rev : 0;
   return FG_OK;
 }
 

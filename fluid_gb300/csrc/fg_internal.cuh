@@ -177,7 +177,7 @@ struct fg_fluid {
   // Differentiable rollouts: the adjoint of the state (U, V, M and the
   // staging fields) and the adjoint work fields, allocated by the first
   // recorded rollout; the rollout's tape (fg_api.cu).
-  enum { A_U, A_V, A_M, A_NU, A_NV, A_NM, A_CU, A_CV, A_FU, A_FV, A_BU, A_BV, A_CM, A_FM, A_BM,
+  enum { A_U, A_V, A_M, A_NU, A_NV, A_NM, A_CU, A_CV, A_FU, A_FV, A_CM, A_FM,
          A_COUNT };
   float* adj[A_COUNT] = {};
   struct Tape* tape = nullptr;
@@ -235,6 +235,10 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
 // buffer holding x.
 cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const float* bw, float* x0,
                                 float* x1, int iters);
+// Copies the last solve's potential to dst.
+cudaError_t launch_store_phi(fg_fluid* f, float* dst);
+// Gradient subtract with a stored potential (a recorded step's replay).
+cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi);
 // k_adjoint.cu
 constexpr int kTapeFields = 13;  // U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM corrM
 cudaError_t launch_add_forces(fg_fluid* f, const float* fu, const float* fv);

@@ -182,17 +182,16 @@ __device__ __forceinline__ int clamp_source(float val, const float* __restrict__
   return -1;
 }
 
-// Adjoint of BFECC's compensation + clamp for velocity (fluid.go:968-987):
-// corr = clamp(o - (bwd - o) * 0.5) on interior faces, corr = o on the ring.
-// Reads lamC (adjoint of corr); writes lamB (adjoint of bwd, 0 where bwd is
-// the constant 0 of a non-advected face) and accumulates into dO.
-__global__ void k_adj_bfecc_vel_correct(const float* __restrict__ lamCu,
-                                        const float* __restrict__ lamCv,
-                                        const float* __restrict__ Ou, const float* __restrict__ Ov,
-                                        const float* __restrict__ Fu, const float* __restrict__ Fv,
-                                        float* __restrict__ lamBu, float* __restrict__ lamBv,
-                                        float* dOu, float* dOv, const uint8_t* __restrict__ flags,
-                                        float dt, Grid g) {
+// Adjoint of BFECC's passes 2-3 for velocity (fluid.go:931-987), fused:
+// bwd = sample(fwd; trace with (Ou, Ov) at -dt) on advected interior faces
+// (0 on the others), corr = clamp(o - (bwd - o) * 0.5) on interior faces,
+// corr = o on the ring.  Reads lamC (adjoint of corr); accumulates into dO
+// (the original field, which is also the tracing velocity) and dF (fwd).
+__global__ void k_adj_bfecc_vel(const float* __restrict__ lamCu, const float* __restrict__ lamCv,
+                                const float* __restrict__ Ou, const float* __restrict__ Ov,
+                                const float* __restrict__ Fu, const float* __restrict__ Fv,
+                                float* dOu, float* dOv, float* dFu, float* dFv,
+                                const uint8_t* __restrict__ flags, float dt, Grid g) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
@@ -200,54 +199,68 @@ __global__ void k_adj_bfecc_vel_correct(const float* __restrict__ lamCu,
   int c = i * P + j;
   float lu = lamCu[c], lv = lamCv[c];
   if (on_ring(i, j, g)) {
-    lamBu[c] = 0.0f;
-    lamBv[c] = 0.0f;
     if (lu != 0.0f) atomicAdd(&dOu[c], lu);
     if (lv != 0.0f) atomicAdd(&dOv[c], lv);
     return;
   }
   uint8_t fl = flags[c];
-  // Recompute bwd and the raw compensated value (as k_bfecc_vel_correct).
+#pragma unroll
   for (int comp = 0; comp < 2; ++comp) {
     const float* O = comp == 0 ? Ou : Ov;
     const float* F = comp == 0 ? Fu : Fv;
+    float* dO = comp == 0 ? dOu : dOv;
     float lam = comp == 0 ? lu : lv;
     bool adv = comp == 0 ? u_advected(fl, i, j, g) : v_advected(fl, i, j, g);
-    float b = 0.0f;
+    float x = 0.0f, y = 0.0f, dx = 0.0f, dy = 0.0f, b = 0.0f;
     if (adv) {
-      float x, y, dx, dy;
+      // The reverse trace of trace_sample_u / _v with sdt = -dt.
       if (comp == 0) {
-        x = (float)i * g.h;
-        y = (float)j * g.h + g.hh;
         float u = Ou[c];
         float v = (Ov[c - P] + Ov[c] + Ov[c - P + 1] + Ov[c + 1]) * 0.25f;
-        x = x + dt * u;
-        y = y + dt * v;
-        dx = 0.0f;
+        x = (float)i * g.h + dt * u;
+        y = ((float)j * g.h + g.hh) + dt * v;
         dy = g.hh;
       } else {
-        x = (float)i * g.h + g.hh;
-        y = (float)j * g.h;
         float u = (Ou[c - 1] + Ou[c] + Ou[c + P - 1] + Ou[c + P]) * 0.25f;
         float v = Ov[c];
-        x = x + dt * u;
-        y = y + dt * v;
+        x = ((float)i * g.h + g.hh) + dt * u;
+        y = (float)j * g.h + dt * v;
         dx = g.hh;
-        dy = 0.0f;
       }
       b = sample_field(F, x, y, dx, dy, g);
     }
     float o = O[c];
     float raw = o - (b - o) * 0.5f;
     int src = clamp_source(raw, O, c, P);
-    float* dO = comp == 0 ? dOu : dOv;
-    float* lamB = comp == 0 ? lamBu : lamBv;
     if (src >= 0) {
       if (lam != 0.0f) atomicAdd(&dO[c + (src - 0x40000000)], lam);
-      lamB[c] = 0.0f;
+      continue;
+    }
+    if (lam == 0.0f) continue;
+    atomicAdd(&dO[c], 1.5f * lam);
+    if (!adv) continue;
+    float lb = -0.5f * lam;  // adjoint of bwd
+    float gx, gy;
+    sample_adjoint(F, comp == 0 ? dFu : dFv, x, y, dx, dy, lb, g, &gx, &gy);
+    float du = dt * gx * lb, dv = dt * gy * lb;
+    if (comp == 0) {
+      if (du != 0.0f) atomicAdd(&dOu[c], du);
+      if (dv != 0.0f) {
+        float q = 0.25f * dv;
+        atomicAdd(&dOv[c - P], q);
+        atomicAdd(&dOv[c], q);
+        atomicAdd(&dOv[c - P + 1], q);
+        atomicAdd(&dOv[c + 1], q);
+      }
     } else {
-      if (lam != 0.0f) atomicAdd(&dO[c], 1.5f * lam);
-      lamB[c] = adv ? -0.5f * lam : 0.0f;
+      if (dv != 0.0f) atomicAdd(&dOv[c], dv);
+      if (du != 0.0f) {
+        float q = 0.25f * du;
+        atomicAdd(&dOu[c - 1], q);
+        atomicAdd(&dOu[c], q);
+        atomicAdd(&dOu[c + P - 1], q);
+        atomicAdd(&dOu[c + P], q);
+      }
     }
   }
 }
@@ -300,15 +313,16 @@ __global__ void k_adj_sl_smoke(const float* __restrict__ lamM, const float* __re
   }
 }
 
-// Adjoint of BFECC's smoke compensation (fluid.go:1029-1046): corr =
-// clamp(o - (bwd - o) * 0.5), then max(corr, 0), on interior cells; o on the
-// ring.  Writes lamB, accumulates into dO.
-__global__ void k_adj_bfecc_smoke_correct(const float* __restrict__ lamC,
-                                          const float* __restrict__ U, const float* __restrict__ V,
-                                          const float* __restrict__ Mo, const float* __restrict__ Fm,
-                                          float* __restrict__ lamB, float* dO,
-                                          const uint8_t* __restrict__ flags, float dt,
-                                          float smokeAdv, Grid g) {
+// Adjoint of BFECC's smoke passes 2-3 (fluid.go:1013-1046), fused: bwd =
+// sample(fwd; trace with (U, V) at -dt) on fluid interior cells (0 on the
+// others), corr = max(clamp(o - (bwd - o) * 0.5), 0) on interior cells, o on
+// the ring.  Reads lamC; accumulates into dO (original smoke), dF (fwd) and
+// dU, dV (the tracing velocity).
+__global__ void k_adj_bfecc_smoke(const float* __restrict__ lamC, const float* __restrict__ U,
+                                  const float* __restrict__ V, const float* __restrict__ Mo,
+                                  const float* __restrict__ Fm, float* dO, float* dF, float* dU,
+                                  float* dV, const uint8_t* __restrict__ flags, float dt,
+                                  float smokeAdv, Grid g) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
@@ -316,32 +330,41 @@ __global__ void k_adj_bfecc_smoke_correct(const float* __restrict__ lamC,
   int c = i * P + j;
   float lam = lamC[c];
   if (on_ring(i, j, g)) {
-    lamB[c] = 0.0f;
     if (lam != 0.0f) atomicAdd(&dO[c], lam);
     return;
   }
   uint8_t fl = flags[c];
-  float b = 0.0f;
   bool adv = (fl & F_FLUID) != 0;
+  float b = 0.0f, x = 0.0f, y = 0.0f;
   if (adv) {
     float u = (U[c] + U[c + P]) * 0.5f * smokeAdv;
     float v = (V[c] + V[c + 1]) * 0.5f * smokeAdv;
-    float x = (float)i * g.h + g.hh + dt * u;
-    float y = (float)j * g.h + g.hh + dt * v;
+    x = (float)i * g.h + g.hh + dt * u;
+    y = (float)j * g.h + g.hh + dt * v;
     b = sample_field(Fm, x, y, g.hh, g.hh, g);
   }
   float o = Mo[c];
   float raw = o - (b - o) * 0.5f;
   int src = clamp_source(raw, Mo, c, P);
-  float cm = raw;
-  if (src >= 0) cm = Mo[c + (src - 0x40000000)];
-  if (cm < 0.0f) lam = 0.0f;  // the final max(., 0)
+  float cm = src >= 0 ? Mo[c + (src - 0x40000000)] : raw;
+  if (cm < 0.0f || lam == 0.0f) return;  // the final max(., 0) passes nothing
   if (src >= 0) {
-    if (lam != 0.0f) atomicAdd(&dO[c + (src - 0x40000000)], lam);
-    lamB[c] = 0.0f;
-  } else {
-    if (lam != 0.0f) atomicAdd(&dO[c], 1.5f * lam);
-    lamB[c] = adv ? -0.5f * lam : 0.0f;
+    atomicAdd(&dO[c + (src - 0x40000000)], lam);
+    return;
+  }
+  atomicAdd(&dO[c], 1.5f * lam);
+  if (!adv) return;
+  float lb = -0.5f * lam;
+  float gx, gy;
+  sample_adjoint(Fm, dF, x, y, g.hh, g.hh, lb, g, &gx, &gy);
+  float du = dt * gx * lb * 0.5f * smokeAdv, dv = dt * gy * lb * 0.5f * smokeAdv;
+  if (du != 0.0f) {
+    atomicAdd(&dU[c], du);
+    atomicAdd(&dU[c + P], du);
+  }
+  if (dv != 0.0f) {
+    atomicAdd(&dV[c], dv);
+    atomicAdd(&dV[c + 1], dv);
   }
 }
 
@@ -605,15 +628,12 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
     count(f);
     k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_M], U5, V5, corrM, A[F::A_U], A[F::A_V], A[F::A_CM],
                                       A[F::A_NM], f->flags, dt, sa, 0, g);
-    // compensation + clamp: dM1 (orig) and dbwd
+    // compensation + clamp and the reverse sample of fwdM traced with U5,
+    // V5 at +dt: dM1 (orig), dfwdM, dU5
     if ((e = cudaMemsetAsync(A[F::A_M], 0, bytes, st)) != cudaSuccess) return e;
     count(f);
-    k_adj_bfecc_smoke_correct<<<gr, bl, 0, st>>>(A[F::A_CM], U5, V5, M1, fwdM, A[F::A_BM],
-                                                 A[F::A_M], f->flags, dt, sa, g);
-    // reverse sample of fwdM traced with U5, V5 at +dt
-    count(f);
-    k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_BM], U5, V5, fwdM, A[F::A_U], A[F::A_V], A[F::A_FM],
-                                      nullptr, f->flags, -dt, sa, 1, g);
+    k_adj_bfecc_smoke<<<gr, bl, 0, st>>>(A[F::A_CM], U5, V5, M1, fwdM, A[F::A_M], A[F::A_FM],
+                                         A[F::A_U], A[F::A_V], f->flags, dt, sa, g);
     // pass 1: forward SL of M1
     count(f);
     k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_FM], U5, V5, M1, A[F::A_U], A[F::A_V], A[F::A_M],
@@ -634,18 +654,13 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
                                          A[F::A_CU], A[F::A_CV], A[F::A_CU], A[F::A_CV],
                                          A[F::A_CU], A[F::A_CV], A[F::A_NU], A[F::A_NV], f->flags,
                                          dt, g);
-    // dU4 accumulates into A_U/A_V (reset first)
+    // dU4 accumulates into A_U/A_V (reset first); compensation + clamp and
+    // the reverse sample of fwd traced with U4 at +dt: dfwd (A_FU/A_FV), dU4
     if ((e = cudaMemsetAsync(A[F::A_U], 0, bytes, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(A[F::A_V], 0, bytes, st)) != cudaSuccess) return e;
     count(f);
-    k_adj_bfecc_vel_correct<<<gr, bl, 0, st>>>(A[F::A_CU], A[F::A_CV], U4, V4, fwdU, fwdV,
-                                               A[F::A_BU], A[F::A_BV], A[F::A_U], A[F::A_V],
-                                               f->flags, dt, g);
-    // reverse sample of fwd traced with U4 at +dt: dfwd (A_FU/A_FV), dU4
-    count(f);
-    k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_BU], A[F::A_BV], U4, V4, fwdU, fwdV, A[F::A_U],
-                                         A[F::A_V], A[F::A_FU], A[F::A_FV], nullptr, nullptr,
-                                         nullptr, nullptr, f->flags, -dt, g);
+    k_adj_bfecc_vel<<<gr, bl, 0, st>>>(A[F::A_CU], A[F::A_CV], U4, V4, fwdU, fwdV, A[F::A_U],
+                                       A[F::A_V], A[F::A_FU], A[F::A_FV], f->flags, dt, g);
     // pass 1: forward SL of U4 traced with U4
     count(f);
     k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_FU], A[F::A_FV], U4, V4, U4, V4, A[F::A_U],

@@ -596,6 +596,14 @@ __global__ void __launch_bounds__(256)
   block_row<5, 0x4u>(row, 0x12u, shr, part + 10 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x));
 }
 
+// Copies the solve's final potential (the buffer the control block names).
+__global__ void k_store_phi(const float* __restrict__ phi0, const float* __restrict__ phi1,
+                            const PCtl* __restrict__ ctl, float* __restrict__ dst, int n) {
+  const float* src = ctl->sel ? phi1 : phi0;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = src[k];
+}
+
 __global__ void k_store_div_p(const float* __restrict__ r, DevStats* st) {
   st->div_l2_sq = row_sum(r, 0);
   st->div_max = (double)r[2];
@@ -749,6 +757,29 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   float* out = nullptr;
   count(f, combine_rows<5>(f->stream, f->partials, nb, 0x12u, &out));
   k_store_div_p<<<1, 1, 0, f->stream>>>(out, f->dstats);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_store_phi(fg_fluid* f, float* dst) {
+  int n = f->NX * f->P;
+  count(f);
+  k_store_phi<<<(n + 255) / 256, 256, 0, f->stream>>>(f->phi, f->phi2, (const PCtl*)f->pctl, dst, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi) {
+  float cp = f->density * f->h / dt;  // fluid.go:158
+  dim3 rg((f->NY + BX - 1) / BX, (f->NX + BY * GR - 1) / (BY * GR)), bl(BX, BY);
+  if (!partials_fit(f, 5, rg.x * rg.y)) return cudaErrorInvalidValue;
+  count(f);
+  // The potential is the same buffer whichever one the control block names;
+  // the statistics partials it writes are not combined.
+  k_grad_fused<<<rg, bl, 0, f->stream>>>(
+      f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], phi, phi,
+      (const PCtl*)f->pctl, nullptr, nullptr, nullptr, f->rhs, f->flags, cp, f->noise, 0.0f, 0,
+      f->partials, f->g);
+  swap_state(f, FG_U);
+  swap_state(f, FG_V);
   return cudaGetLastError();
 }
 

@@ -246,9 +246,15 @@ int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x, 
  * becomes that of the state before the step, and dL/d(force_u, force_v) of
  * that step is written to grad_force_u / grad_force_v (NULL: skipped).  The
  * steps of a checkpoint interval are recomputed from its checkpoint when the
- * interval is first reversed.  After the last step is reversed the handle's
- * state is back at the end of the forward pass, and fg_tape_grad returns
- * dL/d(initial U, V, M, newU, newV, newM).
+ * interval is first reversed (each step's pressure potential is kept from the
+ * forward pass, so the recomputation skips the pressure solve).  After the
+ * last step is reversed the handle's state is back at the end of the forward
+ * pass, and fg_tape_grad returns dL/d(initial U, V, M, newU, newV, newM).
+ *
+ * fg_tape_end closes the rollout (restoring the end-of-rollout state if it
+ * was left mid-reverse).  The rollout's device buffers (per step: two force
+ * fields and a potential; one interval of 13 recorded fields; 6 fields per
+ * checkpoint) stay allocated for the next rollout until fg_destroy.
  *
  * All fields (forces, seeds, target, gradients) use the mirrors' layout
  * (NumX * NumY floats, index i*NumY + j) in host or device memory.  Adjoint
