@@ -262,6 +262,106 @@ def fwd_adjoint(fluid_gb300, args):
     }
 
 
+def rollout256(fluid_gb300, args):
+    """The differentiable-rollout configuration: 256^2 jet (walls left, top,
+    bottom; 8-row jet at U = 2 with smoke assigned to 1 before every step),
+    FP32, 64 steps, BFECC, 60 Jacobi sweeps, checkpoint every 8, loss
+    ||M_64 - target||_2 against 4 seeded Gaussian blobs (sigma 10-30 cells,
+    amplitude 0.5-1.0), gradients w.r.t. U0, V0 and the 64 two-channel force
+    fields.  Device-timed fwd+adjoint per step, and the adjoint's directional
+    derivatives against central differences (eps 1e-3) of the FP32 forward
+    pass on 32 seeded directions."""
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import scenes
+
+    side, steps, iters, every = 256, 64, 60, 8
+    f = fluid_gb300.Fluid(1.0, side, side, 1.0, auto_sync=False, scheme=1, num_iters=iters,
+                          tb_depth=8, early_exit=False, UseBFECC=True)
+    scenes.jet_rollout_scene(f)
+    n = f.numCells
+    target = torch.from_numpy(scenes.gaussian_target(f.NumX, f.NumY, seed=4)).cuda()
+    gfu = torch.empty((steps, n), device="cuda")
+    gfv = torch.empty((steps, n), device="cuda")
+    dforce = torch.empty((steps, 2, n), device="cuda")
+    stream = torch.cuda.ExternalStream(f.stream)
+    torch.cuda.synchronize()
+
+    def prep(dU=None, dV=None, s=0.0):
+        f.Reset()
+        f.download()
+        if dU is not None:
+            f.U[:] = s * dU
+            f.V[:] = s * dV
+            f.mark_dirty(3)
+            fp = dforce * s
+        else:
+            fp = torch.zeros((steps, 2, n), device="cuda")
+        torch.cuda.synchronize()
+        return fp
+
+    def run(fp, grads=True):
+        f.tape_begin(steps, every)
+        for t in range(steps):
+            f.step_forward(DT, fp[t, 0], fp[t, 1])
+        loss = f.tape_seed_smoke_l2(target)
+        if grads:
+            for t in reversed(range(steps)):
+                f.step_adjoint(gfu[t], gfv[t])
+        return loss
+
+    run(prep())
+    f.tape_end()
+    fp = prep()
+    f.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    loss = run(fp)
+    e1.record(stream)
+    f.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    g = f.tape_grad()
+    f.tape_end()
+    gu = (gfu.double().cpu().numpy(), gfv.double().cpu().numpy())
+    prep()
+    f.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        f.Simulate(DT)
+    e1.record(stream)
+    f.synchronize()
+    ms_fwd = e0.elapsed_time(e1) / steps
+    rel = []
+    for k in range(32):
+        rng = np.random.default_rng(4000 + k)
+        dU = rng.standard_normal(n).astype(np.float32)
+        dV = rng.standard_normal(n).astype(np.float32)
+        df = rng.standard_normal((steps, 2, n)).astype(np.float32) * 0.1
+        dforce.copy_(torch.from_numpy(df))
+        torch.cuda.synchronize()
+        ad = float(np.dot(g["U"].astype(np.float64), dU) + np.dot(g["V"].astype(np.float64), dV)
+                   + np.sum(gu[0] * df[:, 0]) + np.sum(gu[1] * df[:, 1]))
+        eps = 1e-3
+        lp = run(prep(dU, dV, eps), grads=False)
+        f.tape_end()
+        lm = run(prep(dU, dV, -eps), grads=False)
+        f.tape_end()
+        fd = (lp - lm) / (2 * eps)
+        rel.append(abs(ad - fd) / max(abs(fd), 1e-2))
+    return {
+        "config": "256x256 jet, FP32, 64 steps, BFECC, 60 Jacobi sweeps, checkpoint every 8; "
+                  "loss ||M_64 - target||_2 (4 seeded Gaussians); grads w.r.t. U0, V0 and "
+                  "64 x 2 force fields",
+        "value": side * side / ms / 1e3, "unit": "Mcell-steps/s fwd+adjoint",
+        "ms_per_step": ms, "fwd_ms_per_step": ms_fwd, "ratio_to_fwd": ms / ms_fwd, "loss": loss,
+        "fd_check": {"directions": 32, "eps": 1e-3, "reference": "FP32 forward central differences",
+                     "median_rel_err": float(np.median(rel)), "max_rel_err": float(np.max(rel))},
+    }
+
+
 # ---------------------------------------------------------------- CPU legs
 def cpu_reference_steps(steps, threads, budget_s=None):
     """Times the reference algorithm (FP32, serial SOR pressure, parallelRange
@@ -423,6 +523,7 @@ def run_ours(args):
         del g
 
     adj = fwd_adjoint(fluid_gb300, args) if rank == 0 and not args.no_adjoint else None
+    roll = rollout256(fluid_gb300, args) if rank == 0 and not args.no_adjoint else None
 
     # ------------------------------------------------------------ CPU baseline
     cpu = None
@@ -442,7 +543,7 @@ def run_ours(args):
             "data": "synthetic",
             "config": workload_config({"parallelism": "replicas%d" % world if world > 1 else "single"}),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "fwd_adjoint": adj,
+            "fwd_adjoint": adj, "rollout_256": roll,
             "clocks": sampler.summary(),
             "host_ms_per_step": 1e3 * t_host / args.steps,
             "stage_ms": stage_ms,

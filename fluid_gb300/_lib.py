@@ -98,7 +98,7 @@ SIGNATURES = {
     "fg_tape_begin": (_c_i, [_vp, _c_i, _c_i]),
     "fg_step_forward": (_c_i, [_vp, _c_f, _vp, _vp]),
     "fg_tape_seed": (_c_i, [_vp, _vp, _vp, _vp]),
-    "fg_tape_seed_smoke_l2": (_c_i, [_vp, _vp, _fp]),
+    "fg_tape_seed_smoke_l2": (_c_i, [_vp, _vp, ctypes.POINTER(_c_d)]),
     "fg_step_adjoint": (_c_i, [_vp, _vp, _vp]),
     "fg_tape_grad": (_c_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fg_tape_steps": (_c_i, [_vp, ctypes.POINTER(_c_i), ctypes.POINTER(_c_i)]),

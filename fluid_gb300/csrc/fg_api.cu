@@ -742,6 +742,7 @@ int fg_set_sources(fg_fluid* f, int n, const int* is, const int* js, const float
   std::vector<SourceRec> recs;
   for (int k = 0; k < n; ++k) {
     if (!in_grid(f, is[k], js[k])) return fail(f, FG_ERR_INDEX, "invalid source index");
+    if (mode[k] & ~15) return fail(f, FG_ERR_INVALID, "unknown source mode bits");
     SourceRec r;
     r.cell = (uint32_t)(is[k] * f->NY + js[k]);
     r.mode = (uint32_t)mode[k];
@@ -1043,8 +1044,6 @@ int tape_supported(fg_fluid* f) {
     return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support refine_sweeps");
   if (p.viscosity_diffusion > 0.0f)
     return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support viscosity");
-  if (p.confinement != 0.0f)
-    return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support confinement");
   if (p.use_multigrid && p.multigrid_levels > 1)
     return fail(f, FG_ERR_UNSUPPORTED, "UseMultigrid is not built for the GPU step");
   return FG_OK;
@@ -1085,9 +1084,10 @@ int get_field(fg_fluid* f, float* dst, const float* dev) {
 }
 
 // One recorded step: Simulate (fluid.go:79-109) with the force field added
-// to U, V before the sources, turbulence run as its own pass, and the
-// intermediates the adjoint reads written to `rec` (kTapeFields fields:
-// U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM corrM).  The BFECC
+// to U, V before the sources, confinement / turbulence run as their own
+// pass, and the intermediates the adjoint reads written to `rec`
+// (kTapeFields fields: U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM
+// corrM).  The BFECC
 // intermediates are produced in place: the scratch pointers are redirected
 // to the record for the step.  The pressure potential is stored to `phi`
 // (replay = false) or, on a replay of a step already run, read from it in
@@ -1107,9 +1107,10 @@ int enqueue_step_record(fg_fluid* f, float dt, const float* fu, const float* fv,
     if ((rc = enqueue_pressure(f, p.num_iters, dt, false))) return rc;
     CK(f, launch_store_phi(f, phi), "store potential");
   }
-  if (p.turbulence_strength > 0.0f) {
+  const bool conf = p.confinement != 0.0f, turb = p.turbulence_strength > 0.0f;
+  if (conf || turb) {
     if ((rc = copy_field(f, R(0), f->d[FG_U])) || (rc = copy_field(f, R(1), f->d[FG_V]))) return rc;
-    CK(f, launch_confinement_turbulence(f, dt, false, true), "turbulence");
+    CK(f, launch_confinement_turbulence(f, dt, conf, turb), "confinement/turbulence");
   }
   CK(f, launch_borders(f), "borders");
   if ((rc = copy_field(f, R(2), f->d[FG_U])) || (rc = copy_field(f, R(3), f->d[FG_V]))) return rc;
@@ -1289,7 +1290,7 @@ int fg_tape_seed(fg_fluid* f, const float* dU, const float* dV, const float* dM)
   return FG_OK;
 }
 
-int fg_tape_seed_smoke_l2(fg_fluid* f, const float* target, float* loss) {
+int fg_tape_seed_smoke_l2(fg_fluid* f, const float* target, double* loss) {
   if (!f || !target) return FG_ERR_INVALID;
   int rc = tape_usable(f);
   if (rc) return rc;
@@ -1297,14 +1298,15 @@ int fg_tape_seed_smoke_l2(fg_fluid* f, const float* target, float* loss) {
   if (t->n_fwd == 0 || t->n_rev > 0)
     return fail(f, FG_ERR_INVALID, "seed the adjoint after the forward steps, before reversing");
   if ((rc = put_field(f, t->aux, target))) return rc;
-  float* slot = dev_scalar_slot(f);
+  // An 8-byte aligned double in the scalar slots.
+  double* slot = (double*)dev_scalar_slot(f);
   CK(f, launch_loss_seed(f, t->aux, slot), "loss");
   t->seeded = true;
   if (loss) {
-    CK(f, cudaMemcpyAsync(f->scalar_pinned, slot, sizeof(float), cudaMemcpyDeviceToHost, f->stream),
-       "loss");
+    CK(f, cudaMemcpyAsync(f->scalar_pinned, slot, sizeof(double), cudaMemcpyDeviceToHost,
+                          f->stream), "loss");
     CK(f, cudaStreamSynchronize(f->stream), "loss sync");
-    *loss = f->scalar_pinned[0];
+    memcpy(loss, f->scalar_pinned, sizeof(double));
   }
   return FG_OK;
 }

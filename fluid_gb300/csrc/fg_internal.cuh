@@ -246,7 +246,7 @@ cudaError_t launch_add_forces(fg_fluid* f, const float* fu, const float* fv);
 // state after the step to that of the state before it; adj[A_U], adj[A_V]
 // then also hold the adjoint of the step's force field.
 cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape);
-cudaError_t launch_loss_seed(fg_fluid* f, const float* target, float* dev_loss);
+cudaError_t launch_loss_seed(fg_fluid* f, const float* target, double* dev_loss);
 // k_diag.cu
 cudaError_t launch_div_stats(fg_fluid* f);
 cudaError_t launch_smoke_mass(fg_fluid* f);

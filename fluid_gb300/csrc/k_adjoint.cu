@@ -452,6 +452,127 @@ __global__ void k_adj_turbulence(float* __restrict__ dU, float* __restrict__ dV,
   dV[c] = lv + s * av;
 }
 
+// ---------------------------------------------------------------- confinement
+// applyVorticityConfinement (fluid.go:449-493) followed by addTurbulence on
+// the pre-confinement field (U2, V2).  curl_at restates k_curl for one cell.
+__device__ __forceinline__ float curl_at(const float* __restrict__ U, const float* __restrict__ V,
+                                         const uint8_t* __restrict__ flags, int c, const Grid& g) {
+  if (!fluid_interior(flags[c])) return 0.0f;
+  float dvdx = (V[c + g.P] - V[c - g.P]) * 0.5f / g.h;
+  float dudy = (U[c + 1] - U[c - 1]) * 0.5f / g.h;
+  return dvdx - dudy;
+}
+
+// Per fluid interior cell: the turbulence adjoint at the post-confinement
+// velocity (recomputed), then the confinement adjoint of the cell's own
+// terms.  In place on (dU, dV) for the identity and speed terms; writes the
+// adjoint of the cell's curl through its direct use (lw) and of the
+// normalised gradient's inputs (lgx, lgy: d/d gx, d/d gy), 0 on every other
+// cell.  Subgradients: |curl| passes sign(curl) (0 at 0); at |grad| = 0 the
+// normalisation's derivative is I / eps.
+__global__ void k_adj_conf_local(float* __restrict__ dU, float* __restrict__ dV,
+                                 const float* __restrict__ U2, const float* __restrict__ V2,
+                                 const float2* __restrict__ noise,
+                                 const uint8_t* __restrict__ flags, float conf, float dt,
+                                 float turbStrength, int do_turb, float* __restrict__ lw,
+                                 float* __restrict__ lgx, float* __restrict__ lgy, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  if (!fluid_interior(flags[c])) {
+    lw[c] = 0.0f;
+    lgx[c] = 0.0f;
+    lgy[c] = 0.0f;
+    return;
+  }
+  const float eps = 1e-5f;
+  float w = curl_at(U2, V2, flags, c, g);
+  float aE = fabsf(curl_at(U2, V2, flags, c + P, g)), aW = fabsf(curl_at(U2, V2, flags, c - P, g));
+  float aN = fabsf(curl_at(U2, V2, flags, c + 1, g)), aS = fabsf(curl_at(U2, V2, flags, c - 1, g));
+  float gx = (aE - aW) * 0.5f / g.h;
+  float gy = (aN - aS) * 0.5f / g.h;
+  float rg = sqrtf(gx * gx + gy * gy);
+  float m = rg + eps;
+  float nx = gx / m, ny = gy / m;
+  float u = U2[c], v = V2[c];
+  float r = sqrtf(u * u + v * v);
+  float K = conf * (1.0f + r * 0.1f);
+  // Forward confinement (as k_conf_turb), then the turbulence adjoint at it.
+  float u1 = u + K * ny * w * dt;
+  float v1 = v - K * nx * w * dt;
+  float lu = dU[c], lv = dV[c];
+  if (do_turb) {
+    float r1 = sqrtf(u1 * u1 + v1 * v1);
+    if (r1 > 0.1f && 0.5f * r1 < 1.0f) {
+      float2 nz = noise[c];
+      float s = (lu * nz.x * turbStrength + lv * nz.y * turbStrength) * 0.5f;
+      lu = lu + s * (u1 / r1);
+      lv = lv + s * (v1 / r1);
+    }
+  }
+  // Confinement: u1 = u + K ny w dt, v1 = v - K nx w dt.
+  float a = lu * dt, b = -lv * dt;
+  float S = a * ny + b * nx;
+  float lK = w * S;
+  float ou = lu, ov = lv;
+  if (r > 0.0f) {
+    ou = ou + lK * conf * 0.1f * (u / r);
+    ov = ov + lK * conf * 0.1f * (v / r);
+  }
+  dU[c] = ou;
+  dV[c] = ov;
+  lw[c] = K * S;
+  float Lnx = K * w * b, Lny = K * w * a;
+  float im = 1.0f / m;
+  float qx = Lnx * im, qy = Lny * im;
+  if (rg > 0.0f) {
+    float t = (Lnx * gx + Lny * gy) / (rg * m * m);
+    qx = qx - t * gx;
+    qy = qy - t * gy;
+  }
+  lgx[c] = qx;
+  lgy[c] = qy;
+}
+
+// Adjoint of every cell's curl: its direct use plus the |curl| terms of the
+// four neighbours' gradients.  Gathers lgx, lgy from the neighbours.
+__global__ void k_adj_conf_curl(const float* __restrict__ U2, const float* __restrict__ V2,
+                                const float* __restrict__ lwd, const float* __restrict__ lgx,
+                                const float* __restrict__ lgy, float* __restrict__ lw,
+                                const uint8_t* __restrict__ flags, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  float out = 0.0f;
+  if (fluid_interior(flags[c])) {
+    float w = curl_at(U2, V2, flags, c, g);
+    float sg = w > 0.0f ? 1.0f : (w < 0.0f ? -1.0f : 0.0f);
+    float k = 0.5f / g.h;
+    out = lwd[c] + sg * k * ((lgx[c - P] - lgx[c + P]) + (lgy[c - 1] - lgy[c + 1]));
+  }
+  lw[c] = out;
+}
+
+// curl^T: dU[m] += (lw[m+1] - lw[m-1]) / 2h, dV[m] += (lw[m-P] - lw[m+P]) / 2h
+// (lw is 0 off the fluid interior cells).
+__global__ void k_adj_conf_apply(float* __restrict__ dU, float* __restrict__ dV,
+                                 const float* __restrict__ lw, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  float k = 0.5f / g.h;
+  float wN = j + 1 < g.NY ? lw[c + 1] : 0.0f, wS = j >= 1 ? lw[c - 1] : 0.0f;
+  float wE = i + 1 < g.NX ? lw[c + P] : 0.0f, wW = i >= 1 ? lw[c - P] : 0.0f;
+  dU[c] = dU[c] + k * (wN - wS);
+  dV[c] = dV[c] + k * (wW - wE);
+}
+
 // G^T: the adjoint of the gradient subtract with respect to phi, as the
 // Jacobi right-hand side of the adjoint solve: rhs = G^T (dU, dV) on active
 // cells, and bw = w * rhs.
@@ -497,10 +618,12 @@ __global__ void k_adj_div_t(float* __restrict__ dU, float* __restrict__ dV,
   }
 }
 
-// Sources that set U, V (fluid SetVelocity) cut the derivative there.
+// Sources that set U, V (SetVelocity) or M (a smoke assignment) cut the
+// derivative there.
 __global__ void k_adj_sources(float* __restrict__ dU, float* __restrict__ dV,
-                              const SourceRec* __restrict__ recs, const uint32_t* __restrict__ off,
-                              int n_groups, const uint8_t* __restrict__ flags, Grid g) {
+                              float* __restrict__ dM, const SourceRec* __restrict__ recs,
+                              const uint32_t* __restrict__ off, int n_groups,
+                              const uint8_t* __restrict__ flags, Grid g) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_groups) return;
   uint32_t b = off[k], e = off[k + 1];
@@ -508,16 +631,18 @@ __global__ void k_adj_sources(float* __restrict__ dU, float* __restrict__ dV,
   int i = (int)(cell / (uint32_t)g.NY), j = (int)(cell % (uint32_t)g.NY);
   int c = i * g.P + j;
   bool fluid = (flags[c] & F_FLUID) != 0;
-  bool set = false;
+  bool set = false, set_m = false;
   for (uint32_t q = b; q < e; ++q) {
     SourceRec r = recs[q];
     if ((r.mode & 1u) && !fluid) continue;
     if (r.mode & 2u) set = true;
+    if (r.mode & 8u) set_m = true;
   }
   if (set) {
     dU[c] = 0.0f;
     dV[c] = 0.0f;
   }
+  if (set_m) dM[c] = 0.0f;
 }
 
 // Loss L = ||M - target||_2 over interior cells: float-pair block rows of
@@ -536,14 +661,15 @@ __global__ void k_loss_partials(const float* __restrict__ M, const float* __rest
 }
 
 // Seeds the adjoint state with dL/dM = (M - target) / L on interior cells,
-// zero elsewhere and for every other field; stores L.
+// zero elsewhere and for every other field; stores L in FP64 (the float-pair
+// sum carries ~48 bits, so differences of nearby losses stay resolved).
 __global__ void k_loss_seed(const float* __restrict__ M, const float* __restrict__ T,
                             const float* __restrict__ row, float* __restrict__ lamM,
-                            float* __restrict__ loss, Grid g) {
+                            double* __restrict__ loss, Grid g) {
   double L = sqrt((double)row[0] + (double)row[1]);
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i == 0 && j == 0) loss[0] = (float)L;
+  if (i == 0 && j == 0) loss[0] = L;
   if (i >= g.NX || j >= g.NY) return;
   int c = i * g.P + j;
   float v = 0.0f;
@@ -580,7 +706,7 @@ __global__ void k_adj_begin(float* __restrict__ aU, float* __restrict__ aV, floa
 
 }  // namespace
 
-cudaError_t launch_loss_seed(fg_fluid* f, const float* target, float* dev_loss) {
+cudaError_t launch_loss_seed(fg_fluid* f, const float* target, double* dev_loss) {
   dim3 gr = cell_grid(f), bl(BX, BY);
   int nb = gr.x * gr.y;
   if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
@@ -674,11 +800,21 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
                                          A[F::A_V], A[F::A_U], A[F::A_V], A[F::A_U], A[F::A_V],
                                          A[F::A_NU], A[F::A_NV], f->flags, dt, g);
   }
-  // ---- borders, turbulence (A_U/A_V: dU4 -> dU3 -> dU2)
+  // ---- borders, confinement + turbulence (A_U/A_V: dU4 -> dU3 -> dU2)
   int nbd = f->NX > f->NY ? f->NX : f->NY;
   count(f);
   k_adj_borders<<<(nbd + 127) / 128, 128, 0, st>>>(A[F::A_U], A[F::A_V], f->flags, g);
-  if (p.turbulence_strength > 0.0f) {
+  if (p.confinement != 0.0f) {
+    // Work fields A_CU, A_CV, A_FU, A_FV are free again here.
+    count(f, 3);
+    k_adj_conf_local<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], U2, V2, f->noise, f->flags,
+                                        p.confinement, dt, p.turbulence_strength * dt,
+                                        p.turbulence_strength > 0.0f ? 1 : 0, A[F::A_CU],
+                                        A[F::A_CV], A[F::A_FU], g);
+    k_adj_conf_curl<<<gr, bl, 0, st>>>(U2, V2, A[F::A_CU], A[F::A_CV], A[F::A_FU], A[F::A_FV],
+                                       f->flags, g);
+    k_adj_conf_apply<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], A[F::A_FV], g);
+  } else if (p.turbulence_strength > 0.0f) {
     count(f);
     k_adj_turbulence<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], U2, V2, f->noise, f->flags,
                                         p.turbulence_strength * dt, g);
@@ -701,7 +837,8 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
   if (f->n_src_groups > 0) {
     count(f);
     k_adj_sources<<<(f->n_src_groups + 255) / 256, 256, 0, st>>>(
-        A[F::A_U], A[F::A_V], f->src_dev, f->src_off_dev, f->n_src_groups, f->flags, g);
+        A[F::A_U], A[F::A_V], A[F::A_M], f->src_dev, f->src_off_dev, f->n_src_groups, f->flags,
+        g);
   }
   return cudaGetLastError();
 }

@@ -60,8 +60,9 @@ __global__ void k_apply_edits(const EditRec* __restrict__ recs, const uint32_t* 
 
 // Persistent sources: per cell group, in list order, the app's
 // SetVelocity(i, j, u, v) and AddSmoke(i, j, s) calls made before each step
-// (main/main.go:236-241 jet, 474-486 sources), optionally skipped on solid
-// cells (the IsSolid check of applySources).
+// (main/main.go:236-241 jet, 474-486 sources) or a smoke assignment
+// (fluid_test.go:396-401), optionally skipped on solid cells (the IsSolid
+// check of applySources).
 __global__ void k_apply_sources(const SourceRec* __restrict__ recs,
                                 const uint32_t* __restrict__ off, int n_groups, float* U,
                                 float* V, float* M, const uint8_t* __restrict__ flags, Grid g) {
@@ -80,7 +81,10 @@ __global__ void k_apply_sources(const SourceRec* __restrict__ recs,
       u = r.u;
       v = r.v;
     }
-    if (r.mode & 4u) m = m + r.smoke;
+    if (r.mode & 8u)
+      m = r.smoke;
+    else if (r.mode & 4u)
+      m = m + r.smoke;
   }
   U[c] = u;
   V[c] = v;

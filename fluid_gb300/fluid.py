@@ -286,7 +286,7 @@ class Fluid:
             raise IndexError("invalid index")
         self._check(rc, "AddSmokeMany")
 
-    SRC_SKIP_SOLID, SRC_SET_VELOCITY, SRC_ADD_SMOKE = 1, 2, 4
+    SRC_SKIP_SOLID, SRC_SET_VELOCITY, SRC_ADD_SMOKE, SRC_SET_SMOKE = 1, 2, 4, 8
 
     def set_sources(self, i, j, u=None, v=None, smoke=None, mode=None):
         """Persistent per-step sources applied on the device before every step."""
@@ -368,8 +368,8 @@ class Fluid:
                                          self._field_ptr(dM)), "fg_tape_seed")
 
     def tape_seed_smoke_l2(self, target):
-        """Seeds dL/dM for L = ||M - target||_2 over the interior; returns L."""
-        loss = ctypes.c_float()
+        """Seeds dL/dM for L = ||M - target||_2 over the interior; returns L (FP64)."""
+        loss = ctypes.c_double()
         self._check(self._L.fg_tape_seed_smoke_l2(self._h, self._field_ptr(target),
                                                   ctypes.byref(loss)), "fg_tape_seed_smoke_l2")
         return loss.value

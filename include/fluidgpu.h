@@ -171,10 +171,13 @@ int fg_add_smoke_many(fg_fluid* f, int n, const int* i, const int* j, const floa
  * reference app makes before Simulate for its jet and its sources
  * (main/main.go:236-241, 474-486).  mode bit 0: skip the source while its
  * cell is solid (applySources' IsSolid check); bit 1: set U and V to u, v;
- * bit 2: add `smoke` to M.  n = 0 clears the list. */
+ * bit 2: add `smoke` to M; bit 3: set M to `smoke` (the reference tests' jet
+ * assignment M[i*n+j] = 1, fluid_test.go:396-401; it takes precedence over
+ * bit 2).  Other bits: FG_ERR_INVALID.  n = 0 clears the list. */
 #define FG_SRC_SKIP_SOLID 1
 #define FG_SRC_SET_VELOCITY 2
 #define FG_SRC_ADD_SMOKE 4
+#define FG_SRC_SET_SMOKE 8
 int fg_set_sources(fg_fluid* f, int n, const int* i, const int* j, const float* u,
                    const float* v, const float* smoke, const int* mode);
 
@@ -230,8 +233,8 @@ int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x, 
  *
  * fg_tape_begin(f, max_steps, every) starts a recorded rollout from the
  * current state and saves it as the first checkpoint.  It needs the JACOBI
- * scheme with early_exit 0, refine_sweeps 0, viscosity_diffusion 0 and
- * confinement 0 (else FG_ERR_UNSUPPORTED); the parameters, the sources and
+ * scheme with early_exit 0, refine_sweeps 0 and viscosity_diffusion 0
+ * (else FG_ERR_UNSUPPORTED); the parameters, the sources and
  * the state must not change until fg_tape_end (else FG_ERR_INVALID).
  *
  * fg_step_forward(f, dt, force_u, force_v) runs one step with the force
@@ -240,7 +243,8 @@ int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x, 
  *
  * fg_tape_seed sets the adjoint of the final state (dL/dU, dL/dV, dL/dM;
  * NULL = zero); fg_tape_seed_smoke_l2 sets it for L = ||M - target||_2 over
- * the interior cells and returns L.
+ * the interior cells and returns L (summed in double-float, returned in
+ * FP64).
  *
  * fg_step_adjoint reverses the latest step not yet reversed: the adjoint
  * becomes that of the state before the step, and dL/d(force_u, force_v) of
@@ -263,7 +267,7 @@ int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x, 
 int fg_tape_begin(fg_fluid* f, int max_steps, int every);
 int fg_step_forward(fg_fluid* f, float dt, const float* force_u, const float* force_v);
 int fg_tape_seed(fg_fluid* f, const float* dU, const float* dV, const float* dM);
-int fg_tape_seed_smoke_l2(fg_fluid* f, const float* target, float* loss);
+int fg_tape_seed_smoke_l2(fg_fluid* f, const float* target, double* loss);
 int fg_step_adjoint(fg_fluid* f, float* grad_force_u, float* grad_force_v);
 int fg_tape_grad(fg_fluid* f, float* dU, float* dV, float* dM, float* dNU, float* dNV, float* dNM);
 int fg_tape_steps(const fg_fluid* f, int* forward, int* reversed);

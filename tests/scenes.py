@@ -83,3 +83,31 @@ def random_state(f, seed=0, amp=1.0, smoke=True):
     f.V[:] = rng.uniform(-amp, amp, f.numCells).astype(f.dtype)
     if smoke:
         f.M[:] = rng.uniform(0, 1, f.numCells).astype(f.dtype)
+
+
+# ---------------------------------------------------------------- differentiable rollout
+def jet_rollout_scene(f, speed=2.0, smoke=1.0, half=4):
+    """Jet scene of the differentiable rollout: walls left, top and bottom,
+    open right; a jet of 2*half rows at i = 1 held by device sources (U =
+    speed, V = 0, M = smoke assigned before every step, as fluid_test.go
+    :396-401 does on the host).  Zero initial state."""
+    fast_walls(f)
+    f.mark_dirty()
+    rows = np.array(list(jet_rows(f, half)), np.int32)
+    f.set_sources(np.ones_like(rows), rows, u=speed, v=0.0, smoke=smoke,
+                  mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY | f.SRC_SET_SMOKE)
+
+
+def gaussian_target(nx, ny, seed=4, n=4, sigma=(10.0, 30.0), amp=(0.5, 1.0)):
+    """Sum of n seeded isotropic Gaussian blobs (sigma and amplitude drawn
+    uniformly, centres uniform over the interior), as NX*NY float32."""
+    rng = np.random.default_rng(seed)
+    i = np.arange(nx)[:, None]
+    j = np.arange(ny)[None, :]
+    T = np.zeros((nx, ny))
+    for _ in range(n):
+        s = rng.uniform(*sigma)
+        a = rng.uniform(*amp)
+        ci, cj = rng.uniform(1, nx - 1), rng.uniform(1, ny - 1)
+        T += a * np.exp(-((i - ci) ** 2 + (j - cj) ** 2) / (2 * s * s))
+    return T.ravel().astype(np.float32)
