@@ -6,7 +6,7 @@ Python mirror of the Go type ``fluid.Fluid`` over that ABI.
 """
 from . import fluid as _fluid_mod
 from ._build import build
-from .fluid import (ALL_FIELDS, FIELDS, SCHEME_JACOBI, SCHEME_LEXSOR, Fluid, FluidError,
+from .fluid import (ALL_FIELDS, FIELDS, SCHEME_JACOBI, SCHEME_LEXSOR, Batch, Fluid, FluidError,
                     ScalarField, VectorField)
 
 
@@ -21,5 +21,5 @@ def set_relaxation(value: float) -> None:
     _fluid_mod.Relaxation = float(value)
 
 
-__all__ = ["Fluid", "FluidError", "ScalarField", "VectorField", "build", "set_relaxation",
+__all__ = ["Fluid", "Batch", "FluidError", "ScalarField", "VectorField", "build", "set_relaxation",
            "FIELDS", "ALL_FIELDS", "SCHEME_LEXSOR", "SCHEME_JACOBI"]

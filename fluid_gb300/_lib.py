@@ -103,6 +103,16 @@ SIGNATURES = {
     "fg_tape_grad": (_c_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fg_tape_steps": (_c_i, [_vp, ctypes.POINTER(_c_i), ctypes.POINTER(_c_i)]),
     "fg_tape_end": (_c_i, [_vp]),
+    "fg_batch_create": (_c_i, [_vp, _c_i, ctypes.POINTER(_vp)]),
+    "fg_batch_size": (_c_i, [_vp, ctypes.POINTER(_c_i)]),
+    "fg_batch_step": (_c_i, [_vp, _c_f]),
+    "fg_batch_step_adjoint": (_c_i, [_vp]),
+    "fg_batch_gather": (_c_i, [_vp]),
+    "fg_batch_scatter": (_c_i, [_vp]),
+    "fg_batch_seed_smoke_l2": (_c_i, [_vp, _vp, ctypes.POINTER(_c_d)]),
+    "fg_batch_grad": (_c_i, [_vp, _c_i, _vp, _vp, _vp]),
+    "fg_batch_autotune": (_c_i, [_vp, _c_f, _c_i, ctypes.POINTER(_c_i), ctypes.POINTER(_c_i),
+                                 ctypes.POINTER(_c_i), _fp]),
     "fg_last_error": (ctypes.c_char_p, [_vp]),
 }
 

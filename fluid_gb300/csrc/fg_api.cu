@@ -19,6 +19,15 @@ namespace {
 constexpr int kSlots = 4096;
 
 void tape_free(fg_fluid* f);  // differentiable rollouts, at the end of the file
+void batch_free(fg::BatchGeom* b);  // batches, at the end of the file
+
+// Entry points that address one scene's cells, mirrors or views are not
+// available on a batch handle.
+bool is_batch(const fg_fluid* f) { return f && f->batch; }
+int batch_unsupported(const fg_fluid* f) {
+  const_cast<fg_fluid*>(f)->last_error = "not available on a batch handle";
+  return FG_ERR_UNSUPPORTED;
+}
 
 int fail(fg_fluid* f, int code, const char* what, cudaError_t e = cudaSuccess) {
   if (f) {
@@ -383,6 +392,7 @@ int fg_destroy(fg_fluid* f) {
   if (f->stream) cudaStreamSynchronize(f->stream);
   clear_graphs(f);
   tape_free(f);
+  batch_free(f->batch);
   for (int k = 0; k < fg_fluid::A_COUNT; ++k) cudaFree(f->adj[k]);
   for (int k = 0; k < FG_NUM_FIELDS; ++k) {
     cudaFree(f->d[k]);
@@ -419,6 +429,7 @@ int fg_destroy(fg_fluid* f) {
 }
 
 int fg_dims(const fg_fluid* f, int* nx, int* ny) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || !nx || !ny) return FG_ERR_INVALID;
   *nx = f->NX;
   *ny = f->NY;
@@ -434,6 +445,7 @@ int fg_get_params(const fg_fluid* f, fg_params* out) {
 }
 
 int fg_set_params(fg_fluid* f, const fg_params* p) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || !p) return FG_ERR_INVALID;
   int rc = check_params(f, p);
   if (rc) return rc;
@@ -445,12 +457,14 @@ int fg_set_params(fg_fluid* f, const fg_params* p) {
 }
 
 int fg_field(fg_fluid* f, int field, float** host_ptr) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || !host_ptr || field < 0 || field >= FG_NUM_FIELDS) return FG_ERR_INVALID;
   *host_ptr = f->hm[field];
   return FG_OK;
 }
 
 int fg_mark_dirty(fg_fluid* f, unsigned mask) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   for (int k = 0; k < FG_NUM_FIELDS; ++k)
     if ((mask & FG_FIELD_BIT(k)) && !f->host_valid[k])
@@ -460,6 +474,7 @@ int fg_mark_dirty(fg_fluid* f, unsigned mask) {
 }
 
 int fg_download(fg_fluid* f, unsigned mask) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   int rc = flush(f);
   if (rc) return rc;
@@ -552,6 +567,7 @@ int fg_simulate(fg_fluid* f, float dt) {
 }
 
 int fg_get_stats(fg_fluid* f, fg_stats* out) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || !out) return FG_ERR_INVALID;
   int rc = bind(f);
   if (rc) return rc;
@@ -578,6 +594,7 @@ int fg_get_stats(fg_fluid* f, fg_stats* out) {
   if (rc) return rc;
 
 int fg_make_incompressible(fg_fluid* f, int num_iters, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   if ((rc = check_iters(f, num_iters))) return rc;
   invalidate(f, kStepFields);
@@ -589,6 +606,7 @@ int fg_make_incompressible(fg_fluid* f, int num_iters, float dt) {
 }
 
 int fg_advect_velocity(fg_fluid* f, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   invalidate(f, kStepFields);
   CK(f, launch_advect_velocity(f, dt), "advect velocity");
@@ -596,6 +614,7 @@ int fg_advect_velocity(fg_fluid* f, float dt) {
 }
 
 int fg_advect_smoke(fg_fluid* f, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   invalidate(f, kStepFields);
   CK(f, launch_advect_smoke(f, dt), "advect smoke");
@@ -603,6 +622,7 @@ int fg_advect_smoke(fg_fluid* f, float dt) {
 }
 
 int fg_advect_velocity_bfecc(fg_fluid* f, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   invalidate(f, kStepFields);
   CK(f, launch_advect_velocity_bfecc(f, dt), "advect velocity bfecc");
@@ -610,6 +630,7 @@ int fg_advect_velocity_bfecc(fg_fluid* f, float dt) {
 }
 
 int fg_advect_smoke_bfecc(fg_fluid* f, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   invalidate(f, kStepFields);
   CK(f, launch_advect_smoke_bfecc(f, dt), "advect smoke bfecc");
@@ -617,6 +638,7 @@ int fg_advect_smoke_bfecc(fg_fluid* f, float dt) {
 }
 
 int fg_handle_borders(fg_fluid* f) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   invalidate(f, kStepFields);
   CK(f, launch_borders(f), "borders");
@@ -624,6 +646,7 @@ int fg_handle_borders(fg_fluid* f) {
 }
 
 int fg_apply_vorticity_confinement(fg_fluid* f, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   invalidate(f, kStepFields);
   CK(f, launch_confinement_turbulence(f, dt, true, false), "confinement");
@@ -631,6 +654,7 @@ int fg_apply_vorticity_confinement(fg_fluid* f, float dt) {
 }
 
 int fg_apply_viscosity(fg_fluid* f, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   if (!(f->prm.viscosity_diffusion > 0.0f)) return FG_OK;  // fluid.go:113-115
   invalidate(f, kStepFields);
@@ -639,6 +663,7 @@ int fg_apply_viscosity(fg_fluid* f, float dt) {
 }
 
 int fg_add_turbulence(fg_fluid* f, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   if (!(f->prm.turbulence_strength > 0.0f)) return FG_OK;  // fluid.go:497-499
   invalidate(f, kStepFields);
@@ -647,6 +672,7 @@ int fg_add_turbulence(fg_fluid* f, float dt) {
 }
 
 int fg_clear_pressure(fg_fluid* f) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   invalidate(f, FG_FIELD_BIT(FG_P));
   CK(f, cudaMemsetAsync(f->d[FG_P], 0, field_bytes(f), f->stream), "fill p");
@@ -654,6 +680,7 @@ int fg_clear_pressure(fg_fluid* f) {
 }
 
 int fg_copy_border(fg_fluid* f, float* dst, const float* src) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   if (!dst || !src) return fail(f, FG_ERR_INVALID, "null buffer");
   if (!f->copy_tmp)
@@ -671,6 +698,7 @@ int fg_copy_border(fg_fluid* f, float* dst, const float* src) {
 
 // ------------------------------------------------------------------ tools
 int fg_set_solid(fg_fluid* f, int i, int j, int value) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   if (!in_grid(f, i, j)) return fail(f, FG_ERR_INDEX, i < 0 || i >= f->NX ? "invalid x-index" : "invalid y-index");
   int n = f->NY;
@@ -691,6 +719,7 @@ int fg_set_solid(fg_fluid* f, int i, int j, int value) {
 }
 
 int fg_is_solid(const fg_fluid* f, int i, int j, int* out) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || !out) return FG_ERR_INVALID;
   if (!in_grid(f, i, j)) return FG_ERR_INDEX;
   *out = f->hm[FG_S][i * f->NY + j] == 0.0f ? 1 : 0;
@@ -698,6 +727,7 @@ int fg_is_solid(const fg_fluid* f, int i, int j, int* out) {
 }
 
 int fg_set_velocity(fg_fluid* f, int i, int j, float u, float v) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   if (!in_grid(f, i, j)) return fail(f, FG_ERR_INDEX, i < 0 || i >= f->NX ? "invalid x-index" : "invalid y-index");
   int cell = i * f->NY + j;
@@ -707,6 +737,7 @@ int fg_set_velocity(fg_fluid* f, int i, int j, float u, float v) {
 }
 
 int fg_add_smoke(fg_fluid* f, int i, int j, float smoke) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   if (!in_grid(f, i, j)) return fail(f, FG_ERR_INDEX, i < 0 || i >= f->NX ? "invalid x-index" : "invalid y-index");
   edit(f, FG_M, i * f->NY + j, 1, smoke);
@@ -715,6 +746,7 @@ int fg_add_smoke(fg_fluid* f, int i, int j, float smoke) {
 
 int fg_set_velocity_many(fg_fluid* f, int n, const int* is, const int* js, const float* us,
                          const float* vs) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || n < 0 || (n && (!is || !js || !us || !vs))) return FG_ERR_INVALID;
   for (int k = 0; k < n; ++k)
     if (!in_grid(f, is[k], js[k])) return fail(f, FG_ERR_INDEX, "invalid index");
@@ -727,6 +759,7 @@ int fg_set_velocity_many(fg_fluid* f, int n, const int* is, const int* js, const
 }
 
 int fg_add_smoke_many(fg_fluid* f, int n, const int* is, const int* js, const float* ss) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || n < 0 || (n && (!is || !js || !ss))) return FG_ERR_INVALID;
   for (int k = 0; k < n; ++k)
     if (!in_grid(f, is[k], js[k])) return fail(f, FG_ERR_INDEX, "invalid index");
@@ -736,6 +769,7 @@ int fg_add_smoke_many(fg_fluid* f, int n, const int* is, const int* js, const fl
 
 int fg_set_sources(fg_fluid* f, int n, const int* is, const int* js, const float* us,
                    const float* vs, const float* smoke, const int* mode) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || n < 0 || (n && (!is || !js || !mode))) return FG_ERR_INVALID;
   int rc = bind(f);
   if (rc) return rc;
@@ -780,6 +814,7 @@ int fg_set_sources(fg_fluid* f, int n, const int* is, const int* js, const float
 }
 
 int fg_reset(fg_fluid* f) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   int rc = bind(f);
   if (rc) return rc;
@@ -801,6 +836,7 @@ int fg_reset(fg_fluid* f) {
 }
 
 int fg_apply_force(fg_fluid* f, int i, int j, float fx, float fy) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   if (i < 1 || i >= f->NX - 1 || j < 1 || j >= f->NY - 1) return FG_OK;  // fluid.go:762-764
   int cell = i * f->NY + j;
@@ -811,6 +847,7 @@ int fg_apply_force(fg_fluid* f, int i, int j, float fx, float fy) {
 }
 
 int fg_apply_force_radius(fg_fluid* f, int cx, int cy, float fx, float fy, int radius) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   if (radius <= 0) return fg_apply_force(f, cx, cy, fx, fy);
   float r2 = (float)(radius * radius);
@@ -827,6 +864,7 @@ int fg_apply_force_radius(fg_fluid* f, int cx, int cy, float fx, float fy, int r
 }
 
 int fg_set_circular_obstacle(fg_fluid* f, int cx, int cy, int radius) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   for (int i = cx - radius; i <= cx + radius; ++i)
     for (int j = cy - radius; j <= cy + radius; ++j) {
@@ -851,6 +889,7 @@ static float* dev_scalar_slot(fg_fluid* f) {
 }
 
 int fg_max_divergence(fg_fluid* f, float* out) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   if (!out) return FG_ERR_INVALID;
   float* slot = dev_scalar_slot(f);
@@ -880,16 +919,19 @@ static int view_common(fg_fluid* f, int kind, float* out_host, float* mn, float*
 }
 
 int fg_vorticity(fg_fluid* f, float* out_host, float* mn, float* mx) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   return view_common(f, 0, out_host, mn, mx);
 }
 
 int fg_velocity_magnitude(fg_fluid* f, float* out_host, float* mn, float* mx) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   return view_common(f, 1, out_host, mn, mx);
 }
 
 int fg_field_min_max(fg_fluid* f, int field, float* mn, float* mx) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   if (field < 0 || field >= FG_NUM_FIELDS) return fail(f, FG_ERR_INVALID, "bad field");
   float* slot = dev_scalar_slot(f);
@@ -903,6 +945,7 @@ int fg_field_min_max(fg_fluid* f, int field, float* mn, float* mx) {
 }
 
 int fg_sample_velocity(fg_fluid* f, float x, float y, float* u, float* v) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   float* slot = dev_scalar_slot(f);
   CK(f, launch_sample_velocity(f, x, y, slot), "sample");
@@ -915,6 +958,7 @@ int fg_sample_velocity(fg_fluid* f, float x, float y, float* u, float* v) {
 }
 
 int fg_adaptive_time_step(fg_fluid* f, float basedt, float* out) {
+  if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
   if (!out) return FG_ERR_INVALID;
   float* slot = dev_scalar_slot(f);
@@ -1252,6 +1296,7 @@ int fg_step_forward(fg_fluid* f, float dt, const float* force_u, const float* fo
   if (t->n_fwd >= t->max_steps) return fail(f, FG_ERR_INVALID, "rollout longer than max_steps");
   if ((force_u == nullptr) != (force_v == nullptr))
     return fail(f, FG_ERR_INVALID, "give both force components or neither");
+  if (f->batch && force_u) return fail(f, FG_ERR_UNSUPPORTED, "batches take no force fields");
   int k = t->n_fwd;
   if (k > 0 && k % t->every == 0 && (rc = save_state(f, ckpt_at(f, k / t->every)))) return rc;
   if (force_u) {
@@ -1272,6 +1317,7 @@ int fg_step_forward(fg_fluid* f, float dt, const float* force_u, const float* fo
 }
 
 int fg_tape_seed(fg_fluid* f, const float* dU, const float* dV, const float* dM) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   int rc = tape_usable(f);
   if (rc) return rc;
@@ -1291,6 +1337,7 @@ int fg_tape_seed(fg_fluid* f, const float* dU, const float* dV, const float* dM)
 }
 
 int fg_tape_seed_smoke_l2(fg_fluid* f, const float* target, double* loss) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f || !target) return FG_ERR_INVALID;
   int rc = tape_usable(f);
   if (rc) return rc;
@@ -1317,6 +1364,8 @@ int fg_step_adjoint(fg_fluid* f, float* grad_force_u, float* grad_force_v) {
   if (rc) return rc;
   Tape* t = f->tape;
   if (!t->seeded) return fail(f, FG_ERR_INVALID, "seed the adjoint first (fg_tape_seed)");
+  if (f->batch && (grad_force_u || grad_force_v))
+    return fail(f, FG_ERR_UNSUPPORTED, "batches take no force fields");
   if (t->n_rev >= t->n_fwd) return fail(f, FG_ERR_INVALID, "every recorded step is reversed");
   if (!t->final_saved) {
     if ((rc = save_state(f, ckpt_at(f, t->n_ckpt)))) return rc;
@@ -1341,6 +1390,7 @@ int fg_step_adjoint(fg_fluid* f, float* grad_force_u, float* grad_force_v) {
 }
 
 int fg_tape_grad(fg_fluid* f, float* dU, float* dV, float* dM, float* dNU, float* dNV, float* dNM) {
+  if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
   int rc = bind(f);
   if (rc) return rc;
@@ -1360,6 +1410,431 @@ int fg_tape_steps(const fg_fluid* f, int* forward, int* reversed) {
   bool on = f->tape && f->tape->active;
   *forward = on ? f->tape->n_fwd : 0;
   *reversed = on ? f->tape->n_rev : 0;
+  return FG_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batches: many independent scenes of different sizes stepped together.
+//
+// fg_batch_create packs the state of n scene handles into one handle whose
+// fields are the concatenation of the scenes' pitched fields.  Every stage
+// then runs as one launch over a block table that names each block's scene
+// and tile (a pressure solve runs each scene's own sweep count), so a step
+// of the whole batch is a few dozen launches, captured in one CUDA graph by
+// fg_simulate like a single scene's.  The batch handle accepts fg_simulate,
+// the recorded-rollout calls (without force fields) and the batch calls
+// below; entry points that address one scene's cells or mirrors return
+// FG_ERR_UNSUPPORTED.  The member handles are not touched until
+// fg_batch_scatter copies the batch's state back into them.
+// ===========================================================================
+namespace {
+
+// Thread-block shapes (x = j, y = i) the autotuner tries for the per-cell
+// kernels of a batch.
+constexpr int kBatchShapes[5][2] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {128, 2}};
+
+void batch_free(fg::BatchGeom* b) {
+  if (!b) return;
+  cudaFree(b->scenes_dev);
+  cudaFree(b->cell_tiles);
+  cudaFree(b->cell_range);
+  cudaFree(b->border_tiles);
+  cudaFree(b->jac_tiles);
+  cudaFree(b->src_scene);
+  cudaFree(b->losses);
+  delete b;
+}
+
+// Order in which scenes' blocks are laid out: largest first, so the long
+// scenes start early and the small ones fill the tail.
+std::vector<int> batch_order(const fg::BatchGeom* b) {
+  std::vector<int> ord(b->n);
+  for (int s = 0; s < b->n; ++s) ord[s] = s;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) {
+    return (long long)b->scenes[a].g.NX * b->scenes[a].g.NY >
+           (long long)b->scenes[c].g.NX * b->scenes[c].g.NY;
+  });
+  return ord;
+}
+
+template <class T>
+int upload_table(fg_fluid* f, T** dev, const std::vector<T>& host) {
+  cudaFree(*dev);
+  *dev = nullptr;
+  if (host.empty()) return FG_OK;
+  CK(f, cudaMalloc((void**)dev, host.size() * sizeof(T)), "batch table");
+  CK(f, cudaMemcpy(*dev, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice),
+     "batch table");
+  return FG_OK;
+}
+
+// Block table of the per-cell kernels for a bx x by thread-block shape.
+int batch_cell_tiles(fg_fluid* f, int bx, int by) {
+  fg::BatchGeom* b = f->batch;
+  std::vector<BTile> tiles;
+  std::vector<int> range(2 * b->n);
+  for (int s : batch_order(b)) {
+    const Grid& g = b->scenes[s].g;
+    range[2 * s] = (int)tiles.size();
+    for (int ty = 0; ty < (g.NX + by - 1) / by; ++ty)
+      for (int tx = 0; tx < (g.NY + bx - 1) / bx; ++tx) tiles.push_back(BTile{s, tx, ty, 0});
+    range[2 * s + 1] = (int)tiles.size();
+  }
+  CK(f, cudaStreamSynchronize(f->stream), "batch sync");
+  int rc = upload_table(f, &b->cell_tiles, tiles);
+  if (rc || (rc = upload_table(f, &b->cell_range, range))) return rc;
+  b->bx = bx;
+  b->by = by;
+  b->n_cell_tiles = (int)tiles.size();
+  return FG_OK;
+}
+
+// Copies the members' state, flags and noise into the packed fields.
+int batch_pack(fg_fluid* f) {
+  fg::BatchGeom* b = f->batch;
+  for (int s = 0; s < b->n; ++s) {
+    fg_fluid* m = b->members[s];
+    int rc = flush(m);
+    if (rc) return fail(f, rc, "member flush failed");
+    CK(f, cudaStreamSynchronize(m->stream), "member sync");
+    long long off = b->scenes[s].off;
+    size_t n = (size_t)m->NX * m->P;
+    for (int k = 0; k < FG_NUM_FIELDS; ++k)
+      CK(f, cudaMemcpyAsync(f->d[k] + off, m->d[k], n * sizeof(float), cudaMemcpyDeviceToDevice,
+                            f->stream), "batch pack");
+    CK(f, cudaMemcpyAsync(f->flags + off, m->flags, n, cudaMemcpyDeviceToDevice, f->stream),
+       "batch pack");
+    CK(f, cudaMemcpyAsync(f->noise + off, m->noise, n * sizeof(float2), cudaMemcpyDeviceToDevice,
+                          f->stream), "batch pack");
+  }
+  CK(f, cudaStreamSynchronize(f->stream), "batch pack");
+  return FG_OK;
+}
+
+int batch_check_member(fg_fluid* f, const fg_fluid* m, const fg_fluid* m0) {
+  const fg_params& p = m->prm;
+  if (m->batch) return fail(f, FG_ERR_INVALID, "a batch cannot hold a batch");
+  if (m->device != m0->device) return fail(f, FG_ERR_INVALID, "batch members on different devices");
+  if (p.scheme != FG_SCHEME_JACOBI || p.early_exit || p.refine_sweeps > 0 ||
+      p.viscosity_diffusion > 0.0f || (p.use_multigrid && p.multigrid_levels > 1))
+    return fail(f, FG_ERR_UNSUPPORTED,
+                "batch members need the Jacobi scheme without early exit, refinement, "
+                "viscosity or multigrid");
+  if (p.num_iters < 1) return fail(f, FG_ERR_INVALID, "batch members need num_iters >= 1");
+  fg_params a = p, c = m0->prm;
+  a.num_iters = c.num_iters = 0;
+  a.tb_depth = c.tb_depth = 0;
+  a.use_graphs = c.use_graphs = 0;
+  if (memcmp(&a, &c, sizeof a) != 0 || m->density != m0->density || m->h != m0->h)
+    return fail(f, FG_ERR_INVALID, "batch members must share parameters except num_iters");
+  return FG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_batch_create(fg_fluid* const* scenes, int n, fg_fluid** out) {
+  if (!scenes || n < 1 || !out) return FG_ERR_INVALID;
+  *out = nullptr;
+  for (int s = 0; s < n; ++s)
+    if (!scenes[s]) return FG_ERR_INVALID;
+  fg_fluid* f = new fg_fluid();
+  auto bail = [&](int code) {
+    std::string msg = f->last_error;
+    fg_destroy(f);
+    // The reason stays readable on the first member.
+    if (!msg.empty()) scenes[0]->last_error = msg;
+    return code;
+  };
+  f->batch = new fg::BatchGeom();
+  fg::BatchGeom* b = f->batch;
+  b->n = n;
+  int rc;
+  for (int s = 0; s < n; ++s)
+    if ((rc = batch_check_member(f, scenes[s], scenes[0]))) return bail(rc);
+  f->device = scenes[0]->device;
+  if (cudaSetDevice(f->device) != cudaSuccess) return bail(FG_ERR_CUDA);
+  f->prm = scenes[0]->prm;
+  f->density = scenes[0]->density;
+  f->h = scenes[0]->h;
+  // Packed layout: scene s at element offset off_s, each slice a multiple of
+  // 32 floats (128 bytes) long.
+  long long total = 0;
+  for (int s = 0; s < n; ++s) {
+    const fg_fluid* m = scenes[s];
+    BScene sc;
+    sc.g = m->g;
+    sc.off = total;
+    sc.iters = m->prm.num_iters;
+    sc.pad = 0;
+    b->scenes.push_back(sc);
+    b->members.push_back(scenes[s]);
+    b->max_iters = std::max(b->max_iters, m->prm.num_iters);
+    total += (long long)m->NX * m->P;
+  }
+  f->prm.num_iters = b->max_iters;
+  f->NX = 1;
+  f->NY = (int)std::min<long long>(total, 1 << 30);
+  f->P = (int)total;
+  if (total >= (1ll << 31)) return bail(fail(f, FG_ERR_INVALID, "batch larger than 2^31 cells"));
+  f->g = make_grid(1, f->NY, f->P, f->h);
+  if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(FG_ERR_CUDA);
+  for (int k = 0; k < 2; ++k) {
+    if (cudaEventCreateWithFlags(&f->edit_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return bail(FG_ERR_CUDA);
+    if (cudaEventCreate(&f->prof_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
+  }
+  for (int k = 0; k < fg_fluid::kMaxMarks; ++k)
+    if (cudaEventCreate(&f->mark_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
+  for (int k = 0; k < FG_NUM_FIELDS; ++k)
+    if ((rc = alloc_dev(f, &f->d[k]))) return bail(rc);
+  for (int k : {FG_U, FG_V, FG_M})
+    if ((rc = alloc_dev(f, &f->partner[k]))) return bail(rc);
+  float** scratch[] = {&f->fwdU, &f->fwdV, &f->fwdM, &f->corrU, &f->corrV, &f->corrM,
+                       &f->phi,  &f->phi2, &f->rhs,  &f->err,   &f->err2,  &f->rhs_e,
+                       &f->curl, &f->view, &f->wgt,  &f->bw,    &f->bwe};
+  for (float** sp : scratch)
+    if ((rc = alloc_dev(f, sp))) return bail(rc);
+  if (cudaMalloc((void**)&f->noise, total * sizeof(float2)) != cudaSuccess ||
+      cudaMalloc((void**)&f->flags, total) != cudaSuccess)
+    return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
+  cudaMemsetAsync(f->flags, 0, total, f->stream);
+  f->n_slots = kSlots;
+  if (cudaMalloc(&f->pctl, pctl_bytes(f->n_slots)) != cudaSuccess ||
+      cudaMalloc(&f->ectl, pctl_bytes(f->n_slots)) != cudaSuccess ||
+      cudaMalloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess ||
+      cudaMalloc((void**)&b->losses, sizeof(double) * n) != cudaSuccess)
+    return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
+  cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream);
+  cudaMemsetAsync(f->ectl, 0, pctl_bytes(f->n_slots), f->stream);
+  cudaMemsetAsync(f->dstats, 0, sizeof(DevStats), f->stream);
+  if (cudaMallocHost((void**)&f->scalar_pinned, 64 * sizeof(float)) != cudaSuccess ||
+      cudaMallocHost((void**)&f->stats_pinned, sizeof(DevStats)) != cudaSuccess)
+    return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
+  // Block tables.
+  if ((rc = upload_table(f, &b->scenes_dev, b->scenes))) return bail(rc);
+  if ((rc = batch_cell_tiles(f, 32, 8))) return bail(rc);
+  std::vector<BTile> bt, jt;
+  for (int s : batch_order(b)) {
+    const Grid& g = b->scenes[s].g;
+    for (int t = 0; t < (std::max(g.NX, g.NY) + 127) / 128; ++t) bt.push_back(BTile{s, t, 0, 0});
+    for (int ty = 0; ty < (g.NX + kJacTileRows - 1) / kJacTileRows; ++ty)
+      for (int tx = 0; tx < (g.NY + kJacTileCols - 1) / kJacTileCols; ++tx)
+        jt.push_back(BTile{s, tx, ty, 0});
+  }
+  if ((rc = upload_table(f, &b->border_tiles, bt)) || (rc = upload_table(f, &b->jac_tiles, jt)))
+    return bail(rc);
+  b->n_border_tiles = (int)bt.size();
+  b->n_jac_tiles = (int)jt.size();
+  // Partial rows of the per-scene loss: one float pair per cell tile for the
+  // block shape with the most tiles, plus the reserve partials_fit keeps.
+  long long max_tiles = 0;
+  for (const auto& sh : kBatchShapes) {
+    long long nt = 0;
+    for (const BScene& sc : b->scenes)
+      nt += (long long)((sc.g.NX + sh[1] - 1) / sh[1]) * ((sc.g.NY + sh[0] - 1) / sh[0]);
+    max_tiles = std::max(max_tiles, nt);
+  }
+  f->n_partials = (int)(2 * (max_tiles + max_tiles / 2048 + 2) + 512);
+  if (cudaMalloc((void**)&f->partials, sizeof(float) * f->n_partials) != cudaSuccess)
+    return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
+  // Sources: the members' groups, each tagged with its scene.
+  std::vector<SourceRec> recs;
+  std::vector<uint32_t> off;
+  std::vector<int> gscene;
+  for (int s = 0; s < n; ++s) {
+    const fg_fluid* m = scenes[s];
+    if (m->n_src_groups <= 0) continue;
+    std::vector<uint32_t> moff(m->n_src_groups + 1);
+    if (cudaMemcpy(moff.data(), m->src_off_dev, moff.size() * sizeof(uint32_t),
+                   cudaMemcpyDeviceToHost) != cudaSuccess)
+      return bail(FG_ERR_CUDA);
+    std::vector<SourceRec> mr(moff.back());
+    if (cudaMemcpy(mr.data(), m->src_dev, mr.size() * sizeof(SourceRec),
+                   cudaMemcpyDeviceToHost) != cudaSuccess)
+      return bail(FG_ERR_CUDA);
+    for (int k = 0; k < m->n_src_groups; ++k) {
+      off.push_back((uint32_t)recs.size());
+      for (uint32_t q = moff[k]; q < moff[k + 1]; ++q) recs.push_back(mr[q]);
+      gscene.push_back(s);
+    }
+  }
+  if (!recs.empty()) {
+    off.push_back((uint32_t)recs.size());
+    if ((rc = upload_table(f, &f->src_dev, recs)) || (rc = upload_table(f, &f->src_off_dev, off)) ||
+        (rc = upload_table(f, &b->src_scene, gscene)))
+      return bail(rc);
+    f->n_src_groups = (int)gscene.size();
+  }
+  if ((rc = batch_pack(f))) return bail(rc);
+  f->masks_stale = false;
+  *out = f;
+  return FG_OK;
+}
+
+int fg_batch_step(fg_fluid* f, float dt) {
+  if (!f || !f->batch) return FG_ERR_INVALID;
+  return fg_simulate(f, dt);
+}
+
+int fg_batch_step_adjoint(fg_fluid* f) {
+  if (!f || !f->batch) return FG_ERR_INVALID;
+  return fg_step_adjoint(f, nullptr, nullptr);
+}
+
+int fg_batch_size(const fg_fluid* f, int* n) {
+  if (!f || !f->batch || !n) return FG_ERR_INVALID;
+  *n = f->batch->n;
+  return FG_OK;
+}
+
+int fg_batch_gather(fg_fluid* f) {
+  if (!f || !f->batch) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  if (f->tape && f->tape->active) return fail(f, FG_ERR_INVALID, "a recorded rollout is open");
+  return batch_pack(f);
+}
+
+int fg_batch_scatter(fg_fluid* f) {
+  if (!f || !f->batch) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  const fg::BatchGeom* b = f->batch;
+  CK(f, cudaStreamSynchronize(f->stream), "batch sync");
+  for (int s = 0; s < b->n; ++s) {
+    fg_fluid* m = b->members[s];
+    size_t n = (size_t)m->NX * m->P;
+    for (int k = 0; k < FG_NUM_FIELDS; ++k) {
+      if (k == FG_S) continue;
+      CK(f, cudaMemcpyAsync(m->d[k], f->d[k] + b->scenes[s].off, n * sizeof(float),
+                            cudaMemcpyDeviceToDevice, f->stream), "batch scatter");
+    }
+    invalidate(m, kStepFields);
+  }
+  CK(f, cudaStreamSynchronize(f->stream), "batch scatter");
+  return FG_OK;
+}
+
+// Seeds a batch's rollout with L_s = ||M_s - target_s||_2 for every scene
+// (targets[s]: the scene's NumX * NumY values, host or device memory).
+int fg_batch_seed_smoke_l2(fg_fluid* f, const float* const* targets, double* losses) {
+  if (!f || !f->batch || !targets) return FG_ERR_INVALID;
+  int rc = tape_usable(f);
+  if (rc) return rc;
+  Tape* t = f->tape;
+  if (t->n_fwd == 0 || t->n_rev > 0)
+    return fail(f, FG_ERR_INVALID, "seed the adjoint after the forward steps, before reversing");
+  const fg::BatchGeom* b = f->batch;
+  CK(f, cudaMemsetAsync(t->aux, 0, field_bytes(f), f->stream), "seed");
+  for (int s = 0; s < b->n; ++s) {
+    if (!targets[s]) return fail(f, FG_ERR_INVALID, "missing target");
+    const Grid& g = b->scenes[s].g;
+    size_t hp = sizeof(float) * g.NY, dp = sizeof(float) * g.P;
+    CK(f, cudaMemcpy2DAsync(t->aux + b->scenes[s].off, dp, targets[s], hp, hp, g.NX,
+                            cudaMemcpyDefault, f->stream), "target upload");
+  }
+  CK(f, launch_loss_seed(f, t->aux, nullptr), "loss");
+  t->seeded = true;
+  if (losses) {
+    CK(f, cudaMemcpyAsync(losses, b->losses, sizeof(double) * b->n, cudaMemcpyDefault, f->stream),
+       "losses");
+    CK(f, cudaStreamSynchronize(f->stream), "losses");
+  }
+  return FG_OK;
+}
+
+// dL/d(initial U, V, M) of scene s after a batch's reverse pass (the
+// scene's NumX * NumY layout; NULL: skipped).
+int fg_batch_grad(fg_fluid* f, int s, float* dU, float* dV, float* dM) {
+  if (!f || !f->batch || s < 0 || s >= f->batch->n) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  if (!f->tape || !f->tape->active || !f->tape->seeded)
+    return fail(f, FG_ERR_INVALID, "no seeded rollout");
+  const BScene& sc = f->batch->scenes[s];
+  float* out[3] = {dU, dV, dM};
+  const int src[3] = {fg_fluid::A_U, fg_fluid::A_V, fg_fluid::A_M};
+  size_t hp = sizeof(float) * sc.g.NY, dp = sizeof(float) * sc.g.P;
+  for (int k = 0; k < 3; ++k)
+    if (out[k])
+      CK(f, cudaMemcpy2DAsync(out[k], hp, f->adj[src[k]] + sc.off, dp, hp, sc.g.NX,
+                              cudaMemcpyDefault, f->stream), "grad");
+  CK(f, cudaStreamSynchronize(f->stream), "grad sync");
+  return FG_OK;
+}
+
+// Picks the per-cell thread-block shape and the Jacobi sweeps per launch
+// that step this batch fastest: each candidate runs `reps` timed steps
+// (after one untimed step that also captures its graph) from the same
+// saved state, which is restored afterwards.  Neither choice changes any
+// result bit.
+int fg_batch_autotune(fg_fluid* f, float dt, int reps, int* tb_depth, int* block_x, int* block_y,
+                      float* ms_per_step) {
+  if (!f || !f->batch || reps < 1) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  if (f->tape && f->tape->active) return fail(f, FG_ERR_INVALID, "a recorded rollout is open");
+  const auto& shapes = kBatchShapes;
+  static const int depths[] = {4, 6, 8};
+  size_t fb = field_bytes(f);
+  float* saved = nullptr;
+  CK(f, cudaMalloc((void**)&saved, fb * 7), "autotune");
+  auto save = [&]() {
+    int r = save_state(f, saved);
+    if (!r) r = copy_field(f, saved + 6 * field_elems(f), f->d[FG_P]);
+    return r;
+  };
+  auto restore = [&]() {
+    int r = load_state(f, saved);
+    if (!r) r = copy_field(f, f->d[FG_P], saved + 6 * field_elems(f));
+    return r;
+  };
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int bb = 0, bd = 0;
+  rc = save();
+  for (int si = 0; !rc && si < (int)(sizeof shapes / sizeof shapes[0]); ++si) {
+    if ((rc = batch_cell_tiles(f, shapes[si][0], shapes[si][1]))) break;
+    for (int di = 0; !rc && di < (int)(sizeof depths / sizeof depths[0]); ++di) {
+      f->prm.tb_depth = depths[di];
+      f->params_version++;
+      clear_graphs(f);
+      if ((rc = fg_simulate(f, dt))) break;
+      cudaEventRecord(e0, f->stream);
+      for (int r = 0; r < reps && !rc; ++r) rc = fg_simulate(f, dt);
+      cudaEventRecord(e1, f->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(f, FG_ERR_CUDA, "autotune");
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= (float)reps;
+      if (!rc && ms < best) {
+        best = ms;
+        bb = si;
+        bd = di;
+      }
+      if (!rc) rc = restore();
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!rc) rc = batch_cell_tiles(f, shapes[bb][0], shapes[bb][1]);
+  f->prm.tb_depth = depths[bd];
+  f->params_version++;
+  clear_graphs(f);
+  cudaStreamSynchronize(f->stream);
+  cudaFree(saved);
+  if (rc) return rc;
+  if (tb_depth) *tb_depth = depths[bd];
+  if (block_x) *block_x = shapes[bb][0];
+  if (block_y) *block_y = shapes[bb][1];
+  if (ms_per_step) *ms_per_step = best;
   return FG_OK;
 }
 

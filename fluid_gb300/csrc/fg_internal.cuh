@@ -122,6 +122,42 @@ struct DevStats {  // device-side accumulation target (finalised per step)
   int pad;
 };
 
+// ---------------------------------------------------------------- batches
+// A batch packs many scenes of different sizes into the same per-field
+// arrays: scene s occupies NX_s rows of pitch P_s starting at element
+// offset off_s of every field (the flag bytes and noise pairs at the same
+// element offset of theirs).  Kernels run over a block table: one entry per
+// thread block naming the scene and the tile within it.
+struct BScene {
+  Grid g;
+  long long off;  // element offset of the scene in the packed arrays
+  int iters;      // Jacobi sweeps of the scene's pressure solve
+  int pad;
+};
+struct BTile {
+  int s, x, y, pad;  // scene, tile column, tile row
+};
+// Cells a Jacobi thread block owns (rows x columns; k_pressure.cu).
+constexpr int kJacTileRows = 48, kJacTileCols = 112;
+
+struct BatchGeom {
+  int n = 0;
+  std::vector<BScene> scenes;
+  std::vector<fg_fluid*> members;  // the scene handles (not owned)
+  BScene* scenes_dev = nullptr;
+  int bx = 32, by = 8;  // thread-block shape of the per-cell kernels (autotuned)
+  BTile* cell_tiles = nullptr;
+  int n_cell_tiles = 0;
+  int* cell_range = nullptr;  // device: [first, end) cell tiles of each scene (2 n entries)
+  BTile* border_tiles = nullptr;
+  int n_border_tiles = 0;
+  BTile* jac_tiles = nullptr;
+  int n_jac_tiles = 0;
+  int max_iters = 0;
+  int* src_scene = nullptr;  // device: scene of each source group
+  double* losses = nullptr;  // device: per-scene loss of the last seed
+};
+
 }  // namespace fg
 
 struct fg_fluid {
@@ -181,6 +217,8 @@ struct fg_fluid {
          A_COUNT };
   float* adj[A_COUNT] = {};
   struct Tape* tape = nullptr;
+  // Non-null when this handle is a batch of scenes (fg_batch_create).
+  fg::BatchGeom* batch = nullptr;
   // Kernel launches enqueued so far (graph replays add the captured count).
   unsigned long long launches = 0;
   // Optional CUDA-event bracket around the main Jacobi launches of a solve.

@@ -28,6 +28,7 @@
 // about 1e-7 relative, not bit for bit.
 #include <utility>
 
+#include "fg_batch.cuh"
 #include "fg_internal.cuh"
 #include "fg_reduce.cuh"
 
@@ -52,14 +53,19 @@ __device__ __forceinline__ bool fluid_interior(uint8_t fl) {
 }
 
 // Forward: U += Fu, V += Fv on every cell.
+__device__ __forceinline__ void add_forces_cell(int i, int j, float* __restrict__ U,
+                                                float* __restrict__ V, const float* __restrict__ Fu,
+                                                const float* __restrict__ Fv, const Grid& g) {
+  int c = i * g.P + j;
+  U[c] = U[c] + Fu[c];
+  V[c] = V[c] + Fv[c];
+}
 __global__ void k_add_forces(float* __restrict__ U, float* __restrict__ V,
                              const float* __restrict__ Fu, const float* __restrict__ Fv, Grid g) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
-  int c = i * g.P + j;
-  U[c] = U[c] + Fu[c];
-  V[c] = V[c] + Fv[c];
+  add_forces_cell(i, j, U, V, Fu, Fv, g);
 }
 
 // Adjoint of a bilinear sample of field F at (x, y) (sampleField): scatters
@@ -95,15 +101,16 @@ __device__ __forceinline__ void sample_adjoint(const float* __restrict__ F, floa
 // : ring ? R : stale.  lamU/lamV hold the output adjoint.  Accumulates into
 // dFu/dFv (sampled field), dUt/dVt (tracing velocity), dRu/dRv (ring source,
 // may be null: no ring term) and dNu/dNv (stale source, may be null).
-__global__ void k_adj_sl_velocity(const float* __restrict__ lamU, const float* __restrict__ lamV,
-                                  const float* __restrict__ Ut, const float* __restrict__ Vt,
-                                  const float* __restrict__ Fu, const float* __restrict__ Fv,
-                                  float* dUt, float* dVt, float* dFu, float* dFv, float* dRu,
-                                  float* dRv, float* dNu, float* dNv,
-                                  const uint8_t* __restrict__ flags, float sdt, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void adj_sl_velocity_cell(int i, int j, const float* __restrict__ lamU,
+                                                     const float* __restrict__ lamV,
+                                                     const float* __restrict__ Ut,
+                                                     const float* __restrict__ Vt,
+                                                     const float* __restrict__ Fu,
+                                                     const float* __restrict__ Fv, float* dUt,
+                                                     float* dVt, float* dFu, float* dFv, float* dRu,
+                                                     float* dRv, float* dNu, float* dNv,
+                                                     const uint8_t* __restrict__ flags, float sdt,
+                                                     const Grid& g) {
   const int P = g.P;
   int c = i * P + j;
   uint8_t fl = flags[c];
@@ -154,6 +161,17 @@ __global__ void k_adj_sl_velocity(const float* __restrict__ lamU, const float* _
     dNv[c] += lv;
   }
 }
+__global__ void k_adj_sl_velocity(const float* __restrict__ lamU, const float* __restrict__ lamV,
+                                  const float* __restrict__ Ut, const float* __restrict__ Vt,
+                                  const float* __restrict__ Fu, const float* __restrict__ Fv,
+                                  float* dUt, float* dVt, float* dFu, float* dFv, float* dRu,
+                                  float* dRv, float* dNu, float* dNv,
+                                  const uint8_t* __restrict__ flags, float sdt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  adj_sl_velocity_cell(i, j, lamU, lamV, Ut, Vt, Fu, Fv, dUt, dVt, dFu, dFv, dRu, dRv, dNu, dNv, flags, sdt, g);
+}
 
 // clampToNeighbors (fluid.go:1094-1120) on an interior cell: returns the
 // offset (in elements) of the neighbour whose value bounded `val`, or -1 if
@@ -187,14 +205,15 @@ __device__ __forceinline__ int clamp_source(float val, const float* __restrict__
 // (0 on the others), corr = clamp(o - (bwd - o) * 0.5) on interior faces,
 // corr = o on the ring.  Reads lamC (adjoint of corr); accumulates into dO
 // (the original field, which is also the tracing velocity) and dF (fwd).
-__global__ void k_adj_bfecc_vel(const float* __restrict__ lamCu, const float* __restrict__ lamCv,
-                                const float* __restrict__ Ou, const float* __restrict__ Ov,
-                                const float* __restrict__ Fu, const float* __restrict__ Fv,
-                                float* dOu, float* dOv, float* dFu, float* dFv,
-                                const uint8_t* __restrict__ flags, float dt, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void adj_bfecc_vel_cell(int i, int j, const float* __restrict__ lamCu,
+                                                   const float* __restrict__ lamCv,
+                                                   const float* __restrict__ Ou,
+                                                   const float* __restrict__ Ov,
+                                                   const float* __restrict__ Fu,
+                                                   const float* __restrict__ Fv, float* dOu,
+                                                   float* dOv, float* dFu, float* dFv,
+                                                   const uint8_t* __restrict__ flags, float dt,
+                                                   const Grid& g) {
   const int P = g.P;
   int c = i * P + j;
   float lu = lamCu[c], lv = lamCv[c];
@@ -264,20 +283,29 @@ __global__ void k_adj_bfecc_vel(const float* __restrict__ lamCu, const float* __
     }
   }
 }
+__global__ void k_adj_bfecc_vel(const float* __restrict__ lamCu, const float* __restrict__ lamCv,
+                                const float* __restrict__ Ou, const float* __restrict__ Ov,
+                                const float* __restrict__ Fu, const float* __restrict__ Fv,
+                                float* dOu, float* dOv, float* dFu, float* dFv,
+                                const uint8_t* __restrict__ flags, float dt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  adj_bfecc_vel_cell(i, j, lamCu, lamCv, Ou, Ov, Fu, Fv, dOu, dOv, dFu, dFv, flags, dt, g);
+}
 
 // Adjoint of a semi-Lagrangian smoke pass (advectSmoke fluid.go:400-434,
 // without the diffusion term): out = fluid interior ? max(sample(Ms), 0) :
 // ring ? Ms : stale.  With bwd = 1 the pass is BFECC's reverse sample (no
 // max, non-fluid cells constant 0, no ring / stale terms).  The trace
 // velocity is ((U[c] + U[c+P]) / 2 * SA, (V[c] + V[c+1]) / 2 * SA).
-__global__ void k_adj_sl_smoke(const float* __restrict__ lamM, const float* __restrict__ U,
-                               const float* __restrict__ V, const float* __restrict__ Ms,
-                               float* dU, float* dV, float* dMs, float* dN,
-                               const uint8_t* __restrict__ flags, float sdt, float smokeAdv,
-                               int bwd, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void adj_sl_smoke_cell(int i, int j, const float* __restrict__ lamM,
+                                                  const float* __restrict__ U,
+                                                  const float* __restrict__ V,
+                                                  const float* __restrict__ Ms, float* dU,
+                                                  float* dV, float* dMs, float* dN,
+                                                  const uint8_t* __restrict__ flags, float sdt,
+                                                  float smokeAdv, int bwd, const Grid& g) {
   const int P = g.P;
   int c = i * P + j;
   uint8_t fl = flags[c];
@@ -312,20 +340,30 @@ __global__ void k_adj_sl_smoke(const float* __restrict__ lamM, const float* __re
     }
   }
 }
+__global__ void k_adj_sl_smoke(const float* __restrict__ lamM, const float* __restrict__ U,
+                               const float* __restrict__ V, const float* __restrict__ Ms,
+                               float* dU, float* dV, float* dMs, float* dN,
+                               const uint8_t* __restrict__ flags, float sdt, float smokeAdv,
+                               int bwd, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  adj_sl_smoke_cell(i, j, lamM, U, V, Ms, dU, dV, dMs, dN, flags, sdt, smokeAdv, bwd, g);
+}
 
 // Adjoint of BFECC's smoke passes 2-3 (fluid.go:1013-1046), fused: bwd =
 // sample(fwd; trace with (U, V) at -dt) on fluid interior cells (0 on the
 // others), corr = max(clamp(o - (bwd - o) * 0.5), 0) on interior cells, o on
 // the ring.  Reads lamC; accumulates into dO (original smoke), dF (fwd) and
 // dU, dV (the tracing velocity).
-__global__ void k_adj_bfecc_smoke(const float* __restrict__ lamC, const float* __restrict__ U,
-                                  const float* __restrict__ V, const float* __restrict__ Mo,
-                                  const float* __restrict__ Fm, float* dO, float* dF, float* dU,
-                                  float* dV, const uint8_t* __restrict__ flags, float dt,
-                                  float smokeAdv, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void adj_bfecc_smoke_cell(int i, int j, const float* __restrict__ lamC,
+                                                     const float* __restrict__ U,
+                                                     const float* __restrict__ V,
+                                                     const float* __restrict__ Mo,
+                                                     const float* __restrict__ Fm, float* dO,
+                                                     float* dF, float* dU, float* dV,
+                                                     const uint8_t* __restrict__ flags, float dt,
+                                                     float smokeAdv, const Grid& g) {
   const int P = g.P;
   int c = i * P + j;
   float lam = lamC[c];
@@ -367,14 +405,25 @@ __global__ void k_adj_bfecc_smoke(const float* __restrict__ lamC, const float* _
     atomicAdd(&dV[c + 1], dv);
   }
 }
+__global__ void k_adj_bfecc_smoke(const float* __restrict__ lamC, const float* __restrict__ U,
+                                  const float* __restrict__ V, const float* __restrict__ Mo,
+                                  const float* __restrict__ Fm, float* dO, float* dF, float* dU,
+                                  float* dV, const uint8_t* __restrict__ flags, float dt,
+                                  float smokeAdv, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  adj_bfecc_smoke_cell(i, j, lamC, U, V, Mo, Fm, dO, dF, dU, dV, flags, dt, smokeAdv, g);
+}
 
 // Adjoint of handleBorders (fluid.go:236-289), in place on (dU, dV): each
 // ghost value was written from interior values or 0.  Thread t reverses the
 // U rows of column i = t (bottom row first: it was written last) and the V
 // columns of row j = t.
-__global__ void k_adj_borders(float* __restrict__ dU, float* __restrict__ dV,
-                              const uint8_t* __restrict__ flags, Grid g) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void adj_borders_border(int t, float* __restrict__ dU,
+                                                   float* __restrict__ dV,
+                                                   const uint8_t* __restrict__ flags,
+                                                   const Grid& g) {
   const int P = g.P, NX = g.NX, NY = g.NY;
   auto fluid = [&](int i, int j) { return (flags[i * P + j] & F_FLUID) != 0; };
   if (t < NX) {
@@ -426,16 +475,21 @@ __global__ void k_adj_borders(float* __restrict__ dU, float* __restrict__ dV,
     }
   }
 }
+__global__ void k_adj_borders(float* __restrict__ dU, float* __restrict__ dV,
+                              const uint8_t* __restrict__ flags, Grid g) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  adj_borders_border(t, dU, dV, flags, g);
+}
 
 // Adjoint of addTurbulence (fluid.go:496-526) at the pre-turbulence field
 // (U2, V2), in place on (dU, dV).
-__global__ void k_adj_turbulence(float* __restrict__ dU, float* __restrict__ dV,
-                                 const float* __restrict__ U2, const float* __restrict__ V2,
-                                 const float2* __restrict__ noise,
-                                 const uint8_t* __restrict__ flags, float turbStrength, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void adj_turbulence_cell(int i, int j, float* __restrict__ dU,
+                                                    float* __restrict__ dV,
+                                                    const float* __restrict__ U2,
+                                                    const float* __restrict__ V2,
+                                                    const float2* __restrict__ noise,
+                                                    const uint8_t* __restrict__ flags,
+                                                    float turbStrength, const Grid& g) {
   int c = i * g.P + j;
   if (!fluid_interior(flags[c])) return;
   float u = U2[c], v = V2[c];
@@ -450,6 +504,15 @@ __global__ void k_adj_turbulence(float* __restrict__ dU, float* __restrict__ dV,
   float s = (lu * nu + lv * nv) * fp;
   dU[c] = lu + s * au;
   dV[c] = lv + s * av;
+}
+__global__ void k_adj_turbulence(float* __restrict__ dU, float* __restrict__ dV,
+                                 const float* __restrict__ U2, const float* __restrict__ V2,
+                                 const float2* __restrict__ noise,
+                                 const uint8_t* __restrict__ flags, float turbStrength, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  adj_turbulence_cell(i, j, dU, dV, U2, V2, noise, flags, turbStrength, g);
 }
 
 // ---------------------------------------------------------------- confinement
@@ -470,15 +533,15 @@ __device__ __forceinline__ float curl_at(const float* __restrict__ U, const floa
 // normalised gradient's inputs (lgx, lgy: d/d gx, d/d gy), 0 on every other
 // cell.  Subgradients: |curl| passes sign(curl) (0 at 0); at |grad| = 0 the
 // normalisation's derivative is I / eps.
-__global__ void k_adj_conf_local(float* __restrict__ dU, float* __restrict__ dV,
-                                 const float* __restrict__ U2, const float* __restrict__ V2,
-                                 const float2* __restrict__ noise,
-                                 const uint8_t* __restrict__ flags, float conf, float dt,
-                                 float turbStrength, int do_turb, float* __restrict__ lw,
-                                 float* __restrict__ lgx, float* __restrict__ lgy, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void adj_conf_local_cell(int i, int j, float* __restrict__ dU,
+                                                    float* __restrict__ dV,
+                                                    const float* __restrict__ U2,
+                                                    const float* __restrict__ V2,
+                                                    const float2* __restrict__ noise,
+                                                    const uint8_t* __restrict__ flags, float conf,
+                                                    float dt, float turbStrength, int do_turb,
+                                                    float* __restrict__ lw, float* __restrict__ lgx,
+                                                    float* __restrict__ lgy, const Grid& g) {
   const int P = g.P;
   int c = i * P + j;
   if (!fluid_interior(flags[c])) {
@@ -535,16 +598,28 @@ __global__ void k_adj_conf_local(float* __restrict__ dU, float* __restrict__ dV,
   lgx[c] = qx;
   lgy[c] = qy;
 }
-
-// Adjoint of every cell's curl: its direct use plus the |curl| terms of the
-// four neighbours' gradients.  Gathers lgx, lgy from the neighbours.
-__global__ void k_adj_conf_curl(const float* __restrict__ U2, const float* __restrict__ V2,
-                                const float* __restrict__ lwd, const float* __restrict__ lgx,
-                                const float* __restrict__ lgy, float* __restrict__ lw,
-                                const uint8_t* __restrict__ flags, Grid g) {
+__global__ void k_adj_conf_local(float* __restrict__ dU, float* __restrict__ dV,
+                                 const float* __restrict__ U2, const float* __restrict__ V2,
+                                 const float2* __restrict__ noise,
+                                 const uint8_t* __restrict__ flags, float conf, float dt,
+                                 float turbStrength, int do_turb, float* __restrict__ lw,
+                                 float* __restrict__ lgx, float* __restrict__ lgy, Grid g) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
+  adj_conf_local_cell(i, j, dU, dV, U2, V2, noise, flags, conf, dt, turbStrength, do_turb, lw, lgx, lgy, g);
+}
+
+// Adjoint of every cell's curl: its direct use plus the |curl| terms of the
+// four neighbours' gradients.  Gathers lgx, lgy from the neighbours.
+__device__ __forceinline__ void adj_conf_curl_cell(int i, int j, const float* __restrict__ U2,
+                                                   const float* __restrict__ V2,
+                                                   const float* __restrict__ lwd,
+                                                   const float* __restrict__ lgx,
+                                                   const float* __restrict__ lgy,
+                                                   float* __restrict__ lw,
+                                                   const uint8_t* __restrict__ flags,
+                                                   const Grid& g) {
   const int P = g.P;
   int c = i * P + j;
   float out = 0.0f;
@@ -556,14 +631,21 @@ __global__ void k_adj_conf_curl(const float* __restrict__ U2, const float* __res
   }
   lw[c] = out;
 }
-
-// curl^T: dU[m] += (lw[m+1] - lw[m-1]) / 2h, dV[m] += (lw[m-P] - lw[m+P]) / 2h
-// (lw is 0 off the fluid interior cells).
-__global__ void k_adj_conf_apply(float* __restrict__ dU, float* __restrict__ dV,
-                                 const float* __restrict__ lw, Grid g) {
+__global__ void k_adj_conf_curl(const float* __restrict__ U2, const float* __restrict__ V2,
+                                const float* __restrict__ lwd, const float* __restrict__ lgx,
+                                const float* __restrict__ lgy, float* __restrict__ lw,
+                                const uint8_t* __restrict__ flags, Grid g) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
+  adj_conf_curl_cell(i, j, U2, V2, lwd, lgx, lgy, lw, flags, g);
+}
+
+// curl^T: dU[m] += (lw[m+1] - lw[m-1]) / 2h, dV[m] += (lw[m-P] - lw[m+P]) / 2h
+// (lw is 0 off the fluid interior cells).
+__device__ __forceinline__ void adj_conf_apply_cell(int i, int j, float* __restrict__ dU,
+                                                    float* __restrict__ dV,
+                                                    const float* __restrict__ lw, const Grid& g) {
   const int P = g.P;
   int c = i * P + j;
   float k = 0.5f / g.h;
@@ -572,16 +654,22 @@ __global__ void k_adj_conf_apply(float* __restrict__ dU, float* __restrict__ dV,
   dU[c] = dU[c] + k * (wN - wS);
   dV[c] = dV[c] + k * (wW - wE);
 }
+__global__ void k_adj_conf_apply(float* __restrict__ dU, float* __restrict__ dV,
+                                 const float* __restrict__ lw, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  adj_conf_apply_cell(i, j, dU, dV, lw, g);
+}
 
 // G^T: the adjoint of the gradient subtract with respect to phi, as the
 // Jacobi right-hand side of the adjoint solve: rhs = G^T (dU, dV) on active
 // cells, and bw = w * rhs.
-__global__ void k_adj_grad_t(const float* __restrict__ dU, const float* __restrict__ dV,
-                             const float* __restrict__ W, float* __restrict__ rhs,
-                             float* __restrict__ BW, const uint8_t* __restrict__ flags, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void adj_grad_t_cell(int i, int j, const float* __restrict__ dU,
+                                                const float* __restrict__ dV,
+                                                const float* __restrict__ W,
+                                                float* __restrict__ rhs, float* __restrict__ BW,
+                                                const uint8_t* __restrict__ flags, const Grid& g) {
   const int P = g.P;
   int c = i * P + j;
   uint8_t fl = flags[c];
@@ -593,16 +681,22 @@ __global__ void k_adj_grad_t(const float* __restrict__ dU, const float* __restri
   rhs[c] = r;
   BW[c] = W[c] * r;
 }
-
-// div^T: with b = -div on active cells, d(face) += db(cell on its high side)
-// - db(cell on its low side), db = the adjoint solve's result (0 off active).
-__global__ void k_adj_div_t(float* __restrict__ dU, float* __restrict__ dV,
-                            const float* __restrict__ x0, const float* __restrict__ x1,
-                            const void* __restrict__ ctl_sel, const uint8_t* __restrict__ flags,
-                            Grid g) {
+__global__ void k_adj_grad_t(const float* __restrict__ dU, const float* __restrict__ dV,
+                             const float* __restrict__ W, float* __restrict__ rhs,
+                             float* __restrict__ BW, const uint8_t* __restrict__ flags, Grid g) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
+  adj_grad_t_cell(i, j, dU, dV, W, rhs, BW, flags, g);
+}
+
+// div^T: with b = -div on active cells, d(face) += db(cell on its high side)
+// - db(cell on its low side), db = the adjoint solve's result (0 off active).
+__device__ __forceinline__ void adj_div_t_cell(int i, int j, float* __restrict__ dU,
+                                               float* __restrict__ dV, const float* __restrict__ x0,
+                                               const float* __restrict__ x1,
+                                               const void* __restrict__ ctl_sel,
+                                               const uint8_t* __restrict__ flags, const Grid& g) {
   const int P = g.P;
   const float* db = (*(const int*)ctl_sel) ? x1 : x0;
   int c = i * P + j;
@@ -617,16 +711,22 @@ __global__ void k_adj_div_t(float* __restrict__ dU, float* __restrict__ dV,
     dV[c] = dV[c] + (bc - bb);
   }
 }
+__global__ void k_adj_div_t(float* __restrict__ dU, float* __restrict__ dV,
+                            const float* __restrict__ x0, const float* __restrict__ x1,
+                            const void* __restrict__ ctl_sel, const uint8_t* __restrict__ flags,
+                            Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  adj_div_t_cell(i, j, dU, dV, x0, x1, ctl_sel, flags, g);
+}
 
 // Sources that set U, V (SetVelocity) or M (a smoke assignment) cut the
 // derivative there.
-__global__ void k_adj_sources(float* __restrict__ dU, float* __restrict__ dV,
-                              float* __restrict__ dM, const SourceRec* __restrict__ recs,
-                              const uint32_t* __restrict__ off, int n_groups,
-                              const uint8_t* __restrict__ flags, Grid g) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n_groups) return;
-  uint32_t b = off[k], e = off[k + 1];
+__device__ __forceinline__ void adj_sources_group(float* dU, float* dV, float* dM,
+                                                  const SourceRec* __restrict__ recs, uint32_t b,
+                                                  uint32_t e, const uint8_t* __restrict__ flags,
+                                                  const Grid& g) {
   uint32_t cell = recs[b].cell;
   int i = (int)(cell / (uint32_t)g.NY), j = (int)(cell % (uint32_t)g.NY);
   int c = i * g.P + j;
@@ -643,6 +743,73 @@ __global__ void k_adj_sources(float* __restrict__ dU, float* __restrict__ dV,
     dV[c] = 0.0f;
   }
   if (set_m) dM[c] = 0.0f;
+}
+__global__ void k_adj_sources(float* __restrict__ dU, float* __restrict__ dV,
+                              float* __restrict__ dM, const SourceRec* __restrict__ recs,
+                              const uint32_t* __restrict__ off, int n_groups,
+                              const uint8_t* __restrict__ flags, Grid g) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_groups) return;
+  adj_sources_group(dU, dV, dM, recs, off[k], off[k + 1], flags, g);
+}
+__global__ void kb_adj_sources(float* __restrict__ dU, float* __restrict__ dV,
+                               float* __restrict__ dM, const SourceRec* __restrict__ recs,
+                               const uint32_t* __restrict__ off, const int* __restrict__ gs,
+                               int n_groups, const uint8_t* __restrict__ flags,
+                               const BScene* __restrict__ sc) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_groups) return;
+  const BScene& s = sc[gs[k]];
+  adj_sources_group(dU + s.off, dV + s.off, dM + s.off, recs, off[k], off[k + 1], flags + s.off,
+                    s.g);
+}
+
+// A batch's loss: L_s = ||M_s - target_s||_2 per scene.  Block rows of the
+// sums of squares per cell tile, one block per scene to combine its tiles'
+// rows, then the seed dL/dM_s = (M_s - target_s) / L_s.
+__global__ void kb_loss_partials(const BTile* __restrict__ tiles, const BScene* __restrict__ sc,
+                                 const float* __restrict__ M, const float* __restrict__ T,
+                                 float* __restrict__ part) {
+  __shared__ float sh[64];
+  const BTile t = tiles[blockIdx.x];
+  const BScene& s = sc[t.s];
+  int j = t.x * blockDim.x + threadIdx.x;
+  int i = t.y * blockDim.y + threadIdx.y;
+  FF v[1] = {{0.0f, 0.0f}};
+  if (i >= 1 && i <= s.g.NX - 2 && j >= 1 && j <= s.g.NY - 2) {
+    long long c = s.off + (long long)i * s.g.P + j;
+    v[0] = ff_sq(M[c] - T[c]);
+  }
+  block_row<1>(v, 0u, sh, part + 2 * (size_t)blockIdx.x);
+}
+__global__ void kb_loss_combine(const float* __restrict__ part, const int* __restrict__ range,
+                                double* __restrict__ losses) {
+  __shared__ float sh[64];
+  __shared__ float row[2];
+  const int s = blockIdx.x;
+  FF v[1] = {{0.0f, 0.0f}};
+  for (int k = range[2 * s] + threadIdx.x; k < range[2 * s + 1]; k += blockDim.x) {
+    FF w[1] = {{part[2 * (size_t)k], part[2 * (size_t)k + 1]}};
+    slots_merge<1>(v, w, 0u);
+  }
+  block_row<1>(v, 0u, sh, row);
+  __syncthreads();
+  if (threadIdx.x == 0) losses[s] = sqrt((double)row[0] + (double)row[1]);
+}
+__global__ void kb_loss_seed(const BTile* __restrict__ tiles, const BScene* __restrict__ sc,
+                             const float* __restrict__ M, const float* __restrict__ T,
+                             const double* __restrict__ losses, float* __restrict__ lamM) {
+  const BTile t = tiles[blockIdx.x];
+  const BScene& s = sc[t.s];
+  int j = t.x * blockDim.x + threadIdx.x;
+  int i = t.y * blockDim.y + threadIdx.y;
+  if (i >= s.g.NX || j >= s.g.NY) return;
+  long long c = s.off + (long long)i * s.g.P + j;
+  double L = losses[t.s];
+  float v = 0.0f;
+  if (i >= 1 && i <= s.g.NX - 2 && j >= 1 && j <= s.g.NY - 2 && L > 0.0)
+    v = (float)((double)(M[c] - T[c]) / L);
+  lamM[c] = v;
 }
 
 // Loss L = ||M - target||_2 over interior cells: float-pair block rows of
@@ -707,6 +874,23 @@ __global__ void k_adj_begin(float* __restrict__ aU, float* __restrict__ aV, floa
 }  // namespace
 
 cudaError_t launch_loss_seed(fg_fluid* f, const float* target, double* dev_loss) {
+  if (f->batch) {
+    const BatchGeom* b = f->batch;
+    if (!partials_fit(f, 1, b->n_cell_tiles)) return cudaErrorInvalidValue;
+    count(f, 3);
+    kb_loss_partials<<<b->n_cell_tiles, dim3(b->bx, b->by), 0, f->stream>>>(
+        b->cell_tiles, b->scenes_dev, f->d[FG_M], target, f->partials);
+    kb_loss_combine<<<b->n, 256, 0, f->stream>>>(f->partials, b->cell_range, b->losses);
+    kb_loss_seed<<<b->n_cell_tiles, dim3(b->bx, b->by), 0, f->stream>>>(
+        b->cell_tiles, b->scenes_dev, f->d[FG_M], target, b->losses, f->adj[fg_fluid::A_M]);
+    size_t bytes = sizeof(float) * (size_t)f->NX * f->P;
+    for (int k : {fg_fluid::A_U, fg_fluid::A_V, fg_fluid::A_NU, fg_fluid::A_NV, fg_fluid::A_NM}) {
+      cudaError_t e = cudaMemsetAsync(f->adj[k], 0, bytes, f->stream);
+      if (e != cudaSuccess) return e;
+    }
+    (void)dev_loss;
+    return cudaGetLastError();
+  }
   dim3 gr = cell_grid(f), bl(BX, BY);
   int nb = gr.x * gr.y;
   if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
@@ -752,76 +936,76 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
   if (p.use_bfecc) {
     // pass 4: final SL of corrM
     count(f);
-    k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_M], U5, V5, corrM, A[F::A_U], A[F::A_V], A[F::A_CM],
-                                      A[F::A_NM], f->flags, dt, sa, 0, g);
+    FG_CELLS(f, k_adj_sl_smoke, adj_sl_smoke_cell, A[F::A_M], U5, V5, corrM, A[F::A_U], A[F::A_V], A[F::A_CM],
+                                      A[F::A_NM], f->flags, dt, sa, 0);
     // compensation + clamp and the reverse sample of fwdM traced with U5,
     // V5 at +dt: dM1 (orig), dfwdM, dU5
     if ((e = cudaMemsetAsync(A[F::A_M], 0, bytes, st)) != cudaSuccess) return e;
     count(f);
-    k_adj_bfecc_smoke<<<gr, bl, 0, st>>>(A[F::A_CM], U5, V5, M1, fwdM, A[F::A_M], A[F::A_FM],
-                                         A[F::A_U], A[F::A_V], f->flags, dt, sa, g);
+    FG_CELLS(f, k_adj_bfecc_smoke, adj_bfecc_smoke_cell, A[F::A_CM], U5, V5, M1, fwdM, A[F::A_M], A[F::A_FM],
+                                         A[F::A_U], A[F::A_V], f->flags, dt, sa);
     // pass 1: forward SL of M1
     count(f);
-    k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_FM], U5, V5, M1, A[F::A_U], A[F::A_V], A[F::A_M],
-                                      A[F::A_NM], f->flags, dt, sa, 0, g);
+    FG_CELLS(f, k_adj_sl_smoke, adj_sl_smoke_cell, A[F::A_FM], U5, V5, M1, A[F::A_U], A[F::A_V], A[F::A_M],
+                                      A[F::A_NM], f->flags, dt, sa, 0);
   } else {
     // single SL pass of M1: dM2 moves to the zeroed work field, dM1
     // accumulates in the other
     std::swap(A[F::A_M], A[F::A_CM]);
     count(f);
-    k_adj_sl_smoke<<<gr, bl, 0, st>>>(A[F::A_CM], U5, V5, M1, A[F::A_U], A[F::A_V], A[F::A_M],
-                                      A[F::A_NM], f->flags, dt, sa, 0, g);
+    FG_CELLS(f, k_adj_sl_smoke, adj_sl_smoke_cell, A[F::A_CM], U5, V5, M1, A[F::A_U], A[F::A_V], A[F::A_M],
+                                      A[F::A_NM], f->flags, dt, sa, 0);
   }
   // ---- velocity advection: A_U/A_V hold dU5/dV5; produce dU4 in A_CU..
   if (p.use_bfecc) {
     // pass 4: final SL of corr traced with corr: d -> dcorr (A_CU/A_CV)
     count(f);
-    k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], corrU, corrV, corrU, corrV,
+    FG_CELLS(f, k_adj_sl_velocity, adj_sl_velocity_cell, A[F::A_U], A[F::A_V], corrU, corrV, corrU, corrV,
                                          A[F::A_CU], A[F::A_CV], A[F::A_CU], A[F::A_CV],
                                          A[F::A_CU], A[F::A_CV], A[F::A_NU], A[F::A_NV], f->flags,
-                                         dt, g);
+                                         dt);
     // dU4 accumulates into A_U/A_V (reset first); compensation + clamp and
     // the reverse sample of fwd traced with U4 at +dt: dfwd (A_FU/A_FV), dU4
     if ((e = cudaMemsetAsync(A[F::A_U], 0, bytes, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(A[F::A_V], 0, bytes, st)) != cudaSuccess) return e;
     count(f);
-    k_adj_bfecc_vel<<<gr, bl, 0, st>>>(A[F::A_CU], A[F::A_CV], U4, V4, fwdU, fwdV, A[F::A_U],
-                                       A[F::A_V], A[F::A_FU], A[F::A_FV], f->flags, dt, g);
+    FG_CELLS(f, k_adj_bfecc_vel, adj_bfecc_vel_cell, A[F::A_CU], A[F::A_CV], U4, V4, fwdU, fwdV, A[F::A_U],
+                                       A[F::A_V], A[F::A_FU], A[F::A_FV], f->flags, dt);
     // pass 1: forward SL of U4 traced with U4
     count(f);
-    k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_FU], A[F::A_FV], U4, V4, U4, V4, A[F::A_U],
+    FG_CELLS(f, k_adj_sl_velocity, adj_sl_velocity_cell, A[F::A_FU], A[F::A_FV], U4, V4, U4, V4, A[F::A_U],
                                          A[F::A_V], A[F::A_U], A[F::A_V], A[F::A_U], A[F::A_V],
-                                         A[F::A_NU], A[F::A_NV], f->flags, dt, g);
+                                         A[F::A_NU], A[F::A_NV], f->flags, dt);
   } else {
     std::swap(A[F::A_U], A[F::A_CU]);
     std::swap(A[F::A_V], A[F::A_CV]);
     count(f);
-    k_adj_sl_velocity<<<gr, bl, 0, st>>>(A[F::A_CU], A[F::A_CV], U4, V4, U4, V4, A[F::A_U],
+    FG_CELLS(f, k_adj_sl_velocity, adj_sl_velocity_cell, A[F::A_CU], A[F::A_CV], U4, V4, U4, V4, A[F::A_U],
                                          A[F::A_V], A[F::A_U], A[F::A_V], A[F::A_U], A[F::A_V],
-                                         A[F::A_NU], A[F::A_NV], f->flags, dt, g);
+                                         A[F::A_NU], A[F::A_NV], f->flags, dt);
   }
   // ---- borders, confinement + turbulence (A_U/A_V: dU4 -> dU3 -> dU2)
-  int nbd = f->NX > f->NY ? f->NX : f->NY;
   count(f);
-  k_adj_borders<<<(nbd + 127) / 128, 128, 0, st>>>(A[F::A_U], A[F::A_V], f->flags, g);
+  FG_BORDER(f, k_adj_borders, adj_borders_border, A[F::A_U], A[F::A_V],
+            (const uint8_t*)f->flags);
   if (p.confinement != 0.0f) {
     // Work fields A_CU, A_CV, A_FU, A_FV are free again here.
     count(f, 3);
-    k_adj_conf_local<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], U2, V2, f->noise, f->flags,
+    FG_CELLS(f, k_adj_conf_local, adj_conf_local_cell, A[F::A_U], A[F::A_V], U2, V2, f->noise, f->flags,
                                         p.confinement, dt, p.turbulence_strength * dt,
                                         p.turbulence_strength > 0.0f ? 1 : 0, A[F::A_CU],
-                                        A[F::A_CV], A[F::A_FU], g);
-    k_adj_conf_curl<<<gr, bl, 0, st>>>(U2, V2, A[F::A_CU], A[F::A_CV], A[F::A_FU], A[F::A_FV],
-                                       f->flags, g);
-    k_adj_conf_apply<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], A[F::A_FV], g);
+                                        A[F::A_CV], A[F::A_FU]);
+    FG_CELLS(f, k_adj_conf_curl, adj_conf_curl_cell, U2, V2, A[F::A_CU], A[F::A_CV], A[F::A_FU], A[F::A_FV],
+                                       f->flags);
+    FG_CELLS(f, k_adj_conf_apply, adj_conf_apply_cell, A[F::A_U], A[F::A_V], A[F::A_FV]);
   } else if (p.turbulence_strength > 0.0f) {
     count(f);
-    k_adj_turbulence<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], U2, V2, f->noise, f->flags,
-                                        p.turbulence_strength * dt, g);
+    FG_CELLS(f, k_adj_turbulence, adj_turbulence_cell, A[F::A_U], A[F::A_V], U2, V2, f->noise, f->flags,
+                                        p.turbulence_strength * dt);
   }
   // ---- projection: dU1 = dU2 + div^T P_K G^T dU2
   count(f);
-  k_adj_grad_t<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], f->wgt, f->rhs, f->bw, f->flags, g);
+  FG_CELLS(f, k_adj_grad_t, adj_grad_t_cell, A[F::A_U], A[F::A_V], f->wgt, f->rhs, f->bw, f->flags);
   if (p.num_iters > 0) {
     if ((e = launch_jacobi_solve(f, f->ectl, f->rhs, f->bw, f->phi, f->phi2, p.num_iters)) !=
         cudaSuccess)
@@ -831,21 +1015,26 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
     if ((e = cudaMemsetAsync(f->ectl, 0, sizeof(int) * 8, st)) != cudaSuccess) return e;
   }
   count(f);
-  k_adj_div_t<<<gr, bl, 0, st>>>(A[F::A_U], A[F::A_V], f->phi, f->phi2,
-                                 (const int*)f->ectl + 1, f->flags, g);
+  FG_CELLS(f, k_adj_div_t, adj_div_t_cell, A[F::A_U], A[F::A_V], f->phi, f->phi2,
+                                 (const int*)f->ectl + 1, f->flags);
   // ---- sources (the forces' adjoint is then the state's)
   if (f->n_src_groups > 0) {
     count(f);
-    k_adj_sources<<<(f->n_src_groups + 255) / 256, 256, 0, st>>>(
-        A[F::A_U], A[F::A_V], A[F::A_M], f->src_dev, f->src_off_dev, f->n_src_groups, f->flags,
-        g);
+    if (f->batch)
+      kb_adj_sources<<<(f->n_src_groups + 255) / 256, 256, 0, st>>>(
+          A[F::A_U], A[F::A_V], A[F::A_M], f->src_dev, f->src_off_dev, f->batch->src_scene,
+          f->n_src_groups, f->flags, f->batch->scenes_dev);
+    else
+      k_adj_sources<<<(f->n_src_groups + 255) / 256, 256, 0, st>>>(
+          A[F::A_U], A[F::A_V], A[F::A_M], f->src_dev, f->src_off_dev, f->n_src_groups, f->flags,
+          g);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_add_forces(fg_fluid* f, const float* fu, const float* fv) {
   count(f);
-  k_add_forces<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], fu, fv, f->g);
+  FG_CELLS(f, k_add_forces, add_forces_cell, f->d[FG_U], f->d[FG_V], fu, fv);
   return cudaGetLastError();
 }
 

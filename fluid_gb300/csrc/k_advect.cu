@@ -9,6 +9,7 @@
 // lies on the ghost ring (copyBorder, fluid.go:293-294), else the stale
 // staging value.  The result is written to the rotation partner of the state
 // field and to the staging buffer, after which state and partner swap.
+#include "fg_batch.cuh"
 #include "fg_internal.cuh"
 #include "fg_reduce.cuh"
 
@@ -68,12 +69,12 @@ __device__ __forceinline__ float trace_sample_v(const float* __restrict__ Ut,
 // advectVelocity (fluid.go:291-333) with trace field = sampled field =
 // border field = (Ui, Vi); stale values from the staging buffers nU, nV;
 // result to (Uo, Vo) and back into (nU, nV).
-__global__ void k_sl_velocity(const float* __restrict__ Ui, const float* __restrict__ Vi,
-                              float* __restrict__ Uo, float* __restrict__ Vo, float* nU,
-                              float* nV, const uint8_t* __restrict__ flags, float dt, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void sl_velocity_cell(int i, int j, const float* __restrict__ Ui,
+                                                 const float* __restrict__ Vi,
+                                                 float* __restrict__ Uo, float* __restrict__ Vo,
+                                                 float* nU, float* nV,
+                                                 const uint8_t* __restrict__ flags, float dt,
+                                                 const Grid& g) {
   int c = i * g.P + j;
   uint8_t fl = flags[c];
   bool ring = on_ring(i, j, g);
@@ -91,10 +92,31 @@ __global__ void k_sl_velocity(const float* __restrict__ Ui, const float* __restr
   nU[c] = u;
   nV[c] = v;
 }
+__global__ void k_sl_velocity(const float* __restrict__ Ui, const float* __restrict__ Vi,
+                              float* __restrict__ Uo, float* __restrict__ Vo, float* nU,
+                              float* nV, const uint8_t* __restrict__ flags, float dt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  sl_velocity_cell(i, j, Ui, Vi, Uo, Vo, nU, nV, flags, dt, g);
+}
 
 // BFECC pass 1 (fluid.go:923): forward advection of the original field into
 // (Fu, Fv).  The staging buffers are not written: the final pass reads the
 // same stale values from them (newU = fwdU on the faces that are stale).
+__device__ __forceinline__ void bfecc_vel_fwd_cell(int i, int j, const float* __restrict__ Ui,
+                                                   const float* __restrict__ Vi,
+                                                   const float* __restrict__ nU,
+                                                   const float* __restrict__ nV,
+                                                   float* __restrict__ Fu, float* __restrict__ Fv,
+                                                   const uint8_t* __restrict__ flags, float dt,
+                                                   const Grid& g) {
+  int c = i * g.P + j;
+  uint8_t fl = flags[c];
+  bool ring = on_ring(i, j, g);
+  Fu[c] = u_advected(fl, i, j, g) ? trace_sample_u(Ui, Vi, Ui, i, j, dt, g) : (ring ? Ui[c] : nU[c]);
+  Fv[c] = v_advected(fl, i, j, g) ? trace_sample_v(Ui, Vi, Vi, i, j, dt, g) : (ring ? Vi[c] : nV[c]);
+}
 __global__ void k_bfecc_vel_fwd(const float* __restrict__ Ui, const float* __restrict__ Vi,
                                 const float* __restrict__ nU, const float* __restrict__ nV,
                                 float* __restrict__ Fu, float* __restrict__ Fv,
@@ -102,11 +124,7 @@ __global__ void k_bfecc_vel_fwd(const float* __restrict__ Ui, const float* __res
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
-  int c = i * g.P + j;
-  uint8_t fl = flags[c];
-  bool ring = on_ring(i, j, g);
-  Fu[c] = u_advected(fl, i, j, g) ? trace_sample_u(Ui, Vi, Ui, i, j, dt, g) : (ring ? Ui[c] : nU[c]);
-  Fv[c] = v_advected(fl, i, j, g) ? trace_sample_v(Ui, Vi, Vi, i, j, dt, g) : (ring ? Vi[c] : nV[c]);
+  bfecc_vel_fwd_cell(i, j, Ui, Vi, nU, nV, Fu, Fv, flags, dt, g);
 }
 
 // clampToNeighbors (fluid.go:1094-1120) for an interior cell (all 3x3
@@ -131,13 +149,14 @@ __device__ __forceinline__ float clamp3x3(float val, const float* __restrict__ s
 // result traced with the original velocity, error compensation on every
 // interior face (non-advected faces see bwd = 0), clamp to the original
 // field's 3x3 range.  Ring faces keep the original value.
-__global__ void k_bfecc_vel_correct(const float* __restrict__ Ui, const float* __restrict__ Vi,
-                                    const float* __restrict__ Fu, const float* __restrict__ Fv,
-                                    float* __restrict__ Cu, float* __restrict__ Cv,
-                                    const uint8_t* __restrict__ flags, float dt, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void bfecc_vel_correct_cell(int i, int j, const float* __restrict__ Ui,
+                                                       const float* __restrict__ Vi,
+                                                       const float* __restrict__ Fu,
+                                                       const float* __restrict__ Fv,
+                                                       float* __restrict__ Cu,
+                                                       float* __restrict__ Cv,
+                                                       const uint8_t* __restrict__ flags, float dt,
+                                                       const Grid& g) {
   int c = i * g.P + j;
   if (on_ring(i, j, g)) {
     Cu[c] = Ui[c];
@@ -152,6 +171,15 @@ __global__ void k_bfecc_vel_correct(const float* __restrict__ Ui, const float* _
   float cv = ov - (bv - ov) * 0.5f;
   Cu[c] = clamp3x3(cu, Ui, c, g.P);
   Cv[c] = clamp3x3(cv, Vi, c, g.P);
+}
+__global__ void k_bfecc_vel_correct(const float* __restrict__ Ui, const float* __restrict__ Vi,
+                                    const float* __restrict__ Fu, const float* __restrict__ Fv,
+                                    float* __restrict__ Cu, float* __restrict__ Cv,
+                                    const uint8_t* __restrict__ flags, float dt, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  bfecc_vel_correct_cell(i, j, Ui, Vi, Fu, Fv, Cu, Cv, flags, dt, g);
 }
 
 // advectSmoke (fluid.go:400-434).  Trace velocity (Ut, Vt); sampled field Ms
@@ -169,6 +197,41 @@ __device__ __forceinline__ float smoke_value(const float* __restrict__ Ut,
   return sample_field(Ms, x, y, g.hh, g.hh, g);
 }
 
+// One cell of advectSmoke: writes Mo and nM, returns the new value.
+__device__ __forceinline__ float sl_smoke_value(int i, int j, const float* __restrict__ Ut,
+                                                const float* __restrict__ Vt,
+                                                const float* __restrict__ Ms,
+                                                float* __restrict__ Mo, float* nM,
+                                                const uint8_t* __restrict__ flags, float dt,
+                                                float smokeAdv, int diffuse,
+                                                float smokeDiffusion, const Grid& g) {
+  int c = i * g.P + j;
+  uint8_t fl = flags[c];
+  float m;
+  if ((fl & (F_INTERIOR | F_FLUID)) == (F_INTERIOR | F_FLUID)) {
+    float s = smoke_value(Ut, Vt, Ms, i, j, dt, smokeAdv, g);
+    if (diffuse) {
+      float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
+      s += smokeDiffusion * neighbors;
+    }
+    m = go_max(s, 0.0f);
+  } else {
+    m = on_ring(i, j, g) ? Ms[c] : nM[c];
+  }
+  Mo[c] = m;
+  nM[c] = m;
+  return m;
+}
+__device__ __forceinline__ void sl_smoke_cell(int i, int j, const float* __restrict__ Ut,
+                                              const float* __restrict__ Vt,
+                                              const float* __restrict__ Ms,
+                                              float* __restrict__ Mo, float* nM,
+                                              const uint8_t* __restrict__ flags, float dt,
+                                              float smokeAdv, int diffuse, float smokeDiffusion,
+                                              const Grid& g) {
+  sl_smoke_value(i, j, Ut, Vt, Ms, Mo, nM, flags, dt, smokeAdv, diffuse, smokeDiffusion, g);
+}
+
 __global__ void k_sl_smoke(const float* __restrict__ Ut, const float* __restrict__ Vt,
                            const float* __restrict__ Ms, float* __restrict__ Mo, float* nM,
                            const uint8_t* __restrict__ flags, float dt, float smokeAdv,
@@ -179,21 +242,8 @@ __global__ void k_sl_smoke(const float* __restrict__ Ut, const float* __restrict
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   FF mass{0.0f, 0.0f};
   if (i < g.NX && j < g.NY) {
-    int c = i * g.P + j;
-    uint8_t fl = flags[c];
-    float m;
-    if ((fl & (F_INTERIOR | F_FLUID)) == (F_INTERIOR | F_FLUID)) {
-      float s = smoke_value(Ut, Vt, Ms, i, j, dt, smokeAdv, g);
-      if (diffuse) {
-        float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
-        s += smokeDiffusion * neighbors;
-      }
-      m = go_max(s, 0.0f);
-    } else {
-      m = on_ring(i, j, g) ? Ms[c] : nM[c];
-    }
-    Mo[c] = m;
-    nM[c] = m;
+    float m = sl_smoke_value(i, j, Ut, Vt, Ms, Mo, nM, flags, dt, smokeAdv, diffuse,
+                             smokeDiffusion, g);
     if (!on_ring(i, j, g)) mass.hi = m;
   }
   // Smoke mass of the result over interior cells (float pairs within the
@@ -206,14 +256,14 @@ __global__ void k_sl_smoke(const float* __restrict__ Ut, const float* __restrict
 
 // BFECC smoke pass 1 (fluid.go:1007): forward advection into Fm without
 // touching the staging buffer.
-__global__ void k_bfecc_smoke_fwd(const float* __restrict__ Ut, const float* __restrict__ Vt,
-                                  const float* __restrict__ Ms, const float* __restrict__ nM,
-                                  float* __restrict__ Fm, const uint8_t* __restrict__ flags,
-                                  float dt, float smokeAdv, int diffuse, float smokeDiffusion,
-                                  Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void bfecc_smoke_fwd_cell(int i, int j, const float* __restrict__ Ut,
+                                                     const float* __restrict__ Vt,
+                                                     const float* __restrict__ Ms,
+                                                     const float* __restrict__ nM,
+                                                     float* __restrict__ Fm,
+                                                     const uint8_t* __restrict__ flags, float dt,
+                                                     float smokeAdv, int diffuse,
+                                                     float smokeDiffusion, const Grid& g) {
   int c = i * g.P + j;
   uint8_t fl = flags[c];
   float m;
@@ -229,17 +279,27 @@ __global__ void k_bfecc_smoke_fwd(const float* __restrict__ Ut, const float* __r
   }
   Fm[c] = m;
 }
+__global__ void k_bfecc_smoke_fwd(const float* __restrict__ Ut, const float* __restrict__ Vt,
+                                  const float* __restrict__ Ms, const float* __restrict__ nM,
+                                  float* __restrict__ Fm, const uint8_t* __restrict__ flags,
+                                  float dt, float smokeAdv, int diffuse, float smokeDiffusion,
+                                  Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  bfecc_smoke_fwd_cell(i, j, Ut, Vt, Ms, nM, Fm, flags, dt, smokeAdv, diffuse, smokeDiffusion, g);
+}
 
 // BFECC smoke passes 2-3 (fluid.go:1013-1046): reverse advection of the
 // forward result, compensation on every interior cell (non-fluid cells see
 // bwd = 0), clamp to the original 3x3 range, then to >= 0.
-__global__ void k_bfecc_smoke_correct(const float* __restrict__ Ut, const float* __restrict__ Vt,
-                                      const float* __restrict__ Mi, const float* __restrict__ Fm,
-                                      float* __restrict__ Cm, const uint8_t* __restrict__ flags,
-                                      float dt, float smokeAdv, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void bfecc_smoke_correct_cell(int i, int j, const float* __restrict__ Ut,
+                                                         const float* __restrict__ Vt,
+                                                         const float* __restrict__ Mi,
+                                                         const float* __restrict__ Fm,
+                                                         float* __restrict__ Cm,
+                                                         const uint8_t* __restrict__ flags,
+                                                         float dt, float smokeAdv, const Grid& g) {
   int c = i * g.P + j;
   if (on_ring(i, j, g)) {
     Cm[c] = Mi[c];
@@ -253,14 +313,23 @@ __global__ void k_bfecc_smoke_correct(const float* __restrict__ Ut, const float*
   if (cm < 0.0f) cm = 0.0f;
   Cm[c] = cm;
 }
+__global__ void k_bfecc_smoke_correct(const float* __restrict__ Ut, const float* __restrict__ Vt,
+                                      const float* __restrict__ Mi, const float* __restrict__ Fm,
+                                      float* __restrict__ Cm, const uint8_t* __restrict__ flags,
+                                      float dt, float smokeAdv, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  bfecc_smoke_correct_cell(i, j, Ut, Vt, Mi, Fm, Cm, flags, dt, smokeAdv, g);
+}
 
 }  // namespace
 
 cudaError_t launch_advect_velocity(fg_fluid* f, float dt) {
   count(f);
-  k_sl_velocity<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(
-      f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV],
-      f->flags, dt, f->g);
+  FG_CELLS(f, k_sl_velocity, sl_velocity_cell, (const float*)f->d[FG_U],
+           (const float*)f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU],
+           f->d[FG_NEWV], (const uint8_t*)f->flags, dt);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   return cudaGetLastError();
@@ -271,56 +340,62 @@ static float smoke_diffusion(const fg_fluid* f, float dt, int* diffuse) {
   return f->prm.viscosity_diffusion * 0.3f * dt;  // fluid.go:422
 }
 
-cudaError_t launch_advect_smoke(fg_fluid* f, float dt) {
+// Final smoke pass from Ms; a single handle also sums the smoke mass.
+static cudaError_t smoke_pass(fg_fluid* f, const float* Ms, float dt) {
   int diffuse;
   float sd = smoke_diffusion(f, dt, &diffuse);
+  float sa = f->prm.smoke_advection;
   count(f);
+  if (f->batch) {
+    FG_CELLS_BATCH(f, sl_smoke_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V], Ms,
+                   f->partner[FG_M], f->d[FG_NEWM], (const uint8_t*)f->flags, dt, sa, diffuse,
+                   sd);
+    swap_state(f, FG_M);
+    return cudaGetLastError();
+  }
   dim3 gr = cell_grid(f);
   if (!partials_fit(f, 1, gr.x * gr.y)) return cudaErrorInvalidValue;
-  k_sl_smoke<<<gr, dim3(BX, BY), 0, f->stream>>>(
-      f->d[FG_U], f->d[FG_V], f->d[FG_M], f->partner[FG_M], f->d[FG_NEWM], f->flags, dt,
-      f->prm.smoke_advection, diffuse, sd, f->partials, f->g);
+  k_sl_smoke<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], Ms, f->partner[FG_M],
+                                                 f->d[FG_NEWM], f->flags, dt, sa, diffuse, sd,
+                                                 f->partials, f->g);
   swap_state(f, FG_M);
   return launch_store_mass(f, gr.x * gr.y);
 }
 
+cudaError_t launch_advect_smoke(fg_fluid* f, float dt) { return smoke_pass(f, f->d[FG_M], dt); }
+
 cudaError_t launch_advect_velocity_bfecc(fg_fluid* f, float dt) {
-  dim3 gr = cell_grid(f), bl(BX, BY);
   count(f);
-  k_bfecc_vel_fwd<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_NEWU],
-                                            f->d[FG_NEWV], f->fwdU, f->fwdV, f->flags, dt, f->g);
+  FG_CELLS(f, k_bfecc_vel_fwd, bfecc_vel_fwd_cell, (const float*)f->d[FG_U],
+           (const float*)f->d[FG_V], (const float*)f->d[FG_NEWU], (const float*)f->d[FG_NEWV],
+           f->fwdU, f->fwdV, (const uint8_t*)f->flags, dt);
   count(f);
-  k_bfecc_vel_correct<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->fwdU, f->fwdV,
-                                                f->corrU, f->corrV, f->flags, dt, f->g);
+  FG_CELLS(f, k_bfecc_vel_correct, bfecc_vel_correct_cell, (const float*)f->d[FG_U],
+           (const float*)f->d[FG_V], (const float*)f->fwdU, (const float*)f->fwdV, f->corrU,
+           f->corrV, (const uint8_t*)f->flags, dt);
   // Pass 4 (fluid.go:991-993): advect the corrected field with itself.
   count(f);
-  k_sl_velocity<<<gr, bl, 0, f->stream>>>(f->corrU, f->corrV, f->partner[FG_U],
-                                          f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV],
-                                          f->flags, dt, f->g);
+  FG_CELLS(f, k_sl_velocity, sl_velocity_cell, (const float*)f->corrU, (const float*)f->corrV,
+           f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV],
+           (const uint8_t*)f->flags, dt);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   return cudaGetLastError();
 }
 
 cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt) {
-  dim3 gr = cell_grid(f), bl(BX, BY);
-  if (!partials_fit(f, 1, gr.x * gr.y)) return cudaErrorInvalidValue;
   int diffuse;
   float sd = smoke_diffusion(f, dt, &diffuse);
   float sa = f->prm.smoke_advection;
   count(f);
-  k_bfecc_smoke_fwd<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_M],
-                                              f->d[FG_NEWM], f->fwdM, f->flags, dt, sa, diffuse,
-                                              sd, f->g);
+  FG_CELLS(f, k_bfecc_smoke_fwd, bfecc_smoke_fwd_cell, (const float*)f->d[FG_U],
+           (const float*)f->d[FG_V], (const float*)f->d[FG_M], (const float*)f->d[FG_NEWM],
+           f->fwdM, (const uint8_t*)f->flags, dt, sa, diffuse, sd);
   count(f);
-  k_bfecc_smoke_correct<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_M], f->fwdM,
-                                                  f->corrM, f->flags, dt, sa, f->g);
-  count(f);
-  k_sl_smoke<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->corrM, f->partner[FG_M],
-                                       f->d[FG_NEWM], f->flags, dt, sa, diffuse, sd, f->partials,
-                                       f->g);
-  swap_state(f, FG_M);
-  return launch_store_mass(f, gr.x * gr.y);
+  FG_CELLS(f, k_bfecc_smoke_correct, bfecc_smoke_correct_cell, (const float*)f->d[FG_U],
+           (const float*)f->d[FG_V], (const float*)f->d[FG_M], (const float*)f->fwdM, f->corrM,
+           (const uint8_t*)f->flags, dt, sa);
+  return smoke_pass(f, f->corrM, dt);
 }
 
 }  // namespace fg

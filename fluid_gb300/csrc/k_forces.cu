@@ -6,6 +6,7 @@
 // match the reference arithmetic bit for bit.
 #include <cmath>
 
+#include "fg_batch.cuh"
 #include "fg_internal.cuh"
 
 namespace fg {
@@ -63,12 +64,10 @@ __global__ void k_apply_edits(const EditRec* __restrict__ recs, const uint32_t* 
 // (main/main.go:236-241 jet, 474-486 sources) or a smoke assignment
 // (fluid_test.go:396-401), optionally skipped on solid cells (the IsSolid
 // check of applySources).
-__global__ void k_apply_sources(const SourceRec* __restrict__ recs,
-                                const uint32_t* __restrict__ off, int n_groups, float* U,
-                                float* V, float* M, const uint8_t* __restrict__ flags, Grid g) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n_groups) return;
-  uint32_t b = off[k], e = off[k + 1];
+__device__ __forceinline__ void apply_sources_group(const SourceRec* __restrict__ recs,
+                                                    uint32_t b, uint32_t e, float* U, float* V,
+                                                    float* M, const uint8_t* __restrict__ flags,
+                                                    const Grid& g) {
   uint32_t cell = recs[b].cell;
   int i = (int)(cell / (uint32_t)g.NY), j = (int)(cell % (uint32_t)g.NY);
   int c = i * g.P + j;
@@ -89,6 +88,27 @@ __global__ void k_apply_sources(const SourceRec* __restrict__ recs,
   U[c] = u;
   V[c] = v;
   M[c] = m;
+}
+
+__global__ void k_apply_sources(const SourceRec* __restrict__ recs,
+                                const uint32_t* __restrict__ off, int n_groups, float* U,
+                                float* V, float* M, const uint8_t* __restrict__ flags, Grid g) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_groups) return;
+  apply_sources_group(recs, off[k], off[k + 1], U, V, M, flags, g);
+}
+
+// A batch's sources: group k belongs to scene gs[k].
+__global__ void kb_apply_sources(const SourceRec* __restrict__ recs,
+                                 const uint32_t* __restrict__ off, const int* __restrict__ gs,
+                                 int n_groups, float* U, float* V, float* M,
+                                 const uint8_t* __restrict__ flags,
+                                 const BScene* __restrict__ sc) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_groups) return;
+  const BScene& s = sc[gs[k]];
+  apply_sources_group(recs, off[k], off[k + 1], U + s.off, V + s.off, M + s.off, flags + s.off,
+                      s.g);
 }
 
 // applyViscosity (fluid.go:112-142): out = U + visc*lap(U) on fluid interior
@@ -118,11 +138,9 @@ __global__ void k_viscosity(const float* __restrict__ U, const float* __restrict
 
 // Curl pass of applyVorticityConfinement (fluid.go:455-466); zero on cells
 // the reference leaves at the fresh array's zero.
-__global__ void k_curl(const float* __restrict__ U, const float* __restrict__ V,
-                       float* __restrict__ curl, const uint8_t* __restrict__ flags, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void curl_cell(int i, int j, const float* __restrict__ U,
+                                          const float* __restrict__ V, float* __restrict__ curl,
+                                          const uint8_t* __restrict__ flags, const Grid& g) {
   int c = i * g.P + j;
   float w = 0.0f;
   uint8_t fl = flags[c];
@@ -133,17 +151,24 @@ __global__ void k_curl(const float* __restrict__ U, const float* __restrict__ V,
   }
   curl[c] = w;
 }
+__global__ void k_curl(const float* __restrict__ U, const float* __restrict__ V,
+                       float* __restrict__ curl, const uint8_t* __restrict__ flags, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  curl_cell(i, j, U, V, curl, flags, g);
+}
 
 // Force pass of applyVorticityConfinement (fluid.go:468-492) followed by
 // addTurbulence (fluid.go:496-526).  Both touch only the cell's own U, V, so
 // running them per cell in that order equals the reference's two loops.
-__global__ void k_conf_turb(float* __restrict__ U, float* __restrict__ V,
-                            const float* __restrict__ curl, const float2* __restrict__ noise,
-                            const uint8_t* __restrict__ flags, float conf, float dt,
-                            float turbStrength, int do_conf, int do_turb, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void conf_turb_cell(int i, int j, float* __restrict__ U,
+                                               float* __restrict__ V,
+                                               const float* __restrict__ curl,
+                                               const float2* __restrict__ noise,
+                                               const uint8_t* __restrict__ flags, float conf,
+                                               float dt, float turbStrength, int do_conf,
+                                               int do_turb, const Grid& g) {
   int c = i * g.P + j;
   uint8_t fl = flags[c];
   if ((fl & (F_INTERIOR | F_FLUID)) != (F_INTERIOR | F_FLUID)) return;
@@ -175,13 +200,21 @@ __global__ void k_conf_turb(float* __restrict__ U, float* __restrict__ V,
   U[c] = u;
   V[c] = v;
 }
+__global__ void k_conf_turb(float* __restrict__ U, float* __restrict__ V,
+                            const float* __restrict__ curl, const float2* __restrict__ noise,
+                            const uint8_t* __restrict__ flags, float conf, float dt,
+                            float turbStrength, int do_conf, int do_turb, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  conf_turb_cell(i, j, U, V, curl, noise, flags, conf, dt, turbStrength, do_conf, do_turb, g);
+}
 
 // handleBorders (fluid.go:236-289): thread t does the ghost rows j = 0 and
 // j = NY-1 of U for i = t, and the ghost columns i = 0 and i = NX-1 of V for
 // j = t.  The two loops touch disjoint data.
-__global__ void k_borders(float* __restrict__ U, float* __restrict__ V,
-                          const uint8_t* __restrict__ flags, Grid g) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void borders_border(int t, float* __restrict__ U, float* __restrict__ V,
+                                               const uint8_t* __restrict__ flags, const Grid& g) {
   const int P = g.P, NX = g.NX, NY = g.NY;
   auto fluid = [&](int i, int j) { return (flags[i * P + j] & F_FLUID) != 0; };
   if (t < NX) {
@@ -221,6 +254,11 @@ __global__ void k_borders(float* __restrict__ U, float* __restrict__ V,
     }
   }
 }
+__global__ void k_borders(float* __restrict__ U, float* __restrict__ V,
+                          const uint8_t* __restrict__ flags, Grid g) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  borders_border(t, U, V, flags, g);
+}
 
 // copyBorder (fluid.go:436-446).
 __global__ void k_copy_border(float* __restrict__ dst, const float* __restrict__ src, Grid g) {
@@ -256,9 +294,14 @@ cudaError_t launch_apply_edits(fg_fluid* f, int n_groups, int slot) {
 cudaError_t launch_apply_sources(fg_fluid* f) {
   if (f->n_src_groups <= 0) return cudaSuccess;
   count(f);
-  k_apply_sources<<<(f->n_src_groups + 255) / 256, 256, 0, f->stream>>>(
-      f->src_dev, f->src_off_dev, f->n_src_groups, f->d[FG_U], f->d[FG_V], f->d[FG_M], f->flags,
-      f->g);
+  if (f->batch)
+    kb_apply_sources<<<(f->n_src_groups + 255) / 256, 256, 0, f->stream>>>(
+        f->src_dev, f->src_off_dev, f->batch->src_scene, f->n_src_groups, f->d[FG_U],
+        f->d[FG_V], f->d[FG_M], f->flags, f->batch->scenes_dev);
+  else
+    k_apply_sources<<<(f->n_src_groups + 255) / 256, 256, 0, f->stream>>>(
+        f->src_dev, f->src_off_dev, f->n_src_groups, f->d[FG_U], f->d[FG_V], f->d[FG_M],
+        f->flags, f->g);
   return cudaGetLastError();
 }
 
@@ -277,21 +320,20 @@ cudaError_t launch_confinement_turbulence(fg_fluid* f, float dt, bool conf, bool
   if (!conf && !turb) return cudaSuccess;
   if (conf) {
     count(f);
-    k_curl<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->curl,
-                                                          f->flags, f->g);
+    FG_CELLS(f, k_curl, curl_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V], f->curl,
+             (const uint8_t*)f->flags);
   }
   float turbStrength = f->prm.turbulence_strength * dt;
   count(f);
-  k_conf_turb<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(
-      f->d[FG_U], f->d[FG_V], f->curl, f->noise, f->flags, f->prm.confinement, dt, turbStrength,
-      conf ? 1 : 0, turb ? 1 : 0, f->g);
+  FG_CELLS(f, k_conf_turb, conf_turb_cell, f->d[FG_U], f->d[FG_V], (const float*)f->curl,
+           (const float2*)f->noise, (const uint8_t*)f->flags, f->prm.confinement, dt,
+           turbStrength, conf ? 1 : 0, turb ? 1 : 0);
   return cudaGetLastError();
 }
 
 cudaError_t launch_borders(fg_fluid* f) {
-  int n = f->NX > f->NY ? f->NX : f->NY;
   count(f);
-  k_borders<<<(n + 127) / 128, 128, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->flags, f->g);
+  FG_BORDER(f, k_borders, borders_border, f->d[FG_U], f->d[FG_V], (const uint8_t*)f->flags);
   return cudaGetLastError();
 }
 

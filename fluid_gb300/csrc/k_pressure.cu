@@ -22,6 +22,7 @@
 //    solve on it, phi += e.
 #include <mutex>
 
+#include "fg_batch.cuh"
 #include "fg_internal.cuh"
 #include "fg_reduce.cuh"
 
@@ -165,14 +166,12 @@ struct WTab {
 // elsewhere (ring included); phi = 0 when `zero_phi` (a solve with no sweeps
 // reads it directly).
 // U, V use the grid pitch g.P, the solver arrays the pitch Ps.
-__global__ void k_setup_system(const float* __restrict__ U, const float* __restrict__ V,
-                               float* __restrict__ phi, float* __restrict__ rhs,
-                               float* __restrict__ W, float* __restrict__ BW,
-                               const uint8_t* __restrict__ flags, float om, int zero_phi, Grid g,
-                               int Ps) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
+__device__ __forceinline__ void setup_cell_p(int i, int j, const float* __restrict__ U,
+                                             const float* __restrict__ V, float* __restrict__ phi,
+                                             float* __restrict__ rhs, float* __restrict__ W,
+                                             float* __restrict__ BW,
+                                             const uint8_t* __restrict__ flags, float om,
+                                             int zero_phi, const Grid& g, int Ps) {
   int u = i * g.P + j;
   int c = i * Ps + j;
   float b = 0.0f, w = 0.0f, bw = 0.0f;
@@ -187,6 +186,24 @@ __global__ void k_setup_system(const float* __restrict__ U, const float* __restr
   W[c] = w;
   BW[c] = bw;
   if (zero_phi) phi[c] = 0.0f;
+}
+__device__ __forceinline__ void setup_cell(int i, int j, const float* __restrict__ U,
+                                           const float* __restrict__ V, float* __restrict__ phi,
+                                           float* __restrict__ rhs, float* __restrict__ W,
+                                           float* __restrict__ BW,
+                                           const uint8_t* __restrict__ flags, float om,
+                                           int zero_phi, const Grid& g) {
+  setup_cell_p(i, j, U, V, phi, rhs, W, BW, flags, om, zero_phi, g, g.P);
+}
+__global__ void k_setup_system(const float* __restrict__ U, const float* __restrict__ V,
+                               float* __restrict__ phi, float* __restrict__ rhs,
+                               float* __restrict__ W, float* __restrict__ BW,
+                               const uint8_t* __restrict__ flags, float om, int zero_phi, Grid g,
+                               int Ps) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  setup_cell_p(i, j, U, V, phi, rhs, W, BW, flags, om, zero_phi, g, Ps);
 }
 
 // Register-blocked, temporally blocked Jacobi.  A CTA of 8 warps holds a
@@ -207,6 +224,7 @@ constexpr int RI = NWARP * RT;     // 64 region rows
 constexpr int OJ = RJ - 2 * TMAX;  // 112 owned columns
 constexpr int OI = RI - 2 * TMAX;  // 48 owned rows
 constexpr int TB_THREADS = 32 * NWARP;
+static_assert(OI == kJacTileRows && OJ == kJacTileCols, "batch Jacobi tiles");
 
 // RINIT (first launch of the outer correction): instead of loading bw, the
 // kernel loads the main potential phi (from the buffer the main solve's
@@ -216,14 +234,13 @@ constexpr int TB_THREADS = 32 * NWARP;
 // sets bw = w * b_e, starts the correction from 0 and, when more launches
 // follow, writes b_e and bw_e of the owned cells to rhs_e / bwe.
 template <bool OMEGA1, bool FULL, bool CHECK, bool RINIT>
-__global__ void __launch_bounds__(TB_THREADS, 2)
-    k_jacobi_rb(const float* __restrict__ src, float* __restrict__ dst,
-                const float* __restrict__ W, const float* __restrict__ BW,
-                const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float om1,
-                PCtl* ctl, int k, int t0, int ns, float tol, int out_sel, int zero_init, Grid g,
-                const float* __restrict__ mphi0, const float* __restrict__ mphi1,
-                const PCtl* __restrict__ mctl, float* __restrict__ rhs_e,
-                float* __restrict__ bwe) {
+__device__ __forceinline__ void jacobi_tile(
+    int tbx, int tby, bool lead, const float* __restrict__ src, float* __restrict__ dst,
+    const float* __restrict__ W, const float* __restrict__ BW, const float* __restrict__ rhs,
+    const uint8_t* __restrict__ flags, float om1, PCtl* ctl, int k, int t0, int ns, float tol,
+    int out_sel, int zero_init, Grid g, const float* __restrict__ mphi0,
+    const float* __restrict__ mphi1, const PCtl* __restrict__ mctl, float* __restrict__ rhs_e,
+    float* __restrict__ bwe) {
   __shared__ float4 xch[2][2][NWARP][32];
   __shared__ float red[NWARP];
   __shared__ int skip;
@@ -238,8 +255,8 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   __syncthreads();
   if (skip) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int gi0 = blockIdx.y * OI - TMAX + warp * RT;
-  const int gj = blockIdx.x * OJ - TMAX + lane * JT;
+  const int gi0 = tby * OI - TMAX + warp * RT;
+  const int gj = tbx * OJ - TMAX + lane * JT;
   // gj is a multiple of 4 and the pitch a multiple of 4: a 4-column group is
   // either wholly left of the grid or a 16-byte aligned read inside the row.
   const bool colok = gj >= 0 && gj < g.P;
@@ -425,13 +442,58 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
       for (int q = 0; q < NWARP; ++q) m = fmaxf(m, red[q]);
       if (m > 0.0f) atomicMax(&ctl->slots[k], __float_as_uint(m));
     }
-    if (blockIdx.x == 0 && blockIdx.y == 0) {
+    if (lead) {
       ctl->sweeps = t0 + ns;
       ctl->last_launch = k;
       ctl->sel = out_sel;
     }
   }
 }
+
+template <bool OMEGA1, bool FULL, bool CHECK, bool RINIT>
+__global__ void __launch_bounds__(TB_THREADS, 2)
+    k_jacobi_rb(const float* __restrict__ src, float* __restrict__ dst,
+                const float* __restrict__ W, const float* __restrict__ BW,
+                const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float om1,
+                PCtl* ctl, int k, int t0, int ns, float tol, int out_sel, int zero_init, Grid g,
+                const float* __restrict__ mphi0, const float* __restrict__ mphi1,
+                const PCtl* __restrict__ mctl, float* __restrict__ rhs_e,
+                float* __restrict__ bwe) {
+  jacobi_tile<OMEGA1, FULL, CHECK, RINIT>(blockIdx.x, blockIdx.y,
+                                          blockIdx.x == 0 && blockIdx.y == 0, src, dst, W, BW,
+                                          rhs, flags, om1, ctl, k, t0, ns, tol, out_sel,
+                                          zero_init, g, mphi0, mphi1, mctl, rhs_e, bwe);
+}
+
+// A batch's Jacobi launch k of L: scene s runs its nl_s = ceil(iters_s / T)
+// launches as the last nl_s of the L, the first of them with the remainder
+// sweeps, so every scene ends in the same buffer.  Blocks of scenes that
+// have not started return at once.
+template <bool OMEGA1>
+__global__ void __launch_bounds__(TB_THREADS, 2)
+    kb_jacobi(const BTile* __restrict__ tiles, const BScene* __restrict__ sc,
+              const float* __restrict__ src, float* __restrict__ dst, const float* __restrict__ W,
+              const float* __restrict__ BW, const uint8_t* __restrict__ flags, float om1,
+              PCtl* ctl, int k, int L, int T, int out_sel) {
+  const BTile t = tiles[blockIdx.x];
+  const BScene& s = sc[t.s];
+  const int nl = (s.iters + T - 1) / T;
+  const int first = L - nl;
+  if (k < first) return;
+  const int ns = k == first ? s.iters - (nl - 1) * T : T;
+  const long long o = s.off;
+  if (ns == TMAX)
+    jacobi_tile<OMEGA1, true, false, false>(t.x, t.y, blockIdx.x == 0, src + o, dst + o, W + o,
+                                            BW + o, nullptr, flags + o, om1, ctl, k, 0, ns, 0.0f,
+                                            out_sel, k == first, s.g, nullptr, nullptr, nullptr,
+                                            nullptr, nullptr);
+  else
+    jacobi_tile<OMEGA1, false, false, false>(t.x, t.y, blockIdx.x == 0, src + o, dst + o, W + o,
+                                             BW + o, nullptr, flags + o, om1, ctl, k, 0, ns, 0.0f,
+                                             out_sel, k == first, s.g, nullptr, nullptr, nullptr,
+                                             nullptr, nullptr);
+}
+
 
 // Final potential at cell c: the main iterate, plus the outer correction on
 // active cells when one ran (phi = phi + e, fluid.go's p accumulation aside).
@@ -604,6 +666,23 @@ __global__ void k_store_phi(const float* __restrict__ phi0, const float* __restr
   if (k < n) dst[k] = src[k];
 }
 
+// A batch's gradient subtract: grad_cell without the statistics.
+__device__ __forceinline__ void grad_batch_cell(int i, int j, const float* __restrict__ U,
+                                                const float* __restrict__ V,
+                                                float* __restrict__ Uo, float* __restrict__ Vo,
+                                                float* __restrict__ p,
+                                                const float* __restrict__ phi0,
+                                                const float* __restrict__ phi1,
+                                                const PCtl* __restrict__ ctl,
+                                                const float* __restrict__ rhs,
+                                                const uint8_t* __restrict__ flags, float cp,
+                                                const float2* __restrict__ noise,
+                                                float turbStrength, int do_turb, const Grid& g) {
+  GradAcc acc{{0.0f, 0.0f}, {0.0f, 0.0f}, 0.0f, 0.0f, 0.0f};
+  grad_cell(i, j, U, V, Uo, Vo, p, ctl->sel ? phi1 : phi0, nullptr, rhs, flags, cp, noise,
+            turbStrength, do_turb, g, acc);
+}
+
 __global__ void k_store_div_p(const float* __restrict__ r, DevStats* st) {
   st->div_l2_sq = row_sum(r, 0);
   st->div_max = (double)r[2];
@@ -677,8 +756,34 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
   return cudaGetLastError();
 }
 
+// A batch's solves: every scene runs its own sweep count, no early exit.
+static cudaError_t jacobi_solve_batch(fg_fluid* f, PCtl* ctl, const float* bw, float* x0,
+                                      float* x1) {
+  const BatchGeom* bt = f->batch;
+  int T = clamp_tb(f->prm.tb_depth);
+  int L = (bt->max_iters + T - 1) / T;
+  cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(PCtl), f->stream);
+  if (e != cudaSuccess) return e;
+  float om = f->prm.jacobi_omega * f->prm.pressure_damping;
+  float om1 = 1.0f - om;
+  for (int k = 0; k < L; ++k) {
+    const float* src = (k & 1) ? x1 : x0;
+    float* dst = (k & 1) ? x0 : x1;
+    int sel = (k & 1) ? 0 : 1;
+    if (om1 == 0.0f)
+      kb_jacobi<true><<<bt->n_jac_tiles, TB_THREADS, 0, f->stream>>>(
+          bt->jac_tiles, bt->scenes_dev, src, dst, f->wgt, bw, f->flags, om1, ctl, k, L, T, sel);
+    else
+      kb_jacobi<false><<<bt->n_jac_tiles, TB_THREADS, 0, f->stream>>>(
+          bt->jac_tiles, bt->scenes_dev, src, dst, f->wgt, bw, f->flags, om1, ctl, k, L, T, sel);
+  }
+  count(f, L);
+  return cudaGetLastError();
+}
+
 static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const float* bw, float* x0,
                                 float* x1, int iters, bool allow_exit, bool rinit = false) {
+  if (f->batch) return jacobi_solve_batch(f, ctl, bw, x0, x1);
   int T = clamp_tb(f->prm.tb_depth);
   int nlaunch = (iters + T - 1) / T;
   if (nlaunch > f->n_slots) return cudaErrorInvalidValue;
@@ -724,6 +829,23 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   PCtl* ectl = (PCtl*)f->ectl;
   dim3 gr = cell_grid(f), bl(BX, BY);
   float om = f->prm.jacobi_omega * f->prm.pressure_damping;
+  if (f->batch) {
+    // Every scene solves (the batch forbids early exit and refinement);
+    // no statistics.
+    count(f);
+    FG_CELLS_BATCH(f, setup_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V], f->phi,
+                   f->rhs, f->wgt, f->bw, (const uint8_t*)f->flags, om, 1);
+    if ((e = jacobi_solve_batch(f, ctl, f->bw, f->phi, f->phi2)) != cudaSuccess) return e;
+    count(f);
+    FG_CELLS_BATCH(f, grad_batch_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V],
+                   f->partner[FG_U], f->partner[FG_V], f->d[FG_P], (const float*)f->phi,
+                   (const float*)f->phi2, (const PCtl*)ctl, (const float*)f->rhs,
+                   (const uint8_t*)f->flags, cp, (const float2*)f->noise,
+                   f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0);
+    swap_state(f, FG_U);
+    swap_state(f, FG_V);
+    return cudaGetLastError();
+  }
   // sel = 0 (phi) until a launch runs.
   if ((e = cudaMemsetAsync(ctl, 0, sizeof(PCtl), f->stream)) != cudaSuccess) return e;
   count(f);
@@ -769,6 +891,16 @@ cudaError_t launch_store_phi(fg_fluid* f, float* dst) {
 
 cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi) {
   float cp = f->density * f->h / dt;  // fluid.go:158
+  if (f->batch) {
+    count(f);
+    FG_CELLS_BATCH(f, grad_batch_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V],
+                   f->partner[FG_U], f->partner[FG_V], f->d[FG_P], phi, phi,
+                   (const PCtl*)f->pctl, (const float*)f->rhs, (const uint8_t*)f->flags, cp,
+                   (const float2*)f->noise, 0.0f, 0);
+    swap_state(f, FG_U);
+    swap_state(f, FG_V);
+    return cudaGetLastError();
+  }
   dim3 rg((f->NY + BX - 1) / BX, (f->NX + BY * GR - 1) / (BY * GR)), bl(BX, BY);
   if (!partials_fit(f, 5, rg.x * rg.y)) return cudaErrorInvalidValue;
   count(f);

@@ -483,3 +483,140 @@ class Fluid:
         if not self.auto_sync:
             self.download((1 << FIELDS["U"]) | (1 << FIELDS["V"]))
         return VectorField(self.NumX, self.NumY, self.U, self.V)
+
+
+class Batch:
+    """Many Fluid scenes stepped together (fg_batch_create).
+
+    The scenes keep their own sizes, obstacles, sources and num_iters; they
+    must share every other parameter (Jacobi scheme, no early exit,
+    refinement or viscosity).  ``step`` advances every scene; ``scatter``
+    copies the batch's state back into the scene objects (whose mirrors are
+    then refreshed on ``download``).  The scene objects must outlive the
+    batch; the batch holds references to them.
+    """
+
+    def __init__(self, scenes):
+        scenes = list(scenes)
+        if not scenes:
+            raise ValueError("empty batch")
+        L = _lib.lib()
+        self._L = L
+        self.scenes = scenes
+        for s in scenes:
+            s._before()  # push parameters and, with auto_sync, the mirrors
+        arr = (ctypes.c_void_p * len(scenes))(*[s.handle.value for s in scenes])
+        h = ctypes.c_void_p()
+        rc = L.fg_batch_create(arr, len(scenes), ctypes.byref(h))
+        if rc != 0:
+            msg = L.fg_last_error(scenes[0].handle)
+            raise FluidError(rc, "fg_batch_create: %s" % (msg.decode() if msg else ""))
+        self._h = h
+
+    def __del__(self):
+        h = self.__dict__.get("_h")
+        if h:
+            self._L.fg_destroy(h)
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    def __len__(self):
+        return len(self.scenes)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self._L.fg_last_error(self._h)
+            raise FluidError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self):
+        return self._L.fg_stream(self._h)
+
+    def step(self, dt):
+        self._check(self._L.fg_batch_step(self._h, ctypes.c_float(dt)), "fg_batch_step")
+
+    def synchronize(self):
+        self._check(self._L.fg_synchronize(self._h), "fg_synchronize")
+
+    def scatter(self):
+        """Copies every scene's state from the batch into its Fluid object."""
+        self._check(self._L.fg_batch_scatter(self._h), "fg_batch_scatter")
+        for s in self.scenes:
+            if s.auto_sync:
+                s.download()
+
+    def gather(self):
+        """Copies every Fluid object's state into the batch."""
+        for s in self.scenes:
+            s._before()
+        self._check(self._L.fg_batch_gather(self._h), "fg_batch_gather")
+
+    def autotune(self, dt, reps=3):
+        """(tb_depth, block_x, block_y, ms_per_step) of the fastest candidate."""
+        tb, bx, by = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ms = ctypes.c_float()
+        self._check(self._L.fg_batch_autotune(self._h, ctypes.c_float(dt), int(reps),
+                                              ctypes.byref(tb), ctypes.byref(bx),
+                                              ctypes.byref(by), ctypes.byref(ms)),
+                    "fg_batch_autotune")
+        return tb.value, bx.value, by.value, ms.value
+
+    def launch_count(self):
+        return int(self._L.fg_launch_count(self._h))
+
+    def profile(self, on=True):
+        self._check(self._L.fg_profile_enable(self._h, int(bool(on))), "fg_profile_enable")
+
+    # ------------------------------------------------------------ recorded rollouts
+    def tape_begin(self, max_steps, every=8):
+        self._check(self._L.fg_tape_begin(self._h, int(max_steps), int(every)), "fg_tape_begin")
+
+    def step_forward(self, dt):
+        self._check(self._L.fg_step_forward(self._h, ctypes.c_float(dt), None, None),
+                    "fg_step_forward")
+
+    def seed_smoke_l2(self, targets):
+        """Seeds L_s = ||M_s - targets[s]||_2 per scene; returns the n losses."""
+        keep = [np.ascontiguousarray(t, np.float32) if isinstance(t, np.ndarray) else t
+                for t in targets]
+        ptrs = (ctypes.c_void_p * len(keep))(
+            *[t.ctypes.data if isinstance(t, np.ndarray) else t.data_ptr() for t in keep])
+        losses = (ctypes.c_double * len(keep))()
+        self._check(self._L.fg_batch_seed_smoke_l2(self._h, ptrs, losses),
+                    "fg_batch_seed_smoke_l2")
+        return np.array(losses[:], np.float64)
+
+    def step_adjoint(self):
+        self._check(self._L.fg_batch_step_adjoint(self._h), "fg_batch_step_adjoint")
+
+    def grad(self, s):
+        """dL_s/d(initial U, V, M) of scene s."""
+        n = self.scenes[s].numCells
+        out = [np.zeros(n, np.float32) for _ in range(3)]
+        self._check(self._L.fg_batch_grad(self._h, int(s), *[o.ctypes.data for o in out]),
+                    "fg_batch_grad")
+        return dict(zip(("U", "V", "M"), out))
+
+    def tape_end(self):
+        self._check(self._L.fg_tape_end(self._h), "fg_tape_end")
+
+    def rollout_grad(self, dt, steps, targets, every=8):
+        """Per-scene losses ||M_s - targets[s]||_2 after `steps` steps and each
+        scene's gradients w.r.t. its initial U, V, M."""
+        self.tape_begin(steps, every)
+        try:
+            for _ in range(steps):
+                self.step_forward(dt)
+            losses = self.seed_smoke_l2(targets)
+            for _ in range(steps):
+                self.step_adjoint()
+            grads = [self.grad(s) for s in range(len(self.scenes))]
+        finally:
+            self.tape_end()
+        return losses, grads

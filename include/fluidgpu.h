@@ -273,6 +273,46 @@ int fg_tape_grad(fg_fluid* f, float* dU, float* dV, float* dM, float* dNU, float
 int fg_tape_steps(const fg_fluid* f, int* forward, int* reversed);
 int fg_tape_end(fg_fluid* f);
 
+/* Batches: many independent scenes of different sizes stepped together (no
+ * counterpart in the reference, which steps one Fluid at a time).
+ *
+ * fg_batch_create(scenes, n, &batch) packs the state of n scene handles into
+ * one batch handle: every stage then runs as one launch over all scenes
+ * (each scene keeping its own size, obstacles, sources and pressure sweep
+ * count), and fg_simulate / fg_batch_step capture a whole batch step in one
+ * CUDA graph.  The members must use the JACOBI scheme without early exit,
+ * refinement, viscosity or multigrid, and share every parameter except
+ * num_iters (>= 1); else FG_ERR_UNSUPPORTED / FG_ERR_INVALID.  A batch step
+ * gives each scene the same bits as fg_simulate on its handle; it computes
+ * no statistics.  The members are left as they were: fg_batch_scatter copies
+ * the batch's state into them, fg_batch_gather copies theirs into the batch
+ * (the sources and parameters are fixed at creation).  Destroy the batch
+ * before its members.
+ *
+ * A batch takes the recorded-rollout calls (fg_tape_begin, fg_step_forward
+ * without force fields, fg_step_adjoint without force gradients,
+ * fg_tape_end); fg_batch_seed_smoke_l2 seeds L_s = ||M_s - target_s||_2 per
+ * scene (targets[s]: NumX_s * NumY_s values) and returns the n losses;
+ * fg_batch_grad returns scene s's dL_s/d(initial U, V, M).
+ *
+ * fg_batch_autotune times each candidate thread-block shape of the per-cell
+ * kernels and Jacobi sweeps per launch (tb_depth) on `reps` steps of this
+ * batch from its current state (restored afterwards), keeps the fastest and
+ * reports it.  The choice changes no result bit.
+ *
+ * Entry points that address one scene's cells, mirrors or views return
+ * FG_ERR_UNSUPPORTED on a batch handle. */
+int fg_batch_create(fg_fluid* const* scenes, int n, fg_fluid** batch);
+int fg_batch_size(const fg_fluid* batch, int* n);
+int fg_batch_step(fg_fluid* batch, float dt);
+int fg_batch_step_adjoint(fg_fluid* batch);
+int fg_batch_gather(fg_fluid* batch);
+int fg_batch_scatter(fg_fluid* batch);
+int fg_batch_seed_smoke_l2(fg_fluid* batch, const float* const* targets, double* losses);
+int fg_batch_grad(fg_fluid* batch, int scene, float* dU, float* dV, float* dM);
+int fg_batch_autotune(fg_fluid* batch, float dt, int reps, int* tb_depth, int* block_x,
+                      int* block_y, float* ms_per_step);
+
 /* Text of the last error on the handle ("" if none); static text for a
  * NULL handle. */
 const char* fg_last_error(const fg_fluid* f);

@@ -111,3 +111,35 @@ def gaussian_target(nx, ny, seed=4, n=4, sigma=(10.0, 30.0), amp=(0.5, 1.0)):
         ci, cj = rng.uniform(1, nx - 1), rng.uniform(1, ny - 1)
         T += a * np.exp(-((i - ci) ** 2 + (j - cj) ** 2) / (2 * s * s))
     return T.ravel().astype(np.float32)
+
+
+# ---------------------------------------------------------------- ensembles
+def ensemble_scene(f, rng, radius=(4.0, 32.0), speed=(0.5, 2.0)):
+    """One scene of a batched ensemble on f: walls left, top and bottom, open
+    right; 0-5 solid discs (radius drawn from `radius`, capped at a sixth of
+    the smaller side) and 1-3 jet inlets of 8 rows on the left wall (U drawn
+    from `speed`, smoke assigned 1) held by device sources."""
+    fast_walls(f)
+    f.mark_dirty()
+    nx, ny = f.NumX - 2, f.NumY - 2
+    for _ in range(int(rng.integers(0, 6))):
+        r = int(min(rng.uniform(*radius), max(1, min(nx, ny) // 6)))
+        cx = int(rng.uniform(nx * 0.3, max(nx * 0.3 + 1, nx - r - 1)))
+        cy = int(rng.uniform(r + 2, max(r + 3, ny - r - 2)))
+        f.SetCircularObstacle(cx, cy, r)
+    rows, us = [], []
+    for _ in range(int(rng.integers(1, 4))):
+        c = int(rng.uniform(5, max(6, ny - 4)))
+        sp = float(rng.uniform(*speed))
+        for j in range(max(1, c - 4), min(ny + 1, c + 4)):
+            rows.append(j)
+            us.append(sp)
+    rows = np.array(rows, np.int32)
+    f.set_sources(np.ones_like(rows), rows, u=np.array(us, np.float32), v=0.0, smoke=1.0,
+                  mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY | f.SRC_SET_SMOKE)
+
+
+def ensemble_sides(n, seed=5, lo=64, hi=512):
+    """Square grid sides drawn log-uniformly from [lo, hi] (seeded)."""
+    rng = np.random.default_rng(seed)
+    return [int(round(np.exp(rng.uniform(np.log(lo), np.log(hi))))) for _ in range(n)]
