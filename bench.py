@@ -362,6 +362,101 @@ def rollout256(fluid_gb300, args):
     }
 
 
+def ensemble(fluid_gb300, args, n=256, steps=20, roll=16, every=8):
+    """The batched-ensemble configuration: n scenes (seed 5), square sides
+    log-uniform in [64, 512], 0-5 discs of radius 4-32, 1-3 jets at U(0.5, 2)
+    with smoke, 40-120 Jacobi sweeps per scene, BFECC, FP32.  One batch
+    (autotuned block shape and sweeps per launch, each step one CUDA graph)
+    against the same scenes stepped one handle at a time, forward and
+    forward+adjoint (a `roll`-step rollout, checkpoint every `every`, loss
+    ||M_s - target_s||_2 per scene, gradients w.r.t. each initial state)."""
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import scenes
+
+    sides = scenes.ensemble_sides(n, seed=5)
+    iters = np.random.default_rng(5).integers(40, 121, n)
+
+    def build():
+        out = []
+        for k, side in enumerate(sides):
+            f = fluid_gb300.Fluid(1.0, side, side, 1.0, auto_sync=False, scheme=1,
+                                  num_iters=int(iters[k]), tb_depth=8, early_exit=False,
+                                  UseBFECC=True)
+            scenes.ensemble_scene(f, np.random.default_rng(5000 + k))
+            out.append(f)
+        return out
+
+    cells = sum(side * side for side in sides)
+    one = build()
+    mem = build()
+    targets = [scenes.gaussian_target(f.NumX, f.NumY, seed=50 + k) for k, f in enumerate(one)]
+    batch = fluid_gb300.Batch(mem)
+    tb, bx, by, _ = batch.autotune(DT, reps=3)
+    stream = torch.cuda.ExternalStream(batch.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(2):
+        batch.step(DT)
+    batch.synchronize()
+    l0 = batch.launch_count()
+    e0.record(stream)
+    for _ in range(steps):
+        batch.step(DT)
+    e1.record(stream)
+    batch.synchronize()
+    ms_b = e0.elapsed_time(e1) / steps
+    launches_b = (batch.launch_count() - l0) / steps
+
+    for f in one:  # warm (graph capture)
+        f.Simulate(DT)
+        f.Simulate(DT)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for f in one:
+            f.Simulate(DT)
+    for f in one:
+        f.synchronize()
+    ms_1 = 1e3 * (time.perf_counter() - t0) / steps
+
+    batch.rollout_grad(DT, roll, targets, every=every)
+    batch.synchronize()
+    e0.record(stream)
+    losses, _ = batch.rollout_grad(DT, roll, targets, every=every)
+    e1.record(stream)
+    batch.synchronize()
+    ms_ba = e0.elapsed_time(e1) / roll
+    t0 = time.perf_counter()
+    for k, f in enumerate(one):
+        f.rollout_grad(DT, roll, targets[k], every=every)
+    for f in one:
+        f.synchronize()
+    ms_1a = 1e3 * (time.perf_counter() - t0) / roll
+    batch.close()
+    return {
+        "config": "%d scenes (seed 5): sides log-uniform 64-512, 0-5 discs r 4-32, 1-3 jets "
+                  "U(0.5,2) with smoke, 40-120 Jacobi sweeps per scene, BFECC, FP32" % n,
+        "interior_cells": cells,
+        "autotune": {"tb_depth": tb, "block": [bx, by]},
+        "batch_fwd": {"value": cells / ms_b / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms_b,
+                      "launches_per_step": launches_b, "timing": "CUDA events, one graph per step"},
+        "one_at_a_time_fwd": {"value": cells / ms_1 / 1e3, "unit": "Mcell-steps/s",
+                              "ms_per_step": ms_1,
+                              "timing": "host clock around fg_simulate on each handle in turn"},
+        "batch_speedup_fwd": ms_1 / ms_b,
+        "batch_fwd_adjoint": {"value": cells / ms_ba / 1e3, "unit": "Mcell-steps/s",
+                              "ms_per_step": ms_ba, "rollout_steps": roll,
+                              "checkpoint_every": every},
+        "one_at_a_time_fwd_adjoint": {"value": cells / ms_1a / 1e3, "unit": "Mcell-steps/s",
+                                      "ms_per_step": ms_1a},
+        "batch_speedup_fwd_adjoint": ms_1a / ms_ba,
+        "loss_sum": float(np.sum(losses)),
+    }
+
+
 # ---------------------------------------------------------------- CPU legs
 def cpu_reference_steps(steps, threads, budget_s=None):
     """Times the reference algorithm (FP32, serial SOR pressure, parallelRange
@@ -524,6 +619,7 @@ def run_ours(args):
 
     adj = fwd_adjoint(fluid_gb300, args) if rank == 0 and not args.no_adjoint else None
     roll = rollout256(fluid_gb300, args) if rank == 0 and not args.no_adjoint else None
+    ens = ensemble(fluid_gb300, args) if rank == 0 and not args.no_ensemble else None
 
     # ------------------------------------------------------------ CPU baseline
     cpu = None
@@ -543,7 +639,7 @@ def run_ours(args):
             "data": "synthetic",
             "config": workload_config({"parallelism": "replicas%d" % world if world > 1 else "single"}),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "fwd_adjoint": adj, "rollout_256": roll,
+            "fwd_adjoint": adj, "rollout_256": roll, "ensemble": ens,
             "clocks": sampler.summary(),
             "host_ms_per_step": 1e3 * t_host / args.steps,
             "stage_ms": stage_ms,
@@ -564,6 +660,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
