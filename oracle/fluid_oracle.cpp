@@ -992,7 +992,8 @@ struct Fluid {
     if (val > hi) return hi;
     return val;
   }
-  void advectVelocityBFECC(T dt) {
+  // keep (optional): receives fwdU, fwdV, corrU, corrV for the adjoint.
+  void advectVelocityBFECC(T dt, std::vector<T>* keep = nullptr) {
     int n = NY;
     T hh = h, h2 = hh / (T)2;
     std::vector<T> origU = U, origV = V;
@@ -1032,11 +1033,18 @@ struct Fluid {
         corrU[i * n + j] = clampToNeighbors(corrU[i * n + j], origU, i, j);
         corrV[i * n + j] = clampToNeighbors(corrV[i * n + j], origV, i, j);
       }
+    if (keep) {
+      keep[0] = fwdU;
+      keep[1] = fwdV;
+      keep[2] = corrU;
+      keep[3] = corrV;
+    }
     U = corrU;
     V = corrV;
     advectVelocity(dt);
   }
-  void advectSmokeBFECC(T dt) {
+  // keep (optional): receives fwdM, corrM for the adjoint.
+  void advectSmokeBFECC(T dt, std::vector<T>* keep = nullptr) {
     int n = NY;
     T hh = h, h2 = (T)0.5 * hh;
     std::vector<T> origM = M;
@@ -1064,8 +1072,529 @@ struct Fluid {
         corrM[i * n + j] = clampToNeighbors(corrM[i * n + j], origM, i, j);
         if (corrM[i * n + j] < 0) corrM[i * n + j] = 0;
       }
+    if (keep) {
+      keep[0] = fwdM;
+      keep[1] = corrM;
+    }
     M = corrM;
     advectSmoke(dt);
+  }
+};
+
+}  // namespace orc
+
+// ===========================================================================
+// Reverse mode of a recorded rollout: the FP64 reference for the CUDA
+// adjoint (test infrastructure; the reference has no derivatives).  A step
+// is Simulate (fluid.go:79-109) with the parallel Jacobi scheme and a fixed
+// sweep count, a force field added to U, V before the sources, and the
+// sources of the rollout (the app's per-step SetVelocity / smoke calls).
+// Every step's intermediates are kept (small grids only); the reverse pass
+// runs the transposed stages sequentially, so it is deterministic.  The
+// subgradient conventions are those of the CUDA adjoint: a clamped sample
+// coordinate passes no position derivative, floor is locally constant, a
+// clamped BFECC value takes the derivative of the first bounding neighbour
+// in scan order, max(x, 0) passes for x >= 0, |x| passes sign(x) (0 at 0),
+// the turbulence gate passes its term only for |u| > 0.1 and below the
+// min(0.5|u|, 1) kink.
+// ===========================================================================
+namespace orc {
+
+struct Source {
+  int i, j;
+  double u, v, smoke;
+  int mode;  // bit 0 skip if solid, 1 set U V, 2 add smoke, 3 set smoke
+};
+
+template <typename T>
+struct Rollout {
+  Fluid<T>& f;
+  std::vector<Source> src;
+  struct Rec {
+    std::vector<T> U2, V2, U4, V4, k[4], U5, V5, M1, km[2];
+  };
+  std::vector<Rec> recs;
+  std::vector<T> dts;
+  std::vector<T> aU, aV, aM, aNU, aNV, aNM;
+  explicit Rollout(Fluid<T>& f_) : f(f_) {}
+
+  int n() const { return f.NY; }
+  bool ring(int i, int j) const { return i == 0 || j == 0 || i == f.NX - 1 || j == f.NY - 1; }
+  bool uadv(int i, int j) const {
+    return i >= 1 && j >= 1 && j <= f.NY - 2 && f.S[i * n() + j] != 0 && f.S[(i - 1) * n() + j] != 0;
+  }
+  bool vadv(int i, int j) const {
+    return i >= 1 && i <= f.NX - 2 && j >= 1 && f.S[i * n() + j] != 0 && f.S[i * n() + j - 1] != 0;
+  }
+  bool fluid_interior(int i, int j) const {
+    return i >= 1 && i <= f.NX - 2 && j >= 1 && j <= f.NY - 2 && f.S[i * n() + j] != 0;
+  }
+
+  void apply_sources() {
+    for (const Source& s : src) {
+      int c = s.i * n() + s.j;
+      if ((s.mode & 1) && f.S[c] == 0) continue;
+      if (s.mode & 2) {
+        f.U[c] = (T)s.u;
+        f.V[c] = (T)s.v;
+      }
+      if (s.mode & 8)
+        f.M[c] = (T)s.smoke;
+      else if (s.mode & 4)
+        f.M[c] = f.M[c] + (T)s.smoke;
+    }
+  }
+
+  void step(T dt, const T* fu, const T* fv) {
+    Rec r;
+    if (fu)
+      for (int c = 0; c < f.N; ++c) {
+        f.U[c] += fu[c];
+        f.V[c] += fv[c];
+      }
+    apply_sources();
+    std::fill(f.p.begin(), f.p.end(), (T)0);
+    f.makeIncompressible(f.num_iters, dt);
+    r.U2 = f.U;
+    r.V2 = f.V;
+    if (f.Confinement != 0) f.applyVorticityConfinement(dt);
+    if (f.TurbulenceStrength > 0) f.addTurbulence(dt);
+    f.handleBorders();
+    r.U4 = f.U;
+    r.V4 = f.V;
+    if (f.UseBFECC)
+      f.advectVelocityBFECC(dt, r.k);
+    else
+      f.advectVelocity(dt);
+    r.U5 = f.U;
+    r.V5 = f.V;
+    r.M1 = f.M;
+    if (f.UseBFECC)
+      f.advectSmokeBFECC(dt, r.km);
+    else
+      f.advectSmoke(dt);
+    recs.push_back(std::move(r));
+    dts.push_back(dt);
+  }
+
+  // d sample / d (x, y) and the scatter of lam into dD (sampleFrom's
+  // bilinear weights); fld as sampleFrom.
+  void sample_adj(T x, T y, const std::vector<T>& D, std::vector<T>& dD, int fld, T lam, T* gx,
+                  T* gy) const {
+    const int NX = f.NX, NY = f.NY;
+    const T h = f.h, h1 = (T)1.0 / h, h2 = (T)0.5 * h;
+    T xc = std::fmax(std::fmin(x, (T)NX * h), h), yc = std::fmax(std::fmin(y, (T)NY * h), h);
+    T dx = fld == 0 ? 0 : h2, dy = fld == 1 ? 0 : h2;
+    int x0 = std::min((int)std::floor((double)((xc - dx) * h1)), NX - 1);
+    T tx = ((xc - dx) - (T)x0 * h) * h1;
+    int x1 = std::min(x0 + 1, NX - 1);
+    int y0 = std::min((int)std::floor((double)((yc - dy) * h1)), NY - 1);
+    T ty = ((yc - dy) - (T)y0 * h) * h1;
+    int y1 = std::min(y0 + 1, NY - 1);
+    T sx = 1 - tx, sy = 1 - ty;
+    T f00 = D[x0 * NY + y0], f10 = D[x1 * NY + y0], f11 = D[x1 * NY + y1], f01 = D[x0 * NY + y1];
+    dD[x0 * NY + y0] += sx * sy * lam;
+    dD[x1 * NY + y0] += tx * sy * lam;
+    dD[x1 * NY + y1] += tx * ty * lam;
+    dD[x0 * NY + y1] += sx * ty * lam;
+    *gx = xc == x ? h1 * (sy * (f10 - f00) + ty * (f11 - f01)) : (T)0;
+    *gy = yc == y ? h1 * (sx * (f01 - f00) + tx * (f11 - f10)) : (T)0;
+  }
+
+  // Adjoint of advectVelocity with trace field = sampled field = border
+  // field (Ut, Vt) traced at sdt (-dt: BFECC's reverse sample, whose faces
+  // that are not advected are constant 0: dR = dN = null).
+  void sl_vel_adj(const std::vector<T>& lu, const std::vector<T>& lv, const std::vector<T>& Ut,
+                  const std::vector<T>& Vt, const std::vector<T>& Fu, const std::vector<T>& Fv,
+                  std::vector<T>& dUt, std::vector<T>& dVt, std::vector<T>& dFu,
+                  std::vector<T>& dFv, std::vector<T>* dRu, std::vector<T>* dRv,
+                  std::vector<T>* dNu, std::vector<T>* dNv, T sdt) const {
+    const int nn = n();
+    const T h = f.h, h2 = h / (T)2;
+    for (int i = 0; i < f.NX; ++i)
+      for (int j = 0; j < f.NY; ++j) {
+        int c = i * nn + j;
+        if (uadv(i, j)) {
+          T x = (T)i * h - sdt * Ut[c];
+          T y = (T)j * h + h2 - sdt * f.avgV(Vt, i, j);
+          T gx, gy;
+          sample_adj(x, y, Fu, dFu, 0, lu[c], &gx, &gy);
+          dUt[c] += -sdt * gx * lu[c];
+          T q = (T)0.25 * (-sdt * gy * lu[c]);
+          dVt[c - nn] += q;
+          dVt[c] += q;
+          dVt[c - nn + 1] += q;
+          dVt[c + 1] += q;
+        } else if (ring(i, j)) {
+          if (dRu) (*dRu)[c] += lu[c];
+        } else if (dNu) {
+          (*dNu)[c] += lu[c];
+        }
+        if (vadv(i, j)) {
+          T x = (T)i * h + h2 - sdt * f.avgU(Ut, i, j);
+          T y = (T)j * h - sdt * Vt[c];
+          T gx, gy;
+          sample_adj(x, y, Fv, dFv, 1, lv[c], &gx, &gy);
+          dVt[c] += -sdt * gy * lv[c];
+          T q = (T)0.25 * (-sdt * gx * lv[c]);
+          dUt[c - 1] += q;
+          dUt[c] += q;
+          dUt[c + nn - 1] += q;
+          dUt[c + nn] += q;
+        } else if (ring(i, j)) {
+          if (dRv) (*dRv)[c] += lv[c];
+        } else if (dNv) {
+          (*dNv)[c] += lv[c];
+        }
+      }
+  }
+
+  // Offset of the neighbour that bounded val in clampToNeighbors' scan, or
+  // INT_MIN when val was inside the range.
+  int clamp_src(T val, const std::vector<T>& O, int i, int j) const {
+    const int nn = n();
+    T lo = O[i * nn + j], hi = lo;
+    int klo = 0, khi = 0;
+    for (int di = -1; di <= 1; ++di)
+      for (int dj = -1; dj <= 1; ++dj) {
+        T v = O[(i + di) * nn + j + dj];
+        if (v < lo) {
+          lo = v;
+          klo = di * nn + dj;
+        }
+        if (v > hi) {
+          hi = v;
+          khi = di * nn + dj;
+        }
+      }
+    if (val < lo) return klo;
+    if (val > hi) return khi;
+    return INT32_MIN;
+  }
+
+  // Adjoint of a semi-Lagrangian smoke pass traced with (U, V) at sdt; bwd:
+  // BFECC's reverse sample (no max, non-fluid cells constant 0).
+  void sl_smoke_adj(const std::vector<T>& lam, const std::vector<T>& U, const std::vector<T>& V,
+                    const std::vector<T>& Ms, std::vector<T>& dU, std::vector<T>& dV,
+                    std::vector<T>& dMs, std::vector<T>* dN, T sdt, bool bwd) const {
+    const int nn = n();
+    const T h = f.h, h2 = (T)0.5 * h, sa = f.SmokeAdvection;
+    for (int i = 0; i < f.NX; ++i)
+      for (int j = 0; j < f.NY; ++j) {
+        int c = i * nn + j;
+        T l = lam[c];
+        if (fluid_interior(i, j)) {
+          T u = (U[c] + U[c + nn]) * (T)0.5 * sa;
+          T v = (V[c] + V[c + 1]) * (T)0.5 * sa;
+          T x = (T)i * h + h2 - sdt * u;
+          T y = (T)j * h + h2 - sdt * v;
+          if (!bwd && !(f.sampleFrom(x, y, Ms, 2) >= 0)) l = 0;
+          T gx, gy;
+          sample_adj(x, y, Ms, dMs, 2, l, &gx, &gy);
+          T du = -sdt * gx * l * (T)0.5 * sa, dv = -sdt * gy * l * (T)0.5 * sa;
+          dU[c] += du;
+          dU[c + nn] += du;
+          dV[c] += dv;
+          dV[c + 1] += dv;
+        } else if (!bwd) {
+          if (ring(i, j))
+            dMs[c] += l;
+          else if (dN)
+            (*dN)[c] += l;
+        }
+      }
+  }
+
+  void adjoint_step(int k, std::vector<T>* dfu, std::vector<T>* dfv) {
+    const Rec& r = recs[k];
+    const T dt = dts[k];
+    const int N = f.N, nn = n(), NX = f.NX, NY = f.NY;
+    std::vector<T> dU5(N), dV5(N), dM2(N);
+    for (int c = 0; c < N; ++c) {
+      dU5[c] = aU[c] + aNU[c];
+      dV5[c] = aV[c] + aNV[c];
+      dM2[c] = aM[c] + aNM[c];
+    }
+    std::fill(aNU.begin(), aNU.end(), (T)0);
+    std::fill(aNV.begin(), aNV.end(), (T)0);
+    std::fill(aNM.begin(), aNM.end(), (T)0);
+    // ---- smoke
+    std::vector<T> dM1(N, 0);
+    if (f.UseBFECC) {
+      const std::vector<T>&fwdM = r.km[0], &corrM = r.km[1];
+      std::vector<T> dcorr(N, 0), dfwd(N, 0);
+      sl_smoke_adj(dM2, r.U5, r.V5, corrM, dU5, dV5, dcorr, &aNM, dt, false);
+      for (int i = 1; i < NX - 1; ++i)
+        for (int j = 1; j < NY - 1; ++j) {
+          int c = i * nn + j;
+          T lam = dcorr[c];
+          bool adv = f.S[c] != 0;
+          T b = 0, x = 0, y = 0;
+          if (adv) {
+            T u = (r.U5[c] + r.U5[c + nn]) * (T)0.5 * f.SmokeAdvection;
+            T v = (r.V5[c] + r.V5[c + 1]) * (T)0.5 * f.SmokeAdvection;
+            x = (T)i * f.h + (T)0.5 * f.h + dt * u;
+            y = (T)j * f.h + (T)0.5 * f.h + dt * v;
+            b = f.sampleFrom(x, y, fwdM, 2);
+          }
+          T o = r.M1[c];
+          T raw = o - (b - o) * (T)0.5;
+          int sk = clamp_src(raw, r.M1, i, j);
+          T cm = sk != INT32_MIN ? r.M1[c + sk] : raw;
+          if (cm < 0) continue;
+          if (sk != INT32_MIN) {
+            dM1[c + sk] += lam;
+            continue;
+          }
+          dM1[c] += (T)1.5 * lam;
+          if (!adv) continue;
+          T lb = (T)-0.5 * lam, gx, gy;
+          sample_adj(x, y, fwdM, dfwd, 2, lb, &gx, &gy);
+          T du = dt * gx * lb * (T)0.5 * f.SmokeAdvection;
+          T dv = dt * gy * lb * (T)0.5 * f.SmokeAdvection;
+          dU5[c] += du;
+          dU5[c + nn] += du;
+          dV5[c] += dv;
+          dV5[c + 1] += dv;
+        }
+      for (int i = 0; i < NX; ++i)
+        for (int j = 0; j < NY; ++j)
+          if (ring(i, j)) dM1[i * nn + j] += dcorr[i * nn + j];
+      sl_smoke_adj(dfwd, r.U5, r.V5, r.M1, dU5, dV5, dM1, &aNM, dt, false);
+    } else {
+      sl_smoke_adj(dM2, r.U5, r.V5, r.M1, dU5, dV5, dM1, &aNM, dt, false);
+    }
+    // ---- velocity
+    std::vector<T> dU(N, 0), dV(N, 0);  // dU4, dV4
+    if (f.UseBFECC) {
+      const std::vector<T>&fwdU = r.k[0], &fwdV = r.k[1], &corrU = r.k[2], &corrV = r.k[3];
+      std::vector<T> dcU(N, 0), dcV(N, 0), dfU(N, 0), dfV(N, 0);
+      sl_vel_adj(dU5, dV5, corrU, corrV, corrU, corrV, dcU, dcV, dcU, dcV, &dcU, &dcV, &aNU, &aNV,
+                 dt);
+      for (int i = 0; i < NX; ++i)
+        for (int j = 0; j < NY; ++j) {
+          int c = i * nn + j;
+          if (ring(i, j)) {
+            dU[c] += dcU[c];
+            dV[c] += dcV[c];
+            continue;
+          }
+          for (int comp = 0; comp < 2; ++comp) {
+            const std::vector<T>& O = comp == 0 ? r.U4 : r.V4;
+            const std::vector<T>& F = comp == 0 ? fwdU : fwdV;
+            std::vector<T>& dO = comp == 0 ? dU : dV;
+            T lam = comp == 0 ? dcU[c] : dcV[c];
+            bool adv = comp == 0 ? uadv(i, j) : vadv(i, j);
+            T b = 0, x = 0, y = 0;
+            if (adv) {
+              if (comp == 0) {
+                x = (T)i * f.h + dt * r.U4[c];
+                y = (T)j * f.h + f.h / (T)2 + dt * f.avgV(r.V4, i, j);
+              } else {
+                x = (T)i * f.h + f.h / (T)2 + dt * f.avgU(r.U4, i, j);
+                y = (T)j * f.h + dt * r.V4[c];
+              }
+              b = f.sampleFrom(x, y, F, comp);
+            }
+            T o = O[c];
+            T raw = o - (b - o) * (T)0.5;
+            int sk = clamp_src(raw, O, i, j);
+            if (sk != INT32_MIN) {
+              dO[c + sk] += lam;
+              continue;
+            }
+            dO[c] += (T)1.5 * lam;
+            if (!adv) continue;
+            T lb = (T)-0.5 * lam, gx, gy;
+            sample_adj(x, y, F, comp == 0 ? dfU : dfV, comp, lb, &gx, &gy);
+            T du = dt * gx * lb, dv = dt * gy * lb;
+            if (comp == 0) {
+              dU[c] += du;
+              T q = (T)0.25 * dv;
+              dV[c - nn] += q;
+              dV[c] += q;
+              dV[c - nn + 1] += q;
+              dV[c + 1] += q;
+            } else {
+              dV[c] += dv;
+              T q = (T)0.25 * du;
+              dU[c - 1] += q;
+              dU[c] += q;
+              dU[c + nn - 1] += q;
+              dU[c + nn] += q;
+            }
+          }
+        }
+      sl_vel_adj(dfU, dfV, r.U4, r.V4, r.U4, r.V4, dU, dV, dU, dV, &dU, &dV, &aNU, &aNV, dt);
+    } else {
+      sl_vel_adj(dU5, dV5, r.U4, r.V4, r.U4, r.V4, dU, dV, dU, dV, &dU, &dV, &aNU, &aNV, dt);
+    }
+    // ---- borders (fluid.go:236-289), reversed: the last write first
+    auto fl = [&](int i, int j) { return f.S[i * nn + j] != 0; };
+    for (int i = 0; i < NX; ++i) {
+      T* d = &dU[i * nn];
+      T l = d[NY - 1];
+      d[NY - 1] = 0;
+      if (fl(i, NY - 1) && fl(i, NY - 2)) {
+        if (i > 0 && i < NX - 1 && fl(i, NY - 3)) {
+          d[NY - 2] += 2 * l;
+          d[NY - 3] -= l;
+        } else {
+          d[NY - 2] += l;
+        }
+      }
+      l = d[0];
+      d[0] = 0;
+      if (fl(i, 0) && fl(i, 1)) {
+        if (i > 0 && i < NX - 1 && fl(i, 2)) {
+          d[1] += 2 * l;
+          d[2] -= l;
+        } else {
+          d[1] += l;
+        }
+      }
+    }
+    for (int j = 0; j < NY; ++j) {
+      int a = (NX - 1) * nn + j, b = (NX - 2) * nn + j, c3 = (NX - 3) * nn + j;
+      T l = dV[a];
+      dV[a] = 0;
+      if (fl(NX - 1, j) && fl(NX - 2, j)) {
+        if (j > 0 && j < NY - 1 && fl(NX - 3, j)) {
+          dV[b] += 2 * l;
+          dV[c3] -= l;
+        } else {
+          dV[b] += l;
+        }
+      }
+      l = dV[j];
+      dV[j] = 0;
+      if (fl(0, j) && fl(1, j)) {
+        if (j > 0 && j < NY - 1 && fl(2, j)) {
+          dV[nn + j] += 2 * l;
+          dV[2 * nn + j] -= l;
+        } else {
+          dV[nn + j] += l;
+        }
+      }
+    }
+    // ---- confinement (fluid.go:449-493) and turbulence (fluid.go:496-526)
+    std::vector<T> Uc = r.U2, Vc = r.V2;  // after confinement
+    std::vector<T> curl(N, 0);
+    const T h = f.h;
+    if (f.Confinement != 0) {
+      std::swap(f.U, Uc);
+      std::swap(f.V, Vc);
+      f.applyVorticityConfinement(dt);
+      std::swap(f.U, Uc);
+      std::swap(f.V, Vc);
+      for (int i = 1; i < NX - 1; ++i)
+        for (int j = 1; j < NY - 1; ++j)
+          if (f.S[i * nn + j] != 0)
+            curl[i * nn + j] = (r.V2[(i + 1) * nn + j] - r.V2[(i - 1) * nn + j]) * (T)0.5 / h -
+                               (r.U2[i * nn + j + 1] - r.U2[i * nn + j - 1]) * (T)0.5 / h;
+    }
+    if (f.TurbulenceStrength > 0) {
+      T ts = f.TurbulenceStrength * dt;
+      for (int i = 1; i < NX - 1; ++i)
+        for (int j = 1; j < NY - 1; ++j) {
+          int c = i * nn + j;
+          if (f.S[c] == 0) continue;
+          T u = Uc[c], v = Vc[c];
+          T rr = go_sqrt(u * u + v * v);
+          if (!(rr > (T)0.1) || !((T)0.5 * rr < 1)) continue;
+          T seedU = (T)(i * 137 + j * 241) * (T)0.01;
+          T seedV = (T)(i * 157 + j * 263) * (T)0.01;
+          T nU = (T)std::sin((double)seedU) * ts, nV = (T)std::sin((double)seedV) * ts;
+          T sc = (dU[c] * nU + dV[c] * nV) * (T)0.5;
+          dU[c] += sc * u / rr;
+          dV[c] += sc * v / rr;
+        }
+    }
+    if (f.Confinement != 0) {
+      const T conf = f.Confinement, eps = (T)1e-5, k2 = (T)0.5 / h;
+      std::vector<T> lwd(N, 0), lgx(N, 0), lgy(N, 0);
+      for (int i = 1; i < NX - 1; ++i)
+        for (int j = 1; j < NY - 1; ++j) {
+          int c = i * nn + j;
+          if (f.S[c] == 0) continue;
+          T gx = (go_abs(curl[c + nn]) - go_abs(curl[c - nn])) * (T)0.5 / h;
+          T gy = (go_abs(curl[c + 1]) - go_abs(curl[c - 1])) * (T)0.5 / h;
+          T rg = go_sqrt(gx * gx + gy * gy), m = rg + eps;
+          T nx = gx / m, ny = gy / m, w = curl[c];
+          T u = r.U2[c], v = r.V2[c], rr = go_sqrt(u * u + v * v);
+          T K = conf * ((T)1.0 + rr * (T)0.1);
+          T a = dU[c] * dt, b = -dV[c] * dt;
+          T Sm = a * ny + b * nx;
+          if (rr > 0) {
+            dU[c] += w * Sm * conf * (T)0.1 * u / rr;
+            dV[c] += w * Sm * conf * (T)0.1 * v / rr;
+          }
+          lwd[c] = K * Sm;
+          T Lnx = K * w * b, Lny = K * w * a;
+          T qx = Lnx / m, qy = Lny / m;
+          if (rg > 0) {
+            T t = (Lnx * gx + Lny * gy) / (rg * m * m);
+            qx -= t * gx;
+            qy -= t * gy;
+          }
+          lgx[c] = qx;
+          lgy[c] = qy;
+        }
+      std::vector<T> lw(N, 0);
+      for (int i = 1; i < NX - 1; ++i)
+        for (int j = 1; j < NY - 1; ++j) {
+          int c = i * nn + j;
+          if (f.S[c] == 0) continue;
+          T w = curl[c];
+          T sg = w > 0 ? (T)1 : (w < 0 ? (T)-1 : (T)0);
+          lw[c] = lwd[c] + sg * k2 * ((lgx[c - nn] - lgx[c + nn]) + (lgy[c - 1] - lgy[c + 1]));
+        }
+      for (int i = 1; i < NX - 1; ++i)
+        for (int j = 1; j < NY - 1; ++j) {
+          int c = i * nn + j;
+          T l = lw[c] * k2;
+          if (l == 0) continue;
+          dV[c + nn] += l;
+          dV[c - nn] -= l;
+          dU[c + 1] -= l;
+          dU[c - 1] += l;
+        }
+    }
+    // ---- projection: dU1 = dU2 + div^T P_K G^T dU2 (P_K symmetric)
+    {
+      std::vector<T> g(N, 0), bw(N, 0), x(N, 0), tmp(N, 0);
+      for (int c = 0; c < N; ++c)
+        if (f.cnt[c]) {
+          g[c] = f.S[c + nn] * dU[c + nn] - f.S[c - nn] * dU[c] + f.S[c + 1] * dV[c + 1] -
+                 f.S[c - 1] * dV[c];
+          bw[c] = f.Wc[c] * g[c];
+        }
+      T keep = f.st.last_maxdiv;
+      f.relax(g, bw, x, tmp, f.num_iters, false);
+      f.st.last_maxdiv = keep;
+      for (int i = 1; i < NX; ++i)
+        for (int j = 0; j < NY; ++j) {
+          int c = i * nn + j;
+          dU[c] += x[c] - x[c - nn];
+        }
+      for (int i = 0; i < NX; ++i)
+        for (int j = 1; j < NY; ++j) {
+          int c = i * nn + j;
+          dV[c] += x[c] - x[c - 1];
+        }
+    }
+    // ---- sources, forces
+    for (const Source& s : src) {
+      int c = s.i * nn + s.j;
+      if ((s.mode & 1) && f.S[c] == 0) continue;
+      if (s.mode & 2) dU[c] = dV[c] = 0;
+      if (s.mode & 8) dM1[c] = 0;
+    }
+    if (dfu) *dfu = dU;
+    if (dfv) *dfv = dV;
+    aU = dU;
+    aV = dV;
+    aM = dM1;
   }
 };
 
@@ -1324,5 +1853,60 @@ int orc_stats(void* p, double* out) {
   });
 }
 int orc_threads(void* p) { return ((Handle*)p)->pool->size(); }
+
+// Recorded rollout of `steps` steps from the handle's state (FP64 handles
+// only) with per-step forces (steps x 2 x N, NULL = none) and n_src sources
+// applied before every step; loss L = ||M - target||_2 over interior cells
+// and its reverse pass.  Outputs dL/d(initial U, V, M) and dL/d(forces)
+// (steps x 2 x N, may be NULL).  The handle ends at the end of the rollout.
+int orc_rollout_grad(void* p, int steps, double dt, const double* forces, int n_src,
+                     const int* si, const int* sj, const double* su, const double* sv,
+                     const double* ssmoke, const int* smode, const double* target, double* loss,
+                     double* dU, double* dV, double* dM, double* dF) {
+  Handle* hd = (Handle*)p;
+  if (hd->prec != 64 || steps < 1) return -1;
+  orc::Fluid<double>& f = *hd->f64;
+  if (f.scheme != orc::Jacobi || f.early_exit || f.refine_sweeps > 0 ||
+      f.ViscosityDiffusion > 0)
+    return -4;
+  orc::Rollout<double> r(f);
+  for (int k = 0; k < n_src; ++k)
+    r.src.push_back(orc::Source{si[k], sj[k], su[k], sv[k], ssmoke[k], smode[k]});
+  const int N = f.N;
+  for (int t = 0; t < steps; ++t)
+    r.step(dt, forces ? forces + (size_t)t * 2 * N : nullptr,
+           forces ? forces + (size_t)t * 2 * N + N : nullptr);
+  double L2 = 0;
+  for (int i = 1; i < f.NX - 1; ++i)
+    for (int j = 1; j < f.NY - 1; ++j) {
+      double d = f.M[i * f.NY + j] - target[i * f.NY + j];
+      L2 += d * d;
+    }
+  double L = std::sqrt(L2);
+  *loss = L;
+  r.aU.assign(N, 0);
+  r.aV.assign(N, 0);
+  r.aM.assign(N, 0);
+  r.aNU.assign(N, 0);
+  r.aNV.assign(N, 0);
+  r.aNM.assign(N, 0);
+  for (int i = 1; i < f.NX - 1; ++i)
+    for (int j = 1; j < f.NY - 1; ++j) {
+      int c = i * f.NY + j;
+      r.aM[c] = L > 0 ? (f.M[c] - target[c]) / L : 0;
+    }
+  std::vector<double> gu, gv;
+  for (int t = steps - 1; t >= 0; --t) {
+    r.adjoint_step(t, &gu, &gv);
+    if (dF) {
+      std::copy(gu.begin(), gu.end(), dF + (size_t)t * 2 * N);
+      std::copy(gv.begin(), gv.end(), dF + (size_t)t * 2 * N + N);
+    }
+  }
+  if (dU) std::copy(r.aU.begin(), r.aU.end(), dU);
+  if (dV) std::copy(r.aV.begin(), r.aV.end(), dV);
+  if (dM) std::copy(r.aM.begin(), r.aM.end(), dM);
+  return 0;
+}
 
 }  // extern "C"

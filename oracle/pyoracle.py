@@ -66,6 +66,8 @@ def lib():
                 "orc_sample_velocity": (i, [vp, d, d, ctypes.POINTER(d)]),
                 "orc_stats": (i, [vp, ctypes.POINTER(d)]),
                 "orc_threads": (i, [vp]),
+                "orc_rollout_grad": (i, [vp, i, d, vp, i, vp, vp, vp, vp, vp, vp, vp,
+                                         ctypes.POINTER(d), vp, vp, vp, vp]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(L, name)
@@ -292,3 +294,33 @@ class OracleFluid:
         keys = ("div_l2_post", "div_max_post", "div_count_post", "resid_l2", "resid_max",
                 "smoke_mass", "sweeps", "last_maxdiv")
         return dict(zip(keys, list(out)))
+
+    def rollout_grad(self, dt, steps, target, forces=None, sources=()):
+        """FP64 reverse-mode reference of a recorded rollout (prec=64 only):
+        `steps` steps with per-step forces (steps x 2 x N array or None) and
+        sources [(i, j, u, v, smoke, mode)] applied before every step, loss
+        ||M - target||_2 over the interior.  Returns {"loss", "U", "V", "M",
+        "force_u", "force_v"}; the oracle ends at the end of the rollout."""
+        n = self.NumX * self.NumY
+        tgt = np.ascontiguousarray(target, np.float64)
+        fr = None if forces is None else np.ascontiguousarray(forces, np.float64)
+        src = list(sources)
+        si = np.array([s[0] for s in src] or [0], np.int32)
+        sj = np.array([s[1] for s in src] or [0], np.int32)
+        su = np.array([s[2] for s in src] or [0], np.float64)
+        sv = np.array([s[3] for s in src] or [0], np.float64)
+        ss = np.array([s[4] for s in src] or [0], np.float64)
+        sm = np.array([s[5] for s in src] or [0], np.int32)
+        out = [np.zeros(n) for _ in range(3)]
+        dF = np.zeros((steps, 2, n))
+        loss = ctypes.c_double()
+        rc = self._lib.orc_rollout_grad(self._h, int(steps), float(dt),
+                                      None if fr is None else fr.ctypes.data, len(src),
+                                      si.ctypes.data, sj.ctypes.data, su.ctypes.data,
+                                      sv.ctypes.data, ss.ctypes.data, sm.ctypes.data,
+                                      tgt.ctypes.data, ctypes.byref(loss), out[0].ctypes.data,
+                                      out[1].ctypes.data, out[2].ctypes.data, dF.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("orc_rollout_grad failed (%d)" % rc)
+        return {"loss": loss.value, "U": out[0], "V": out[1], "M": out[2],
+                "force_u": dF[:, 0], "force_v": dF[:, 1]}

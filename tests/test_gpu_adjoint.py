@@ -493,3 +493,38 @@ def test_rollout256_fp32_central_differences_32_directions(gpu, rollout256):
     print("rollout256: loss %.6g  |dL/dU0| %.4g  median rel err %.3g  max %.3g"
           % (out["loss"], float(np.linalg.norm(out["U"])), np.median(rel), rel.max()))
     assert np.median(rel) < 5e-2
+
+
+# ------------------------------------------------------------------ 64^2 vs the FP64 reverse mode
+def test_rollout64_gradient_fields_vs_fp64_reference_adjoint(gpu):
+    """64^2 jet, 64 steps, BFECC, 60 sweeps, checkpoint every 8: every
+    gradient field (initial U, V, M and all 64 x 2 force fields) against the
+    oracle's FP64 reverse mode of the same rollout.  The GPU trajectory is
+    FP32, so the fields agree to FP32 accuracy, not bit for bit."""
+    side, steps = 64, 64
+    f = gpu.Fluid(1.0, side, side, 1.0, auto_sync=False, scheme=1, num_iters=R_ITERS,
+                  tb_depth=8, early_exit=False, UseBFECC=True)
+    scenes.jet_rollout_scene(f)
+    n = f.numCells
+    target = scenes.gaussian_target(f.NumX, f.NumY, seed=4, sigma=(2.5, 7.5))
+    rng = np.random.default_rng(64)
+    forces = [(rng.uniform(-0.02, 0.02, n).astype(np.float32),
+               rng.uniform(-0.02, 0.02, n).astype(np.float32)) for _ in range(steps)]
+    out = f.rollout_grad(DT, steps, target, forces, every=R_EVERY)
+    f.download()
+    o = OracleFluid(1.0, side, side, 1.0, prec=64, scheme=1, num_iters=R_ITERS, check_every=8,
+                    early_exit=False, UseBFECC=True)
+    o.S[:] = f.S
+    srcs = [(1, j, 2.0, 0.0, 1.0, 1 | 2 | 8) for j in scenes.jet_rows(o)]
+    F = np.stack([np.stack([a, b]) for a, b in forces]).astype(np.float64)
+    ref = o.rollout_grad(DT, steps, target.astype(np.float64), F, srcs)
+    assert out["loss"] == pytest.approx(ref["loss"], rel=1e-5)
+    errs = {}
+    for k in ("U", "V", "M"):
+        errs[k] = float(np.linalg.norm(out[k] - ref[k]) / np.linalg.norm(ref[k]))
+    gf = np.stack([np.stack([a, b]) for a, b in zip(out["force_u"], out["force_v"])])
+    rf = np.stack([ref["force_u"], ref["force_v"]], axis=1)
+    errs["forces"] = float(np.linalg.norm(gf - rf) / np.linalg.norm(rf))
+    print("rollout64 relative L2 error of the gradient fields vs FP64 reverse mode:", errs)
+    for k, e in errs.items():
+        assert e < 1e-3, (k, e)
