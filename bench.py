@@ -184,6 +184,24 @@ def lid_cells(f):
     return i, j
 
 
+def profile_leg(args, name):
+    """With --profile-leg NAME, brackets that leg's timed region with
+    cudaProfilerStart/Stop (for ncu --profile-from-start off); returns the
+    closing call."""
+    import torch
+
+    if getattr(args, "profile_leg", None) != name:
+        return lambda: None
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+
+    def stop():
+        torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
+
+    return stop
+
+
 def fwd_adjoint(fluid_gb300, args):
     """Forward + adjoint rollout on the cavity (refine_sweeps 0, the recorded
     rollouts' form): ROLL steps with a device-resident per-step force field,
@@ -235,11 +253,13 @@ def fwd_adjoint(fluid_gb300, args):
     rollout()
     f.synchronize()
     reps = max(1, min(3, args.steps // 8))
+    prof = profile_leg(args, "adjoint")
     e0.record(stream)
     for _ in range(reps):
         loss = rollout()
     e1.record(stream)
     f.synchronize()
+    prof()
     ms_roll = e0.elapsed_time(e1) / (reps * roll)
     l0 = f.launch_count()
     e0.record(stream)
@@ -402,11 +422,13 @@ def ensemble(fluid_gb300, args, n=256, steps=20, roll=16, every=8):
         batch.step(DT)
     batch.synchronize()
     l0 = batch.launch_count()
+    prof = profile_leg(args, "ensemble")
     e0.record(stream)
     for _ in range(steps):
         batch.step(DT)
     e1.record(stream)
     batch.synchronize()
+    prof()
     ms_b = e0.elapsed_time(e1) / steps
     launches_b = (batch.launch_count() - l0) / steps
 
@@ -618,7 +640,8 @@ def run_ours(args):
         del g
 
     adj = fwd_adjoint(fluid_gb300, args) if rank == 0 and not args.no_adjoint else None
-    roll = rollout256(fluid_gb300, args) if rank == 0 and not args.no_adjoint else None
+    roll = (rollout256(fluid_gb300, args)
+            if rank == 0 and not (args.no_adjoint or args.no_rollout) else None)
     ens = ensemble(fluid_gb300, args) if rank == 0 and not args.no_ensemble else None
 
     # ------------------------------------------------------------ CPU baseline
@@ -661,6 +684,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-rollout", action="store_true")
+    ap.add_argument("--profile-leg", choices=["adjoint", "ensemble"], default=None,
+                    help="bracket that leg's timed region for ncu --profile-from-start off")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -1058,6 +1058,18 @@ struct Tape {
   float* ckpt = nullptr;    // cap_ckpt x {U, V, M, newU, newV, newM}; slot n_ckpt: the final state
   float* rec = nullptr;     // cap_every x kTapeFields
   float* aux = nullptr;     // loss target
+  // CUDA graphs of recorded, replayed and adjoint steps (see run_graphed).
+  struct Graph {
+    int kind;
+    uint32_t dt_bits;
+    uint64_t version;
+    const void* ptrs[4];
+    float* pre[6 + fg_fluid::A_COUNT];
+    float* post[6 + fg_fluid::A_COUNT];
+    unsigned long long launches;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;
 };
 
 namespace {
@@ -1066,9 +1078,15 @@ constexpr int kStateFields[6] = {FG_U, FG_V, FG_M, FG_NEWU, FG_NEWV, FG_NEWM};
 
 size_t field_elems(const fg_fluid* f) { return (size_t)f->NX * f->P; }
 
+void tape_clear_graphs(Tape* t) {
+  for (auto& g : t->graphs) cudaGraphExecDestroy(g.exec);
+  t->graphs.clear();
+}
+
 void tape_free(fg_fluid* f) {
   if (!f->tape) return;
   cudaStreamSynchronize(f->stream);
+  tape_clear_graphs(f->tape);
   cudaFree(f->tape->forces);
   cudaFree(f->tape->phis);
   cudaFree(f->tape->ckpt);
@@ -1128,8 +1146,9 @@ int get_field(fg_fluid* f, float* dst, const float* dev) {
 }
 
 // One recorded step: Simulate (fluid.go:79-109) with the force field added
-// to U, V before the sources, confinement / turbulence run as their own
-// pass, and the intermediates the adjoint reads written to `rec`
+// to U, V before the sources (`fu`, `fv` already zero where the sources set
+// U, V), confinement / turbulence run as their own pass, and the
+// intermediates the adjoint reads written to `rec`
 // (kTapeFields fields: U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM
 // corrM).  The BFECC
 // intermediates are produced in place: the scratch pointers are redirected
@@ -1142,15 +1161,23 @@ int enqueue_step_record(fg_fluid* f, float dt, const float* fu, const float* fv,
   const size_t n = field_elems(f);
   auto R = [&](int k) { return rec + (size_t)k * n; };
   int rc;
-  if (fu) CK(f, launch_add_forces(f, fu, fv), "forces");
   CK(f, launch_apply_sources(f), "sources");
+  // The forces (zero where the sources set U, V) are added by the pressure
+  // setup and the gradient kernel as they read U, V: U1 = sources(U0 + F).
+  f->step_fu = fu;
+  f->step_fv = fv;
+  cudaError_t ep = cudaSuccess;
+  rc = FG_OK;
   if (replay) {
-    CK(f, launch_grad_replay(f, dt, phi), "gradient replay");
+    ep = launch_grad_replay(f, dt, phi);
   } else {
-    CK(f, launch_clear_stats(f), "clear stats");
-    if ((rc = enqueue_pressure(f, p.num_iters, dt, false))) return rc;
-    CK(f, launch_store_phi(f, phi), "store potential");
+    ep = launch_clear_stats(f);
+    if (ep == cudaSuccess) rc = enqueue_pressure(f, p.num_iters, dt, false);
+    if (ep == cudaSuccess && !rc) ep = launch_store_phi(f, phi);
   }
+  f->step_fu = f->step_fv = nullptr;
+  if (rc) return rc;
+  if (ep != cudaSuccess) return fail(f, FG_ERR_CUDA, "pressure", ep);
   const bool conf = p.confinement != 0.0f, turb = p.turbulence_strength > 0.0f;
   if (conf || turb) {
     if ((rc = copy_field(f, R(0), f->d[FG_U])) || (rc = copy_field(f, R(1), f->d[FG_V]))) return rc;
@@ -1201,6 +1228,83 @@ float* force_at(fg_fluid* f, int t, int c) {
 }
 float* phi_at(fg_fluid* f, int t) { return f->tape->phis + (size_t)t * field_elems(f); }
 
+// The pointers a captured step bakes in and may rotate: the state and its
+// rotation partners, and the adjoint fields.
+constexpr int kSnap = 6 + fg_fluid::A_COUNT;
+void snap_ptrs(const fg_fluid* f, float** out) {
+  out[0] = f->d[FG_U];
+  out[1] = f->d[FG_V];
+  out[2] = f->d[FG_M];
+  out[3] = f->partner[FG_U];
+  out[4] = f->partner[FG_V];
+  out[5] = f->partner[FG_M];
+  for (int k = 0; k < fg_fluid::A_COUNT; ++k) out[6 + k] = f->adj[k];
+}
+void set_ptrs(fg_fluid* f, float* const* in) {
+  f->d[FG_U] = in[0];
+  f->d[FG_V] = in[1];
+  f->d[FG_M] = in[2];
+  f->partner[FG_U] = in[3];
+  f->partner[FG_V] = in[4];
+  f->partner[FG_M] = in[5];
+  for (int k = 0; k < fg_fluid::A_COUNT; ++k) f->adj[k] = in[6 + k];
+}
+
+// Runs enqueue() as a CUDA graph: replays the graph captured for the same
+// kind, dt, parameters, tape pointers (ptrs) and rotation state, or captures
+// a new one.  The tape buffers persist across rollouts, so a training loop
+// captures each step once.  Profiling or use_graphs = 0 run it uncaptured.
+template <class Fn>
+int run_graphed(fg_fluid* f, int kind, float dt, const void* const* ptrs, Fn&& enqueue) {
+  Tape* t = f->tape;
+  if (!f->prm.use_graphs || f->profile) return enqueue();
+  float* pre[kSnap];
+  snap_ptrs(f, pre);
+  uint32_t dtb;
+  memcpy(&dtb, &dt, 4);
+  for (auto& g : t->graphs) {
+    if (g.kind == kind && g.dt_bits == dtb && g.version == f->params_version &&
+        memcmp(g.ptrs, ptrs, sizeof g.ptrs) == 0 && memcmp(g.pre, pre, sizeof pre) == 0) {
+      CK(f, cudaGraphLaunch(g.exec, f->stream), "graph launch");
+      f->launches += g.launches;
+      set_ptrs(f, g.post);
+      return FG_OK;
+    }
+  }
+  if (t->graphs.size() >= (size_t)(4 * t->cap_steps + 64)) tape_clear_graphs(t);
+  Tape::Graph ent;
+  ent.kind = kind;
+  ent.dt_bits = dtb;
+  ent.version = f->params_version;
+  memcpy(ent.ptrs, ptrs, sizeof ent.ptrs);
+  memcpy(ent.pre, pre, sizeof pre);
+  CK(f, cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  unsigned long long before = f->launches;
+  int rc = enqueue();
+  ent.launches = f->launches - before;
+  f->launches = before;
+  cudaGraph_t graph = nullptr;
+  cudaError_t ec = cudaStreamEndCapture(f->stream, &graph);
+  if (rc || ec != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    set_ptrs(f, pre);  // nothing ran
+    return rc ? rc : fail(f, FG_ERR_CUDA, "end capture", ec);
+  }
+  snap_ptrs(f, ent.post);
+  ec = cudaGraphInstantiate(&ent.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ec != cudaSuccess) {
+    set_ptrs(f, pre);
+    return fail(f, FG_ERR_CUDA, "graph instantiate", ec);
+  }
+  t->graphs.push_back(ent);
+  CK(f, cudaGraphLaunch(ent.exec, f->stream), "graph launch");
+  f->launches += ent.launches;
+  return FG_OK;
+}
+
+enum { kGraphForward = 1, kGraphReplay = 2, kGraphAdjoint = 3 };
+
 // Recomputes the steps of interval s from its checkpoint, recording them.
 int tape_load_interval(fg_fluid* f, int s) {
   Tape* t = f->tape;
@@ -1209,9 +1313,14 @@ int tape_load_interval(fg_fluid* f, int s) {
   int t1 = std::min((s + 1) * t->every, t->n_fwd);
   for (int k = s * t->every; k < t1; ++k) {
     bool hf = t->has_force[k] != 0;
-    rc = enqueue_step_record(f, t->dts[k], hf ? force_at(f, k, 0) : nullptr,
-                             hf ? force_at(f, k, 1) : nullptr, rec_at(f, k - s * t->every),
-                             phi_at(f, k), true);
+    const float* fu = hf ? force_at(f, k, 0) : nullptr;
+    const float* fv = hf ? force_at(f, k, 1) : nullptr;
+    float* rec = rec_at(f, k - s * t->every);
+    float* phi = phi_at(f, k);
+    const void* ptrs[4] = {rec, phi, fu, fv};
+    rc = run_graphed(f, kGraphReplay, t->dts[k], ptrs, [&] {
+      return enqueue_step_record(f, t->dts[k], fu, fv, rec, phi, true);
+    });
     if (rc) return rc;
   }
   t->seg_loaded = s;
@@ -1258,6 +1367,7 @@ int fg_tape_begin(fg_fluid* f, int max_steps, int every) {
     CK(f, cudaMemsetAsync(t->rec, 0, fb * kTapeFields * every, f->stream), "tape");
     CK(f, cudaMemsetAsync(t->aux, 0, fb, f->stream), "tape");
   }
+  if (t->version != f->params_version) tape_clear_graphs(t);
   t->active = true;
   t->max_steps = max_steps;
   t->every = every;
@@ -1303,12 +1413,19 @@ int fg_step_forward(fg_fluid* f, float dt, const float* force_u, const float* fo
     if ((rc = put_field(f, force_at(f, k, 0), force_u)) ||
         (rc = put_field(f, force_at(f, k, 1), force_v)))
       return rc;
+    CK(f, launch_mask_forces(f, force_at(f, k, 0), force_at(f, k, 1)), "forces");
   }
   invalidate(f, kStepFields);
-  rc = enqueue_step_record(f, dt, force_u ? force_at(f, k, 0) : nullptr,
-                           force_u ? force_at(f, k, 1) : nullptr, rec_at(f, k % t->every),
-                           phi_at(f, k), false);
-  if (rc) return rc;
+  {
+    const float* fu = force_u ? force_at(f, k, 0) : nullptr;
+    const float* fv = force_u ? force_at(f, k, 1) : nullptr;
+    float* rec = rec_at(f, k % t->every);
+    float* phi = phi_at(f, k);
+    const void* ptrs[4] = {rec, phi, fu, fv};
+    rc = run_graphed(f, kGraphForward, dt, ptrs,
+                     [&] { return enqueue_step_record(f, dt, fu, fv, rec, phi, false); });
+    if (rc) return rc;
+  }
   t->dts[k] = dt;
   t->has_force[k] = force_u ? 1 : 0;
   t->seg_loaded = k / t->every;
@@ -1377,7 +1494,12 @@ int fg_step_adjoint(fg_fluid* f, float* grad_force_u, float* grad_force_v) {
   float* rec[kTapeFields];
   for (int q = 0; q < kTapeFields; ++q)
     rec[q] = rec_at(f, k - s * t->every) + (size_t)q * field_elems(f);
-  CK(f, launch_step_adjoint(f, t->dts[k], rec), "step adjoint");
+  const void* ptrs[4] = {rec[0], nullptr, nullptr, nullptr};
+  rc = run_graphed(f, kGraphAdjoint, t->dts[k], ptrs, [&] {
+    cudaError_t e = launch_step_adjoint(f, t->dts[k], rec);
+    return e == cudaSuccess ? FG_OK : fail(f, FG_ERR_CUDA, "step adjoint", e);
+  });
+  if (rc) return rc;
   if (grad_force_u && (rc = get_field(f, grad_force_u, f->adj[fg_fluid::A_U]))) return rc;
   if (grad_force_v && (rc = get_field(f, grad_force_v, f->adj[fg_fluid::A_V]))) return rc;
   t->n_rev++;
@@ -1607,7 +1729,7 @@ int fg_batch_create(fg_fluid* const* scenes, int n, fg_fluid** out) {
   if (cudaMalloc(&f->pctl, pctl_bytes(f->n_slots)) != cudaSuccess ||
       cudaMalloc(&f->ectl, pctl_bytes(f->n_slots)) != cudaSuccess ||
       cudaMalloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess ||
-      cudaMalloc((void**)&b->losses, sizeof(double) * n) != cudaSuccess)
+      cudaMalloc((void**)&b->losses, sizeof(double) * 2 * n) != cudaSuccess)
     return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
   cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream);
   cudaMemsetAsync(f->ectl, 0, pctl_bytes(f->n_slots), f->stream);

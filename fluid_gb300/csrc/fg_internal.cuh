@@ -155,7 +155,7 @@ struct BatchGeom {
   int n_jac_tiles = 0;
   int max_iters = 0;
   int* src_scene = nullptr;  // device: scene of each source group
-  double* losses = nullptr;  // device: per-scene loss of the last seed
+  double* losses = nullptr;  // device: per-scene loss of the last seed, then n floats 1 / L
 };
 
 }  // namespace fg
@@ -217,6 +217,10 @@ struct fg_fluid {
          A_COUNT };
   float* adj[A_COUNT] = {};
   struct Tape* tape = nullptr;
+  // The force field of the recorded step being enqueued (added to U, V by
+  // the pressure setup and the gradient kernel), null otherwise.
+  const float* step_fu = nullptr;
+  const float* step_fv = nullptr;
   // Non-null when this handle is a batch of scenes (fg_batch_create).
   fg::BatchGeom* batch = nullptr;
   // Kernel launches enqueued so far (graph replays add the captured count).
@@ -280,6 +284,9 @@ cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi);
 // k_adjoint.cu
 constexpr int kTapeFields = 13;  // U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM corrM
 cudaError_t launch_add_forces(fg_fluid* f, const float* fu, const float* fv);
+// Zeroes a force field on the cells whose velocity the sources set (they
+// overwrite the forced value), so the forces can be added after them.
+cudaError_t launch_mask_forces(fg_fluid* f, float* fu, float* fv);
 // Adjoint of one recorded step: adj[A_U..A_NM] go from the adjoint of the
 // state after the step to that of the state before it; adj[A_U], adj[A_V]
 // then also hold the adjoint of the step's force field.

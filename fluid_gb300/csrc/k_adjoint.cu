@@ -764,6 +764,28 @@ __global__ void kb_adj_sources(float* __restrict__ dU, float* __restrict__ dV,
                     s.g);
 }
 
+// Zeroes the force field where a source sets U, V (the forward adds the
+// forces before the sources, which overwrite those cells).
+__global__ void k_mask_forces(float* __restrict__ Fu, float* __restrict__ Fv,
+                              const SourceRec* __restrict__ recs,
+                              const uint32_t* __restrict__ off, int n_groups,
+                              const uint8_t* __restrict__ flags, Grid g) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_groups) return;
+  uint32_t cell = recs[off[k]].cell;
+  int i = (int)(cell / (uint32_t)g.NY), j = (int)(cell % (uint32_t)g.NY);
+  int c = i * g.P + j;
+  bool fluid = (flags[c] & F_FLUID) != 0;
+  for (uint32_t q = off[k]; q < off[k + 1]; ++q) {
+    SourceRec r = recs[q];
+    if ((r.mode & 1u) && !fluid) continue;
+    if (r.mode & 2u) {
+      Fu[c] = 0.0f;
+      Fv[c] = 0.0f;
+    }
+  }
+}
+
 // A batch's loss: L_s = ||M_s - target_s||_2 per scene.  Block rows of the
 // sums of squares per cell tile, one block per scene to combine its tiles'
 // rows, then the seed dL/dM_s = (M_s - target_s) / L_s.
@@ -794,21 +816,26 @@ __global__ void kb_loss_combine(const float* __restrict__ part, const int* __res
   }
   block_row<1>(v, 0u, sh, row);
   __syncthreads();
-  if (threadIdx.x == 0) losses[s] = sqrt((double)row[0] + (double)row[1]);
+  if (threadIdx.x == 0) {
+    double L = sqrt((double)row[0] + (double)row[1]);
+    losses[s] = L;
+    // 1 / L_s as floats after the n losses.
+    reinterpret_cast<float*>(losses + gridDim.x)[s] = L > 0.0 ? (float)(1.0 / L) : 0.0f;
+  }
 }
 __global__ void kb_loss_seed(const BTile* __restrict__ tiles, const BScene* __restrict__ sc,
                              const float* __restrict__ M, const float* __restrict__ T,
-                             const double* __restrict__ losses, float* __restrict__ lamM) {
+                             const double* __restrict__ losses, int n_scenes,
+                             float* __restrict__ lamM) {
   const BTile t = tiles[blockIdx.x];
   const BScene& s = sc[t.s];
   int j = t.x * blockDim.x + threadIdx.x;
   int i = t.y * blockDim.y + threadIdx.y;
   if (i >= s.g.NX || j >= s.g.NY) return;
   long long c = s.off + (long long)i * s.g.P + j;
-  double L = losses[t.s];
+  float inv = reinterpret_cast<const float*>(losses + n_scenes)[t.s];
   float v = 0.0f;
-  if (i >= 1 && i <= s.g.NX - 2 && j >= 1 && j <= s.g.NY - 2 && L > 0.0)
-    v = (float)((double)(M[c] - T[c]) / L);
+  if (i >= 1 && i <= s.g.NX - 2 && j >= 1 && j <= s.g.NY - 2) v = (M[c] - T[c]) * inv;
   lamM[c] = v;
 }
 
@@ -827,21 +854,25 @@ __global__ void k_loss_partials(const float* __restrict__ M, const float* __rest
   block_row<1>(v, 0u, sh, part + 2 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x));
 }
 
-// Seeds the adjoint state with dL/dM = (M - target) / L on interior cells,
-// zero elsewhere and for every other field; stores L in FP64 (the float-pair
-// sum carries ~48 bits, so differences of nearby losses stay resolved).
-__global__ void k_loss_seed(const float* __restrict__ M, const float* __restrict__ T,
-                            const float* __restrict__ row, float* __restrict__ lamM,
-                            double* __restrict__ loss, Grid g) {
+// L = sqrt(sum) in FP64 (the float-pair sum carries ~48 bits, so
+// differences of nearby losses stay resolved) and 1 / L rounded to float.
+__global__ void k_loss_finish(const float* __restrict__ row, double* __restrict__ loss,
+                              float* __restrict__ inv) {
   double L = sqrt((double)row[0] + (double)row[1]);
+  loss[0] = L;
+  inv[0] = L > 0.0 ? (float)(1.0 / L) : 0.0f;
+}
+
+// Seeds the adjoint state with dL/dM = (M - target) / L on interior cells,
+// zero elsewhere.
+__global__ void k_loss_seed(const float* __restrict__ M, const float* __restrict__ T,
+                            const float* __restrict__ inv, float* __restrict__ lamM, Grid g) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i == 0 && j == 0) loss[0] = L;
   if (i >= g.NX || j >= g.NY) return;
   int c = i * g.P + j;
   float v = 0.0f;
-  if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2 && L > 0.0)
-    v = (float)((double)(M[c] - T[c]) / L);
+  if (i >= 1 && i <= g.NX - 2 && j >= 1 && j <= g.NY - 2) v = (M[c] - T[c]) * inv[0];
   lamM[c] = v;
 }
 
@@ -882,7 +913,8 @@ cudaError_t launch_loss_seed(fg_fluid* f, const float* target, double* dev_loss)
         b->cell_tiles, b->scenes_dev, f->d[FG_M], target, f->partials);
     kb_loss_combine<<<b->n, 256, 0, f->stream>>>(f->partials, b->cell_range, b->losses);
     kb_loss_seed<<<b->n_cell_tiles, dim3(b->bx, b->by), 0, f->stream>>>(
-        b->cell_tiles, b->scenes_dev, f->d[FG_M], target, b->losses, f->adj[fg_fluid::A_M]);
+        b->cell_tiles, b->scenes_dev, f->d[FG_M], target, b->losses, b->n,
+        f->adj[fg_fluid::A_M]);
     size_t bytes = sizeof(float) * (size_t)f->NX * f->P;
     for (int k : {fg_fluid::A_U, fg_fluid::A_V, fg_fluid::A_NU, fg_fluid::A_NV, fg_fluid::A_NM}) {
       cudaError_t e = cudaMemsetAsync(f->adj[k], 0, bytes, f->stream);
@@ -898,9 +930,11 @@ cudaError_t launch_loss_seed(fg_fluid* f, const float* target, double* dev_loss)
   k_loss_partials<<<gr, bl, 0, f->stream>>>(f->d[FG_M], target, f->partials, f->g);
   float* row = nullptr;
   count(f, combine_rows<1>(f->stream, f->partials, nb, 0u, &row));
-  count(f);
-  k_loss_seed<<<gr, bl, 0, f->stream>>>(f->d[FG_M], target, row, f->adj[fg_fluid::A_M], dev_loss,
-                                        f->g);
+  // 1 / L in the float after the FP64 loss (the scalar slots hold 8 floats).
+  float* inv = reinterpret_cast<float*>(dev_loss) + 2;
+  count(f, 2);
+  k_loss_finish<<<1, 1, 0, f->stream>>>(row, dev_loss, inv);
+  k_loss_seed<<<gr, bl, 0, f->stream>>>(f->d[FG_M], target, inv, f->adj[fg_fluid::A_M], f->g);
   size_t bytes = sizeof(float) * (size_t)f->NX * f->P;
   for (int k : {fg_fluid::A_U, fg_fluid::A_V, fg_fluid::A_NU, fg_fluid::A_NV, fg_fluid::A_NM}) {
     cudaError_t e = cudaMemsetAsync(f->adj[k], 0, bytes, f->stream);
@@ -1029,6 +1063,14 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
           A[F::A_U], A[F::A_V], A[F::A_M], f->src_dev, f->src_off_dev, f->n_src_groups, f->flags,
           g);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask_forces(fg_fluid* f, float* fu, float* fv) {
+  if (f->n_src_groups <= 0 || f->batch) return cudaSuccess;
+  count(f);
+  k_mask_forces<<<(f->n_src_groups + 255) / 256, 256, 0, f->stream>>>(
+      fu, fv, f->src_dev, f->src_off_dev, f->n_src_groups, f->flags, f->g);
   return cudaGetLastError();
 }
 

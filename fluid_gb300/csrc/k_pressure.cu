@@ -166,18 +166,27 @@ struct WTab {
 // elsewhere (ring included); phi = 0 when `zero_phi` (a solve with no sweeps
 // reads it directly).
 // U, V use the grid pitch g.P, the solver arrays the pitch Ps.
+// U + Fu at face u (the force field of a recorded step, null otherwise).
+__device__ __forceinline__ float with_force(const float* __restrict__ U,
+                                            const float* __restrict__ F, int u) {
+  return F ? U[u] + F[u] : U[u];
+}
+
 __device__ __forceinline__ void setup_cell_p(int i, int j, const float* __restrict__ U,
                                              const float* __restrict__ V, float* __restrict__ phi,
                                              float* __restrict__ rhs, float* __restrict__ W,
                                              float* __restrict__ BW,
                                              const uint8_t* __restrict__ flags, float om,
-                                             int zero_phi, const Grid& g, int Ps) {
+                                             int zero_phi, const Grid& g, int Ps,
+                                             const float* __restrict__ Fu = nullptr,
+                                             const float* __restrict__ Fv = nullptr) {
   int u = i * g.P + j;
   int c = i * Ps + j;
   float b = 0.0f, w = 0.0f, bw = 0.0f;
   uint8_t fl = flags[c];
   if (flag_active(fl)) {
-    float div = U[u + g.P] - U[u] + V[u + 1] - V[u];
+    float div = with_force(U, Fu, u + g.P) - with_force(U, Fu, u) + with_force(V, Fv, u + 1) -
+                with_force(V, Fv, u);
     b = -div;
     w = om / (float)flag_count(fl);
     bw = w * b;
@@ -199,11 +208,11 @@ __global__ void k_setup_system(const float* __restrict__ U, const float* __restr
                                float* __restrict__ phi, float* __restrict__ rhs,
                                float* __restrict__ W, float* __restrict__ BW,
                                const uint8_t* __restrict__ flags, float om, int zero_phi, Grid g,
-                               int Ps) {
+                               int Ps, const float* __restrict__ Fu, const float* __restrict__ Fv) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
-  setup_cell_p(i, j, U, V, phi, rhs, W, BW, flags, om, zero_phi, g, Ps);
+  setup_cell_p(i, j, U, V, phi, rhs, W, BW, flags, om, zero_phi, g, Ps, Fu, Fv);
 }
 
 // Register-blocked, temporally blocked Jacobi.  A CTA of 8 warps holds a
@@ -565,7 +574,9 @@ __device__ __forceinline__ void grad_cell(int i, int j, const float* __restrict_
                                           const float* __restrict__ rhs,
                                           const uint8_t* __restrict__ flags, float cp,
                                           const float2* __restrict__ noise, float turbStrength,
-                                          int do_turb, const Grid& g, GradAcc& acc) {
+                                          int do_turb, const Grid& g, GradAcc& acc,
+                                          const float* __restrict__ Fu = nullptr,
+                                          const float* __restrict__ Fv = nullptr) {
   const int P = g.P;
   const int c = i * P + j;
   const bool hasL = i >= 1, hasR = i <= g.NX - 2, hasB = j >= 1, hasT = j <= g.NY - 2;
@@ -592,8 +603,9 @@ __device__ __forceinline__ void grad_cell(int i, int j, const float* __restrict_
   if (!hasR) pR = 0.0f;
   if (!hasB) pB = 0.0f;
   if (!hasT) pT = 0.0f;
-  float u = U[c], v = V[c];
-  const float uR0 = U[cR], vT0 = V[cT], bc = rhs[c];
+  // U1 = U + the recorded step's forces (when given).
+  float u = with_force(U, Fu, c), v = with_force(V, Fv, c);
+  const float uR0 = with_force(U, Fu, cR), vT0 = with_force(V, Fv, cT), bc = rhs[c];
   const float2 nz = do_turb ? noise[c] : make_float2(0.0f, 0.0f);
   if (hasL && hasB && hasT && (act || aL)) u = u + (fbit(fl, F_FLUID) * pL - fbit(fl, F_W) * pc);
   if (hasB && hasL && hasR && (act || aB)) v = v + (fbit(fl, F_FLUID) * pB - fbit(fl, F_S) * pc);
@@ -638,7 +650,8 @@ __global__ void __launch_bounds__(256)
                  const float* __restrict__ e1, const PCtl* __restrict__ ectl,
                  const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float cp,
                  const float2* __restrict__ noise, float turbStrength, int do_turb,
-                 float* __restrict__ part, Grid g) {
+                 float* __restrict__ part, Grid g, const float* __restrict__ Fu,
+                 const float* __restrict__ Fv) {
   __shared__ float shr[64 * 5];
   const float* phi = ctl->sel ? phi1 : phi0;
   const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
@@ -650,7 +663,7 @@ __global__ void __launch_bounds__(256)
       const int i = (blockIdx.y * GR + k) * blockDim.y + threadIdx.y;
       if (i < g.NX)
         grad_cell(i, j, U, V, Uo, Vo, p, phi, e, rhs, flags, cp, noise, turbStrength, do_turb, g,
-                  acc);
+                  acc, Fu, Fv);
     }
   }
   // Row slots: sum div^2, max |div|, fluid cells (exact), sum r^2, max |r|.
@@ -850,7 +863,8 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   if ((e = cudaMemsetAsync(ctl, 0, sizeof(PCtl), f->stream)) != cudaSuccess) return e;
   count(f);
   k_setup_system<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->phi, f->rhs, f->wgt, f->bw,
-                                           f->flags, om, num_iters == 0 ? 1 : 0, f->g, f->P);
+                                           f->flags, om, num_iters == 0 ? 1 : 0, f->g, f->P,
+                                           f->step_fu, f->step_fv);
   mark(f, "pressure setup");
   if (num_iters > 0) {
     if ((e = jacobi_solve(f, ctl, f->rhs, f->bw, f->phi, f->phi2, num_iters, true)) != cudaSuccess)
@@ -873,7 +887,8 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   k_grad_fused<<<rg, bl, 0, f->stream>>>(
       f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
       f->err, f->err2, refine ? ectl : nullptr, f->rhs, f->flags, cp, f->noise,
-      f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g);
+      f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g, f->step_fu,
+      f->step_fv);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   float* out = nullptr;
@@ -909,7 +924,7 @@ cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi) {
   k_grad_fused<<<rg, bl, 0, f->stream>>>(
       f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], phi, phi,
       (const PCtl*)f->pctl, nullptr, nullptr, nullptr, f->rhs, f->flags, cp, f->noise, 0.0f, 0,
-      f->partials, f->g);
+      f->partials, f->g, f->step_fu, f->step_fv);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   return cudaGetLastError();
@@ -1017,7 +1032,7 @@ extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, 
   if (cudaMemsetAsync(ctl, 0, pctl_bytes(nlaunch), st) != cudaSuccess) return FG_ERR_CUDA;
   k_noalloc_flags<<<gr, bl, 0, st>>>(s, flags, g, Ps);
   k_setup_system<<<gr, bl, 0, st>>>(u, v, phi, rhs, W, BW, flags, om, num_iters == 0 ? 1 : 0, g,
-                                    Ps);
+                                    Ps, nullptr, nullptr);
   int n = 0;
   if (num_iters > 0 &&
       enqueue_jacobi(st, gs, ctl, rhs, BW, W, flags, phi, phi2, num_iters, T, om,
