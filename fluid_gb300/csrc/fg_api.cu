@@ -1134,12 +1134,28 @@ int load_state(fg_fluid* f, const float* src) {
 
 // Copies a field in the Go slice layout (host or device memory) to a
 // pitched device field, or back.
+bool on_device(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
 int put_field(fg_fluid* f, float* dev, const float* src) {
+  if (on_device(src)) {
+    CK(f, launch_repitch(f, dev, src, f->P, f->NY), "upload");
+    return FG_OK;
+  }
   size_t hp = sizeof(float) * f->NY, dp = sizeof(float) * f->P;
   CK(f, cudaMemcpy2DAsync(dev, dp, src, hp, hp, f->NX, cudaMemcpyDefault, f->stream), "upload");
   return FG_OK;
 }
 int get_field(fg_fluid* f, float* dst, const float* dev) {
+  if (on_device(dst)) {
+    CK(f, launch_repitch(f, dst, dev, f->NY, f->P), "download");
+    return FG_OK;
+  }
   size_t hp = sizeof(float) * f->NY, dp = sizeof(float) * f->P;
   CK(f, cudaMemcpy2DAsync(dst, hp, dev, dp, hp, f->NX, cudaMemcpyDefault, f->stream), "download");
   return FG_OK;
@@ -1164,22 +1180,31 @@ int enqueue_step_record(fg_fluid* f, float dt, const float* fu, const float* fv,
   CK(f, launch_apply_sources(f), "sources");
   // The forces (zero where the sources set U, V) are added by the pressure
   // setup and the gradient kernel as they read U, V: U1 = sources(U0 + F).
+  // Without confinement the gradient kernel also applies the turbulence and
+  // writes U2 to the record; with it, U2 is copied and confinement and
+  // turbulence run as their own pass.
+  const bool conf = p.confinement != 0.0f, turb = p.turbulence_strength > 0.0f;
+  const bool fuse = turb && !conf;
   f->step_fu = fu;
   f->step_fv = fv;
+  if (fuse) {
+    f->step_u2 = R(0);
+    f->step_v2 = R(1);
+  }
   cudaError_t ep = cudaSuccess;
   rc = FG_OK;
   if (replay) {
-    ep = launch_grad_replay(f, dt, phi);
+    ep = launch_grad_replay(f, dt, phi, fuse);
   } else {
     ep = launch_clear_stats(f);
-    if (ep == cudaSuccess) rc = enqueue_pressure(f, p.num_iters, dt, false);
+    if (ep == cudaSuccess) rc = enqueue_pressure(f, p.num_iters, dt, fuse);
     if (ep == cudaSuccess && !rc) ep = launch_store_phi(f, phi);
   }
   f->step_fu = f->step_fv = nullptr;
+  f->step_u2 = f->step_v2 = nullptr;
   if (rc) return rc;
   if (ep != cudaSuccess) return fail(f, FG_ERR_CUDA, "pressure", ep);
-  const bool conf = p.confinement != 0.0f, turb = p.turbulence_strength > 0.0f;
-  if (conf || turb) {
+  if (conf) {
     if ((rc = copy_field(f, R(0), f->d[FG_U])) || (rc = copy_field(f, R(1), f->d[FG_V]))) return rc;
     CK(f, launch_confinement_turbulence(f, dt, conf, turb), "confinement/turbulence");
   }

@@ -221,6 +221,10 @@ struct fg_fluid {
   // the pressure setup and the gradient kernel), null otherwise.
   const float* step_fu = nullptr;
   const float* step_fv = nullptr;
+  // Where the gradient kernel also writes the projected field before the
+  // turbulence it applies (a recorded step's U2, V2), null otherwise.
+  float* step_u2 = nullptr;
+  float* step_v2 = nullptr;
   // Non-null when this handle is a batch of scenes (fg_batch_create).
   fg::BatchGeom* batch = nullptr;
   // Kernel launches enqueued so far (graph replays add the captured count).
@@ -280,7 +284,7 @@ cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const fl
 // Copies the last solve's potential to dst.
 cudaError_t launch_store_phi(fg_fluid* f, float* dst);
 // Gradient subtract with a stored potential (a recorded step's replay).
-cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi);
+cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi, bool fuse_turb);
 // k_adjoint.cu
 constexpr int kTapeFields = 13;  // U2 V2 U4 V4 fwdU fwdV corrU corrV U5 V5 M1 fwdM corrM
 cudaError_t launch_add_forces(fg_fluid* f, const float* fu, const float* fv);
@@ -303,6 +307,8 @@ cudaError_t launch_view(fg_fluid* f, int kind, float* dev_minmax);  // 0 vortici
 cudaError_t launch_field_minmax(fg_fluid* f, int field, float* dev_minmax);
 cudaError_t launch_sample_velocity(fg_fluid* f, float x, float y, float* dev_uv);
 cudaError_t launch_max_speed(fg_fluid* f, float* dev_out);
+// Device-to-device copy of an NX x NY field between two row pitches.
+cudaError_t launch_repitch(fg_fluid* f, float* dst, const float* src, int dpitch, int spitch);
 
 // Grid of the reduction kernels: 32 x 8 threads per block over (j, i), at
 // most about 1200 blocks; each block strides down the rows, so the single-

@@ -576,7 +576,9 @@ __device__ __forceinline__ void grad_cell(int i, int j, const float* __restrict_
                                           const float2* __restrict__ noise, float turbStrength,
                                           int do_turb, const Grid& g, GradAcc& acc,
                                           const float* __restrict__ Fu = nullptr,
-                                          const float* __restrict__ Fv = nullptr) {
+                                          const float* __restrict__ Fv = nullptr,
+                                          float* __restrict__ U2o = nullptr,
+                                          float* __restrict__ V2o = nullptr) {
   const int P = g.P;
   const int c = i * P + j;
   const bool hasL = i >= 1, hasR = i <= g.NX - 2, hasB = j >= 1, hasT = j <= g.NY - 2;
@@ -627,6 +629,11 @@ __device__ __forceinline__ void grad_cell(int i, int j, const float* __restrict_
     acc.d2 = ff_add(acc.d2, ff_sq(div));
     acc.dmax = fmaxf(acc.dmax, fabsf(div));
     acc.n = acc.n + 1.0f;
+    if (U2o) {
+      // The projected field before turbulence (a recorded step keeps it).
+      U2o[c] = u;
+      V2o[c] = v;
+    }
     if (do_turb) {
       float noiseU = nz.x * turbStrength;
       float noiseV = nz.y * turbStrength;
@@ -637,6 +644,10 @@ __device__ __forceinline__ void grad_cell(int i, int j, const float* __restrict_
         v += noiseV * turbulenceFactor;
       }
     }
+  }
+  if (U2o && (fl & (F_FLUID | F_INTERIOR)) != (F_FLUID | F_INTERIOR)) {
+    U2o[c] = u;
+    V2o[c] = v;
   }
   Uo[c] = u;
   Vo[c] = v;
@@ -651,7 +662,8 @@ __global__ void __launch_bounds__(256)
                  const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float cp,
                  const float2* __restrict__ noise, float turbStrength, int do_turb,
                  float* __restrict__ part, Grid g, const float* __restrict__ Fu,
-                 const float* __restrict__ Fv) {
+                 const float* __restrict__ Fv, float* __restrict__ U2o,
+                 float* __restrict__ V2o) {
   __shared__ float shr[64 * 5];
   const float* phi = ctl->sel ? phi1 : phi0;
   const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
@@ -663,7 +675,7 @@ __global__ void __launch_bounds__(256)
       const int i = (blockIdx.y * GR + k) * blockDim.y + threadIdx.y;
       if (i < g.NX)
         grad_cell(i, j, U, V, Uo, Vo, p, phi, e, rhs, flags, cp, noise, turbStrength, do_turb, g,
-                  acc, Fu, Fv);
+                  acc, Fu, Fv, U2o, V2o);
     }
   }
   // Row slots: sum div^2, max |div|, fluid cells (exact), sum r^2, max |r|.
@@ -690,10 +702,12 @@ __device__ __forceinline__ void grad_batch_cell(int i, int j, const float* __res
                                                 const float* __restrict__ rhs,
                                                 const uint8_t* __restrict__ flags, float cp,
                                                 const float2* __restrict__ noise,
-                                                float turbStrength, int do_turb, const Grid& g) {
+                                                float turbStrength, int do_turb,
+                                                float* __restrict__ U2o, float* __restrict__ V2o,
+                                                const Grid& g) {
   GradAcc acc{{0.0f, 0.0f}, {0.0f, 0.0f}, 0.0f, 0.0f, 0.0f};
   grad_cell(i, j, U, V, Uo, Vo, p, ctl->sel ? phi1 : phi0, nullptr, rhs, flags, cp, noise,
-            turbStrength, do_turb, g, acc);
+            turbStrength, do_turb, g, acc, nullptr, nullptr, U2o, V2o);
 }
 
 __global__ void k_store_div_p(const float* __restrict__ r, DevStats* st) {
@@ -854,7 +868,7 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
                    f->partner[FG_U], f->partner[FG_V], f->d[FG_P], (const float*)f->phi,
                    (const float*)f->phi2, (const PCtl*)ctl, (const float*)f->rhs,
                    (const uint8_t*)f->flags, cp, (const float2*)f->noise,
-                   f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0);
+                   f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->step_u2, f->step_v2);
     swap_state(f, FG_U);
     swap_state(f, FG_V);
     return cudaGetLastError();
@@ -888,7 +902,7 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
       f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
       f->err, f->err2, refine ? ectl : nullptr, f->rhs, f->flags, cp, f->noise,
       f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g, f->step_fu,
-      f->step_fv);
+      f->step_fv, f->step_u2, f->step_v2);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   float* out = nullptr;
@@ -904,14 +918,15 @@ cudaError_t launch_store_phi(fg_fluid* f, float* dst) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi) {
+cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi, bool fuse_turb) {
   float cp = f->density * f->h / dt;  // fluid.go:158
   if (f->batch) {
     count(f);
     FG_CELLS_BATCH(f, grad_batch_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V],
                    f->partner[FG_U], f->partner[FG_V], f->d[FG_P], phi, phi,
                    (const PCtl*)f->pctl, (const float*)f->rhs, (const uint8_t*)f->flags, cp,
-                   (const float2*)f->noise, 0.0f, 0);
+                   (const float2*)f->noise, f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0,
+                   f->step_u2, f->step_v2);
     swap_state(f, FG_U);
     swap_state(f, FG_V);
     return cudaGetLastError();
@@ -923,8 +938,9 @@ cudaError_t launch_grad_replay(fg_fluid* f, float dt, const float* phi) {
   // the statistics partials it writes are not combined.
   k_grad_fused<<<rg, bl, 0, f->stream>>>(
       f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], phi, phi,
-      (const PCtl*)f->pctl, nullptr, nullptr, nullptr, f->rhs, f->flags, cp, f->noise, 0.0f, 0,
-      f->partials, f->g, f->step_fu, f->step_fv);
+      (const PCtl*)f->pctl, nullptr, nullptr, nullptr, f->rhs, f->flags, cp, f->noise,
+      f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g, f->step_fu,
+      f->step_fv, f->step_u2, f->step_v2);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   return cudaGetLastError();
