@@ -19,7 +19,7 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfluidgpu.so")
-SOURCES = ["fg_api.cu", "k_forces.cu", "k_advect.cu", "k_pressure.cu", "k_diag.cu", "k_adjoint.cu"]
+SOURCES = ["fg_api.cu", "k_forces.cu", "k_advect.cu", "k_pressure.cu", "k_diag.cu", "k_adjoint.cu", "k_particles.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

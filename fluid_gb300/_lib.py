@@ -113,6 +113,12 @@ SIGNATURES = {
     "fg_batch_grad": (_c_i, [_vp, _c_i, _vp, _vp, _vp]),
     "fg_batch_autotune": (_c_i, [_vp, _c_f, _c_i, ctypes.POINTER(_c_i), ctypes.POINTER(_c_i),
                                  ctypes.POINTER(_c_i), _fp]),
+    "fg_particles_add": (_c_i, [_vp, _c_i, _vp, _vp, _vp, _vp, _c_i]),
+    "fg_particles_advect": (_c_i, [_vp, _c_f]),
+    "fg_particles_count": (_c_i, [_vp, ctypes.POINTER(_c_i)]),
+    "fg_particles_get": (_c_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "fg_particles_clear": (_c_i, [_vp]),
+    "fg_render": (_c_i, [_vp, _c_i, _vp]),
     "fg_last_error": (ctypes.c_char_p, [_vp]),
 }
 

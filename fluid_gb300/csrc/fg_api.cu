@@ -394,6 +394,14 @@ int fg_destroy(fg_fluid* f) {
   tape_free(f);
   batch_free(f->batch);
   for (int k = 0; k < fg_fluid::A_COUNT; ++k) cudaFree(f->adj[k]);
+  for (int b = 0; b < 2; ++b) {
+    for (int q = 0; q < 4; ++q) cudaFree(f->parts.a[b][q]);
+    cudaFree(f->parts.rgb[b]);
+  }
+  cudaFree(f->parts.count);
+  cudaFree(f->parts.keep);
+  cudaFree(f->parts.block_keep);
+  cudaFree(f->image);
   for (int k = 0; k < FG_NUM_FIELDS; ++k) {
     cudaFree(f->d[k]);
     cudaFree(f->partner[k]);
@@ -1986,3 +1994,201 @@ int fg_batch_autotune(fg_fluid* f, float dt, int reps, int* tb_depth, int* block
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Tracer particles (main/main.go:489-546) and rendering (main/main.go:619-650,
+// main/colors.go:10-84).
+// ===========================================================================
+namespace {
+
+constexpr int kParticleBlock = 1024;
+
+int particles_read_count(fg_fluid* f, int* out) {
+  auto& P = f->parts;
+  if (!P.count) {
+    *out = 0;
+    return FG_OK;
+  }
+  CK(f, cudaMemcpyAsync(f->scalar_pinned, P.count, sizeof(int), cudaMemcpyDeviceToHost,
+                        f->stream), "particle count");
+  CK(f, cudaStreamSynchronize(f->stream), "particle count");
+  memcpy(out, f->scalar_pinned, sizeof(int));
+  P.n_upper = *out;
+  return FG_OK;
+}
+
+// Grows the particle buffers to hold `need` particles, keeping the first n.
+int particles_reserve(fg_fluid* f, int need, int n) {
+  auto& P = f->parts;
+  if (need <= P.cap && P.count) return FG_OK;
+  int cap = std::max(need, std::max(2 * P.cap, kParticleBlock));
+  cap = (cap + kParticleBlock - 1) / kParticleBlock * kParticleBlock;
+  fg_fluid::Particles Q;
+  Q.cap = cap;
+  Q.cur = 0;
+  Q.n_upper = P.n_upper;
+  cudaError_t e = cudaSuccess;
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+      e = cudaMalloc((void**)&Q.a[b][q], sizeof(float) * cap);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&Q.rgb[b], sizeof(uint32_t) * cap);
+  }
+  if (e == cudaSuccess) e = cudaMalloc((void**)&Q.keep, cap);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&Q.block_keep, sizeof(int) * (cap / kParticleBlock));
+  if (e == cudaSuccess && !P.count) {
+    e = cudaMalloc((void**)&Q.count, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(Q.count, 0, sizeof(int), f->stream);
+  } else {
+    Q.count = P.count;
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(Q.keep, 0, cap, f->stream);
+  for (int q = 0; q < 4 && e == cudaSuccess && n > 0; ++q)
+    e = cudaMemcpyAsync(Q.a[0][q], P.a[P.cur][q], sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                        f->stream);
+  if (e == cudaSuccess && n > 0)
+    e = cudaMemcpyAsync(Q.rgb[0], P.rgb[P.cur], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice,
+                        f->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
+  if (e != cudaSuccess) {
+    for (int b = 0; b < 2; ++b) {
+      for (int q = 0; q < 4; ++q) cudaFree(Q.a[b][q]);
+      cudaFree(Q.rgb[b]);
+    }
+    cudaFree(Q.keep);
+    cudaFree(Q.block_keep);
+    if (Q.count != P.count) cudaFree(Q.count);
+    return fail(f, FG_ERR_NOMEM, "particle buffers", e);
+  }
+  for (int b = 0; b < 2; ++b) {
+    for (int q = 0; q < 4; ++q) cudaFree(P.a[b][q]);
+    cudaFree(P.rgb[b]);
+  }
+  cudaFree(P.keep);
+  cudaFree(P.block_keep);
+  P = Q;
+  return FG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_particles_add(fg_fluid* f, int n, const float* x, const float* y, const float* max_age,
+                     const unsigned char* rgb, int max_total) {
+  if (is_batch(f)) return batch_unsupported(f);
+  if (!f || n < 0 || (n && (!x || !y || !max_age || !rgb))) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  int have = 0;
+  if ((rc = particles_read_count(f, &have))) return rc;
+  if (max_total > 0) n = std::max(0, std::min(n, max_total - have));
+  if (n == 0) return FG_OK;
+  if ((rc = particles_reserve(f, have + n, have))) return rc;
+  auto& P = f->parts;
+  std::vector<float> age(n, 0.0f);
+  std::vector<uint32_t> packed(n);
+  for (int k = 0; k < n; ++k)
+    packed[k] = (uint32_t)rgb[3 * k] | ((uint32_t)rgb[3 * k + 1] << 8) |
+                ((uint32_t)rgb[3 * k + 2] << 16);
+  const float* src[4] = {x, y, age.data(), max_age};
+  for (int q = 0; q < 4; ++q)
+    CK(f, cudaMemcpyAsync(P.a[P.cur][q] + have, src[q], sizeof(float) * n, cudaMemcpyDefault,
+                          f->stream), "particle upload");
+  CK(f, cudaMemcpyAsync(P.rgb[P.cur] + have, packed.data(), sizeof(uint32_t) * n,
+                        cudaMemcpyHostToDevice, f->stream), "particle upload");
+  int total = have + n;
+  CK(f, cudaMemcpyAsync(P.count, &total, sizeof(int), cudaMemcpyHostToDevice, f->stream),
+     "particle count");
+  CK(f, cudaStreamSynchronize(f->stream), "particle upload");
+  P.n_upper = total;
+  return FG_OK;
+}
+
+int fg_particles_advect(fg_fluid* f, float dt) {
+  if (is_batch(f)) return batch_unsupported(f);
+  if (!f) return FG_ERR_INVALID;
+  int rc = flush(f);
+  if (rc) return rc;
+  auto& P = f->parts;
+  if (!P.count || P.n_upper == 0) return FG_OK;
+  const int o = P.cur ^ 1;
+  const float* in[4] = {P.a[P.cur][0], P.a[P.cur][1], P.a[P.cur][2], P.a[P.cur][3]};
+  float* out[4] = {P.a[o][0], P.a[o][1], P.a[o][2], P.a[o][3]};
+  CK(f, launch_particles_advect(f, dt, P.n_upper, in, P.rgb[P.cur], out, P.rgb[o], P.count,
+                                P.keep, P.block_keep), "particles");
+  P.cur = o;
+  return FG_OK;
+}
+
+int fg_particles_count(fg_fluid* f, int* n) {
+  if (is_batch(f)) return batch_unsupported(f);
+  if (!f || !n) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  return particles_read_count(f, n);
+}
+
+int fg_particles_get(fg_fluid* f, float* x, float* y, float* age, float* max_age,
+                     unsigned char* rgb) {
+  if (is_batch(f)) return batch_unsupported(f);
+  if (!f) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  int n = 0;
+  if ((rc = particles_read_count(f, &n))) return rc;
+  if (n == 0) return FG_OK;
+  auto& P = f->parts;
+  float* dst[4] = {x, y, age, max_age};
+  for (int q = 0; q < 4; ++q)
+    if (dst[q])
+      CK(f, cudaMemcpyAsync(dst[q], P.a[P.cur][q], sizeof(float) * n, cudaMemcpyDefault,
+                            f->stream), "particle download");
+  std::vector<uint32_t> packed(rgb ? n : 0);
+  if (rgb)
+    CK(f, cudaMemcpyAsync(packed.data(), P.rgb[P.cur], sizeof(uint32_t) * n,
+                          cudaMemcpyDeviceToHost, f->stream), "particle download");
+  CK(f, cudaStreamSynchronize(f->stream), "particle download");
+  for (int k = 0; rgb && k < n; ++k) {
+    rgb[3 * k] = (unsigned char)(packed[k] & 0xff);
+    rgb[3 * k + 1] = (unsigned char)((packed[k] >> 8) & 0xff);
+    rgb[3 * k + 2] = (unsigned char)((packed[k] >> 16) & 0xff);
+  }
+  return FG_OK;
+}
+
+int fg_particles_clear(fg_fluid* f) {
+  if (is_batch(f)) return batch_unsupported(f);
+  if (!f) return FG_ERR_INVALID;
+  int rc = bind(f);
+  if (rc) return rc;
+  if (f->parts.count)
+    CK(f, cudaMemsetAsync(f->parts.count, 0, sizeof(int), f->stream), "particles");
+  f->parts.n_upper = 0;
+  return FG_OK;
+}
+
+int fg_render(fg_fluid* f, int kind, void* rgba) {
+  if (is_batch(f)) return batch_unsupported(f);
+  if (!f || !rgba || kind < FG_RENDER_SMOKE || kind > FG_RENDER_VORTICITY) return FG_ERR_INVALID;
+  int rc = flush(f);
+  if (rc) return rc;
+  size_t bytes = (size_t)f->NX * f->NY * 4;
+  if (!f->image) CK(f, cudaMalloc((void**)&f->image, bytes), "render target");
+  float* mm = dev_scalar_slot(f);
+  const float* field = nullptr;
+  if (kind == FG_RENDER_SMOKE || kind == FG_RENDER_PRESSURE) {
+    int fld = kind == FG_RENDER_SMOKE ? FG_M : FG_P;
+    CK(f, launch_field_minmax(f, fld, mm), "render");
+    field = f->d[fld];
+  } else {
+    CK(f, launch_view(f, kind == FG_RENDER_VORTICITY ? 0 : 1, mm), "render");
+    field = f->view;
+  }
+  CK(f, launch_render(f, field, mm, kind == FG_RENDER_VORTICITY ? 1 : 0, f->image), "render");
+  CK(f, cudaMemcpyAsync(rgba, f->image, bytes, cudaMemcpyDefault, f->stream), "render");
+  CK(f, cudaStreamSynchronize(f->stream), "render");
+  return FG_OK;
+}
+
+}  // extern "C"
+

@@ -225,6 +225,17 @@ struct fg_fluid {
   // turbulence it applies (a recorded step's U2, V2), null otherwise.
   float* step_u2 = nullptr;
   float* step_v2 = nullptr;
+  // Tracer particles (structure of arrays, two buffers) and the render
+  // target, allocated on first use.
+  struct Particles {
+    int cap = 0, n_upper = 0, cur = 0;
+    float* a[2][4] = {};  // x, y, age, max age
+    uint32_t* rgb[2] = {};
+    int* count = nullptr;      // device: live particles
+    uint8_t* keep = nullptr;   // device: survivor flags (cap rounded up to whole blocks)
+    int* block_keep = nullptr;
+  } parts;
+  uint32_t* image = nullptr;
   // Non-null when this handle is a batch of scenes (fg_batch_create).
   fg::BatchGeom* batch = nullptr;
   // Kernel launches enqueued so far (graph replays add the captured count).
@@ -307,6 +318,16 @@ cudaError_t launch_view(fg_fluid* f, int kind, float* dev_minmax);  // 0 vortici
 cudaError_t launch_field_minmax(fg_fluid* f, int field, float* dev_minmax);
 cudaError_t launch_sample_velocity(fg_fluid* f, float x, float y, float* dev_uv);
 cudaError_t launch_max_speed(fg_fluid* f, float* dev_out);
+// k_particles.cu: one advectParticles step from buffers `in` (x, y, age,
+// max age; rgb_in) into `out`, survivors in order; *count is the live
+// count, read and rewritten on the device; n_upper bounds it.
+cudaError_t launch_particles_advect(fg_fluid* f, float dt, int n_upper, const float* const* in,
+                                    const uint32_t* rgb_in, float* const* out, uint32_t* rgb_out,
+                                    int* count, uint8_t* keep, int* block_keep);
+// Renders `field` with the scientific (or, with diverging, the blue-white-
+// red) colormap between dev_minmax[0..1] into an NX x NY RGBA8 image.
+cudaError_t launch_render(fg_fluid* f, const float* field, const float* dev_minmax, int diverging,
+                          uint32_t* img);
 // Device-to-device copy of an NX x NY field between two row pitches.
 cudaError_t launch_repitch(fg_fluid* f, float* dst, const float* src, int dpitch, int spitch);
 

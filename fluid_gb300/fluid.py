@@ -415,6 +415,48 @@ class Fluid:
         out.update(loss=loss, force_u=gfu, force_v=gfv)
         return out
 
+    # ------------------------------------------------------------ particles, rendering
+    def particles_add(self, x, y, max_age, rgb, max_total=0):
+        """Appends particles at world positions (x, y) with age 0 (the app's
+        spawnParticles, main/main.go:489-510); rgb: (n, 3) uint8."""
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        ma = np.ascontiguousarray(np.broadcast_to(max_age, x.shape), np.float32)
+        c = np.ascontiguousarray(np.broadcast_to(rgb, (x.size, 3)), np.uint8)
+        self._check(self._L.fg_particles_add(self._h, x.size, x.ctypes.data, y.ctypes.data,
+                                             ma.ctypes.data, c.ctypes.data, int(max_total)),
+                    "fg_particles_add")
+
+    def particles_advect(self, dt):
+        """advectParticles (main/main.go:512-546) on the device."""
+        self._check(self._L.fg_particles_advect(self._h, ctypes.c_float(dt)),
+                    "fg_particles_advect")
+
+    def particles(self):
+        n = ctypes.c_int()
+        self._check(self._L.fg_particles_count(self._h, ctypes.byref(n)), "fg_particles_count")
+        out = {k: np.zeros(n.value, np.float32) for k in ("X", "Y", "Age", "MaxAge")}
+        rgb = np.zeros((n.value, 3), np.uint8)
+        self._check(self._L.fg_particles_get(self._h, out["X"].ctypes.data, out["Y"].ctypes.data,
+                                             out["Age"].ctypes.data, out["MaxAge"].ctypes.data,
+                                             rgb.ctypes.data), "fg_particles_get")
+        out["RGB"] = rgb
+        return out
+
+    def particles_clear(self):
+        self._check(self._L.fg_particles_clear(self._h), "fg_particles_clear")
+
+    RENDER_SMOKE, RENDER_PRESSURE, RENDER_SPEED, RENDER_VORTICITY = 0, 1, 2, 3
+
+    def render(self, kind):
+        """The app's drawScalarField / drawVorticityField image (NumX * NumY *
+        4 bytes RGBA, pixel (i, j) showing cell (i, NumY - 1 - j))."""
+        self._before()
+        out = np.zeros(self.numCells * 4, np.uint8)
+        self._check(self._L.fg_render(self._h, int(kind), out.ctypes.data), "fg_render")
+        self._after()
+        return out
+
     def Reset(self):
         self._check(self._L.fg_reset(self._h), "Reset")
 

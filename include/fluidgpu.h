@@ -313,6 +313,33 @@ int fg_batch_grad(fg_fluid* batch, int scene, float* dU, float* dV, float* dM);
 int fg_batch_autotune(fg_fluid* batch, float dt, int reps, int* tb_depth, int* block_x,
                       int* block_y, float* ms_per_step);
 
+/* Tracer particles: the app's advectParticles (main/main.go:512-546) on the
+ * device.  fg_particles_add appends n particles at world positions (x, y)
+ * with age 0, the given maximum age and colour (rgb: 3 bytes each), keeping
+ * the total at most max_total (the app's maxParticles; <= 0: no limit);
+ * host or device arrays.  fg_particles_advect(dt) ages every particle, drops
+ * those older than their maximum age, moves the others by RK2 midpoint steps
+ * through SampleVelocity (fluid.go:799-803) and drops those that leave the
+ * grid or enter a solid cell, keeping the survivors in order.
+ * fg_particles_get copies the live particles out (NULL: skipped; fg_particles
+ * _count gives their number). */
+int fg_particles_add(fg_fluid* f, int n, const float* x, const float* y, const float* max_age,
+                     const unsigned char* rgb, int max_total);
+int fg_particles_advect(fg_fluid* f, float dt);
+int fg_particles_count(fg_fluid* f, int* n);
+int fg_particles_get(fg_fluid* f, float* x, float* y, float* age, float* max_age,
+                     unsigned char* rgb);
+int fg_particles_clear(fg_fluid* f);
+
+/* Renders a field as the app draws it (main/main.go:619-650): an RGBA8
+ * image of NumX x NumY pixels, row stride 4 * NumX, pixel (i, j) showing cell
+ * (i, NumY - 1 - j); smoke, pressure and speed with the scientific colormap
+ * (getSciValue, main/colors.go:47-84) between the view's min and max,
+ * vorticity with the blue-white-red one (getDivergingColor,
+ * main/colors.go:10-44).  rgba: NumX * NumY * 4 bytes, host or device. */
+enum { FG_RENDER_SMOKE = 0, FG_RENDER_PRESSURE = 1, FG_RENDER_SPEED = 2, FG_RENDER_VORTICITY = 3 };
+int fg_render(fg_fluid* f, int kind, void* rgba);
+
 /* Text of the last error on the handle ("" if none); static text for a
  * NULL handle. */
 const char* fg_last_error(const fg_fluid* f);

@@ -1084,6 +1084,141 @@ struct Fluid {
 }  // namespace orc
 
 // ===========================================================================
+// App-side loops that read the simulation every frame: tracer particles
+// (main/main.go:512-546 advectParticles) and the field rendering
+// (main/main.go:619-650 drawScalarField / drawVorticityField with
+// main/colors.go:10-84).
+// ===========================================================================
+namespace orc {
+
+// advectParticles: ages, culls, RK2-advects and bounds-checks the particles
+// in place, keeping the survivors in order; returns their number.
+template <typename T>
+int advect_particles(const Fluid<T>& f, int n, T* X, T* Y, T* Age, T* MaxAge, uint32_t* RGB,
+                     T dt) {
+  const T h = f.h;
+  int w = 0;
+  for (int k = 0; k < n; ++k) {
+    T age = Age[k] + dt;
+    if (age > MaxAge[k]) continue;
+    T x = X[k], y = Y[k];
+    T u1 = f.sampleFrom(x, y, f.U, 0), v1 = f.sampleFrom(x, y, f.V, 1);
+    T midX = x + (T)0.5 * dt * u1;
+    T midY = y + (T)0.5 * dt * v1;
+    T u2 = f.sampleFrom(midX, midY, f.U, 0), v2 = f.sampleFrom(midX, midY, f.V, 1);
+    x += dt * u2;
+    y += dt * v2;
+    T qi = x / h, qj = y / h;
+    if (!(qi > (T)-2147483648.0 && qi < (T)2147483648.0 && qj > (T)-2147483648.0 &&
+          qj < (T)2147483648.0))
+      continue;
+    int fi = (int)qi, fj = (int)qj;
+    if (fi < 0 || fi >= f.NX || fj < 0 || fj >= f.NY) continue;
+    if (f.S[fi * f.NY + fj] == 0) continue;
+    X[w] = x;
+    Y[w] = y;
+    Age[w] = age;
+    MaxAge[w] = MaxAge[k];
+    RGB[w] = RGB[k];
+    ++w;
+  }
+  return w;
+}
+
+template <typename T>
+void rgba_store(uint8_t* px, T r, T g, T b) {
+  px[0] = (uint8_t)(T)(255 * r);
+  px[1] = (uint8_t)(T)(255 * g);
+  px[2] = (uint8_t)(T)(255 * b);
+  px[3] = 0xff;
+}
+
+// getSciValue (main/colors.go:47-84)
+template <typename T>
+void sci_value(T val, T mn, T mx, uint8_t* px) {
+  val = go_min(go_max(val, mn), mx - (T)0.0001);
+  T d = mx - mn;
+  if (d <= 0)
+    val = (T)0.5;
+  else
+    val = (val - mn) / d;
+  T m = (T)0.25;
+  T num = (T)std::floor((double)(val / m));
+  T s = (val - num * m) / m;
+  T r = 0, g = 0, b = 0;
+  if (num == 0) {
+    g = s;
+    b = 1;
+  } else if (num == 1) {
+    g = 1;
+    b = 1 - s;
+  } else if (num == 2) {
+    r = s;
+    g = 1;
+  } else if (num == 3) {
+    r = 1;
+    g = 1 - s;
+  }
+  rgba_store(px, r, g, b);
+}
+
+// getDivergingColor (main/colors.go:10-44)
+template <typename T>
+void diverging_color(T val, T mn, T mx, uint8_t* px) {
+  T absMax = (T)std::max(std::fabs((double)mn), std::fabs((double)mx));
+  if (absMax < (T)1e-8) {
+    px[0] = px[1] = px[2] = px[3] = 255;
+    return;
+  }
+  T t = val / absMax;
+  if (t > 1) t = 1;
+  if (t < -1) t = -1;
+  T r, g, b;
+  if (t >= 0) {
+    r = 1;
+    g = 1 - t;
+    b = 1 - t;
+  } else {
+    T a = -t;
+    r = 1 - a;
+    g = 1 - a;
+    b = 1;
+  }
+  rgba_store(px, r, g, b);
+}
+
+// kind: 0 smoke, 1 pressure, 2 speed, 3 vorticity.  out: NX x NY RGBA8,
+// pixel (i, j) showing cell (i, NY - 1 - j).
+template <typename T>
+void render(const Fluid<T>& f, int kind, uint8_t* out) {
+  std::vector<T> vals(f.N);
+  T mn = std::numeric_limits<T>::max(), mx = -(std::numeric_limits<T>::max() - 1);
+  if (kind == 0 || kind == 1) {
+    const std::vector<T>& F = kind == 0 ? f.M : f.p;
+    for (int c = 0; c < f.N; ++c) {
+      vals[c] = F[c];
+      if (F[c] < mn) mn = F[c];
+      if (F[c] > mx) mx = F[c];
+    }
+  } else if (kind == 2) {
+    f.velocityMagnitude(vals.data(), &mn, &mx);
+  } else {
+    f.vorticity(vals.data(), &mn, &mx);
+  }
+  for (int i = 0; i < f.NX; ++i)
+    for (int j = 0; j < f.NY; ++j) {
+      T v = vals[i * f.NY + (f.NY - j - 1)];
+      uint8_t* px = out + 4 * ((size_t)j * f.NX + i);
+      if (kind == 3)
+        diverging_color(v, mn, mx, px);
+      else
+        sci_value(v, mn, mx, px);
+    }
+}
+
+}  // namespace orc
+
+// ===========================================================================
 // Reverse mode of a recorded rollout: the FP64 reference for the CUDA
 // adjoint (test infrastructure; the reference has no derivatives).  A step
 // is Simulate (fluid.go:79-109) with the parallel Jacobi scheme and a fixed
@@ -1853,6 +1988,25 @@ int orc_stats(void* p, double* out) {
   });
 }
 int orc_threads(void* p) { return ((Handle*)p)->pool->size(); }
+
+// Tracer particles: advances n particles in place (the survivors first, in
+// order); returns their number.  Arrays hold the handle's precision.
+int orc_particles_advect(void* p, int n, void* x, void* y, void* age, void* max_age,
+                         uint32_t* rgb, double dt) {
+  return with((Handle*)p, [&](auto& f) {
+    using T = typename std::remove_reference<decltype(f.U[0])>::type;
+    return orc::advect_particles(f, n, (T*)x, (T*)y, (T*)age, (T*)max_age, rgb, (T)dt);
+  });
+}
+
+// Renders field `kind` (0 smoke, 1 pressure, 2 speed, 3 vorticity) into out
+// (NX x NY RGBA8).
+int orc_render(void* p, int kind, uint8_t* out) {
+  return with((Handle*)p, [&](auto& f) {
+    orc::render(f, kind, out);
+    return 0;
+  });
+}
 
 // Recorded rollout of `steps` steps from the handle's state (FP64 handles
 // only) with per-step forces (steps x 2 x N, NULL = none) and n_src sources

@@ -66,6 +66,8 @@ def lib():
                 "orc_sample_velocity": (i, [vp, d, d, ctypes.POINTER(d)]),
                 "orc_stats": (i, [vp, ctypes.POINTER(d)]),
                 "orc_threads": (i, [vp]),
+                "orc_particles_advect": (i, [vp, i, vp, vp, vp, vp, vp, d]),
+                "orc_render": (i, [vp, i, vp]),
                 "orc_rollout_grad": (i, [vp, i, d, vp, i, vp, vp, vp, vp, vp, vp, vp,
                                          ctypes.POINTER(d), vp, vp, vp, vp]),
             }
@@ -324,3 +326,17 @@ class OracleFluid:
             raise RuntimeError("orc_rollout_grad failed (%d)" % rc)
         return {"loss": loss.value, "U": out[0], "V": out[1], "M": out[2],
                 "force_u": dF[:, 0], "force_v": dF[:, 1]}
+
+    def particles_advect(self, dt, x, y, age, max_age, rgb):
+        """advectParticles (main/main.go:512-546) on arrays of this oracle's
+        precision, in place; returns the number of survivors (first)."""
+        return self._lib.orc_particles_advect(self._h, len(x), x.ctypes.data, y.ctypes.data,
+                                              age.ctypes.data, max_age.ctypes.data,
+                                              rgb.ctypes.data, float(dt))
+
+    def render(self, kind):
+        """drawScalarField / drawVorticityField: NumX * NumY * 4 bytes."""
+        out = np.zeros(self.NumX * self.NumY * 4, np.uint8)
+        self._lib.orc_render(self._h, int(kind), out.ctypes.data)
+        return out
+
