@@ -229,9 +229,16 @@ int check_iters(fg_fluid* f, int iters) {
 // Enqueues makeIncompressible's solve with the statistics of the projected
 // field.
 // fuse_turb: run addTurbulence inside the parallel scheme's gradient kernel.
+bool multigrid(const fg_fluid* f) { return f->prm.use_multigrid && f->prm.multigrid_levels > 1; }
+
 int enqueue_pressure(fg_fluid* f, int iters, float dt, bool fuse_turb) {
-  if (f->prm.use_multigrid && f->prm.multigrid_levels > 1)
-    return fail(f, FG_ERR_UNSUPPORTED, "UseMultigrid is not built for the GPU step");
+  if (multigrid(f)) {
+    // UseMultigrid (fluid.go:148-149) runs the reference's V-cycle whatever
+    // the single-grid scheme.
+    CK(f, launch_multigrid(f, iters, dt), "multigrid");
+    CK(f, launch_div_stats(f), "div stats");
+    return FG_OK;
+  }
   CK(f, launch_pressure(f, iters, dt, fuse_turb), "pressure");
   if (f->prm.scheme == FG_SCHEME_LEXSOR) CK(f, launch_div_stats(f), "div stats");
   return FG_OK;
@@ -245,12 +252,12 @@ int enqueue_step(fg_fluid* f, float dt) {
   mark(f, "start");
   CK(f, launch_apply_sources(f), "sources");
   CK(f, launch_clear_stats(f), "clear stats");
-  if (p.scheme == FG_SCHEME_LEXSOR)
+  if (p.scheme == FG_SCHEME_LEXSOR || multigrid(f))
     CK(f, cudaMemsetAsync(f->d[FG_P], 0, field_bytes(f), f->stream), "fill p");
   if (p.viscosity_diffusion > 0.0f) CK(f, launch_viscosity(f, dt), "viscosity");
   mark(f, "sources+viscosity");
   const bool conf = p.confinement != 0.0f, turb = p.turbulence_strength > 0.0f;
-  const bool fuse_turb = p.scheme == FG_SCHEME_JACOBI && !conf && turb;
+  const bool fuse_turb = p.scheme == FG_SCHEME_JACOBI && !multigrid(f) && !conf && turb;
   int rc = enqueue_pressure(f, p.num_iters, dt, fuse_turb);
   if (rc) return rc;
   mark(f, "gradient+div stats");
@@ -510,8 +517,6 @@ int fg_simulate(fg_fluid* f, float dt) {
   int rc = flush(f);
   if (rc) return rc;
   if ((rc = check_iters(f, f->prm.num_iters))) return rc;
-  if (f->prm.use_multigrid && f->prm.multigrid_levels > 1)
-    return fail(f, FG_ERR_UNSUPPORTED, "UseMultigrid is not built for the GPU step");
   invalidate(f, kStepFields);
   // Profiling brackets the Jacobi launches with timed events, which plain
   // capture would turn into graph-internal dependencies: run it uncaptured.
@@ -1115,7 +1120,7 @@ int tape_supported(fg_fluid* f) {
   if (p.viscosity_diffusion > 0.0f)
     return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support viscosity");
   if (p.use_multigrid && p.multigrid_levels > 1)
-    return fail(f, FG_ERR_UNSUPPORTED, "UseMultigrid is not built for the GPU step");
+    return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support UseMultigrid");
   return FG_OK;
 }
 

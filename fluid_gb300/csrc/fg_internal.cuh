@@ -288,6 +288,9 @@ cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt);
 // Pressure solve + gradient subtract + post-projection divergence statistics;
 // with fuse_turb (parallel scheme only) also addTurbulence.
 cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb);
+// solveMultigridVCycle (fluid.go:559-594) with the reference's serial
+// smoothers, bit for bit.
+cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt);
 // K Jacobi sweeps of A x = b from x = 0 (no early exit); ctl->sel names the
 // buffer holding x.
 cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const float* bw, float* x0,

@@ -53,7 +53,7 @@ constexpr int LEX_RING = 2048;  // sweeps in flight (a new sweep waits while the
 __global__ void __launch_bounds__(LEX_THREADS)
     k_lexsor(float* U, float* V, float* p, const uint8_t* __restrict__ flags, Grid g,
              int numIters, float relax0, float damping, float cp, float tol, int early_exit,
-             DevStats* st) {
+             DevStats* st, float minRelax = 1.2f, const int* __restrict__ stop = nullptr) {
   __shared__ int s_start[LEX_RING];
   __shared__ unsigned s_max[LEX_RING];
   __shared__ int s_cont[LEX_RING];
@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(LEX_THREADS)
   }
   __syncthreads();
   if (numIters <= 0 || ni <= 0 || nj <= 0) return;
+  if (stop && *stop) return;  // a multigrid solve that already converged
   // Start sweep 0 at step 0.
   if (threadIdx.x == 0) {
     s_start[0] = 0;
@@ -79,7 +80,6 @@ __global__ void __launch_bounds__(LEX_THREADS)
     s_hi = 1;
   }
   __syncthreads();
-  const float minRelax = 1.2f;
   // Bounded: each sweep takes D steps and starts at most D + 2 steps after
   // the previous one.
   const long long max_steps = (long long)numIters * (D + 2) + D + 4;
@@ -154,6 +154,177 @@ __global__ void __launch_bounds__(LEX_THREADS)
   if (threadIdx.x == 0) {
     st->sweeps = s_hi;
     st->last_maxdiv = s_last >= 0 ? (double)__uint_as_float(s_max[s_last & (LEX_RING - 1)]) : 0.0;
+  }
+}
+
+// ------------------------------------------------------------------ multigrid
+// solveMultigridVCycle (fluid.go:559-594) with its helpers (fluid.go:596-758,
+// 1122-1149): per iteration three SOR sweeps at relaxation 1.5 (k_lexsor),
+// the early exit on the last sweep's max |div|, the residual restricted by
+// full weighting to the (NX+1)/2 x (NY+1)/2 grid, 40 lexicographic
+// Gauss-Seidel sweeps there at relaxation 1.6, the bilinear prolongation
+// applied to p and the faces, three SOR sweeps at 1.2.  Every stage keeps
+// the reference's per-cell operation order; the serial loops become a
+// wavefront (the SOR sweeps, the coarse sweeps) or a per-face kernel that
+// applies a face's two updates in the loop's order (the correction).  Once
+// a solve exits early, *stop makes every later kernel of it return.
+
+// After the three pre-smoothing sweeps: count them and latch the exit when
+// the last one's max |div| is below the tolerance.
+__global__ void k_mg_check(const DevStats* __restrict__ sm, DevStats* st, int* stop, float tol,
+                           int post) {
+  if (*stop) return;
+  st->sweeps += 3;
+  if (post) return;
+  float maxDiv = (float)sm->last_maxdiv;
+  st->last_maxdiv = sm->last_maxdiv;
+  if (maxDiv < tol) *stop = 1;
+}
+
+// computePressureResidual (fluid.go:596-628): r = -div - laplacian(p) on
+// fluid interior cells, 0 elsewhere.
+__global__ void k_mg_residual(const float* __restrict__ U, const float* __restrict__ V,
+                              const float* __restrict__ p, const uint8_t* __restrict__ flags,
+                              float* __restrict__ r, const int* __restrict__ stop, Grid g) {
+  if (*stop) return;
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  uint8_t fl = flags[c];
+  float out = 0.0f;
+  if ((fl & (F_FLUID | F_INTERIOR)) == (F_FLUID | F_INTERIOR)) {
+    float div = U[c + P] - U[c] + V[c + 1] - V[c];
+    float sx0 = fbit(fl, F_W), sx1 = fbit(fl, F_E), sy0 = fbit(fl, F_S), sy1 = fbit(fl, F_N);
+    float lap = sx0 * (p[c - P] - p[c]) + sx1 * (p[c + P] - p[c]) + sy0 * (p[c - 1] - p[c]) +
+                sy1 * (p[c + 1] - p[c]);
+    out = -div - lap;
+  }
+  r[c] = out;
+}
+
+// restrictResidual (fluid.go:630-660) into the coarse grid (pitch cP = cNY).
+__global__ void k_mg_restrict(const float* __restrict__ r, float* __restrict__ cr,
+                              const int* __restrict__ stop, Grid g, int cNX, int cNY) {
+  if (*stop) return;
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= cNX || j >= cNY) return;
+  float out = 0.0f;
+  int fi = 2 * i, fj = 2 * j;
+  if (i >= 1 && i < cNX - 1 && j >= 1 && j < cNY - 1 && fi < g.NX - 1 && fj < g.NY - 1) {
+    const int P = g.P;
+    int c = fi * P + fj;
+    float center = r[c] * 0.25f;
+    float nb = (r[c - P] + r[c + P] + r[c - 1] + r[c + 1]) * 0.125f;
+    float cr4 = (r[c - P - 1] + r[c + P - 1] + r[c - P + 1] + r[c + P + 1]) * 0.0625f;
+    out = center + nb + cr4;
+  }
+  cr[i * cNY + j] = out;
+}
+
+// The coarse solid mask: the fine cell (2i, 2j) (fluid.go:672-685).
+__device__ __forceinline__ float coarse_s(const uint8_t* __restrict__ flags, int i, int j,
+                                          const Grid& g) {
+  int fi = 2 * i, fj = 2 * j;
+  if (fi >= g.NX || fj >= g.NY) return 0.0f;
+  return (flags[fi * g.P + fj] & F_FLUID) ? 1.0f : 0.0f;
+}
+
+// solveCoarseGrid (fluid.go:662-715): 40 lexicographic Gauss-Seidel sweeps
+// from zero, in one block.  Cell (i, j) of a sweep needs (i-1, j), (i, j-1)
+// of that sweep and (i+1, j), (i, j+1) of the previous one, so the sweeps
+// run as anti-diagonal wavefronts, each two diagonals behind the previous.
+constexpr int MG_THREADS = 1024;
+__global__ void __launch_bounds__(MG_THREADS)
+    k_mg_coarse(const float* __restrict__ cr, float* __restrict__ cp_,
+                const uint8_t* __restrict__ flags, const int* __restrict__ stop, Grid g, int cNX,
+                int cNY, int sweeps, float relaxation) {
+  if (*stop) return;
+  const int ni = cNX - 2, nj = cNY - 2;
+  for (int k = threadIdx.x; k < cNX * cNY; k += MG_THREADS) cp_[k] = 0.0f;
+  __syncthreads();
+  if (ni <= 0 || nj <= 0) return;
+  const int D = ni + nj - 1;
+  const int L = ni < nj ? ni : nj;
+  const long long steps = (long long)D + 2LL * (sweeps - 1);
+  for (long long tau = 0; tau < steps; ++tau) {
+    // Sweeps t with 0 <= tau - 2t < D, each on diagonal d = tau - 2t + 2.
+    int t_lo = (int)((tau - D + 2) / 2);
+    if (t_lo < 0) t_lo = 0;
+    while (tau - 2LL * t_lo >= D) ++t_lo;
+    int t_hi = (int)(tau / 2);
+    if (t_hi > sweeps - 1) t_hi = sweeps - 1;
+    int nact = t_hi - t_lo + 1;
+    for (int q = threadIdx.x; q < nact * L; q += MG_THREADS) {
+      int t = t_lo + q / L;
+      int k = q - (q / L) * L;
+      int d = (int)(tau - 2LL * t) + 2;
+      int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
+      int i = i_lo + k;
+      if (i > i_hi) continue;
+      int j = d - i;
+      if (coarse_s(flags, i, j, g) == 0.0f) continue;
+      float sx0 = coarse_s(flags, i - 1, j, g), sx1 = coarse_s(flags, i + 1, j, g);
+      float sy0 = coarse_s(flags, i, j - 1, g), sy1 = coarse_s(flags, i, j + 1, g);
+      float s = sx0 + sx1 + sy0 + sy1;
+      if (s == 0.0f) continue;
+      int c = i * cNY + j;
+      float pc = cp_[c];
+      float lap = sx0 * (cp_[c - cNY] - pc) + sx1 * (cp_[c + cNY] - pc) + sy0 * (cp_[c - 1] - pc) +
+                  sy1 * (cp_[c + 1] - pc);
+      float residual = cr[c] - lap;
+      float correction = -residual / s * relaxation;
+      cp_[c] = pc + correction;
+    }
+    __syncthreads();
+  }
+}
+
+// prolongateCorrection (fluid.go:717-758) at fine cell (i, j).
+__device__ __forceinline__ float mg_corr(const float* __restrict__ cc, int i, int j, int cNX,
+                                         int cNY) {
+  int ci = i / 2, cj = j / 2;
+  if (ci >= cNX - 1 || cj >= cNY - 1) return 0.0f;
+  float fI = (float)(i % 2) * 0.5f, fJ = (float)(j % 2) * 0.5f;
+  return (1.0f - fI) * (1.0f - fJ) * cc[ci * cNY + cj] +
+         fI * (1.0f - fJ) * cc[(ci + 1) * cNY + cj] + (1.0f - fI) * fJ * cc[ci * cNY + cj + 1] +
+         fI * fJ * cc[(ci + 1) * cNY + cj + 1];
+}
+
+// applePressureCorrection (fluid.go:1122-1149): p += corr * cp on fluid
+// interior cells; face (i, j) of U first gets + S_i corr(i-1, j) from cell
+// (i-1, j), then - S_{i-1} corr(i, j) from cell (i, j), as the loop visits
+// them; V likewise along j.
+__global__ void k_mg_apply(float* __restrict__ U, float* __restrict__ V, float* __restrict__ p,
+                           const float* __restrict__ cc, const uint8_t* __restrict__ flags,
+                           const int* __restrict__ stop, float cp, Grid g, int cNX, int cNY) {
+  if (*stop) return;
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const int P = g.P;
+  int c = i * P + j;
+  auto fluid_int = [&](int a, int b) {
+    return a >= 1 && a <= g.NX - 2 && b >= 1 && b <= g.NY - 2 &&
+           (flags[a * P + b] & F_FLUID) != 0;
+  };
+  bool self = fluid_int(i, j);
+  float corr = self ? mg_corr(cc, i, j, cNX, cNY) : 0.0f;
+  if (self) p[c] += corr * cp;
+  uint8_t fl = flags[c];
+  if (i >= 1) {
+    float u = U[c];
+    if (fluid_int(i - 1, j)) u += fbit(fl, F_FLUID) * mg_corr(cc, i - 1, j, cNX, cNY);
+    if (self) u -= fbit(fl, F_W) * corr;
+    U[c] = u;
+  }
+  if (j >= 1) {
+    float v = V[c];
+    if (fluid_int(i, j - 1)) v += fbit(fl, F_FLUID) * mg_corr(cc, i, j - 1, cNX, cNY);
+    if (self) v -= fbit(fl, F_S) * corr;
+    V[c] = v;
   }
 }
 
@@ -839,6 +1010,40 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
 cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const float* bw, float* x0,
                                 float* x1, int iters) {
   return jacobi_solve(f, (PCtl*)ctl, b, bw, x0, x1, iters, false);
+}
+
+cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt) {
+  float cp = f->density * f->h / dt;  // fluid.go:560
+  const int cNX = (f->NX + 1) / 2, cNY = (f->NY + 1) / 2;
+  if ((size_t)cNX * cNY > (size_t)f->NX * f->P) return cudaErrorInvalidValue;
+  // Scratch: the fine residual in rhs, the coarse right-hand side and
+  // solution in err / err2, the stop latch and the smoothers' statistics in
+  // the correction solve's control block (unused by this scheme).
+  int* stop = reinterpret_cast<int*>(f->ectl);
+  DevStats* sm = reinterpret_cast<DevStats*>(reinterpret_cast<char*>(f->ectl) + 64);
+  cudaError_t e = cudaMemsetAsync(f->ectl, 0, 64 + sizeof(DevStats), f->stream);
+  if (e != cudaSuccess) return e;
+  dim3 gr = cell_grid(f), bl(BX, BY);
+  dim3 cg((cNY + BX - 1) / BX, (cNX + BY - 1) / BY);
+  for (int it = 0; it < num_iters; ++it) {
+    count(f, 8);
+    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->g,
+                                                3, 1.5f, f->prm.pressure_damping, cp,
+                                                f->prm.tolerance, 0, sm, 1.5f, stop);
+    k_mg_check<<<1, 1, 0, f->stream>>>(sm, f->dstats, stop, f->prm.tolerance, 0);
+    k_mg_residual<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->rhs,
+                                            stop, f->g);
+    k_mg_restrict<<<cg, bl, 0, f->stream>>>(f->rhs, f->err, stop, f->g, cNX, cNY);
+    k_mg_coarse<<<1, MG_THREADS, 0, f->stream>>>(f->err, f->err2, f->flags, stop, f->g, cNX, cNY,
+                                                 40, 1.6f);
+    k_mg_apply<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->err2, f->flags,
+                                         stop, cp, f->g, cNX, cNY);
+    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->g,
+                                                3, 1.2f, f->prm.pressure_damping, cp,
+                                                f->prm.tolerance, 0, sm, 1.2f, stop);
+    k_mg_check<<<1, 1, 0, f->stream>>>(sm, f->dstats, stop, f->prm.tolerance, 1);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb) {

@@ -36,7 +36,7 @@ extern "C" {
 #define FG_ERR_INVALID (-1)     /* bad argument: dimensions, pointer, parameter range   */
 #define FG_ERR_INDEX (-2)       /* cell index out of range (the Go API panics)          */
 #define FG_ERR_CUDA (-3)        /* a CUDA runtime call failed                            */
-#define FG_ERR_UNSUPPORTED (-4) /* option not built for the GPU (UseMultigrid)          */
+#define FG_ERR_UNSUPPORTED (-4) /* option not available on this path (see the call)      */
 #define FG_ERR_MASK (-5)        /* S holds a value other than 0 or 1                     */
 #define FG_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up                    */
 #define FG_ERR_NOMEM (-7)       /* device or pinned allocation failed                    */
@@ -70,7 +70,7 @@ typedef struct fg_params {
   float pressure_damping;     /* PressureDamping                              */
   float turbulence_strength;  /* TurbulenceStrength                           */
   float smoke_advection;      /* SmokeAdvection                               */
-  int use_multigrid;          /* UseMultigrid (GPU: FG_ERR_UNSUPPORTED if set) */
+  int use_multigrid;          /* UseMultigrid: the reference's V-cycle, bit for bit */
   int multigrid_levels;       /* MultigridLevels                              */
   int use_bfecc;              /* UseBFECC                                     */
   float relaxation;           /* package var fluid.Relaxation (fluid.go:7-9)  */

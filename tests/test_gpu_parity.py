@@ -51,7 +51,8 @@ def assert_bitwise(g, o, fields=FIELDS, where=""):
 
 
 # ------------------------------------------------------------------ reference tests on the GPU
-@pytest.mark.parametrize("case", rc.ALL_CASES, ids=lambda c: c.__name__)
+@pytest.mark.parametrize("case", rc.ALL_CASES + [rc.case_multigrid_stability],
+                         ids=lambda c: c.__name__)
 def test_reference_case_on_gpu(gpu, case):
     case(lambda d, w, h, hh: gpu.Fluid(d, w, h, hh))
 
@@ -270,12 +271,34 @@ def test_invalid_mask_fails_loudly(gpu):
     assert e.value.code == -5
 
 
-def test_multigrid_reports_unsupported(gpu):
-    f = gpu.Fluid(1.0, 8, 8, 1.0, UseMultigrid=True)
-    f.S[:] = 1.0
-    with pytest.raises(gpu.FluidError) as e:
+@pytest.mark.parametrize("w,h,bfecc", [(70, 45, True), (33, 20, False), (64, 64, True),
+                                         (12, 9, False)])
+def test_multigrid_bitwise(gpu, w, h, bfecc):
+    """UseMultigrid (fluid.go:559-758, 1122-1149): the V-cycle with the
+    reference's serial smoothers and coarse Gauss-Seidel, bit for bit, on
+    odd and even grid sizes, with obstacles and the app's jet."""
+    g, o = both(gpu, w, h, UseMultigrid=True, UseBFECC=bfecc, Confinement=0.1)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        if w > 20:
+            f.SetCircularObstacle(w // 2, h // 2, 4)
+    for _ in range(10):
+        for f in (g, o):
+            scenes.jet_inject(f, speed=2.5)
+            f.Simulate(0.1)
+    assert_bitwise(g, o)
+    assert g.stats()["sweeps"] == o.stats()["sweeps"]
+
+
+def test_multigrid_early_break(gpu):
+    """A field already divergence-free leaves the V-cycle after the first
+    three smoothing sweeps."""
+    g, o = both(gpu, 24, 18, UseMultigrid=True)
+    for f in (g, o):
+        scenes.jet_scene(f)
         f.Simulate(0.1)
-    assert e.value.code == -4
+    assert g.stats()["sweeps"] == o.stats()["sweeps"] == 3
+    assert_bitwise(g, o)
 
 
 @pytest.mark.parametrize("w,h", [(1, 1), (1, 7), (9, 1), (2, 3), (65, 33)])
