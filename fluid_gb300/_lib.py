@@ -57,6 +57,8 @@ SIGNATURES = {
     "fg_mark_dirty": (_c_i, [_vp, ctypes.c_uint]),
     "fg_download": (_c_i, [_vp, ctypes.c_uint]),
     "fg_synchronize": (_c_i, [_vp]),
+    "fg_download_async": (_c_i, [_vp, ctypes.c_uint]),
+    "fg_download_wait": (_c_i, [_vp]),
     "fg_stream": (_vp, [_vp]),
     "fg_simulate": (_c_i, [_vp, _c_f]),
     "fg_get_stats": (_c_i, [_vp, ctypes.POINTER(Stats)]),

@@ -105,9 +105,24 @@ int check_mask(fg_fluid* f) {
 
 // Applies pending mirror uploads and queued tool edits, rebuilds the flag
 // bytes if S changed.  Called at the start of every device operation.
+// Orders device work after a pending asynchronous smoke download: the copy
+// reads the smoke buffer of the step before it; the next operation writes
+// the other buffer and may run beside it unless something writes M in place
+// (an upload, an edit, a smoke source); every later operation waits for it.
+int async_guard(fg_fluid* f) {
+  if (!f->async_pending) return FG_OK;
+  bool in_place = (f->dirty & FG_FIELD_BIT(FG_M)) || f->src_smoke;
+  for (const EditRec& e : f->edits) in_place = in_place || e.field == (uint32_t)FG_M;
+  if (in_place || f->async_ops > 0)
+    CK(f, cudaStreamWaitEvent(f->stream, f->async_ev[1], 0), "async wait");
+  f->async_ops++;
+  return FG_OK;
+}
+
 int flush(fg_fluid* f) {
   int rc = bind(f);
   if (rc) return rc;
+  if ((rc = async_guard(f))) return rc;
   unsigned up = f->dirty;
   if (up & FG_FIELD_BIT(FG_S)) {
     if ((rc = check_mask(f))) {
@@ -397,6 +412,7 @@ int fg_destroy(fg_fluid* f) {
   if (!f) return FG_ERR_INVALID;
   cudaSetDevice(f->device);
   if (f->stream) cudaStreamSynchronize(f->stream);
+  if (f->copy_stream) cudaStreamSynchronize(f->copy_stream);
   clear_graphs(f);
   tape_free(f);
   batch_free(f->batch);
@@ -409,6 +425,9 @@ int fg_destroy(fg_fluid* f) {
   cudaFree(f->parts.keep);
   cudaFree(f->parts.block_keep);
   cudaFree(f->image);
+  if (f->copy_stream) cudaStreamDestroy(f->copy_stream);
+  for (int k = 0; k < 2; ++k)
+    if (f->async_ev[k]) cudaEventDestroy(f->async_ev[k]);
   for (int k = 0; k < FG_NUM_FIELDS; ++k) {
     cudaFree(f->d[k]);
     cudaFree(f->partner[k]);
@@ -488,17 +507,61 @@ int fg_mark_dirty(fg_fluid* f, unsigned mask) {
   return FG_OK;
 }
 
+int fg_download_wait(fg_fluid* f);
+
 int fg_download(fg_fluid* f, unsigned mask) {
   if (is_batch(f)) return batch_unsupported(f);
   if (!f) return FG_ERR_INVALID;
-  int rc = flush(f);
+  int rc = fg_download_wait(f);
   if (rc) return rc;
+  if ((rc = flush(f))) return rc;
   for (int k = 0; k < FG_NUM_FIELDS; ++k)
     if ((mask & FG_FIELD_BIT(k)) && !f->host_valid[k])
       if ((rc = download_field(f, k))) return rc;
   CK(f, cudaStreamSynchronize(f->stream), "download sync");
   for (int k = 0; k < FG_NUM_FIELDS; ++k)
     if (mask & FG_FIELD_BIT(k)) f->host_valid[k] = true;
+  return FG_OK;
+}
+
+// Starts copying the smoke field M of the work enqueued so far into its host
+// mirror on a second stream, so the copy runs beside the next step;
+// fg_download_wait completes it (the mirror is not current until then).
+int fg_download_async(fg_fluid* f, unsigned mask) {
+  if (is_batch(f)) return batch_unsupported(f);
+  if (!f) return FG_ERR_INVALID;
+  if (mask & ~FG_FIELD_BIT(FG_M))
+    return fail(f, FG_ERR_UNSUPPORTED, "asynchronous downloads take the smoke field only");
+  int rc = fg_download_wait(f);
+  if (rc || !mask) return rc;
+  if ((rc = flush(f))) return rc;
+  if (f->host_valid[FG_M]) return FG_OK;
+  if (!f->copy_stream) {
+    CK(f, cudaStreamCreateWithFlags(&f->copy_stream, cudaStreamNonBlocking), "copy stream");
+    for (int k = 0; k < 2; ++k)
+      CK(f, cudaEventCreateWithFlags(&f->async_ev[k], cudaEventDisableTiming), "copy event");
+  }
+  CK(f, cudaEventRecord(f->async_ev[0], f->stream), "copy event");
+  CK(f, cudaStreamWaitEvent(f->copy_stream, f->async_ev[0], 0), "copy event");
+  CK(f, cudaMemcpy2DAsync(f->hm[FG_M], sizeof(float) * f->NY, f->d[FG_M], sizeof(float) * f->P,
+                          sizeof(float) * f->NY, f->NX, cudaMemcpyDeviceToHost, f->copy_stream),
+     "async download");
+  CK(f, cudaEventRecord(f->async_ev[1], f->copy_stream), "copy event");
+  f->async_pending = true;
+  f->async_ops = 0;
+  return FG_OK;
+}
+
+int fg_download_wait(fg_fluid* f) {
+  if (!f) return FG_ERR_INVALID;
+  if (!f->async_pending) return FG_OK;
+  int rc = bind(f);
+  if (rc) return rc;
+  CK(f, cudaEventSynchronize(f->async_ev[1]), "async download");
+  f->async_pending = false;
+  // The mirror holds the copied frame; it is the device's M only if nothing
+  // has run since the copy was issued.
+  f->host_valid[FG_M] = f->async_ops == 0;
   return FG_OK;
 }
 
@@ -822,6 +885,8 @@ int fg_set_sources(fg_fluid* f, int n, const int* is, const int* js, const float
                      cudaMemcpyHostToDevice), "sources upload");
     f->n_src_groups = (int)off.size() - 1;
   }
+  f->src_smoke = false;
+  for (const SourceRec& r : recs) f->src_smoke = f->src_smoke || (r.mode & 12u) != 0;
   f->params_version++;  // the step graph embeds the source list
   return FG_OK;
 }
@@ -1256,7 +1321,9 @@ int tape_usable(fg_fluid* f) {
     return fail(f, FG_ERR_INVALID, "parameters or sources changed during a recorded rollout");
   if (!f->edits.empty() || f->dirty || f->masks_stale)
     return fail(f, FG_ERR_INVALID, "the state was edited during a recorded rollout");
-  return bind(f);
+  int rc = bind(f);
+  if (rc) return rc;
+  return async_guard(f);
 }
 
 float* ckpt_at(fg_fluid* f, int k) { return f->tape->ckpt + (size_t)k * 6 * field_elems(f); }

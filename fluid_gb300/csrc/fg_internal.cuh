@@ -238,6 +238,14 @@ struct fg_fluid {
   uint32_t* image = nullptr;
   // Non-null when this handle is a batch of scenes (fg_batch_create).
   fg::BatchGeom* batch = nullptr;
+  // Asynchronous smoke download (fg_download_async): a copy stream, the event
+  // it starts after and the copy's completion event; device operations after
+  // the first one that follows the copy wait for it.
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t async_ev[2] = {};
+  bool async_pending = false;
+  int async_ops = 0;
+  bool src_smoke = false;  // a persistent source writes M in place
   // Kernel launches enqueued so far (graph replays add the captured count).
   unsigned long long launches = 0;
   // Optional CUDA-event bracket around the main Jacobi launches of a solve.

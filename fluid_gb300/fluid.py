@@ -152,6 +152,14 @@ class Fluid:
     def download(self, mask=ALL_FIELDS):
         self._check(self._L.fg_download(self._h, mask), "fg_download")
 
+    def download_async(self, mask=1 << FIELDS["M"]):
+        """Starts the smoke download beside the next step (download_wait
+        completes it)."""
+        self._check(self._L.fg_download_async(self._h, mask), "fg_download_async")
+
+    def download_wait(self):
+        self._check(self._L.fg_download_wait(self._h), "fg_download_wait")
+
     def mark_dirty(self, mask=ALL_FIELDS):
         self._check(self._L.fg_mark_dirty(self._h, mask), "fg_mark_dirty")
 

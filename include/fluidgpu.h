@@ -125,6 +125,15 @@ int fg_field(fg_fluid* f, int field, float** host_ptr);
 int fg_mark_dirty(fg_fluid* f, unsigned mask);
 /* Copies the device fields in `mask` into their mirrors (waits). */
 int fg_download(fg_fluid* f, unsigned mask);
+/* Starts copying the smoke field (mask = FG_FIELD_BIT(FG_M); other fields:
+ * FG_ERR_UNSUPPORTED) of the work queued so far into its mirror on a second
+ * stream and returns; the copy runs beside the next fg_simulate (which
+ * writes the other smoke buffer).  The mirror is current after
+ * fg_download_wait (fg_download and the next fg_download_async wait too);
+ * do not read or write it before.  For a frame loop that reads the smoke
+ * every frame: simulate, wait, read, start the next copy. */
+int fg_download_async(fg_fluid* f, unsigned mask);
+int fg_download_wait(fg_fluid* f);
 /* Waits for all queued work on the handle's stream. */
 int fg_synchronize(fg_fluid* f);
 /* The handle's CUDA stream (cudaStream_t), for callers that time it. */

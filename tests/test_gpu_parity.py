@@ -382,3 +382,31 @@ def test_karman_512x256_fp32_against_fp64_every_100_steps(gpu):
     for step, err, dg, do in per_step:
         assert err <= 1e-4, (step, err)
         assert abs(dg - do) <= 1e-5, (step, dg, do)
+
+
+def test_async_smoke_download_frames(gpu):
+    """The frame loop with fg_download_async / fg_download_wait: every
+    frame's smoke equals a synchronous download's, with smoke sources and
+    smoke edits writing M in place between frames."""
+    a = gpu.Fluid(1.0, 40, 30, 1.0, auto_sync=False, UseBFECC=True)
+    b = gpu.Fluid(1.0, 40, 30, 1.0, auto_sync=False, UseBFECC=True)
+    for f in (a, b):
+        scenes.fast_walls(f)
+        f.mark_dirty()
+        rows = np.array(list(scenes.jet_rows(f)), np.int32)
+        f.set_sources(np.ones_like(rows), rows, u=2.0, v=0.0, smoke=0.5,
+                      mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY | f.SRC_ADD_SMOKE)
+    prev = None
+    for k in range(12):
+        for f in (a, b):
+            if k % 4 == 3:
+                f.AddSmoke(10, 10, 1.0)
+            f.Simulate(0.1)
+        a.download_wait()
+        if prev is not None:
+            assert np.array_equal(a.M.view(np.uint32), prev.view(np.uint32)), k
+        a.download_async()
+        b.download(1 << gpu.FIELDS["M"])
+        prev = b.M.copy()
+    a.download_wait()
+    assert np.array_equal(a.M.view(np.uint32), prev.view(np.uint32))
