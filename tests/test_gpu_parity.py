@@ -410,3 +410,28 @@ def test_async_smoke_download_frames(gpu):
         prev = b.M.copy()
     a.download_wait()
     assert np.array_equal(a.M.view(np.uint32), prev.view(np.uint32))
+
+
+def test_jet128_against_golden_fixtures(gpu):
+    """The 128x128 jet of the golden fixtures (200 steps, 40 iterations, the
+    reference's early exit): the GPU's reference scheme equals the FP32
+    fixture bit for bit, and stays within 1e-4 of max |U| (velocity) of the
+    FP64 fixture."""
+    import os
+    import sys
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    import make_golden
+
+    gold = np.load(os.path.join(here, "jet128_fp32.npz"))
+    f, trace = make_golden.run(lambda *a: gpu.Fluid(*a))
+    for k in ("U", "V", "M", "p", "newU", "newV", "newM", "S"):
+        a = np.asarray(getattr(f, k))
+        assert np.array_equal(a.view(np.uint32), gold[k].view(np.uint32)), k
+    gold64 = np.load(os.path.join(here, "jet128_fp64.npz"))
+    scale = float(np.abs(gold64["U"]).max())
+    err = max(float(np.abs(f.U.astype(np.float64) - gold64["U"]).max()),
+              float(np.abs(f.V.astype(np.float64) - gold64["V"]).max())) / scale
+    print("jet128 after 200 steps: velocity max-abs error vs FP64 / max|U| = %.3e" % err)
+    assert err <= 1e-4, err

@@ -98,3 +98,25 @@ def test_refinement_reduces_fp64_residual():
     # its residual and the divergence of the projected field.
     assert b.stats()["resid_l2"] < a.stats()["resid_l2"]
     assert b.stats()["div_l2_post"] < a.stats()["div_l2_post"]
+
+
+def test_oracle_reproduces_golden_jet128():
+    """The committed fixtures of the 128x128 jet (tests/golden/make_golden.py)
+    pin the oracle: the FP32 restatement reproduces them bit for bit and the
+    FP64 one exactly."""
+    import os
+    import sys
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    import make_golden
+
+    gold = np.load(os.path.join(here, "jet128_fp32.npz"))
+    f, trace = make_golden.run(lambda *a: OracleFluid(*a, prec=32))
+    for k in ("U", "V", "M", "p", "newU", "newV", "newM", "S"):
+        assert np.array_equal(np.asarray(getattr(f, k)).view(np.uint32), gold[k].view(np.uint32)), k
+    assert np.array_equal(trace, gold["max_u_every_20"])
+    gold64 = np.load(os.path.join(here, "jet128_fp64.npz"))
+    g, _ = make_golden.run(lambda *a: OracleFluid(*a, prec=64))
+    for k in ("U", "V", "M", "p"):
+        assert np.array_equal(np.asarray(getattr(g, k)), gold64[k]), k
