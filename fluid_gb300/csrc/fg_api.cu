@@ -356,6 +356,7 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
     return code;
   };
   if (cudaGetDevice(&f->device) != cudaSuccess) return bail(FG_ERR_CUDA);
+  init_jacobi_tma();
   if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(FG_ERR_CUDA);
   for (int k = 0; k < 2; ++k) {
@@ -387,6 +388,9 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
   f->n_slots = kSlots;
   if (cudaMalloc(&f->pctl, pctl_bytes(f->n_slots)) != cudaSuccess) return bail(FG_ERR_NOMEM);
   if (cudaMalloc(&f->ectl, pctl_bytes(f->n_slots)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  if (cudaMalloc((void**)&f->tile_done, sizeof(int) * ((size_t)jacobi_tile_count(f->NX, f->NY) + 1)) !=
+      cudaSuccess)
+    return bail(FG_ERR_NOMEM);
   cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream);
   cudaMemsetAsync(f->ectl, 0, pctl_bytes(f->n_slots), f->stream);
   cudaMemsetAsync(f->dstats, 0, sizeof(DevStats), f->stream);
@@ -445,6 +449,7 @@ int fg_destroy(fg_fluid* f) {
   cudaFree(f->dstats);
   cudaFree(f->pctl);
   cudaFree(f->ectl);
+  cudaFree(f->tile_done);
   for (int k = 0; k < 2; ++k) {
     cudaFree(f->edit_dev[k]);
     cudaFree(f->edit_off_dev[k]);
@@ -660,7 +665,7 @@ int fg_get_stats(fg_fluid* f, fg_stats* out) {
   out->smoke_mass = s.smoke_mass;
   out->last_maxdiv = s.last_maxdiv;
   out->sweeps = s.sweeps;
-  return FG_OK;
+  return s.timeout ? fail(f, FG_ERR_TIMEOUT, "a device-side wait of the last step gave up") : FG_OK;
 }
 
 // ------------------------------------------------------------------ stages

@@ -119,7 +119,7 @@ struct DevStats {  // device-side accumulation target (finalised per step)
   double smoke_mass;
   double last_maxdiv;
   int sweeps;
-  int pad;
+  int timeout;  // 1: a bounded device-side wait of the step gave up
 };
 
 // ---------------------------------------------------------------- batches
@@ -186,6 +186,7 @@ struct fg_fluid {
   int n_partials = 0;          // floats
   fg::DevStats* dstats = nullptr;
   void* pctl = nullptr;   // control block of the main Jacobi solve (k_pressure.cu PCtl)
+  int* tile_done = nullptr;  // dataflow Jacobi kernel: per-tile phase flags + item counter
   void* ectl = nullptr;   // control block of the FP64-residual correction solve
   int n_slots = 0;        // launch slots per control block
   float* copy_tmp = nullptr;        // fg_copy_border staging (2 fields)
@@ -301,6 +302,8 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
 cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt);
 // K Jacobi sweeps of A x = b from x = 0 (no early exit); ctl->sel names the
 // buffer holding x.
+void init_jacobi_tma();
+int jacobi_tile_count(int NX, int NY);
 cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const float* bw, float* x0,
                                 float* x1, int iters);
 // Copies the last solve's potential to dst.

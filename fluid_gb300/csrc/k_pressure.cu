@@ -20,6 +20,10 @@
 //    there, so HBM sees one read and one write of phi per launch.  Optional
 //    outer correction: an FP64 residual of the FP32 iterate, a correction
 //    solve on it, phi += e.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <atomic>
 #include <mutex>
 
 #include "fg_batch.cuh"
@@ -675,6 +679,417 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
 }
 
 
+// ------------------------------------------------------------------ TMA-fed Jacobi
+// The full 8-sweep launches without residual check, as a persistent kernel:
+// each block (two per SM) walks tiles t = blockIdx.x, + gridDim.x, ...; the
+// tensor memory accelerator copies the next tile's phi, w and w*b boxes (64 x
+// 128, zero outside the arrays) into shared memory while the block sweeps the
+// current tile in registers, so the loads no longer sit in front of the
+// sweeps.  Same per-cell arithmetic as k_jacobi_rb, same results.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* tm, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+constexpr int TILE_FLOATS = RI * RJ;  // one 64 x 128 box
+constexpr unsigned long long MBAR_WAIT_NS = 1000000000ull;  // 1 s
+constexpr int MBAR_MAX_TRIES = 1 << 24;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for phase `parity` of the barrier for at most about a second (and a
+// bounded number of polls); false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (int it = 0; it < MBAR_MAX_TRIES; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > MBAR_WAIT_NS) return false;
+  }
+  return false;
+}
+
+// The TMAX sweeps of one tile in registers, with the arithmetic of
+// jacobi_tile.
+template <bool OMEGA1>
+__device__ __forceinline__ void tile_sweeps(float (&x)[RT][JT], const float (&w)[RT][JT],
+                                            const float (&bw)[RT][JT], float om1,
+                                            float4 (&xch)[2][2][NWARP][32], int warp, int lane) {
+#pragma unroll
+  for (int sw = 0; sw < TMAX; ++sw) {
+    const int buf = sw & 1;
+    xch[buf][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
+    xch[buf][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
+    __syncthreads();
+    float4 u4 = warp > 0 ? xch[buf][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 d4 = warp < NWARP - 1 ? xch[buf][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
+#pragma unroll
+    for (int r = 0; r < RT; ++r) {
+      float lf = __shfl_up_sync(0xffffffffu, x[r][JT - 1], 1);
+      float rt = __shfl_down_sync(0xffffffffu, x[r][0], 1);
+      float nxt[JT];
+      if (r < RT - 1) {
+#pragma unroll
+        for (int q = 0; q < JT; ++q) nxt[q] = x[r + 1][q];
+      } else {
+        nxt[0] = d4.x; nxt[1] = d4.y; nxt[2] = d4.z; nxt[3] = d4.w;
+      }
+      float nw[JT];
+#pragma unroll
+      for (int q = 0; q < JT; ++q) {
+        float left = q == 0 ? lf : x[r][q - 1];
+        float right = q == JT - 1 ? rt : x[r][q + 1];
+        float nb = prev[q] + nxt[q] + left + right;  // (i-1) + (i+1) + (j-1) + (j+1)
+        float y = __fmaf_rn(w[r][q], nb, bw[r][q]);
+        if (!OMEGA1) y = __fmaf_rn(om1, x[r][q], y);
+        nw[q] = y;
+      }
+#pragma unroll
+      for (int q = 0; q < JT; ++q) {
+        prev[q] = x[r][q];
+        x[r][q] = nw[q];
+      }
+    }
+  }
+}
+
+template <bool OMEGA1>
+__global__ void __launch_bounds__(TB_THREADS, 2)
+    k_jacobi_tma(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw,
+                 const __grid_constant__ CUtensorMap tmb, float* __restrict__ dst, float om1,
+                 PCtl* ctl, int k, int t0, int out_sel, int zero_init, Grid g, int ntx,
+                 int ntiles, int* err) {
+  extern __shared__ __align__(128) float4 tbuf4[];  // [3][RI][RJ] floats: phi, w, w*b
+  float* tbuf = reinterpret_cast<float*>(tbuf4);
+  __shared__ float4 xch[2][2][NWARP][32];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_skip;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    s_skip = ctl->stop;
+    if (!s_skip) mbar_init(&bar, 1);
+  }
+  __syncthreads();
+  if (s_skip) return;
+  const unsigned bytes = (zero_init ? 2u : 3u) * TILE_FLOATS * 4u;
+  auto issue = [&](int t) {
+    const int ty = t / ntx, tx = t - ty * ntx;
+    const int x = tx * OJ - TMAX, y = ty * OI - TMAX;  // x: a multiple of 4 floats (16 bytes)
+    // Order this block's earlier shared-memory reads before the copy's writes.
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bar, bytes);
+    if (!zero_init) tma_load_2d(tbuf, &tmx, x, y, &bar);
+    tma_load_2d(tbuf + TILE_FLOATS, &tmw, x, y, &bar);
+    tma_load_2d(tbuf + 2 * TILE_FLOATS, &tmb, x, y, &bar);
+  };
+  if (tid == 0 && (int)blockIdx.x < ntiles) issue(blockIdx.x);
+  unsigned parity = 0;
+  const bool own_col = lane * JT >= TMAX && lane * JT < RJ - TMAX;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const bool landed = mbar_wait_bounded(&bar, parity);
+    if (__syncthreads_or(!landed)) {
+      // A copy did not land in time (the whole block agrees): flag it, give
+      // it one more bounded wait, stop.
+      if (tid == 0) {
+        atomicExch(&ctl->pad[0], 1);
+        if (err) atomicExch(err, 1);
+      }
+      if (!landed) mbar_wait_bounded(&bar, parity);
+      return;
+    }
+    parity ^= 1u;
+    const int ty = t / ntx, tx = t - ty * ntx;
+    const int gi0 = ty * OI - TMAX + warp * RT;
+    const int gj = tx * OJ - TMAX + lane * JT;
+    float x[RT][JT], w[RT][JT], bw[RT][JT];
+#pragma unroll
+    for (int r = 0; r < RT; ++r) {
+      const int o = (warp * RT + r) * RJ + lane * JT;
+      float4 a = zero_init ? make_float4(0.f, 0.f, 0.f, 0.f)
+                           : *reinterpret_cast<const float4*>(tbuf + o);
+      float4 ww = *reinterpret_cast<const float4*>(tbuf + TILE_FLOATS + o);
+      float4 bb = *reinterpret_cast<const float4*>(tbuf + 2 * TILE_FLOATS + o);
+      x[r][0] = a.x; x[r][1] = a.y; x[r][2] = a.z; x[r][3] = a.w;
+      w[r][0] = ww.x; w[r][1] = ww.y; w[r][2] = ww.z; w[r][3] = ww.w;
+      bw[r][0] = bb.x; bw[r][1] = bb.y; bw[r][2] = bb.z; bw[r][3] = bb.w;
+#pragma unroll
+      for (int q = 0; q < JT; ++q)
+        if (gj + q >= g.NY) {  // the pitch padding (outside the grid: zero-filled)
+          x[r][q] = 0.0f;
+          w[r][q] = 0.0f;
+          bw[r][q] = 0.0f;
+        }
+    }
+    __syncthreads();  // the boxes are in registers: the buffer takes the next tile
+    if (tid == 0 && t + (int)gridDim.x < ntiles) issue(t + gridDim.x);
+    tile_sweeps<OMEGA1>(x, w, bw, om1, xch, warp, lane);
+    if (own_col && warp >= TMAX / RT && warp < NWARP - TMAX / RT) {
+#pragma unroll
+      for (int r = 0; r < RT; ++r) {
+        int gi = gi0 + r;
+        if (gi >= g.NX || gj >= g.NY) continue;
+        size_t c = (size_t)gi * g.P + gj;
+        if (gj + JT <= g.NY) {
+          *reinterpret_cast<float4*>(dst + c) = make_float4(x[r][0], x[r][1], x[r][2], x[r][3]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < JT; ++q)
+            if (gj + q < g.NY) dst[c + q] = x[r][q];
+        }
+      }
+    }
+  }
+  if (tid == 0 && blockIdx.x == 0) {
+    ctl->sweeps = t0 + TMAX;
+    ctl->last_launch = k;
+    ctl->sel = out_sel;
+  }
+}
+
+// ------------------------------------------------------------------ dataflow Jacobi
+// A whole fixed-count solve (nphase launches of TMAX sweeps) as one
+// cooperative persistent kernel.  Items (phase, tile) are numbered phase
+// by phase and handed out by an atomic counter (done[ntiles]): a block
+// claims its next item while it sweeps the current one, so the tensor
+// memory accelerator copies the next boxes meanwhile.  Item (ph, t) starts
+// once the up to nine tiles whose owned cells its region reads have
+// finished phase ph - 1 (done[n] >= ph; done[t] = ph + 1 is published with
+// release semantics after the tile's stores).  That one wait covers both
+// hazards of the ping-pong buffers: the neighbours' phase ph - 1 results
+// are in src(ph), and they no longer read src(ph - 1), which this item
+// overwrites.  Items are claimed in increasing order and depend only on
+// smaller ones, so the smallest unfinished item can always proceed (all
+// blocks are resident: cooperative launch).  No block idles at a launch
+// boundary or in a partial last wave.  Same per-cell arithmetic, same
+// results.
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Whether the tiles around t (3 x 3, clipped to the tile grid) finished
+// phase ph - 1.  All 32 lanes of a warp call it: lane l < 9 reads the flag
+// of neighbour (l / 3 - 1, l % 3 - 1) with a relaxed load followed by an
+// acquire fence.
+__device__ __forceinline__ bool flow_ready_warp(const int* done, int ph, int t, int ntx, int nty,
+                                                int lane) {
+  bool ok = true;
+  if (ph > 0 && lane < 9) {
+    const int ty = t / ntx, tx = t - ty * ntx;
+    const int y = ty + lane / 3 - 1, x = tx + lane % 3 - 1;
+    if (y >= 0 && y < nty && x >= 0 && x < ntx) {
+      int v;
+      asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(done + y * ntx + x)
+                   : "memory");
+      ok = v >= ph;
+      asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    }
+  }
+  return __all_sync(0xffffffffu, ok);
+}
+
+template <bool OMEGA1>
+__global__ void __launch_bounds__(TB_THREADS, 2)
+    k_jacobi_flow(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
+                  const __grid_constant__ CUtensorMap tmw, const __grid_constant__ CUtensorMap tmb,
+                  float* __restrict__ x0, float* __restrict__ x1, float om1, PCtl* ctl,
+                  int* __restrict__ done, int nphase, int zero_first, Grid g, int ntx, int nty,
+                  int* err) {
+  extern __shared__ __align__(128) float4 tbuf4[];  // [3][RI][RJ] floats: phi, w, w*b
+  float* tbuf = reinterpret_cast<float*>(tbuf4);
+  __shared__ float4 xch[2][2][NWARP][32];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_item;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ntiles = ntx * nty, total = ntiles * nphase;
+  int* counter = done + ntiles;
+  // Thread 0: copy item i's boxes (phi of its phase's source, w, w*b).
+  auto issue = [&](int i) {
+    const int ph = i / ntiles, t = i - ph * ntiles;
+    const int ty = t / ntx, tx = t - ty * ntx;
+    const int x = tx * OJ - TMAX, y = ty * OI - TMAX;  // x: a multiple of 4 floats (16 bytes)
+    const bool zi = zero_first && ph == 0;
+    // The neighbours' (generic) stores, acquired above, before the copy's
+    // reads; this block's earlier shared-memory reads before its writes.
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bar, (zi ? 2u : 3u) * TILE_FLOATS * 4u);
+    if (!zi) tma_load_2d(tbuf, (ph & 1) ? &tm1 : &tm0, x, y, &bar);
+    tma_load_2d(tbuf + TILE_FLOATS, &tmw, x, y, &bar);
+    tma_load_2d(tbuf + 2 * TILE_FLOATS, &tmb, x, y, &bar);
+  };
+  // Warp 0 (all lanes): whether item i's inputs are final.
+  auto ready = [&](int i) {
+    const int ph = i / ntiles;
+    return flow_ready_warp(done, ph, i - ph * ntiles, ntx, nty, lane);
+  };
+  // Warp 0: bounded wait (about a second) for item i's inputs.
+  auto wait_ready = [&](int i) -> bool {
+    if (ready(i)) return true;
+    const unsigned long long t0 = global_ns();
+    for (int it = 0; it < MBAR_MAX_TRIES; ++it) {
+      if (ready(i)) return true;
+      if (global_ns() - t0 > MBAR_WAIT_NS) return false;
+    }
+    return false;
+  };
+  int fail = 0;            // thread 0: a wait gave up
+  bool in_flight = false;  // thread 0: a copy issued and not consumed
+  if (warp == 0) {
+    int i = 0;
+    if (lane == 0) {
+      mbar_init(&bar, 1);
+      i = atomicAdd(counter, 1);
+    }
+    i = __shfl_sync(0xffffffffu, i, 0);
+    const bool ok = i < total ? wait_ready(i) : true;
+    if (lane == 0) {
+      if (i < total) {
+        if (ok) {
+          issue(i);
+          in_flight = true;
+        } else {
+          fail = 1;
+        }
+      }
+      s_item = i;
+    }
+  }
+  unsigned parity = 0;
+  const bool own_col = lane * JT >= TMAX && lane * JT < RJ - TMAX;
+  while (true) {
+    if (__syncthreads_or(fail)) break;
+    const int item = s_item;
+    if (item >= total) break;
+    const bool landed = mbar_wait_bounded(&bar, parity);
+    if (__syncthreads_or(!landed)) {
+      if (tid == 0) fail = 1;
+      break;
+    }
+    if (tid == 0) in_flight = false;
+    parity ^= 1u;
+    const int ph = item / ntiles, t = item - ph * ntiles;
+    const int ty = t / ntx, tx = t - ty * ntx;
+    const int gi0 = ty * OI - TMAX + warp * RT;
+    const int gj = tx * OJ - TMAX + lane * JT;
+    const bool zi = zero_first && ph == 0;
+    float x[RT][JT], w[RT][JT], bw[RT][JT];
+#pragma unroll
+    for (int r = 0; r < RT; ++r) {
+      const int o = (warp * RT + r) * RJ + lane * JT;
+      float4 a = zi ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4*>(tbuf + o);
+      float4 ww = *reinterpret_cast<const float4*>(tbuf + TILE_FLOATS + o);
+      float4 bb = *reinterpret_cast<const float4*>(tbuf + 2 * TILE_FLOATS + o);
+      x[r][0] = a.x; x[r][1] = a.y; x[r][2] = a.z; x[r][3] = a.w;
+      w[r][0] = ww.x; w[r][1] = ww.y; w[r][2] = ww.z; w[r][3] = ww.w;
+      bw[r][0] = bb.x; bw[r][1] = bb.y; bw[r][2] = bb.z; bw[r][3] = bb.w;
+#pragma unroll
+      for (int q = 0; q < JT; ++q)
+        if (gj + q >= g.NY) {  // the pitch padding (outside the grid: zero-filled)
+          x[r][q] = 0.0f;
+          w[r][q] = 0.0f;
+          bw[r][q] = 0.0f;
+        }
+    }
+    __syncthreads();  // the boxes are in registers: the buffer takes the next item
+    int next = total;
+    bool pending = false;
+    if (warp == 0) {
+      if (lane == 0) next = atomicAdd(counter, 1);
+      next = __shfl_sync(0xffffffffu, next, 0);
+      const bool ok = next < total ? ready(next) : true;
+      if (lane == 0 && next < total) {
+        if (ok) {
+          issue(next);
+          in_flight = true;
+        } else {
+          pending = true;  // issued after this tile, once its inputs are final
+        }
+      }
+      pending = __shfl_sync(0xffffffffu, pending, 0);
+    }
+    tile_sweeps<OMEGA1>(x, w, bw, om1, xch, warp, lane);
+    float* dst = (ph & 1) ? x0 : x1;
+    if (own_col && warp >= TMAX / RT && warp < NWARP - TMAX / RT) {
+#pragma unroll
+      for (int r = 0; r < RT; ++r) {
+        int gi = gi0 + r;
+        if (gi >= g.NX || gj >= g.NY) continue;
+        size_t c = (size_t)gi * g.P + gj;
+        if (gj + JT <= g.NY) {
+          *reinterpret_cast<float4*>(dst + c) = make_float4(x[r][0], x[r][1], x[r][2], x[r][3]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < JT; ++q)
+            if (gj + q < g.NY) dst[c + q] = x[r][q];
+        }
+      }
+    }
+    __syncthreads();  // the tile's stores precede its publication
+    if (warp == 0) {
+      if (lane == 0) {
+        __threadfence();
+        st_release(done + t, ph + 1);
+      }
+      if (pending) {
+        const bool ok = wait_ready(next);
+        if (lane == 0) {
+          if (ok) {
+            issue(next);
+            in_flight = true;
+          } else {
+            fail = 1;
+          }
+        }
+      }
+      if (lane == 0) s_item = next;
+    }
+  }
+  if (tid == 0) {
+    if (fail) {
+      atomicExch(&ctl->pad[0], 1);
+      if (err) atomicExch(err, 1);
+    }
+    if (in_flight) mbar_wait_bounded(&bar, parity);  // a copy still landing
+    if (blockIdx.x == 0 && nphase > 0) {
+      ctl->sweeps = nphase * TMAX;
+      ctl->last_launch = nphase - 1;
+      ctl->sel = ((nphase - 1) & 1) ? 0 : 1;
+    }
+  }
+}
+
 // Final potential at cell c: the main iterate, plus the outer correction on
 // active cells when one ran (phi = phi + e, fluid.go's p accumulation aside).
 __device__ __forceinline__ float phi_final(const float* __restrict__ phi,
@@ -899,11 +1314,144 @@ __global__ void k_finish_parallel(const PCtl* __restrict__ ctl, DevStats* st) {
 
 size_t pctl_bytes(int n_slots) { return sizeof(PCtl) + sizeof(unsigned) * (size_t)n_slots; }
 
+// Tensor maps of the TMA-fed Jacobi kernel: a 2D float array of rows x
+// pitch, boxes of 64 rows x 128 columns, zero outside.  false when the
+// driver entry point or the encoding is unavailable (the plain kernel runs).
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+static int g_sms = 0;
+static std::once_flag g_tma_once;
+static std::atomic<bool> g_tma_init{false};
+static int g_flow_per_sm = 0;
+
+static bool encode_box_map(CUtensorMap* tm, const float* base, int rows, int pitch) {
+  if (!g_encode || (reinterpret_cast<uintptr_t>(base) & 15) || (pitch % 4) != 0) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)RJ, (cuuint32_t)RI};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// Resolves the tensor-map encoder, the SM count and the kernel's shared
+// memory limit once per process (outside any stream capture).
+void init_jacobi_tma() {
+  std::call_once(g_tma_once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      g_sms = n;
+    const int smem = 3 * TILE_FLOATS * (int)sizeof(float);
+    if (cudaFuncSetAttribute(k_jacobi_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_jacobi_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+      g_sms = 0;
+    // Blocks of the dataflow kernel that fit on one SM (co-residency bound).
+    int b1 = 0, b2 = 0;
+    if (cudaFuncSetAttribute(k_jacobi_flow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) == cudaSuccess &&
+        cudaFuncSetAttribute(k_jacobi_flow<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_jacobi_flow<true>, TB_THREADS,
+                                                      smem) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_jacobi_flow<false>, TB_THREADS,
+                                                      smem) == cudaSuccess)
+      g_flow_per_sm = b1 < b2 ? b1 : b2;
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
+      g_flow_per_sm = 0;
+    cudaGetLastError();
+    g_tma_init.store(true);
+  });
+}
+
+// Launches one full, unchecked Jacobi launch through the TMA-fed kernel;
+// false (nothing launched) when the tensor maps cannot be made.
+static bool launch_jacobi_tma(cudaStream_t st, const Grid& g, PCtl* ctl, const float* src,
+                              float* dst, const float* W, const float* BW, float om1, bool o1,
+                              int k, int t0, int sel, int zero_init, int* err) {
+  if (!g_tma_init.load()) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusActive;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+      return false;
+    init_jacobi_tma();
+  }
+  CUtensorMap tmx, tmw, tmb;
+  if (!encode_box_map(&tmx, src, g.NX, g.P) || !encode_box_map(&tmw, W, g.NX, g.P) ||
+      !encode_box_map(&tmb, BW, g.NX, g.P))
+    return false;
+  const int nsm = g_sms;
+  if (nsm <= 0) return false;
+  const int ntx = (g.NY + OJ - 1) / OJ, nty = (g.NX + OI - 1) / OI;
+  const int ntiles = ntx * nty;
+  const int grid = ntiles < 2 * nsm ? ntiles : 2 * nsm;
+  const size_t smem = 3 * (size_t)TILE_FLOATS * sizeof(float);
+  if (o1)
+    k_jacobi_tma<true><<<grid, TB_THREADS, smem, st>>>(tmx, tmw, tmb, dst, om1, ctl, k, t0, sel,
+                                                       zero_init, g, ntx, ntiles, err);
+  else
+    k_jacobi_tma<false><<<grid, TB_THREADS, smem, st>>>(tmx, tmw, tmb, dst, om1, ctl, k, t0, sel,
+                                                        zero_init, g, ntx, ntiles, err);
+  return true;
+}
+
 inline int clamp_tb(int t) { return t < 1 ? 1 : (t > TMAX ? TMAX : t); }
 
 int jacobi_launches(const fg_fluid* f, int iters) {
   int T = clamp_tb(f->prm.tb_depth);
   return (iters + T - 1) / T;
+}
+
+int jacobi_tile_count(int NX, int NY) {
+  return ((NY + OJ - 1) / OJ) * ((NX + OI - 1) / OI);
+}
+
+// Launches the first `nphase` full phases of a fixed-count solve as one
+// cooperative dataflow kernel (x0 -> x1 -> x0 ...); `done` holds one flag
+// per tile and the item counter.  false (nothing launched) when the grid is
+// below one tile per SM, the flags are missing, or the tensor maps or the
+// cooperative launch are unavailable.
+static bool launch_jacobi_flow(cudaStream_t st, const Grid& g, PCtl* ctl, float* x0, float* x1,
+                               const float* W, const float* BW, float om1, bool o1, int nphase,
+                               int* done, int* err) {
+  if (!done || nphase < 2 || !g_tma_init.load() || g_flow_per_sm <= 0 || g_sms <= 0) return false;
+  const int ntx = (g.NY + OJ - 1) / OJ, nty = (g.NX + OI - 1) / OI;
+  const int ntiles = ntx * nty;
+  if (ntiles < g_sms) return false;
+  CUtensorMap tm0, tm1, tmw, tmb;
+  if (!encode_box_map(&tm0, x0, g.NX, g.P) || !encode_box_map(&tm1, x1, g.NX, g.P) ||
+      !encode_box_map(&tmw, W, g.NX, g.P) || !encode_box_map(&tmb, BW, g.NX, g.P))
+    return false;
+  // The tile flags and the item counter.
+  if (cudaMemsetAsync(done, 0, sizeof(int) * ((size_t)ntiles + 1), st) != cudaSuccess) return false;
+  const int cap = g_flow_per_sm * g_sms;
+  const int grid = ntiles < cap ? ntiles : cap;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(TB_THREADS);
+  cfg.dynamicSmemBytes = 3 * (size_t)TILE_FLOATS * sizeof(float);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const int zero_first = 1;
+  cudaError_t e = o1 ? cudaLaunchKernelEx(&cfg, k_jacobi_flow<true>, tm0, tm1, tmw, tmb, x0, x1,
+                                          om1, ctl, done, nphase, zero_first, g, ntx, nty, err)
+                     : cudaLaunchKernelEx(&cfg, k_jacobi_flow<false>, tm0, tm1, tmw, tmb, x0, x1,
+                                          om1, ctl, done, nphase, zero_first, g, ntx, nty, err);
+  return e == cudaSuccess;
 }
 
 // Enqueues `iters` Jacobi sweeps of A x = b from x = 0 in launches of T
@@ -917,12 +1465,22 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
                                   float* x1, int iters, int T, float om, int check, float tol,
                                   int* n_launched, const float* mphi0 = nullptr,
                                   const float* mphi1 = nullptr, const PCtl* mctl = nullptr,
-                                  float* rhs_e = nullptr, float* bwe = nullptr) {
+                                  float* rhs_e = nullptr, float* bwe = nullptr,
+                                  int* err = nullptr, int* done = nullptr) {
   float om1 = 1.0f - om;
   bool o1 = om1 == 0.0f;
   dim3 gr((g.NY + OJ - 1) / OJ, (g.NX + OI - 1) / OI);
   int nlaunch = (iters + T - 1) / T;
-  for (int k = 0; k < nlaunch; ++k) {
+  int k0 = 0, kernels = 0;
+  // Fixed sweep counts in full launches: the leading full phases as one
+  // dataflow kernel where the grid is large enough.
+  if (!check && !mphi0 && T == TMAX && iters / TMAX >= 2 &&
+      launch_jacobi_flow(st, g, ctl, x0, x1, W, bw, om1, o1, iters / TMAX, done, err)) {
+    k0 = iters / TMAX;
+    kernels = 1;
+  }
+  for (int k = k0; k < nlaunch; ++k) {
+    ++kernels;
     int t0 = k * T;
     int ns = iters - t0 < T ? iters - t0 : T;
     const float* src = (k & 1) ? x1 : x0;
@@ -934,6 +1492,9 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
     const float* bk = rinit ? b : (mphi0 ? rhs_e : b);
     const float* bwk = mphi0 && k > 0 ? bwe : bw;
     float* re = rinit && nlaunch > 1 ? rhs_e : nullptr;
+    if (full && !check && !rinit && !mphi0 &&
+        launch_jacobi_tma(st, g, ctl, src, dst, W, bwk, om1, o1, k, t0, sel, zi, err))
+      continue;
 #define FG_JAC(O, F, C, R)                                                                      \
   k_jacobi_rb<O, F, C, R><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bwk, bk, flags, om1, ctl, k, t0, \
                                                      ns, tol, sel, zi, g, mphi0, mphi1, mctl, re, \
@@ -950,7 +1511,7 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
     }
 #undef FG_JAC
   }
-  *n_launched = nlaunch;
+  *n_launched = kernels;
   return cudaGetLastError();
 }
 
@@ -997,7 +1558,9 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
                        f->phi, f->phi2, (const PCtl*)f->pctl, f->rhs_e, f->bwe);
   else
     e = enqueue_jacobi(f->stream, f->g, ctl, b, bw, f->wgt, f->flags, x0, x1, iters, T,
-                       f->prm.jacobi_omega * f->prm.pressure_damping, check, f->prm.tolerance, &n);
+                       f->prm.jacobi_omega * f->prm.pressure_damping, check, f->prm.tolerance, &n,
+                       nullptr, nullptr, nullptr, nullptr, nullptr, &f->dstats->timeout,
+                       f->tile_done);
   count(f, n);
   if (e != cudaSuccess) return e;
   if (prof) {

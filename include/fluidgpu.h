@@ -142,7 +142,8 @@ void* fg_stream(fg_fluid* f);
 /* (*Fluid).Simulate(dt) -- fluid.go:79-109.  Enqueues one step; returns when
  * it is queued.  Results are read with fg_download / fg_get_stats. */
 int fg_simulate(fg_fluid* f, float dt);
-/* Statistics of the last step or stage (waits). */
+/* Statistics of the last step or stage (waits).  FG_ERR_TIMEOUT (with the
+ * statistics filled in) when a bounded device-side wait of that step gave up. */
 int fg_get_stats(fg_fluid* f, fg_stats* out);
 
 /* Stage entry points (the unexported methods the reference tests call). */

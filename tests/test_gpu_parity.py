@@ -148,6 +148,39 @@ def test_jacobi_refinement_bitwise(gpu):
     assert sg["resid_l2"] == pytest.approx(so["resid_l2"], rel=1e-9)
 
 
+@pytest.mark.parametrize("w,h", [(70, 45), (333, 222), (1100, 1500)])
+def test_jacobi_fixed_sweeps_bitwise(gpu, w, h):
+    """Fixed sweep counts in full 8-sweep launches: the persistent kernel fed
+    by tensor-memory-accelerator copies (at 1100x1500, 322 tiles: more than
+    one tile per block) against the oracle, bit for bit."""
+    g, o = both(gpu, w, h, scheme=1, num_iters=40, tb_depth=8, early_exit=False, UseBFECC=True)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        f.SetCircularObstacle(w // 3, h // 2, max(3, min(w, h) // 8))
+    for _ in range(3):
+        for f in (g, o):
+            scenes.jet_inject(f, speed=3.0)
+            f.Simulate(0.1)
+    assert_bitwise(g, o, where="%dx%d" % (w, h))
+
+
+def test_jacobi_fixed_sweeps_2048_matches_checked_launches(gpu):
+    """At 2046x2046 (817 tiles) the unchecked launches give the same fields
+    as the residual-checking kernel with a tolerance that never stops."""
+    fs = [gpu.Fluid(1.0, 2046, 2046, 1.0, scheme=1, num_iters=200, tb_depth=8, UseBFECC=True,
+                    early_exit=ee, tolerance=0.0) for ee in (False, True)]
+    for f in fs:
+        scenes.cavity_scene(f)
+        scenes.random_state(f, seed=11)
+    for _ in range(2):
+        for f in fs:
+            f.Simulate(0.05)
+    for k in ("U", "V", "p", "M"):
+        a, b = getattr(fs[0], k), getattr(fs[1], k)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), k
+    assert fs[0].stats()["sweeps"] == fs[1].stats()["sweeps"] == 200
+
+
 def test_jacobi_against_fp64_oracle(gpu):
     """Per-step error of the FP32 GPU step against the FP64 oracle."""
     g = gpu.Fluid(1.0, 96, 64, 1.0, scheme=1, num_iters=100, tb_depth=8, UseBFECC=True,
