@@ -605,7 +605,8 @@ def run_ours(args):
     peak, peak_kind = measured_hbm()
     tr = committed_traffic()
     roofline = {
-        "kernel": "k_jacobi_rb (8 Jacobi sweeps per launch)",
+        "kernel": "k_jacobi_flow (one cooperative launch per solve: 25 phases of 8 sweeps; "
+                  "figures per phase)",
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "peak_source": peak_kind + " MEASURED_PEAKS.json hbm_gbs"
         if peak_kind == "measured" else "fallback 6.8 TB/s",

@@ -24,6 +24,7 @@
 #include <cudaTypedefs.h>
 
 #include <atomic>
+#include <climits>
 #include <mutex>
 
 #include "fg_batch.cuh"
@@ -741,13 +742,19 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
 }
 
 // The TMAX sweeps of one tile in registers, with the arithmetic of
-// jacobi_tile.
-template <bool OMEGA1>
+// jacobi_tile.  hook(sw) runs before sweep sw (sw a constant after
+// unrolling), so callers can spread latency-bound side work over the sweeps.
+struct NoHook {
+  __device__ __forceinline__ void operator()(int) const {}
+};
+template <bool OMEGA1, typename Hook = NoHook>
 __device__ __forceinline__ void tile_sweeps(float (&x)[RT][JT], const float (&w)[RT][JT],
                                             const float (&bw)[RT][JT], float om1,
-                                            float4 (&xch)[2][2][NWARP][32], int warp, int lane) {
+                                            float4 (&xch)[2][2][NWARP][32], int warp, int lane,
+                                            Hook hook = Hook()) {
 #pragma unroll
   for (int sw = 0; sw < TMAX; ++sw) {
+    hook(sw);
     const int buf = sw & 1;
     xch[buf][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
     xch[buf][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
@@ -1023,23 +1030,47 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
         }
     }
     __syncthreads();  // the boxes are in registers: the buffer takes the next item
-    int next = total;
+    // Warp 0 claims and prepares the next item while it sweeps this one:
+    // the claim is sent before sweep 0, the neighbours' flags are read
+    // before sweep 2 and looked at before sweep 4, where the copy of the
+    // next boxes starts if they are final (else after this tile).  No wait
+    // on an atomic or a flag sits in front of a sweep barrier.
+    int next = total, flag = 0;
     bool pending = false;
-    if (warp == 0) {
-      if (lane == 0) next = atomicAdd(counter, 1);
-      next = __shfl_sync(0xffffffffu, next, 0);
-      const bool ok = next < total ? ready(next) : true;
-      if (lane == 0 && next < total) {
-        if (ok) {
-          issue(next);
-          in_flight = true;
-        } else {
-          pending = true;  // issued after this tile, once its inputs are final
+    auto hook = [&](int sw) {
+      if (warp != 0) return;
+      if (sw == 0) {
+        if (lane == 0) next = atomicAdd(counter, 1);
+      } else if (sw == 2) {
+        next = __shfl_sync(0xffffffffu, next, 0);
+        flag = INT_MAX;
+        const int nph = next / ntiles, nt = next - nph * ntiles;
+        if (next < total && nph > 0 && lane < 9) {
+          const int nty0 = nt / ntx, ntx0 = nt - nty0 * ntx;
+          const int y = nty0 + lane / 3 - 1, xx = ntx0 + lane % 3 - 1;
+          if (y >= 0 && y < nty && xx >= 0 && xx < ntx)
+            asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];"
+                         : "=r"(flag)
+                         : "l"(done + y * ntx + xx)
+                         : "memory");
+        }
+      } else if (sw == 4) {
+        const bool ok = __all_sync(0xffffffffu, flag >= next / ntiles);
+        if (next < total) {
+          if (ok) {
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");  // the flags acquired
+            __syncwarp();
+            if (lane == 0) {
+              issue(next);
+              in_flight = true;
+            }
+          } else {
+            pending = true;  // issued after this tile, once its inputs are final
+          }
         }
       }
-      pending = __shfl_sync(0xffffffffu, pending, 0);
-    }
-    tile_sweeps<OMEGA1>(x, w, bw, om1, xch, warp, lane);
+    };
+    tile_sweeps<OMEGA1>(x, w, bw, om1, xch, warp, lane, hook);
     float* dst = (ph & 1) ? x0 : x1;
     if (own_col && warp >= TMAX / RT && warp < NWARP - TMAX / RT) {
 #pragma unroll

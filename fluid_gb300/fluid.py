@@ -323,7 +323,8 @@ class Fluid:
         self._check(self._L.fg_profile_enable(self._h, int(bool(on))), "fg_profile_enable")
 
     def jacobi_span(self):
-        """(milliseconds, launches) of the main Jacobi launches of the last solve."""
+        """(milliseconds, sweep blocks) of the main Jacobi solve of the last step
+        (blocks of tb_depth sweeps: launches, or phases of the dataflow kernel)."""
         ms, n = ctypes.c_float(), ctypes.c_int()
         self._check(self._L.fg_profile_jacobi(self._h, ctypes.byref(ms), ctypes.byref(n)),
                     "fg_profile_jacobi")

@@ -201,7 +201,8 @@ int fg_adaptive_time_step(fg_fluid* f, float basedt, float* out);               
 
 /* Measurement hooks (no counterpart in the reference).  With profiling on,
  * CUDA events bracket the main Jacobi launches of each pressure solve;
- * fg_profile_jacobi waits and returns that span and its launch count.
+ * fg_profile_jacobi waits and returns that span and its number of sweep
+ * blocks (per-launch kernels, or phases of the one dataflow launch).
  * fg_launch_count is the number of kernels the handle has enqueued;
  * fg_edit_bytes the bytes of queued tool edits uploaded so far. */
 int fg_profile_enable(fg_fluid* f, int on);
