@@ -19,6 +19,7 @@ FG_ERR_MASK = -5
 FG_ERR_TIMEOUT = -6
 FG_ERR_NOMEM = -7
 FG_ERR_TOO_LARGE = -8
+FG_ERR_NONFINITE = -9
 NOALLOC_MAX_CELLS = 1 << 20
 
 _c_i, _c_f, _c_d = ctypes.c_int, ctypes.c_float, ctypes.c_double
@@ -97,6 +98,8 @@ SIGNATURES = {
     "fg_edit_bytes": (ctypes.c_ulonglong, [_vp]),
     "fg_project_noalloc": (_c_i, [_vp, _vp, _vp, _vp, _c_i, _c_i, _c_i, _c_f, _c_f, _c_f, _c_i,
                                   _c_f, _c_f, _c_i, _c_i, _c_f, _vp]),
+    "fg_debug_fail_alloc": (_c_i, [_c_i]),
+    "fg_debug_stall_tile": (_c_i, [_vp, _c_i]),
     "fg_tape_begin": (_c_i, [_vp, _c_i, _c_i]),
     "fg_step_forward": (_c_i, [_vp, _c_f, _vp, _vp]),
     "fg_tape_seed": (_c_i, [_vp, _vp, _vp, _vp]),

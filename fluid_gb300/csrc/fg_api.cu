@@ -1,3 +1,4 @@
+#include <atomic>
 // C ABI of libfluidgpu: handle lifetime, host mirrors, tool edits, the step
 // driver and the views.  The kernels live in k_*.cu.
 #include <algorithm>
@@ -27,6 +28,31 @@ bool is_batch(const fg_fluid* f) { return f && f->batch; }
 int batch_unsupported(const fg_fluid* f) {
   const_cast<fg_fluid*>(f)->last_error = "not available on a batch handle";
   return FG_ERR_UNSUPPORTED;
+}
+
+// Allocation-failure injection (fg_debug_fail_alloc): -1 off, else the
+// number of allocations still to succeed before one fails.
+std::atomic<int> g_alloc_fail_in{-1};
+bool inject_alloc_failure() {
+  int v = g_alloc_fail_in.load();
+  while (v >= 0) {
+    if (g_alloc_fail_in.compare_exchange_weak(v, v - 1)) return v == 0;
+  }
+  return false;
+}
+cudaError_t dev_malloc(void** p, size_t n) {
+  if (inject_alloc_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, n);
+}
+cudaError_t host_malloc(void** p, size_t n) {
+  if (inject_alloc_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocHost(p, n);
 }
 
 int fail(fg_fluid* f, int code, const char* what, cudaError_t e = cudaSuccess) {
@@ -69,7 +95,7 @@ int bind(fg_fluid* f) {
 size_t field_bytes(const fg_fluid* f) { return sizeof(float) * (size_t)f->NX * f->P; }
 
 int alloc_dev(fg_fluid* f, float** p) {
-  cudaError_t e = cudaMalloc((void**)p, field_bytes(f));
+  cudaError_t e = dev_malloc((void**)p, field_bytes(f));
   if (e != cudaSuccess) return fail(f, FG_ERR_NOMEM, "cudaMalloc", e);
   e = cudaMemsetAsync(*p, 0, field_bytes(f), f->stream);
   if (e != cudaSuccess) return fail(f, FG_ERR_CUDA, "cudaMemsetAsync", e);
@@ -165,11 +191,11 @@ int flush(fg_fluid* f) {
         cudaFree(f->edit_dev[sl]);
         cudaFree(f->edit_off_dev[sl]);
         size_t cap = std::max<size_t>(ed.size(), off.size()) * 2;
-        CK(f, cudaMallocHost((void**)&f->edit_pinned[sl], cap * sizeof(EditRec)), "edit alloc");
-        CK(f, cudaMallocHost((void**)&f->edit_off_pinned[sl], (cap + 1) * sizeof(uint32_t)),
+        CK(f, host_malloc((void**)&f->edit_pinned[sl], cap * sizeof(EditRec)), "edit alloc");
+        CK(f, host_malloc((void**)&f->edit_off_pinned[sl], (cap + 1) * sizeof(uint32_t)),
            "edit alloc");
-        CK(f, cudaMalloc((void**)&f->edit_dev[sl], cap * sizeof(EditRec)), "edit alloc");
-        CK(f, cudaMalloc((void**)&f->edit_off_dev[sl], (cap + 1) * sizeof(uint32_t)), "edit alloc");
+        CK(f, dev_malloc((void**)&f->edit_dev[sl], cap * sizeof(EditRec)), "edit alloc");
+        CK(f, dev_malloc((void**)&f->edit_off_dev[sl], (cap + 1) * sizeof(uint32_t)), "edit alloc");
         f->edit_cap[sl] = cap;
       }
       memcpy(f->edit_pinned[sl], ed.data(), ed.size() * sizeof(EditRec));
@@ -231,8 +257,8 @@ int check_iters(fg_fluid* f, int iters) {
       cudaFree(f->pctl);
       cudaFree(f->ectl);
       f->n_slots = need * 2;
-      CK(f, cudaMalloc(&f->pctl, pctl_bytes(f->n_slots)), "pctl alloc");
-      CK(f, cudaMalloc(&f->ectl, pctl_bytes(f->n_slots)), "pctl alloc");
+      CK(f, dev_malloc(&f->pctl, pctl_bytes(f->n_slots)), "pctl alloc");
+      CK(f, dev_malloc(&f->ectl, pctl_bytes(f->n_slots)), "pctl alloc");
       CK(f, cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream), "pctl");
       CK(f, cudaMemsetAsync(f->ectl, 0, pctl_bytes(f->n_slots), f->stream), "pctl");
       clear_graphs(f);
@@ -376,19 +402,19 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
   for (float** s : scratch)
     if ((rc = alloc_dev(f, s))) return bail(rc);
   size_t cells = (size_t)f->NX * f->P;
-  if (cudaMalloc((void**)&f->noise, cells * sizeof(float2)) != cudaSuccess) return bail(FG_ERR_NOMEM);
-  if (cudaMalloc((void**)&f->flags, cells) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  if (dev_malloc((void**)&f->noise, cells * sizeof(float2)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  if (dev_malloc((void**)&f->flags, cells) != cudaSuccess) return bail(FG_ERR_NOMEM);
   int nb = ((f->NY + 31) / 32) * ((f->NX + 7) / 8);
   // Rows of up to 5 float-pair slots per block, the combine levels and the
   // scalar result slots at the end.
   f->n_partials = 16 * nb + 512;
-  if (cudaMalloc((void**)&f->partials, sizeof(float) * f->n_partials) != cudaSuccess)
+  if (dev_malloc((void**)&f->partials, sizeof(float) * f->n_partials) != cudaSuccess)
     return bail(FG_ERR_NOMEM);
-  if (cudaMalloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  if (dev_malloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess) return bail(FG_ERR_NOMEM);
   f->n_slots = kSlots;
-  if (cudaMalloc(&f->pctl, pctl_bytes(f->n_slots)) != cudaSuccess) return bail(FG_ERR_NOMEM);
-  if (cudaMalloc(&f->ectl, pctl_bytes(f->n_slots)) != cudaSuccess) return bail(FG_ERR_NOMEM);
-  if (cudaMalloc((void**)&f->tile_done, sizeof(int) * ((size_t)jacobi_tile_count(f->NX, f->NY) + 1)) !=
+  if (dev_malloc(&f->pctl, pctl_bytes(f->n_slots)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  if (dev_malloc(&f->ectl, pctl_bytes(f->n_slots)) != cudaSuccess) return bail(FG_ERR_NOMEM);
+  if (dev_malloc((void**)&f->tile_done, sizeof(int) * ((size_t)jacobi_tile_count(f->NX, f->NY) + 1)) !=
       cudaSuccess)
     return bail(FG_ERR_NOMEM);
   cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream);
@@ -397,13 +423,13 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
   cudaMemsetAsync(f->flags, 0, cells, f->stream);
   size_t hbytes = sizeof(float) * (size_t)f->NX * f->NY;
   for (int k = 0; k < FG_NUM_FIELDS; ++k) {
-    if (cudaMallocHost((void**)&f->hm[k], hbytes) != cudaSuccess) return bail(FG_ERR_NOMEM);
+    if (host_malloc((void**)&f->hm[k], hbytes) != cudaSuccess) return bail(FG_ERR_NOMEM);
     memset(f->hm[k], 0, hbytes);
     f->host_valid[k] = true;
   }
-  if (cudaMallocHost((void**)&f->scalar_pinned, 64 * sizeof(float)) != cudaSuccess)
+  if (host_malloc((void**)&f->scalar_pinned, 64 * sizeof(float)) != cudaSuccess)
     return bail(FG_ERR_NOMEM);
-  if (cudaMallocHost((void**)&f->stats_pinned, sizeof(DevStats)) != cudaSuccess)
+  if (host_malloc((void**)&f->stats_pinned, sizeof(DevStats)) != cudaSuccess)
     return bail(FG_ERR_NOMEM);
   if (launch_noise_table(f) != cudaSuccess) return bail(FG_ERR_CUDA);
   f->masks_stale = true;
@@ -665,7 +691,10 @@ int fg_get_stats(fg_fluid* f, fg_stats* out) {
   out->smoke_mass = s.smoke_mass;
   out->last_maxdiv = s.last_maxdiv;
   out->sweeps = s.sweeps;
-  return s.timeout ? fail(f, FG_ERR_TIMEOUT, "a device-side wait of the last step gave up") : FG_OK;
+  if (s.timeout) return fail(f, FG_ERR_TIMEOUT, "a device-side wait of the last step gave up");
+  for (double v : {s.div_l2_sq, s.div_max, s.resid_l2_sq, s.resid_max, s.smoke_mass, s.last_maxdiv})
+    if (!std::isfinite(v)) return fail(f, FG_ERR_NONFINITE, "the last step produced non-finite values");
+  return FG_OK;
 }
 
 // ------------------------------------------------------------------ stages
@@ -765,7 +794,7 @@ int fg_copy_border(fg_fluid* f, float* dst, const float* src) {
   STAGE_PROLOGUE(f);
   if (!dst || !src) return fail(f, FG_ERR_INVALID, "null buffer");
   if (!f->copy_tmp)
-    CK(f, cudaMalloc((void**)&f->copy_tmp, 2 * field_bytes(f)), "copy_border alloc");
+    CK(f, dev_malloc((void**)&f->copy_tmp, 2 * field_bytes(f)), "copy_border alloc");
   float* dd = f->copy_tmp;
   float* ds = f->copy_tmp + (size_t)f->NX * f->P;
   size_t hp = sizeof(float) * f->NY, dp = sizeof(float) * f->P;
@@ -882,8 +911,8 @@ int fg_set_sources(fg_fluid* f, int n, const int* is, const int* js, const float
   f->src_off_dev = nullptr;
   f->n_src_groups = 0;
   if (!recs.empty()) {
-    CK(f, cudaMalloc((void**)&f->src_dev, recs.size() * sizeof(SourceRec)), "sources alloc");
-    CK(f, cudaMalloc((void**)&f->src_off_dev, off.size() * sizeof(uint32_t)), "sources alloc");
+    CK(f, dev_malloc((void**)&f->src_dev, recs.size() * sizeof(SourceRec)), "sources alloc");
+    CK(f, dev_malloc((void**)&f->src_off_dev, off.size() * sizeof(uint32_t)), "sources alloc");
     CK(f, cudaMemcpy(f->src_dev, recs.data(), recs.size() * sizeof(SourceRec),
                      cudaMemcpyHostToDevice), "sources upload");
     CK(f, cudaMemcpy(f->src_off_dev, off.data(), off.size() * sizeof(uint32_t),
@@ -1464,11 +1493,11 @@ int fg_tape_begin(fg_fluid* f, int max_steps, int every) {
     t->cap_ckpt = n_ckpt + 1;
     size_t fb = field_bytes(f);
     cudaError_t e;
-    if ((e = cudaMalloc((void**)&t->forces, fb * 2 * max_steps)) != cudaSuccess ||
-        (e = cudaMalloc((void**)&t->phis, fb * max_steps)) != cudaSuccess ||
-        (e = cudaMalloc((void**)&t->ckpt, fb * 6 * t->cap_ckpt)) != cudaSuccess ||
-        (e = cudaMalloc((void**)&t->rec, fb * kTapeFields * every)) != cudaSuccess ||
-        (e = cudaMalloc((void**)&t->aux, fb)) != cudaSuccess) {
+    if ((e = dev_malloc((void**)&t->forces, fb * 2 * max_steps)) != cudaSuccess ||
+        (e = dev_malloc((void**)&t->phis, fb * max_steps)) != cudaSuccess ||
+        (e = dev_malloc((void**)&t->ckpt, fb * 6 * t->cap_ckpt)) != cudaSuccess ||
+        (e = dev_malloc((void**)&t->rec, fb * kTapeFields * every)) != cudaSuccess ||
+        (e = dev_malloc((void**)&t->aux, fb)) != cudaSuccess) {
       tape_free(f);
       return fail(f, FG_ERR_NOMEM, "tape allocation", e);
     }
@@ -1696,7 +1725,7 @@ int upload_table(fg_fluid* f, T** dev, const std::vector<T>& host) {
   cudaFree(*dev);
   *dev = nullptr;
   if (host.empty()) return FG_OK;
-  CK(f, cudaMalloc((void**)dev, host.size() * sizeof(T)), "batch table");
+  CK(f, dev_malloc((void**)dev, host.size() * sizeof(T)), "batch table");
   CK(f, cudaMemcpy(*dev, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice),
      "batch table");
   return FG_OK;
@@ -1831,21 +1860,21 @@ int fg_batch_create(fg_fluid* const* scenes, int n, fg_fluid** out) {
                        &f->curl, &f->view, &f->wgt,  &f->bw,    &f->bwe};
   for (float** sp : scratch)
     if ((rc = alloc_dev(f, sp))) return bail(rc);
-  if (cudaMalloc((void**)&f->noise, total * sizeof(float2)) != cudaSuccess ||
-      cudaMalloc((void**)&f->flags, total) != cudaSuccess)
+  if (dev_malloc((void**)&f->noise, total * sizeof(float2)) != cudaSuccess ||
+      dev_malloc((void**)&f->flags, total) != cudaSuccess)
     return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
   cudaMemsetAsync(f->flags, 0, total, f->stream);
   f->n_slots = kSlots;
-  if (cudaMalloc(&f->pctl, pctl_bytes(f->n_slots)) != cudaSuccess ||
-      cudaMalloc(&f->ectl, pctl_bytes(f->n_slots)) != cudaSuccess ||
-      cudaMalloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess ||
-      cudaMalloc((void**)&b->losses, sizeof(double) * 2 * n) != cudaSuccess)
+  if (dev_malloc(&f->pctl, pctl_bytes(f->n_slots)) != cudaSuccess ||
+      dev_malloc(&f->ectl, pctl_bytes(f->n_slots)) != cudaSuccess ||
+      dev_malloc((void**)&f->dstats, sizeof(DevStats)) != cudaSuccess ||
+      dev_malloc((void**)&b->losses, sizeof(double) * 2 * n) != cudaSuccess)
     return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
   cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream);
   cudaMemsetAsync(f->ectl, 0, pctl_bytes(f->n_slots), f->stream);
   cudaMemsetAsync(f->dstats, 0, sizeof(DevStats), f->stream);
-  if (cudaMallocHost((void**)&f->scalar_pinned, 64 * sizeof(float)) != cudaSuccess ||
-      cudaMallocHost((void**)&f->stats_pinned, sizeof(DevStats)) != cudaSuccess)
+  if (host_malloc((void**)&f->scalar_pinned, 64 * sizeof(float)) != cudaSuccess ||
+      host_malloc((void**)&f->stats_pinned, sizeof(DevStats)) != cudaSuccess)
     return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
   // Block tables.
   if ((rc = upload_table(f, &b->scenes_dev, b->scenes))) return bail(rc);
@@ -1872,7 +1901,7 @@ int fg_batch_create(fg_fluid* const* scenes, int n, fg_fluid** out) {
     max_tiles = std::max(max_tiles, nt);
   }
   f->n_partials = (int)(2 * (max_tiles + max_tiles / 2048 + 2) + 512);
-  if (cudaMalloc((void**)&f->partials, sizeof(float) * f->n_partials) != cudaSuccess)
+  if (dev_malloc((void**)&f->partials, sizeof(float) * f->n_partials) != cudaSuccess)
     return bail(fail(f, FG_ERR_NOMEM, "batch allocation"));
   // Sources: the members' groups, each tagged with its scene.
   std::vector<SourceRec> recs;
@@ -2015,7 +2044,7 @@ int fg_batch_autotune(fg_fluid* f, float dt, int reps, int* tb_depth, int* block
   static const int depths[] = {4, 6, 8};
   size_t fb = field_bytes(f);
   float* saved = nullptr;
-  CK(f, cudaMalloc((void**)&saved, fb * 7), "autotune");
+  CK(f, dev_malloc((void**)&saved, fb * 7), "autotune");
   auto save = [&]() {
     int r = save_state(f, saved);
     if (!r) r = copy_field(f, saved + 6 * field_elems(f), f->d[FG_P]);
@@ -2107,13 +2136,13 @@ int particles_reserve(fg_fluid* f, int need, int n) {
   cudaError_t e = cudaSuccess;
   for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
     for (int q = 0; q < 4 && e == cudaSuccess; ++q)
-      e = cudaMalloc((void**)&Q.a[b][q], sizeof(float) * cap);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&Q.rgb[b], sizeof(uint32_t) * cap);
+      e = dev_malloc((void**)&Q.a[b][q], sizeof(float) * cap);
+    if (e == cudaSuccess) e = dev_malloc((void**)&Q.rgb[b], sizeof(uint32_t) * cap);
   }
-  if (e == cudaSuccess) e = cudaMalloc((void**)&Q.keep, cap);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&Q.block_keep, sizeof(int) * (cap / kParticleBlock));
+  if (e == cudaSuccess) e = dev_malloc((void**)&Q.keep, cap);
+  if (e == cudaSuccess) e = dev_malloc((void**)&Q.block_keep, sizeof(int) * (cap / kParticleBlock));
   if (e == cudaSuccess && !P.count) {
-    e = cudaMalloc((void**)&Q.count, sizeof(int));
+    e = dev_malloc((void**)&Q.count, sizeof(int));
     if (e == cudaSuccess) e = cudaMemsetAsync(Q.count, 0, sizeof(int), f->stream);
   } else {
     Q.count = P.count;
@@ -2250,7 +2279,7 @@ int fg_render(fg_fluid* f, int kind, void* rgba) {
   int rc = flush(f);
   if (rc) return rc;
   size_t bytes = (size_t)f->NX * f->NY * 4;
-  if (!f->image) CK(f, cudaMalloc((void**)&f->image, bytes), "render target");
+  if (!f->image) CK(f, dev_malloc((void**)&f->image, bytes), "render target");
   float* mm = dev_scalar_slot(f);
   const float* field = nullptr;
   if (kind == FG_RENDER_SMOKE || kind == FG_RENDER_PRESSURE) {
@@ -2269,3 +2298,19 @@ int fg_render(fg_fluid* f, int kind, void* rgba) {
 
 }  // extern "C"
 
+
+// ------------------------------------------------------------ fault injection
+int fg_debug_fail_alloc(int n) {
+  g_alloc_fail_in.store(n < 0 ? -1 : n);
+  return FG_OK;
+}
+
+int fg_debug_stall_tile(fg_fluid* f, int tile) {
+  if (!f) return FG_ERR_INVALID;
+  if (is_batch(f)) return batch_unsupported(f);
+  int rc = flush(f);
+  if (rc) return rc;
+  f->stall_tile = tile < 0 ? -1 : tile;
+  f->params_version++;  // captured steps embed the kernel's arguments
+  return FG_OK;
+}

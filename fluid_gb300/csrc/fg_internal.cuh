@@ -187,6 +187,7 @@ struct fg_fluid {
   fg::DevStats* dstats = nullptr;
   void* pctl = nullptr;   // control block of the main Jacobi solve (k_pressure.cu PCtl)
   int* tile_done = nullptr;  // dataflow Jacobi kernel: per-tile phase flags + item counter
+  int stall_tile = -1;       // fault injection: a tile the dataflow kernel never publishes
   void* ectl = nullptr;   // control block of the FP64-residual correction solve
   int n_slots = 0;        // launch slots per control block
   float* copy_tmp = nullptr;        // fg_copy_border staging (2 fields)

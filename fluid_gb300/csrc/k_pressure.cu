@@ -932,7 +932,7 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
                   const __grid_constant__ CUtensorMap tmw, const __grid_constant__ CUtensorMap tmb,
                   float* __restrict__ x0, float* __restrict__ x1, float om1, PCtl* ctl,
                   int* __restrict__ done, int nphase, int zero_first, Grid g, int ntx, int nty,
-                  int* err) {
+                  int* err, int stall_tile) {
   extern __shared__ __align__(128) float4 tbuf4[];  // [3][RI][RJ] floats: phi, w, w*b
   float* tbuf = reinterpret_cast<float*>(tbuf4);
   __shared__ float4 xch[2][2][NWARP][32];
@@ -1089,7 +1089,7 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
     }
     __syncthreads();  // the tile's stores precede its publication
     if (warp == 0) {
-      if (lane == 0) {
+      if (lane == 0 && t != stall_tile) {  // (a stalled tile: fault injection)
         __threadfence();
         st_release(done + t, ph + 1);
       }
@@ -1454,7 +1454,7 @@ int jacobi_tile_count(int NX, int NY) {
 // cooperative launch are unavailable.
 static bool launch_jacobi_flow(cudaStream_t st, const Grid& g, PCtl* ctl, float* x0, float* x1,
                                const float* W, const float* BW, float om1, bool o1, int nphase,
-                               int* done, int* err) {
+                               int* done, int* err, int stall_tile) {
   if (!done || nphase < 2 || !g_tma_init.load() || g_flow_per_sm <= 0 || g_sms <= 0) return false;
   const int ntx = (g.NY + OJ - 1) / OJ, nty = (g.NX + OI - 1) / OI;
   const int ntiles = ntx * nty;
@@ -1479,9 +1479,11 @@ static bool launch_jacobi_flow(cudaStream_t st, const Grid& g, PCtl* ctl, float*
   cfg.numAttrs = 1;
   const int zero_first = 1;
   cudaError_t e = o1 ? cudaLaunchKernelEx(&cfg, k_jacobi_flow<true>, tm0, tm1, tmw, tmb, x0, x1,
-                                          om1, ctl, done, nphase, zero_first, g, ntx, nty, err)
+                                          om1, ctl, done, nphase, zero_first, g, ntx, nty, err,
+                                          stall_tile)
                      : cudaLaunchKernelEx(&cfg, k_jacobi_flow<false>, tm0, tm1, tmw, tmb, x0, x1,
-                                          om1, ctl, done, nphase, zero_first, g, ntx, nty, err);
+                                          om1, ctl, done, nphase, zero_first, g, ntx, nty, err,
+                                          stall_tile);
   return e == cudaSuccess;
 }
 
@@ -1497,7 +1499,8 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
                                   int* n_launched, const float* mphi0 = nullptr,
                                   const float* mphi1 = nullptr, const PCtl* mctl = nullptr,
                                   float* rhs_e = nullptr, float* bwe = nullptr,
-                                  int* err = nullptr, int* done = nullptr) {
+                                  int* err = nullptr, int* done = nullptr,
+                                  int stall_tile = -1) {
   float om1 = 1.0f - om;
   bool o1 = om1 == 0.0f;
   dim3 gr((g.NY + OJ - 1) / OJ, (g.NX + OI - 1) / OI);
@@ -1506,7 +1509,8 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
   // Fixed sweep counts in full launches: the leading full phases as one
   // dataflow kernel where the grid is large enough.
   if (!check && !mphi0 && T == TMAX && iters / TMAX >= 2 &&
-      launch_jacobi_flow(st, g, ctl, x0, x1, W, bw, om1, o1, iters / TMAX, done, err)) {
+      launch_jacobi_flow(st, g, ctl, x0, x1, W, bw, om1, o1, iters / TMAX, done, err,
+                         stall_tile)) {
     k0 = iters / TMAX;
     kernels = 1;
   }
@@ -1591,7 +1595,7 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
     e = enqueue_jacobi(f->stream, f->g, ctl, b, bw, f->wgt, f->flags, x0, x1, iters, T,
                        f->prm.jacobi_omega * f->prm.pressure_damping, check, f->prm.tolerance, &n,
                        nullptr, nullptr, nullptr, nullptr, nullptr, &f->dstats->timeout,
-                       f->tile_done);
+                       f->tile_done, f->stall_tile);
   count(f, n);
   if (e != cudaSuccess) return e;
   if (prof) {

@@ -49,6 +49,13 @@ _PARAMS = {
 _BOOL = {"UseMultigrid", "UseBFECC", "early_exit", "use_graphs"}
 
 
+def debug_fail_alloc(n):
+    """Fault injection: the n-th next device or pinned allocation of the
+    library (process-wide, from 0) fails as if memory were exhausted; n < 0
+    disarms."""
+    _lib.lib().fg_debug_fail_alloc(int(n))
+
+
 class FluidError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s (code %d)" % (msg, code))
@@ -451,6 +458,12 @@ class Fluid:
                                              rgb.ctypes.data), "fg_particles_get")
         out["RGB"] = rgb
         return out
+
+    def debug_stall_tile(self, tile):
+        """Fault injection: the dataflow Jacobi kernel never publishes `tile`,
+        so the step's bounded waits give up and stats() raises FG_ERR_TIMEOUT
+        (tile < 0 disarms)."""
+        self._check(self._L.fg_debug_stall_tile(self._h, int(tile)), "fg_debug_stall_tile")
 
     def particles_clear(self):
         self._check(self._L.fg_particles_clear(self._h), "fg_particles_clear")

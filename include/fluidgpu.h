@@ -41,6 +41,7 @@ extern "C" {
 #define FG_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up                    */
 #define FG_ERR_NOMEM (-7)       /* device or pinned allocation failed                    */
 #define FG_ERR_TOO_LARGE (-8)   /* grid beyond the fixed scratch of fg_project_noalloc    */
+#define FG_ERR_NONFINITE (-9)   /* a statistic of the last step is NaN or infinite        */
 
 /* Field identifiers (Fluid.U, .V, .newU, .newV, .p, .S, .M, .newM). */
 enum {
@@ -142,8 +143,10 @@ void* fg_stream(fg_fluid* f);
 /* (*Fluid).Simulate(dt) -- fluid.go:79-109.  Enqueues one step; returns when
  * it is queued.  Results are read with fg_download / fg_get_stats. */
 int fg_simulate(fg_fluid* f, float dt);
-/* Statistics of the last step or stage (waits).  FG_ERR_TIMEOUT (with the
- * statistics filled in) when a bounded device-side wait of that step gave up. */
+/* Statistics of the last step or stage (waits).  With the statistics filled
+ * in, FG_ERR_TIMEOUT when a bounded device-side wait of that step gave up
+ * (its fields are then not to be used), else FG_ERR_NONFINITE when one of
+ * the statistics is NaN or infinite (the step produced non-finite values). */
 int fg_get_stats(fg_fluid* f, fg_stats* out);
 
 /* Stage entry points (the unexported methods the reference tests call). */
@@ -354,6 +357,19 @@ int fg_render(fg_fluid* f, int kind, void* rgba);
 /* Text of the last error on the handle ("" if none); static text for a
  * NULL handle. */
 const char* fg_last_error(const fg_fluid* f);
+
+/* Fault injection (no counterpart in the reference), for tests of the
+ * error paths without a GPU fault.
+ * fg_debug_fail_alloc(n): the n-th next device or pinned allocation made by
+ * the library (counting from 0, process-wide) fails as if memory were
+ * exhausted; n < 0 disarms.  The call that made it returns FG_ERR_NOMEM (or
+ * FG_ERR_CUDA where a CUDA failure is reported) and frees what it took.
+ * fg_debug_stall_tile(f, t): the dataflow Jacobi kernel never publishes tile
+ * t of the handle's solves, so the tiles that read it wait until their
+ * bounded waits (about a second) give up; the step's fg_get_stats returns
+ * FG_ERR_TIMEOUT.  t < 0 disarms.  Changes the handle's captured graphs. */
+int fg_debug_fail_alloc(int n);
+int fg_debug_stall_tile(fg_fluid* f, int tile);
 
 #ifdef __cplusplus
 }
