@@ -148,11 +148,12 @@ def test_jacobi_refinement_bitwise(gpu):
     assert sg["resid_l2"] == pytest.approx(so["resid_l2"], rel=1e-9)
 
 
-@pytest.mark.parametrize("w,h", [(70, 45), (333, 222), (1100, 1500)])
+@pytest.mark.parametrize("w,h", [(70, 45), (333, 222), (1100, 1500), (9000, 100), (300, 2700)])
 def test_jacobi_fixed_sweeps_bitwise(gpu, w, h):
-    """Fixed sweep counts in full 8-sweep launches: the persistent kernel fed
-    by tensor-memory-accelerator copies (at 1100x1500, 322 tiles: more than
-    one tile per block) against the oracle, bit for bit."""
+    """Fixed sweep counts in full 8-sweep launches against the oracle, bit for
+    bit: the persistent kernel fed by tensor-memory-accelerator copies (70x45,
+    333x222) and the dataflow kernel (1100x1500: 322 tiles; 9000x100: one
+    tile column of 188 tiles; 300x2700: 7 tile rows of 25)."""
     g, o = both(gpu, w, h, scheme=1, num_iters=40, tb_depth=8, early_exit=False, UseBFECC=True)
     for f in (g, o):
         scenes.jet_scene(f)
@@ -162,6 +163,18 @@ def test_jacobi_fixed_sweeps_bitwise(gpu, w, h):
             scenes.jet_inject(f, speed=3.0)
             f.Simulate(0.1)
     assert_bitwise(g, o, where="%dx%d" % (w, h))
+
+
+def test_jacobi_dataflow_then_partial_launch_bitwise(gpu):
+    """44 sweeps at 1100x1500: five dataflow phases, then one 4-sweep launch
+    of the per-launch kernel continuing from the dataflow result."""
+    g, o = both(gpu, 1100, 1500, scheme=1, num_iters=44, tb_depth=8, early_exit=False)
+    for f in (g, o):
+        scenes.cavity_scene(f)
+        scenes.random_state(f, seed=21)
+        f.makeIncompressible(44, 0.1)
+    assert_bitwise(g, o, fields=("U", "V", "p"))
+    assert g.stats()["sweeps"] == 44
 
 
 def test_jacobi_fixed_sweeps_2048_matches_checked_launches(gpu):
