@@ -1348,11 +1348,18 @@ size_t pctl_bytes(int n_slots) { return sizeof(PCtl) + sizeof(unsigned) * (size_
 // Tensor maps of the TMA-fed Jacobi kernel: a 2D float array of rows x
 // pitch, boxes of 64 rows x 128 columns, zero outside.  false when the
 // driver entry point or the encoding is unavailable (the plain kernel runs).
+// Per device: the SM count, the dataflow kernel's blocks per SM, whether the
+// set-up ran (the kernels' shared-memory limit is a per-device attribute).
+constexpr int kMaxDevices = 64;
+struct TmaDevice {
+  std::once_flag once;
+  std::atomic<bool> ready{false};
+  int sms = 0;
+  int flow_per_sm = 0;
+};
+static TmaDevice g_tma_dev[kMaxDevices];
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-static int g_sms = 0;
-static std::once_flag g_tma_once;
-static std::atomic<bool> g_tma_init{false};
-static int g_flow_per_sm = 0;
+static std::once_flag g_encode_once;
 
 static bool encode_box_map(CUtensorMap* tm, const float* base, int rows, int pitch) {
   if (!g_encode || (reinterpret_cast<uintptr_t>(base) & 15) || (pitch % 4) != 0) return false;
@@ -1367,26 +1374,42 @@ static bool encode_box_map(CUtensorMap* tm, const float* base, int rows, int pit
   return r == CUDA_SUCCESS;
 }
 
-// Resolves the tensor-map encoder, the SM count and the kernel's shared
-// memory limit once per process (outside any stream capture).
+// The current device's entry, or nullptr.
+static TmaDevice* tma_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return &g_tma_dev[dev];
+}
+
+// Resolves the tensor-map encoder (once per process) and, once per device,
+// the SM count and the TMA kernels' shared-memory limit (outside any stream
+// capture).
 void init_jacobi_tma() {
-  std::call_once(g_tma_once, [] {
+  std::call_once(g_encode_once, [] {
     cudaDriverEntryPointQueryResult q;
     void* fn = nullptr;
     if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    cudaGetLastError();
+  });
+  TmaDevice* d = tma_device();
+  if (!d) return;
+  std::call_once(d->once, [d] {
     int dev = 0, n = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
-      g_sms = n;
+      d->sms = n;
     const int smem = 3 * TILE_FLOATS * (int)sizeof(float);
     if (cudaFuncSetAttribute(k_jacobi_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem) != cudaSuccess ||
         cudaFuncSetAttribute(k_jacobi_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem) != cudaSuccess)
-      g_sms = 0;
+      d->sms = 0;
     // Blocks of the dataflow kernel that fit on one SM (co-residency bound).
     int b1 = 0, b2 = 0;
     if (cudaFuncSetAttribute(k_jacobi_flow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1397,13 +1420,29 @@ void init_jacobi_tma() {
                                                       smem) == cudaSuccess &&
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_jacobi_flow<false>, TB_THREADS,
                                                       smem) == cudaSuccess)
-      g_flow_per_sm = b1 < b2 ? b1 : b2;
+      d->flow_per_sm = b1 < b2 ? b1 : b2;
     int coop = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
-      g_flow_per_sm = 0;
+      d->flow_per_sm = 0;
     cudaGetLastError();
-    g_tma_init.store(true);
+    d->ready.store(true);
   });
+}
+
+// The current device's set-up, done here unless the stream is capturing
+// (then nullptr: the plain kernels run).
+static const TmaDevice* tma_ready(cudaStream_t st) {
+  TmaDevice* d = tma_device();
+  if (!d) return nullptr;
+  if (!d->ready.load()) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusActive;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    init_jacobi_tma();
+  }
+  return d->ready.load() ? d : nullptr;
 }
 
 // Launches one full, unchecked Jacobi launch through the TMA-fed kernel;
@@ -1411,17 +1450,13 @@ void init_jacobi_tma() {
 static bool launch_jacobi_tma(cudaStream_t st, const Grid& g, PCtl* ctl, const float* src,
                               float* dst, const float* W, const float* BW, float om1, bool o1,
                               int k, int t0, int sel, int zero_init, int* err) {
-  if (!g_tma_init.load()) {
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusActive;
-    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
-      return false;
-    init_jacobi_tma();
-  }
+  const TmaDevice* dv = tma_ready(st);
+  if (!dv) return false;
   CUtensorMap tmx, tmw, tmb;
   if (!encode_box_map(&tmx, src, g.NX, g.P) || !encode_box_map(&tmw, W, g.NX, g.P) ||
       !encode_box_map(&tmb, BW, g.NX, g.P))
     return false;
-  const int nsm = g_sms;
+  const int nsm = dv->sms;
   if (nsm <= 0) return false;
   const int ntx = (g.NY + OJ - 1) / OJ, nty = (g.NX + OI - 1) / OI;
   const int ntiles = ntx * nty;
@@ -1455,17 +1490,19 @@ int jacobi_tile_count(int NX, int NY) {
 static bool launch_jacobi_flow(cudaStream_t st, const Grid& g, PCtl* ctl, float* x0, float* x1,
                                const float* W, const float* BW, float om1, bool o1, int nphase,
                                int* done, int* err, int stall_tile) {
-  if (!done || nphase < 2 || !g_tma_init.load() || g_flow_per_sm <= 0 || g_sms <= 0) return false;
+  if (!done || nphase < 2) return false;
+  const TmaDevice* dv = tma_ready(st);
+  if (!dv || dv->flow_per_sm <= 0 || dv->sms <= 0) return false;
   const int ntx = (g.NY + OJ - 1) / OJ, nty = (g.NX + OI - 1) / OI;
   const int ntiles = ntx * nty;
-  if (ntiles < g_sms) return false;
+  if (ntiles < dv->sms) return false;
   CUtensorMap tm0, tm1, tmw, tmb;
   if (!encode_box_map(&tm0, x0, g.NX, g.P) || !encode_box_map(&tm1, x1, g.NX, g.P) ||
       !encode_box_map(&tmw, W, g.NX, g.P) || !encode_box_map(&tmb, BW, g.NX, g.P))
     return false;
   // The tile flags and the item counter.
   if (cudaMemsetAsync(done, 0, sizeof(int) * ((size_t)ntiles + 1), st) != cudaSuccess) return false;
-  const int cap = g_flow_per_sm * g_sms;
+  const int cap = dv->flow_per_sm * dv->sms;
   const int grid = ntiles < cap ? ntiles : cap;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
