@@ -28,9 +28,6 @@
 #include <mutex>
 
 #include "fg_batch.cuh"
-#ifndef NB_EXTRA_SYNC
-#define NB_EXTRA_SYNC
-#endif
 #include "fg_internal.cuh"
 #include "fg_reduce.cuh"
 
@@ -702,9 +699,6 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
                "r"(bytes)
                : "memory");
 }
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   uint32_t ok;
   asm volatile(
@@ -795,80 +789,6 @@ __device__ __forceinline__ void tile_sweeps(float (&x)[RT][JT], const float (&w)
         x[r][q] = nw[q];
       }
     }
-  }
-}
-
-__device__ __forceinline__ void nb_wait(uint64_t* up, uint64_t* dn, unsigned parity, int* err) {
-  uint32_t a = up ? 0u : 1u, b = dn ? 0u : 1u;
-  for (int it = 0; it < (1 << 20) && !(a & b); ++it) {
-    if (!a)
-      asm volatile(
-          "{\n\t.reg .pred p;\n\t"
-          "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-          "selp.u32 %0, 1, 0, p;\n\t}"
-          : "=r"(a)
-          : "r"(smem_u32(up)), "r"(parity), "r"(1000u)
-          : "memory");
-    if (!b)
-      asm volatile(
-          "{\n\t.reg .pred p;\n\t"
-          "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-          "selp.u32 %0, 1, 0, p;\n\t}"
-          : "=r"(b)
-          : "r"(smem_u32(dn)), "r"(parity), "r"(1000u)
-          : "memory");
-  }
-  if (!(a & b)) *err = 1;
-}
-
-template <bool OMEGA1, typename Hook = NoHook>
-__device__ __forceinline__ void tile_sweeps_nb(float (&x)[RT][JT], const float (&w)[RT][JT],
-                                               const float (&bw)[RT][JT], float om1,
-                                               float4 (&xch)[2][2][NWARP][32],
-                                               uint64_t (&xbar)[2][NWARP], int* err, int warp,
-                                               int lane, Hook hook = Hook()) {
-#pragma unroll
-  for (int sw = 0; sw < TMAX; ++sw) {
-    hook(sw);
-    const int buf = sw & 1;
-    const unsigned par = (sw >> 1) & 1;
-    xch[buf][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
-    xch[buf][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&xbar[buf][warp]);
-    nb_wait(warp > 0 ? &xbar[buf][warp - 1] : nullptr,
-            warp < NWARP - 1 ? &xbar[buf][warp + 1] : nullptr, par, err);
-    float4 u4 = warp > 0 ? xch[buf][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 d4 = warp < NWARP - 1 ? xch[buf][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
-#pragma unroll
-    for (int r = 0; r < RT; ++r) {
-      float lf = __shfl_up_sync(0xffffffffu, x[r][JT - 1], 1);
-      float rt = __shfl_down_sync(0xffffffffu, x[r][0], 1);
-      float nxt[JT];
-      if (r < RT - 1) {
-#pragma unroll
-        for (int q = 0; q < JT; ++q) nxt[q] = x[r + 1][q];
-      } else {
-        nxt[0] = d4.x; nxt[1] = d4.y; nxt[2] = d4.z; nxt[3] = d4.w;
-      }
-      float nw[JT];
-#pragma unroll
-      for (int q = 0; q < JT; ++q) {
-        float left = q == 0 ? lf : x[r][q - 1];
-        float right = q == JT - 1 ? rt : x[r][q + 1];
-        float nb = prev[q] + nxt[q] + left + right;
-        float y = __fmaf_rn(w[r][q], nb, bw[r][q]);
-        if (!OMEGA1) y = __fmaf_rn(om1, x[r][q], y);
-        nw[q] = y;
-      }
-#pragma unroll
-      for (int q = 0; q < JT; ++q) {
-        prev[q] = x[r][q];
-        x[r][q] = nw[q];
-      }
-    }
-    NB_EXTRA_SYNC
   }
 }
 
@@ -1017,8 +937,6 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   float* tbuf = reinterpret_cast<float*>(tbuf4);
   __shared__ float4 xch[2][2][NWARP][32];
   __shared__ __align__(8) uint64_t bar;
-  __shared__ __align__(8) uint64_t xbar[2][NWARP];
-  __shared__ int s_xerr;
   __shared__ int s_item;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ntiles = ntx * nty, total = ntiles * nphase;
@@ -1058,9 +976,6 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   if (warp == 0) {
     int i = 0;
     if (lane == 0) {
-      for (int b2 = 0; b2 < 2; ++b2)
-        for (int q = 0; q < NWARP; ++q) mbar_init(&xbar[b2][q], 1);
-      s_xerr = 0;
       mbar_init(&bar, 1);
       i = atomicAdd(counter, 1);
     }
@@ -1081,7 +996,7 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   unsigned parity = 0;
   const bool own_col = lane * JT >= TMAX && lane * JT < RJ - TMAX;
   while (true) {
-    if (__syncthreads_or(fail || s_xerr)) { if (tid == 0) fail = 1; break; }
+    if (__syncthreads_or(fail)) break;
     const int item = s_item;
     if (item >= total) break;
     const bool landed = mbar_wait_bounded(&bar, parity);
@@ -1155,7 +1070,7 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
         }
       }
     };
-    tile_sweeps_nb<OMEGA1>(x, w, bw, om1, xch, xbar, &s_xerr, warp, lane, hook);
+    tile_sweeps<OMEGA1>(x, w, bw, om1, xch, warp, lane, hook);
     float* dst = (ph & 1) ? x0 : x1;
     if (own_col && warp >= TMAX / RT && warp < NWARP - TMAX / RT) {
 #pragma unroll
