@@ -1,7 +1,7 @@
-#include <atomic>
 // C ABI of libfluidgpu: handle lifetime, host mirrors, tool edits, the step
-// driver and the views.  The kernels live in k_*.cu.
+// sequence and the views.  The kernels live in k_*.cu.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
