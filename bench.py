@@ -480,6 +480,207 @@ def ensemble(fluid_gb300, args, n=256, steps=20, roll=16, every=8):
 
 
 # ---------------------------------------------------------------- CPU legs
+# ---------------------------------------------------------------- the app-side rows
+APP_W, APP_H = 300, 251          # the app-size jet
+N_PARTICLES = 10000              # the app's particle budget
+MG_SIDE = 512                    # the multigrid (UseMultigrid) cavity
+
+
+def jet_setup(f):
+    """The app-size jet: walls left, top and bottom, jet of 8 rows at i = 1
+    (U = 2, smoke 1) held by device sources."""
+    import numpy as np
+
+    S = f.S.reshape(f.NumX, f.NumY)
+    S[:] = 1.0
+    S[:, 0] = S[:, -1] = S[0, :] = 0.0
+    f.mark_dirty()
+    n = f.NumY
+    rows = np.arange(n // 2 - 4, n // 2 + 4, dtype=np.int32)
+    f.set_sources(np.ones_like(rows), rows, u=2.0, v=0.0, smoke=1.0,
+                  mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY | f.SRC_SET_SMOKE)
+
+
+def spawn_positions(nx, ny, n, seed=9):
+    """n particle positions (world units, h = 1) at cell centres near the jet."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    i = rng.integers(1, min(nx - 1, 40), n)
+    j = rng.integers(ny // 2 - 30, ny // 2 + 30, n)
+    return (i + 0.5).astype(np.float32), (j + 0.5).astype(np.float32)
+
+
+def device_ms(stream, fn, reps):
+    """Mean milliseconds of fn() over reps calls, CUDA events on `stream`."""
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def app_rows(fluid_gb300):
+    """The rows next to the step: the reference's multigrid V-cycle
+    (UseMultigrid, bit for bit) as a whole step, the app's particle advection
+    and field rendering, and a view (Vorticity), timed on the GPU."""
+    import numpy as np
+    import torch
+
+    rows = {}
+    # The reference scheme (serial SOR, bit for bit) as the wavefront kernel:
+    # the 512^2 cavity, the reference's 8 iterations per step.
+    f = fluid_gb300.Fluid(1.0, MG_SIDE, MG_SIDE, 1.0, auto_sync=False, UseBFECC=True, num_iters=8,
+                          early_exit=False)
+    S = f.S.reshape(f.NumX, f.NumY)
+    S[:] = 1.0
+    S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
+    f.mark_dirty()
+    li, lj = lid_cells(f)
+    f.set_sources(li, lj, u=1.0, v=0.0, mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY)
+    st = torch.cuda.ExternalStream(f.stream)
+    for _ in range(3):
+        f.Simulate(DT)
+    ms = device_ms(st, lambda: f.Simulate(DT), 10)
+    rows["reference_sor"] = {"value": MG_SIDE * MG_SIDE / ms / 1e3, "unit": "Mcell-steps/s",
+                             "ms_per_step": ms,
+                             "config": "%dx%d cavity, the reference's lexicographic SOR bit for bit "
+                                       "(8 sweeps, one-block wavefront), BFECC; device-timed steps"
+                                       % (MG_SIDE, MG_SIDE)}
+    del f
+    # Multigrid: a lid-driven cavity stepped with UseMultigrid (8 V-cycles).
+    f = fluid_gb300.Fluid(1.0, MG_SIDE, MG_SIDE, 1.0, auto_sync=False, UseMultigrid=True,
+                          UseBFECC=True, num_iters=8)
+    S = f.S.reshape(f.NumX, f.NumY)
+    S[:] = 1.0
+    S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
+    f.mark_dirty()
+    li, lj = lid_cells(f)
+    f.set_sources(li, lj, u=1.0, v=0.0, mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY)
+    st = torch.cuda.ExternalStream(f.stream)
+    for _ in range(3):
+        f.Simulate(DT)
+    ms = device_ms(st, lambda: f.Simulate(DT), 10)
+    rows["multigrid"] = {"value": MG_SIDE * MG_SIDE / ms / 1e3, "unit": "Mcell-steps/s",
+                         "ms_per_step": ms,
+                         "config": "%dx%d cavity, UseMultigrid (the reference's V-cycle bit for "
+                                   "bit, 8 cycles), BFECC; device-timed steps" % (MG_SIDE, MG_SIDE)}
+    del f
+    # Particles and rendering on the app-size jet.
+    f = fluid_gb300.Fluid(1.0, APP_W, APP_H, 1.0, auto_sync=False, scheme=fluid_gb300.SCHEME_JACOBI,
+                          num_iters=40, early_exit=False, UseBFECC=True)
+    jet_setup(f)
+    for _ in range(20):
+        f.Simulate(DT)
+    x, y = spawn_positions(f.NumX, f.NumY, N_PARTICLES)
+    rgb = np.full((N_PARTICLES, 3), 200, np.uint8)
+    f.particles_add(x, y, 1e9, rgb)
+    st = torch.cuda.ExternalStream(f.stream)
+    f.particles_advect(DT)
+    ms = device_ms(st, lambda: f.particles_advect(0.01), 200)
+    live = len(f.particles()["X"])
+    rows["particles"] = {"value": N_PARTICLES / ms / 1e3, "unit": "Mparticles/s",
+                         "us_per_frame": 1e3 * ms, "live_after": live,
+                         "config": "%d particles on the %dx%d jet (RK2 through SampleVelocity, "
+                                   "culling, order-preserving compaction); device-timed calls"
+                                   % (N_PARTICLES, APP_W, APP_H)}
+    img = f.render(f.RENDER_SMOKE)
+    t0 = time.perf_counter()
+    for _ in range(50):
+        img = f.render(f.RENDER_SMOKE)
+    ms_app = 1e3 * (time.perf_counter() - t0) / 50
+    del f
+    g = build_cavity(fluid_gb300)
+    gi, gj = lid_cells(g)
+    g.set_sources(gi, gj, u=1.0, v=0.0, mode=g.SRC_SKIP_SOLID | g.SRC_SET_VELOCITY)
+    for _ in range(3):
+        g.Simulate(DT)
+    g.render(g.RENDER_VORTICITY)
+    t0 = time.perf_counter()
+    for _ in range(10):
+        img = g.render(g.RENDER_VORTICITY)
+    ms_big = 1e3 * (time.perf_counter() - t0) / 10
+    rows["render"] = {"value": g.NumX * g.NumY / ms_big / 1e3, "unit": "Mpixel/s",
+                      "ms_per_frame_2048": ms_big, "ms_per_frame_app": ms_app,
+                      "config": "fg_render (vorticity with getDivergingColor at 2048^2, smoke with "
+                                "getSciValue at %dx%d) through the C ABI: min/max, colormap, "
+                                "RGBA copied to the host; host wall clock" % (APP_W, APP_H)}
+    g.Vorticity()
+    t0 = time.perf_counter()
+    for _ in range(10):
+        g.Vorticity()
+    ms_v = 1e3 * (time.perf_counter() - t0) / 10
+    rows["views"] = {"value": g.NumX * g.NumY / ms_v / 1e3, "unit": "Mcell/s", "ms_per_view": ms_v,
+                     "config": "Vorticity() of the 2048^2 cavity through the C ABI (curl kernel, "
+                               "field copied to the host); host wall clock"}
+    del g, img
+    return rows
+
+
+def cpu_app_rows(threads):
+    """The CPU baseline of the app-side rows: the oracle's restatement of the
+    reference on the same inputs, one bounded sample each."""
+    import numpy as np
+    from oracle.pyoracle import LEXSOR, OracleFluid
+
+    out = {}
+    for key, mg in (("reference_sor", False), ("multigrid", True)):
+        o = OracleFluid(1.0, MG_SIDE, MG_SIDE, 1.0, prec=32, threads=threads, scheme=LEXSOR,
+                        UseMultigrid=mg, UseBFECC=True, num_iters=8, early_exit=mg)
+        S = o.S.reshape(o.NumX, o.NumY)
+        S[:] = 1.0
+        S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
+        for i in range(2, o.NumX - 2):
+            o.SetVelocity(i, o.NumY - 2, 1.0, 0.0)
+        t0 = time.perf_counter()
+        o.Simulate(DT)
+        sec = time.perf_counter() - t0
+        out[key] = {"value": MG_SIDE * MG_SIDE / sec / 1e6, "unit": "Mcell-steps/s",
+                    "cores": threads, "kind": "port", "sample": "1 step"}
+    o = OracleFluid(1.0, APP_W, APP_H, 1.0, prec=32, threads=threads, scheme=LEXSOR, num_iters=40,
+                    UseBFECC=True)
+
+    S = o.S.reshape(o.NumX, o.NumY)
+    S[:] = 1.0
+    S[:, 0] = S[:, -1] = S[0, :] = 0.0
+    n = o.NumY
+    for _ in range(5):
+        for j in range(n // 2 - 4, n // 2 + 4):
+            o.SetVelocity(1, j, 2.0, 0.0)
+            o.M[n + j] = 1.0
+        o.Simulate(DT)
+    x, y = spawn_positions(o.NumX, o.NumY, N_PARTICLES)
+    age = np.zeros(N_PARTICLES, np.float32)
+    mx = np.full(N_PARTICLES, 1e9, np.float32)
+    rgb = np.zeros(N_PARTICLES, np.uint32)
+    t0 = time.perf_counter()
+    reps, done = 20, 0
+    for _ in range(reps):
+        k = o.particles_advect(0.01, x, y, age, mx, rgb)
+        done += x.size
+        x, y, age, mx, rgb = x[:k], y[:k], age[:k], mx[:k], rgb[:k]
+    sec = (time.perf_counter() - t0) / max(done, 1) * N_PARTICLES
+    out["particles"] = {"value": N_PARTICLES / sec / 1e6, "unit": "Mparticles/s", "cores": 1,
+                        "kind": "port", "sample": "%d calls over %d particles" % (reps, N_PARTICLES)}
+    big = OracleFluid(1.0, W, H, 1.0, prec=32, threads=threads, scheme=LEXSOR)
+    t0 = time.perf_counter()
+    big.render(3)
+    sec = time.perf_counter() - t0
+    out["render"] = {"value": big.NumX * big.NumY / sec / 1e6, "unit": "Mpixel/s", "cores": 1,
+                     "kind": "port", "sample": "1 vorticity frame at 2048^2"}
+    t0 = time.perf_counter()
+    big.Vorticity()
+    sec = time.perf_counter() - t0
+    out["views"] = {"value": big.NumX * big.NumY / sec / 1e6, "unit": "Mcell/s", "cores": 1,
+                    "kind": "port", "sample": "1 Vorticity() at 2048^2"}
+    return out
+
+
 def cpu_reference_steps(steps, threads, budget_s=None):
     """Times the reference algorithm (FP32, serial SOR pressure, parallelRange
     stages on `threads` host threads) on the cavity workload."""
@@ -656,6 +857,7 @@ def run_ours(args):
     roll = (rollout256(fluid_gb300, args)
             if rank == 0 and not (args.no_adjoint or args.no_rollout) else None)
     ens = ensemble(fluid_gb300, args) if rank == 0 and not args.no_ensemble else None
+    app = app_rows(fluid_gb300) if rank == 0 and not args.no_app else None
 
     # ------------------------------------------------------------ CPU baseline
     cpu = None
@@ -666,6 +868,9 @@ def run_ours(args):
                "cores": threads, "kind": "port",
                "sample": "%d full 2048x2048 step(s) of the reference algorithm (serial SOR "
                          "pressure, FP32), stages on %d host threads" % (len(times), threads)}
+        if app is not None:
+            for k, v in cpu_app_rows(threads).items():
+                app[k]["cpu_baseline"] = v
 
     if rank == 0:
         line = {
@@ -675,7 +880,7 @@ def run_ours(args):
             "data": "synthetic",
             "config": workload_config({"parallelism": "replicas%d" % world if world > 1 else "single"}),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "fwd_adjoint": adj, "rollout_256": roll, "ensemble": ens,
+            "fwd_adjoint": adj, "rollout_256": roll, "ensemble": ens, "app_rows": app,
             "clocks": sampler.summary(),
             "host_ms_per_step": 1e3 * t_host / args.steps,
             "stage_ms": stage_ms,
@@ -698,6 +903,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-rollout", action="store_true")
+    ap.add_argument("--no-app", action="store_true",
+                    help="skip the multigrid, particle, rendering and view rows")
     ap.add_argument("--profile-leg", choices=["adjoint", "ensemble"], default=None,
                     help="bracket that leg's timed region for ncu --profile-from-start off")
     args = ap.parse_args()

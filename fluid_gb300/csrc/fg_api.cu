@@ -476,6 +476,8 @@ int fg_destroy(fg_fluid* f) {
   cudaFree(f->pctl);
   cudaFree(f->ectl);
   cudaFree(f->tile_done);
+  for (float* q : f->skew) cudaFree(q);
+  cudaFree(f->skew_flags);
   for (int k = 0; k < 2; ++k) {
     cudaFree(f->edit_dev[k]);
     cudaFree(f->edit_off_dev[k]);
@@ -606,10 +608,35 @@ int fg_synchronize(fg_fluid* f) {
 
 void* fg_stream(fg_fluid* f) { return f ? (void*)f->stream : nullptr; }
 
+// The diagonal-major copies of the wavefront SOR (LEXSOR and the multigrid
+// smoothers), allocated before the first step that uses them (outside any
+// capture); without them the row-major kernel runs.
+void ensure_skew(fg_fluid* f) {
+  if (f->skew[0] || f->batch || !(f->prm.scheme == FG_SCHEME_LEXSOR || multigrid(f))) return;
+  const int sp = (f->NX + 31) / 32 * 32;
+  const size_t n = (size_t)(f->NX + f->NY - 1) * sp;
+  float* a[3] = {};
+  uint8_t* fl = nullptr;
+  bool ok = true;
+  for (auto& q : a) ok = ok && dev_malloc((void**)&q, n * sizeof(float)) == cudaSuccess;
+  ok = ok && dev_malloc((void**)&fl, n) == cudaSuccess;
+  if (!ok) {
+    for (auto& q : a) cudaFree(q);
+    cudaFree(fl);
+    cudaGetLastError();
+    return;
+  }
+  for (int k = 0; k < 3; ++k) f->skew[k] = a[k];
+  f->skew_flags = fl;
+  f->skew_sp = sp;
+  f->params_version++;  // captured steps run the other kernel sequence
+}
+
 int fg_simulate(fg_fluid* f, float dt) {
   if (!f) return FG_ERR_INVALID;
   int rc = flush(f);
   if (rc) return rc;
+  ensure_skew(f);
   if ((rc = check_iters(f, f->prm.num_iters))) return rc;
   invalidate(f, kStepFields);
   // Profiling brackets the Jacobi launches with timed events, which plain
@@ -706,6 +733,7 @@ int fg_get_stats(fg_fluid* f, fg_stats* out) {
 int fg_make_incompressible(fg_fluid* f, int num_iters, float dt) {
   if (is_batch(f)) return batch_unsupported(f);
   STAGE_PROLOGUE(f);
+  ensure_skew(f);
   if ((rc = check_iters(f, num_iters))) return rc;
   invalidate(f, kStepFields);
   CK(f, launch_clear_stats(f), "clear stats");

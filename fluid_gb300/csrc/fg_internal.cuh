@@ -188,6 +188,9 @@ struct fg_fluid {
   void* pctl = nullptr;   // control block of the main Jacobi solve (k_pressure.cu PCtl)
   int* tile_done = nullptr;  // dataflow Jacobi kernel: per-tile phase flags + item counter
   int stall_tile = -1;       // fault injection: a tile the dataflow kernel never publishes
+  float* skew[3] = {};       // diagonal-major U, V, p of the wavefront SOR (or none)
+  uint8_t* skew_flags = nullptr;
+  int skew_sp = 0;           // their row stride (cells per diagonal)
   void* ectl = nullptr;   // control block of the FP64-residual correction solve
   int n_slots = 0;        // launch slots per control block
   float* copy_tmp = nullptr;        // fg_copy_border staging (2 fields)

@@ -54,11 +54,13 @@ inline dim3 cell_grid(const fg_fluid* f) {
 // ------------------------------------------------------------------ LEXSOR
 constexpr int LEX_THREADS = 1024;
 constexpr int LEX_RING = 2048;  // sweeps in flight (a new sweep waits while the ring is full)
+constexpr int LEX_CHUNK = 4;    // cells whose loads a thread issues together
 
 __global__ void __launch_bounds__(LEX_THREADS)
     k_lexsor(float* U, float* V, float* p, const uint8_t* __restrict__ flags, Grid g,
              int numIters, float relax0, float damping, float cp, float tol, int early_exit,
-             DevStats* st, float minRelax = 1.2f, const int* __restrict__ stop = nullptr) {
+             DevStats* st, float minRelax = 1.2f, const int* __restrict__ stop = nullptr,
+             int SP = 0) {
   __shared__ int s_start[LEX_RING];
   __shared__ unsigned s_max[LEX_RING];
   __shared__ int s_cont[LEX_RING];
@@ -66,6 +68,11 @@ __global__ void __launch_bounds__(LEX_THREADS)
   const int P = g.P;
   const int ni = g.NX - 2, nj = g.NY - 2;  // interior extent
   const int D = ni + nj - 1;               // anti-diagonals d = i + j in [2, NX+NY-4]
+  // Row-major fields (SP = 0): cell (i, j) at i * P + j, its east face +P,
+  // its north face +1.  Diagonal-major copies (SP > 0): cell (i, j) at
+  // (i + j) * SP + i, east +SP+1, north +SP, so a step's accesses are
+  // contiguous along the diagonal.
+  const int offE = SP ? SP + 1 : P, offN = SP ? SP : 1;
   const int L = ni < nj ? ni : nj;         // longest diagonal
   if (threadIdx.x == 0) {
     s_lo = 0;
@@ -91,41 +98,76 @@ __global__ void __launch_bounds__(LEX_THREADS)
   for (long long tau = 0; tau < max_steps; ++tau) {
     int lo = s_lo, hi = s_hi;
     int W = hi - lo;
-    int items = W * L;
-    for (int q = threadIdx.x; q < items; q += LEX_THREADS) {
-      int t = lo + q / L;
-      int k = q - (q / L) * L;
-      int r = t & (LEX_RING - 1);
-      int delta = (int)(tau - s_start[r]);
-      if (delta < 0 || delta >= D) continue;
-      int d = 2 + delta;
-      int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
-      int i = i_lo + k;
-      if (i > i_hi) continue;
-      int j = d - i;
-      int c = i * P + j;
-      uint8_t fl = flags[c];
-      if (!(fl & F_FLUID)) continue;
-      float sx0 = fbit(fl, F_W), sx1 = fbit(fl, F_E), sy0 = fbit(fl, F_S), sy1 = fbit(fl, F_N);
-      float s = sx0 + sx1 + sy0 + sy1;
-      if (s == 0.0f) continue;
-      float div = U[c + P] - U[c] + V[c + 1] - V[c];
-      float absDiv = fabsf(div);
-      if (!isnan(absDiv)) {
-        atomicMax(&s_max[r], __float_as_uint(absDiv));
-        if (absDiv >= tol) s_cont[r] = 1;
+    // Each warp takes 32 cells of one sweep's diagonal (the diagonal length
+    // padded to a multiple of 32), so the sweep's max |div| and its
+    // "cannot exit" mark are reduced in the warp and stored once per warp.
+    // The cells a step updates share no face or pressure value (cells of one
+    // diagonal are not neighbours; sweeps in flight are two diagonals
+    // apart), so a thread loads the inputs of LEX_CHUNK cells at once and
+    // then updates them: one memory round trip per chunk instead of one per
+    // cell.
+    const int Lp = (L + 31) & ~31;
+    const int items = W * Lp;
+    for (int base = 0; base < items; base += LEX_CHUNK * LEX_THREADS) {
+      int cc[LEX_CHUNK], rr[LEX_CHUNK], tt[LEX_CHUNK];
+      bool act[LEX_CHUNK];
+      uint8_t fl[LEX_CHUNK];
+      float u0[LEX_CHUNK], u1[LEX_CHUNK], v0[LEX_CHUNK], v1[LEX_CHUNK], p0[LEX_CHUNK];
+#pragma unroll
+      for (int m = 0; m < LEX_CHUNK; ++m) {
+        const int q = base + m * LEX_THREADS + (int)threadIdx.x;
+        const int t = lo + q / Lp;
+        const int k = q - (q / Lp) * Lp;
+        const int r = t & (LEX_RING - 1);
+        const int delta = q < items ? (int)(tau - s_start[r]) : -1;
+        const int d = 2 + delta;
+        const int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
+        const int i = i_lo + k;
+        const bool in = delta >= 0 && delta < D && k < L && i <= i_hi;
+        const int c = in ? (SP ? d * SP + i : i * P + (d - i)) : 0;
+        cc[m] = c;
+        rr[m] = r;
+        tt[m] = t;
+        act[m] = in;
+        fl[m] = in ? flags[c] : 0;
+        u0[m] = in ? U[c] : 0.0f;
+        u1[m] = in ? U[c + offE] : 0.0f;
+        v0[m] = in ? V[c] : 0.0f;
+        v1[m] = in ? V[c + offN] : 0.0f;
+        p0[m] = in ? p[c] : 0.0f;
       }
-      // Relaxation of sweep t (fluid.go:169-170).
-      float iterProgress = (float)t / (float)numIters;
-      float rel = relax0 - (relax0 - minRelax) * iterProgress;
-      float pp = -div / s;
-      pp *= rel;
-      pp *= damping;
-      p[c] += cp * pp;
-      U[c] -= sx0 * pp;
-      U[c + P] += sx1 * pp;
-      V[c] -= sy0 * pp;
-      V[c + 1] += sy1 * pp;
+#pragma unroll
+      for (int m = 0; m < LEX_CHUNK; ++m) {
+        if (base + m * LEX_THREADS >= items) break;  // (whole warps: items is a multiple of 32)
+        const uint8_t f = fl[m];
+        bool a = act[m] && (f & F_FLUID);
+        const float sx0 = fbit(f, F_W), sx1 = fbit(f, F_E), sy0 = fbit(f, F_S),
+                    sy1 = fbit(f, F_N);
+        const float s = sx0 + sx1 + sy0 + sy1;
+        a = a && s != 0.0f;
+        const float div = a ? u1[m] - u0[m] + v1[m] - v0[m] : 0.0f;
+        const float absDiv = fabsf(div);
+        const bool counted = a && !isnan(absDiv);
+        const unsigned mx = __reduce_max_sync(0xffffffffu, counted ? __float_as_uint(absDiv) : 0u);
+        const bool cont = __any_sync(0xffffffffu, counted && absDiv >= tol);
+        if ((threadIdx.x & 31) == 0) {
+          if (mx) atomicMax(&s_max[rr[m]], mx);
+          if (cont) s_cont[rr[m]] = 1;
+        }
+        if (!a) continue;
+        const int c = cc[m];
+        // Relaxation of sweep t (fluid.go:169-170).
+        float iterProgress = (float)tt[m] / (float)numIters;
+        float rel = relax0 - (relax0 - minRelax) * iterProgress;
+        float pp = -div / s;
+        pp *= rel;
+        pp *= damping;
+        p[c] = p0[m] + cp * pp;
+        U[c] = u0[m] - sx0 * pp;
+        U[c + offE] = u1[m] + sx1 * pp;
+        V[c] = v0[m] - sy0 * pp;
+        V[c + offN] = v1[m] + sy1 * pp;
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -160,6 +202,33 @@ __global__ void __launch_bounds__(LEX_THREADS)
     st->sweeps = s_hi;
     st->last_maxdiv = s_last >= 0 ? (double)__uint_as_float(s_max[s_last & (LEX_RING - 1)]) : 0.0;
   }
+}
+
+// Copies of U, V, p and the flags into the diagonal-major layout of the
+// wavefront kernel (cell (i, j) at (i + j) * SP + i) and of U, V, p back.
+__global__ void k_skew_in(const float* __restrict__ U, const float* __restrict__ V,
+                          const float* __restrict__ p, const uint8_t* __restrict__ flags,
+                          float* __restrict__ sU, float* __restrict__ sV, float* __restrict__ sp,
+                          uint8_t* __restrict__ sf, Grid g, int SP) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const size_t c = (size_t)i * g.P + j, s = (size_t)(i + j) * SP + i;
+  sU[s] = U[c];
+  sV[s] = V[c];
+  sp[s] = p[c];
+  sf[s] = flags[c];
+}
+__global__ void k_skew_out(const float* __restrict__ sU, const float* __restrict__ sV,
+                           const float* __restrict__ sp, float* __restrict__ U,
+                           float* __restrict__ V, float* __restrict__ p, Grid g, int SP) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const size_t c = (size_t)i * g.P + j, s = (size_t)(i + j) * SP + i;
+  U[c] = sU[s];
+  V[c] = sV[s];
+  p[c] = sp[s];
 }
 
 // ------------------------------------------------------------------ multigrid
@@ -210,8 +279,25 @@ __global__ void k_mg_residual(const float* __restrict__ U, const float* __restri
 }
 
 // restrictResidual (fluid.go:630-660) into the coarse grid (pitch cP = cNY).
+// Coarse-grid index of cell (i, j): row-major i * cNY + j (CSP = 0) or
+// diagonal-major (i + j) * CSP + i.
+__device__ __forceinline__ int cidx(int i, int j, int cNY, int CSP) {
+  return CSP ? (i + j) * CSP + i : i * cNY + j;
+}
+
+// The coarse solid mask: the fine cell (2i, 2j) (fluid.go:672-685).
+__device__ __forceinline__ float coarse_s(const uint8_t* __restrict__ flags, int i, int j,
+                                          const Grid& g) {
+  int fi = 2 * i, fj = 2 * j;
+  if (fi >= g.NX || fj >= g.NY) return 0.0f;
+  return (flags[fi * g.P + fj] & F_FLUID) ? 1.0f : 0.0f;
+}
+
+// restrictResidual (fluid.go:630-660) into cr at cidx; with CSP > 0 also the
+// coarse mask of every coarse cell into cmask (same layout).
 __global__ void k_mg_restrict(const float* __restrict__ r, float* __restrict__ cr,
-                              const int* __restrict__ stop, Grid g, int cNX, int cNY) {
+                              const int* __restrict__ stop, Grid g, int cNX, int cNY, int CSP,
+                              const uint8_t* __restrict__ flags, uint8_t* __restrict__ cmask) {
   if (*stop) return;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -226,15 +312,9 @@ __global__ void k_mg_restrict(const float* __restrict__ r, float* __restrict__ c
     float cr4 = (r[c - P - 1] + r[c + P - 1] + r[c - P + 1] + r[c + P + 1]) * 0.0625f;
     out = center + nb + cr4;
   }
-  cr[i * cNY + j] = out;
-}
-
-// The coarse solid mask: the fine cell (2i, 2j) (fluid.go:672-685).
-__device__ __forceinline__ float coarse_s(const uint8_t* __restrict__ flags, int i, int j,
-                                          const Grid& g) {
-  int fi = 2 * i, fj = 2 * j;
-  if (fi >= g.NX || fj >= g.NY) return 0.0f;
-  return (flags[fi * g.P + fj] & F_FLUID) ? 1.0f : 0.0f;
+  const int ci = cidx(i, j, cNY, CSP);
+  cr[ci] = out;
+  if (CSP) cmask[ci] = coarse_s(flags, i, j, g) != 0.0f ? 1 : 0;
 }
 
 // solveCoarseGrid (fluid.go:662-715): 40 lexicographic Gauss-Seidel sweeps
@@ -242,13 +322,20 @@ __device__ __forceinline__ float coarse_s(const uint8_t* __restrict__ flags, int
 // of that sweep and (i+1, j), (i, j+1) of the previous one, so the sweeps
 // run as anti-diagonal wavefronts, each two diagonals behind the previous.
 constexpr int MG_THREADS = 1024;
+constexpr int MG_CHUNK = 4;  // cells whose loads a thread issues together
 __global__ void __launch_bounds__(MG_THREADS)
     k_mg_coarse(const float* __restrict__ cr, float* __restrict__ cp_,
                 const uint8_t* __restrict__ flags, const int* __restrict__ stop, Grid g, int cNX,
-                int cNY, int sweeps, float relaxation) {
+                int cNY, int sweeps, float relaxation, int CSP,
+                const uint8_t* __restrict__ cmask) {
   if (*stop) return;
   const int ni = cNX - 2, nj = cNY - 2;
-  for (int k = threadIdx.x; k < cNX * cNY; k += MG_THREADS) cp_[k] = 0.0f;
+  // Row-major (CSP = 0): neighbours at -cNY, +cNY, -1, +1.  Diagonal-major:
+  // west -(CSP+1), east +(CSP+1), south -CSP, north +CSP, and the cells of a
+  // step contiguous along their diagonal.
+  const int oW = CSP ? CSP + 1 : cNY, oS = CSP ? CSP : 1;
+  const int n0 = CSP ? (cNX + cNY - 1) * CSP : cNX * cNY;
+  for (int k = threadIdx.x; k < n0; k += MG_THREADS) cp_[k] = 0.0f;
   __syncthreads();
   if (ni <= 0 || nj <= 0) return;
   const int D = ni + nj - 1;
@@ -262,26 +349,61 @@ __global__ void __launch_bounds__(MG_THREADS)
     int t_hi = (int)(tau / 2);
     if (t_hi > sweeps - 1) t_hi = sweeps - 1;
     int nact = t_hi - t_lo + 1;
-    for (int q = threadIdx.x; q < nact * L; q += MG_THREADS) {
-      int t = t_lo + q / L;
-      int k = q - (q / L) * L;
-      int d = (int)(tau - 2LL * t) + 2;
-      int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
-      int i = i_lo + k;
-      if (i > i_hi) continue;
-      int j = d - i;
-      if (coarse_s(flags, i, j, g) == 0.0f) continue;
-      float sx0 = coarse_s(flags, i - 1, j, g), sx1 = coarse_s(flags, i + 1, j, g);
-      float sy0 = coarse_s(flags, i, j - 1, g), sy1 = coarse_s(flags, i, j + 1, g);
-      float s = sx0 + sx1 + sy0 + sy1;
-      if (s == 0.0f) continue;
-      int c = i * cNY + j;
-      float pc = cp_[c];
-      float lap = sx0 * (cp_[c - cNY] - pc) + sx1 * (cp_[c + cNY] - pc) + sy0 * (cp_[c - 1] - pc) +
-                  sy1 * (cp_[c + 1] - pc);
-      float residual = cr[c] - lap;
-      float correction = -residual / s * relaxation;
-      cp_[c] = pc + correction;
+    // The cells of a step are independent (one diagonal per sweep in flight,
+    // sweeps two diagonals apart, no cell reads another's value): a thread
+    // loads the inputs of MG_CHUNK cells at once, then updates them.
+    const int items = nact * L;
+    for (int base = 0; base < items; base += MG_CHUNK * MG_THREADS) {
+      int cc[MG_CHUNK];
+      bool in[MG_CHUNK];
+      float s0[MG_CHUNK], s1[MG_CHUNK], s2[MG_CHUNK], s3[MG_CHUNK], sc[MG_CHUNK];
+      float pc[MG_CHUNK], pw[MG_CHUNK], pe[MG_CHUNK], ps[MG_CHUNK], pn[MG_CHUNK], rc[MG_CHUNK];
+#pragma unroll
+      for (int m = 0; m < MG_CHUNK; ++m) {
+        const int q = base + m * MG_THREADS + (int)threadIdx.x;
+        const int t = t_lo + q / L;
+        const int k = q - (q / L) * L;
+        const int d = (int)(tau - 2LL * t) + 2;
+        const int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
+        const int i = i_lo + k;
+        const bool ok = q < items && i <= i_hi;
+        const int j = d - i;
+        const int c = ok ? cidx(i, j, cNY, CSP) : 0;
+        cc[m] = c;
+        in[m] = ok;
+        if (CSP) {
+          sc[m] = ok ? (float)cmask[c] : 0.0f;
+          s0[m] = ok ? (float)cmask[c - oW] : 0.0f;
+          s1[m] = ok ? (float)cmask[c + oW] : 0.0f;
+          s2[m] = ok ? (float)cmask[c - oS] : 0.0f;
+          s3[m] = ok ? (float)cmask[c + oS] : 0.0f;
+        } else {
+          sc[m] = ok ? coarse_s(flags, i, j, g) : 0.0f;
+          s0[m] = ok ? coarse_s(flags, i - 1, j, g) : 0.0f;
+          s1[m] = ok ? coarse_s(flags, i + 1, j, g) : 0.0f;
+          s2[m] = ok ? coarse_s(flags, i, j - 1, g) : 0.0f;
+          s3[m] = ok ? coarse_s(flags, i, j + 1, g) : 0.0f;
+        }
+        pc[m] = ok ? cp_[c] : 0.0f;
+        pw[m] = ok ? cp_[c - oW] : 0.0f;
+        pe[m] = ok ? cp_[c + oW] : 0.0f;
+        ps[m] = ok ? cp_[c - oS] : 0.0f;
+        pn[m] = ok ? cp_[c + oS] : 0.0f;
+        rc[m] = ok ? cr[c] : 0.0f;
+      }
+#pragma unroll
+      for (int m = 0; m < MG_CHUNK; ++m) {
+        if (!in[m] || sc[m] == 0.0f) continue;
+        const float sx0 = s0[m], sx1 = s1[m], sy0 = s2[m], sy1 = s3[m];
+        const float s = sx0 + sx1 + sy0 + sy1;
+        if (s == 0.0f) continue;
+        const float p0 = pc[m];
+        float lap = sx0 * (pw[m] - p0) + sx1 * (pe[m] - p0) + sy0 * (ps[m] - p0) +
+                    sy1 * (pn[m] - p0);
+        float residual = rc[m] - lap;
+        float correction = -residual / s * relaxation;
+        cp_[cc[m]] = p0 + correction;
+      }
     }
     __syncthreads();
   }
@@ -289,13 +411,14 @@ __global__ void __launch_bounds__(MG_THREADS)
 
 // prolongateCorrection (fluid.go:717-758) at fine cell (i, j).
 __device__ __forceinline__ float mg_corr(const float* __restrict__ cc, int i, int j, int cNX,
-                                         int cNY) {
+                                         int cNY, int CSP) {
   int ci = i / 2, cj = j / 2;
   if (ci >= cNX - 1 || cj >= cNY - 1) return 0.0f;
   float fI = (float)(i % 2) * 0.5f, fJ = (float)(j % 2) * 0.5f;
-  return (1.0f - fI) * (1.0f - fJ) * cc[ci * cNY + cj] +
-         fI * (1.0f - fJ) * cc[(ci + 1) * cNY + cj] + (1.0f - fI) * fJ * cc[ci * cNY + cj + 1] +
-         fI * fJ * cc[(ci + 1) * cNY + cj + 1];
+  return (1.0f - fI) * (1.0f - fJ) * cc[cidx(ci, cj, cNY, CSP)] +
+         fI * (1.0f - fJ) * cc[cidx(ci + 1, cj, cNY, CSP)] +
+         (1.0f - fI) * fJ * cc[cidx(ci, cj + 1, cNY, CSP)] +
+         fI * fJ * cc[cidx(ci + 1, cj + 1, cNY, CSP)];
 }
 
 // applePressureCorrection (fluid.go:1122-1149): p += corr * cp on fluid
@@ -304,7 +427,8 @@ __device__ __forceinline__ float mg_corr(const float* __restrict__ cc, int i, in
 // them; V likewise along j.
 __global__ void k_mg_apply(float* __restrict__ U, float* __restrict__ V, float* __restrict__ p,
                            const float* __restrict__ cc, const uint8_t* __restrict__ flags,
-                           const int* __restrict__ stop, float cp, Grid g, int cNX, int cNY) {
+                           const int* __restrict__ stop, float cp, Grid g, int cNX, int cNY,
+                           int CSP) {
   if (*stop) return;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -316,18 +440,18 @@ __global__ void k_mg_apply(float* __restrict__ U, float* __restrict__ V, float* 
            (flags[a * P + b] & F_FLUID) != 0;
   };
   bool self = fluid_int(i, j);
-  float corr = self ? mg_corr(cc, i, j, cNX, cNY) : 0.0f;
+  float corr = self ? mg_corr(cc, i, j, cNX, cNY, CSP) : 0.0f;
   if (self) p[c] += corr * cp;
   uint8_t fl = flags[c];
   if (i >= 1) {
     float u = U[c];
-    if (fluid_int(i - 1, j)) u += fbit(fl, F_FLUID) * mg_corr(cc, i - 1, j, cNX, cNY);
+    if (fluid_int(i - 1, j)) u += fbit(fl, F_FLUID) * mg_corr(cc, i - 1, j, cNX, cNY, CSP);
     if (self) u -= fbit(fl, F_W) * corr;
     U[c] = u;
   }
   if (j >= 1) {
     float v = V[c];
-    if (fluid_int(i, j - 1)) v += fbit(fl, F_FLUID) * mg_corr(cc, i, j - 1, cNX, cNY);
+    if (fluid_int(i, j - 1)) v += fbit(fl, F_FLUID) * mg_corr(cc, i, j - 1, cNX, cNY, CSP);
     if (self) v -= fbit(fl, F_S) * corr;
     V[c] = v;
   }
@@ -1647,6 +1771,30 @@ cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const fl
   return jacobi_solve(f, (PCtl*)ctl, b, bw, x0, x1, iters, false);
 }
 
+// One k_lexsor solve on the handle's fields: on the diagonal-major copies
+// when the handle has them (copied in and back around the solve), else on
+// the row-major fields.
+static void run_lexsor(fg_fluid* f, int iters, float relax0, float cp, int early_exit,
+                       DevStats* st, float minRelax, const int* stop) {
+  if (f->skew[0]) {
+    dim3 gr = cell_grid(f), bl(BX, BY);
+    const Grid& g = f->g;
+    k_skew_in<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->skew[0],
+                                        f->skew[1], f->skew[2], f->skew_flags, g, f->skew_sp);
+    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->skew[0], f->skew[1], f->skew[2], f->skew_flags,
+                                                g, iters, relax0, f->prm.pressure_damping, cp,
+                                                f->prm.tolerance, early_exit, st, minRelax, stop,
+                                                f->skew_sp);
+    k_skew_out<<<gr, bl, 0, f->stream>>>(f->skew[0], f->skew[1], f->skew[2], f->d[FG_U],
+                                         f->d[FG_V], f->d[FG_P], g, f->skew_sp);
+    count(f, 2);
+  } else {
+    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->g,
+                                                iters, relax0, f->prm.pressure_damping, cp,
+                                                f->prm.tolerance, early_exit, st, minRelax, stop);
+  }
+}
+
 cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt) {
   float cp = f->density * f->h / dt;  // fluid.go:560
   const int cNX = (f->NX + 1) / 2, cNY = (f->NY + 1) / 2;
@@ -1660,22 +1808,24 @@ cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt) {
   if (e != cudaSuccess) return e;
   dim3 gr = cell_grid(f), bl(BX, BY);
   dim3 cg((cNY + BX - 1) / BX, (cNX + BY - 1) / BY);
+  // The coarse grid diagonal-major when it fits the scratch fields (err,
+  // err2; its mask in rhs_e) and the fine one is (the handle has the copies).
+  const int csp = (cNX + 31) / 32 * 32;
+  const int CSP = f->skew[0] && (size_t)(cNX + cNY - 1) * csp <= (size_t)f->NX * f->P ? csp : 0;
+  uint8_t* cmask = reinterpret_cast<uint8_t*>(f->rhs_e);
   for (int it = 0; it < num_iters; ++it) {
     count(f, 8);
-    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->g,
-                                                3, 1.5f, f->prm.pressure_damping, cp,
-                                                f->prm.tolerance, 0, sm, 1.5f, stop);
+    run_lexsor(f, 3, 1.5f, cp, 0, sm, 1.5f, stop);
     k_mg_check<<<1, 1, 0, f->stream>>>(sm, f->dstats, stop, f->prm.tolerance, 0);
     k_mg_residual<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->rhs,
                                             stop, f->g);
-    k_mg_restrict<<<cg, bl, 0, f->stream>>>(f->rhs, f->err, stop, f->g, cNX, cNY);
+    k_mg_restrict<<<cg, bl, 0, f->stream>>>(f->rhs, f->err, stop, f->g, cNX, cNY, CSP, f->flags,
+                                            cmask);
     k_mg_coarse<<<1, MG_THREADS, 0, f->stream>>>(f->err, f->err2, f->flags, stop, f->g, cNX, cNY,
-                                                 40, 1.6f);
+                                                 40, 1.6f, CSP, cmask);
     k_mg_apply<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->err2, f->flags,
-                                         stop, cp, f->g, cNX, cNY);
-    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->g,
-                                                3, 1.2f, f->prm.pressure_damping, cp,
-                                                f->prm.tolerance, 0, sm, 1.2f, stop);
+                                         stop, cp, f->g, cNX, cNY, CSP);
+    run_lexsor(f, 3, 1.2f, cp, 0, sm, 1.2f, stop);
     k_mg_check<<<1, 1, 0, f->stream>>>(sm, f->dstats, stop, f->prm.tolerance, 1);
   }
   return cudaGetLastError();
@@ -1686,10 +1836,7 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   cudaError_t e;
   if (f->prm.scheme == FG_SCHEME_LEXSOR) {
     count(f);
-    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags,
-                                                f->g, num_iters, f->prm.relaxation,
-                                                f->prm.pressure_damping, cp, f->prm.tolerance,
-                                                f->prm.early_exit, f->dstats);
+    run_lexsor(f, num_iters, f->prm.relaxation, cp, f->prm.early_exit, f->dstats, 1.2f, nullptr);
     return cudaGetLastError();
   }
   PCtl* ctl = (PCtl*)f->pctl;
