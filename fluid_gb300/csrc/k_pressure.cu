@@ -84,6 +84,107 @@ __global__ void __launch_bounds__(LEX_THREADS)
   __syncthreads();
   if (numIters <= 0 || ni <= 0 || nj <= 0) return;
   if (stop && *stop) return;  // a multigrid solve that already converged
+  // The cells of the W sweeps lo .. lo+W-1 that step tau reaches; sweep t is
+  // on diagonal 2 + delta_of(t) (out of range: not running) and its max
+  // |div| goes to s_max[r] (r = t mod LEX_RING).
+  auto step = [&](long long tau, int lo, int W, auto delta_of) {
+      // Each warp takes 32 cells of one sweep's diagonal (the diagonal length
+      // padded to a multiple of 32), so the sweep's max |div| and its
+      // "cannot exit" mark are reduced in the warp and stored once per warp.
+      // The cells a step updates share no face or pressure value (cells of one
+      // diagonal are not neighbours; sweeps in flight are two diagonals
+      // apart), so a thread loads the inputs of LEX_CHUNK cells at once and
+      // then updates them: one memory round trip per chunk instead of one per
+      // cell.
+      const int Lp = (L + 31) & ~31;
+      const int items = W * Lp;
+      for (int base = 0; base < items; base += LEX_CHUNK * LEX_THREADS) {
+        int cc[LEX_CHUNK], rr[LEX_CHUNK], tt[LEX_CHUNK];
+        bool act[LEX_CHUNK];
+        uint8_t fl[LEX_CHUNK];
+        float u0[LEX_CHUNK], u1[LEX_CHUNK], v0[LEX_CHUNK], v1[LEX_CHUNK], p0[LEX_CHUNK];
+#pragma unroll
+        for (int m = 0; m < LEX_CHUNK; ++m) {
+          const int q = base + m * LEX_THREADS + (int)threadIdx.x;
+          const int t = lo + q / Lp;
+          const int k = q - (q / Lp) * Lp;
+          const int r = t & (LEX_RING - 1);
+          const int delta = q < items ? delta_of(t) : -1;
+          const int d = 2 + delta;
+          const int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
+          const int i = i_lo + k;
+          const bool in = delta >= 0 && delta < D && k < L && i <= i_hi;
+          const int c = in ? (SP ? d * SP + i : i * P + (d - i)) : 0;
+          cc[m] = c;
+          rr[m] = r;
+          tt[m] = t;
+          act[m] = in;
+          fl[m] = in ? flags[c] : 0;
+          u0[m] = in ? U[c] : 0.0f;
+          u1[m] = in ? U[c + offE] : 0.0f;
+          v0[m] = in ? V[c] : 0.0f;
+          v1[m] = in ? V[c + offN] : 0.0f;
+          p0[m] = in ? p[c] : 0.0f;
+        }
+#pragma unroll
+        for (int m = 0; m < LEX_CHUNK; ++m) {
+          if (base + m * LEX_THREADS >= items) break;  // (whole warps: items is a multiple of 32)
+          const uint8_t f = fl[m];
+          bool a = act[m] && (f & F_FLUID);
+          const float sx0 = fbit(f, F_W), sx1 = fbit(f, F_E), sy0 = fbit(f, F_S),
+                      sy1 = fbit(f, F_N);
+          const float s = sx0 + sx1 + sy0 + sy1;
+          a = a && s != 0.0f;
+          const float div = a ? u1[m] - u0[m] + v1[m] - v0[m] : 0.0f;
+          const float absDiv = fabsf(div);
+          const bool counted = a && !isnan(absDiv);
+          const unsigned mx = __reduce_max_sync(0xffffffffu, counted ? __float_as_uint(absDiv) : 0u);
+          const bool cont = __any_sync(0xffffffffu, counted && absDiv >= tol);
+          // (Without the early exit only the last sweep's max is reported,
+          // and more sweeps than ring slots may be in flight.)
+          if ((threadIdx.x & 31) == 0 && (early_exit || tt[m] == numIters - 1)) {
+            if (mx) atomicMax(&s_max[rr[m]], mx);
+            if (cont) s_cont[rr[m]] = 1;
+          }
+          if (!a) continue;
+          const int c = cc[m];
+          // Relaxation of sweep t (fluid.go:169-170).
+          float iterProgress = (float)tt[m] / (float)numIters;
+          float rel = relax0 - (relax0 - minRelax) * iterProgress;
+          float pp = -div / s;
+          pp *= rel;
+          pp *= damping;
+          p[c] = p0[m] + cp * pp;
+          U[c] = u0[m] - sx0 * pp;
+          U[c + offE] = u1[m] + sx1 * pp;
+          V[c] = v0[m] - sy0 * pp;
+          V[c + offN] = v1[m] + sy1 * pp;
+        }
+      }
+  };
+  if (!early_exit) {
+    // Without the early exit sweep t always starts at step 2t (two steps
+    // after the previous one, as the bookkeeping below would start it):
+    // sweep t covers steps 2t .. 2t + D - 1 and the steps need no
+    // bookkeeping between them, one barrier each.
+    for (int r = threadIdx.x; r < LEX_RING; r += LEX_THREADS) s_max[r] = 0u;
+    __syncthreads();
+    const long long steps = (long long)D + 2LL * (numIters - 1);
+    for (long long tau = 0; tau < steps; ++tau) {
+      int t_lo = (int)((tau - D + 2) / 2);
+      if (t_lo < 0) t_lo = 0;
+      while (tau - 2LL * t_lo >= D) ++t_lo;
+      int t_hi = (int)(tau / 2);
+      if (t_hi > numIters - 1) t_hi = numIters - 1;
+      step(tau, t_lo, t_hi - t_lo + 1, [&](int t) { return (int)(tau - 2LL * t); });
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      st->sweeps = numIters;
+      st->last_maxdiv = (double)__uint_as_float(s_max[(numIters - 1) & (LEX_RING - 1)]);
+    }
+    return;
+  }
   // Start sweep 0 at step 0.
   if (threadIdx.x == 0) {
     s_start[0] = 0;
@@ -96,79 +197,8 @@ __global__ void __launch_bounds__(LEX_THREADS)
   // the previous one.
   const long long max_steps = (long long)numIters * (D + 2) + D + 4;
   for (long long tau = 0; tau < max_steps; ++tau) {
-    int lo = s_lo, hi = s_hi;
-    int W = hi - lo;
-    // Each warp takes 32 cells of one sweep's diagonal (the diagonal length
-    // padded to a multiple of 32), so the sweep's max |div| and its
-    // "cannot exit" mark are reduced in the warp and stored once per warp.
-    // The cells a step updates share no face or pressure value (cells of one
-    // diagonal are not neighbours; sweeps in flight are two diagonals
-    // apart), so a thread loads the inputs of LEX_CHUNK cells at once and
-    // then updates them: one memory round trip per chunk instead of one per
-    // cell.
-    const int Lp = (L + 31) & ~31;
-    const int items = W * Lp;
-    for (int base = 0; base < items; base += LEX_CHUNK * LEX_THREADS) {
-      int cc[LEX_CHUNK], rr[LEX_CHUNK], tt[LEX_CHUNK];
-      bool act[LEX_CHUNK];
-      uint8_t fl[LEX_CHUNK];
-      float u0[LEX_CHUNK], u1[LEX_CHUNK], v0[LEX_CHUNK], v1[LEX_CHUNK], p0[LEX_CHUNK];
-#pragma unroll
-      for (int m = 0; m < LEX_CHUNK; ++m) {
-        const int q = base + m * LEX_THREADS + (int)threadIdx.x;
-        const int t = lo + q / Lp;
-        const int k = q - (q / Lp) * Lp;
-        const int r = t & (LEX_RING - 1);
-        const int delta = q < items ? (int)(tau - s_start[r]) : -1;
-        const int d = 2 + delta;
-        const int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
-        const int i = i_lo + k;
-        const bool in = delta >= 0 && delta < D && k < L && i <= i_hi;
-        const int c = in ? (SP ? d * SP + i : i * P + (d - i)) : 0;
-        cc[m] = c;
-        rr[m] = r;
-        tt[m] = t;
-        act[m] = in;
-        fl[m] = in ? flags[c] : 0;
-        u0[m] = in ? U[c] : 0.0f;
-        u1[m] = in ? U[c + offE] : 0.0f;
-        v0[m] = in ? V[c] : 0.0f;
-        v1[m] = in ? V[c + offN] : 0.0f;
-        p0[m] = in ? p[c] : 0.0f;
-      }
-#pragma unroll
-      for (int m = 0; m < LEX_CHUNK; ++m) {
-        if (base + m * LEX_THREADS >= items) break;  // (whole warps: items is a multiple of 32)
-        const uint8_t f = fl[m];
-        bool a = act[m] && (f & F_FLUID);
-        const float sx0 = fbit(f, F_W), sx1 = fbit(f, F_E), sy0 = fbit(f, F_S),
-                    sy1 = fbit(f, F_N);
-        const float s = sx0 + sx1 + sy0 + sy1;
-        a = a && s != 0.0f;
-        const float div = a ? u1[m] - u0[m] + v1[m] - v0[m] : 0.0f;
-        const float absDiv = fabsf(div);
-        const bool counted = a && !isnan(absDiv);
-        const unsigned mx = __reduce_max_sync(0xffffffffu, counted ? __float_as_uint(absDiv) : 0u);
-        const bool cont = __any_sync(0xffffffffu, counted && absDiv >= tol);
-        if ((threadIdx.x & 31) == 0) {
-          if (mx) atomicMax(&s_max[rr[m]], mx);
-          if (cont) s_cont[rr[m]] = 1;
-        }
-        if (!a) continue;
-        const int c = cc[m];
-        // Relaxation of sweep t (fluid.go:169-170).
-        float iterProgress = (float)tt[m] / (float)numIters;
-        float rel = relax0 - (relax0 - minRelax) * iterProgress;
-        float pp = -div / s;
-        pp *= rel;
-        pp *= damping;
-        p[c] = p0[m] + cp * pp;
-        U[c] = u0[m] - sx0 * pp;
-        U[c + offE] = u1[m] + sx1 * pp;
-        V[c] = v0[m] - sy0 * pp;
-        V[c + offN] = v1[m] + sy1 * pp;
-      }
-    }
+    const int lo = s_lo, hi = s_hi;
+    step(tau, lo, hi - lo, [&](int t) { return (int)(tau - s_start[t & (LEX_RING - 1)]); });
     __syncthreads();
     if (threadIdx.x == 0) {
       // Retire sweeps whose last diagonal ran in this step.
