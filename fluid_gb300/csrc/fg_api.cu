@@ -383,6 +383,7 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
   };
   if (cudaGetDevice(&f->device) != cudaSuccess) return bail(FG_ERR_CUDA);
   init_jacobi_tma();
+  init_lexsor_cluster();
   if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(FG_ERR_CUDA);
   for (int k = 0; k < 2; ++k) {

@@ -307,6 +307,7 @@ cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt);
 // K Jacobi sweeps of A x = b from x = 0 (no early exit); ctl->sel names the
 // buffer holding x.
 void init_jacobi_tma();
+void init_lexsor_cluster();
 int jacobi_tile_count(int NX, int NY);
 cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const float* bw, float* x0,
                                 float* x1, int iters);

@@ -23,6 +23,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <atomic>
 #include <climits>
 #include <mutex>
@@ -45,6 +46,10 @@ struct PCtl {
 };
 
 namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
 
 constexpr int BX = 32, BY = 8;
 inline dim3 cell_grid(const fg_fluid* f) {
@@ -232,6 +237,206 @@ __global__ void __launch_bounds__(LEX_THREADS)
     st->sweeps = s_hi;
     st->last_maxdiv = s_last >= 0 ? (double)__uint_as_float(s_max[s_last & (LEX_RING - 1)]) : 0.0;
   }
+}
+
+// ------------------------------------------------------------------ LEXSOR on a cluster
+// k_lexsor's schedule on a thread-block cluster of LEX_CLUSTER blocks (one
+// SM each): the cells of a step are spread over all of the cluster's
+// threads and every step ends with a cluster barrier (release / acquire, so
+// the steps' global stores are ordered for the whole cluster; the fields are
+// read past L1).  The sweep bookkeeping (start steps, maxima, "cannot exit"
+// marks, retire / start decisions) lives in the shared memory of block rank
+// 0; the other blocks read and update it through distributed shared memory.
+// With the early exit a step takes two cluster barriers (the step, then rank
+// 0's decisions); without it the closed-form schedule needs one.
+constexpr int LEX_CLUSTER = 8;
+
+__device__ __forceinline__ unsigned cl_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cl_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;"
+               ::: "memory");
+}
+// Shared-window address of `p` (a shared variable) in block `rank` of the cluster.
+__device__ __forceinline__ uint32_t cl_map(const void* p, unsigned rank) {
+  uint32_t a;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(p)), "r"(rank));
+  return a;
+}
+__device__ __forceinline__ int cl_ld(uint32_t a) {
+  int v;
+  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void cl_st(uint32_t a, int v) {
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void cl_max(uint32_t a, unsigned v) {
+  asm volatile("red.shared::cluster.max.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(LEX_THREADS)
+    k_lexsor_cl(float* U, float* V, float* p, const uint8_t* __restrict__ flags, Grid g,
+                int numIters, float relax0, float damping, float cp, float tol, int early_exit,
+                DevStats* st, float minRelax, const int* __restrict__ stop, int SP) {
+  __shared__ int s_start[LEX_RING];
+  __shared__ unsigned s_max[LEX_RING];
+  __shared__ int s_cont[LEX_RING];
+  __shared__ int s_lo, s_hi, s_done, s_exit, s_last;
+  const unsigned rank = cl_rank();
+  const int P = g.P;
+  const int ni = g.NX - 2, nj = g.NY - 2;
+  const int D = ni + nj - 1;
+  const int offE = SP ? SP + 1 : P, offN = SP ? SP : 1;
+  const int L = ni < nj ? ni : nj;
+  // Rank 0's bookkeeping, as seen from this block.
+  const uint32_t a_start = cl_map(s_start, 0), a_max = cl_map(s_max, 0),
+                 a_cont = cl_map(s_cont, 0), a_lo = cl_map(&s_lo, 0), a_hi = cl_map(&s_hi, 0),
+                 a_done = cl_map(&s_done, 0);
+  if (rank == 0) {
+    for (int r = threadIdx.x; r < LEX_RING; r += LEX_THREADS) {
+      s_max[r] = 0u;
+      s_cont[r] = 0;
+    }
+    if (threadIdx.x == 0) {
+      s_start[0] = 0;
+      s_lo = 0;
+      s_hi = 1;
+      s_done = 0;
+      s_exit = 0;
+      s_last = -1;
+    }
+  }
+  cl_sync();
+  if (numIters <= 0 || ni <= 0 || nj <= 0) return;  // (the same in every block)
+  if (stop && *stop) return;
+  const int gt = (int)rank * LEX_THREADS + (int)threadIdx.x;
+  const int stride = LEX_CLUSTER * LEX_THREADS;
+  const int Lp = (L + 31) & ~31;
+  auto step = [&](long long tau, int lo, int W, auto delta_of) {
+    const int items = W * Lp;
+    for (int base = 0; base < items; base += LEX_CHUNK * stride) {
+      int cc[LEX_CHUNK], rr[LEX_CHUNK], tt[LEX_CHUNK];
+      bool act[LEX_CHUNK];
+      uint8_t fl[LEX_CHUNK];
+      float u0[LEX_CHUNK], u1[LEX_CHUNK], v0[LEX_CHUNK], v1[LEX_CHUNK], p0[LEX_CHUNK];
+#pragma unroll
+      for (int m = 0; m < LEX_CHUNK; ++m) {
+        const int q = base + m * stride + gt;
+        const int t = lo + q / Lp;
+        const int k = q - (q / Lp) * Lp;
+        const int r = t & (LEX_RING - 1);
+        const int delta = q < items ? delta_of(t) : -1;
+        const int d = 2 + delta;
+        const int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
+        const int i = i_lo + k;
+        const bool in = delta >= 0 && delta < D && k < L && i <= i_hi;
+        const int c = in ? (SP ? d * SP + i : i * P + (d - i)) : 0;
+        cc[m] = c;
+        rr[m] = r;
+        tt[m] = t;
+        act[m] = in;
+        fl[m] = in ? __ldcg(flags + c) : 0;
+        u0[m] = in ? __ldcg(U + c) : 0.0f;
+        u1[m] = in ? __ldcg(U + c + offE) : 0.0f;
+        v0[m] = in ? __ldcg(V + c) : 0.0f;
+        v1[m] = in ? __ldcg(V + c + offN) : 0.0f;
+        p0[m] = in ? __ldcg(p + c) : 0.0f;
+      }
+#pragma unroll
+      for (int m = 0; m < LEX_CHUNK; ++m) {
+        if (base + m * stride >= items) break;  // (whole warps: items is a multiple of 32)
+        const uint8_t f = fl[m];
+        bool a = act[m] && (f & F_FLUID);
+        const float sx0 = fbit(f, F_W), sx1 = fbit(f, F_E), sy0 = fbit(f, F_S),
+                    sy1 = fbit(f, F_N);
+        const float s = sx0 + sx1 + sy0 + sy1;
+        a = a && s != 0.0f;
+        const float div = a ? u1[m] - u0[m] + v1[m] - v0[m] : 0.0f;
+        const float absDiv = fabsf(div);
+        const bool counted = a && !isnan(absDiv);
+        const unsigned mx = __reduce_max_sync(0xffffffffu, counted ? __float_as_uint(absDiv) : 0u);
+        const bool cont = __any_sync(0xffffffffu, counted && absDiv >= tol);
+        if ((threadIdx.x & 31) == 0 && (early_exit || tt[m] == numIters - 1)) {
+          if (mx) cl_max(a_max + 4u * rr[m], mx);
+          if (cont) cl_st(a_cont + 4u * rr[m], 1);
+        }
+        if (!a) continue;
+        const int c = cc[m];
+        // Relaxation of sweep t (fluid.go:169-170).
+        float iterProgress = (float)tt[m] / (float)numIters;
+        float rel = relax0 - (relax0 - minRelax) * iterProgress;
+        float pp = -div / s;
+        pp *= rel;
+        pp *= damping;
+        p[c] = p0[m] + cp * pp;
+        U[c] = u0[m] - sx0 * pp;
+        U[c + offE] = u1[m] + sx1 * pp;
+        V[c] = v0[m] - sy0 * pp;
+        V[c + offN] = v1[m] + sy1 * pp;
+      }
+    }
+  };
+  if (!early_exit) {
+    const long long steps = (long long)D + 2LL * (numIters - 1);
+    for (long long tau = 0; tau < steps; ++tau) {
+      int t_lo = (int)((tau - D + 2) / 2);
+      if (t_lo < 0) t_lo = 0;
+      while (tau - 2LL * t_lo >= D) ++t_lo;
+      int t_hi = (int)(tau / 2);
+      if (t_hi > numIters - 1) t_hi = numIters - 1;
+      step(tau, t_lo, t_hi - t_lo + 1, [&](int t) { return (int)(tau - 2LL * t); });
+      cl_sync();
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+      st->sweeps = numIters;
+      st->last_maxdiv = (double)__uint_as_float(s_max[(numIters - 1) & (LEX_RING - 1)]);
+    }
+    cl_sync();  // (no block leaves while others may still address rank 0)
+    return;
+  }
+  const long long max_steps = (long long)numIters * (D + 2) + D + 4;
+  for (long long tau = 0; tau < max_steps; ++tau) {
+    const int lo = cl_ld(a_lo), hi = cl_ld(a_hi);
+    step(tau, lo, hi - lo,
+         [&](int t) { return (int)(tau - cl_ld(a_start + 4u * (t & (LEX_RING - 1)))); });
+    cl_sync();
+    if (rank == 0 && threadIdx.x == 0) {
+      // Retire sweeps whose last diagonal ran in this step.
+      while (s_lo < s_hi && tau - s_start[s_lo & (LEX_RING - 1)] >= D - 1) {
+        int r = s_lo & (LEX_RING - 1);
+        s_last = s_lo;
+        if (__uint_as_float(s_max[r]) < tol) s_exit = 1;
+        ++s_lo;
+      }
+      // Start the next sweep if allowed.
+      int nxt = s_hi;
+      if (!s_exit && nxt < numIters) {
+        int pr = (nxt - 1) & (LEX_RING - 1);
+        bool prev_done = s_lo > nxt - 1;
+        bool gap_ok = prev_done || (tau + 1 - s_start[pr] >= 2);
+        bool safe = prev_done || s_cont[pr];
+        if (gap_ok && safe && nxt - s_lo < LEX_RING) {
+          int r = nxt & (LEX_RING - 1);
+          s_start[r] = (int)(tau + 1);
+          s_max[r] = 0u;
+          s_cont[r] = 0;
+          s_hi = nxt + 1;
+        }
+      }
+      if (s_lo == s_hi && (s_exit || s_hi >= numIters)) s_done = 1;
+    }
+    cl_sync();
+    if (cl_ld(a_done)) break;
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    st->sweeps = s_hi;
+    st->last_maxdiv = s_last >= 0 ? (double)__uint_as_float(s_max[s_last & (LEX_RING - 1)]) : 0.0;
+  }
+  cl_sync();
 }
 
 // Copies of U, V, p and the flags into the diagonal-major layout of the
@@ -841,9 +1046,6 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
 // 128, zero outside the arrays) into shared memory while the block sweeps the
 // current tile in registers, so the loads no longer sit in front of the
 // sweeps.  Same per-cell arithmetic as k_jacobi_rb, same results.
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1804,6 +2006,57 @@ cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const fl
 // One k_lexsor solve on the handle's fields: on the diagonal-major copies
 // when the handle has them (copied in and back around the solve), else on
 // the row-major fields.
+// Whether the cluster form of the wavefront can run on this device (checked
+// once per process, outside any capture: fg_create calls it).
+static std::atomic<int> g_lex_cluster{-1};
+void init_lexsor_cluster() {
+  if (g_lex_cluster.load() >= 0) return;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(LEX_CLUSTER);
+  cfg.blockDim = dim3(LEX_THREADS);
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = LEX_CLUSTER;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  const bool ok = cudaOccupancyMaxActiveClusters(&n, k_lexsor_cl, &cfg) == cudaSuccess && n >= 1;
+  cudaGetLastError();
+  g_lex_cluster.store(ok ? 1 : 0);
+}
+
+// One wavefront solve: the cluster kernel when a step gives its threads work
+// (diagonals of at least 256 cells, at least 8 sweeps in the pipeline), else
+// one block (whose barrier is cheaper than the cluster's).
+static void lexsor_kernel(fg_fluid* f, float* U, float* V, float* p, const uint8_t* flags,
+                          int iters, float relax0, float cp, int early_exit, DevStats* st,
+                          float minRelax, const int* stop, int SP) {
+  const int L = std::min(f->NX - 2, f->NY - 2);
+  if (L >= 256 && iters >= 8 && g_lex_cluster.load() == 1) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(LEX_CLUSTER);
+    cfg.blockDim = dim3(LEX_THREADS);
+    cfg.stream = f->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = LEX_CLUSTER;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_lexsor_cl, U, V, p, flags, f->g, iters, relax0,
+                           f->prm.pressure_damping, cp, f->prm.tolerance, early_exit, st,
+                           minRelax, stop, SP) == cudaSuccess)
+      return;
+    cudaGetLastError();
+  }
+  k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(U, V, p, flags, f->g, iters, relax0,
+                                              f->prm.pressure_damping, cp, f->prm.tolerance,
+                                              early_exit, st, minRelax, stop, SP);
+}
+
 static void run_lexsor(fg_fluid* f, int iters, float relax0, float cp, int early_exit,
                        DevStats* st, float minRelax, const int* stop) {
   if (f->skew[0]) {
@@ -1811,17 +2064,14 @@ static void run_lexsor(fg_fluid* f, int iters, float relax0, float cp, int early
     const Grid& g = f->g;
     k_skew_in<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->skew[0],
                                         f->skew[1], f->skew[2], f->skew_flags, g, f->skew_sp);
-    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->skew[0], f->skew[1], f->skew[2], f->skew_flags,
-                                                g, iters, relax0, f->prm.pressure_damping, cp,
-                                                f->prm.tolerance, early_exit, st, minRelax, stop,
-                                                f->skew_sp);
+    lexsor_kernel(f, f->skew[0], f->skew[1], f->skew[2], f->skew_flags, iters, relax0, cp,
+                  early_exit, st, minRelax, stop, f->skew_sp);
     k_skew_out<<<gr, bl, 0, f->stream>>>(f->skew[0], f->skew[1], f->skew[2], f->d[FG_U],
                                          f->d[FG_V], f->d[FG_P], g, f->skew_sp);
     count(f, 2);
   } else {
-    k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->g,
-                                                iters, relax0, f->prm.pressure_damping, cp,
-                                                f->prm.tolerance, early_exit, st, minRelax, stop);
+    lexsor_kernel(f, f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, iters, relax0, cp, early_exit,
+                  st, minRelax, stop, 0);
   }
 }
 

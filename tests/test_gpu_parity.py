@@ -317,8 +317,26 @@ def test_invalid_mask_fails_loudly(gpu):
     assert e.value.code == -5
 
 
+@pytest.mark.parametrize("w,h,early", [(300, 280, True), (300, 280, False), (640, 300, True)])
+def test_lexsor_cluster_bitwise(gpu, w, h, early):
+    """Grids whose diagonals hold at least 256 cells, 30 sweeps: the
+    reference SOR runs as the cluster form of the wavefront (with the early exit: rank 0's
+    bookkeeping over distributed shared memory; without: the closed-form
+    schedule), bit for bit, sweep count included."""
+    g, o = both(gpu, w, h, num_iters=30, UseBFECC=True, early_exit=early, tolerance=1e-3)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        f.SetCircularObstacle(w // 3, h // 2, 12)
+    for _ in range(4):
+        for f in (g, o):
+            scenes.jet_inject(f, speed=3.0)
+            f.Simulate(0.1)
+    assert_bitwise(g, o, where="%dx%d early %s" % (w, h, early))
+    assert g.stats()["sweeps"] == o.stats()["sweeps"]
+
+
 @pytest.mark.parametrize("w,h,bfecc", [(70, 45, True), (33, 20, False), (64, 64, True),
-                                         (12, 9, False)])
+                                         (12, 9, False), (600, 520, True)])
 def test_multigrid_bitwise(gpu, w, h, bfecc):
     """UseMultigrid (fluid.go:559-758, 1122-1149): the V-cycle with the
     reference's serial smoothers and coarse Gauss-Seidel, bit for bit, on
