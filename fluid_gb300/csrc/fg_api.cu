@@ -477,6 +477,7 @@ int fg_destroy(fg_fluid* f) {
   cudaFree(f->pctl);
   cudaFree(f->ectl);
   cudaFree(f->tile_done);
+  if (f->image_pinned) cudaFreeHost(f->image_pinned);
   for (float* q : f->skew) cudaFree(q);
   cudaFree(f->skew_flags);
   for (int k = 0; k < 2; ++k) {
@@ -2320,6 +2321,25 @@ int fg_render(fg_fluid* f, int kind, void* rgba) {
     field = f->view;
   }
   CK(f, launch_render(f, field, mm, kind == FG_RENDER_VORTICITY ? 1 : 0, f->image), "render");
+  // Pageable host memory (an app's image buffer) gets the frame through a
+  // pinned staging copy: the device copy into pageable memory runs at a
+  // fraction of the link's rate.
+  cudaPointerAttributes pa{};
+  const bool pageable = cudaPointerGetAttributes(&pa, rgba) == cudaSuccess
+                            ? pa.type == cudaMemoryTypeUnregistered
+                            : (cudaGetLastError(), true);
+  if (pageable && !f->image_pinned &&
+      host_malloc((void**)&f->image_pinned, bytes) != cudaSuccess) {
+    f->image_pinned = nullptr;
+    cudaGetLastError();
+  }
+  if (pageable && f->image_pinned) {
+    CK(f, cudaMemcpyAsync(f->image_pinned, f->image, bytes, cudaMemcpyDeviceToHost, f->stream),
+       "render");
+    CK(f, cudaStreamSynchronize(f->stream), "render");
+    memcpy(rgba, f->image_pinned, bytes);
+    return FG_OK;
+  }
   CK(f, cudaMemcpyAsync(rgba, f->image, bytes, cudaMemcpyDefault, f->stream), "render");
   CK(f, cudaStreamSynchronize(f->stream), "render");
   return FG_OK;

@@ -241,6 +241,7 @@ struct fg_fluid {
     int* block_keep = nullptr;
   } parts;
   uint32_t* image = nullptr;
+  void* image_pinned = nullptr;  // pinned staging of fg_render's frames for pageable targets
   // Non-null when this handle is a batch of scenes (fg_batch_create).
   fg::BatchGeom* batch = nullptr;
   // Asynchronous smoke download (fg_download_async): a copy stream, the event
