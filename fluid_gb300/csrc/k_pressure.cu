@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(LEX_THREADS)
     k_lexsor(float* U, float* V, float* p, const uint8_t* __restrict__ flags, Grid g,
              int numIters, float relax0, float damping, float cp, float tol, int early_exit,
              DevStats* st, float minRelax = 1.2f, const int* __restrict__ stop = nullptr,
-             int SP = 0) {
+             int SP = 0, int* __restrict__ exit_out = nullptr,
+             const int* __restrict__ run_from = nullptr) {
   __shared__ int s_start[LEX_RING];
   __shared__ unsigned s_max[LEX_RING];
   __shared__ int s_cont[LEX_RING];
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(LEX_THREADS)
   // The cells of the W sweeps lo .. lo+W-1 that step tau reaches; sweep t is
   // on diagonal 2 + delta_of(t) (out of range: not running) and its max
   // |div| goes to s_max[r] (r = t mod LEX_RING).
-  auto step = [&](long long tau, int lo, int W, auto delta_of) {
+  auto step = [&](long long tau, int lo, int W, auto delta_of, int runIters, bool all) {
       // Each warp takes 32 cells of one sweep's diagonal (the diagonal length
       // padded to a multiple of 32), so the sweep's max |div| and its
       // "cannot exit" mark are reduced in the warp and stored once per warp.
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(LEX_THREADS)
           const bool cont = __any_sync(0xffffffffu, counted && absDiv >= tol);
           // (Without the early exit only the last sweep's max is reported,
           // and more sweeps than ring slots may be in flight.)
-          if ((threadIdx.x & 31) == 0 && (early_exit || tt[m] == numIters - 1)) {
+          if ((threadIdx.x & 31) == 0 && (early_exit || all || tt[m] == runIters - 1)) {
             if (mx) atomicMax(&s_max[rr[m]], mx);
             if (cont) s_cont[rr[m]] = 1;
           }
@@ -171,22 +172,45 @@ __global__ void __launch_bounds__(LEX_THREADS)
     // Without the early exit sweep t always starts at step 2t (two steps
     // after the previous one, as the bookkeeping below would start it):
     // sweep t covers steps 2t .. 2t + D - 1 and the steps need no
-    // bookkeeping between them, one barrier each.
+    // bookkeeping between them, one barrier each.  With exit_out (the
+    // speculative pass of an early-exit solve) every sweep's max |div| is
+    // kept until the sweep retires and the first sweep below the tolerance
+    // is recorded; with run_from (the re-run) only sweeps 0 .. *run_from run,
+    // and nothing at all when no sweep was below it.
+    int runIters = numIters;
+    if (run_from) {
+      const int e = *run_from;
+      if (e < 0 || e >= numIters) return;
+      runIters = e + 1;
+    }
     for (int r = threadIdx.x; r < LEX_RING; r += LEX_THREADS) s_max[r] = 0u;
+    __shared__ unsigned s_lastmax;
+    if (threadIdx.x == 0) s_lastmax = 0u;
     __syncthreads();
-    const long long steps = (long long)D + 2LL * (numIters - 1);
+    const long long steps = (long long)D + 2LL * (runIters - 1);
     for (long long tau = 0; tau < steps; ++tau) {
       int t_lo = (int)((tau - D + 2) / 2);
       if (t_lo < 0) t_lo = 0;
       while (tau - 2LL * t_lo >= D) ++t_lo;
       int t_hi = (int)(tau / 2);
-      if (t_hi > numIters - 1) t_hi = numIters - 1;
-      step(tau, t_lo, t_hi - t_lo + 1, [&](int t) { return (int)(tau - 2LL * t); });
+      if (t_hi > runIters - 1) t_hi = runIters - 1;
+      step(tau, t_lo, t_hi - t_lo + 1, [&](int t) { return (int)(tau - 2LL * t); }, runIters,
+           exit_out != nullptr);
       __syncthreads();
+      // The sweep whose last diagonal ran in this step retires.
+      const long long rt = tau - (D - 1);
+      if (threadIdx.x == 0 && rt >= 0 && (rt & 1) == 0 && rt / 2 < runIters) {
+        const int t = (int)(rt / 2), r = t & (LEX_RING - 1);
+        const unsigned m = s_max[r];
+        if (exit_out && __uint_as_float(m) < tol) atomicMin(exit_out, t);
+        if (t == runIters - 1) s_lastmax = m;
+        s_max[r] = 0u;  // (slot reused by sweep t + LEX_RING, not yet started)
+      }
     }
+    __syncthreads();
     if (threadIdx.x == 0) {
-      st->sweeps = numIters;
-      st->last_maxdiv = (double)__uint_as_float(s_max[(numIters - 1) & (LEX_RING - 1)]);
+      st->sweeps = runIters;
+      st->last_maxdiv = (double)__uint_as_float(s_lastmax);
     }
     return;
   }
@@ -203,7 +227,8 @@ __global__ void __launch_bounds__(LEX_THREADS)
   const long long max_steps = (long long)numIters * (D + 2) + D + 4;
   for (long long tau = 0; tau < max_steps; ++tau) {
     const int lo = s_lo, hi = s_hi;
-    step(tau, lo, hi - lo, [&](int t) { return (int)(tau - s_start[t & (LEX_RING - 1)]); });
+    step(tau, lo, hi - lo, [&](int t) { return (int)(tau - s_start[t & (LEX_RING - 1)]); },
+         numIters, false);
     __syncthreads();
     if (threadIdx.x == 0) {
       // Retire sweeps whose last diagonal ran in this step.
@@ -281,7 +306,8 @@ __device__ __forceinline__ void cl_max(uint32_t a, unsigned v) {
 __global__ void __launch_bounds__(LEX_THREADS)
     k_lexsor_cl(float* U, float* V, float* p, const uint8_t* __restrict__ flags, Grid g,
                 int numIters, float relax0, float damping, float cp, float tol, int early_exit,
-                DevStats* st, float minRelax, const int* __restrict__ stop, int SP) {
+                DevStats* st, float minRelax, const int* __restrict__ stop, int SP,
+                int* __restrict__ exit_out, const int* __restrict__ run_from) {
   __shared__ int s_start[LEX_RING];
   __shared__ unsigned s_max[LEX_RING];
   __shared__ int s_cont[LEX_RING];
@@ -316,7 +342,7 @@ __global__ void __launch_bounds__(LEX_THREADS)
   const int gt = (int)rank * LEX_THREADS + (int)threadIdx.x;
   const int stride = LEX_CLUSTER * LEX_THREADS;
   const int Lp = (L + 31) & ~31;
-  auto step = [&](long long tau, int lo, int W, auto delta_of) {
+  auto step = [&](long long tau, int lo, int W, auto delta_of, int runIters, bool all) {
     const int items = W * Lp;
     for (int base = 0; base < items; base += LEX_CHUNK * stride) {
       int cc[LEX_CHUNK], rr[LEX_CHUNK], tt[LEX_CHUNK];
@@ -360,7 +386,7 @@ __global__ void __launch_bounds__(LEX_THREADS)
         const bool counted = a && !isnan(absDiv);
         const unsigned mx = __reduce_max_sync(0xffffffffu, counted ? __float_as_uint(absDiv) : 0u);
         const bool cont = __any_sync(0xffffffffu, counted && absDiv >= tol);
-        if ((threadIdx.x & 31) == 0 && (early_exit || tt[m] == numIters - 1)) {
+        if ((threadIdx.x & 31) == 0 && (early_exit || all || tt[m] == runIters - 1)) {
           if (mx) cl_max(a_max + 4u * rr[m], mx);
           if (cont) cl_st(a_cont + 4u * rr[m], 1);
         }
@@ -381,19 +407,40 @@ __global__ void __launch_bounds__(LEX_THREADS)
     }
   };
   if (!early_exit) {
-    const long long steps = (long long)D + 2LL * (numIters - 1);
+    // The closed-form schedule, as in k_lexsor (exit_out / run_from alike);
+    // rank 0's thread 0 retires the sweeps.
+    int runIters = numIters;
+    if (run_from) {
+      const int e = *run_from;
+      if (e < 0 || e >= numIters) {
+        cl_sync();
+        return;
+      }
+      runIters = e + 1;
+    }
+    const long long steps = (long long)D + 2LL * (runIters - 1);
     for (long long tau = 0; tau < steps; ++tau) {
       int t_lo = (int)((tau - D + 2) / 2);
       if (t_lo < 0) t_lo = 0;
       while (tau - 2LL * t_lo >= D) ++t_lo;
       int t_hi = (int)(tau / 2);
-      if (t_hi > numIters - 1) t_hi = numIters - 1;
-      step(tau, t_lo, t_hi - t_lo + 1, [&](int t) { return (int)(tau - 2LL * t); });
+      if (t_hi > runIters - 1) t_hi = runIters - 1;
+      step(tau, t_lo, t_hi - t_lo + 1, [&](int t) { return (int)(tau - 2LL * t); }, runIters,
+           exit_out != nullptr);
       cl_sync();
+      const long long rt = tau - (D - 1);
+      if (rank == 0 && threadIdx.x == 0 && rt >= 0 && (rt & 1) == 0 && rt / 2 < runIters) {
+        const int t = (int)(rt / 2), r = t & (LEX_RING - 1);
+        const unsigned m = s_max[r];
+        if (exit_out && __uint_as_float(m) < tol) atomicMin(exit_out, t);
+        if (t == runIters - 1) s_last = (int)m;
+        s_max[r] = 0u;  // (slot reused by sweep t + LEX_RING, not yet started)
+      }
     }
+    cl_sync();
     if (rank == 0 && threadIdx.x == 0) {
-      st->sweeps = numIters;
-      st->last_maxdiv = (double)__uint_as_float(s_max[(numIters - 1) & (LEX_RING - 1)]);
+      st->sweeps = runIters;
+      st->last_maxdiv = (double)__uint_as_float((unsigned)s_last);
     }
     cl_sync();  // (no block leaves while others may still address rank 0)
     return;
@@ -402,7 +449,8 @@ __global__ void __launch_bounds__(LEX_THREADS)
   for (long long tau = 0; tau < max_steps; ++tau) {
     const int lo = cl_ld(a_lo), hi = cl_ld(a_hi);
     step(tau, lo, hi - lo,
-         [&](int t) { return (int)(tau - cl_ld(a_start + 4u * (t & (LEX_RING - 1)))); });
+         [&](int t) { return (int)(tau - cl_ld(a_start + 4u * (t & (LEX_RING - 1)))); },
+         numIters, false);
     cl_sync();
     if (rank == 0 && threadIdx.x == 0) {
       // Retire sweeps whose last diagonal ran in this step.
@@ -444,7 +492,9 @@ __global__ void __launch_bounds__(LEX_THREADS)
 __global__ void k_skew_in(const float* __restrict__ U, const float* __restrict__ V,
                           const float* __restrict__ p, const uint8_t* __restrict__ flags,
                           float* __restrict__ sU, float* __restrict__ sV, float* __restrict__ sp,
-                          uint8_t* __restrict__ sf, Grid g, int SP) {
+                          uint8_t* __restrict__ sf, Grid g, int SP,
+                          const int* __restrict__ only_if = nullptr, int limit = 0) {
+  if (only_if && *only_if >= limit) return;  // (the re-run copy: only when it runs)
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
@@ -2032,7 +2082,8 @@ void init_lexsor_cluster() {
 // one block (whose barrier is cheaper than the cluster's).
 static void lexsor_kernel(fg_fluid* f, float* U, float* V, float* p, const uint8_t* flags,
                           int iters, float relax0, float cp, int early_exit, DevStats* st,
-                          float minRelax, const int* stop, int SP) {
+                          float minRelax, const int* stop, int SP, int* exit_out = nullptr,
+                          const int* run_from = nullptr) {
   const int L = std::min(f->NX - 2, f->NY - 2);
   if (L >= 256 && iters >= 8 && g_lex_cluster.load() == 1) {
     cudaLaunchConfig_t cfg = {};
@@ -2048,24 +2099,44 @@ static void lexsor_kernel(fg_fluid* f, float* U, float* V, float* p, const uint8
     cfg.numAttrs = 1;
     if (cudaLaunchKernelEx(&cfg, k_lexsor_cl, U, V, p, flags, f->g, iters, relax0,
                            f->prm.pressure_damping, cp, f->prm.tolerance, early_exit, st,
-                           minRelax, stop, SP) == cudaSuccess)
+                           minRelax, stop, SP, exit_out, run_from) == cudaSuccess)
       return;
     cudaGetLastError();
   }
   k_lexsor<<<1, LEX_THREADS, 0, f->stream>>>(U, V, p, flags, f->g, iters, relax0,
                                               f->prm.pressure_damping, cp, f->prm.tolerance,
-                                              early_exit, st, minRelax, stop, SP);
+                                              early_exit, st, minRelax, stop, SP, exit_out,
+                                              run_from);
 }
 
 static void run_lexsor(fg_fluid* f, int iters, float relax0, float cp, int early_exit,
-                       DevStats* st, float minRelax, const int* stop) {
+                       DevStats* st, float minRelax, const int* stop, int* exit_slot) {
   if (f->skew[0]) {
     dim3 gr = cell_grid(f), bl(BX, BY);
     const Grid& g = f->g;
     k_skew_in<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->skew[0],
                                         f->skew[1], f->skew[2], f->skew_flags, g, f->skew_sp);
-    lexsor_kernel(f, f->skew[0], f->skew[1], f->skew[2], f->skew_flags, iters, relax0, cp,
-                  early_exit, st, minRelax, stop, f->skew_sp);
+    const int D = f->NX + f->NY - 5;  // anti-diagonals of the interior
+    if (early_exit && exit_slot && D / 2 + 4 < LEX_RING) {
+      // The early exit, speculatively: all sweeps on the closed-form
+      // schedule, recording the first sweep whose max |div| is below the
+      // tolerance; if there is one, the fields (untouched so far) are copied
+      // in again and exactly that many sweeps run.  Sweeps up to that one
+      // are the same in both runs, so this is the serial loop's result and
+      // the steps never wait for a "cannot exit" mark.
+      cudaMemsetAsync(exit_slot, 0x7f, sizeof(int), f->stream);
+      lexsor_kernel(f, f->skew[0], f->skew[1], f->skew[2], f->skew_flags, iters, relax0, cp, 0,
+                    st, minRelax, stop, f->skew_sp, exit_slot, nullptr);
+      k_skew_in<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags,
+                                          f->skew[0], f->skew[1], f->skew[2], f->skew_flags, g,
+                                          f->skew_sp, exit_slot, iters);
+      lexsor_kernel(f, f->skew[0], f->skew[1], f->skew[2], f->skew_flags, iters, relax0, cp, 0,
+                    st, minRelax, stop, f->skew_sp, nullptr, exit_slot);
+      count(f, 3);
+    } else {
+      lexsor_kernel(f, f->skew[0], f->skew[1], f->skew[2], f->skew_flags, iters, relax0, cp,
+                    early_exit, st, minRelax, stop, f->skew_sp);
+    }
     k_skew_out<<<gr, bl, 0, f->stream>>>(f->skew[0], f->skew[1], f->skew[2], f->d[FG_U],
                                          f->d[FG_V], f->d[FG_P], g, f->skew_sp);
     count(f, 2);
@@ -2095,7 +2166,7 @@ cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt) {
   uint8_t* cmask = reinterpret_cast<uint8_t*>(f->rhs_e);
   for (int it = 0; it < num_iters; ++it) {
     count(f, 8);
-    run_lexsor(f, 3, 1.5f, cp, 0, sm, 1.5f, stop);
+    run_lexsor(f, 3, 1.5f, cp, 0, sm, 1.5f, stop, nullptr);
     k_mg_check<<<1, 1, 0, f->stream>>>(sm, f->dstats, stop, f->prm.tolerance, 0);
     k_mg_residual<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->flags, f->rhs,
                                             stop, f->g);
@@ -2105,7 +2176,7 @@ cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt) {
                                                  40, 1.6f, CSP, cmask);
     k_mg_apply<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->err2, f->flags,
                                          stop, cp, f->g, cNX, cNY, CSP);
-    run_lexsor(f, 3, 1.2f, cp, 0, sm, 1.2f, stop);
+    run_lexsor(f, 3, 1.2f, cp, 0, sm, 1.2f, stop, nullptr);
     k_mg_check<<<1, 1, 0, f->stream>>>(sm, f->dstats, stop, f->prm.tolerance, 1);
   }
   return cudaGetLastError();
@@ -2116,7 +2187,10 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   cudaError_t e;
   if (f->prm.scheme == FG_SCHEME_LEXSOR) {
     count(f);
-    run_lexsor(f, num_iters, f->prm.relaxation, cp, f->prm.early_exit, f->dstats, 1.2f, nullptr);
+    // (The correction solve's control block is free in this scheme: its
+    // first words hold the speculative early exit's sweep index.)
+    run_lexsor(f, num_iters, f->prm.relaxation, cp, f->prm.early_exit, f->dstats, 1.2f, nullptr,
+               reinterpret_cast<int*>(f->ectl));
     return cudaGetLastError();
   }
   PCtl* ctl = (PCtl*)f->pctl;

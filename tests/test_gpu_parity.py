@@ -335,6 +335,22 @@ def test_lexsor_cluster_bitwise(gpu, w, h, early):
     assert g.stats()["sweeps"] == o.stats()["sweeps"]
 
 
+@pytest.mark.parametrize("w,h", [(40, 30), (320, 300)])
+def test_lexsor_early_exit_mid_solve_bitwise(gpu, w, h):
+    """A nearly divergence-free state whose solve stops part way: the
+    speculative early exit (all sweeps, then a re-run of exactly the sweeps
+    the serial loop makes) on one block and on the cluster, bit for bit."""
+    g, o = both(gpu, w, h, num_iters=60, tolerance=1e-3)
+    for f in (g, o):
+        f.S[:] = 1.0
+        f.S[: f.NumY] = 0.0
+        scenes.random_state(f, seed=17, amp=1e-3)
+        f.makeIncompressible(60, 0.1)
+    sg, so = g.stats(), o.stats()
+    assert sg["sweeps"] == so["sweeps"] < 60
+    assert_bitwise(g, o, fields=("U", "V", "p"))
+
+
 @pytest.mark.parametrize("w,h,bfecc", [(70, 45, True), (33, 20, False), (64, 64, True),
                                          (12, 9, False), (600, 520, True)])
 def test_multigrid_bitwise(gpu, w, h, bfecc):
