@@ -857,7 +857,11 @@ def run_ours(args):
     roll = (rollout256(fluid_gb300, args)
             if rank == 0 and not (args.no_adjoint or args.no_rollout) else None)
     ens = ensemble(fluid_gb300, args) if rank == 0 and not args.no_ensemble else None
-    app = app_rows(fluid_gb300) if rank == 0 and not args.no_app else None
+    app = None
+    if rank == 0 and not args.no_app:
+        stop_app = profile_leg(args, "app")
+        app = app_rows(fluid_gb300)
+        stop_app()
 
     # ------------------------------------------------------------ CPU baseline
     cpu = None
@@ -905,7 +909,7 @@ def main():
     ap.add_argument("--no-rollout", action="store_true")
     ap.add_argument("--no-app", action="store_true",
                     help="skip the multigrid, particle, rendering and view rows")
-    ap.add_argument("--profile-leg", choices=["adjoint", "ensemble"], default=None,
+    ap.add_argument("--profile-leg", choices=["adjoint", "ensemble", "app"], default=None,
                     help="bracket that leg's timed region for ncu --profile-from-start off")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
