@@ -608,20 +608,32 @@ __global__ void k_mg_restrict(const float* __restrict__ r, float* __restrict__ c
 // run as anti-diagonal wavefronts, each two diagonals behind the previous.
 constexpr int MG_THREADS = 1024;
 constexpr int MG_CHUNK = 4;  // cells whose loads a thread issues together
+// CLUSTER: the same schedule on a thread-block cluster of LEX_CLUSTER blocks
+// (a step's cells over all of its threads, a cluster barrier per step, the
+// solution read past L1), for coarse grids whose steps hold many cells.
+template <bool CLUSTER>
 __global__ void __launch_bounds__(MG_THREADS)
     k_mg_coarse(const float* __restrict__ cr, float* __restrict__ cp_,
                 const uint8_t* __restrict__ flags, const int* __restrict__ stop, Grid g, int cNX,
                 int cNY, int sweeps, float relaxation, int CSP,
                 const uint8_t* __restrict__ cmask) {
-  if (*stop) return;
+  if (*stop) return;  // (the same in every block)
   const int ni = cNX - 2, nj = cNY - 2;
   // Row-major (CSP = 0): neighbours at -cNY, +cNY, -1, +1.  Diagonal-major:
   // west -(CSP+1), east +(CSP+1), south -CSP, north +CSP, and the cells of a
   // step contiguous along their diagonal.
   const int oW = CSP ? CSP + 1 : cNY, oS = CSP ? CSP : 1;
   const int n0 = CSP ? (cNX + cNY - 1) * CSP : cNX * cNY;
-  for (int k = threadIdx.x; k < n0; k += MG_THREADS) cp_[k] = 0.0f;
-  __syncthreads();
+  const int gt = CLUSTER ? (int)cl_rank() * MG_THREADS + (int)threadIdx.x : (int)threadIdx.x;
+  const int stride = CLUSTER ? LEX_CLUSTER * MG_THREADS : MG_THREADS;
+  auto barrier = [] {
+    if (CLUSTER)
+      cl_sync();
+    else
+      __syncthreads();
+  };
+  for (int k = gt; k < n0; k += stride) cp_[k] = 0.0f;
+  barrier();
   if (ni <= 0 || nj <= 0) return;
   const int D = ni + nj - 1;
   const int L = ni < nj ? ni : nj;
@@ -638,14 +650,14 @@ __global__ void __launch_bounds__(MG_THREADS)
     // sweeps two diagonals apart, no cell reads another's value): a thread
     // loads the inputs of MG_CHUNK cells at once, then updates them.
     const int items = nact * L;
-    for (int base = 0; base < items; base += MG_CHUNK * MG_THREADS) {
+    for (int base = 0; base < items; base += MG_CHUNK * stride) {
       int cc[MG_CHUNK];
       bool in[MG_CHUNK];
       float s0[MG_CHUNK], s1[MG_CHUNK], s2[MG_CHUNK], s3[MG_CHUNK], sc[MG_CHUNK];
       float pc[MG_CHUNK], pw[MG_CHUNK], pe[MG_CHUNK], ps[MG_CHUNK], pn[MG_CHUNK], rc[MG_CHUNK];
 #pragma unroll
       for (int m = 0; m < MG_CHUNK; ++m) {
-        const int q = base + m * MG_THREADS + (int)threadIdx.x;
+        const int q = base + m * stride + gt;
         const int t = t_lo + q / L;
         const int k = q - (q / L) * L;
         const int d = (int)(tau - 2LL * t) + 2;
@@ -669,11 +681,12 @@ __global__ void __launch_bounds__(MG_THREADS)
           s2[m] = ok ? coarse_s(flags, i, j - 1, g) : 0.0f;
           s3[m] = ok ? coarse_s(flags, i, j + 1, g) : 0.0f;
         }
-        pc[m] = ok ? cp_[c] : 0.0f;
-        pw[m] = ok ? cp_[c - oW] : 0.0f;
-        pe[m] = ok ? cp_[c + oW] : 0.0f;
-        ps[m] = ok ? cp_[c - oS] : 0.0f;
-        pn[m] = ok ? cp_[c + oS] : 0.0f;
+        auto ld = [&](int a) { return CLUSTER ? __ldcg(cp_ + a) : cp_[a]; };
+        pc[m] = ok ? ld(c) : 0.0f;
+        pw[m] = ok ? ld(c - oW) : 0.0f;
+        pe[m] = ok ? ld(c + oW) : 0.0f;
+        ps[m] = ok ? ld(c - oS) : 0.0f;
+        pn[m] = ok ? ld(c + oS) : 0.0f;
         rc[m] = ok ? cr[c] : 0.0f;
       }
 #pragma unroll
@@ -690,7 +703,7 @@ __global__ void __launch_bounds__(MG_THREADS)
         cp_[cc[m]] = p0 + correction;
       }
     }
-    __syncthreads();
+    barrier();
   }
 }
 
@@ -2146,6 +2159,33 @@ static void run_lexsor(fg_fluid* f, int iters, float relax0, float cp, int early
   }
 }
 
+// solveCoarseGrid's 40 sweeps: on the cluster when the coarse diagonals hold
+// at least 128 cells (a step then spans thousands), else on one block.
+static void launch_mg_coarse(fg_fluid* f, const int* stop, int cNX, int cNY, int CSP,
+                             const uint8_t* cmask) {
+  const int L = std::min(cNX - 2, cNY - 2);
+  if (CSP && L >= 128 && g_lex_cluster.load() == 1) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(LEX_CLUSTER);
+    cfg.blockDim = dim3(MG_THREADS);
+    cfg.stream = f->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = LEX_CLUSTER;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_mg_coarse<true>, (const float*)f->err, f->err2,
+                           (const uint8_t*)f->flags, stop, f->g, cNX, cNY, 40, 1.6f, CSP,
+                           cmask) == cudaSuccess)
+      return;
+    cudaGetLastError();
+  }
+  k_mg_coarse<false><<<1, MG_THREADS, 0, f->stream>>>(f->err, f->err2, f->flags, stop, f->g,
+                                                       cNX, cNY, 40, 1.6f, CSP, cmask);
+}
+
 cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt) {
   float cp = f->density * f->h / dt;  // fluid.go:560
   const int cNX = (f->NX + 1) / 2, cNY = (f->NY + 1) / 2;
@@ -2172,8 +2212,7 @@ cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt) {
                                             stop, f->g);
     k_mg_restrict<<<cg, bl, 0, f->stream>>>(f->rhs, f->err, stop, f->g, cNX, cNY, CSP, f->flags,
                                             cmask);
-    k_mg_coarse<<<1, MG_THREADS, 0, f->stream>>>(f->err, f->err2, f->flags, stop, f->g, cNX, cNY,
-                                                 40, 1.6f, CSP, cmask);
+    launch_mg_coarse(f, stop, cNX, cNY, CSP, cmask);
     k_mg_apply<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->d[FG_P], f->err2, f->flags,
                                          stop, cp, f->g, cNX, cNY, CSP);
     run_lexsor(f, 3, 1.2f, cp, 0, sm, 1.2f, stop, nullptr);
