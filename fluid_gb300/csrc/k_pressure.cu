@@ -56,6 +56,23 @@ inline dim3 cell_grid(const fg_fluid* f) {
   return dim3((f->NY + BX - 1) / BX, (f->NX + BY - 1) / BY);
 }
 
+// q / n and q % n for 0 <= q < 2^24, n > 0, from a float reciprocal and one
+// correction step (exact: q and the candidate products are exact in float
+// range, and the float quotient is off by at most one).
+__device__ __forceinline__ int div_small(int q, int n, float inv_n, int& rem) {
+  int t = __float2int_rz((float)q * inv_n);
+  int r = q - t * n;
+  if (r < 0) {
+    --t;
+    r += n;
+  } else if (r >= n) {
+    ++t;
+    r -= n;
+  }
+  rem = r;
+  return t;
+}
+
 // ------------------------------------------------------------------ LEXSOR
 constexpr int LEX_THREADS = 1024;
 constexpr int LEX_RING = 2048;  // sweeps in flight (a new sweep waits while the ring is full)
@@ -103,17 +120,19 @@ __global__ void __launch_bounds__(LEX_THREADS)
       // then updates them: one memory round trip per chunk instead of one per
       // cell.
       const int Lp = (L + 31) & ~31;
+      const float invLp = 1.0f / (float)Lp;
       const int items = W * Lp;
       for (int base = 0; base < items; base += LEX_CHUNK * LEX_THREADS) {
         int cc[LEX_CHUNK], rr[LEX_CHUNK], tt[LEX_CHUNK];
-        bool act[LEX_CHUNK];
+        bool act[LEX_CHUNK] = {};
         uint8_t fl[LEX_CHUNK];
         float u0[LEX_CHUNK], u1[LEX_CHUNK], v0[LEX_CHUNK], v1[LEX_CHUNK], p0[LEX_CHUNK];
 #pragma unroll
         for (int m = 0; m < LEX_CHUNK; ++m) {
+          if (base + m * LEX_THREADS >= items) break;  // (block-uniform)
           const int q = base + m * LEX_THREADS + (int)threadIdx.x;
-          const int t = lo + q / Lp;
-          const int k = q - (q / Lp) * Lp;
+          int k;
+          const int t = lo + (items < (1 << 24) ? div_small(q, Lp, invLp, k) : (k = q % Lp, q / Lp));
           const int r = t & (LEX_RING - 1);
           const int delta = q < items ? delta_of(t) : -1;
           const int d = 2 + delta;
@@ -342,18 +361,20 @@ __global__ void __launch_bounds__(LEX_THREADS)
   const int gt = (int)rank * LEX_THREADS + (int)threadIdx.x;
   const int stride = LEX_CLUSTER * LEX_THREADS;
   const int Lp = (L + 31) & ~31;
+  const float invLp = 1.0f / (float)Lp;
   auto step = [&](long long tau, int lo, int W, auto delta_of, int runIters, bool all) {
     const int items = W * Lp;
     for (int base = 0; base < items; base += LEX_CHUNK * stride) {
       int cc[LEX_CHUNK], rr[LEX_CHUNK], tt[LEX_CHUNK];
-      bool act[LEX_CHUNK];
+      bool act[LEX_CHUNK] = {};
       uint8_t fl[LEX_CHUNK];
       float u0[LEX_CHUNK], u1[LEX_CHUNK], v0[LEX_CHUNK], v1[LEX_CHUNK], p0[LEX_CHUNK];
 #pragma unroll
       for (int m = 0; m < LEX_CHUNK; ++m) {
+        if (base + m * stride >= items) break;  // (uniform over the cluster)
         const int q = base + m * stride + gt;
-        const int t = lo + q / Lp;
-        const int k = q - (q / Lp) * Lp;
+        int k;
+        const int t = lo + (items < (1 << 24) ? div_small(q, Lp, invLp, k) : (k = q % Lp, q / Lp));
         const int r = t & (LEX_RING - 1);
         const int delta = q < items ? delta_of(t) : -1;
         const int d = 2 + delta;
@@ -637,6 +658,7 @@ __global__ void __launch_bounds__(MG_THREADS)
   if (ni <= 0 || nj <= 0) return;
   const int D = ni + nj - 1;
   const int L = ni < nj ? ni : nj;
+  const float invL = 1.0f / (float)L;
   const long long steps = (long long)D + 2LL * (sweeps - 1);
   for (long long tau = 0; tau < steps; ++tau) {
     // Sweeps t with 0 <= tau - 2t < D, each on diagonal d = tau - 2t + 2.
@@ -652,14 +674,15 @@ __global__ void __launch_bounds__(MG_THREADS)
     const int items = nact * L;
     for (int base = 0; base < items; base += MG_CHUNK * stride) {
       int cc[MG_CHUNK];
-      bool in[MG_CHUNK];
+      bool in[MG_CHUNK] = {};  // (slots past the step's cells stay out)
       float s0[MG_CHUNK], s1[MG_CHUNK], s2[MG_CHUNK], s3[MG_CHUNK], sc[MG_CHUNK];
       float pc[MG_CHUNK], pw[MG_CHUNK], pe[MG_CHUNK], ps[MG_CHUNK], pn[MG_CHUNK], rc[MG_CHUNK];
 #pragma unroll
       for (int m = 0; m < MG_CHUNK; ++m) {
+        if (base + m * stride >= items) break;  // (uniform over the block or cluster)
         const int q = base + m * stride + gt;
-        const int t = t_lo + q / L;
-        const int k = q - (q / L) * L;
+        int k;
+        const int t = t_lo + (items < (1 << 24) ? div_small(q, L, invL, k) : (k = q % L, q / L));
         const int d = (int)(tau - 2LL * t) + 2;
         const int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
         const int i = i_lo + k;
@@ -691,6 +714,7 @@ __global__ void __launch_bounds__(MG_THREADS)
       }
 #pragma unroll
       for (int m = 0; m < MG_CHUNK; ++m) {
+        if (base + m * stride >= items) break;  // (the slots the loads filled)
         if (!in[m] || sc[m] == 0.0f) continue;
         const float sx0 = s0[m], sx1 = s1[m], sy0 = s2[m], sy1 = s3[m];
         const float s = sx0 + sx1 + sy0 + sy1;
