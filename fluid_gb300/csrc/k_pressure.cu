@@ -8,18 +8,23 @@
 //    on (i+1, j), (i, j+1) of the previous one, so the sweep runs as a
 //    wavefront over anti-diagonals, with consecutive sweeps pipelined two
 //    diagonals apart.  Every face sees the same sequence of floating-point
-//    updates as in the serial loop, so the result is bit-identical.  One CTA
-//    owns one grid; a new sweep starts only once the previous sweep is known
-//    not to trigger the early exit (some cell with |div| >= tolerance).
+//    updates as in the serial loop, so the result is bit-identical.  The
+//    wavefront runs on one block (k_lexsor) or an 8-block cluster
+//    (k_lexsor_cl), on diagonal-major copies of the fields; the early exit
+//    either waits, step by step, for the previous sweep to be known not to
+//    exit, or runs speculatively (all sweeps, then an exact re-run of the
+//    sweeps the serial loop makes when one falls below the tolerance).
 //  * JACOBI relaxes the same masked Poisson system for the cell potential
 //    phi (the accumulated per-cell correction of the SOR loop):
 //        s_c phi_c - sum_n phi_n = -div_c,   phi = 0 off the active cells,
 //    then applies U_face += S_R phi_L - S_L phi_R (and likewise V) and
-//    p = cp * phi.  Sweeps run temporally blocked: each launch loads a tile
-//    with a halo as wide as its sweep count into shared memory and relaxes it
-//    there, so HBM sees one read and one write of phi per launch.  Optional
-//    outer correction: an FP64 residual of the FP32 iterate, a correction
-//    solve on it, phi += e.
+//    p = cp * phi.  Sweeps run temporally blocked: a block relaxes a tile
+//    with a halo as wide as its sweep count (8) in registers, so memory sees
+//    one read and one write of phi per block of sweeps (k_jacobi_rb; fed by
+//    TMA copies in k_jacobi_tma; a whole fixed-count solve as one cooperative
+//    dataflow launch in k_jacobi_flow).  Optional outer correction: an
+//    FP64-class residual of the FP32 iterate, a correction solve on it,
+//    phi += e.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
