@@ -80,7 +80,7 @@ __device__ __forceinline__ int div_small(int q, int n, float inv_n, int& rem) {
 
 // ------------------------------------------------------------------ LEXSOR
 constexpr int LEX_THREADS = 1024;
-constexpr int LEX_RING = 2048;  // sweeps in flight (a new sweep waits while the ring is full)
+constexpr int LEX_RING = 4096;  // sweeps in flight (a new sweep waits while the ring is full)
 constexpr int LEX_CHUNK = 4;    // cells whose loads a thread issues together
 
 __global__ void __launch_bounds__(LEX_THREADS)
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(LEX_THREADS)
              const int* __restrict__ run_from = nullptr) {
   __shared__ int s_start[LEX_RING];
   __shared__ unsigned s_max[LEX_RING];
-  __shared__ int s_cont[LEX_RING];
+  __shared__ uint8_t s_cont[LEX_RING];
   __shared__ int s_lo, s_hi, s_done, s_exit, s_last;
   const int P = g.P;
   const int ni = g.NX - 2, nj = g.NY - 2;  // interior extent
@@ -323,6 +323,9 @@ __device__ __forceinline__ int cl_ld(uint32_t a) {
 __device__ __forceinline__ void cl_st(uint32_t a, int v) {
   asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
+__device__ __forceinline__ void cl_st8(uint32_t a, unsigned v) {
+  asm volatile("st.shared::cluster.u8 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
 __device__ __forceinline__ void cl_max(uint32_t a, unsigned v) {
   asm volatile("red.shared::cluster.max.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
@@ -334,7 +337,7 @@ __global__ void __launch_bounds__(LEX_THREADS)
                 int* __restrict__ exit_out, const int* __restrict__ run_from) {
   __shared__ int s_start[LEX_RING];
   __shared__ unsigned s_max[LEX_RING];
-  __shared__ int s_cont[LEX_RING];
+  __shared__ uint8_t s_cont[LEX_RING];
   __shared__ int s_lo, s_hi, s_done, s_exit, s_last;
   const unsigned rank = cl_rank();
   const int P = g.P;
@@ -414,7 +417,7 @@ __global__ void __launch_bounds__(LEX_THREADS)
         const bool cont = __any_sync(0xffffffffu, counted && absDiv >= tol);
         if ((threadIdx.x & 31) == 0 && (early_exit || all || tt[m] == runIters - 1)) {
           if (mx) cl_max(a_max + 4u * rr[m], mx);
-          if (cont) cl_st(a_cont + 4u * rr[m], 1);
+          if (cont) cl_st8(a_cont + (unsigned)rr[m], 1u);
         }
         if (!a) continue;
         const int c = cc[m];

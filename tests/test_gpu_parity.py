@@ -335,11 +335,12 @@ def test_lexsor_cluster_bitwise(gpu, w, h, early):
     assert g.stats()["sweeps"] == o.stats()["sweeps"]
 
 
-@pytest.mark.parametrize("w,h", [(40, 30), (320, 300)])
+@pytest.mark.parametrize("w,h", [(40, 30), (320, 300), (4000, 100)])
 def test_lexsor_early_exit_mid_solve_bitwise(gpu, w, h):
     """A nearly divergence-free state whose solve stops part way: the
     speculative early exit (all sweeps, then a re-run of exactly the sweeps
-    the serial loop makes) on one block and on the cluster, bit for bit."""
+    the serial loop makes) on one block, on the cluster, and with more than
+    2048 sweeps' worth of diagonals in the ring (4000x100), bit for bit."""
     g, o = both(gpu, w, h, num_iters=60, tolerance=1e-3)
     for f in (g, o):
         f.S[:] = 1.0
