@@ -533,6 +533,28 @@ def app_rows(fluid_gb300):
     import torch
 
     rows = {}
+    # The CPU baseline's own workload on the GPU: the 2048^2 cavity with the
+    # reference's serial SOR (200 sweeps, no early exit), bit for bit, as the
+    # cluster wavefront -- the drop-in path for a caller who keeps the
+    # reference's scheme.
+    f = fluid_gb300.Fluid(1.0, W, H, 1.0, auto_sync=False, UseBFECC=True, num_iters=ITERS,
+                          early_exit=False)
+    S = f.S.reshape(f.NumX, f.NumY)
+    S[:] = 1.0
+    S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
+    f.mark_dirty()
+    li, lj = lid_cells(f)
+    f.set_sources(li, lj, u=1.0, v=0.0, mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY)
+    st = torch.cuda.ExternalStream(f.stream)
+    for _ in range(2):
+        f.Simulate(DT)
+    ms = device_ms(st, lambda: f.Simulate(DT), 3)
+    rows["reference_sor_2048"] = {
+        "value": W * H / ms / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms,
+        "config": "the CPU baseline's workload (2048^2 cavity, BFECC, the reference's serial SOR "
+                  "with 200 sweeps) bit for bit on the GPU (cluster wavefront on diagonal-major "
+                  "copies); device-timed steps; its CPU baseline is the line's cpu_baseline"}
+    del f
     # The reference scheme (serial SOR, bit for bit) as the wavefront kernel:
     # the 512^2 cavity, the reference's 8 iterations per step.
     f = fluid_gb300.Fluid(1.0, MG_SIDE, MG_SIDE, 1.0, auto_sync=False, UseBFECC=True, num_iters=8)
@@ -875,6 +897,7 @@ def run_ours(args):
         if app is not None:
             for k, v in cpu_app_rows(threads).items():
                 app[k]["cpu_baseline"] = v
+            app["reference_sor_2048"]["cpu_baseline"] = dict(cpu)
 
     if rank == 0:
         line = {

@@ -480,6 +480,7 @@ int fg_destroy(fg_fluid* f) {
   if (f->image_pinned) cudaFreeHost(f->image_pinned);
   for (float* q : f->skew) cudaFree(q);
   cudaFree(f->skew_flags);
+  cudaFree(f->lex_scratch);
   for (int k = 0; k < 2; ++k) {
     cudaFree(f->edit_dev[k]);
     cudaFree(f->edit_off_dev[k]);
@@ -622,12 +623,16 @@ void ensure_skew(fg_fluid* f) {
   bool ok = true;
   for (auto& q : a) ok = ok && dev_malloc((void**)&q, n * sizeof(float)) == cudaSuccess;
   ok = ok && dev_malloc((void**)&fl, n) == cudaSuccess;
+  unsigned* lex = nullptr;
+  ok = ok && dev_malloc((void**)&lex, sizeof(unsigned) * lexsor_scratch_words()) == cudaSuccess;
   if (!ok) {
     for (auto& q : a) cudaFree(q);
     cudaFree(fl);
+    cudaFree(lex);
     cudaGetLastError();
     return;
   }
+  f->lex_scratch = lex;
   for (int k = 0; k < 3; ++k) f->skew[k] = a[k];
   f->skew_flags = fl;
   f->skew_sp = sp;

@@ -191,6 +191,7 @@ struct fg_fluid {
   float* skew[3] = {};       // diagonal-major U, V, p of the wavefront SOR (or none)
   uint8_t* skew_flags = nullptr;
   int skew_sp = 0;           // their row stride (cells per diagonal)
+  unsigned* lex_scratch = nullptr;  // grid-wide wavefront: sweep maxima, barrier words
   void* ectl = nullptr;   // control block of the FP64-residual correction solve
   int n_slots = 0;        // launch slots per control block
   float* copy_tmp = nullptr;        // fg_copy_border staging (2 fields)
@@ -309,6 +310,7 @@ cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt);
 // buffer holding x.
 void init_jacobi_tma();
 void init_lexsor_cluster();
+int lexsor_scratch_words();
 int jacobi_tile_count(int NX, int NY);
 cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const float* bw, float* x0,
                                 float* x1, int iters);

@@ -52,6 +52,14 @@ struct PCtl {
 
 namespace {
 
+constexpr unsigned long long MBAR_WAIT_NS = 1000000000ull;  // 1 s
+constexpr int MBAR_MAX_TRIES = 1 << 24;
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -514,6 +522,160 @@ __global__ void __launch_bounds__(LEX_THREADS)
     st->last_maxdiv = s_last >= 0 ? (double)__uint_as_float(s_max[s_last & (LEX_RING - 1)]) : 0.0;
   }
   cl_sync();
+}
+
+// ------------------------------------------------------------------ LEXSOR on the whole GPU
+// The closed-form schedule (no early exit, or the speculative early exit's
+// two passes) over every SM: a cooperative launch of one block per SM, a
+// grid barrier per step.  For solves with many sweeps in flight (a step
+// then holds hundreds of thousands of cells: the reference's 200-sweep
+// workload at 2048^2) the step is compute-bound and the cluster's 8 SMs are
+// too few.  Scratch (lex): [0, LEX_RING) the sweeps' maxima, then the
+// barrier's arrival count and generation, then its give-up flag.
+constexpr int LEX_GRID_SCRATCH = LEX_RING + 4;
+
+// A grid barrier: the block's last arrival advances the generation; the
+// others wait for it, for at most about a second (then *fail is set and
+// they go on; the solve's result is then not to be used).  Release / acquire
+// at GPU scope around it order the steps' stores.
+__device__ __forceinline__ void grid_barrier(unsigned* count, unsigned* gen, unsigned nblocks,
+                                             int* fail) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned g0;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g0) : "l"(gen) : "memory");
+    __threadfence();
+    if (atomicAdd(count, 1u) == nblocks - 1) {
+      *count = 0u;
+      __threadfence();
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(gen) : "memory");
+    } else {
+      const unsigned long long t0 = global_ns();
+      for (int it = 0; it < MBAR_MAX_TRIES; ++it) {
+        unsigned gv;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(gv) : "l"(gen) : "memory");
+        if (gv != g0) break;
+        if (global_ns() - t0 > MBAR_WAIT_NS) {
+          atomicExch(fail, 1);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(LEX_THREADS)
+    k_lexsor_grid(float* U, float* V, float* p, const uint8_t* __restrict__ flags, Grid g,
+                  int numIters, float relax0, float damping, float cp, float tol, DevStats* st,
+                  float minRelax, int SP, int* __restrict__ exit_out,
+                  const int* __restrict__ run_from, unsigned* __restrict__ lex, int* err) {
+  const int P = g.P;
+  const int ni = g.NX - 2, nj = g.NY - 2;
+  const int D = ni + nj - 1;
+  const int offE = SP ? SP + 1 : P, offN = SP ? SP : 1;
+  const int L = ni < nj ? ni : nj;
+  unsigned* gmax = lex;
+  unsigned* bcount = lex + LEX_RING;
+  unsigned* bgen = lex + LEX_RING + 1;
+  int* bfail = reinterpret_cast<int*>(lex + LEX_RING + 2);
+  const unsigned nb = gridDim.x;
+  if (numIters <= 0 || ni <= 0 || nj <= 0) return;  // (the same in every block)
+  int runIters = numIters;
+  if (run_from) {
+    const int e = *run_from;
+    if (e < 0 || e >= numIters) return;
+    runIters = e + 1;
+  }
+  // (gmax and the barrier words were zeroed before the launch.)
+  const int gt = (int)blockIdx.x * LEX_THREADS + (int)threadIdx.x;
+  const int stride = (int)nb * LEX_THREADS;
+  const int Lp = (L + 31) & ~31;
+  const float invLp = 1.0f / (float)Lp;
+  const long long steps = (long long)D + 2LL * (runIters - 1);
+  for (long long tau = 0; tau < steps; ++tau) {
+    int t_lo = (int)((tau - D + 2) / 2);
+    if (t_lo < 0) t_lo = 0;
+    while (tau - 2LL * t_lo >= D) ++t_lo;
+    int t_hi = (int)(tau / 2);
+    if (t_hi > runIters - 1) t_hi = runIters - 1;
+    const int lo = t_lo, W = t_hi - t_lo + 1;
+    const int items = W * Lp;
+    for (int base = 0; base < items; base += LEX_CHUNK * stride) {
+      int cc[LEX_CHUNK], rr[LEX_CHUNK], tt[LEX_CHUNK];
+      bool act[LEX_CHUNK] = {};
+      uint8_t fl[LEX_CHUNK];
+      float u0[LEX_CHUNK], u1[LEX_CHUNK], v0[LEX_CHUNK], v1[LEX_CHUNK], p0[LEX_CHUNK];
+#pragma unroll
+      for (int m = 0; m < LEX_CHUNK; ++m) {
+        if (base + m * stride >= items) break;  // (uniform over the grid)
+        const int q = base + m * stride + gt;
+        int k;
+        const int t = lo + (items < (1 << 24) ? div_small(q, Lp, invLp, k) : (k = q % Lp, q / Lp));
+        const int r = t & (LEX_RING - 1);
+        const int delta = q < items ? (int)(tau - 2LL * t) : -1;
+        const int d = 2 + delta;
+        const int i_lo = max(1, d - nj), i_hi = min(ni, d - 1);
+        const int i = i_lo + k;
+        const bool in = delta >= 0 && delta < D && k < L && i <= i_hi;
+        const int c = in ? (SP ? d * SP + i : i * P + (d - i)) : 0;
+        cc[m] = c;
+        rr[m] = r;
+        tt[m] = t;
+        act[m] = in;
+        fl[m] = in ? __ldcg(flags + c) : 0;
+        u0[m] = in ? __ldcg(U + c) : 0.0f;
+        u1[m] = in ? __ldcg(U + c + offE) : 0.0f;
+        v0[m] = in ? __ldcg(V + c) : 0.0f;
+        v1[m] = in ? __ldcg(V + c + offN) : 0.0f;
+        p0[m] = in ? __ldcg(p + c) : 0.0f;
+      }
+#pragma unroll
+      for (int m = 0; m < LEX_CHUNK; ++m) {
+        if (base + m * stride >= items) break;  // (the slots the loads filled)
+        const uint8_t f = fl[m];
+        bool a = act[m] && (f & F_FLUID);
+        const float sx0 = fbit(f, F_W), sx1 = fbit(f, F_E), sy0 = fbit(f, F_S),
+                    sy1 = fbit(f, F_N);
+        const float s = sx0 + sx1 + sy0 + sy1;
+        a = a && s != 0.0f;
+        const float div = a ? u1[m] - u0[m] + v1[m] - v0[m] : 0.0f;
+        const float absDiv = fabsf(div);
+        const bool counted = a && !isnan(absDiv);
+        const unsigned mx = __reduce_max_sync(0xffffffffu, counted ? __float_as_uint(absDiv) : 0u);
+        if ((threadIdx.x & 31) == 0 && mx && (exit_out || tt[m] == runIters - 1))
+          atomicMax(&gmax[rr[m]], mx);
+        if (!a) continue;
+        const int c = cc[m];
+        // Relaxation of sweep t (fluid.go:169-170).
+        float iterProgress = (float)tt[m] / (float)numIters;
+        float rel = relax0 - (relax0 - minRelax) * iterProgress;
+        float pp = -div / s;
+        pp *= rel;
+        pp *= damping;
+        p[c] = p0[m] + cp * pp;
+        U[c] = u0[m] - sx0 * pp;
+        U[c + offE] = u1[m] + sx1 * pp;
+        V[c] = v0[m] - sy0 * pp;
+        V[c + offN] = v1[m] + sy1 * pp;
+      }
+    }
+    grid_barrier(bcount, bgen, nb, bfail);
+    // Block 0 retires the sweep whose last diagonal ran in this step (its
+    // slot is next used LEX_RING sweeps later).
+    const long long rt = tau - (D - 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && rt >= 0 && (rt & 1) == 0 && rt / 2 < runIters) {
+      const int t = (int)(rt / 2), r = t & (LEX_RING - 1);
+      const unsigned m = atomicExch(&gmax[r], 0u);
+      if (exit_out && __uint_as_float(m) < tol) atomicMin(exit_out, t);
+      if (t == runIters - 1) {
+        st->sweeps = runIters;
+        st->last_maxdiv = (double)__uint_as_float(m);
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && *bfail) atomicExch(err, 1);
 }
 
 // Copies of U, V, p and the flags into the diagonal-major layout of the
@@ -1171,14 +1333,7 @@ __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* tm, i
 }
 
 constexpr int TILE_FLOATS = RI * RJ;  // one 64 x 128 box
-constexpr unsigned long long MBAR_WAIT_NS = 1000000000ull;  // 1 s
-constexpr int MBAR_MAX_TRIES = 1 << 24;
 
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
 // Waits for phase `parity` of the barrier for at most about a second (and a
 // bounded number of polls); false when it gave up.
@@ -2101,6 +2256,10 @@ cudaError_t launch_jacobi_solve(fg_fluid* f, void* ctl, const float* b, const fl
 // One k_lexsor solve on the handle's fields: on the diagonal-major copies
 // when the handle has them (copied in and back around the solve), else on
 // the row-major fields.
+// Blocks of the grid-wide wavefront the GPU holds at once (0: unavailable);
+// checked once per process by init_lexsor_cluster.
+static std::atomic<int> g_lex_grid_blocks{0};
+
 // Whether the cluster form of the wavefront can run on this device (checked
 // once per process, outside any capture: fg_create calls it).
 static std::atomic<int> g_lex_cluster{-1};
@@ -2120,7 +2279,18 @@ void init_lexsor_cluster() {
   const bool ok = cudaOccupancyMaxActiveClusters(&n, k_lexsor_cl, &cfg) == cudaSuccess && n >= 1;
   cudaGetLastError();
   g_lex_cluster.store(ok ? 1 : 0);
+  int dev = 0, coop = 0, per = 0, sms = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop &&
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lexsor_grid, LEX_THREADS, 0) ==
+          cudaSuccess &&
+      per >= 1)
+    g_lex_grid_blocks.store(per * sms);
+  cudaGetLastError();
 }
+
+int lexsor_scratch_words() { return LEX_GRID_SCRATCH; }
 
 // One wavefront solve: the cluster kernel when a step gives its threads work
 // (diagonals of at least 256 cells, at least 8 sweeps in the pipeline), else
@@ -2130,6 +2300,31 @@ static void lexsor_kernel(fg_fluid* f, float* U, float* V, float* p, const uint8
                           float minRelax, const int* stop, int SP, int* exit_out = nullptr,
                           const int* run_from = nullptr) {
   const int L = std::min(f->NX - 2, f->NY - 2);
+  // Many sweeps in flight on long diagonals (the closed-form schedule only;
+  // no multigrid stop latch): every SM, a grid barrier per step.
+  const int nblk = g_lex_grid_blocks.load();
+  const int D = f->NX + f->NY - 5;  // (sweeps in flight must fit the maxima's ring)
+  if (!early_exit && !stop && f->lex_scratch && nblk > 0 && L >= 256 && iters >= 32 &&
+      D / 2 + 4 < LEX_RING) {
+    cudaMemsetAsync(f->lex_scratch, 0, sizeof(unsigned) * LEX_GRID_SCRATCH, f->stream);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nblk);
+    cfg.blockDim = dim3(LEX_THREADS);
+    cfg.stream = f->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_lexsor_grid, U, V, p, flags, f->g, iters, relax0,
+                           f->prm.pressure_damping, cp, f->prm.tolerance, st, minRelax, SP,
+                           exit_out, run_from, f->lex_scratch, &f->dstats->timeout) ==
+        cudaSuccess) {
+      count(f);
+      return;
+    }
+    cudaGetLastError();
+  }
   if (L >= 256 && iters >= 8 && g_lex_cluster.load() == 1) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(LEX_CLUSTER);

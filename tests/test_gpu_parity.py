@@ -317,13 +317,15 @@ def test_invalid_mask_fails_loudly(gpu):
     assert e.value.code == -5
 
 
-@pytest.mark.parametrize("w,h,early", [(300, 280, True), (300, 280, False), (640, 300, True)])
-def test_lexsor_cluster_bitwise(gpu, w, h, early):
-    """Grids whose diagonals hold at least 256 cells, 30 sweeps: the
-    reference SOR runs as the cluster form of the wavefront (with the early exit: rank 0's
-    bookkeeping over distributed shared memory; without: the closed-form
-    schedule), bit for bit, sweep count included."""
-    g, o = both(gpu, w, h, num_iters=30, UseBFECC=True, early_exit=early, tolerance=1e-3)
+@pytest.mark.parametrize("w,h,early,iters", [(300, 280, True, 30), (300, 280, False, 30),
+                                              (640, 300, True, 30), (300, 280, False, 40),
+                                              (300, 280, True, 40)])
+def test_lexsor_cluster_bitwise(gpu, w, h, early, iters):
+    """Grids whose diagonals hold at least 256 cells: the reference SOR runs
+    as the cluster form of the wavefront (30 sweeps) or, with 32 sweeps or
+    more, on every SM with a grid barrier per step; with the early exit as
+    the speculative passes; bit for bit, sweep count included."""
+    g, o = both(gpu, w, h, num_iters=iters, UseBFECC=True, early_exit=early, tolerance=1e-3)
     for f in (g, o):
         scenes.jet_scene(f)
         f.SetCircularObstacle(w // 3, h // 2, 12)
