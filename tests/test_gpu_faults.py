@@ -132,3 +132,29 @@ def test_concurrent_dataflow_solves_on_two_streams(gpu):
         for k in ("U", "V", "M", "p"):
             x, y = getattr(f, k), getattr(r, k)
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (seed, k)
+
+
+def test_reference_sor_without_its_copies_falls_back_bitwise(gpu):
+    """When the diagonal-major copies cannot be allocated (an injected
+    allocation failure at the first step), the reference SOR runs on the
+    row-major fields and still equals the oracle bit for bit."""
+    from oracle.pyoracle import OracleFluid
+
+    for w, h in ((60, 40), (300, 280)):  # one block, the cluster
+        g = gpu.Fluid(1.0, w, h, 1.0, num_iters=30, UseBFECC=True, tolerance=1e-3)
+        o = OracleFluid(1.0, w, h, 1.0, prec=32, num_iters=30, UseBFECC=True, tolerance=1e-3)
+        for f in (g, o):
+            scenes.jet_scene(f)
+            scenes.random_state(f, seed=5, amp=0.5)
+        g.mark_dirty()
+        g.download()  # (queued edits and mirrors reach the device first)
+        gpu.debug_fail_alloc(0)
+        try:
+            g.Simulate(0.1)
+        finally:
+            gpu.debug_fail_alloc(-1)
+        o.Simulate(0.1)
+        for k in ("U", "V", "M", "p"):
+            a, b = getattr(g, k), getattr(o, k)
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (w, k)
+        assert g.stats()["sweeps"] == o.stats()["sweeps"]

@@ -337,6 +337,20 @@ def test_lexsor_cluster_bitwise(gpu, w, h, early, iters):
     assert g.stats()["sweeps"] == o.stats()["sweeps"]
 
 
+@pytest.mark.parametrize("w,h", [(8200, 10), (8000, 300)])
+def test_lexsor_bookkeeping_early_exit_bitwise(gpu, w, h):
+    """Grids whose diagonals outnumber the sweep ring (NX + NY > 8190): the
+    early exit runs with the step-by-step bookkeeping (one block; the
+    cluster with the bookkeeping in rank 0's shared memory), bit for bit."""
+    g, o = both(gpu, w, h, num_iters=30, UseBFECC=True, tolerance=1e-3)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        scenes.jet_inject(f, speed=3.0)
+        f.Simulate(0.1)
+    assert_bitwise(g, o, where="%dx%d" % (w, h))
+    assert g.stats()["sweeps"] == o.stats()["sweeps"]
+
+
 @pytest.mark.parametrize("w,h", [(40, 30), (320, 300), (4000, 100)])
 def test_lexsor_early_exit_mid_solve_bitwise(gpu, w, h):
     """A nearly divergence-free state whose solve stops part way: the
