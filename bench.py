@@ -836,6 +836,13 @@ def run_ours(args):
         "bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
         "traffic": tr.get("dram_bytes_per_launch_full") if tr else None,
         "traffic_source": tr.get("source") if tr else None,
+        "model": "13 B per cell-sweep (phi r/w 8, rhs 4, mask 1), each of the phase's 8 sweeps "
+                 "counted; the sweeps run in registers, so this model exceeds the HBM peak",
+        # The compulsory traffic of a phase -- phi read and written, w and w*b
+        # read once (16 B per cell) -- over the same time.
+        "compulsory": {"bytes_per_launch": 16 * n_cells,
+                       "achieved": 16 * n_cells / (launch_ms / 1e3) / 1e9,
+                       "frac": 16 * n_cells / (launch_ms / 1e3) / 1e9 / peak},
     }
 
     # ------------------------------------------------------------ e2e through the C ABI
