@@ -66,6 +66,33 @@ __device__ __forceinline__ float trace_sample_v(const float* __restrict__ Ut,
   return sample_field(Fs, x, y, g.hh, 0.0f, g);
 }
 
+// Interior cells (1 <= i <= NX-2, 1 <= j <= NY-2): every load of the two
+// traces is in range whatever the flags say, so the interior paths below
+// issue them beside the flag load instead of after it, and sample before
+// selecting.  The departure points are the same expressions as in
+// trace_sample_u/v, so the results are bitwise the same.
+__device__ __forceinline__ bool interior_ij(int i, int j, const Grid& g) {
+  return i >= 1 && j >= 1 && i <= g.NX - 2 && j <= g.NY - 2;
+}
+struct Departure {
+  float xu, yu;  // from the U face
+  float xv, yv;  // from the V face
+};
+__device__ __forceinline__ Departure departures(const float* __restrict__ Ut,
+                                                const float* __restrict__ Vt, int i, int j,
+                                                int c, float sdt, const Grid& g) {
+  float uu = Ut[c];
+  float vu = (Vt[c - g.P] + Vt[c] + Vt[c - g.P + 1] + Vt[c + 1]) * 0.25f;
+  float uv = (Ut[c - 1] + Ut[c] + Ut[c + g.P - 1] + Ut[c + g.P]) * 0.25f;
+  float vv = Vt[c];
+  Departure d;
+  d.xu = (float)i * g.h - sdt * uu;
+  d.yu = ((float)j * g.h + g.hh) - sdt * vu;
+  d.xv = ((float)i * g.h + g.hh) - sdt * uv;
+  d.yv = (float)j * g.h - sdt * vv;
+  return d;
+}
+
 // advectVelocity (fluid.go:291-333) with trace field = sampled field =
 // border field = (Ui, Vi); stale values from the staging buffers nU, nV;
 // result to (Uo, Vo) and back into (nU, nV).
@@ -76,9 +103,22 @@ __device__ __forceinline__ void sl_velocity_cell(int i, int j, const float* __re
                                                  const uint8_t* __restrict__ flags, float dt,
                                                  const Grid& g) {
   int c = i * g.P + j;
+  float u, v;
+  if (interior_ij(i, j, g)) {
+    uint8_t fl = flags[c];
+    Departure d = departures(Ui, Vi, i, j, c, dt, g);
+    float su = sample_field(Ui, d.xu, d.yu, 0.0f, g.hh, g);
+    float sv = sample_field(Vi, d.xv, d.yv, g.hh, 0.0f, g);
+    u = u_advected(fl, i, j, g) ? su : nU[c];
+    v = v_advected(fl, i, j, g) ? sv : nV[c];
+    Uo[c] = u;
+    Vo[c] = v;
+    nU[c] = u;
+    nV[c] = v;
+    return;
+  }
   uint8_t fl = flags[c];
   bool ring = on_ring(i, j, g);
-  float u, v;
   if (u_advected(fl, i, j, g))
     u = trace_sample_u(Ui, Vi, Ui, i, j, dt, g);
   else
@@ -112,6 +152,15 @@ __device__ __forceinline__ void bfecc_vel_fwd_cell(int i, int j, const float* __
                                                    const uint8_t* __restrict__ flags, float dt,
                                                    const Grid& g) {
   int c = i * g.P + j;
+  if (interior_ij(i, j, g)) {
+    uint8_t fl = flags[c];
+    Departure d = departures(Ui, Vi, i, j, c, dt, g);
+    float su = sample_field(Ui, d.xu, d.yu, 0.0f, g.hh, g);
+    float sv = sample_field(Vi, d.xv, d.yv, g.hh, 0.0f, g);
+    Fu[c] = u_advected(fl, i, j, g) ? su : nU[c];
+    Fv[c] = v_advected(fl, i, j, g) ? sv : nV[c];
+    return;
+  }
   uint8_t fl = flags[c];
   bool ring = on_ring(i, j, g);
   Fu[c] = u_advected(fl, i, j, g) ? trace_sample_u(Ui, Vi, Ui, i, j, dt, g) : (ring ? Ui[c] : nU[c]);
@@ -129,9 +178,10 @@ __global__ void k_bfecc_vel_fwd(const float* __restrict__ Ui, const float* __res
 
 // clampToNeighbors (fluid.go:1094-1120) for an interior cell (all 3x3
 // neighbours in range).
-__device__ __forceinline__ float clamp3x3(float val, const float* __restrict__ src, int c,
-                                          int P) {
-  float lo = src[c], hi = src[c];
+__device__ __forceinline__ void range3x3(const float* __restrict__ src, int c, int P, float& lo,
+                                         float& hi) {
+  lo = src[c];
+  hi = src[c];
 #pragma unroll
   for (int di = -1; di <= 1; ++di)
 #pragma unroll
@@ -140,6 +190,8 @@ __device__ __forceinline__ float clamp3x3(float val, const float* __restrict__ s
       if (v < lo) lo = v;
       if (v > hi) hi = v;
     }
+}
+__device__ __forceinline__ float clamp_to(float val, float lo, float hi) {
   if (val < lo) return lo;
   if (val > hi) return hi;
   return val;
@@ -163,14 +215,22 @@ __device__ __forceinline__ void bfecc_vel_correct_cell(int i, int j, const float
     Cv[c] = Vi[c];
     return;
   }
+  // Off the ring every cell is interior: all loads below are in range, so
+  // they are issued together and the samples are taken before selecting.
   uint8_t fl = flags[c];
-  float bu = u_advected(fl, i, j, g) ? trace_sample_u(Ui, Vi, Fu, i, j, -dt, g) : 0.0f;
-  float bv = v_advected(fl, i, j, g) ? trace_sample_v(Ui, Vi, Fv, i, j, -dt, g) : 0.0f;
+  Departure d = departures(Ui, Vi, i, j, c, -dt, g);
   float ou = Ui[c], ov = Vi[c];
+  float lou, hiu, lov, hiv;
+  range3x3(Ui, c, g.P, lou, hiu);
+  range3x3(Vi, c, g.P, lov, hiv);
+  float su = sample_field(Fu, d.xu, d.yu, 0.0f, g.hh, g);
+  float sv = sample_field(Fv, d.xv, d.yv, g.hh, 0.0f, g);
+  float bu = u_advected(fl, i, j, g) ? su : 0.0f;
+  float bv = v_advected(fl, i, j, g) ? sv : 0.0f;
   float cu = ou - (bu - ou) * 0.5f;
   float cv = ov - (bv - ov) * 0.5f;
-  Cu[c] = clamp3x3(cu, Ui, c, g.P);
-  Cv[c] = clamp3x3(cv, Vi, c, g.P);
+  Cu[c] = clamp_to(cu, lou, hiu);
+  Cv[c] = clamp_to(cv, lov, hiv);
 }
 __global__ void k_bfecc_vel_correct(const float* __restrict__ Ui, const float* __restrict__ Vi,
                                     const float* __restrict__ Fu, const float* __restrict__ Fv,
@@ -197,6 +257,7 @@ __device__ __forceinline__ float smoke_value(const float* __restrict__ Ut,
   return sample_field(Ms, x, y, g.hh, g.hh, g);
 }
 
+
 // One cell of advectSmoke: writes Mo and nM, returns the new value.
 __device__ __forceinline__ float sl_smoke_value(int i, int j, const float* __restrict__ Ut,
                                                 const float* __restrict__ Vt,
@@ -208,15 +269,22 @@ __device__ __forceinline__ float sl_smoke_value(int i, int j, const float* __res
   int c = i * g.P + j;
   uint8_t fl = flags[c];
   float m;
-  if ((fl & (F_INTERIOR | F_FLUID)) == (F_INTERIOR | F_FLUID)) {
+  if (interior_ij(i, j, g)) {
+    // The trace's loads are in range on interior cells: the sample is taken
+    // whatever the flags say (its loads issue beside the flag load) and
+    // kept on fluid cells.
     float s = smoke_value(Ut, Vt, Ms, i, j, dt, smokeAdv, g);
-    if (diffuse) {
-      float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
-      s += smokeDiffusion * neighbors;
+    if (fl & F_FLUID) {
+      if (diffuse) {
+        float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
+        s += smokeDiffusion * neighbors;
+      }
+      m = go_max(s, 0.0f);
+    } else {
+      m = nM[c];
     }
-    m = go_max(s, 0.0f);
   } else {
-    m = on_ring(i, j, g) ? Ms[c] : nM[c];
+    m = Ms[c];  // off the interior every cell is on the ring
   }
   Mo[c] = m;
   nM[c] = m;
@@ -267,15 +335,22 @@ __device__ __forceinline__ void bfecc_smoke_fwd_cell(int i, int j, const float* 
   int c = i * g.P + j;
   uint8_t fl = flags[c];
   float m;
-  if ((fl & (F_INTERIOR | F_FLUID)) == (F_INTERIOR | F_FLUID)) {
+  if (interior_ij(i, j, g)) {
+    // The trace's loads are in range on interior cells: the sample is taken
+    // whatever the flags say (its loads issue beside the flag load) and
+    // kept on fluid cells.
     float s = smoke_value(Ut, Vt, Ms, i, j, dt, smokeAdv, g);
-    if (diffuse) {
-      float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
-      s += smokeDiffusion * neighbors;
+    if (fl & F_FLUID) {
+      if (diffuse) {
+        float neighbors = Ms[c - g.P] + Ms[c + g.P] + Ms[c - 1] + Ms[c + 1] - 4.0f * Ms[c];
+        s += smokeDiffusion * neighbors;
+      }
+      m = go_max(s, 0.0f);
+    } else {
+      m = nM[c];
     }
-    m = go_max(s, 0.0f);
   } else {
-    m = on_ring(i, j, g) ? Ms[c] : nM[c];
+    m = Ms[c];  // off the interior every cell is on the ring
   }
   Fm[c] = m;
 }
@@ -305,11 +380,16 @@ __device__ __forceinline__ void bfecc_smoke_correct_cell(int i, int j, const flo
     Cm[c] = Mi[c];
     return;
   }
+  // Off the ring every cell is interior: the sample's loads are in range and
+  // issue with the flag load.
   uint8_t fl = flags[c];
-  float b = (fl & F_FLUID) ? smoke_value(Ut, Vt, Fm, i, j, -dt, smokeAdv, g) : 0.0f;
   float o = Mi[c];
+  float lo, hi;
+  range3x3(Mi, c, g.P, lo, hi);
+  float s = smoke_value(Ut, Vt, Fm, i, j, -dt, smokeAdv, g);
+  float b = (fl & F_FLUID) ? s : 0.0f;
   float cm = o - (b - o) * 0.5f;
-  cm = clamp3x3(cm, Mi, c, g.P);
+  cm = clamp_to(cm, lo, hi);
   if (cm < 0.0f) cm = 0.0f;
   Cm[c] = cm;
 }
