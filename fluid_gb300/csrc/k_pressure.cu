@@ -976,11 +976,15 @@ __device__ __forceinline__ void setup_cell_p(int i, int j, const float* __restri
   int c = i * Ps + j;
   float b = 0.0f, w = 0.0f, bw = 0.0f;
   uint8_t fl = flags[c];
-  if (flag_active(fl)) {
+  // Active cells are interior.  Below the last row and column the four face
+  // loads are in range whatever the flags say, so they issue beside the flag
+  // load and the flags only select the result.
+  if (i <= g.NX - 2 && j <= g.NY - 2) {
     float div = with_force(U, Fu, u + g.P) - with_force(U, Fu, u) + with_force(V, Fv, u + 1) -
                 with_force(V, Fv, u);
-    b = -div;
-    w = om / (float)flag_count(fl);
+    bool act = flag_active(fl);
+    b = act ? -div : 0.0f;
+    w = act ? om / (float)flag_count(fl) : 0.0f;
     bw = w * b;
   }
   rhs[c] = b;
