@@ -2,6 +2,7 @@
 // sequence and the views.  The kernels live in k_*.cu.
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -359,7 +360,10 @@ int fg_params_default(fg_params* out) {
 int fg_create(int width, int height, float density, float h, const fg_params* params,
               fg_fluid** out) {
   if (!out || width < 1 || height < 1 || !(h > 0.0f)) return FG_ERR_INVALID;
-  if ((long long)(width + 2) * (height + 2) > (1ll << 30)) return FG_ERR_INVALID;
+  // Cell indices are 32-bit: the padded grid (rows of NY rounded up to 32)
+  // stays within 2^30 cells.
+  const long long nx = (long long)width + 2, pitch = ((long long)height + 2 + 31) / 32 * 32;
+  if (nx * pitch > (1ll << 30)) return FG_ERR_INVALID;
   *out = nullptr;
   fg_fluid* f = new fg_fluid();
   fg_params_default(&f->prm);
@@ -618,6 +622,9 @@ void ensure_skew(fg_fluid* f) {
   if (f->skew[0] || f->batch || !(f->prm.scheme == FG_SCHEME_LEXSOR || multigrid(f))) return;
   const int sp = (f->NX + 31) / 32 * 32;
   const size_t n = (size_t)(f->NX + f->NY - 1) * sp;
+  // The wavefront kernels index the copies with 32-bit integers: a grid much
+  // wider than tall whose copies exceed that keeps the row-major kernel.
+  if (n > (size_t)INT_MAX) return;
   float* a[3] = {};
   uint8_t* fl = nullptr;
   bool ok = true;

@@ -2636,6 +2636,8 @@ extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, 
     return FG_ERR_INVALID;
   const int Ps = (num_y + 31) / 32 * 32;  // solver pitch inside the scratch
   if ((size_t)num_x * (size_t)Ps > kNoAllocMaxCells) return FG_ERR_TOO_LARGE;
+  // The caller's fields are indexed with 32-bit integers too.
+  if ((size_t)num_x * (size_t)pitch > (size_t)INT_MAX) return FG_ERR_TOO_LARGE;
   int T = clamp_tb(tb_depth);
   int nlaunch = (num_iters + T - 1) / T;
   if (nlaunch > kNoAllocSlots) return FG_ERR_TOO_LARGE;

@@ -107,7 +107,9 @@ typedef struct fg_fluid fg_fluid;
 int fg_params_default(fg_params* out);
 
 /* fluid.New(density, width, height, h) -- fluid.go:42-68.  Allocates the
- * NumX = width+2 by NumY = height+2 grid on the current device. */
+ * NumX = width+2 by NumY = height+2 grid on the current device.  Cells are
+ * indexed with 32-bit integers: NumX * (NumY rounded up to 32) above 2^30
+ * returns FG_ERR_INVALID (before any device call). */
 int fg_create(int width, int height, float density, float h, const fg_params* params,
               fg_fluid** out);
 /* Releases the handle (no counterpart: Go frees by GC). */

@@ -52,3 +52,23 @@ def test_null_handle_is_rejected_without_device():
     assert L.fg_last_error(None) == b"invalid handle"
     assert L.fg_simulate(None, 0.1) == _lib.FG_ERR_INVALID
     assert L.fg_destroy(None) == _lib.FG_ERR_INVALID
+
+
+def test_oversized_grids_are_rejected_before_any_device_call():
+    """Cell indices are 32-bit: fg_create refuses a padded grid above 2^30
+    cells and fg_project_noalloc a caller pitch whose fields exceed 2^31
+    cells, both before touching a device (so this runs without a GPU)."""
+    L = _lib.load()
+    h = _lib._vp()
+    for w, hh in ((2 ** 15, 2 ** 15), (40_000_000, 1), (2 ** 31 - 2, 1), (1, 2 ** 31 - 2)):
+        assert L.fg_create(w, hh, 1.0, 1.0, None, ctypes.byref(h)) == _lib.FG_ERR_INVALID, (w, hh)
+        assert not h.value
+    # A normal grid passes the check: without a GPU it stops at the device.
+    rc = L.fg_create(64, 48, 1.0, 1.0, None, ctypes.byref(h))
+    if rc == 0:
+        L.fg_destroy(h)
+    assert rc in (0, _lib.FG_ERR_CUDA)
+    dummy = ctypes.c_void_p(256)
+    rc = L.fg_project_noalloc(dummy, dummy, dummy, dummy, 3, 3, 2 ** 30, 1.0, 1.0, 0.1, 8,
+                              1.0, 1.0, 8, 0, 1e-5, None)
+    assert rc == _lib.FG_ERR_TOO_LARGE
