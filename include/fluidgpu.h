@@ -40,7 +40,7 @@ extern "C" {
 #define FG_ERR_MASK (-5)        /* S holds a value other than 0 or 1                     */
 #define FG_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up                    */
 #define FG_ERR_NOMEM (-7)       /* device or pinned allocation failed                    */
-#define FG_ERR_TOO_LARGE (-8)   /* grid beyond the fixed scratch of fg_project_noalloc    */
+#define FG_ERR_TOO_LARGE (-8)   /* fg_project_noalloc: grid beyond its scratch or indices */
 #define FG_ERR_NONFINITE (-9)   /* a statistic of the last step is NaN or infinite        */
 
 /* Field identifiers (Fluid.U, .V, .newU, .newV, .p, .S, .M, .newM). */
@@ -229,7 +229,8 @@ unsigned long long fg_edit_bytes(const fg_fluid* f);
  * floats (pitch >= num_y), cell (i, j) at i*pitch + j.  Its scratch is a
  * fixed array inside the library of FG_NOALLOC_MAX_CELLS cells (about
  * 21 MiB, held on every GPU that loads the library until the process exits):
- * num_x * (num_y rounded up to 32) above FG_NOALLOC_MAX_CELLS, or more than
+ * num_x * (num_y rounded up to 32) above FG_NOALLOC_MAX_CELLS, num_x * pitch
+ * above 2^31 - 1 (cells are indexed with 32-bit integers), or more than
  * 4096 Jacobi launches (num_iters / tb_depth), returns FG_ERR_TOO_LARGE.  The work is
  * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream)
  * and the call returns without waiting.  The first call on a device looks up
