@@ -703,9 +703,12 @@ def cpu_app_rows(threads):
     return out
 
 
-def cpu_reference_steps(steps, threads, budget_s=None):
+def cpu_reference_steps(steps, threads, warmup=0, budget_s=None):
     """Times the reference algorithm (FP32, serial SOR pressure, parallelRange
-    stages on `threads` host threads) on the cavity workload."""
+    stages on `threads` host threads) on the cavity workload: `warmup`
+    untimed steps, then up to `steps` timed ones on the same state (fewer
+    when `budget_s` seconds, estimated from the last warm-up step, would
+    not hold them all)."""
     from oracle.pyoracle import LEXSOR, OracleFluid
 
     o = OracleFluid(1.0, W, H, 1.0, prec=32, threads=threads, scheme=LEXSOR, num_iters=ITERS,
@@ -713,16 +716,20 @@ def cpu_reference_steps(steps, threads, budget_s=None):
     S = o.S.reshape(o.NumX, o.NumY)
     S[:] = 1.0
     S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
-    times = []
-    for k in range(steps):
+
+    def step():
         for i in range(2, o.NumX - 2):
             o.SetVelocity(i, o.NumY - 2, 1.0, 0.0)
         t0 = time.perf_counter()
         o.Simulate(DT)
-        times.append(time.perf_counter() - t0)
-        if budget_s is not None and sum(times) > budget_s:
-            break
-    return times
+        return time.perf_counter() - t0
+
+    last = None
+    for _ in range(warmup):
+        last = step()
+    if budget_s is not None and last is not None:
+        steps = max(1, min(steps, int(budget_s / max(last, 1e-3))))
+    return [step() for _ in range(steps)]
 
 
 # ---------------------------------------------------------------- arms
@@ -732,23 +739,22 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     # Each step is one full 2048^2 step of the reference algorithm (~seconds
-    # on the host); the count is bounded so the whole run ends in minutes.
-    warm = cpu_reference_steps(1, threads)
-    per = warm[0]
-    n = max(1, min(args.steps, int(90.0 / max(per, 1e-3))))
-    times = cpu_reference_steps(n, threads)
+    # on the host): W warm-up steps (1 to 10), then the timed steps on the
+    # same state, their count bounded so the whole run ends in minutes.
+    warmup = max(1, min(args.warmup, 10))
+    times = cpu_reference_steps(args.steps, threads, warmup=warmup, budget_s=90.0)
     sec = sum(times)
     value = W * H * len(times) / sec / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mcell-steps/s",
-        "n_gpus": args.gpus, "steps": len(times), "warmup": 1,
+        "n_gpus": args.gpus, "steps": len(times), "warmup": warmup,
         "ms_per_step": 1e3 * sec / len(times), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config({"scheme": "reference serial lexicographic SOR (fluid.go:157-234)"}),
         "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
-                         "sample": "%d full 2048x2048 steps after 1 warm-up step; pressure loop "
-                                   "serial as in the reference, other stages on %d threads"
-                                   % (len(times), threads)},
+                         "sample": "%d full 2048x2048 steps after %d warm-up step(s); pressure "
+                                   "loop serial as in the reference, other stages on %d threads"
+                                   % (len(times), warmup, threads)},
         "e2e": {"value": value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
