@@ -44,7 +44,23 @@ TB = 8
 REFINE = 8
 # Algorithmic bytes per cell per Jacobi sweep (phi read + write, rhs, 1-byte mask).
 JACOBI_BYTES_PER_CELL_SWEEP = 13
+# Compulsory bytes per cell of one 8-sweep phase run in registers: phi read and
+# written, w and w*b read once.
+JACOBI_BYTES_PER_CELL_PHASE = 16
 FALLBACK_HBM_GBS = 6800.0
+# Compulsory bytes per cell of each stage of the headline step (each pass
+# reads each of its inputs once and writes each output once; FP32 fields,
+# 1-byte flags).  Keys are the step's profiled stages.
+STAGE_BYTES_PER_CELL = {
+    "sources+viscosity": 0,            # lid cells only; viscosity off
+    "pressure setup": 21,              # U, V, flags -> b, w, w*b
+    "jacobi sweeps": JACOBI_BYTES_PER_CELL_PHASE * ITERS // TB,  # 25 phases
+    "outer correction": 17,            # phi, w, b, flags -> e (one launch of 8 sweeps)
+    "gradient+div stats": 45,          # U, V, phi, e, b, flags, noise -> U, V, p
+    "confinement/turbulence+borders": 0,  # confinement off, turbulence fused; perimeter only
+    "advect velocity": 59,             # BFECC: fwd 17 + bwd/correct/clamp 25 + final 17
+    "advect smoke+mass": 55,           # BFECC: 17 + 21 + 17
+}
 
 
 def workload_config(extra=None):
@@ -200,6 +216,193 @@ def profile_leg(args, name):
         torch.cuda.cudart().cudaProfilerStop()
 
     return stop
+
+
+def jacobi_roofline(n_cells, phase_ms, peak, peak_kind, tr, clocks):
+    """Roofline of the dominant kernel, k_jacobi_flow, per 8-sweep phase.
+
+    `achieved` counts the phase's compulsory bytes: an 8-sweep phase run in
+    registers must read phi, w and w*b and write phi once (16 B per cell),
+    over the phase's CUDA-event time.  The solve's arrays stay in L2 across
+    phases, so the DRAM traffic ncu measures (`traffic`) is below that, and
+    the kernel's binding limit is instruction issue: `issue` compares the
+    phase's warp instructions (ncu) with what 4 schedulers per SM issue at the
+    sampled SM clock.  The per-sweep model (13 B per cell and sweep, every
+    sweep of the phase counted) is kept beside it."""
+    sec = phase_ms / 1e3
+    comp = JACOBI_BYTES_PER_CELL_PHASE * n_cells
+    model = JACOBI_BYTES_PER_CELL_SWEEP * TB * n_cells
+    achieved = comp / sec / 1e9
+    out = {
+        "kernel": "k_jacobi_flow (one cooperative launch per solve: 25 phases of 8 sweeps; "
+                  "figures per phase)",
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak,
+        "peak_source": peak_kind + " MEASURED_PEAKS.json hbm_gbs" if peak_kind == "measured"
+        else "fallback 6.8 TB/s",
+        "bytes_per_launch": comp, "launch_ms": phase_ms,
+        "traffic": tr.get("dram_bytes_per_launch_full") if tr else None,
+        "traffic_source": tr.get("source") if tr else None,
+        "model": "compulsory bytes of an 8-sweep phase run in registers: phi read and written, "
+                 "w and w*b read (16 B per cell)",
+        "per_sweep_model": {"bytes_per_launch": model, "achieved": model / sec / 1e9,
+                            "ratio_to_peak": model / sec / 1e9 / peak,
+                            "model": "13 B per cell-sweep (phi r/w 8, rhs 4, mask 1), all 8 "
+                                     "sweeps of the phase counted; the sweeps run in registers, "
+                                     "so this exceeds the HBM peak"},
+    }
+    inst = tr.get("warp_inst_per_phase") if tr else None
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if inst and mhz:
+        sms = tr.get("sms", 152)
+        peak_inst = sms * 4 * mhz * 1e6  # one warp instruction per scheduler per clock
+        out["issue"] = {"warp_inst_per_phase": inst, "achieved_warp_inst_per_s": inst / sec,
+                        "peak_warp_inst_per_s": peak_inst, "frac": inst / sec / peak_inst,
+                        "source": tr.get("inst_source")}
+    return out
+
+
+def step_roofline(stage_ms, n_cells, ms_per_step, peak):
+    """The whole step against HBM: the compulsory bytes of every stage
+    (STAGE_BYTES_PER_CELL) over the device-timed step, and each stage's
+    bytes over its own profiled time."""
+    per_cell = sum(STAGE_BYTES_PER_CELL.values())
+    total = per_cell * n_cells
+    achieved = total / (ms_per_step / 1e3) / 1e9
+    stages = {}
+    for name, ms in stage_ms.items():
+        b = STAGE_BYTES_PER_CELL.get(name)
+        if b and ms > 0:
+            gbs = b * n_cells / (ms / 1e3) / 1e9
+            stages[name] = {"bytes_per_cell": b, "ms": ms, "gbs": gbs, "frac": gbs / peak}
+    return {"bytes_per_cell": per_cell, "bytes_per_step": total, "ms_per_step": ms_per_step,
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "stages": stages}
+
+
+def fp64_error(f):
+    """One step of the FP64 oracle from the GPU's current state beside the
+    GPU's own step: velocity max-abs error relative to max |U|, and the two
+    post-projection divergence L2 norms."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import scenes
+    from oracle.pyoracle import OracleFluid
+
+    o = OracleFluid(1.0, W, H, 1.0, prec=64, threads=os.cpu_count() or 1, scheme=1,
+                    num_iters=ITERS, check_every=TB, UseBFECC=True, early_exit=False,
+                    refine_sweeps=REFINE)
+    f.synchronize()
+    f.download()
+    for k in ("U", "V", "M", "newU", "newV", "newM", "S"):
+        getattr(o, k)[:] = getattr(f, k)
+    f.Simulate(DT)
+    scenes.cavity_lid(o)
+    o.Simulate(DT)
+    f.synchronize()
+    f.download()
+    scale = float(np.abs(o.U).max())
+    err = max(float(np.abs(f.U.astype(np.float64) - o.U).max()),
+              float(np.abs(f.V.astype(np.float64) - o.V).max())) / scale
+    dg, do = f.stats()["div_l2_post"], o.stats()["div_l2_post"]
+    return {"vel_maxabs_rel": err, "div_l2_post_gpu": dg, "div_l2_post_fp64": do,
+            "div_l2_abs_diff": abs(dg - do), "bound": {"vel_maxabs_rel": 1e-4, "div_l2": 1e-5},
+            "how": "after the timed steps the FP64 oracle is set to the GPU's state and both "
+                   "take one step; tests/test_gpu_headline.py asserts the bounds every 100 "
+                   "steps over 500"}
+
+
+def config_rows(fluid_gb300, threads):
+    """The two smaller configurations, each against its CPU port: the 128^2
+    jet (walls left, top and bottom; 8-row jet U = 2 with smoke 1; BFECC and
+    confinement off; 40 iterations) and the 512x256 Karman street (disc
+    r = 24, inflow U = 1, BFECC, confinement 0.3, 100 Jacobi sweeps)."""
+    import numpy as np
+    import torch
+    from oracle.pyoracle import LEXSOR, OracleFluid
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import scenes
+
+    rows = {}
+    # Config 1: the reference scheme bit for bit, and the Jacobi scheme.
+    for key, params in (("jet128_reference_sor", dict(num_iters=40)),
+                        ("jet128_jacobi", dict(scheme=fluid_gb300.SCHEME_JACOBI, num_iters=40,
+                                               tb_depth=8, early_exit=False))):
+        f = fluid_gb300.Fluid(1.0, 128, 128, 1.0, auto_sync=False, **params)
+        jet_setup(f)
+        st = torch.cuda.ExternalStream(f.stream)
+        for _ in range(3):
+            f.Simulate(DT)
+        ms = device_ms(st, lambda: f.Simulate(DT), 200)
+        rows[key] = {"value": 128 * 128 / ms / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms,
+                     "steps": 200}
+        del f
+    o = OracleFluid(1.0, 128, 128, 1.0, prec=32, threads=threads, scheme=LEXSOR, num_iters=40)
+    scenes.jet_scene(o)
+    for _ in range(3):
+        scenes.jet_inject(o)
+        o.Simulate(DT)
+    t0 = time.perf_counter()
+    for _ in range(200):
+        scenes.jet_inject(o)
+        o.Simulate(DT)
+    sec = (time.perf_counter() - t0) / 200
+    cpu1 = {"value": 128 * 128 / sec / 1e6, "unit": "Mcell-steps/s", "cores": threads,
+            "kind": "port", "sample": "200 steps after 3 warm-up steps (reference SOR, 40 "
+                                      "iterations with early exit; jet edits on the host)"}
+    rows["jet128_reference_sor"]["cpu_baseline"] = cpu1
+    rows["jet128_jacobi"]["cpu_baseline"] = cpu1
+    rows["jet128_reference_sor"]["config"] = ("128x128 jet (config 1): reference lexicographic SOR "
+                                              "bit for bit, 40 iterations with early exit, jet "
+                                              "held by device sources; device-timed")
+    rows["jet128_jacobi"]["config"] = ("128x128 jet (config 1) with the Jacobi scheme, 40 fixed "
+                                       "sweeps; device-timed")
+    # Config 2: Karman street.
+    kw = dict(scheme=fluid_gb300.SCHEME_JACOBI, num_iters=100, tb_depth=4, early_exit=False,
+              UseBFECC=True, Confinement=0.3)
+    g = fluid_gb300.Fluid(1.0, 512, 256, 1.0, auto_sync=False, **kw)
+    scenes.fast_walls(g, top=True, bottom=True, left=False, right=False)
+    g.mark_dirty()
+    g.SetCircularObstacle(128, 128, 24)
+    g.download()
+    rng = np.random.default_rng(2)
+    U0 = ((1.0 + rng.uniform(-1e-3, 1e-3, g.numCells)) * (g.S != 0)).reshape(g.NumX, g.NumY)
+    U0[0, :] = 0.0
+    U0[:, 0] = U0[:, -1] = 0.0
+    g.U[:] = U0.ravel()
+    g.mark_dirty()
+    S0 = g.S.copy()
+    rr = np.arange(1, g.NumY - 1, dtype=np.int32)
+    g.set_sources(np.ones_like(rr), rr, u=1.0, v=0.0, mode=g.SRC_SKIP_SOLID | g.SRC_SET_VELOCITY)
+    st = torch.cuda.ExternalStream(g.stream)
+    for _ in range(3):
+        g.Simulate(DT)
+    ms = device_ms(st, lambda: g.Simulate(DT), 200)
+    rows["karman512x256_jacobi"] = {
+        "value": 512 * 256 / ms / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms, "steps": 200,
+        "config": "512x256 Karman street (config 2): disc r 24 at (128, 128), inflow U = 1, "
+                  "BFECC, confinement 0.3, 100 Jacobi sweeps (blocks of 4); device-timed"}
+    del g
+    o = OracleFluid(1.0, 512, 256, 1.0, prec=32, threads=threads, scheme=LEXSOR, num_iters=100,
+                    UseBFECC=True, Confinement=0.3)
+    o.S[:] = S0
+    o.U[:] = U0.ravel()
+    for _ in range(2):
+        scenes.karman_inflow(o)
+        o.Simulate(DT)
+    t0 = time.perf_counter()
+    n = 5
+    for _ in range(n):
+        scenes.karman_inflow(o)
+        o.Simulate(DT)
+    sec = (time.perf_counter() - t0) / n
+    rows["karman512x256_jacobi"]["cpu_baseline"] = {
+        "value": 512 * 256 / sec / 1e6, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
+        "sample": "%d steps after 2 warm-up steps (reference SOR, 100 iterations with the "
+                  "reference's early exit, other stages on %d threads)" % (n, threads)}
+    return rows
 
 
 def fwd_adjoint(fluid_gb300, args):
@@ -644,9 +847,10 @@ def app_rows(fluid_gb300):
     return rows
 
 
-def cpu_app_rows(threads):
+def cpu_app_rows(threads, warm=3, timed=3):
     """The CPU baseline of the app-side rows: the oracle's restatement of the
-    reference on the same inputs, one bounded sample each."""
+    reference on the same inputs, one bounded sample each (the step rows:
+    `warm` warm-up steps, as the GPU rows take, then `timed` steps)."""
     import numpy as np
     from oracle.pyoracle import LEXSOR, OracleFluid
 
@@ -657,13 +861,20 @@ def cpu_app_rows(threads):
         S = o.S.reshape(o.NumX, o.NumY)
         S[:] = 1.0
         S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
-        for i in range(2, o.NumX - 2):
-            o.SetVelocity(i, o.NumY - 2, 1.0, 0.0)
+        def step():
+            for i in range(2, o.NumX - 2):
+                o.SetVelocity(i, o.NumY - 2, 1.0, 0.0)
+            o.Simulate(DT)
+
+        for _ in range(warm):
+            step()
         t0 = time.perf_counter()
-        o.Simulate(DT)
-        sec = time.perf_counter() - t0
+        for _ in range(timed):
+            step()
+        sec = (time.perf_counter() - t0) / timed
         out[key] = {"value": MG_SIDE * MG_SIDE / sec / 1e6, "unit": "Mcell-steps/s",
-                    "cores": threads, "kind": "port", "sample": "1 step"}
+                    "cores": threads, "kind": "port",
+                    "sample": "%d steps after %d warm-up steps" % (timed, warm)}
     o = OracleFluid(1.0, APP_W, APP_H, 1.0, prec=32, threads=threads, scheme=LEXSOR, num_iters=40,
                     UseBFECC=True)
 
@@ -829,27 +1040,11 @@ def run_ours(args):
     launch_ms = statistics.median(spans)
     stage_ms = {k: round(statistics.median(v), 4) for k, v in stages.items()}
     n_cells = f.NumX * f.NumY
-    alg_bytes = JACOBI_BYTES_PER_CELL_SWEEP * TB * n_cells
-    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_hbm()
     tr = committed_traffic()
-    roofline = {
-        "kernel": "k_jacobi_flow (one cooperative launch per solve: 25 phases of 8 sweeps; "
-                  "figures per phase)",
-        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": achieved / peak, "peak_source": peak_kind + " MEASURED_PEAKS.json hbm_gbs"
-        if peak_kind == "measured" else "fallback 6.8 TB/s",
-        "bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
-        "traffic": tr.get("dram_bytes_per_launch_full") if tr else None,
-        "traffic_source": tr.get("source") if tr else None,
-        "model": "13 B per cell-sweep (phi r/w 8, rhs 4, mask 1), each of the phase's 8 sweeps "
-                 "counted; the sweeps run in registers, so this model exceeds the HBM peak",
-        # The compulsory traffic of a phase -- phi read and written, w and w*b
-        # read once (16 B per cell) -- over the same time.
-        "compulsory": {"bytes_per_launch": 16 * n_cells,
-                       "achieved": 16 * n_cells / (launch_ms / 1e3) / 1e9,
-                       "frac": 16 * n_cells / (launch_ms / 1e3) / 1e9 / peak},
-    }
+    clocks = sampler.summary()
+    roofline = jacobi_roofline(n_cells, launch_ms, peak, peak_kind, tr, clocks)
+    step_roof = step_roofline(stage_ms, n_cells, t_max / args.steps, peak)
 
     # ------------------------------------------------------------ e2e through the C ABI
     e2e = None
@@ -899,18 +1094,34 @@ def run_ours(args):
         stop_app()
 
     # ------------------------------------------------------------ CPU baseline
-    cpu = None
+    cpu = err64 = configs = ratios = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        times = cpu_reference_steps(args.cpu_steps, threads)
+        # The reference arm's protocol: W warm-up steps of the reference
+        # algorithm from the zero state (its step time grows as the flow
+        # develops), then timed steps on the same state.
+        warm = max(1, min(args.warmup, 10))
+        times = cpu_reference_steps(max(2, args.cpu_steps), threads, warmup=warm,
+                                    budget_s=args.cpu_budget)
         cpu = {"value": W * H * len(times) / sum(times) / 1e6, "unit": "Mcell-steps/s",
                "cores": threads, "kind": "port",
-               "sample": "%d full 2048x2048 step(s) of the reference algorithm (serial SOR "
-                         "pressure, FP32), stages on %d host threads" % (len(times), threads)}
+               "sample": "%d full 2048x2048 steps after %d warm-up step(s) of the reference "
+                         "algorithm (serial SOR pressure, FP32), other stages on %d host threads "
+                         "(the reference arm's protocol)" % (len(times), warm, threads)}
         if app is not None:
             for k, v in cpu_app_rows(threads).items():
                 app[k]["cpu_baseline"] = v
             app["reference_sor_2048"]["cpu_baseline"] = dict(cpu)
+        err64 = fp64_error(f)
+        if not args.no_configs:
+            configs = config_rows(fluid_gb300, threads)
+        ratios = {"jacobi_gpu_over_sor_cpu": value / cpu["value"],
+                  "note": "the line's value (Jacobi scheme) over cpu_baseline (the reference's "
+                          "serial SOR on the host): same workload, different pressure algorithm"}
+        if app is not None:
+            ratios["sor_gpu_over_sor_cpu"] = app["reference_sor_2048"]["value"] / cpu["value"]
+            ratios["note"] += ("; sor_gpu_over_sor_cpu: the reference's SOR bit for bit on the GPU "
+                               "(app_rows.reference_sor_2048) over the same cpu_baseline")
 
     if rank == 0:
         line = {
@@ -919,9 +1130,10 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": workload_config({"parallelism": "replicas%d" % world if world > 1 else "single"}),
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "roofline": roofline, "step_roofline": step_roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches, "error_vs_fp64": err64, "ratios": ratios,
             "fwd_adjoint": adj, "rollout_256": roll, "ensemble": ens, "app_rows": app,
-            "clocks": sampler.summary(),
+            "configs": configs, "clocks": clocks,
             "host_ms_per_step": 1e3 * t_host / args.steps,
             "stage_ms": stage_ms,
             "step_stats": {"div_l2_post": st["div_l2_post"], "resid_l2": st["resid_l2"],
@@ -938,7 +1150,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--cpu-steps", type=int, default=2,
+                    help="timed CPU steps of the line's cpu_baseline (at least 2)")
+    ap.add_argument("--cpu-budget", type=float, default=30.0,
+                    help="seconds of timed CPU steps for the line's cpu_baseline")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 128^2 jet and 512x256 Karman rows")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
