@@ -7,7 +7,8 @@ Workload (one "step" = one Simulate call): 2048x2048 interior cells, density
 (the app's cavity preset, without its smoke), BFECC advection on, the
 New() default turbulence 0.02, 200 Jacobi pressure sweeps per step run in
 temporal blocks of 8 sweeps per launch, FP64 residual reduction and one FP64
-outer correction of 8 sweeps, fixed sweep count (no early exit).  Fields are
+outer correction of 8 sweeps, fixed sweep count (no early exit), advection
+departure points formed relative to their face (precise_coords).  Fields are
 FP32; inputs are synthetic (zero initial state, seeded scene).
 
 Arms:
@@ -66,7 +67,8 @@ STAGE_BYTES_PER_CELL = {
 def workload_config(extra=None):
     cfg = {
         "workload": "lid-driven cavity 2048x2048, BFECC, turbulence 0.02, 200 Jacobi sweeps "
-                    "(temporal blocks of 8), FP64 residual + 8-sweep FP64 outer correction",
+                    "(temporal blocks of 8), FP64 residual + 8-sweep FP64 outer correction, "
+                    "face-relative departure points",
         "grid": [W, H],
         "dt": DT,
         "pressure_sweeps": ITERS,
@@ -184,7 +186,7 @@ def dist_setup():
 def build_cavity(fluid_gb300, auto_sync=False):
     f = fluid_gb300.Fluid(1.0, W, H, 1.0, auto_sync=auto_sync, scheme=fluid_gb300.SCHEME_JACOBI,
                           num_iters=ITERS, tb_depth=TB, refine_sweeps=REFINE, UseBFECC=True,
-                          early_exit=False)
+                          early_exit=False, precise_coords=True)
     S = f.S.reshape(f.NumX, f.NumY)
     S[:] = 1.0
     S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
@@ -292,7 +294,7 @@ def fp64_error(f):
 
     o = OracleFluid(1.0, W, H, 1.0, prec=64, threads=os.cpu_count() or 1, scheme=1,
                     num_iters=ITERS, check_every=TB, UseBFECC=True, early_exit=False,
-                    refine_sweeps=REFINE)
+                    refine_sweeps=REFINE, precise_coords=True)
     f.synchronize()
     f.download()
     for k in ("U", "V", "M", "newU", "newV", "newM", "S"):
@@ -405,19 +407,72 @@ def config_rows(fluid_gb300, threads):
     return rows
 
 
+def multigrid_leg(fluid_gb300, f, args):
+    """The headline cavity with the MULTIGRID pressure scheme (parallel
+    V(2,2) cycles) in place of the 200 Jacobi sweeps and the outer
+    correction: device-timed steps for 1 and 2 cycles from the main handle's
+    state, and, from one snapshot of that state, one step of each scheme
+    with its FP64-class pressure residual (resid_l2) and post-projection
+    divergence."""
+    import torch
+
+    f.synchronize()
+    f.download()
+    snap = {k: getattr(f, k).copy() for k in ("U", "V", "M", "newU", "newV", "newM")}
+
+    def load(h):
+        for k, v in snap.items():
+            getattr(h, k)[:] = v
+        h.mark_dirty()
+
+    out = {}
+    for cycles in (1, 2):
+        g = fluid_gb300.Fluid(1.0, W, H, 1.0, auto_sync=False, scheme=fluid_gb300.SCHEME_MULTIGRID,
+                              num_iters=cycles, UseBFECC=True, early_exit=False,
+                              precise_coords=True)
+        S = g.S.reshape(g.NumX, g.NumY)
+        S[:] = 1.0
+        S[:, 0] = S[:, -1] = S[0, :] = S[-1, :] = 0.0
+        load(g)
+        li, lj = lid_cells(g)
+        g.set_sources(li, lj, u=1.0, v=0.0, mode=g.SRC_SKIP_SOLID | g.SRC_SET_VELOCITY)
+        g.Simulate(DT)  # the step from the snapshot
+        st = g.stats()
+        stream = torch.cuda.ExternalStream(g.stream)
+        for _ in range(max(3, args.warmup)):
+            g.Simulate(DT)
+        l0 = g.launch_count()
+        ms = device_ms(stream, lambda: g.Simulate(DT), args.steps)
+        launches = (g.launch_count() - l0) / args.steps
+        out["cycles_%d" % cycles] = {
+            "value": W * H / ms / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms,
+            "launches_per_step": launches, "resid_l2": st["resid_l2"],
+            "div_l2_post": st["div_l2_post"]}
+        del g
+    load(f)
+    f.Simulate(DT)
+    st = f.stats()
+    out["jacobi_200_refined"] = {"resid_l2": st["resid_l2"], "div_l2_post": st["div_l2_post"]}
+    out["config"] = ("2048^2 cavity as the headline (BFECC, turbulence, face-relative departures), "
+                     "pressure by MULTIGRID: V(2,2) cycles, damped Jacobi (0.8), levels down to a "
+                     "side of 8; residuals compared on one step from the same snapshot against "
+                     "the headline's 200 sweeps + 8-sweep correction; device-timed steps")
+    return out
+
+
 def fwd_adjoint(fluid_gb300, args):
-    """Forward + adjoint rollout on the cavity (refine_sweeps 0, the recorded
-    rollouts' form): ROLL steps with a device-resident per-step force field,
-    checkpoint every 8 steps, loss ||M_T - target||_2, gradients w.r.t. the
-    initial state and every step's forces.  Returns per-step times of the
-    rollout (forward + recompute + adjoint) and of plain forward steps of the
-    same configuration, both device-timed with CUDA events."""
+    """Forward + adjoint rollout on the cavity with the headline step's
+    settings (outer correction and face-relative departure points included):
+    ROLL steps with a device-resident per-step force field, checkpoint every
+    8 steps, loss ||M_T - target||_2, gradients w.r.t. the initial state and
+    every step's forces.  Returns per-step times of the rollout (forward +
+    recompute + adjoint) and of plain forward steps of the same
+    configuration, both device-timed with CUDA events."""
     import numpy as np
     import torch
 
     roll, every = 16, 8
     f = build_cavity(fluid_gb300)
-    f.refine_sweeps = 0
     li, lj = lid_cells(f)
     f.set_sources(li, lj, u=1.0, v=0.0, smoke=1.0,
                   mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY | f.SRC_ADD_SMOKE)
@@ -455,7 +510,7 @@ def fwd_adjoint(fluid_gb300, args):
     e1 = torch.cuda.Event(enable_timing=True)
     rollout()
     f.synchronize()
-    reps = max(1, min(3, args.steps // 8))
+    reps = max(2, min(5, args.steps // 4))
     prof = profile_leg(args, "adjoint")
     e0.record(stream)
     for _ in range(reps):
@@ -476,11 +531,13 @@ def fwd_adjoint(fluid_gb300, args):
         "value": W * H / ms_roll / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms_roll,
         "fwd_ms_per_step": ms_fwd, "ratio_to_fwd": ms_roll / ms_fwd,
         "rollout_steps": roll, "checkpoint_every": every, "loss": loss,
-        "config": "cavity 2048x2048 as above with refine_sweeps 0 and +1 smoke on the lid row; "
-                  "per-step 2-channel force field on the device; one rollout = %d recorded "
-                  "steps + seed + %d adjoint steps (the first %d steps recomputed from their "
-                  "checkpoint); gradients w.r.t. the initial state and all forces"
-                  % (roll, roll, roll - every),
+        "config": "cavity 2048x2048 as above (outer correction included) with +1 smoke on "
+                  "the lid row; per-step 2-channel force field on the device; one rollout = %d "
+                  "recorded steps + seed + %d adjoint steps (the first %d steps recomputed "
+                  "from their checkpoint); gradients w.r.t. the initial state and all forces; "
+                  "%d rollouts timed" % (roll, roll, roll - every, reps),
+        "checks": "tests/test_gpu_adjoint.py: FP64 central differences of the oracle "
+                  "(with the outer correction: test_directional_derivative_with_outer_correction)",
         "fwd_launches_per_step": (f.launch_count() - l0) / roll,
     }
 
@@ -581,7 +638,10 @@ def rollout256(fluid_gb300, args):
         "value": side * side / ms / 1e3, "unit": "Mcell-steps/s fwd+adjoint",
         "ms_per_step": ms, "fwd_ms_per_step": ms_fwd, "ratio_to_fwd": ms / ms_fwd, "loss": loss,
         "fd_check": {"directions": 32, "eps": 1e-3, "reference": "FP32 forward central differences",
-                     "median_rel_err": float(np.median(rel)), "max_rel_err": float(np.max(rel))},
+                     "median_rel_err": float(np.median(rel)), "max_rel_err": float(np.max(rel)),
+                     "note": "FP32 differences at eps 1e-3 switch BFECC clamps; the pin is "
+                             "tests/test_gpu_adjoint.py::test_rollout256_vs_fp64_oracle_"
+                             "differences (FP64 central differences, within 1e-4 relative)"},
     }
 
 
@@ -1083,6 +1143,7 @@ def run_ours(args):
                        "fg_download_wait before the host reads it)"}
         del g
 
+    mgrow = multigrid_leg(fluid_gb300, f, args) if rank == 0 and not args.no_multigrid else None
     adj = fwd_adjoint(fluid_gb300, args) if rank == 0 and not args.no_adjoint else None
     roll = (rollout256(fluid_gb300, args)
             if rank == 0 and not (args.no_adjoint or args.no_rollout) else None)
@@ -1132,7 +1193,8 @@ def run_ours(args):
             "config": workload_config({"parallelism": "replicas%d" % world if world > 1 else "single"}),
             "roofline": roofline, "step_roofline": step_roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches, "error_vs_fp64": err64, "ratios": ratios,
-            "fwd_adjoint": adj, "rollout_256": roll, "ensemble": ens, "app_rows": app,
+            "multigrid": mgrow, "fwd_adjoint": adj, "rollout_256": roll, "ensemble": ens,
+            "app_rows": app,
             "configs": configs, "clocks": clocks,
             "host_ms_per_step": 1e3 * t_host / args.steps,
             "stage_ms": stage_ms,
@@ -1158,6 +1220,8 @@ def main():
                     help="skip the 128^2 jet and 512x256 Karman rows")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-multigrid", action="store_true",
+                    help="skip the MULTIGRID pressure-scheme rows")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-rollout", action="store_true")
     ap.add_argument("--no-app", action="store_true",

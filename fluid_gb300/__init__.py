@@ -6,8 +6,8 @@ Python mirror of the Go type ``fluid.Fluid`` over that ABI.
 """
 from . import fluid as _fluid_mod
 from ._build import build
-from .fluid import (ALL_FIELDS, FIELDS, SCHEME_JACOBI, SCHEME_LEXSOR, Batch, Fluid, FluidError,
-                    ScalarField, VectorField, debug_fail_alloc)
+from .fluid import (ALL_FIELDS, FIELDS, SCHEME_JACOBI, SCHEME_LEXSOR, SCHEME_MULTIGRID, Batch, Fluid,
+                    FluidError, ScalarField, VectorField, debug_fail_alloc)
 
 
 def __getattr__(name):
@@ -22,4 +22,5 @@ def set_relaxation(value: float) -> None:
 
 
 __all__ = ["Fluid", "Batch", "FluidError", "ScalarField", "VectorField", "build", "set_relaxation",
-           "FIELDS", "ALL_FIELDS", "SCHEME_LEXSOR", "SCHEME_JACOBI", "debug_fail_alloc"]
+           "FIELDS", "ALL_FIELDS", "SCHEME_LEXSOR", "SCHEME_JACOBI", "SCHEME_MULTIGRID",
+           "debug_fail_alloc"]

@@ -32,7 +32,7 @@ class Params(ctypes.Structure):
         ("multigrid_levels", _c_i), ("use_bfecc", _c_i), ("relaxation", _c_f),
         ("num_iters", _c_i), ("tolerance", _c_f), ("early_exit", _c_i), ("scheme", _c_i),
         ("jacobi_omega", _c_f), ("tb_depth", _c_i), ("refine_sweeps", _c_i),
-        ("use_graphs", _c_i), ("reserved", _c_i * 7),
+        ("use_graphs", _c_i), ("precise_coords", _c_i), ("reserved", _c_i * 6),
     ]
 
 
@@ -98,6 +98,7 @@ SIGNATURES = {
     "fg_edit_bytes": (ctypes.c_ulonglong, [_vp]),
     "fg_project_noalloc": (_c_i, [_vp, _vp, _vp, _vp, _c_i, _c_i, _c_i, _c_f, _c_f, _c_f, _c_i,
                                   _c_f, _c_f, _c_i, _c_i, _c_f, _vp]),
+    "fg_project_noalloc_status": (_c_i, [_vp]),
     "fg_debug_fail_alloc": (_c_i, [_c_i]),
     "fg_debug_stall_tile": (_c_i, [_vp, _c_i]),
     "fg_tape_begin": (_c_i, [_vp, _c_i, _c_i]),

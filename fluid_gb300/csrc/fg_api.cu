@@ -12,6 +12,7 @@
 namespace fg {
 size_t pctl_bytes(int n_slots);
 int jacobi_launches(const fg_fluid* f, int iters);
+void set_noalloc_stall(int tile);
 }  // namespace fg
 
 using namespace fg;
@@ -213,6 +214,7 @@ int flush(fg_fluid* f) {
   }
   if (f->masks_stale) {
     CK(f, launch_build_flags(f), "build flags");
+    if (f->mg) CK(f, launch_mg_rebuild(f), "multigrid levels");
     f->masks_stale = false;
   }
   return FG_OK;
@@ -238,8 +240,11 @@ void edit(fg_fluid* f, int field, int cell, int op, float value) {
 
 int check_params(fg_fluid* f, const fg_params* p) {
   if (p->num_iters < 0) return fail(f, FG_ERR_INVALID, "num_iters < 0");
-  if (p->scheme != FG_SCHEME_LEXSOR && p->scheme != FG_SCHEME_JACOBI)
+  if (p->scheme != FG_SCHEME_LEXSOR && p->scheme != FG_SCHEME_JACOBI &&
+      p->scheme != FG_SCHEME_MULTIGRID)
     return fail(f, FG_ERR_INVALID, "unknown pressure scheme");
+  if (p->scheme == FG_SCHEME_MULTIGRID && p->refine_sweeps > 0)
+    return fail(f, FG_ERR_UNSUPPORTED, "MULTIGRID takes no outer correction (refine_sweeps 0)");
   if (p->refine_sweeps < 0) return fail(f, FG_ERR_INVALID, "refine_sweeps < 0");
   return FG_OK;
 }
@@ -252,12 +257,17 @@ void clear_graphs(fg_fluid* f) {
 int check_iters(fg_fluid* f, int iters) {
   if (iters < 0) return fail(f, FG_ERR_INVALID, "num_iters < 0");
   if (f->prm.scheme == FG_SCHEME_JACOBI) {
-    int need = std::max(jacobi_launches(f, iters), jacobi_launches(f, f->prm.refine_sweeps)) + 1;
+    // In 64 bits; a count whose control block would pass 2^24 launch slots
+    // (64 MiB) is refused rather than allowed to wrap.
+    const long long need =
+        (long long)std::max(jacobi_launches(f, iters), jacobi_launches(f, f->prm.refine_sweeps)) +
+        1;
+    if (need > (1ll << 24)) return fail(f, FG_ERR_INVALID, "num_iters: too many Jacobi launches");
     if (need > f->n_slots) {
       CK(f, cudaStreamSynchronize(f->stream), "sync");
       cudaFree(f->pctl);
       cudaFree(f->ectl);
-      f->n_slots = need * 2;
+      f->n_slots = (int)need * 2;
       CK(f, dev_malloc(&f->pctl, pctl_bytes(f->n_slots)), "pctl alloc");
       CK(f, dev_malloc(&f->ectl, pctl_bytes(f->n_slots)), "pctl alloc");
       CK(f, cudaMemsetAsync(f->pctl, 0, pctl_bytes(f->n_slots), f->stream), "pctl");
@@ -299,7 +309,8 @@ int enqueue_step(fg_fluid* f, float dt) {
   if (p.viscosity_diffusion > 0.0f) CK(f, launch_viscosity(f, dt), "viscosity");
   mark(f, "sources+viscosity");
   const bool conf = p.confinement != 0.0f, turb = p.turbulence_strength > 0.0f;
-  const bool fuse_turb = p.scheme == FG_SCHEME_JACOBI && !multigrid(f) && !conf && turb;
+  const bool fuse_turb = (p.scheme == FG_SCHEME_JACOBI || p.scheme == FG_SCHEME_MULTIGRID) &&
+                         !multigrid(f) && !conf && turb;
   int rc = enqueue_pressure(f, p.num_iters, dt, fuse_turb);
   if (rc) return rc;
   mark(f, "gradient+div stats");
@@ -380,6 +391,7 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
   f->density = density;
   f->h = h;
   f->g = make_grid(f->NX, f->NY, f->P, h);
+  f->g.precise = f->prm.precise_coords ? 1 : 0;
   int rc = FG_OK;
   auto bail = [&](int code) {
     fg_destroy(f);
@@ -451,6 +463,7 @@ int fg_destroy(fg_fluid* f) {
   clear_graphs(f);
   tape_free(f);
   batch_free(f->batch);
+  mg_free(f);
   for (int k = 0; k < fg_fluid::A_COUNT; ++k) cudaFree(f->adj[k]);
   for (int b = 0; b < 2; ++b) {
     for (int q = 0; q < 4; ++q) cudaFree(f->parts.a[b][q]);
@@ -525,6 +538,7 @@ int fg_set_params(fg_fluid* f, const fg_params* p) {
   if (rc) return rc;
   if (memcmp(&f->prm, p, sizeof *p) != 0) {
     f->prm = *p;
+    f->g.precise = p->precise_coords ? 1 : 0;
     f->params_version++;
   }
   return FG_OK;
@@ -646,12 +660,79 @@ void ensure_skew(fg_fluid* f) {
   f->params_version++;  // captured steps run the other kernel sequence
 }
 
+// Allocates the MULTIGRID scheme's levels below the handle's grid (interior
+// sides halved until the shorter is at most kMgMinSide) and builds their
+// masks, flags and weights; called outside stream capture before a solve.
+// Rebuilds the coarse weights when PressureDamping changed since.
+static int mg_prepare(fg_fluid* f) {
+  if (f->prm.scheme != FG_SCHEME_MULTIGRID || f->batch) return FG_OK;
+  if (f->mg) {
+    if (f->mg->omega != kMgOmega * f->prm.pressure_damping) {
+      CK(f, launch_mg_rebuild(f), "multigrid levels");
+      f->params_version++;
+    }
+    return FG_OK;
+  }
+  if (std::min(f->NX, f->NY) - 2 <= kMgMinSide)
+    return fail(f, FG_ERR_UNSUPPORTED, "MULTIGRID needs an interior side above 8 cells");
+  MgHier* h = new MgHier();
+  MgLevelDev l0;
+  l0.g = f->g;
+  l0.S = f->d[FG_S];
+  l0.flags = f->flags;
+  l0.w = f->wgt;
+  l0.b = f->rhs;
+  l0.bw = f->bw;
+  l0.x[0] = f->phi;
+  l0.x[1] = f->phi2;
+  h->lv.push_back(l0);
+  std::vector<size_t> off;
+  size_t total = 0;
+  int nx = f->NX, ny = f->NY;
+  while (std::min(nx, ny) - 2 > kMgMinSide) {
+    nx = (nx - 2 + 1) / 2 + 2;
+    ny = (ny - 2 + 1) / 2 + 2;
+    MgLevelDev c;
+    c.g = make_grid(nx, ny, (ny + 31) / 32 * 32, f->h);
+    h->lv.push_back(c);
+    off.push_back(total);
+    total += (6 * sizeof(float) + 1) * (size_t)nx * c.g.P;
+    total = (total + 255) / 256 * 256;
+  }
+  if (dev_malloc(&h->block, total) != cudaSuccess || dev_malloc(&h->ctl, 64) != cudaSuccess) {
+    cudaFree(h->block);
+    delete h;
+    return fail(f, FG_ERR_NOMEM, "multigrid levels");
+  }
+  for (size_t l = 1; l < h->lv.size(); ++l) {
+    MgLevelDev& c = h->lv[l];
+    const size_t cells = (size_t)c.g.NX * c.g.P;
+    float* base = reinterpret_cast<float*>(static_cast<unsigned char*>(h->block) + off[l - 1]);
+    c.S = base;
+    c.w = base + cells;
+    c.b = base + 2 * cells;
+    c.bw = base + 3 * cells;
+    c.x[0] = base + 4 * cells;
+    c.x[1] = base + 5 * cells;
+    c.flags = reinterpret_cast<uint8_t*>(base + 6 * cells);
+  }
+  f->mg = h;
+  // Zeroed once: the padding columns and the ghost rings are never written
+  // and must read as 0.
+  CK(f, cudaMemsetAsync(h->block, 0, total, f->stream), "multigrid levels");
+  CK(f, cudaMemsetAsync(h->ctl, 0, 64, f->stream), "multigrid levels");
+  CK(f, launch_mg_rebuild(f), "multigrid levels");
+  f->params_version++;
+  return FG_OK;
+}
+
 int fg_simulate(fg_fluid* f, float dt) {
   if (!f) return FG_ERR_INVALID;
   int rc = flush(f);
   if (rc) return rc;
   ensure_skew(f);
   if ((rc = check_iters(f, f->prm.num_iters))) return rc;
+  if ((rc = mg_prepare(f))) return rc;
   invalidate(f, kStepFields);
   // Profiling brackets the Jacobi launches with timed events, which plain
   // capture would turn into graph-internal dependencies: run it uncaptured.
@@ -749,6 +830,7 @@ int fg_make_incompressible(fg_fluid* f, int num_iters, float dt) {
   STAGE_PROLOGUE(f);
   ensure_skew(f);
   if ((rc = check_iters(f, num_iters))) return rc;
+  if ((rc = mg_prepare(f))) return rc;
   invalidate(f, kStepFields);
   CK(f, launch_clear_stats(f), "clear stats");
   // copyBorder(newU, U), copyBorder(newV, V) (fluid.go:145-146).
@@ -1256,8 +1338,6 @@ int tape_supported(fg_fluid* f) {
     return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts need the parallel (Jacobi) scheme");
   if (p.early_exit)
     return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts need a fixed sweep count (early_exit 0)");
-  if (p.refine_sweeps > 0)
-    return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support refine_sweeps");
   if (p.viscosity_diffusion > 0.0f)
     return fail(f, FG_ERR_UNSUPPORTED, "recorded rollouts do not support viscosity");
   if (p.use_multigrid && p.multigrid_levels > 1)
@@ -2367,7 +2447,10 @@ int fg_debug_fail_alloc(int n) {
 }
 
 int fg_debug_stall_tile(fg_fluid* f, int tile) {
-  if (!f) return FG_ERR_INVALID;
+  if (!f) {  // the allocation-free projection's TMA-fed Jacobi launches
+    set_noalloc_stall(tile);
+    return FG_OK;
+  }
   if (is_batch(f)) return batch_unsupported(f);
   int rc = flush(f);
   if (rc) return rc;

@@ -43,6 +43,7 @@ struct Grid {
   float h1;        // float32(1.0 / h)           fluid.go:360
   float hh;        // 0.5 * h  (== h / 2)        fluid.go:298, 361, 406
   float NXh, NYh;  // float32(NumX) * h, float32(NumY) * h   fluid.go:363-364
+  int precise;     // departure points relative to their face (fg_params.precise_coords)
 };
 
 inline Grid make_grid(int NX, int NY, int P, float h) {
@@ -55,6 +56,7 @@ inline Grid make_grid(int NX, int NY, int P, float h) {
   g.hh = 0.5f * h;
   g.NXh = (float)NX * h;
   g.NYh = (float)NY * h;
+  g.precise = 0;
   return g;
 }
 
@@ -74,28 +76,108 @@ __device__ __forceinline__ float go_max(float a, float b) {
 }
 __device__ __forceinline__ float fbit(uint8_t f, uint8_t bit) { return (f & bit) ? 1.0f : 0.0f; }
 
-// sampleField / sampleFieldFrom (fluid.go:357-398, 1055-1091).  dx, dy are
-// the staggering offsets of the sampled field (U: 0,h/2; V: h/2,0; M: h/2,h/2).
-// The clamp of the coordinates uses fminf/fmaxf: for any non-NaN coordinate
-// they equal Go's min/max here (the bounds are positive, so no signed-zero
-// ties); a NaN coordinate, where the reference's int conversion of the floor
-// gives an out-of-range index and panics, clamps to the upper bound.
+// The bilinear stencil of one sample: corner indices, weights and whether
+// each coordinate lies inside the clamp range.
+struct Bilin {
+  int x0, x1, y0, y1;
+  float tx, ty;
+  bool inx, iny;
+};
+
+// sampleField / sampleFieldFrom (fluid.go:357-398, 1055-1091) at the
+// absolute point (x, y).  dx, dy are the staggering offsets of the sampled
+// field (U: 0,h/2; V: h/2,0; M: h/2,h/2).  The clamp of the coordinates uses
+// fminf/fmaxf: for any non-NaN coordinate they equal Go's min/max here (the
+// bounds are positive, so no signed-zero ties); a NaN coordinate, where the
+// reference's int conversion of the floor gives an out-of-range index and
+// panics, clamps to the upper bound.
+__device__ __forceinline__ Bilin bilin_abs(float x, float y, float dx, float dy, const Grid& g) {
+  Bilin s;
+  float xc = fmaxf(fminf(x, g.NXh), g.h);
+  float yc = fmaxf(fminf(y, g.NYh), g.h);
+  s.inx = xc == x;
+  s.iny = yc == y;
+  float xs = xc - dx;
+  float ys = yc - dy;
+  s.x0 = min((int)floorf(xs * g.h1), g.NX - 1);
+  s.tx = (xs - (float)s.x0 * g.h) * g.h1;
+  s.x1 = min(s.x0 + 1, g.NX - 1);
+  s.y0 = min((int)floorf(ys * g.h1), g.NY - 1);
+  s.ty = (ys - (float)s.y0 * g.h) * g.h1;
+  s.y1 = min(s.y0 + 1, g.NY - 1);
+  return s;
+}
+
+// The same stencil for a point given relative to index (i, j): its sample
+// coordinates in cells are (i + a, j + b), on a field staggered by (dxr,
+// dyr) cells (0 or 0.5).  Absolute float coordinates near index 2048 are
+// resolved to 2^-12 cells only, which shifts the weights by up to ~1e-4;
+// here the integer part is exact and the weights keep float precision of
+// the displacement.  The clamp to [h, NumX h] (fluid.go:363-364) becomes
+// a in [1 - dxr - i, NumX - dxr - i].
+__device__ __forceinline__ Bilin bilin_local(int i, int j, float a, float b, float dxr, float dyr,
+                                             const Grid& g) {
+  Bilin s;
+  float ac = fmaxf(fminf(a, (float)(g.NX - i) - dxr), (float)(1 - i) - dxr);
+  float bc = fmaxf(fminf(b, (float)(g.NY - j) - dyr), (float)(1 - j) - dyr);
+  s.inx = ac == a;
+  s.iny = bc == b;
+  float fa = floorf(ac), fb = floorf(bc);
+  s.x0 = i + (int)fa;
+  s.tx = ac - fa;
+  if (s.x0 > g.NX - 1) {
+    s.x0 = g.NX - 1;
+    s.tx = ac - (float)(s.x0 - i);
+  }
+  s.y0 = j + (int)fb;
+  s.ty = bc - fb;
+  if (s.y0 > g.NY - 1) {
+    s.y0 = g.NY - 1;
+    s.ty = bc - (float)(s.y0 - j);
+  }
+  s.x1 = min(s.x0 + 1, g.NX - 1);
+  s.y1 = min(s.y0 + 1, g.NY - 1);
+  return s;
+}
+
+// Stencil at the departure point of face / cell (i, j): the point
+// (i h + ox, j h + oy), ox and oy 0 or h/2 (hx, hy), moved by (-su, -sv)
+// (su, sv: the products sdt * u, sdt * v), on a field staggered by the same
+// half cells.  Without g.precise the coordinates are formed as the reference
+// forms them (fluid.go:304-330, 411-414, 940-960).
+__device__ __forceinline__ Bilin bilin_dep(int i, int j, float su, float sv, bool hx, bool hy,
+                                           const Grid& g) {
+  if (g.precise)
+    return bilin_local(i, j, -su * g.h1, -sv * g.h1, hx ? 0.5f : 0.0f, hy ? 0.5f : 0.0f, g);
+  float x = hx ? ((float)i * g.h + g.hh) - su : (float)i * g.h - su;
+  float y = hy ? ((float)j * g.h + g.hh) - sv : (float)j * g.h - sv;
+  return bilin_abs(x, y, hx ? g.hh : 0.0f, hy ? g.hh : 0.0f, g);
+}
+
+// The bilinear value over a stencil; d(i, j) reads the field.
+template <typename A>
+__device__ __forceinline__ float bilin_sample(const A& d, const Bilin& s) {
+  float sx = 1.0f - s.tx;
+  float sy = 1.0f - s.ty;
+  return sx * sy * d(s.x0, s.y0) + s.tx * sy * d(s.x1, s.y0) + s.tx * s.ty * d(s.x1, s.y1) +
+         sx * s.ty * d(s.x0, s.y1);
+}
+
+// A field in global memory with pitch P.
+struct PtrAcc {
+  const float* __restrict__ p;
+  int P;
+  __device__ __forceinline__ float operator()(int i, int j) const { return p[i * P + j]; }
+};
+
 __device__ __forceinline__ float sample_field(const float* __restrict__ d, float x, float y,
                                               float dx, float dy, const Grid& g) {
-  x = fmaxf(fminf(x, g.NXh), g.h);
-  y = fmaxf(fminf(y, g.NYh), g.h);
-  float xs = x - dx;
-  float ys = y - dy;
-  int x0 = min((int)floorf(xs * g.h1), g.NX - 1);
-  float tx = (xs - (float)x0 * g.h) * g.h1;
-  int x1 = min(x0 + 1, g.NX - 1);
-  int y0 = min((int)floorf(ys * g.h1), g.NY - 1);
-  float ty = (ys - (float)y0 * g.h) * g.h1;
-  int y1 = min(y0 + 1, g.NY - 1);
-  float sx = 1.0f - tx;
-  float sy = 1.0f - ty;
-  return sx * sy * d[x0 * g.P + y0] + tx * sy * d[x1 * g.P + y0] + tx * ty * d[x1 * g.P + y1] +
-         sx * ty * d[x0 * g.P + y1];
+  return bilin_sample(PtrAcc{d, g.P}, bilin_abs(x, y, dx, dy, g));
+}
+// Sample of d at the departure point of face / cell (i, j) (bilin_dep).
+__device__ __forceinline__ float sample_dep(const float* __restrict__ d, int i, int j, float su,
+                                            float sv, bool hx, bool hy, const Grid& g) {
+  return bilin_sample(PtrAcc{d, g.P}, bilin_dep(i, j, su, sv, hx, hy, g));
 }
 #endif
 
@@ -158,6 +240,28 @@ struct BatchGeom {
   double* losses = nullptr;  // device: per-scene loss of the last seed, then n floats 1 / L
 };
 
+// One level of the MULTIGRID scheme's hierarchy (k_pressure.cu).  Level 0
+// names the handle's own solver arrays; the coarser levels own theirs.
+struct MgLevelDev {
+  Grid g;
+  float* S = nullptr;        // fluid mask (1 = fluid)
+  uint8_t* flags = nullptr;  // flag bytes built from S
+  float* w = nullptr;        // smoothing weight / s on active cells
+  float* b = nullptr;        // right-hand side
+  float* bw = nullptr;       // w * b
+  float* x[2] = {nullptr, nullptr};  // iterate (ping-pong)
+};
+// The MULTIGRID scheme's smoothing weight (times PressureDamping) and the
+// interior side below which it stops coarsening.
+constexpr float kMgOmega = 0.8f;
+constexpr int kMgMinSide = 8;
+struct MgHier {
+  std::vector<MgLevelDev> lv;
+  void* block = nullptr;  // one allocation holding the coarse levels' arrays
+  void* ctl = nullptr;    // control block of the smoothing launches
+  float omega = -1.0f;    // smoothing weight the coarse weights hold
+};
+
 }  // namespace fg
 
 struct fg_fluid {
@@ -175,6 +279,8 @@ struct fg_fluid {
   // Scratch.
   float *fwdU = nullptr, *fwdV = nullptr, *fwdM = nullptr;
   float *corrU = nullptr, *corrV = nullptr, *corrM = nullptr;
+  // Coarse levels of the MULTIGRID scheme (allocated on its first step).
+  fg::MgHier* mg = nullptr;
   float *phi = nullptr, *phi2 = nullptr, *rhs = nullptr;
   float *err = nullptr, *err2 = nullptr, *rhs_e = nullptr;
   float *wgt = nullptr, *bw = nullptr, *bwe = nullptr;  // Jacobi w = om/s, w*b, w*b_e
@@ -287,6 +393,7 @@ namespace fg {
 // f->stream and return cudaGetLastError().
 // k_forces.cu
 cudaError_t launch_build_flags(fg_fluid* f);
+cudaError_t launch_build_flags_on(cudaStream_t st, const float* S, uint8_t* flags, const Grid& g);
 cudaError_t launch_apply_edits(fg_fluid* f, int n_groups, int slot);
 cudaError_t launch_apply_sources(fg_fluid* f);
 cudaError_t launch_viscosity(fg_fluid* f, float dt);  // U,V -> partner, newU/newV = result; swaps
@@ -303,6 +410,10 @@ cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt);
 // Pressure solve + gradient subtract + post-projection divergence statistics;
 // with fuse_turb (parallel scheme only) also addTurbulence.
 cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb);
+// The MULTIGRID scheme's levels: masks, flags and weights rebuilt from the
+// fine flags (the allocation is fg_api.cu's, outside stream capture).
+cudaError_t launch_mg_rebuild(fg_fluid* f);
+void mg_free(fg_fluid* f);
 // solveMultigridVCycle (fluid.go:559-594) with the reference's serial
 // smoothers, bit for bit.
 cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt);

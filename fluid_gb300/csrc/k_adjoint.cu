@@ -71,18 +71,11 @@ __global__ void k_add_forces(float* __restrict__ U, float* __restrict__ V,
 // Adjoint of a bilinear sample of field F at (x, y) (sampleField): scatters
 // lam * weights into dF and returns d value / d x, d value / d y (0 along a
 // clamped coordinate).
-__device__ __forceinline__ void sample_adjoint(const float* __restrict__ F, float* dF, float x,
-                                               float y, float dx, float dy, float lam,
-                                               const Grid& g, float* dvdx, float* dvdy) {
-  float xc = fmaxf(fminf(x, g.NXh), g.h);
-  float yc = fmaxf(fminf(y, g.NYh), g.h);
-  float xs = xc - dx, ys = yc - dy;
-  int x0 = min((int)floorf(xs * g.h1), g.NX - 1);
-  float tx = (xs - (float)x0 * g.h) * g.h1;
-  int x1 = min(x0 + 1, g.NX - 1);
-  int y0 = min((int)floorf(ys * g.h1), g.NY - 1);
-  float ty = (ys - (float)y0 * g.h) * g.h1;
-  int y1 = min(y0 + 1, g.NY - 1);
+__device__ __forceinline__ void sample_adjoint(const float* __restrict__ F, float* dF,
+                                               const Bilin& s, float lam, const Grid& g,
+                                               float* dvdx, float* dvdy) {
+  const int x0 = s.x0, x1 = s.x1, y0 = s.y0, y1 = s.y1;
+  const float tx = s.tx, ty = s.ty;
   float sx = 1.0f - tx, sy = 1.0f - ty;
   const int P = g.P;
   float f00 = F[x0 * P + y0], f10 = F[x1 * P + y0], f11 = F[x1 * P + y1], f01 = F[x0 * P + y1];
@@ -92,8 +85,8 @@ __device__ __forceinline__ void sample_adjoint(const float* __restrict__ F, floa
     atomicAdd(&dF[x1 * P + y1], tx * ty * lam);
     atomicAdd(&dF[x0 * P + y1], sx * ty * lam);
   }
-  *dvdx = xc == x ? g.h1 * (sy * (f10 - f00) + ty * (f11 - f01)) : 0.0f;
-  *dvdy = yc == y ? g.h1 * (sx * (f01 - f00) + tx * (f11 - f10)) : 0.0f;
+  *dvdx = s.inx ? g.h1 * (sy * (f10 - f00) + ty * (f11 - f01)) : 0.0f;
+  *dvdy = s.iny ? g.h1 * (sx * (f01 - f00) + tx * (f11 - f10)) : 0.0f;
 }
 
 // Adjoint of a semi-Lagrangian velocity pass (advectVelocity fluid.go:291-333
@@ -117,13 +110,10 @@ __device__ __forceinline__ void adj_sl_velocity_cell(int i, int j, const float* 
   bool ring = on_ring(i, j, g);
   float lu = lamU[c], lv = lamV[c];
   if (u_advected(fl, i, j, g)) {
-    float x = (float)i * g.h, y = (float)j * g.h + g.hh;
     float u = Ut[c];
     float v = (Vt[c - P] + Vt[c] + Vt[c - P + 1] + Vt[c + 1]) * 0.25f;
-    x = x - sdt * u;
-    y = y - sdt * v;
     float gx, gy;
-    sample_adjoint(Fu, dFu, x, y, 0.0f, g.hh, lu, g, &gx, &gy);
+    sample_adjoint(Fu, dFu, bilin_dep(i, j, sdt * u, sdt * v, false, true, g), lu, g, &gx, &gy);
     float du = -sdt * gx * lu, dv = -sdt * gy * lu;
     if (du != 0.0f) atomicAdd(&dUt[c], du);
     if (dv != 0.0f) {
@@ -139,13 +129,10 @@ __device__ __forceinline__ void adj_sl_velocity_cell(int i, int j, const float* 
     dNu[c] += lu;
   }
   if (v_advected(fl, i, j, g)) {
-    float x = (float)i * g.h + g.hh, y = (float)j * g.h;
     float u = (Ut[c - 1] + Ut[c] + Ut[c + P - 1] + Ut[c + P]) * 0.25f;
     float v = Vt[c];
-    x = x - sdt * u;
-    y = y - sdt * v;
     float gx, gy;
-    sample_adjoint(Fv, dFv, x, y, g.hh, 0.0f, lv, g, &gx, &gy);
+    sample_adjoint(Fv, dFv, bilin_dep(i, j, sdt * u, sdt * v, true, false, g), lv, g, &gx, &gy);
     float du = -sdt * gx * lv, dv = -sdt * gy * lv;
     if (dv != 0.0f) atomicAdd(&dVt[c], dv);
     if (du != 0.0f) {
@@ -230,23 +217,20 @@ __device__ __forceinline__ void adj_bfecc_vel_cell(int i, int j, const float* __
     float* dO = comp == 0 ? dOu : dOv;
     float lam = comp == 0 ? lu : lv;
     bool adv = comp == 0 ? u_advected(fl, i, j, g) : v_advected(fl, i, j, g);
-    float x = 0.0f, y = 0.0f, dx = 0.0f, dy = 0.0f, b = 0.0f;
+    float b = 0.0f;
+    Bilin st{};
     if (adv) {
       // The reverse trace of trace_sample_u / _v with sdt = -dt.
       if (comp == 0) {
         float u = Ou[c];
         float v = (Ov[c - P] + Ov[c] + Ov[c - P + 1] + Ov[c + 1]) * 0.25f;
-        x = (float)i * g.h + dt * u;
-        y = ((float)j * g.h + g.hh) + dt * v;
-        dy = g.hh;
+        st = bilin_dep(i, j, -dt * u, -dt * v, false, true, g);
       } else {
         float u = (Ou[c - 1] + Ou[c] + Ou[c + P - 1] + Ou[c + P]) * 0.25f;
         float v = Ov[c];
-        x = ((float)i * g.h + g.hh) + dt * u;
-        y = (float)j * g.h + dt * v;
-        dx = g.hh;
+        st = bilin_dep(i, j, -dt * u, -dt * v, true, false, g);
       }
-      b = sample_field(F, x, y, dx, dy, g);
+      b = bilin_sample(PtrAcc{F, P}, st);
     }
     float o = O[c];
     float raw = o - (b - o) * 0.5f;
@@ -260,7 +244,7 @@ __device__ __forceinline__ void adj_bfecc_vel_cell(int i, int j, const float* __
     if (!adv) continue;
     float lb = -0.5f * lam;  // adjoint of bwd
     float gx, gy;
-    sample_adjoint(F, comp == 0 ? dFu : dFv, x, y, dx, dy, lb, g, &gx, &gy);
+    sample_adjoint(F, comp == 0 ? dFu : dFv, st, lb, g, &gx, &gy);
     float du = dt * gx * lb, dv = dt * gy * lb;
     if (comp == 0) {
       if (du != 0.0f) atomicAdd(&dOu[c], du);
@@ -315,14 +299,13 @@ __device__ __forceinline__ void adj_sl_smoke_cell(int i, int j, const float* __r
   if (advected) {
     float u = (U[c] + U[c + P]) * 0.5f * smokeAdv;
     float v = (V[c] + V[c + 1]) * 0.5f * smokeAdv;
-    float x = (float)i * g.h + g.hh - sdt * u;
-    float y = (float)j * g.h + g.hh - sdt * v;
+    const Bilin st = bilin_dep(i, j, sdt * u, sdt * v, true, true, g);
     if (!bwd) {
-      float s = sample_field(Ms, x, y, g.hh, g.hh, g);
+      float s = bilin_sample(PtrAcc{Ms, P}, st);
       if (!(s >= 0.0f)) lam = 0.0f;  // max(s, 0) clamped
     }
     float gx, gy;
-    sample_adjoint(Ms, dMs, x, y, g.hh, g.hh, lam, g, &gx, &gy);
+    sample_adjoint(Ms, dMs, st, lam, g, &gx, &gy);
     float du = -sdt * gx * lam * 0.5f * smokeAdv, dv = -sdt * gy * lam * 0.5f * smokeAdv;
     if (du != 0.0f) {
       atomicAdd(&dU[c], du);
@@ -373,13 +356,13 @@ __device__ __forceinline__ void adj_bfecc_smoke_cell(int i, int j, const float* 
   }
   uint8_t fl = flags[c];
   bool adv = (fl & F_FLUID) != 0;
-  float b = 0.0f, x = 0.0f, y = 0.0f;
+  float b = 0.0f;
+  Bilin st{};
   if (adv) {
     float u = (U[c] + U[c + P]) * 0.5f * smokeAdv;
     float v = (V[c] + V[c + 1]) * 0.5f * smokeAdv;
-    x = (float)i * g.h + g.hh + dt * u;
-    y = (float)j * g.h + g.hh + dt * v;
-    b = sample_field(Fm, x, y, g.hh, g.hh, g);
+    st = bilin_dep(i, j, -dt * u, -dt * v, true, true, g);
+    b = bilin_sample(PtrAcc{Fm, P}, st);
   }
   float o = Mo[c];
   float raw = o - (b - o) * 0.5f;
@@ -394,7 +377,7 @@ __device__ __forceinline__ void adj_bfecc_smoke_cell(int i, int j, const float* 
   if (!adv) return;
   float lb = -0.5f * lam;
   float gx, gy;
-  sample_adjoint(Fm, dF, x, y, g.hh, g.hh, lb, g, &gx, &gy);
+  sample_adjoint(Fm, dF, st, lb, g, &gx, &gy);
   float du = dt * gx * lb * 0.5f * smokeAdv, dv = dt * gy * lb * 0.5f * smokeAdv;
   if (du != 0.0f) {
     atomicAdd(&dU[c], du);
@@ -690,35 +673,74 @@ __global__ void k_adj_grad_t(const float* __restrict__ dU, const float* __restri
   adj_grad_t_cell(i, j, dU, dV, W, rhs, BW, flags, g);
 }
 
+// The adjoint of the outer correction's right-hand side: r = lam - A e on
+// active cells (e: the correction solve run on lam), the exact residual
+// rounded once as resid_ff forms it, and w * r for the main solve that
+// follows.  e is exactly 0 off the active cells.
+__device__ __forceinline__ void adj_resid_cell(int i, int j, const float* __restrict__ lam,
+                                               const float* __restrict__ e0,
+                                               const float* __restrict__ e1,
+                                               const void* __restrict__ esel,
+                                               const float* __restrict__ W,
+                                               float* __restrict__ rhs, float* __restrict__ BW,
+                                               const uint8_t* __restrict__ flags, const Grid& g) {
+  const int P = g.P;
+  int c = i * P + j;
+  uint8_t fl = flags[c];
+  float r = 0.0f;
+  if (flag_active(fl)) {
+    const float* e = (*(const int*)esel) ? e1 : e0;
+    r = resid_ff(lam[c], e[c - P], e[c + P], e[c - 1], e[c + 1], (float)flag_count(fl), e[c]).hi;
+  }
+  rhs[c] = r;
+  BW[c] = W[c] * r;
+}
+__global__ void k_adj_resid(const float* __restrict__ lam, const float* __restrict__ e0,
+                            const float* __restrict__ e1, const void* __restrict__ esel,
+                            const float* __restrict__ W, float* __restrict__ rhs,
+                            float* __restrict__ BW, const uint8_t* __restrict__ flags, Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  adj_resid_cell(i, j, lam, e0, e1, esel, W, rhs, BW, flags, g);
+}
+
 // div^T: with b = -div on active cells, d(face) += db(cell on its high side)
-// - db(cell on its low side), db = the adjoint solve's result (0 off active).
+// - db(cell on its low side), db = the adjoint solve's result (0 off active)
+// plus, with the outer correction, the correction solve's (e0/e1, else null).
 __device__ __forceinline__ void adj_div_t_cell(int i, int j, float* __restrict__ dU,
                                                float* __restrict__ dV, const float* __restrict__ x0,
                                                const float* __restrict__ x1,
                                                const void* __restrict__ ctl_sel,
+                                               const float* __restrict__ e0,
+                                               const float* __restrict__ e1,
+                                               const void* __restrict__ esel,
                                                const uint8_t* __restrict__ flags, const Grid& g) {
   const int P = g.P;
   const float* db = (*(const int*)ctl_sel) ? x1 : x0;
+  const float* de = e0 ? ((*(const int*)esel) ? e1 : e0) : nullptr;
   int c = i * P + j;
+  auto val = [&](int k) { return de ? db[k] + de[k] : db[k]; };
   bool act = flag_active(flags[c]);
-  float bc = act ? db[c] : 0.0f;
+  float bc = act ? val(c) : 0.0f;
   if (i >= 1) {
-    float bl = flag_active(flags[c - P]) ? db[c - P] : 0.0f;
+    float bl = flag_active(flags[c - P]) ? val(c - P) : 0.0f;
     dU[c] = dU[c] + (bc - bl);
   }
   if (j >= 1) {
-    float bb = flag_active(flags[c - 1]) ? db[c - 1] : 0.0f;
+    float bb = flag_active(flags[c - 1]) ? val(c - 1) : 0.0f;
     dV[c] = dV[c] + (bc - bb);
   }
 }
 __global__ void k_adj_div_t(float* __restrict__ dU, float* __restrict__ dV,
                             const float* __restrict__ x0, const float* __restrict__ x1,
-                            const void* __restrict__ ctl_sel, const uint8_t* __restrict__ flags,
-                            Grid g) {
+                            const void* __restrict__ ctl_sel, const float* __restrict__ e0,
+                            const float* __restrict__ e1, const void* __restrict__ esel,
+                            const uint8_t* __restrict__ flags, Grid g) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
-  adj_div_t_cell(i, j, dU, dV, x0, x1, ctl_sel, flags, g);
+  adj_div_t_cell(i, j, dU, dV, x0, x1, ctl_sel, e0, e1, esel, flags, g);
 }
 
 // Sources that set U, V (SetVelocity) or M (a smoke assignment) cut the
@@ -1037,11 +1059,29 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
     FG_CELLS(f, k_adj_turbulence, adj_turbulence_cell, A[F::A_U], A[F::A_V], U2, V2, f->noise, f->flags,
                                         p.turbulence_strength * dt);
   }
-  // ---- projection: dU1 = dU2 + div^T P_K G^T dU2
+  // ---- projection: dU1 = dU2 + div^T M^T G^T dU2, where the potential is
+  // M b with M = P_K (K sweeps from 0) and, with the outer correction,
+  // M = P_K + P_c (I - A P_K) (P_c: its K_c sweeps).  P_K, P_c and A are
+  // symmetric, so M^T lam = P_K (lam - A P_c lam) + P_c lam: the correction
+  // solve runs first, on lam, then the main solve on the residual.
   count(f);
   FG_CELLS(f, k_adj_grad_t, adj_grad_t_cell, A[F::A_U], A[F::A_V], f->wgt, f->rhs, f->bw, f->flags);
+  const bool refine = p.refine_sweeps > 0;
+  const float* rhs_main = f->rhs;
+  const float* bw_main = f->bw;
+  if (refine) {
+    if ((e = launch_jacobi_solve(f, f->pctl, f->rhs, f->bw, f->err, f->err2,
+                                 p.refine_sweeps)) != cudaSuccess)
+      return e;
+    count(f);
+    FG_CELLS(f, k_adj_resid, adj_resid_cell, (const float*)f->rhs, (const float*)f->err,
+             (const float*)f->err2, (const void*)((const int*)f->pctl + 1),
+             (const float*)f->wgt, f->rhs_e, f->bwe, (const uint8_t*)f->flags);
+    rhs_main = f->rhs_e;
+    bw_main = f->bwe;
+  }
   if (p.num_iters > 0) {
-    if ((e = launch_jacobi_solve(f, f->ectl, f->rhs, f->bw, f->phi, f->phi2, p.num_iters)) !=
+    if ((e = launch_jacobi_solve(f, f->ectl, rhs_main, bw_main, f->phi, f->phi2, p.num_iters)) !=
         cudaSuccess)
       return e;
   } else {
@@ -1050,7 +1090,9 @@ cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
   }
   count(f);
   FG_CELLS(f, k_adj_div_t, adj_div_t_cell, A[F::A_U], A[F::A_V], f->phi, f->phi2,
-                                 (const int*)f->ectl + 1, f->flags);
+           (const void*)((const int*)f->ectl + 1), refine ? (const float*)f->err : nullptr,
+           (const float*)f->err2, (const void*)((const int*)f->pctl + 1),
+           (const uint8_t*)f->flags);
   // ---- sources (the forces' adjoint is then the state's)
   if (f->n_src_groups > 0) {
     count(f);

@@ -44,39 +44,31 @@ __device__ __forceinline__ float trace_sample_u(const float* __restrict__ Ut,
                                                 const float* __restrict__ Fs, int i, int j,
                                                 float sdt, const Grid& g) {
   int c = i * g.P + j;
-  float x = (float)i * g.h;
-  float y = (float)j * g.h + g.hh;
   float u = Ut[c];
   float v = (Vt[c - g.P] + Vt[c] + Vt[c - g.P + 1] + Vt[c + 1]) * 0.25f;  // avgV fluid.go:342-347
-  x = x - sdt * u;
-  y = y - sdt * v;
-  return sample_field(Fs, x, y, 0.0f, g.hh, g);
+  return sample_dep(Fs, i, j, sdt * u, sdt * v, false, true, g);
 }
 __device__ __forceinline__ float trace_sample_v(const float* __restrict__ Ut,
                                                 const float* __restrict__ Vt,
                                                 const float* __restrict__ Fs, int i, int j,
                                                 float sdt, const Grid& g) {
   int c = i * g.P + j;
-  float x = (float)i * g.h + g.hh;
-  float y = (float)j * g.h;
   float u = (Ut[c - 1] + Ut[c] + Ut[c + g.P - 1] + Ut[c + g.P]) * 0.25f;  // avgU fluid.go:335-340
   float v = Vt[c];
-  x = x - sdt * u;
-  y = y - sdt * v;
-  return sample_field(Fs, x, y, g.hh, 0.0f, g);
+  return sample_dep(Fs, i, j, sdt * u, sdt * v, true, false, g);
 }
 
 // Interior cells (1 <= i <= NX-2, 1 <= j <= NY-2): every load of the two
 // traces is in range whatever the flags say, so the interior paths below
 // issue them beside the flag load instead of after it, and sample before
-// selecting.  The departure points are the same expressions as in
-// trace_sample_u/v, so the results are bitwise the same.
+// selecting.  The departure points are formed as in trace_sample_u/v, so
+// the results are bitwise the same.
 __device__ __forceinline__ bool interior_ij(int i, int j, const Grid& g) {
   return i >= 1 && j >= 1 && i <= g.NX - 2 && j <= g.NY - 2;
 }
 struct Departure {
-  float xu, yu;  // from the U face
-  float xv, yv;  // from the V face
+  float su_u, sv_u;  // sdt * (u, v) at the U face
+  float su_v, sv_v;  // sdt * (u, v) at the V face
 };
 __device__ __forceinline__ Departure departures(const float* __restrict__ Ut,
                                                 const float* __restrict__ Vt, int i, int j,
@@ -86,10 +78,10 @@ __device__ __forceinline__ Departure departures(const float* __restrict__ Ut,
   float uv = (Ut[c - 1] + Ut[c] + Ut[c + g.P - 1] + Ut[c + g.P]) * 0.25f;
   float vv = Vt[c];
   Departure d;
-  d.xu = (float)i * g.h - sdt * uu;
-  d.yu = ((float)j * g.h + g.hh) - sdt * vu;
-  d.xv = ((float)i * g.h + g.hh) - sdt * uv;
-  d.yv = (float)j * g.h - sdt * vv;
+  d.su_u = sdt * uu;
+  d.sv_u = sdt * vu;
+  d.su_v = sdt * uv;
+  d.sv_v = sdt * vv;
   return d;
 }
 
@@ -107,8 +99,8 @@ __device__ __forceinline__ void sl_velocity_cell(int i, int j, const float* __re
   if (interior_ij(i, j, g)) {
     uint8_t fl = flags[c];
     Departure d = departures(Ui, Vi, i, j, c, dt, g);
-    float su = sample_field(Ui, d.xu, d.yu, 0.0f, g.hh, g);
-    float sv = sample_field(Vi, d.xv, d.yv, g.hh, 0.0f, g);
+    float su = sample_dep(Ui, i, j, d.su_u, d.sv_u, false, true, g);
+    float sv = sample_dep(Vi, i, j, d.su_v, d.sv_v, true, false, g);
     u = u_advected(fl, i, j, g) ? su : nU[c];
     v = v_advected(fl, i, j, g) ? sv : nV[c];
     Uo[c] = u;
@@ -155,8 +147,8 @@ __device__ __forceinline__ void bfecc_vel_fwd_cell(int i, int j, const float* __
   if (interior_ij(i, j, g)) {
     uint8_t fl = flags[c];
     Departure d = departures(Ui, Vi, i, j, c, dt, g);
-    float su = sample_field(Ui, d.xu, d.yu, 0.0f, g.hh, g);
-    float sv = sample_field(Vi, d.xv, d.yv, g.hh, 0.0f, g);
+    float su = sample_dep(Ui, i, j, d.su_u, d.sv_u, false, true, g);
+    float sv = sample_dep(Vi, i, j, d.su_v, d.sv_v, true, false, g);
     Fu[c] = u_advected(fl, i, j, g) ? su : nU[c];
     Fv[c] = v_advected(fl, i, j, g) ? sv : nV[c];
     return;
@@ -223,8 +215,8 @@ __device__ __forceinline__ void bfecc_vel_correct_cell(int i, int j, const float
   float lou, hiu, lov, hiv;
   range3x3(Ui, c, g.P, lou, hiu);
   range3x3(Vi, c, g.P, lov, hiv);
-  float su = sample_field(Fu, d.xu, d.yu, 0.0f, g.hh, g);
-  float sv = sample_field(Fv, d.xv, d.yv, g.hh, 0.0f, g);
+  float su = sample_dep(Fu, i, j, d.su_u, d.sv_u, false, true, g);
+  float sv = sample_dep(Fv, i, j, d.su_v, d.sv_v, true, false, g);
   float bu = u_advected(fl, i, j, g) ? su : 0.0f;
   float bv = v_advected(fl, i, j, g) ? sv : 0.0f;
   float cu = ou - (bu - ou) * 0.5f;
@@ -252,9 +244,7 @@ __device__ __forceinline__ float smoke_value(const float* __restrict__ Ut,
   int c = i * g.P + j;
   float u = (Ut[c] + Ut[c + g.P]) * 0.5f * smokeAdv;
   float v = (Vt[c] + Vt[c + 1]) * 0.5f * smokeAdv;
-  float x = (float)i * g.h + g.hh - sdt * u;
-  float y = (float)j * g.h + g.hh - sdt * v;
-  return sample_field(Ms, x, y, g.hh, g.hh, g);
+  return sample_dep(Ms, i, j, sdt * u, sdt * v, true, true, g);
 }
 
 

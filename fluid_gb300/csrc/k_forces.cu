@@ -275,6 +275,12 @@ __global__ void k_copy_border(float* __restrict__ dst, const float* __restrict__
 
 }  // namespace
 
+cudaError_t launch_build_flags_on(cudaStream_t st, const float* S, uint8_t* flags, const Grid& g) {
+  k_build_flags<<<dim3((g.NY + BX - 1) / BX, (g.NX + BY - 1) / BY), dim3(BX, BY), 0, st>>>(S, flags,
+                                                                                       g);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_build_flags(fg_fluid* f) {
   count(f);
   k_build_flags<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(f->d[FG_S], f->flags, f->g);

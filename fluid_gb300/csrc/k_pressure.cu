@@ -1351,6 +1351,17 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
   return false;
 }
 
+// After a wait gave up, before the block leaves: waits for its copy in
+// flight for up to about eight more seconds, so a copy that is only slow
+// lands before the block's shared memory passes to another block.  A copy
+// still outstanding after nine seconds means the device is not progressing;
+// the wait stays bounded all the same.
+constexpr int MBAR_DRAIN_SLICES = 8;
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, unsigned parity) {
+  for (int s = 0; s < MBAR_DRAIN_SLICES; ++s)
+    if (mbar_wait_bounded(bar, parity)) return;
+}
+
 // The TMAX sweeps of one tile in registers, with the arithmetic of
 // jacobi_tile.  hook(sw) runs before sweep sw (sw a constant after
 // unrolling), so callers can spread latency-bound side work over the sweeps.
@@ -1407,7 +1418,7 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
     k_jacobi_tma(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw,
                  const __grid_constant__ CUtensorMap tmb, float* __restrict__ dst, float om1,
                  PCtl* ctl, int k, int t0, int out_sel, int zero_init, Grid g, int ntx,
-                 int ntiles, int* err) {
+                 int ntiles, int* err, int stall_tile) {
   extern __shared__ __align__(128) float4 tbuf4[];  // [3][RI][RJ] floats: phi, w, w*b
   float* tbuf = reinterpret_cast<float*>(tbuf4);
   __shared__ float4 xch[2][2][NWARP][32];
@@ -1426,7 +1437,10 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
     const int x = tx * OJ - TMAX, y = ty * OI - TMAX;  // x: a multiple of 4 floats (16 bytes)
     // Order this block's earlier shared-memory reads before the copy's writes.
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(&bar, bytes);
+    // Fault injection: tile `stall_tile` expects 16 bytes more than its
+    // copies bring, so its barrier phase never completes and the bounded
+    // wait below gives up (every copy issued still lands).
+    mbar_expect_tx(&bar, bytes + (t == stall_tile ? 16u : 0u));
     if (!zero_init) tma_load_2d(tbuf, &tmx, x, y, &bar);
     tma_load_2d(tbuf + TILE_FLOATS, &tmw, x, y, &bar);
     tma_load_2d(tbuf + 2 * TILE_FLOATS, &tmb, x, y, &bar);
@@ -1437,13 +1451,14 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const bool landed = mbar_wait_bounded(&bar, parity);
     if (__syncthreads_or(!landed)) {
-      // A copy did not land in time (the whole block agrees): flag it, give
-      // it one more bounded wait, stop.
+      // A copy did not land in time (the whole block agrees): flag it, let
+      // it land (bounded), stop.  The next tile's copy is issued only after
+      // this one landed, so nothing else is in flight.
       if (tid == 0) {
         atomicExch(&ctl->pad[0], 1);
         if (err) atomicExch(err, 1);
       }
-      if (!landed) mbar_wait_bounded(&bar, parity);
+      if (!landed) mbar_drain(&bar, parity);
       return;
     }
     parity ^= 1u;
@@ -1722,7 +1737,7 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
       atomicExch(&ctl->pad[0], 1);
       if (err) atomicExch(err, 1);
     }
-    if (in_flight) mbar_wait_bounded(&bar, parity);  // a copy still landing
+    if (in_flight) mbar_drain(&bar, parity);  // a copy still landing
     if (blockIdx.x == 0 && nphase > 0) {
       ctl->sweeps = nphase * TMAX;
       ctl->last_launch = nphase - 1;
@@ -1910,12 +1925,17 @@ __global__ void __launch_bounds__(256)
   block_row<5, 0x4u>(row, 0x12u, shr, part + 10 * (size_t)(blockIdx.y * gridDim.x + blockIdx.x));
 }
 
-// Copies the solve's final potential (the buffer the control block names).
+// Copies the solve's final potential (the buffer the control block names),
+// plus the outer correction when one ran (both exactly 0 off the active
+// cells, as k_grad_fused adds them).
 __global__ void k_store_phi(const float* __restrict__ phi0, const float* __restrict__ phi1,
-                            const PCtl* __restrict__ ctl, float* __restrict__ dst, int n) {
+                            const PCtl* __restrict__ ctl, const float* __restrict__ e0,
+                            const float* __restrict__ e1, const PCtl* __restrict__ ectl,
+                            float* __restrict__ dst, int n) {
   const float* src = ctl->sel ? phi1 : phi0;
+  const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) dst[k] = src[k];
+  if (k < n) dst[k] = e ? src[k] + e[k] : src[k];
 }
 
 // A batch's gradient subtract: grad_cell without the statistics.
@@ -1958,18 +1978,64 @@ size_t pctl_bytes(int n_slots) { return sizeof(PCtl) + sizeof(unsigned) * (size_
 // Tensor maps of the TMA-fed Jacobi kernel: a 2D float array of rows x
 // pitch, boxes of 64 rows x 128 columns, zero outside.  false when the
 // driver entry point or the encoding is unavailable (the plain kernel runs).
-// Per device: the SM count, the dataflow kernel's blocks per SM, whether the
-// set-up ran (the kernels' shared-memory limit is a per-device attribute).
-constexpr int kMaxDevices = 64;
+// Per CUDA context: the SM count, the dataflow kernel's blocks per SM,
+// whether the set-up ran (the kernels' shared-memory limit is state of the
+// context the module is loaded in).
+constexpr int kMaxContexts = 64;
 struct TmaDevice {
   std::once_flag once;
   std::atomic<bool> ready{false};
   int sms = 0;
   int flow_per_sm = 0;
 };
-static TmaDevice g_tma_dev[kMaxDevices];
+static TmaDevice g_tma_dev[kMaxContexts];
+static unsigned long long g_tma_key[kMaxContexts];
+static int g_tma_used = 0;
+static std::mutex g_tma_mu;
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 static std::once_flag g_encode_once;
+
+// Identity of the CUDA context current on the calling thread: its
+// cuCtxGetId value (unique for the life of the process) with the top bit
+// clear, or, when the driver entry points are missing, the device ordinal
+// with the top bit set; 0 when neither is known (no context yet).  Module
+// state -- a __device__ array's address, a kernel's shared-memory limit --
+// belongs to a context, and a caller may make its own context current
+// (cuCtxCreate, cuCtxSetCurrent) or replace the primary one
+// (cudaDeviceReset), so caches of that state are keyed by this value.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+static PfnCtxGetCurrent g_ctx_current = nullptr;
+static PfnCtxGetId g_ctx_id = nullptr;
+static std::once_flag g_ctx_once;
+
+unsigned long long context_key() {
+  std::call_once(g_ctx_once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &fn, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_current = reinterpret_cast<PfnCtxGetCurrent>(fn);
+    fn = nullptr;
+    if (cudaGetDriverEntryPoint("cuCtxGetId", &fn, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_id = reinterpret_cast<PfnCtxGetId>(fn);
+    cudaGetLastError();
+  });
+  if (g_ctx_current && g_ctx_id) {
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&c) != CUDA_SUCCESS || !c) return 0;
+    if (g_ctx_id(c, &id) != CUDA_SUCCESS) return 0;
+    return (id & ~(1ull << 63)) + 1;  // nonzero, top bit clear
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return (1ull << 63) | (unsigned long long)dev;
+}
 
 static bool encode_box_map(CUtensorMap* tm, const float* base, int rows, int pitch) {
   if (!g_encode || (reinterpret_cast<uintptr_t>(base) & 15) || (pitch % 4) != 0) return false;
@@ -1984,14 +2050,17 @@ static bool encode_box_map(CUtensorMap* tm, const float* base, int rows, int pit
   return r == CUDA_SUCCESS;
 }
 
-// The current device's entry, or nullptr.
+// The current context's entry, or nullptr (no context identity, or more
+// contexts than entries: the plain kernels run).
 static TmaDevice* tma_device() {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  return &g_tma_dev[dev];
+  const unsigned long long key = context_key();
+  if (!key) return nullptr;
+  std::lock_guard<std::mutex> lk(g_tma_mu);
+  for (int k = 0; k < g_tma_used; ++k)
+    if (g_tma_key[k] == key) return &g_tma_dev[k];
+  if (g_tma_used == kMaxContexts) return nullptr;
+  g_tma_key[g_tma_used] = key;
+  return &g_tma_dev[g_tma_used++];
 }
 
 // Resolves the tensor-map encoder (once per process) and, once per device,
@@ -2059,7 +2128,7 @@ static const TmaDevice* tma_ready(cudaStream_t st) {
 // false (nothing launched) when the tensor maps cannot be made.
 static bool launch_jacobi_tma(cudaStream_t st, const Grid& g, PCtl* ctl, const float* src,
                               float* dst, const float* W, const float* BW, float om1, bool o1,
-                              int k, int t0, int sel, int zero_init, int* err) {
+                              int k, int t0, int sel, int zero_init, int* err, int stall_tile) {
   const TmaDevice* dv = tma_ready(st);
   if (!dv) return false;
   CUtensorMap tmx, tmw, tmb;
@@ -2074,18 +2143,19 @@ static bool launch_jacobi_tma(cudaStream_t st, const Grid& g, PCtl* ctl, const f
   const size_t smem = 3 * (size_t)TILE_FLOATS * sizeof(float);
   if (o1)
     k_jacobi_tma<true><<<grid, TB_THREADS, smem, st>>>(tmx, tmw, tmb, dst, om1, ctl, k, t0, sel,
-                                                       zero_init, g, ntx, ntiles, err);
+                                                       zero_init, g, ntx, ntiles, err, stall_tile);
   else
     k_jacobi_tma<false><<<grid, TB_THREADS, smem, st>>>(tmx, tmw, tmb, dst, om1, ctl, k, t0, sel,
-                                                        zero_init, g, ntx, ntiles, err);
+                                                        zero_init, g, ntx, ntiles, err, stall_tile);
   return true;
 }
 
 inline int clamp_tb(int t) { return t < 1 ? 1 : (t > TMAX ? TMAX : t); }
 
 int jacobi_launches(const fg_fluid* f, int iters) {
-  int T = clamp_tb(f->prm.tb_depth);
-  return (iters + T - 1) / T;
+  // In 64 bits: iters near INT_MAX must not wrap (at most INT_MAX launches).
+  const long long T = clamp_tb(f->prm.tb_depth);
+  return (int)(((long long)iters + T - 1) / T);
 }
 
 int jacobi_tile_count(int NX, int NY) {
@@ -2147,11 +2217,11 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
                                   const float* mphi1 = nullptr, const PCtl* mctl = nullptr,
                                   float* rhs_e = nullptr, float* bwe = nullptr,
                                   int* err = nullptr, int* done = nullptr,
-                                  int stall_tile = -1) {
+                                  int stall_tile = -1, int tma_stall_tile = -1) {
   float om1 = 1.0f - om;
   bool o1 = om1 == 0.0f;
   dim3 gr((g.NY + OJ - 1) / OJ, (g.NX + OI - 1) / OI);
-  int nlaunch = (iters + T - 1) / T;
+  int nlaunch = (int)(((long long)iters + T - 1) / T);
   int k0 = 0, kernels = 0;
   // Fixed sweep counts in full launches: the leading full phases as one
   // dataflow kernel where the grid is large enough.
@@ -2175,7 +2245,8 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
     const float* bwk = mphi0 && k > 0 ? bwe : bw;
     float* re = rinit && nlaunch > 1 ? rhs_e : nullptr;
     if (full && !check && !rinit && !mphi0 &&
-        launch_jacobi_tma(st, g, ctl, src, dst, W, bwk, om1, o1, k, t0, sel, zi, err))
+        launch_jacobi_tma(st, g, ctl, src, dst, W, bwk, om1, o1, k, t0, sel, zi, err,
+                          tma_stall_tile))
       continue;
 #define FG_JAC(O, F, C, R)                                                                      \
   k_jacobi_rb<O, F, C, R><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bwk, bk, flags, om1, ctl, k, t0, \
@@ -2226,9 +2297,9 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
                                 float* x1, int iters, bool allow_exit, bool rinit = false) {
   if (f->batch) return jacobi_solve_batch(f, ctl, bw, x0, x1);
   int T = clamp_tb(f->prm.tb_depth);
-  int nlaunch = (iters + T - 1) / T;
+  const long long nlaunch = ((long long)iters + T - 1) / T;
   if (nlaunch > f->n_slots) return cudaErrorInvalidValue;
-  cudaError_t e = cudaMemsetAsync(ctl, 0, pctl_bytes(nlaunch), f->stream);
+  cudaError_t e = cudaMemsetAsync(ctl, 0, pctl_bytes((int)nlaunch), f->stream);
   if (e != cudaSuccess) return e;
   int check = allow_exit && f->prm.early_exit ? 1 : 0;
   const bool prof = f->profile && allow_exit;
@@ -2247,7 +2318,7 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
   if (e != cudaSuccess) return e;
   if (prof) {
     if ((e = cudaEventRecord(f->prof_ev[1], f->stream)) != cudaSuccess) return e;
-    f->prof_launches = nlaunch;
+    f->prof_launches = (int)nlaunch;
   }
   return cudaGetLastError();
 }
@@ -2452,6 +2523,204 @@ cudaError_t launch_multigrid(fg_fluid* f, int num_iters, float dt) {
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ multigrid Jacobi
+// The MULTIGRID scheme: V(2,2) cycles on the masked Poisson system of the
+// Jacobi scheme.  A coarse cell covers up to 2 x 2 fine cells (the ghost
+// ring coarsens along its own row or column) and is fluid if any of them is;
+// its flag bytes come from that mask as the fine ones come from S.  The
+// smoother is the Jacobi scheme's sweep kernel with weight kMgOmega *
+// PressureDamping (undamped Jacobi leaves the high frequencies a coarse grid
+// cannot see); the coarse right-hand side is the sum of the children's
+// residuals (the coarse operator has the fine one's form at twice the
+// spacing, so the sum is the scaled average); the correction returns by
+// bilinear interpolation (weights 9, 3, 3, 1) over the active coarse cells
+// around each fine cell.  Every operation has a fixed order, restated by
+// the oracle, so the result is bitwise reproducible.
+constexpr int kMgPre = 2, kMgPost = 2, kMgCoarse = 32;
+
+namespace {
+
+// Rows of the fine grid (NXf rows) under coarse row I of NXc: the ring row
+// under the ring, else rows 2I-1 and 2I of the interior.
+__host__ __device__ __forceinline__ void mg_children(int I, int NXc, int NXf, int& a, int& b) {
+  if (I == 0) {
+    a = b = 0;
+  } else if (I == NXc - 1) {
+    a = b = NXf - 1;
+  } else {
+    a = 2 * I - 1;
+    b = min(2 * I, NXf - 2);
+  }
+}
+
+__global__ void k_mg_mask(const float* __restrict__ Sf, Grid gf, float* __restrict__ Sc, Grid gc) {
+  int J = blockIdx.x * blockDim.x + threadIdx.x;
+  int I = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I >= gc.NX || J >= gc.NY) return;
+  int a0, a1, b0, b1;
+  mg_children(I, gc.NX, gf.NX, a0, a1);
+  mg_children(J, gc.NY, gf.NY, b0, b1);
+  float v = 0.0f;
+  for (int a = a0; a <= a1; ++a)
+    for (int b = b0; b <= b1; ++b) v = fmaxf(v, Sf[a * gf.P + b]);
+  Sc[I * gc.P + J] = v;
+}
+
+__global__ void k_mg_weights(const uint8_t* __restrict__ flags, float* __restrict__ w, float om,
+                             Grid g) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.NX || j >= g.NY) return;
+  const uint8_t fl = flags[i * g.P + j];
+  w[i * g.P + j] = flag_active(fl) ? om / (float)flag_count(fl) : 0.0f;
+}
+
+// Coarse right-hand side: the sum of the active children's residuals
+// b - (s x - (x_w + x_e + x_s + x_n)), and w * b.
+__global__ void k_mg_restrict(const float* __restrict__ xf, const float* __restrict__ bf,
+                              const uint8_t* __restrict__ flf, Grid gf,
+                              const uint8_t* __restrict__ flc, const float* __restrict__ wc,
+                              float* __restrict__ bc, float* __restrict__ bwc, Grid gc) {
+  int J = blockIdx.x * blockDim.x + threadIdx.x;
+  int I = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I < 1 || J < 1 || I > gc.NX - 2 || J > gc.NY - 2) return;
+  const int cc = I * gc.P + J;
+  float rs = 0.0f;
+  if (flag_active(flc[cc])) {
+    int a0, a1, b0, b1;
+    mg_children(I, gc.NX, gf.NX, a0, a1);
+    mg_children(J, gc.NY, gf.NY, b0, b1);
+    for (int a = a0; a <= a1; ++a)
+      for (int b = b0; b <= b1; ++b) {
+        const int cf = a * gf.P + b;
+        const uint8_t fl = flf[cf];
+        if (!flag_active(fl)) continue;
+        float nb = xf[cf - gf.P] + xf[cf + gf.P] + xf[cf - 1] + xf[cf + 1];
+        float ax = (float)flag_count(fl) * xf[cf] - nb;
+        rs = rs + (bf[cf] - ax);
+      }
+  }
+  bc[cc] = rs;
+  bwc[cc] = wc[cc] * rs;
+}
+
+// x_f += the bilinear interpolation of x_c over the active coarse cells
+// around each active fine cell.
+__global__ void k_mg_prolong(const float* __restrict__ xc, const uint8_t* __restrict__ flc, Grid gc,
+                             float* __restrict__ xf, const uint8_t* __restrict__ flf, Grid gf) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i < 1 || j < 1 || i > gf.NX - 2 || j > gf.NY - 2) return;
+  const int cf = i * gf.P + j;
+  if (!flag_active(flf[cf])) return;
+  const int I = (i - 1) / 2 + 1, J = (j - 1) / 2 + 1;
+  const int di = ((i - 1) & 1) ? 1 : -1, dj = ((j - 1) & 1) ? 1 : -1;
+  const int ci[4] = {I, I + di, I, I + di}, cj[4] = {J, J, J + dj, J + dj};
+  const float wt[4] = {9.0f, 3.0f, 3.0f, 1.0f};
+  float num = 0.0f, den = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int cc = ci[k] * gc.P + cj[k];
+    if (!flag_active(flc[cc])) continue;
+    num = num + wt[k] * xc[cc];
+    den = den + wt[k];
+  }
+  const float e = den > 0.0f ? num / den : 0.0f;
+  xf[cf] = xf[cf] + e;
+}
+
+inline dim3 level_grid(const Grid& g) { return dim3((g.NY + BX - 1) / BX, (g.NX + BY - 1) / BY); }
+
+// ns (<= TMAX) damped Jacobi sweeps src -> dst on one level.
+void mg_sweeps(cudaStream_t st, const MgLevelDev& v, const float* src, float* dst, float om1,
+               PCtl* ctl, int t0, int ns, int sel, int zero) {
+  dim3 gr((v.g.NY + OJ - 1) / OJ, (v.g.NX + OI - 1) / OI);
+  if (ns == TMAX)
+    k_jacobi_rb<false, true, false, false><<<gr, TB_THREADS, 0, st>>>(
+        src, dst, v.w, v.bw, nullptr, v.flags, om1, ctl, 0, t0, ns, 0.0f, sel, zero, v.g, nullptr,
+        nullptr, nullptr, nullptr, nullptr);
+  else
+    k_jacobi_rb<false, false, false, false><<<gr, TB_THREADS, 0, st>>>(
+        src, dst, v.w, v.bw, nullptr, v.flags, om1, ctl, 0, t0, ns, 0.0f, sel, zero, v.g, nullptr,
+        nullptr, nullptr, nullptr, nullptr);
+}
+
+// The V-cycles of one solve.  cur[l] names the buffer of level l holding
+// its iterate; the last smoothing of level 0 reports to the main control
+// block (sweeps = cycles, sel = the buffer of the result).
+struct MgRun {
+  fg_fluid* f;
+  MgHier* h;
+  float om1;
+  int cycles;
+  std::vector<int> cur;
+  int launches = 0;
+  void smooth(int l, int ns, bool zero, bool last) {
+    MgLevelDev& v = h->lv[l];
+    const int to = 1 - cur[l];
+    PCtl* ctl = last ? (PCtl*)f->pctl : (PCtl*)h->ctl;
+    mg_sweeps(f->stream, v, v.x[cur[l]], v.x[to], om1, ctl, last ? cycles - ns : 0, ns, to,
+              zero ? 1 : 0);
+    cur[l] = to;
+    ++launches;
+  }
+  void cycle(int l, bool zero, bool last) {
+    const int L = (int)h->lv.size();
+    if (l == L - 1) {
+      for (int k = 0; k < kMgCoarse / TMAX; ++k) smooth(l, TMAX, zero && k == 0, false);
+      return;
+    }
+    MgLevelDev& v = h->lv[l];
+    MgLevelDev& c = h->lv[l + 1];
+    smooth(l, kMgPre, zero, false);
+    k_mg_restrict<<<level_grid(c.g), dim3(BX, BY), 0, f->stream>>>(v.x[cur[l]], v.b, v.flags, v.g,
+                                                                   c.flags, c.w, c.b, c.bw, c.g);
+    ++launches;
+    cycle(l + 1, true, false);
+    k_mg_prolong<<<level_grid(v.g), dim3(BX, BY), 0, f->stream>>>(c.x[cur[l + 1]], c.flags, c.g,
+                                                                  v.x[cur[l]], v.flags, v.g);
+    ++launches;
+    smooth(l, kMgPost, false, last && l == 0);
+  }
+};
+
+cudaError_t mg_solve(fg_fluid* f, int cycles, float om) {
+  MgHier* h = f->mg;
+  if (!h || h->lv.size() < 2) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(h->ctl, 0, sizeof(PCtl), f->stream);
+  if (e != cudaSuccess) return e;
+  MgRun run{f, h, 1.0f - om, cycles, std::vector<int>(h->lv.size(), 0)};
+  for (int k = 0; k < cycles; ++k) run.cycle(0, k == 0, k == cycles - 1);
+  count(f, run.launches);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+void mg_free(fg_fluid* f) {
+  if (!f->mg) return;
+  cudaFree(f->mg->block);
+  cudaFree(f->mg->ctl);
+  delete f->mg;
+  f->mg = nullptr;
+}
+
+cudaError_t launch_mg_rebuild(fg_fluid* f) {
+  MgHier* h = f->mg;
+  if (!h) return cudaSuccess;
+  const float om = kMgOmega * f->prm.pressure_damping;
+  for (size_t l = 1; l < h->lv.size(); ++l) {
+    const MgLevelDev& p = h->lv[l - 1];
+    const MgLevelDev& c = h->lv[l];
+    k_mg_mask<<<level_grid(c.g), dim3(BX, BY), 0, f->stream>>>(p.S, p.g, c.S, c.g);
+    cudaError_t e = launch_build_flags_on(f->stream, c.S, c.flags, c.g);
+    if (e != cudaSuccess) return e;
+    k_mg_weights<<<level_grid(c.g), dim3(BX, BY), 0, f->stream>>>(c.flags, c.w, om, c.g);
+  }
+  h->omega = om;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb) {
   float cp = f->density * f->h / dt;  // fluid.go:158
   cudaError_t e;
@@ -2466,7 +2735,9 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   PCtl* ctl = (PCtl*)f->pctl;
   PCtl* ectl = (PCtl*)f->ectl;
   dim3 gr = cell_grid(f), bl(BX, BY);
-  float om = f->prm.jacobi_omega * f->prm.pressure_damping;
+  const bool mgs = f->prm.scheme == FG_SCHEME_MULTIGRID && !f->batch;
+  float om = mgs ? kMgOmega * f->prm.pressure_damping
+                 : f->prm.jacobi_omega * f->prm.pressure_damping;
   if (f->batch) {
     // Every scene solves (the batch forbids early exit and refinement);
     // no statistics.
@@ -2492,8 +2763,9 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
                                            f->step_fu, f->step_fv);
   mark(f, "pressure setup");
   if (num_iters > 0) {
-    if ((e = jacobi_solve(f, ctl, f->rhs, f->bw, f->phi, f->phi2, num_iters, true)) != cudaSuccess)
-      return e;
+    e = mgs ? mg_solve(f, num_iters, om)
+            : jacobi_solve(f, ctl, f->rhs, f->bw, f->phi, f->phi2, num_iters, true);
+    if (e != cudaSuccess) return e;
     count(f);
     k_finish_parallel<<<1, 1, 0, f->stream>>>(ctl, f->dstats);
   }
@@ -2525,7 +2797,11 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
 cudaError_t launch_store_phi(fg_fluid* f, float* dst) {
   int n = f->NX * f->P;
   count(f);
-  k_store_phi<<<(n + 255) / 256, 256, 0, f->stream>>>(f->phi, f->phi2, (const PCtl*)f->pctl, dst, n);
+  const bool refine = f->prm.refine_sweeps > 0;
+  k_store_phi<<<(n + 255) / 256, 256, 0, f->stream>>>(f->phi, f->phi2, (const PCtl*)f->pctl,
+                                                      f->err, f->err2,
+                                                      refine ? (const PCtl*)f->ectl : nullptr,
+                                                      dst, n);
   return cudaGetLastError();
 }
 
@@ -2577,12 +2853,14 @@ namespace {
 constexpr size_t kNoAllocMaxCells = (size_t)FG_NOALLOC_MAX_CELLS;  // num_x * padded num_y
 constexpr int kNoAllocSlots = 4096;                                  // Jacobi launches per call
 constexpr size_t kNoAllocCtlBytes = 256 + sizeof(unsigned) * kNoAllocSlots;
-constexpr size_t kNoAllocBytes = 21 * kNoAllocMaxCells + kNoAllocCtlBytes;
+// The status word: nonzero when a bounded wait of the last call gave up.
+constexpr size_t kNoAllocStatusOff = 21 * kNoAllocMaxCells + kNoAllocCtlBytes;
+constexpr size_t kNoAllocBytes = kNoAllocStatusOff + 256;
 
 // Scratch shared by every call on a device: phi, phi2, rhs, w, bw (floats),
-// the flag bytes and the control block, carved at fixed offsets with the
-// solver's own pitch (num_y rounded up to 32).  It keeps the previous call's
-// contents; each call rewrites or clears what it reads.
+// the flag bytes, the control block and the status word, carved at fixed
+// offsets with the solver's own pitch (num_y rounded up to 32).  It keeps
+// the previous call's contents; each call rewrites or clears what it reads.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 // Flag bytes from a caller-owned S (nonzero = fluid).
@@ -2602,28 +2880,45 @@ __global__ void k_noalloc_flags(const float* __restrict__ S, uint8_t* __restrict
   flags[i * Ps + j] = fl;
 }
 
+// The scratch array's address per CUDA context (context_key), looked up by
+// the first call made in each context.  A full table is not an error: the
+// address is then looked up on every call.
+constexpr int kNoAllocCtx = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[256] = {};
+unsigned long long g_noalloc_key[kNoAllocCtx] = {};
+void* g_noalloc_ptr[kNoAllocCtx] = {};
+int g_noalloc_used = 0;
+std::atomic<int> g_noalloc_stall{-1};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the first call on each device does it).
 cudaError_t noalloc_scratch(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_noalloc_ptr[dev] = ptr;
+  unsigned long long key = context_key();
+  if (key) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    for (int k = 0; k < g_noalloc_used; ++k)
+      if (g_noalloc_key[k] == key) {
+        *out = g_noalloc_ptr[k];
+        return cudaSuccess;
+      }
   }
-  *out = g_noalloc_ptr[dev];
+  void* ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  if (!key) key = context_key();  // the lookup made the primary context current
+  if (key) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (g_noalloc_used < kNoAllocCtx) {
+      g_noalloc_key[g_noalloc_used] = key;
+      g_noalloc_ptr[g_noalloc_used++] = ptr;
+    }
+  }
+  *out = ptr;
   return cudaSuccess;
 }
 
 }  // namespace
+
+void set_noalloc_stall(int tile) { g_noalloc_stall.store(tile < 0 ? -1 : tile); }
+
 }  // namespace fg
 
 extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x,
@@ -2638,8 +2933,9 @@ extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, 
   if ((size_t)num_x * (size_t)Ps > kNoAllocMaxCells) return FG_ERR_TOO_LARGE;
   // The caller's fields are indexed with 32-bit integers too.
   if ((size_t)num_x * (size_t)pitch > (size_t)INT_MAX) return FG_ERR_TOO_LARGE;
-  int T = clamp_tb(tb_depth);
-  int nlaunch = (num_iters + T - 1) / T;
+  const int T = clamp_tb(tb_depth);
+  // In 64 bits: a num_iters near INT_MAX must not wrap below the limit.
+  const long long nlaunch = ((long long)num_iters + T - 1) / T;
   if (nlaunch > kNoAllocSlots) return FG_ERR_TOO_LARGE;
   void* base = nullptr;
   if (noalloc_scratch(&base) != cudaSuccess) return FG_ERR_CUDA;
@@ -2652,21 +2948,38 @@ extern "C" int fg_project_noalloc(float* u, float* v, float* p, const float* s, 
   float* BW = (float*)(b + 16 * kNoAllocMaxCells);
   uint8_t* flags = b + 20 * kNoAllocMaxCells;
   PCtl* ctl = (PCtl*)(b + 21 * kNoAllocMaxCells);
+  int* status = (int*)(b + kNoAllocStatusOff);
   Grid g = make_grid(num_x, num_y, pitch, h);   // caller fields
   Grid gs = make_grid(num_x, num_y, Ps, h);     // solver arrays
   float om = jacobi_omega * pressure_damping;
   float cp = density * h / dt;
   dim3 gr((num_y + BX - 1) / BX, (num_x + BY - 1) / BY), bl(BX, BY);
-  // The control words start at zero (sel = 0 until a launch runs).
-  if (cudaMemsetAsync(ctl, 0, pctl_bytes(nlaunch), st) != cudaSuccess) return FG_ERR_CUDA;
+  // The control words and the status word start at zero (sel = 0 until a
+  // launch runs).
+  if (cudaMemsetAsync(ctl, 0, pctl_bytes((int)nlaunch), st) != cudaSuccess ||
+      cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess)
+    return FG_ERR_CUDA;
   k_noalloc_flags<<<gr, bl, 0, st>>>(s, flags, g, Ps);
   k_setup_system<<<gr, bl, 0, st>>>(u, v, phi, rhs, W, BW, flags, om, num_iters == 0 ? 1 : 0, g,
                                     Ps, nullptr, nullptr);
   int n = 0;
   if (num_iters > 0 &&
       enqueue_jacobi(st, gs, ctl, rhs, BW, W, flags, phi, phi2, num_iters, T, om,
-                     early_exit ? 1 : 0, tolerance, &n) != cudaSuccess)
+                     early_exit ? 1 : 0, tolerance, &n, nullptr, nullptr, nullptr, nullptr,
+                     nullptr, status, nullptr, -1, g_noalloc_stall.load()) != cudaSuccess)
     return FG_ERR_CUDA;
   k_grad<<<gr, bl, 0, st>>>(u, v, p, phi, phi2, ctl, nullptr, nullptr, nullptr, flags, cp, g, Ps);
   return cudaGetLastError() == cudaSuccess ? FG_OK : FG_ERR_CUDA;
+}
+
+extern "C" int fg_project_noalloc_status(void* stream) {
+  using namespace fg;
+  int v = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  // The symbol is resolved in the current context, like the scratch itself.
+  if (cudaMemcpyFromSymbolAsync(&v, g_noalloc_scratch, sizeof(int), kNoAllocStatusOff,
+                                cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return FG_ERR_CUDA;
+  return v ? FG_ERR_TIMEOUT : FG_OK;
 }

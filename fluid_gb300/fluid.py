@@ -24,7 +24,7 @@ Relaxation = 1.9  # package var fluid.Relaxation (fluid.go:7-9)
 
 FIELDS = {"U": 0, "V": 1, "newU": 2, "newV": 3, "p": 4, "S": 5, "M": 6, "newM": 7}
 ALL_FIELDS = 0xFF
-SCHEME_LEXSOR, SCHEME_JACOBI = 0, 1
+SCHEME_LEXSOR, SCHEME_JACOBI, SCHEME_MULTIGRID = 0, 1, 3
 
 # Python attribute -> fg_params member.
 _PARAMS = {
@@ -45,8 +45,9 @@ _PARAMS = {
     "check_every": "tb_depth",
     "refine_sweeps": "refine_sweeps",
     "use_graphs": "use_graphs",
+    "precise_coords": "precise_coords",
 }
-_BOOL = {"UseMultigrid", "UseBFECC", "early_exit", "use_graphs"}
+_BOOL = {"UseMultigrid", "UseBFECC", "early_exit", "use_graphs", "precise_coords"}
 
 
 def debug_fail_alloc(n):

@@ -61,8 +61,14 @@ enum {
 /* Pressure schemes.  LEXSOR is the reference's serial lexicographic SOR
  * (fluid.go:157-234) reproduced exactly by a wavefront kernel; JACOBI is the
  * parallel weighted-Jacobi relaxation of the same masked Poisson system with
- * temporal blocking. */
-enum { FG_SCHEME_LEXSOR = 0, FG_SCHEME_JACOBI = 1 };
+ * temporal blocking.  MULTIGRID solves that system by num_iters parallel
+ * V(2,2) cycles (the role the reference's UseMultigrid V-cycle,
+ * fluid.go:559-758, plays for its serial scheme): levels of half the
+ * interior size down to a side of 8, damped Jacobi smoothing with weight
+ * 0.8 * PressureDamping (jacobi_omega, tb_depth and early_exit are not
+ * used), residuals summed into the coarse right-hand side, bilinear
+ * interpolation of the correction; refine_sweeps must be 0. */
+enum { FG_SCHEME_LEXSOR = 0, FG_SCHEME_JACOBI = 1, FG_SCHEME_MULTIGRID = 3 };
 
 typedef struct fg_params {
   /* Exported tuning fields of fluid.Fluid (fluid.go:25-39). */
@@ -85,7 +91,10 @@ typedef struct fg_params {
   int tb_depth;               /* Jacobi sweeps per launch; also the early-exit check interval */
   int refine_sweeps;          /* FP64-residual outer correction sweeps (0 = off) */
   int use_graphs;             /* capture each step in a CUDA graph            */
-  int reserved[7];
+  int precise_coords;         /* 1: advection departure points relative to their face
+                                 (no counterpart in the reference; 0 = the reference's
+                                 absolute float coordinates, fluid.go:357-398) */
+  int reserved[6];
 } fg_params;
 
 /* Per-step diagnostics, accumulated in FP64 on the device. */
@@ -235,14 +244,27 @@ unsigned long long fg_edit_bytes(const fg_fluid* f);
  * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream)
  * and the call returns without waiting.  The first call on a device looks up
  * the scratch array's device address; make that first call before any stream
- * capture.  All calls on a device share the one scratch array, so calls
+ * capture.  The address is kept per CUDA context, so a caller that makes its
+ * own context current (cuCtxCreate / cuCtxSetCurrent) or resets the device
+ * gets the array of the context it runs in; the first call in each context
+ * does the look-up.  All calls on a device share the one scratch array, so calls
  * whose work can overlap on the GPU (other streams, other host threads) race
- * and must be ordered by the caller. */
+ * and must be ordered by the caller.
+ * The call returns before the GPU work ends, so a bounded device-side wait
+ * that gives up (the TMA-fed Jacobi kernel's copy wait, about a second)
+ * cannot be reported by it: the wait sets a status word in the scratch
+ * array, the call's remaining kernels still run, and the fields it wrote are
+ * then not a projection.  fg_project_noalloc_status(stream) waits for
+ * `stream` and returns FG_ERR_TIMEOUT when the last call's status word is
+ * set, FG_OK otherwise (FG_ERR_CUDA when the read fails); it allocates
+ * nothing either.  Call it outside stream capture, after the call whose
+ * status it reads and before the next one. */
 #define FG_NOALLOC_MAX_CELLS (1 << 20)
 int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x, int num_y,
                        int pitch, float density, float h, float dt, int num_iters,
                        float jacobi_omega, float pressure_damping, int tb_depth, int early_exit,
                        float tolerance, void* stream);
+int fg_project_noalloc_status(void* stream);
 
 /* Differentiable rollouts: a Step / StepAdjoint pair standing in for an
  * autograd Function (no counterpart in the reference, which has no
@@ -250,8 +272,9 @@ int fg_project_noalloc(float* u, float* v, float* p, const float* s, int num_x, 
  *
  * fg_tape_begin(f, max_steps, every) starts a recorded rollout from the
  * current state and saves it as the first checkpoint.  It needs the JACOBI
- * scheme with early_exit 0, refine_sweeps 0 and viscosity_diffusion 0
- * (else FG_ERR_UNSUPPORTED); the parameters, the sources and
+ * scheme with early_exit 0 and viscosity_diffusion 0 (else
+ * FG_ERR_UNSUPPORTED); the outer correction (refine_sweeps > 0) and
+ * precise_coords are differentiated.  The parameters, the sources and
  * the state must not change until fg_tape_end (else FG_ERR_INVALID).
  *
  * fg_step_forward(f, dt, force_u, force_v) runs one step with the force
@@ -370,7 +393,12 @@ const char* fg_last_error(const fg_fluid* f);
  * fg_debug_stall_tile(f, t): the dataflow Jacobi kernel never publishes tile
  * t of the handle's solves, so the tiles that read it wait until their
  * bounded waits (about a second) give up; the step's fg_get_stats returns
- * FG_ERR_TIMEOUT.  t < 0 disarms.  Changes the handle's captured graphs. */
+ * FG_ERR_TIMEOUT.  t < 0 disarms.  Changes the handle's captured graphs.
+ * fg_debug_stall_tile(NULL, t): in later fg_project_noalloc calls, the
+ * TMA-fed Jacobi kernel's copy barrier of tile t expects 16 bytes more than
+ * its copies bring, so the block that sweeps tile t gives up after its
+ * bounded waits (about nine seconds) and fg_project_noalloc_status returns
+ * FG_ERR_TIMEOUT; every copy issued still lands.  t < 0 disarms. */
 int fg_debug_fail_alloc(int n);
 int fg_debug_stall_tile(fg_fluid* f, int tile);
 

@@ -41,7 +41,7 @@
 
 namespace orc {
 
-enum Scheme { LexSOR = 0, Jacobi = 1, RedBlack = 2 };
+enum Scheme { LexSOR = 0, Jacobi = 1, RedBlack = 2, MgJacobi = 3 };
 
 // ---------------------------------------------------------------------------
 // Thread pool standing in for parallelRange (pkg/fluid/parallel.go:10-39):
@@ -170,6 +170,9 @@ struct Fluid {
   T jacobi_omega = 1;       // relaxation of the parallel schemes
   int check_every = 1;      // early-exit check interval (sweeps) of the parallel schemes
   int refine_sweeps = 0;    // FP64-residual outer correction sweeps (0 = off)
+  // Departure points of the advection relative to their face (the GPU's
+  // fg_params.precise_coords); off: the reference's absolute coordinates.
+  bool precise_coords = false;
 
   // Parallel-scheme work arrays.
   std::vector<T> phi, phi2, rhs, err, err2;
@@ -301,11 +304,11 @@ struct Fluid {
   //   phi' = (1 - om) phi + w_c (nb + b_c),   w_c = om / s_c,  om = omega * damping,
   // evaluated as fma(w_c, nb, bw_c) with bw_c = w_c * b_c precomputed (and an
   // outer fma with 1 - om when om != 1); W = BW = 0 off the active cells.
-  void setupSystem() {
+  void setupSystem() { setupSystemOm(jacobi_omega * PressureDamping); }
+  void setupSystemOm(T om) {
     int n = NY;
     phi.assign(N, 0); phi2.assign(N, 0); rhs.assign(N, 0); cnt.assign(N, 0);
     Wc.assign(N, 0); BWc.assign(N, 0);
-    T om = jacobi_omega * PressureDamping;
     par(1, NX - 1, [&](int i) {
       for (int j = 1; j < NY - 1; ++j) {
         int c = i * n + j;
@@ -401,9 +404,167 @@ struct Fluid {
     }
     return done;
   }
+  // ---------------------------------------------------------------- multigrid Jacobi
+  // The GPU's parallel V-cycle (scheme MgJacobi) for the same system
+  // s_c phi_c - sum_n phi_n = b_c: levels of half the interior size (a
+  // coarse cell is fluid if any of its up to 2 x 2 children is; the ghost
+  // ring coarsens along its own row or column), damped Jacobi smoothing
+  // (weight kMgOmega * PressureDamping, the Jacobi scheme's per-cell
+  // arithmetic), the residuals of the children summed into the coarse
+  // right-hand side, and the coarse correction interpolated back bilinearly
+  // (weights 9, 3, 3, 1 over the active coarse cells around the child).
+  // V(2, 2) cycles, 32 sweeps on the coarsest level (interior side <= 8).
+  static constexpr float kMgOmega = 0.8f;
+  static constexpr int kMgPre = 2, kMgPost = 2, kMgCoarse = 32, kMgMinSide = 8;
+  struct MgLevel {
+    int NX, NY;
+    std::vector<T> S, w, b, bw, x, tmp;
+    std::vector<uint8_t> cnt;
+  };
+  std::vector<MgLevel> mg;
+  // Children rows of coarse row I (fine rows of NXf): the ring row for the
+  // ring, else the interior rows 2I-1 and 2I that exist.
+  static void mgChildren(int I, int NXc, int NXf, int& a, int& b) {
+    if (I == 0) { a = b = 0; return; }
+    if (I == NXc - 1) { a = b = NXf - 1; return; }
+    a = 2 * I - 1;
+    b = std::min(2 * I, NXf - 2);
+  }
+  void mgCounts(MgLevel& L, T om) {
+    int n = L.NY;
+    L.cnt.assign((size_t)L.NX * n, 0);
+    L.w.assign((size_t)L.NX * n, 0);
+    for (int i = 1; i < L.NX - 1; ++i)
+      for (int j = 1; j < L.NY - 1; ++j) {
+        int c = i * n + j;
+        if (L.S[c] == 0) continue;
+        T s = L.S[c - n] + L.S[c + n] + L.S[c - 1] + L.S[c + 1];
+        if (s == 0) continue;
+        L.cnt[c] = (uint8_t)s;
+        L.w[c] = om / s;
+      }
+  }
+  void mgBuild(T om) {
+    mg.assign(1, MgLevel());
+    MgLevel& L0 = mg[0];
+    L0.NX = NX; L0.NY = NY;
+    L0.S = S; L0.cnt = cnt; L0.w = Wc; L0.b = rhs; L0.bw = BWc;
+    L0.x.assign(N, 0); L0.tmp.assign(N, 0);
+    while (std::min(mg.back().NX, mg.back().NY) - 2 > kMgMinSide) {
+      const MgLevel& F = mg.back();
+      MgLevel C;
+      C.NX = (F.NX - 2 + 1) / 2 + 2;
+      C.NY = (F.NY - 2 + 1) / 2 + 2;
+      C.S.assign((size_t)C.NX * C.NY, 0);
+      for (int I = 0; I < C.NX; ++I)
+        for (int J = 0; J < C.NY; ++J) {
+          int a0, a1, b0, b1;
+          mgChildren(I, C.NX, F.NX, a0, a1);
+          mgChildren(J, C.NY, F.NY, b0, b1);
+          T v = 0;
+          for (int a = a0; a <= a1; ++a)
+            for (int b = b0; b <= b1; ++b) v = std::max(v, F.S[a * F.NY + b]);
+          C.S[I * C.NY + J] = v;
+        }
+      mgCounts(C, om);
+      size_t nc = (size_t)C.NX * C.NY;
+      C.b.assign(nc, 0); C.bw.assign(nc, 0); C.x.assign(nc, 0); C.tmp.assign(nc, 0);
+      mg.push_back(std::move(C));
+    }
+  }
+  void mgSmooth(MgLevel& L, int ns, bool zero, T om1) {
+    int n = L.NY;
+    if (zero) std::fill(L.x.begin(), L.x.end(), (T)0);
+    for (int t = 0; t < ns; ++t) {
+      par(1, L.NX - 1, [&](int i) {
+        for (int j = 1; j < L.NY - 1; ++j) {
+          int c = i * n + j;
+          T nb = L.x[c - n] + L.x[c + n] + L.x[c - 1] + L.x[c + 1];
+          T y = std::fma(L.w[c], nb, L.bw[c]);
+          if (om1 != 0) y = std::fma(om1, L.x[c], y);
+          L.tmp[c] = y;
+        }
+      });
+      std::swap(L.x, L.tmp);
+    }
+  }
+  void mgRestrict(const MgLevel& F, MgLevel& C) {
+    int nf = F.NY, nc = C.NY;
+    par(1, C.NX - 1, [&](int I) {
+      for (int J = 1; J < C.NY - 1; ++J) {
+        int cc = I * nc + J;
+        T rs = 0;
+        if (C.cnt[cc]) {
+          int a0, a1, b0, b1;
+          mgChildren(I, C.NX, F.NX, a0, a1);
+          mgChildren(J, C.NY, F.NY, b0, b1);
+          for (int a = a0; a <= a1; ++a)
+            for (int b = b0; b <= b1; ++b) {
+              int cf = a * nf + b;
+              if (!F.cnt[cf]) continue;
+              T nb = F.x[cf - nf] + F.x[cf + nf] + F.x[cf - 1] + F.x[cf + 1];
+              T ax = (T)F.cnt[cf] * F.x[cf] - nb;
+              rs = rs + (F.b[cf] - ax);
+            }
+        }
+        C.b[cc] = rs;
+        C.bw[cc] = C.w[cc] * rs;
+      }
+    });
+  }
+  void mgProlong(const MgLevel& C, MgLevel& F) {
+    int nf = F.NY, nc = C.NY;
+    par(1, F.NX - 1, [&](int i) {
+      for (int j = 1; j < F.NY - 1; ++j) {
+        int cf = i * nf + j;
+        if (!F.cnt[cf]) continue;
+        int I = (i - 1) / 2 + 1, J = (j - 1) / 2 + 1;
+        int di = ((i - 1) & 1) ? 1 : -1, dj = ((j - 1) & 1) ? 1 : -1;
+        const int ci[4] = {I, I + di, I, I + di}, cj[4] = {J, J, J + dj, J + dj};
+        const T wt[4] = {(T)9, (T)3, (T)3, (T)1};
+        T num = 0, den = 0;
+        for (int k = 0; k < 4; ++k) {
+          int cc = ci[k] * nc + cj[k];
+          if (!C.cnt[cc]) continue;
+          num = num + wt[k] * C.x[cc];
+          den = den + wt[k];
+        }
+        T e = den > 0 ? num / den : (T)0;
+        F.x[cf] = F.x[cf] + e;
+      }
+    });
+  }
+  void mgCycle(int l, bool zero, T om1) {
+    MgLevel& L = mg[l];
+    if (l == (int)mg.size() - 1) {
+      mgSmooth(L, kMgCoarse, true, om1);
+      return;
+    }
+    mgSmooth(L, kMgPre, zero, om1);
+    mgRestrict(L, mg[l + 1]);
+    mgCycle(l + 1, true, om1);
+    mgProlong(mg[l + 1], L);
+    mgSmooth(L, kMgPost, false, om1);
+  }
+  void solveMg(int numCycles, T dt) {
+    T om = (T)kMgOmega * PressureDamping;
+    setupSystemOm(om);
+    mgBuild(om);
+    for (int k = 0; k < numCycles; ++k) mgCycle(0, k == 0, (T)1 - om);
+    phi = mg[0].x;
+    st.sweeps = numCycles;
+    st.last_maxdiv = 0;
+    residualFP64();
+    gradientAndPressure(dt);
+  }
+
   void solveParallel(int numIters, T dt) {
-    int n = NY;
+    if (scheme == MgJacobi) {
+      solveMg(numIters, dt);
+      return;
+    }
     T cp = density * h / dt;
+    (void)cp;
     setupSystem();
     st.sweeps = relax(rhs, BWc, phi, phi2, numIters, true);
     residualFP64();
@@ -426,7 +587,12 @@ struct Fluid {
       // Statistics: the residual of the final potential.
       residualFP64();
     }
-    // Gradient subtract + pressure.
+    gradientAndPressure(dt);
+  }
+  // Gradient subtract + pressure from the potential phi.
+  void gradientAndPressure(T dt) {
+    int n = NY;
+    T cp = density * h / dt;
     par(1, NX, [&](int i) {
       for (int j = 1; j < NY - 1; ++j) {
         int c = i * n + j;
@@ -619,6 +785,46 @@ struct Fluid {
            tx * ty * data[x1 * n + y1] + sx * ty * data[x0 * n + y1];
   }
 
+  // Sample at the departure point of face / cell (i, j) moved by (-su, -sv)
+  // (su, sv: the products dt * u, dt * v; fld as sampleFrom, whose
+  // staggering is also the face's offset in the cell).  Without
+  // precise_coords the point is formed in absolute coordinates exactly as
+  // the reference forms it (fluid.go:304-330, 411-414, 940-960); with it,
+  // as index plus offset in cells, (i + a, j + b), a = -su / h: the floor
+  // and the weights are taken from the small offset, exact to the float
+  // precision of the displacement.
+  T sampleDep(int i, int j, T su, T sv, const std::vector<T>& data, int fld) const {
+    const bool hx = fld != 0, hy = fld != 1;
+    const T h2 = h / (T)2;
+    if (!precise_coords) {
+      T x = hx ? ((T)i * h + h2) - su : (T)i * h - su;
+      T y = hy ? ((T)j * h + h2) - sv : (T)j * h - sv;
+      return sampleFrom(x, y, data, fld);
+    }
+    const int n = NY;
+    const T h1 = (T)1.0 / h;
+    const T dxr = hx ? (T)0.5 : (T)0, dyr = hy ? (T)0.5 : (T)0;
+    T a = -su * h1, b = -sv * h1;
+    a = std::fmax(std::fmin(a, (T)(NX - i) - dxr), (T)(1 - i) - dxr);
+    b = std::fmax(std::fmin(b, (T)(NY - j) - dyr), (T)(1 - j) - dyr);
+    T fa = std::floor(a), fb = std::floor(b);
+    int x0 = i + (int)fa, y0 = j + (int)fb;
+    T tx = a - fa, ty = b - fb;
+    if (x0 > NX - 1) {
+      x0 = NX - 1;
+      tx = a - (T)(x0 - i);
+    }
+    if (y0 > NY - 1) {
+      y0 = NY - 1;
+      ty = b - (T)(y0 - j);
+    }
+    int x1 = std::min(x0 + 1, NX - 1), y1 = std::min(y0 + 1, NY - 1);
+    T sx = (T)1.0 - tx;
+    T sy = (T)1.0 - ty;
+    return sx * sy * data[x0 * n + y0] + tx * sy * data[x1 * n + y0] +
+           tx * ty * data[x1 * n + y1] + sx * ty * data[x0 * n + y1];
+  }
+
   // fluid.go:291-333
   void advectVelocity(T dt) {
     copyBorder(newU, U);
@@ -629,22 +835,14 @@ struct Fluid {
     par(1, NX, [&](int i) {
       for (int j = 1; j < NY; ++j) {
         if (S[i * n + j] != 0 && S[(i - 1) * n + j] != 0 && j < NY - 1) {
-          T x = (T)i * hh;
-          T y = (T)j * hh + h2;
           T u = U[i * n + j];
           T v = avgV(V, i, j);
-          x = x - dt * u;
-          y = y - dt * v;
-          newU[i * n + j] = sampleFrom(x, y, U, 0);
+          newU[i * n + j] = sampleDep(i, j, dt * u, dt * v, U, 0);
         }
         if (S[i * n + j] != 0 && S[i * n + j - 1] != 0 && i < NX - 1) {
-          T x = (T)i * hh + h2;
-          T y = (T)j * hh;
           T u = avgU(U, i, j);
           T v = V[i * n + j];
-          x = x - dt * u;
-          y = y - dt * v;
-          newV[i * n + j] = sampleFrom(x, y, V, 1);
+          newV[i * n + j] = sampleDep(i, j, dt * u, dt * v, V, 1);
         }
       }
     });
@@ -663,9 +861,7 @@ struct Fluid {
         if (S[i * n + j] != 0) {
           T u = (U[i * n + j] + U[(i + 1) * n + j]) * (T)0.5 * SmokeAdvection;
           T v = (V[i * n + j] + V[i * n + j + 1]) * (T)0.5 * SmokeAdvection;
-          T x = (T)i * hh + h2 - dt * u;
-          T y = (T)j * hh + h2 - dt * v;
-          T smokeValue = sampleFrom(x, y, M, 2);
+          T smokeValue = sampleDep(i, j, dt * u, dt * v, M, 2);
           if (ViscosityDiffusion > 0) {
             T smokeDiffusion = ViscosityDiffusion * (T)0.3 * dt;
             T neighbors = M[(i - 1) * n + j] + M[(i + 1) * n + j] + M[i * n + j - 1] +
@@ -1007,18 +1203,12 @@ struct Fluid {
     par(1, NX, [&](int i) {
       for (int j = 1; j < NY; ++j) {
         if (S[i * n + j] != 0 && S[(i - 1) * n + j] != 0 && j < NY - 1) {
-          T x = (T)i * hh, y = (T)j * hh + h2;
           T u = U[i * n + j], v = avgV(V, i, j);
-          x = x + dt * u;
-          y = y + dt * v;
-          bwdU[i * n + j] = sampleFrom(x, y, fwdU, 0);
+          bwdU[i * n + j] = sampleDep(i, j, -dt * u, -dt * v, fwdU, 0);
         }
         if (S[i * n + j] != 0 && S[i * n + j - 1] != 0 && i < NX - 1) {
-          T x = (T)i * hh + h2, y = (T)j * hh;
           T u = avgU(U, i, j), v = V[i * n + j];
-          x = x + dt * u;
-          y = y + dt * v;
-          bwdV[i * n + j] = sampleFrom(x, y, fwdV, 1);
+          bwdV[i * n + j] = sampleDep(i, j, -dt * u, -dt * v, fwdV, 1);
         }
       }
     });
@@ -1057,9 +1247,7 @@ struct Fluid {
         if (S[i * n + j] != 0) {
           T u = (U[i * n + j] + U[(i + 1) * n + j]) * (T)0.5 * SmokeAdvection;
           T v = (V[i * n + j] + V[i * n + j + 1]) * (T)0.5 * SmokeAdvection;
-          T x = (T)i * hh + h2 + dt * u;
-          T y = (T)j * hh + h2 + dt * v;
-          bwdM[i * n + j] = sampleFrom(x, y, fwdM, 2);
+          bwdM[i * n + j] = sampleDep(i, j, -dt * u, -dt * v, fwdM, 2);
         }
       }
     });
@@ -1822,6 +2010,7 @@ int orc_set_param(void* p, const char* name, double value) {
     else if (k == "jacobi_omega") f.jacobi_omega = (T)value;
     else if (k == "check_every") f.check_every = std::max(1, (int)value);
     else if (k == "refine_sweeps") f.refine_sweeps = (int)value;
+    else if (k == "precise_coords") f.precise_coords = value != 0;
     else return -1;
     return 0;
   });
@@ -1846,6 +2035,7 @@ double orc_get_param(void* p, const char* name) {
     if (k == "jacobi_omega") return f.jacobi_omega;
     if (k == "check_every") return f.check_every;
     if (k == "refine_sweeps") return f.refine_sweeps;
+    if (k == "precise_coords") return f.precise_coords ? 1 : 0;
     if (k == "h") return f.h;
     if (k == "density") return f.density;
     return std::nan("");

@@ -115,9 +115,9 @@ _PARAMS = (
     "Confinement", "ViscosityDiffusion", "PressureDamping", "TurbulenceStrength",
     "SmokeAdvection", "UseMultigrid", "MultigridLevels", "UseBFECC", "Relaxation",
     "num_iters", "tolerance", "early_exit", "scheme", "jacobi_omega", "check_every",
-    "refine_sweeps",
+    "refine_sweeps", "precise_coords",
 )
-_BOOL_PARAMS = ("UseMultigrid", "UseBFECC", "early_exit")
+_BOOL_PARAMS = ("UseMultigrid", "UseBFECC", "early_exit", "precise_coords")
 _INT_PARAMS = ("MultigridLevels", "num_iters", "scheme", "check_every", "refine_sweeps")
 
 

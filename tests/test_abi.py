@@ -72,3 +72,15 @@ def test_oversized_grids_are_rejected_before_any_device_call():
     rc = L.fg_project_noalloc(dummy, dummy, dummy, dummy, 3, 3, 2 ** 30, 1.0, 1.0, 0.1, 8,
                               1.0, 1.0, 8, 0, 1e-5, None)
     assert rc == _lib.FG_ERR_TOO_LARGE
+
+
+def test_noalloc_sweep_counts_near_int_max_are_rejected():
+    """The allocation-free projection's launch count is formed in 64 bits: a
+    num_iters near 2^31 must not wrap below the 4096-launch limit (it is
+    refused before any device call, so this runs without a GPU)."""
+    L = _lib.load()
+    dummy = ctypes.c_void_p(256)
+    for iters, tb in ((2 ** 31 - 1, 8), (2 ** 31 - 1, 1), (2 ** 31 - 8, 4), (4096 * 8 + 1, 8)):
+        rc = L.fg_project_noalloc(dummy, dummy, dummy, dummy, 16, 16, 16, 1.0, 1.0, 0.1, iters,
+                                  1.0, 1.0, tb, 0, 1e-5, None)
+        assert rc == _lib.FG_ERR_TOO_LARGE, (iters, tb, rc)

@@ -127,9 +127,9 @@ def gpu_loss(gpu, U0, V0, M0, forces, target, steps=STEPS, **extra):
     return loss
 
 
-def oracle_loss(U0, V0, M0, forces, target, steps=STEPS, S=None, bfecc=True, conf=0.0):
+def oracle_loss(U0, V0, M0, forces, target, steps=STEPS, S=None, bfecc=True, conf=0.0, **extra):
     o = OracleFluid(1.0, W, H, 1.0, prec=64, scheme=1, num_iters=ITERS, check_every=8,
-                    early_exit=False, UseBFECC=bfecc, Confinement=conf)
+                    early_exit=False, UseBFECC=bfecc, Confinement=conf, **extra)
     o.S[:] = S
     o.U[:] = U0
     o.V[:] = V0
@@ -242,6 +242,45 @@ def test_directional_derivative_with_confinement(gpu, problem, k):
     assert g == pytest.approx(fd, rel=1e-3, abs=5e-6)
 
 
+REFINED = dict(refine_sweeps=8, precise_coords=True)
+
+
+@pytest.fixture(scope="module")
+def problem_refined(gpu):
+    f = make_gpu(gpu, **REFINED)
+    S = f.S.astype(np.float64).copy()
+    U0, V0, M0 = initial_state(f, seed=12)
+    forces = seeded_forces(f.numCells, STEPS, seed=8)
+    target = target_field(f.NumX, f.NumY, seed=5)
+    _, out = gpu_rollout(gpu, U0, V0, M0, forces, target, **REFINED)
+    return dict(S=S, U0=U0, V0=V0, M0=M0, forces=forces, target=target, out=out)
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_directional_derivative_with_outer_correction(gpu, problem_refined, k):
+    """The headline forward's chosen forms in a recorded rollout: the 8-sweep
+    outer correction of the potential (its adjoint: the correction solve on
+    the adjoint right-hand side, then the main solve on that solve's
+    residual) and face-relative departure points.  Directional derivatives
+    against FP64 central differences of the oracle's forward pass with the
+    same settings."""
+    p = problem_refined
+    dU, dV, dF = directions(W + 2, H + 2, p["S"], k, seed=31)
+    g = directional(p["out"], dU, dV, dF)
+    eps = 1e-6
+    f64 = [(fu.astype(np.float64), fv.astype(np.float64)) for fu, fv in p["forces"]]
+
+    def at(s):
+        fs = [(fu + s * du, fv + s * dv) for (fu, fv), (du, dv) in zip(f64, dF)]
+        return oracle_loss(p["U0"] + s * dU, p["V0"] + s * dV, p["M0"], fs, p["target"],
+                           S=p["S"], **REFINED)
+
+    fd = (at(eps) - at(-eps)) / (2 * eps)
+    print("direction %d (outer correction): adjoint %.8g  fp64 central difference %.8g"
+          % (k, g, fd))
+    assert g == pytest.approx(fd, rel=1e-3, abs=5e-6)
+
+
 def test_smoke_gradient_vs_fp64_central_differences(gpu, problem):
     """Relative perturbations of the initial smoke: cells whose smoke is 0
     (where max(s, 0) has a kink, so central differences see half a slope)
@@ -315,10 +354,14 @@ def test_reverse_pass_restores_final_state(gpu, problem):
     f.tape_end()
 
 
-def test_recorded_steps_equal_simulate(gpu, problem):
+@pytest.mark.parametrize("extra", [{}, {"refine_sweeps": 8, "precise_coords": True}],
+                         ids=["plain", "refined"])
+def test_recorded_steps_equal_simulate(gpu, problem, extra):
+    """Recorded steps (the BFECC passes written to the tape, the potential
+    stored with its outer correction) equal fg_simulate's bit for bit."""
     p = problem
-    a = make_gpu(gpu, TurbulenceStrength=0.05)
-    b = make_gpu(gpu, TurbulenceStrength=0.05)
+    a = make_gpu(gpu, TurbulenceStrength=0.05, **extra)
+    b = make_gpu(gpu, TurbulenceStrength=0.05, **extra)
     for f in (a, b):
         jet_sources(f)
         f.U[:], f.V[:], f.M[:] = p["U0"], p["V0"], p["M0"]
@@ -496,14 +539,18 @@ def test_rollout256_fp32_central_differences_32_directions(gpu, rollout256):
 
 
 # ------------------------------------------------------------------ 64^2 vs the FP64 reverse mode
-def test_rollout64_gradient_fields_vs_fp64_reference_adjoint(gpu):
+@pytest.mark.parametrize("precise", [False, True])
+def test_rollout64_gradient_fields_vs_fp64_reference_adjoint(gpu, precise):
     """64^2 jet, 64 steps, BFECC, 60 sweeps, checkpoint every 8: every
     gradient field (initial U, V, M and all 64 x 2 force fields) against the
     oracle's FP64 reverse mode of the same rollout.  The GPU trajectory is
-    FP32, so the fields agree to FP32 accuracy, not bit for bit."""
+    FP32, so the fields agree to FP32 accuracy, not bit for bit.  With
+    precise_coords the forward and adjoint samples take their weights from
+    face-relative offsets (the FP64 reverse mode's absolute coordinates are
+    exact enough for either)."""
     side, steps = 64, 64
     f = gpu.Fluid(1.0, side, side, 1.0, auto_sync=False, scheme=1, num_iters=R_ITERS,
-                  tb_depth=8, early_exit=False, UseBFECC=True)
+                  tb_depth=8, early_exit=False, UseBFECC=True, precise_coords=precise)
     scenes.jet_rollout_scene(f)
     n = f.numCells
     target = scenes.gaussian_target(f.NumX, f.NumY, seed=4, sigma=(2.5, 7.5))

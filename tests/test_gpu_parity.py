@@ -90,6 +90,99 @@ def test_all_stages_bitwise_lexsor(gpu):
     assert_bitwise(g, o)
 
 
+@pytest.mark.parametrize("amp,dt", [(0.5, 0.1), (20.0, 0.5)])
+def test_bfecc_displacements_bitwise(gpu, amp, dt):
+    """BFECC advection with departure points within a cell and many cells
+    away (clamped at the walls), smoke diffusion, confinement, an obstacle
+    and a grid that is no multiple of the thread blocks: every field stays
+    bit for bit the oracle's."""
+    g, o = both(gpu, 95, 70, num_iters=10, UseBFECC=True, ViscosityDiffusion=0.05,
+                Confinement=0.1)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        f.SetCircularObstacle(40, 35, 7)
+        scenes.random_state(f, seed=8, amp=amp)
+    for _ in range(3):
+        for f in (g, o):
+            f.Simulate(dt)
+    assert_bitwise(g, o)
+
+
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_precise_coords_bitwise(gpu, scheme):
+    """precise_coords: advection departure points as face index plus a
+    displacement in cells.  The oracle restates the same arithmetic, so
+    every field stays bit for bit its own: BFECC and plain steps, smoke
+    diffusion, an obstacle, displacements below a cell and of several."""
+    params = dict(scheme=scheme, num_iters=20, precise_coords=True, ViscosityDiffusion=0.05)
+    if scheme == 1:
+        params.update(tb_depth=4, early_exit=False, refine_sweeps=4)
+    for bfecc, amp, dt in ((True, 0.5, 0.1), (True, 6.0, 0.5), (False, 3.0, 0.5)):
+        g, o = both(gpu, 95, 70, UseBFECC=bfecc, **params)
+        for f in (g, o):
+            scenes.jet_scene(f)
+            f.SetCircularObstacle(40, 35, 7)
+            scenes.random_state(f, seed=9, amp=amp)
+        for _ in range(3):
+            for f in (g, o):
+                scenes.jet_inject(f, speed=2.0)
+                f.Simulate(dt)
+        assert_bitwise(g, o, where="BFECC %s amp %g" % (bfecc, amp))
+
+
+@pytest.mark.parametrize("w,h,cycles", [(70, 45, 2), (95, 70, 3), (333, 222, 2), (9, 30, 1),
+                                         (1100, 1500, 1)])
+def test_multigrid_jacobi_bitwise(gpu, w, h, cycles):
+    """The MULTIGRID scheme (parallel V(2,2) cycles: damped Jacobi smoothing,
+    summed residuals, bilinear correction, levels down to a side of 8)
+    against the oracle's restatement, bit for bit: odd and even sizes, a
+    grid with one coarse level, an obstacle, BFECC, confinement."""
+    g, o = both(gpu, w, h, scheme=3, num_iters=cycles, early_exit=False, UseBFECC=True,
+                Confinement=0.1)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        f.SetCircularObstacle(w // 3, h // 2, max(2, min(w, h) // 8))
+    for _ in range(3):
+        for f in (g, o):
+            scenes.jet_inject(f, speed=2.0)
+            f.Simulate(0.1)
+    assert_bitwise(g, o, where="%dx%d" % (w, h))
+    sg, so = g.stats(), o.stats()
+    assert sg["sweeps"] == so["sweeps"] == cycles
+    assert sg["resid_l2"] == pytest.approx(so["resid_l2"], rel=1e-9, abs=1e-12)
+
+
+def test_multigrid_jacobi_residual_below_200_sweeps(gpu):
+    """On a 512^2 lid-driven cavity one V-cycle leaves a smaller pressure
+    residual than 200 Jacobi sweeps, and each further cycle shrinks it by
+    about ten."""
+    res = {}
+    for name, kw in (("jacobi200", dict(scheme=1, num_iters=200, tb_depth=8)),
+                     ("mg1", dict(scheme=3, num_iters=1)), ("mg2", dict(scheme=3, num_iters=2))):
+        f = gpu.Fluid(1.0, 512, 512, 1.0, auto_sync=False, early_exit=False, UseBFECC=True, **kw)
+        scenes.fast_walls(f, top=True, bottom=True, left=True, right=True)
+        f.mark_dirty()
+        i = np.arange(2, f.NumX - 2, dtype=np.int32)
+        f.set_sources(i, np.full_like(i, f.NumY - 2), u=1.0, v=0.0,
+                      mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY)
+        for _ in range(3):
+            f.Simulate(0.1)
+        res[name] = f.stats()["resid_l2"]
+    print("resid_l2 after 3 steps:", res)
+    assert res["mg1"] < res["jacobi200"]
+    assert res["mg2"] < res["mg1"] / 5
+
+
+def test_multigrid_rejects_refinement_and_tiny_grids(gpu):
+    from fluid_gb300 import FluidError
+
+    with pytest.raises(FluidError):
+        gpu.Fluid(1.0, 64, 64, 1.0, scheme=3, refine_sweeps=4)
+    f = gpu.Fluid(1.0, 6, 40, 1.0, scheme=3, num_iters=1)
+    with pytest.raises(FluidError):
+        f.Simulate(0.1)
+
+
 def test_early_exit_matches(gpu):
     g, o = both(gpu, 30, 20, num_iters=40)
     for f in (g, o):
