@@ -442,7 +442,9 @@ def multigrid_leg(fluid_gb300, f, args):
         for _ in range(max(3, args.warmup)):
             g.Simulate(DT)
         l0 = g.launch_count()
+        prof = profile_leg(args, "multigrid")
         ms = device_ms(stream, lambda: g.Simulate(DT), args.steps)
+        prof()
         launches = (g.launch_count() - l0) / args.steps
         out["cycles_%d" % cycles] = {
             "value": W * H / ms / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms,
@@ -977,9 +979,9 @@ def cpu_app_rows(threads, warm=3, timed=3):
 def cpu_reference_steps(steps, threads, warmup=0, budget_s=None):
     """Times the reference algorithm (FP32, serial SOR pressure, parallelRange
     stages on `threads` host threads) on the cavity workload: `warmup`
-    untimed steps, then up to `steps` timed ones on the same state (fewer
-    when `budget_s` seconds, estimated from the last warm-up step, would
-    not hold them all)."""
+    untimed steps, then up to `steps` timed ones on the same state (fewer,
+    but at least 2, when `budget_s` seconds, estimated from the last warm-up
+    step, would not hold them all)."""
     from oracle.pyoracle import LEXSOR, OracleFluid
 
     o = OracleFluid(1.0, W, H, 1.0, prec=32, threads=threads, scheme=LEXSOR, num_iters=ITERS,
@@ -999,7 +1001,7 @@ def cpu_reference_steps(steps, threads, warmup=0, budget_s=None):
     for _ in range(warmup):
         last = step()
     if budget_s is not None and last is not None:
-        steps = max(1, min(steps, int(budget_s / max(last, 1e-3))))
+        steps = max(2, min(steps, int(budget_s / max(last, 1e-3))))
     return [step() for _ in range(steps)]
 
 
@@ -1010,10 +1012,13 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     # Each step is one full 2048^2 step of the reference algorithm (~seconds
-    # on the host): W warm-up steps (1 to 10), then the timed steps on the
-    # same state, their count bounded so the whole run ends in minutes.
+    # on the host, growing as the flow develops): W warm-up steps (1 to 10),
+    # then timed steps on the same state, at least 2 and as many as
+    # --cpu-budget seconds hold -- the protocol of the main arm's
+    # cpu_baseline, so the two agree.
     warmup = max(1, min(args.warmup, 10))
-    times = cpu_reference_steps(args.steps, threads, warmup=warmup, budget_s=90.0)
+    times = cpu_reference_steps(max(2, min(args.steps, args.cpu_steps)), threads, warmup=warmup,
+                                budget_s=args.cpu_budget)
     sec = sum(times)
     value = W * H * len(times) / sec / 1e6
     line = {
@@ -1226,7 +1231,8 @@ def main():
     ap.add_argument("--no-rollout", action="store_true")
     ap.add_argument("--no-app", action="store_true",
                     help="skip the multigrid, particle, rendering and view rows")
-    ap.add_argument("--profile-leg", choices=["adjoint", "ensemble", "app"], default=None,
+    ap.add_argument("--profile-leg", choices=["adjoint", "ensemble", "app", "multigrid"],
+                    default=None,
                     help="bracket that leg's timed region for ncu --profile-from-start off")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

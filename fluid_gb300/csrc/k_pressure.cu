@@ -2575,15 +2575,15 @@ __global__ void k_mg_weights(const uint8_t* __restrict__ flags, float* __restric
   w[i * g.P + j] = flag_active(fl) ? om / (float)flag_count(fl) : 0.0f;
 }
 
-// Coarse right-hand side: the sum of the active children's residuals
-// b - (s x - (x_w + x_e + x_s + x_n)), and w * b.
-__global__ void k_mg_restrict(const float* __restrict__ xf, const float* __restrict__ bf,
-                              const uint8_t* __restrict__ flf, Grid gf,
-                              const uint8_t* __restrict__ flc, const float* __restrict__ wc,
-                              float* __restrict__ bc, float* __restrict__ bwc, Grid gc) {
-  int J = blockIdx.x * blockDim.x + threadIdx.x;
-  int I = blockIdx.y * blockDim.y + threadIdx.y;
-  if (I < 1 || J < 1 || I > gc.NX - 2 || J > gc.NY - 2) return;
+// Coarse right-hand side at coarse cell (I, J): the sum of the active
+// children's residuals b - (s x - (x_w + x_e + x_s + x_n)), and w * b.
+__device__ __forceinline__ void mg_restrict_cell(int I, int J, const float* __restrict__ xf,
+                                                 const float* __restrict__ bf,
+                                                 const uint8_t* __restrict__ flf, const Grid& gf,
+                                                 const uint8_t* __restrict__ flc,
+                                                 const float* __restrict__ wc,
+                                                 float* __restrict__ bc, float* __restrict__ bwc,
+                                                 const Grid& gc) {
   const int cc = I * gc.P + J;
   float rs = 0.0f;
   if (flag_active(flc[cc])) {
@@ -2603,14 +2603,22 @@ __global__ void k_mg_restrict(const float* __restrict__ xf, const float* __restr
   bc[cc] = rs;
   bwc[cc] = wc[cc] * rs;
 }
+__global__ void k_mg_restrict(const float* __restrict__ xf, const float* __restrict__ bf,
+                              const uint8_t* __restrict__ flf, Grid gf,
+                              const uint8_t* __restrict__ flc, const float* __restrict__ wc,
+                              float* __restrict__ bc, float* __restrict__ bwc, Grid gc) {
+  int J = blockIdx.x * blockDim.x + threadIdx.x;
+  int I = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I < 1 || J < 1 || I > gc.NX - 2 || J > gc.NY - 2) return;
+  mg_restrict_cell(I, J, xf, bf, flf, gf, flc, wc, bc, bwc, gc);
+}
 
 // x_f += the bilinear interpolation of x_c over the active coarse cells
-// around each active fine cell.
-__global__ void k_mg_prolong(const float* __restrict__ xc, const uint8_t* __restrict__ flc, Grid gc,
-                             float* __restrict__ xf, const uint8_t* __restrict__ flf, Grid gf) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i < 1 || j < 1 || i > gf.NX - 2 || j > gf.NY - 2) return;
+// around the active fine cell (i, j).
+__device__ __forceinline__ void mg_prolong_cell(int i, int j, const float* __restrict__ xc,
+                                                const uint8_t* __restrict__ flc, const Grid& gc,
+                                                float* __restrict__ xf,
+                                                const uint8_t* __restrict__ flf, const Grid& gf) {
   const int cf = i * gf.P + j;
   if (!flag_active(flf[cf])) return;
   const int I = (i - 1) / 2 + 1, J = (j - 1) / 2 + 1;
@@ -2627,6 +2635,85 @@ __global__ void k_mg_prolong(const float* __restrict__ xc, const uint8_t* __rest
   }
   const float e = den > 0.0f ? num / den : 0.0f;
   xf[cf] = xf[cf] + e;
+}
+__global__ void k_mg_prolong(const float* __restrict__ xc, const uint8_t* __restrict__ flc, Grid gc,
+                             float* __restrict__ xf, const uint8_t* __restrict__ flf, Grid gf) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i < 1 || j < 1 || i > gf.NX - 2 || j > gf.NY - 2) return;
+  mg_prolong_cell(i, j, xc, flc, gc, xf, flf, gf);
+}
+
+// The bottom of the V-cycle in one block: levels l0 .. n-1 (their cells fit
+// in L2 many times over, and a launch per operation would cost more than
+// the work), with the same per-cell arithmetic as the launches above and
+// the Jacobi sweep kernel: zero-started pre-smoothing and restriction down
+// to the coarsest level, its sweeps, then prolongation and post-smoothing
+// back up.  Every level starts in buffer 0 and makes an even number of
+// sweeps, so its iterate ends in buffer 0.  Only interior cells are
+// written; the ghost rings stay 0 as the sweep kernel leaves them.
+constexpr int kMgFuseLevels = 12, kMgFuseThreads = 1024;
+struct MgFused {
+  Grid g[kMgFuseLevels];
+  const uint8_t* flags[kMgFuseLevels];
+  const float* w[kMgFuseLevels];
+  float* b[kMgFuseLevels];
+  float* bw[kMgFuseLevels];
+  float* x0[kMgFuseLevels];
+  float* x1[kMgFuseLevels];
+  int n;  // levels held (the first is l0)
+};
+
+__device__ __forceinline__ void mg_fused_sweeps(const MgFused& m, int l, int ns, bool zero,
+                                                float om1) {
+  const Grid& g = m.g[l];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kMgFuseThreads / 32;
+  for (int s = 0; s < ns; ++s) {
+    const float* xs = (s & 1) ? m.x1[l] : m.x0[l];
+    float* xd = (s & 1) ? m.x0[l] : m.x1[l];
+    const bool z = zero && s == 0;
+    for (int i = 1 + warp; i < g.NX - 1; i += nw)
+      for (int j = 1 + lane; j < g.NY - 1; j += 32) {
+        const int c = i * g.P + j;
+        float xc = 0.0f, nb;
+        if (!z) {
+          xc = xs[c];
+          nb = xs[c - g.P] + xs[c + g.P] + xs[c - 1] + xs[c + 1];
+        } else {
+          nb = 0.0f + 0.0f + 0.0f + 0.0f;
+        }
+        float y = __fmaf_rn(m.w[l][c], nb, m.bw[l][c]);
+        y = __fmaf_rn(om1, xc, y);
+        xd[c] = y;
+      }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kMgFuseThreads)
+    k_mg_bottom(const __grid_constant__ MgFused m, float om1) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kMgFuseThreads / 32;
+  const int last = m.n - 1;
+  for (int l = 0; l < last; ++l) {
+    mg_fused_sweeps(m, l, kMgPre, true, om1);
+    const Grid& gf = m.g[l];
+    const Grid& gc = m.g[l + 1];
+    for (int I = 1 + warp; I < gc.NX - 1; I += nw)
+      for (int J = 1 + lane; J < gc.NY - 1; J += 32)
+        mg_restrict_cell(I, J, m.x0[l], m.b[l], m.flags[l], gf, m.flags[l + 1], m.w[l + 1],
+                         m.b[l + 1], m.bw[l + 1], gc);
+    __syncthreads();
+  }
+  mg_fused_sweeps(m, last, kMgCoarse, true, om1);
+  for (int l = last - 1; l >= 0; --l) {
+    const Grid& gf = m.g[l];
+    const Grid& gc = m.g[l + 1];
+    for (int i = 1 + warp; i < gf.NX - 1; i += nw)
+      for (int j = 1 + lane; j < gf.NY - 1; j += 32)
+        mg_prolong_cell(i, j, m.x0[l + 1], m.flags[l + 1], gc, m.x0[l], m.flags[l], gf);
+    __syncthreads();
+    mg_fused_sweeps(m, l, kMgPost, false, om1);
+  }
 }
 
 inline dim3 level_grid(const Grid& g) { return dim3((g.NY + BX - 1) / BX, (g.NX + BY - 1) / BY); }
@@ -2648,12 +2735,14 @@ void mg_sweeps(cudaStream_t st, const MgLevelDev& v, const float* src, float* ds
 // The V-cycles of one solve.  cur[l] names the buffer of level l holding
 // its iterate; the last smoothing of level 0 reports to the main control
 // block (sweeps = cycles, sel = the buffer of the result).
+constexpr int kMgFuseCells = 20000;  // levels of at most this many cells run in k_mg_bottom
 struct MgRun {
   fg_fluid* f;
   MgHier* h;
   float om1;
   int cycles;
   std::vector<int> cur;
+  int bottom;  // the first level run by k_mg_bottom (levels below it included)
   int launches = 0;
   void smooth(int l, int ns, bool zero, bool last) {
     MgLevelDev& v = h->lv[l];
@@ -2666,6 +2755,24 @@ struct MgRun {
   }
   void cycle(int l, bool zero, bool last) {
     const int L = (int)h->lv.size();
+    if (l == bottom) {
+      MgFused m{};
+      m.n = L - l;
+      for (int k = 0; k < m.n; ++k) {
+        const MgLevelDev& v = h->lv[l + k];
+        m.g[k] = v.g;
+        m.flags[k] = v.flags;
+        m.w[k] = v.w;
+        m.b[k] = v.b;
+        m.bw[k] = v.bw;
+        m.x0[k] = v.x[0];
+        m.x1[k] = v.x[1];
+      }
+      k_mg_bottom<<<1, kMgFuseThreads, 0, f->stream>>>(m, om1);
+      cur[l] = 0;
+      ++launches;
+      return;
+    }
     if (l == L - 1) {
       for (int k = 0; k < kMgCoarse / TMAX; ++k) smooth(l, TMAX, zero && k == 0, false);
       return;
@@ -2689,7 +2796,16 @@ cudaError_t mg_solve(fg_fluid* f, int cycles, float om) {
   if (!h || h->lv.size() < 2) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(h->ctl, 0, sizeof(PCtl), f->stream);
   if (e != cudaSuccess) return e;
-  MgRun run{f, h, 1.0f - om, cycles, std::vector<int>(h->lv.size(), 0)};
+  // The first coarse level small enough for one block (with at most
+  // kMgFuseLevels levels from it down).
+  const int L = (int)h->lv.size();
+  int bottom = L;
+  for (int l = 1; l < L; ++l)
+    if ((long long)h->lv[l].g.NX * h->lv[l].g.NY <= kMgFuseCells && L - l <= kMgFuseLevels) {
+      bottom = l;
+      break;
+    }
+  MgRun run{f, h, 1.0f - om, cycles, std::vector<int>(h->lv.size(), 0), bottom};
   for (int k = 0; k < cycles; ++k) run.cycle(0, k == 0, k == cycles - 1);
   count(f, run.launches);
   return cudaGetLastError();
