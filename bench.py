@@ -701,13 +701,34 @@ def ensemble(fluid_gb300, args, n=256, steps=20, roll=16, every=8):
         f.Simulate(DT)
         f.Simulate(DT)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        for f in one:
-            f.Simulate(DT)
-    for f in one:
-        f.synchronize()
-    ms_1 = 1e3 * (time.perf_counter() - t0) / steps
+
+    def device_span(work):
+        # Device time from the first handle's start event to the last
+        # handle's end event, each recorded on that handle's own stream (the
+        # handles' streams run concurrently; the host issues their work in
+        # turn).
+        streams = [torch.cuda.ExternalStream(f.stream) for f in one]
+        starts = [torch.cuda.Event(enable_timing=True) for _ in one]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in one]
+        torch.cuda.synchronize()
+        for k, st in enumerate(streams):
+            starts[k].record(st)
+        t0 = time.perf_counter()
+        work()
+        host = time.perf_counter() - t0
+        for k, st in enumerate(streams):
+            ends[k].record(st)
+        torch.cuda.synchronize()
+        span = max(starts[0].elapsed_time(e) for e in ends)
+        return span, 1e3 * host
+
+    def fwd_all():
+        for _ in range(steps):
+            for f in one:
+                f.Simulate(DT)
+
+    span_1, host_1 = device_span(fwd_all)
+    ms_1 = span_1 / steps
 
     batch.rollout_grad(DT, roll, targets, every=every)
     batch.synchronize()
@@ -716,12 +737,12 @@ def ensemble(fluid_gb300, args, n=256, steps=20, roll=16, every=8):
     e1.record(stream)
     batch.synchronize()
     ms_ba = e0.elapsed_time(e1) / roll
-    t0 = time.perf_counter()
-    for k, f in enumerate(one):
-        f.rollout_grad(DT, roll, targets[k], every=every)
-    for f in one:
-        f.synchronize()
-    ms_1a = 1e3 * (time.perf_counter() - t0) / roll
+    def adj_all():
+        for k, f in enumerate(one):
+            f.rollout_grad(DT, roll, targets[k], every=every)
+
+    span_1a, host_1a = device_span(adj_all)
+    ms_1a = span_1a / roll
     batch.close()
     return {
         "config": "%d scenes (seed 5): sides log-uniform 64-512, 0-5 discs r 4-32, 1-3 jets "
@@ -731,14 +752,17 @@ def ensemble(fluid_gb300, args, n=256, steps=20, roll=16, every=8):
         "batch_fwd": {"value": cells / ms_b / 1e3, "unit": "Mcell-steps/s", "ms_per_step": ms_b,
                       "launches_per_step": launches_b, "timing": "CUDA events, one graph per step"},
         "one_at_a_time_fwd": {"value": cells / ms_1 / 1e3, "unit": "Mcell-steps/s",
-                              "ms_per_step": ms_1,
-                              "timing": "host clock around fg_simulate on each handle in turn"},
+                              "ms_per_step": ms_1, "host_ms_per_step": host_1 / steps,
+                              "timing": "device span (CUDA events on every handle's stream) of "
+                                        "fg_simulate issued on each handle in turn"},
         "batch_speedup_fwd": ms_1 / ms_b,
         "batch_fwd_adjoint": {"value": cells / ms_ba / 1e3, "unit": "Mcell-steps/s",
                               "ms_per_step": ms_ba, "rollout_steps": roll,
                               "checkpoint_every": every},
         "one_at_a_time_fwd_adjoint": {"value": cells / ms_1a / 1e3, "unit": "Mcell-steps/s",
-                                      "ms_per_step": ms_1a},
+                                      "ms_per_step": ms_1a, "host_ms_per_step": host_1a / roll,
+                                      "timing": "device span (CUDA events on every handle's "
+                                                "stream) of each handle's rollout in turn"},
         "batch_speedup_fwd_adjoint": ms_1a / ms_ba,
         "loss_sum": float(np.sum(losses)),
     }

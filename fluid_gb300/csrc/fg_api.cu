@@ -719,6 +719,7 @@ static int mg_prepare(fg_fluid* f) {
   f->mg = h;
   // Zeroed once: the padding columns and the ghost rings are never written
   // and must read as 0.
+  CK(f, mg_kernel_setup(), "multigrid levels");
   CK(f, cudaMemsetAsync(h->block, 0, total, f->stream), "multigrid levels");
   CK(f, cudaMemsetAsync(h->ctl, 0, 64, f->stream), "multigrid levels");
   CK(f, launch_mg_rebuild(f), "multigrid levels");

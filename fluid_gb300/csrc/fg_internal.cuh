@@ -413,6 +413,7 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
 // The MULTIGRID scheme's levels: masks, flags and weights rebuilt from the
 // fine flags (the allocation is fg_api.cu's, outside stream capture).
 cudaError_t launch_mg_rebuild(fg_fluid* f);
+cudaError_t mg_kernel_setup();  // the bottom kernel's shared-memory limit (outside capture)
 void mg_free(fg_fluid* f);
 // solveMultigridVCycle (fluid.go:559-594) with the reference's serial
 // smoothers, bit for bit.

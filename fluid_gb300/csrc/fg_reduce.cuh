@@ -189,6 +189,28 @@ inline int combine_rows(cudaStream_t st, float* part, int n, unsigned max_mask, 
   return 2;
 }
 
+// Combines all n rows of `in` in one block -- thread k merges rows k,
+// k + blockDim.x, ... in turn, then the block's fixed tree -- and hands the
+// total row to store(row) on thread 0: the per-step statistics in one
+// launch instead of a two-level combine and a store kernel.
+template <int NS, typename Store>
+__global__ void __launch_bounds__(1024)
+    k_combine_store(const float* __restrict__ in, int n, unsigned max_mask, Store store) {
+  __shared__ float sh[64 * NS];
+  __shared__ float row[2 * NS];
+  FF v[NS];
+  slots_identity<NS>(v, max_mask);
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    FF w[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+      w[s] = FF{in[(size_t)k * 2 * NS + 2 * s], in[(size_t)k * 2 * NS + 2 * s + 1]};
+    slots_merge<NS>(v, w, max_mask);
+  }
+  block_row<NS>(v, max_mask, sh, row);  // thread 0 writes the row
+  if (threadIdx.x == 0) store(row);
+}
+
 // Total of a sum slot of a final row, in FP64.
 __device__ __forceinline__ double row_sum(const float* row, int s) {
   return (double)row[2 * s] + (double)row[2 * s + 1];

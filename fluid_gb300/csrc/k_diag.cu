@@ -55,9 +55,10 @@ __global__ void k_mass_partials(const float* __restrict__ M, float* __restrict__
   block_row<1>(v, 0u, sh, part + 2 * (size_t)block_id());
 }
 
-__global__ void k_store_mass(const float* __restrict__ r, DevStats* st) {
-  st->smoke_mass = row_sum(r, 0);
-}
+struct StoreMass {
+  DevStats* st;
+  __device__ void operator()(const float* r) const { st->smoke_mass = row_sum(r, 0); }
+};
 
 // MaxDivergence (fluid.go:876-891): float32 |div|, NaN ignored (fmaxf).
 __global__ void k_maxdiv_partials(const float* __restrict__ U, const float* __restrict__ V,
@@ -182,10 +183,8 @@ cudaError_t launch_div_stats(fg_fluid* f) {
 
 cudaError_t launch_store_mass(fg_fluid* f, int nb) {
   if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
-  float* out = nullptr;
-  count(f, combine_rows<1>(f->stream, f->partials, nb, 0u, &out));
   count(f);
-  k_store_mass<<<1, 1, 0, f->stream>>>(out, f->dstats);
+  k_combine_store<1><<<1, 1024, 0, f->stream>>>(f->partials, nb, 0u, StoreMass{f->dstats});
   return cudaGetLastError();
 }
 

@@ -1957,18 +1957,24 @@ __device__ __forceinline__ void grad_batch_cell(int i, int j, const float* __res
             turbStrength, do_turb, g, acc, nullptr, nullptr, U2o, V2o);
 }
 
-__global__ void k_store_div_p(const float* __restrict__ r, DevStats* st) {
-  st->div_l2_sq = row_sum(r, 0);
-  st->div_max = (double)r[2];
-  st->div_count = row_sum(r, 2);
-  st->resid_l2_sq = row_sum(r, 3);
-  st->resid_max = (double)r[8];
-}
-
-__global__ void k_finish_parallel(const PCtl* __restrict__ ctl, DevStats* st) {
-  st->sweeps = ctl->sweeps;
-  st->last_maxdiv = (double)__uint_as_float(ctl->slots[ctl->last_launch]);
-}
+// The step's statistics from the combined row of k_grad_fused's partials
+// (sum div^2, max |div|, fluid cells, sum r^2, max |r|) and, after a solve,
+// its sweep count and last checked max |r| from the control block.
+struct StoreDivP {
+  DevStats* st;
+  const PCtl* ctl;
+  __device__ void operator()(const float* r) const {
+    st->div_l2_sq = row_sum(r, 0);
+    st->div_max = (double)r[2];
+    st->div_count = row_sum(r, 2);
+    st->resid_l2_sq = row_sum(r, 3);
+    st->resid_max = (double)r[8];
+    if (ctl) {
+      st->sweeps = ctl->sweeps;
+      st->last_maxdiv = (double)__uint_as_float(ctl->slots[ctl->last_launch]);
+    }
+  }
+};
 
 
 }  // namespace
@@ -2644,33 +2650,48 @@ __global__ void k_mg_prolong(const float* __restrict__ xc, const uint8_t* __rest
   mg_prolong_cell(i, j, xc, flc, gc, xf, flf, gf);
 }
 
-// The bottom of the V-cycle in one block: levels l0 .. n-1 (their cells fit
-// in L2 many times over, and a launch per operation would cost more than
-// the work), with the same per-cell arithmetic as the launches above and
-// the Jacobi sweep kernel: zero-started pre-smoothing and restriction down
-// to the coarsest level, its sweeps, then prolongation and post-smoothing
-// back up.  Every level starts in buffer 0 and makes an even number of
-// sweeps, so its iterate ends in buffer 0.  Only interior cells are
-// written; the ghost rings stay 0 as the sweep kernel leaves them.
+// The bottom of the V-cycle in one block, in shared memory: levels l0 ..
+// n-1 (a launch per operation would cost more than their work, and their
+// arrays fit on one SM).  The block copies the levels' weights and flags
+// and level l0's right-hand side into shared memory (rows of NY, no pitch
+// padding), zeroes the iterates, runs the same per-cell operations as the
+// launches above and the Jacobi sweep kernel -- zero-started pre-smoothing
+// and restriction down to the coarsest level, its sweeps, then
+// prolongation and post-smoothing back up -- and writes level l0's iterate
+// back to its buffer 0.  Every level starts in buffer 0 and makes an even
+// number of sweeps, so its iterate ends in buffer 0; only interior cells
+// are written and the ghost rings stay 0 as the sweep kernel leaves them.
 constexpr int kMgFuseLevels = 12, kMgFuseThreads = 1024;
+constexpr int kMgSmemBytes = 200 * 1024;  // dynamic shared memory of k_mg_bottom
 struct MgFused {
-  Grid g[kMgFuseLevels];
-  const uint8_t* flags[kMgFuseLevels];
-  const float* w[kMgFuseLevels];
-  float* b[kMgFuseLevels];
-  float* bw[kMgFuseLevels];
-  float* x0[kMgFuseLevels];
-  float* x1[kMgFuseLevels];
-  int n;  // levels held (the first is l0)
+  Grid gg[kMgFuseLevels];               // the levels in global memory (pitched)
+  Grid gs[kMgFuseLevels];               // the same in shared memory (pitch NY)
+  const uint8_t* flags[kMgFuseLevels];  // global
+  const float* w[kMgFuseLevels];        // global
+  const float* b0;                      // level l0's right-hand side and w * b (global)
+  const float* bw0;
+  float* x0;                            // level l0's buffer 0 (global): the result
+  int foff[kMgFuseLevels];              // first float of each level's arrays in shared memory
+  int boff[kMgFuseLevels];              // first byte of each level's flags in shared memory
+  int n;                                // levels held (the first is l0)
 };
+// A level's arrays in shared memory: five float arrays of NX * NY, then flags.
+struct MgSm {
+  float *x0, *x1, *b, *bw, *w;
+  uint8_t* fl;
+};
+__device__ __forceinline__ MgSm mg_sm(const MgFused& m, int l, float* fs, uint8_t* bs) {
+  const int n = m.gs[l].NX * m.gs[l].NY;
+  float* p = fs + m.foff[l];
+  return MgSm{p, p + n, p + 2 * n, p + 3 * n, p + 4 * n, bs + m.boff[l]};
+}
 
-__device__ __forceinline__ void mg_fused_sweeps(const MgFused& m, int l, int ns, bool zero,
+__device__ __forceinline__ void mg_fused_sweeps(const MgSm& a, const Grid& g, int ns, bool zero,
                                                 float om1) {
-  const Grid& g = m.g[l];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kMgFuseThreads / 32;
   for (int s = 0; s < ns; ++s) {
-    const float* xs = (s & 1) ? m.x1[l] : m.x0[l];
-    float* xd = (s & 1) ? m.x0[l] : m.x1[l];
+    const float* xs = (s & 1) ? a.x1 : a.x0;
+    float* xd = (s & 1) ? a.x0 : a.x1;
     const bool z = zero && s == 0;
     for (int i = 1 + warp; i < g.NX - 1; i += nw)
       for (int j = 1 + lane; j < g.NY - 1; j += 32) {
@@ -2682,7 +2703,7 @@ __device__ __forceinline__ void mg_fused_sweeps(const MgFused& m, int l, int ns,
         } else {
           nb = 0.0f + 0.0f + 0.0f + 0.0f;
         }
-        float y = __fmaf_rn(m.w[l][c], nb, m.bw[l][c]);
+        float y = __fmaf_rn(a.w[c], nb, a.bw[c]);
         y = __fmaf_rn(om1, xc, y);
         xd[c] = y;
       }
@@ -2692,28 +2713,50 @@ __device__ __forceinline__ void mg_fused_sweeps(const MgFused& m, int l, int ns,
 
 __global__ void __launch_bounds__(kMgFuseThreads)
     k_mg_bottom(const __grid_constant__ MgFused m, float om1) {
+  extern __shared__ __align__(16) float mg_smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kMgFuseThreads / 32;
+  uint8_t* bsm = reinterpret_cast<uint8_t*>(mg_smem);
   const int last = m.n - 1;
+  for (int l = 0; l <= last; ++l) {
+    const MgSm a = mg_sm(m, l, mg_smem, bsm);
+    const Grid& gg = m.gg[l];
+    const Grid& gs = m.gs[l];
+    for (int i = warp; i < gs.NX; i += nw)
+      for (int j = lane; j < gs.NY; j += 32) {
+        const int cs = i * gs.P + j, cg = i * gg.P + j;
+        a.w[cs] = m.w[l][cg];
+        a.fl[cs] = m.flags[l][cg];
+        a.b[cs] = l == 0 ? m.b0[cg] : 0.0f;
+        a.bw[cs] = l == 0 ? m.bw0[cg] : 0.0f;
+        a.x0[cs] = 0.0f;
+        a.x1[cs] = 0.0f;
+      }
+  }
+  __syncthreads();
   for (int l = 0; l < last; ++l) {
-    mg_fused_sweeps(m, l, kMgPre, true, om1);
-    const Grid& gf = m.g[l];
-    const Grid& gc = m.g[l + 1];
+    const MgSm f = mg_sm(m, l, mg_smem, bsm), c = mg_sm(m, l + 1, mg_smem, bsm);
+    mg_fused_sweeps(f, m.gs[l], kMgPre, true, om1);
+    const Grid& gf = m.gs[l];
+    const Grid& gc = m.gs[l + 1];
     for (int I = 1 + warp; I < gc.NX - 1; I += nw)
       for (int J = 1 + lane; J < gc.NY - 1; J += 32)
-        mg_restrict_cell(I, J, m.x0[l], m.b[l], m.flags[l], gf, m.flags[l + 1], m.w[l + 1],
-                         m.b[l + 1], m.bw[l + 1], gc);
+        mg_restrict_cell(I, J, f.x0, f.b, f.fl, gf, c.fl, c.w, c.b, c.bw, gc);
     __syncthreads();
   }
-  mg_fused_sweeps(m, last, kMgCoarse, true, om1);
+  mg_fused_sweeps(mg_sm(m, last, mg_smem, bsm), m.gs[last], kMgCoarse, true, om1);
   for (int l = last - 1; l >= 0; --l) {
-    const Grid& gf = m.g[l];
-    const Grid& gc = m.g[l + 1];
+    const MgSm f = mg_sm(m, l, mg_smem, bsm), c = mg_sm(m, l + 1, mg_smem, bsm);
+    const Grid& gf = m.gs[l];
+    const Grid& gc = m.gs[l + 1];
     for (int i = 1 + warp; i < gf.NX - 1; i += nw)
       for (int j = 1 + lane; j < gf.NY - 1; j += 32)
-        mg_prolong_cell(i, j, m.x0[l + 1], m.flags[l + 1], gc, m.x0[l], m.flags[l], gf);
+        mg_prolong_cell(i, j, c.x0, c.fl, gc, f.x0, f.fl, gf);
     __syncthreads();
-    mg_fused_sweeps(m, l, kMgPost, false, om1);
+    mg_fused_sweeps(f, gf, kMgPost, false, om1);
   }
+  const MgSm a = mg_sm(m, 0, mg_smem, bsm);
+  for (int i = warp; i < m.gs[0].NX; i += nw)
+    for (int j = lane; j < m.gs[0].NY; j += 32) m.x0[i * m.gg[0].P + j] = a.x0[i * m.gs[0].P + j];
 }
 
 inline dim3 level_grid(const Grid& g) { return dim3((g.NY + BX - 1) / BX, (g.NX + BY - 1) / BY); }
@@ -2735,7 +2778,21 @@ void mg_sweeps(cudaStream_t st, const MgLevelDev& v, const float* src, float* ds
 // The V-cycles of one solve.  cur[l] names the buffer of level l holding
 // its iterate; the last smoothing of level 0 reports to the main control
 // block (sweeps = cycles, sel = the buffer of the result).
-constexpr int kMgFuseCells = 20000;  // levels of at most this many cells run in k_mg_bottom
+// The first coarse level from which all levels down fit k_mg_bottom's
+// shared memory (at most kMgFuseLevels of them); the level count when none
+// does.
+int mg_bottom_level(const MgHier* h) {
+  const int L = (int)h->lv.size();
+  long long bytes = 0;
+  int bottom = L;
+  for (int l = L - 1; l >= 1 && L - l <= kMgFuseLevels; --l) {
+    bytes += (5 * (long long)sizeof(float) + 1) * h->lv[l].g.NX * h->lv[l].g.NY;
+    if (bytes > kMgSmemBytes - 64) break;
+    bottom = l;
+  }
+  return bottom;
+}
+
 struct MgRun {
   fg_fluid* f;
   MgHier* h;
@@ -2758,17 +2815,25 @@ struct MgRun {
     if (l == bottom) {
       MgFused m{};
       m.n = L - l;
+      int fo = 0;
       for (int k = 0; k < m.n; ++k) {
         const MgLevelDev& v = h->lv[l + k];
-        m.g[k] = v.g;
+        m.gg[k] = v.g;
+        m.gs[k] = make_grid(v.g.NX, v.g.NY, v.g.NY, v.g.h);
         m.flags[k] = v.flags;
         m.w[k] = v.w;
-        m.b[k] = v.b;
-        m.bw[k] = v.bw;
-        m.x0[k] = v.x[0];
-        m.x1[k] = v.x[1];
+        m.foff[k] = fo;
+        fo += 5 * v.g.NX * v.g.NY;
       }
-      k_mg_bottom<<<1, kMgFuseThreads, 0, f->stream>>>(m, om1);
+      int bo = fo * (int)sizeof(float);
+      for (int k = 0; k < m.n; ++k) {
+        m.boff[k] = bo;
+        bo += h->lv[l + k].g.NX * h->lv[l + k].g.NY;
+      }
+      m.b0 = h->lv[l].b;
+      m.bw0 = h->lv[l].bw;
+      m.x0 = h->lv[l].x[0];
+      k_mg_bottom<<<1, kMgFuseThreads, bo, f->stream>>>(m, om1);
       cur[l] = 0;
       ++launches;
       return;
@@ -2796,15 +2861,8 @@ cudaError_t mg_solve(fg_fluid* f, int cycles, float om) {
   if (!h || h->lv.size() < 2) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(h->ctl, 0, sizeof(PCtl), f->stream);
   if (e != cudaSuccess) return e;
-  // The first coarse level small enough for one block (with at most
-  // kMgFuseLevels levels from it down).
   const int L = (int)h->lv.size();
-  int bottom = L;
-  for (int l = 1; l < L; ++l)
-    if ((long long)h->lv[l].g.NX * h->lv[l].g.NY <= kMgFuseCells && L - l <= kMgFuseLevels) {
-      bottom = l;
-      break;
-    }
+  const int bottom = mg_bottom_level(h);
   MgRun run{f, h, 1.0f - om, cycles, std::vector<int>(h->lv.size(), 0), bottom};
   for (int k = 0; k < cycles; ++k) run.cycle(0, k == 0, k == cycles - 1);
   count(f, run.launches);
@@ -2812,6 +2870,11 @@ cudaError_t mg_solve(fg_fluid* f, int cycles, float om) {
 }
 
 }  // namespace
+
+cudaError_t mg_kernel_setup() {
+  return cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              kMgSmemBytes);
+}
 
 void mg_free(fg_fluid* f) {
   if (!f->mg) return;
@@ -2882,8 +2945,6 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
     e = mgs ? mg_solve(f, num_iters, om)
             : jacobi_solve(f, ctl, f->rhs, f->bw, f->phi, f->phi2, num_iters, true);
     if (e != cudaSuccess) return e;
-    count(f);
-    k_finish_parallel<<<1, 1, 0, f->stream>>>(ctl, f->dstats);
   }
   mark(f, "jacobi sweeps");
   bool refine = f->prm.refine_sweeps > 0;
@@ -2904,9 +2965,9 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
       f->step_fv, f->step_u2, f->step_v2);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
-  float* out = nullptr;
-  count(f, combine_rows<5>(f->stream, f->partials, nb, 0x12u, &out));
-  k_store_div_p<<<1, 1, 0, f->stream>>>(out, f->dstats);
+  count(f);
+  k_combine_store<5><<<1, 1024, 0, f->stream>>>(f->partials, nb, 0x12u,
+                                                StoreDivP{f->dstats, num_iters > 0 ? ctl : nullptr});
   return cudaGetLastError();
 }
 
