@@ -6,8 +6,10 @@ Python mirror of the Go type ``fluid.Fluid`` over that ABI.
 """
 from . import fluid as _fluid_mod
 from ._build import build
-from .fluid import (ALL_FIELDS, FIELDS, SCHEME_JACOBI, SCHEME_LEXSOR, SCHEME_MULTIGRID, Batch, Fluid,
-                    FluidError, ScalarField, VectorField, debug_fail_alloc)
+from .fluid import (ALL_FIELDS, FIELDS, JACOBI_KERNEL_DATAFLOW, JACOBI_KERNEL_NONE,
+                    JACOBI_KERNEL_SWEEP, JACOBI_KERNEL_TMA, SCHEME_JACOBI, SCHEME_LEXSOR,
+                    SCHEME_MULTIGRID, Batch, Fluid, FluidError, ScalarField, VectorField,
+                    debug_fail_alloc)
 
 
 def __getattr__(name):
@@ -23,4 +25,5 @@ def set_relaxation(value: float) -> None:
 
 __all__ = ["Fluid", "Batch", "FluidError", "ScalarField", "VectorField", "build", "set_relaxation",
            "FIELDS", "ALL_FIELDS", "SCHEME_LEXSOR", "SCHEME_JACOBI", "SCHEME_MULTIGRID",
-           "debug_fail_alloc"]
+           "JACOBI_KERNEL_NONE", "JACOBI_KERNEL_SWEEP", "JACOBI_KERNEL_TMA",
+           "JACOBI_KERNEL_DATAFLOW", "debug_fail_alloc"]

@@ -40,7 +40,7 @@ class Stats(ctypes.Structure):
     _fields_ = [
         ("div_l2_post", _c_d), ("div_max_post", _c_d), ("div_count_post", _c_d),
         ("resid_l2", _c_d), ("resid_max", _c_d), ("smoke_mass", _c_d), ("last_maxdiv", _c_d),
-        ("sweeps", _c_i), ("reserved", _c_i * 7),
+        ("sweeps", _c_i), ("jacobi_kernel", _c_i), ("reserved", _c_i * 6),
     ]
 
 

@@ -398,6 +398,10 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
     return code;
   };
   if (cudaGetDevice(&f->device) != cudaSuccess) return bail(FG_ERR_CUDA);
+  // The per-context set-up below needs a current context, which
+  // cudaGetDevice does not create; cudaFree(nullptr) makes the runtime use
+  // the caller's current context or create the device's primary one.
+  if (cudaFree(nullptr) != cudaSuccess) return bail(FG_ERR_CUDA);
   init_jacobi_tma();
   init_lexsor_cluster();
   if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -763,6 +767,10 @@ int fg_simulate(fg_fluid* f, float dt) {
   memcpy(ent.key, key, sizeof key);
   ent.dt_bits = dtb;
   ent.version = f->params_version;
+  // The Jacobi kernels' per-context set-up cannot run inside a capture: do
+  // it first (a no-op once done), so the captured step gets the TMA-fed and
+  // dataflow kernels even if this thread's context changed since fg_create.
+  init_jacobi_tma();
   CK(f, cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
   unsigned long long before = f->launches;
   rc = enqueue_step(f, dt);
@@ -814,6 +822,7 @@ int fg_get_stats(fg_fluid* f, fg_stats* out) {
   out->smoke_mass = s.smoke_mass;
   out->last_maxdiv = s.last_maxdiv;
   out->sweeps = s.sweeps;
+  out->jacobi_kernel = f->jacobi_kernel;
   if (s.timeout) return fail(f, FG_ERR_TIMEOUT, "a device-side wait of the last step gave up");
   for (double v : {s.div_l2_sq, s.div_max, s.resid_l2_sq, s.resid_max, s.smoke_mass, s.last_maxdiv})
     if (!std::isfinite(v)) return fail(f, FG_ERR_NONFINITE, "the last step produced non-finite values");
@@ -1540,6 +1549,7 @@ int run_graphed(fg_fluid* f, int kind, float dt, const void* const* ptrs, Fn&& e
   ent.version = f->params_version;
   memcpy(ent.ptrs, ptrs, sizeof ent.ptrs);
   memcpy(ent.pre, pre, sizeof pre);
+  init_jacobi_tma();  // outside the capture, as for the step graphs
   CK(f, cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
   unsigned long long before = f->launches;
   int rc = enqueue();

@@ -294,6 +294,7 @@ struct fg_fluid {
   void* pctl = nullptr;   // control block of the main Jacobi solve (k_pressure.cu PCtl)
   int* tile_done = nullptr;  // dataflow Jacobi kernel: per-tile phase flags + item counter
   int stall_tile = -1;       // fault injection: a tile the dataflow kernel never publishes
+  int jacobi_kernel = 0;     // FG_JACOBI_KERNEL_* of the last main solve (fg_stats)
   float* skew[3] = {};       // diagonal-major U, V, p of the wavefront SOR (or none)
   uint8_t* skew_flags = nullptr;
   int skew_sp = 0;           // their row stride (cells per diagonal)

@@ -124,14 +124,6 @@ __device__ __forceinline__ void sl_velocity_cell(int i, int j, const float* __re
   nU[c] = u;
   nV[c] = v;
 }
-__global__ void k_sl_velocity(const float* __restrict__ Ui, const float* __restrict__ Vi,
-                              float* __restrict__ Uo, float* __restrict__ Vo, float* nU,
-                              float* nV, const uint8_t* __restrict__ flags, float dt, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
-  sl_velocity_cell(i, j, Ui, Vi, Uo, Vo, nU, nV, flags, dt, g);
-}
 
 // BFECC pass 1 (fluid.go:923): forward advection of the original field into
 // (Fu, Fv).  The staging buffers are not written: the final pass reads the
@@ -158,20 +150,74 @@ __device__ __forceinline__ void bfecc_vel_fwd_cell(int i, int j, const float* __
   Fu[c] = u_advected(fl, i, j, g) ? trace_sample_u(Ui, Vi, Ui, i, j, dt, g) : (ring ? Ui[c] : nU[c]);
   Fv[c] = v_advected(fl, i, j, g) ? trace_sample_v(Ui, Vi, Vi, i, j, dt, g) : (ring ? Vi[c] : nV[c]);
 }
-__global__ void k_bfecc_vel_fwd(const float* __restrict__ Ui, const float* __restrict__ Vi,
-                                const float* __restrict__ nU, const float* __restrict__ nV,
-                                float* __restrict__ Fu, float* __restrict__ Fv,
-                                const uint8_t* __restrict__ flags, float dt, Grid g) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
-  bfecc_vel_fwd_cell(i, j, Ui, Vi, nU, nV, Fu, Fv, flags, dt, g);
+
+// One row of a 3-wide window: columns j-1, j, j+1, with their min and max.
+struct Row3 {
+  float l, c, r, mn, mx;
+};
+__device__ __forceinline__ Row3 row3(const float* __restrict__ src, int c) {
+  Row3 w;
+  w.l = src[c - 1];
+  w.c = src[c];
+  w.r = src[c + 1];
+  w.mn = fminf(fminf(w.l, w.c), w.r);
+  w.mx = fmaxf(fmaxf(w.l, w.c), w.r);
+  return w;
 }
 
-// clampToNeighbors (fluid.go:1094-1120) for an interior cell (all 3x3
-// neighbours in range).
+// The range of clampToNeighbors (fluid.go:1094-1120: lo = hi = the centre,
+// then a scan of the 3x3 block row by row that replaces lo on v < lo and hi
+// on v > hi) over the rows a, b, c around the centre b.c, bit for bit, with
+// min / max trees instead of 18 compare-and-selects.  For a centre that is
+// not NaN the scan ignores NaN neighbours, as fminf / fmaxf do, and ends on
+// the first element (in scan order) of the minimum's value; a nonzero
+// minimum has a single bit pattern, so the tree's value is it; a zero
+// minimum with a zero centre is the centre (scanned first, nothing compares
+// below it); a NaN centre is never replaced.  Only a zero extreme with a
+// nonzero centre (a -0/+0 tie that scan order decides) runs the scan.
+__device__ __forceinline__ void range_rows(const Row3& a, const Row3& b, const Row3& c, float& lo,
+                                           float& hi) {
+  const float ctr = b.c;
+  const float m = fminf(fminf(a.mn, b.mn), c.mn);
+  const float M = fmaxf(fmaxf(a.mx, b.mx), c.mx);
+  if (ctr != ctr) {
+    lo = hi = ctr;
+    return;
+  }
+  const float v[9] = {a.l, a.c, a.r, b.l, b.c, b.r, c.l, c.c, c.r};
+  if (m != 0.0f) {
+    lo = m;
+  } else if (ctr == 0.0f) {
+    lo = ctr;
+  } else {
+    lo = ctr;
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      if (v[k] < lo) lo = v[k];
+  }
+  if (M != 0.0f) {
+    hi = M;
+  } else if (ctr == 0.0f) {
+    hi = ctr;
+  } else {
+    hi = ctr;
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      if (v[k] > hi) hi = v[k];
+  }
+}
+
+// clampToNeighbors' range (fluid.go:1094-1120) for an interior cell (all 3x3
+// neighbours in range): range3x3 through the min / max trees, for the
+// velocity; range3x3_scan as the reference scans, for the smoke (measured
+// faster there: a field of zeros always ends in the centre's case, and the
+// smoke pass has fewer instructions to save).
 __device__ __forceinline__ void range3x3(const float* __restrict__ src, int c, int P, float& lo,
                                          float& hi) {
+  range_rows(row3(src, c - P), row3(src, c), row3(src, c + P), lo, hi);
+}
+__device__ __forceinline__ void range3x3_scan(const float* __restrict__ src, int c, int P,
+                                              float& lo, float& hi) {
   lo = src[c];
   hi = src[c];
 #pragma unroll
@@ -375,7 +421,7 @@ __device__ __forceinline__ void bfecc_smoke_correct_cell(int i, int j, const flo
   uint8_t fl = flags[c];
   float o = Mi[c];
   float lo, hi;
-  range3x3(Mi, c, g.P, lo, hi);
+  range3x3_scan(Mi, c, g.P, lo, hi);
   float s = smoke_value(Ut, Vt, Fm, i, j, -dt, smokeAdv, g);
   float b = (fl & F_FLUID) ? s : 0.0f;
   float cm = o - (b - o) * 0.5f;
@@ -393,13 +439,100 @@ __global__ void k_bfecc_smoke_correct(const float* __restrict__ Ut, const float*
   bfecc_smoke_correct_cell(i, j, Ut, Vt, Mi, Fm, Cm, flags, dt, smokeAdv, g);
 }
 
+// ------------------------------------------------------------ strip kernels
+// The single-scene velocity passes without a clamp (BFECC pass 1 and the
+// final advection) run R consecutive rows of one column per thread (a block
+// of 32 x 8 threads covers 32 columns x 8R rows).  Interior strips keep the
+// departure velocities' neighbouring rows in registers, so each U and V load
+// is made once per row instead of twice; the arithmetic of every cell is
+// the same, operation for operation.  Strips that touch the ghost ring (or
+// pass the last row) run the per-cell bodies.  The clamping passes and the
+// smoke passes stay one cell per thread: their strips took 48-64 registers,
+// which halved the resident warps of these load-latency-bound passes and
+// cost more than the shared loads saved (velocity correction 56.8 against
+// 50.4 us, smoke passes +5 to +12 us each, at 2048^2).
+constexpr int kStripRows = 4;
+
+template <int R>
+__device__ __forceinline__ bool strip_interior(int i0, int j, const Grid& g) {
+  return j >= 1 && j <= g.NY - 2 && i0 >= 1 && i0 + R - 1 <= g.NX - 2;
+}
+
+// advectVelocity's interior cells (sl_velocity_cell, MODE 1: result to
+// Uo, Vo and the staging buffers) or BFECC pass 1 (bfecc_vel_fwd_cell,
+// MODE 0: result to Uo = Fu, Vo = Fv; the staging buffers only read).  The
+// departure velocities of row i need U on rows i, i+1 (columns j-1, j) and
+// V on rows i-1, i (columns j, j+1).
+template <int R, int MODE>
+__global__ void __launch_bounds__(256, 4)
+    k_vel_strip(const float* __restrict__ Ui, const float* __restrict__ Vi, float* __restrict__ Uo,
+                float* __restrict__ Vo, float* nU, float* nV, const uint8_t* __restrict__ flags,
+                float dt, Grid g) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i0 = (blockIdx.y * blockDim.y + threadIdx.y) * R;
+  if (j >= g.NY || i0 >= g.NX) return;
+  if (!strip_interior<R>(i0, j, g)) {
+    for (int r = 0; r < R && i0 + r < g.NX; ++r) {
+      if (MODE == 1)
+        sl_velocity_cell(i0 + r, j, Ui, Vi, Uo, Vo, nU, nV, flags, dt, g);
+      else
+        bfecc_vel_fwd_cell(i0 + r, j, Ui, Vi, nU, nV, Uo, Vo, flags, dt, g);
+    }
+    return;
+  }
+  const int P = g.P;
+  int c = i0 * P + j;
+  float ul = Ui[c - 1], uc = Ui[c];          // U row i
+  float vp = Vi[c - P], vpr = Vi[c - P + 1];  // V row i-1
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int i = i0 + r;
+    const float uln = Ui[c + P - 1], ucn = Ui[c + P];  // U row i+1
+    const float vc = Vi[c], vcr = Vi[c + 1];           // V row i
+    const uint8_t fl = flags[c];
+    // departures(): avgV at the U face, avgU at the V face.
+    const float vu = (vp + vc + vpr + vcr) * 0.25f;
+    const float uv = (ul + uc + uln + ucn) * 0.25f;
+    const float su = sample_dep(Ui, i, j, dt * uc, dt * vu, false, true, g);
+    const float sv = sample_dep(Vi, i, j, dt * uv, dt * vc, true, false, g);
+    const float u = u_advected(fl, i, j, g) ? su : nU[c];
+    const float v = v_advected(fl, i, j, g) ? sv : nV[c];
+    Uo[c] = u;
+    Vo[c] = v;
+    if (MODE == 1) {
+      nU[c] = u;
+      nV[c] = v;
+    }
+    ul = uln;
+    uc = ucn;
+    vp = vc;
+    vpr = vcr;
+    c += P;
+  }
+}
+
+inline dim3 strip_grid(const fg_fluid* f) {
+  return dim3((f->NY + BX - 1) / BX, (f->NX + BY * kStripRows - 1) / (BY * kStripRows));
+}
+
 }  // namespace
 
-cudaError_t launch_advect_velocity(fg_fluid* f, float dt) {
+// advectVelocity over (Ui, Vi) into the rotation partners and the staging
+// buffers.
+static void sl_velocity_pass(fg_fluid* f, const float* Ui, const float* Vi, float dt) {
   count(f);
-  FG_CELLS(f, k_sl_velocity, sl_velocity_cell, (const float*)f->d[FG_U],
-           (const float*)f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU],
-           f->d[FG_NEWV], (const uint8_t*)f->flags, dt);
+  if (f->batch) {
+    FG_CELLS_BATCH(f, sl_velocity_cell, Ui, Vi, f->partner[FG_U], f->partner[FG_V],
+                   f->d[FG_NEWU], f->d[FG_NEWV], (const uint8_t*)f->flags, dt);
+    return;
+  }
+  k_vel_strip<kStripRows, 1><<<strip_grid(f), dim3(BX, BY), 0, f->stream>>>(
+      Ui, Vi, f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV], f->flags, dt,
+      f->g);
+}
+
+cudaError_t launch_advect_velocity(fg_fluid* f, float dt) {
+  sl_velocity_pass(f, f->d[FG_U], f->d[FG_V], dt);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   return cudaGetLastError();
@@ -436,18 +569,24 @@ cudaError_t launch_advect_smoke(fg_fluid* f, float dt) { return smoke_pass(f, f-
 
 cudaError_t launch_advect_velocity_bfecc(fg_fluid* f, float dt) {
   count(f);
-  FG_CELLS(f, k_bfecc_vel_fwd, bfecc_vel_fwd_cell, (const float*)f->d[FG_U],
-           (const float*)f->d[FG_V], (const float*)f->d[FG_NEWU], (const float*)f->d[FG_NEWV],
-           f->fwdU, f->fwdV, (const uint8_t*)f->flags, dt);
+  if (f->batch)
+    FG_CELLS_BATCH(f, bfecc_vel_fwd_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V],
+                   (const float*)f->d[FG_NEWU], (const float*)f->d[FG_NEWV], f->fwdU, f->fwdV,
+                   (const uint8_t*)f->flags, dt);
+  else
+    k_vel_strip<kStripRows, 0><<<strip_grid(f), dim3(BX, BY), 0, f->stream>>>(
+        f->d[FG_U], f->d[FG_V], f->fwdU, f->fwdV, f->d[FG_NEWU], f->d[FG_NEWV], f->flags, dt,
+        f->g);
   count(f);
-  FG_CELLS(f, k_bfecc_vel_correct, bfecc_vel_correct_cell, (const float*)f->d[FG_U],
-           (const float*)f->d[FG_V], (const float*)f->fwdU, (const float*)f->fwdV, f->corrU,
-           f->corrV, (const uint8_t*)f->flags, dt);
+  if (f->batch)
+    FG_CELLS_BATCH(f, bfecc_vel_correct_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V],
+                   (const float*)f->fwdU, (const float*)f->fwdV, f->corrU, f->corrV,
+                   (const uint8_t*)f->flags, dt);
+  else
+    k_bfecc_vel_correct<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(
+        f->d[FG_U], f->d[FG_V], f->fwdU, f->fwdV, f->corrU, f->corrV, f->flags, dt, f->g);
   // Pass 4 (fluid.go:991-993): advect the corrected field with itself.
-  count(f);
-  FG_CELLS(f, k_sl_velocity, sl_velocity_cell, (const float*)f->corrU, (const float*)f->corrV,
-           f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV],
-           (const uint8_t*)f->flags, dt);
+  sl_velocity_pass(f, f->corrU, f->corrV, dt);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   return cudaGetLastError();

@@ -2223,8 +2223,10 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
                                   const float* mphi1 = nullptr, const PCtl* mctl = nullptr,
                                   float* rhs_e = nullptr, float* bwe = nullptr,
                                   int* err = nullptr, int* done = nullptr,
-                                  int stall_tile = -1, int tma_stall_tile = -1) {
+                                  int stall_tile = -1, int tma_stall_tile = -1,
+                                  int* kind = nullptr) {
   float om1 = 1.0f - om;
+  int used = FG_JACOBI_KERNEL_SWEEP;
   bool o1 = om1 == 0.0f;
   dim3 gr((g.NY + OJ - 1) / OJ, (g.NX + OI - 1) / OI);
   int nlaunch = (int)(((long long)iters + T - 1) / T);
@@ -2236,6 +2238,7 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
                          stall_tile)) {
     k0 = iters / TMAX;
     kernels = 1;
+    used = FG_JACOBI_KERNEL_DATAFLOW;
   }
   for (int k = k0; k < nlaunch; ++k) {
     ++kernels;
@@ -2252,8 +2255,10 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
     float* re = rinit && nlaunch > 1 ? rhs_e : nullptr;
     if (full && !check && !rinit && !mphi0 &&
         launch_jacobi_tma(st, g, ctl, src, dst, W, bwk, om1, o1, k, t0, sel, zi, err,
-                          tma_stall_tile))
+                          tma_stall_tile)) {
+      if (used == FG_JACOBI_KERNEL_SWEEP) used = FG_JACOBI_KERNEL_TMA;
       continue;
+    }
 #define FG_JAC(O, F, C, R)                                                                      \
   k_jacobi_rb<O, F, C, R><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bwk, bk, flags, om1, ctl, k, t0, \
                                                      ns, tol, sel, zi, g, mphi0, mphi1, mctl, re, \
@@ -2271,6 +2276,7 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
 #undef FG_JAC
   }
   *n_launched = kernels;
+  if (kind) *kind = used;
   return cudaGetLastError();
 }
 
@@ -2319,7 +2325,7 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
     e = enqueue_jacobi(f->stream, f->g, ctl, b, bw, f->wgt, f->flags, x0, x1, iters, T,
                        f->prm.jacobi_omega * f->prm.pressure_damping, check, f->prm.tolerance, &n,
                        nullptr, nullptr, nullptr, nullptr, nullptr, &f->dstats->timeout,
-                       f->tile_done, f->stall_tile);
+                       f->tile_done, f->stall_tile, -1, &f->jacobi_kernel);
   count(f, n);
   if (e != cudaSuccess) return e;
   if (prof) {
@@ -2903,6 +2909,7 @@ cudaError_t launch_mg_rebuild(fg_fluid* f) {
 cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb) {
   float cp = f->density * f->h / dt;  // fluid.go:158
   cudaError_t e;
+  f->jacobi_kernel = FG_JACOBI_KERNEL_NONE;
   if (f->prm.scheme == FG_SCHEME_LEXSOR) {
     count(f);
     // (The correction solve's control block is free in this scheme: its

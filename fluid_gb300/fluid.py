@@ -25,6 +25,8 @@ Relaxation = 1.9  # package var fluid.Relaxation (fluid.go:7-9)
 FIELDS = {"U": 0, "V": 1, "newU": 2, "newV": 3, "p": 4, "S": 5, "M": 6, "newM": 7}
 ALL_FIELDS = 0xFF
 SCHEME_LEXSOR, SCHEME_JACOBI, SCHEME_MULTIGRID = 0, 1, 3
+# stats()["jacobi_kernel"]: the kernel of the last JACOBI-scheme solve (FG_JACOBI_KERNEL_*).
+JACOBI_KERNEL_NONE, JACOBI_KERNEL_SWEEP, JACOBI_KERNEL_TMA, JACOBI_KERNEL_DATAFLOW = 0, 1, 2, 3
 
 # Python attribute -> fg_params member.
 _PARAMS = {

@@ -107,8 +107,22 @@ typedef struct fg_stats {
   double smoke_mass;     /* sum of M over interior cells after the step                   */
   double last_maxdiv;    /* max |div| seen by the last pressure sweep                     */
   int sweeps;            /* pressure sweeps executed (early exit included)                */
-  int reserved[7];
+  int jacobi_kernel;     /* FG_JACOBI_KERNEL_*: the kernel of the last JACOBI-scheme solve */
+  int reserved[6];
 } fg_stats;
+
+/* fg_stats.jacobi_kernel: which kernel ran the sweeps of the last step's main
+ * JACOBI-scheme solve (host-side record of what was enqueued or captured).
+ * NONE for the other schemes and for batches; SWEEP is the per-launch kernel
+ * that loads its tiles itself (early exit, depths below 8, grids without a
+ * tensor map); TMA the per-launch kernel fed by the tensor memory
+ * accelerator; DATAFLOW the one cooperative launch that runs every full
+ * 8-sweep phase (fixed sweep counts of at least 16 on grids of at least one
+ * tile per SM). */
+#define FG_JACOBI_KERNEL_NONE 0
+#define FG_JACOBI_KERNEL_SWEEP 1
+#define FG_JACOBI_KERNEL_TMA 2
+#define FG_JACOBI_KERNEL_DATAFLOW 3
 
 typedef struct fg_fluid fg_fluid;
 

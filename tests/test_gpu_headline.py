@@ -79,6 +79,7 @@ def test_cavity_2048_first_steps_bitwise_against_fp32_oracle(gpu):
             assert same.all(), (step, k, int((~same).sum()))
         sg, so = g.stats(), o.stats()
         assert sg["sweeps"] == so["sweeps"] == 200
+        assert sg["jacobi_kernel"] == gpu.JACOBI_KERNEL_DATAFLOW
         for key in ("div_l2_post", "resid_l2"):
             assert abs(sg[key] - so[key]) <= 1e-9 * abs(so[key]), (step, key, sg[key], so[key])
 

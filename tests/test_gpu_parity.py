@@ -8,6 +8,8 @@
   tolerances of the FP64 oracle: velocity max-abs error <= 1e-4 relative to
   the field's max, post-projection divergence L2 within 1e-5.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -268,6 +270,7 @@ def test_jacobi_dataflow_then_partial_launch_bitwise(gpu):
         f.makeIncompressible(44, 0.1)
     assert_bitwise(g, o, fields=("U", "V", "p"))
     assert g.stats()["sweeps"] == 44
+    assert g.stats()["jacobi_kernel"] == gpu.JACOBI_KERNEL_DATAFLOW
 
 
 def test_jacobi_fixed_sweeps_2048_matches_checked_launches(gpu):
@@ -285,6 +288,44 @@ def test_jacobi_fixed_sweeps_2048_matches_checked_launches(gpu):
         a, b = getattr(fs[0], k), getattr(fs[1], k)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), k
     assert fs[0].stats()["sweeps"] == fs[1].stats()["sweeps"] == 200
+    assert fs[0].stats()["jacobi_kernel"] == gpu.JACOBI_KERNEL_DATAFLOW
+    assert fs[1].stats()["jacobi_kernel"] == gpu.JACOBI_KERNEL_SWEEP
+
+
+FRESH_PROCESS = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+import fluid_gb300 as fg
+# No CUDA call before the handle: the library creates the context itself.
+f = fg.Fluid(1.0, 1200, 800, 1.0, auto_sync=False, scheme=1, num_iters=40, tb_depth=8,
+             early_exit=False)
+S = f.S.reshape(f.NumX, f.NumY)
+S[:] = 1.0
+S[:, 0] = S[:, -1] = S[0, :] = 0.0
+f.mark_dirty()
+kinds = []
+for _ in range(3):
+    f.Simulate(0.1)  # the first call captures the step graph, the others replay it
+    kinds.append(f.stats()["jacobi_kernel"])
+print("KINDS", kinds)
+assert kinds == [fg.JACOBI_KERNEL_DATAFLOW] * 3, kinds
+"""
+
+
+def test_dataflow_kernel_in_graph_of_handle_made_before_any_cuda_call(gpu):
+    """A handle created in a process that has made no CUDA call yet (no
+    context exists) still captures the dataflow kernel in its step graph:
+    the per-context set-up needs a current context, which the library
+    creates before it."""
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", FRESH_PROCESS, root], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "KINDS [3, 3, 3]" in r.stdout
 
 
 def test_jacobi_against_fp64_oracle(gpu):
