@@ -1228,7 +1228,9 @@ def run_ours(args):
             "host_ms_per_step": 1e3 * t_host / args.steps,
             "stage_ms": stage_ms,
             "step_stats": {"div_l2_post": st["div_l2_post"], "resid_l2": st["resid_l2"],
-                           "smoke_mass": st["smoke_mass"], "sweeps": st["sweeps"]},
+                           "smoke_mass": st["smoke_mass"], "sweeps": st["sweeps"],
+                           "jacobi_kernel": {0: "none", 1: "sweep", 2: "tma",
+                                             3: "dataflow"}[st["jacobi_kernel"]]},
         }
         print(json.dumps(line), flush=True)
     if world > 1:

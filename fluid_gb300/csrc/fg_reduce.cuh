@@ -200,7 +200,22 @@ __global__ void __launch_bounds__(1024)
   __shared__ float row[2 * NS];
   FF v[NS];
   slots_identity<NS>(v, max_mask);
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+  // U rows' loads are issued before their merges (in the same order), so
+  // a thread waits for one round trip per U rows instead of one per row.
+  constexpr int U = NS > 2 ? 4 : 8;
+  int k = threadIdx.x;
+  for (; k + (U - 1) * (int)blockDim.x < n; k += U * blockDim.x) {
+    FF w[U][NS];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const size_t r = (size_t)(k + q * blockDim.x) * 2 * NS;
+#pragma unroll
+      for (int s = 0; s < NS; ++s) w[q][s] = FF{in[r + 2 * s], in[r + 2 * s + 1]};
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) slots_merge<NS>(v, w[q], max_mask);
+  }
+  for (; k < n; k += blockDim.x) {
     FF w[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s)

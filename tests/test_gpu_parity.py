@@ -443,6 +443,54 @@ def test_stage_entry_points_bitwise(gpu):
         assert_bitwise(g, o, where=name)
 
 
+@pytest.mark.parametrize("w,h", [(1, 1), (2, 3), (3, 30), (31, 7), (33, 34), (62, 29), (95, 70),
+                                 (130, 66)])
+def test_bfecc_stages_bitwise_across_strip_alignments(gpu, w, h):
+    """The velocity passes run four rows per thread, blocks of 32 x 32
+    cells; strips that reach the ghost ring or pass the last row run cell by
+    cell.  Grids whose rows end inside a strip, with fewer rows than a
+    strip, or one cell wide, with an obstacle and random state: BFECC and
+    plain advection stay bit for bit the oracle's."""
+    g, o = both(gpu, w, h, Confinement=0.3)
+    for f in (g, o):
+        f.S[:] = 1.0
+        if w > 4 and h > 4:
+            f.S[(w // 2) * f.NumY + h // 2] = 0.0
+        scenes.random_state(f, seed=w * 1000 + h, amp=2.0)
+    for name in ("advectVelocityBFECC", "advectSmokeBFECC", "advectVelocity", "advectSmoke"):
+        for f in (g, o):
+            getattr(f, name)(0.4)
+        assert_bitwise(g, o, where="%s %dx%d" % (name, w, h))
+
+
+def test_bfecc_clamp_ties_and_nan_centres(gpu):
+    """The velocity correction forms clampToNeighbors' 3x3 range with min /
+    max trees; it must end on the same element as the reference's scan,
+    including -0/+0 ties (a zero extreme with a nonzero centre, decided by
+    scan order), zero centres, and NaN centres (never replaced) or NaN
+    neighbours (skipped).  Fields drawn from {-1, -0, +0, 1/2, 1} with a
+    few NaNs; every bit equal to the oracle's except NaN payloads, which
+    the two machines form differently (all NaNs compare equal here)."""
+    g, o = both(gpu, 61, 43)
+    rng = np.random.default_rng(12)
+    vals = np.array([-1.0, -0.0, 0.0, 0.5, 1.0], np.float32)
+    U = vals[rng.integers(0, 5, g.numCells)]
+    V = vals[rng.integers(0, 5, g.numCells)]
+    for a in (U, V):
+        a[rng.integers(0, g.numCells, 6)] = np.nan
+    for f in (g, o):
+        f.S[:] = 1.0
+        f.U[:] = U
+        f.V[:] = V
+        f.advectVelocityBFECC(0.3)
+    for k in ("U", "V", "newU", "newV"):
+        a, b = getattr(g, k), getattr(o, k)
+        same = (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))
+        assert same.all(), (k, int((~same).sum()))
+    # The ties occur: zero extremes with a nonzero centre are in the data.
+    assert (np.signbit(U) & (U == 0)).sum() > 100
+
+
 def test_invalid_mask_fails_loudly(gpu):
     f = gpu.Fluid(1.0, 8, 8, 1.0)
     f.S[:] = 0.5
