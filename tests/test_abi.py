@@ -84,3 +84,39 @@ def test_noalloc_sweep_counts_near_int_max_are_rejected():
         rc = L.fg_project_noalloc(dummy, dummy, dummy, dummy, 16, 16, 16, 1.0, 1.0, 0.1, iters,
                                   1.0, 1.0, tb, 0, 1e-5, None)
         assert rc == _lib.FG_ERR_TOO_LARGE, (iters, tb, rc)
+
+
+def test_struct_layouts_and_constants_match_the_header(tmp_path):
+    """The ctypes mirrors of fg_params and fg_stats have the C layout (every
+    field's offset and the size), and the FG_JACOBI_KERNEL_* values are the
+    Python constants: a C probe compiled against include/fluidgpu.h prints
+    them."""
+    import shutil
+    import subprocess
+
+    import fluid_gb300
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "fluidgpu.h"', "int main(void) {"]
+    for cname, pyt in (("fg_params", _lib.Params), ("fg_stats", _lib.Stats)):
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for name, _ in pyt._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, name, cname, name))
+    for k in ("NONE", "SWEEP", "TMA", "DATAFLOW"):
+        lines.append('printf("FG_JACOBI_KERNEL_%s %%d\\n", FG_JACOBI_KERNEL_%s);' % (k, k))
+    lines.append("return 0; }")
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                         text=True).stdout.splitlines())
+    for cname, pyt in (("fg_params", _lib.Params), ("fg_stats", _lib.Stats)):
+        assert int(out["%s size" % cname]) == ctypes.sizeof(pyt), cname
+        for name, _ in pyt._fields_:
+            assert int(out["%s %s" % (cname, name)]) == getattr(pyt, name).offset, (cname, name)
+    for k in ("NONE", "SWEEP", "TMA", "DATAFLOW"):
+        assert int(out["FG_JACOBI_KERNEL_%s" % k]) == getattr(fluid_gb300, "JACOBI_KERNEL_%s" % k)
