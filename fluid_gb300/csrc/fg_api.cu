@@ -137,10 +137,29 @@ int check_mask(fg_fluid* f) {
 // reads the smoke buffer of the step before it; the next operation writes
 // the other buffer and may run beside it unless something writes M in place
 // (an upload, an edit, a smoke source); every later operation waits for it.
+// Issues the deferred smoke read-back on the copy stream once `after` (an
+// event of the handle's stream) has happened.
+int issue_async_copy(fg_fluid* f, cudaEvent_t after) {
+  if (!f->async_deferred) return FG_OK;
+  f->async_deferred = false;
+  CK(f, cudaStreamWaitEvent(f->copy_stream, after, 0), "copy event");
+  CK(f, cudaMemcpy2DAsync(f->hm[FG_M], sizeof(float) * f->NY, f->async_src, sizeof(float) * f->P,
+                          sizeof(float) * f->NY, f->NX, cudaMemcpyDeviceToHost, f->copy_stream),
+     "async download");
+  CK(f, cudaEventRecord(f->async_ev[1], f->copy_stream), "copy event");
+  return FG_OK;
+}
+
 int async_guard(fg_fluid* f) {
   if (!f->async_pending) return FG_OK;
   bool in_place = (f->dirty & FG_FIELD_BIT(FG_M)) || f->src_smoke;
   for (const EditRec& e : f->edits) in_place = in_place || e.field == (uint32_t)FG_M;
+  // A step that writes M only out of place starts the copy itself, after its
+  // projection; anything else starts it now.
+  if (in_place || !f->async_defer_ok || f->async_ops > 0) {
+    int rc = issue_async_copy(f, f->async_ev[0]);
+    if (rc) return rc;
+  }
   if (in_place || f->async_ops > 0)
     CK(f, cudaStreamWaitEvent(f->stream, f->async_ev[1], 0), "async wait");
   f->async_ops++;
@@ -185,31 +204,33 @@ int flush(fg_fluid* f) {
       size_t ng = off.size() - 1;
       int sl = f->edit_slot;
       f->edit_slot ^= 1;
-      // The slot's previous upload must have left its pinned buffers.
+      // The edit kernel reads the log straight from the slot's pinned
+      // buffers (mapped into the device's address space: no upload); the
+      // slot's previous kernel must have finished reading them.
       CK(f, cudaEventSynchronize(f->edit_ev[sl]), "edit slot wait");
       if (ed.size() > f->edit_cap[sl] || off.size() > f->edit_cap[sl] + 1) {
         cudaFreeHost(f->edit_pinned[sl]);
         cudaFreeHost(f->edit_off_pinned[sl]);
-        cudaFree(f->edit_dev[sl]);
-        cudaFree(f->edit_off_dev[sl]);
+        f->edit_pinned[sl] = nullptr;
+        f->edit_off_pinned[sl] = nullptr;
+        f->edit_dev[sl] = nullptr;
+        f->edit_off_dev[sl] = nullptr;
+        f->edit_cap[sl] = 0;
         size_t cap = std::max<size_t>(ed.size(), off.size()) * 2;
         CK(f, host_malloc((void**)&f->edit_pinned[sl], cap * sizeof(EditRec)), "edit alloc");
         CK(f, host_malloc((void**)&f->edit_off_pinned[sl], (cap + 1) * sizeof(uint32_t)),
            "edit alloc");
-        CK(f, dev_malloc((void**)&f->edit_dev[sl], cap * sizeof(EditRec)), "edit alloc");
-        CK(f, dev_malloc((void**)&f->edit_off_dev[sl], (cap + 1) * sizeof(uint32_t)), "edit alloc");
+        CK(f, cudaHostGetDevicePointer((void**)&f->edit_dev[sl], f->edit_pinned[sl], 0),
+           "edit map");
+        CK(f, cudaHostGetDevicePointer((void**)&f->edit_off_dev[sl], f->edit_off_pinned[sl], 0),
+           "edit map");
         f->edit_cap[sl] = cap;
       }
       memcpy(f->edit_pinned[sl], ed.data(), ed.size() * sizeof(EditRec));
       memcpy(f->edit_off_pinned[sl], off.data(), off.size() * sizeof(uint32_t));
-      CK(f, cudaMemcpyAsync(f->edit_dev[sl], f->edit_pinned[sl], ed.size() * sizeof(EditRec),
-                            cudaMemcpyHostToDevice, f->stream), "edit upload");
-      CK(f, cudaMemcpyAsync(f->edit_off_dev[sl], f->edit_off_pinned[sl],
-                            off.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, f->stream),
-         "edit upload");
-      CK(f, cudaEventRecord(f->edit_ev[sl], f->stream), "edit event");
       f->edit_bytes += ed.size() * sizeof(EditRec) + off.size() * sizeof(uint32_t);
       CK(f, launch_apply_edits(f, (int)ng, sl), "apply edits");
+      CK(f, cudaEventRecord(f->edit_ev[sl], f->stream), "edit event");
     }
   }
   if (f->masks_stale) {
@@ -314,6 +335,14 @@ int enqueue_step(fg_fluid* f, float dt) {
   int rc = enqueue_pressure(f, p.num_iters, dt, fuse_turb);
   if (rc) return rc;
   mark(f, "gradient+div stats");
+  // The projection is done: a deferred smoke read-back of the step before
+  // may start (an event-record node when the step is being captured).
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(f, cudaStreamIsCapturing(f->stream, &cs), "capture status");
+  CK(f, cs == cudaStreamCaptureStatusActive
+            ? cudaEventRecordWithFlags(f->mid_ev, f->stream, cudaEventRecordExternal)
+            : cudaEventRecord(f->mid_ev, f->stream),
+     "mid-step event");
   if (!fuse_turb) CK(f, launch_confinement_turbulence(f, dt, conf, turb), "confinement/turbulence");
   CK(f, launch_borders(f), "borders");
   mark(f, "confinement/turbulence+borders");
@@ -411,6 +440,8 @@ int fg_create(int width, int height, float density, float h, const fg_params* pa
       return bail(FG_ERR_CUDA);
     if (cudaEventCreate(&f->prof_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
   }
+  if (cudaEventCreateWithFlags(&f->mid_ev, cudaEventDisableTiming) != cudaSuccess)
+    return bail(FG_ERR_CUDA);
   for (int k = 0; k < fg_fluid::kMaxMarks; ++k)
     if (cudaEventCreate(&f->mark_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
   for (int k = 0; k < FG_NUM_FIELDS; ++k)
@@ -480,6 +511,7 @@ int fg_destroy(fg_fluid* f) {
   if (f->copy_stream) cudaStreamDestroy(f->copy_stream);
   for (int k = 0; k < 2; ++k)
     if (f->async_ev[k]) cudaEventDestroy(f->async_ev[k]);
+  if (f->mid_ev) cudaEventDestroy(f->mid_ev);
   for (int k = 0; k < FG_NUM_FIELDS; ++k) {
     cudaFree(f->d[k]);
     cudaFree(f->partner[k]);
@@ -503,9 +535,7 @@ int fg_destroy(fg_fluid* f) {
   cudaFree(f->skew_flags);
   cudaFree(f->lex_scratch);
   for (int k = 0; k < 2; ++k) {
-    cudaFree(f->edit_dev[k]);
-    cudaFree(f->edit_off_dev[k]);
-    cudaFreeHost(f->edit_pinned[k]);
+    cudaFreeHost(f->edit_pinned[k]);  // edit_dev / edit_off_dev map these
     cudaFreeHost(f->edit_off_pinned[k]);
     if (f->edit_ev[k]) cudaEventDestroy(f->edit_ev[k]);
     if (f->prof_ev[k]) cudaEventDestroy(f->prof_ev[k]);
@@ -582,8 +612,8 @@ int fg_download(fg_fluid* f, unsigned mask) {
   return FG_OK;
 }
 
-// Starts copying the smoke field M of the work enqueued so far into its host
-// mirror on a second stream, so the copy runs beside the next step;
+// Copies the smoke field M of the work enqueued so far into its host mirror
+// on a second stream, beside the next step (after that step's projection);
 // fg_download_wait completes it (the mirror is not current until then).
 int fg_download_async(fg_fluid* f, unsigned mask) {
   if (is_batch(f)) return batch_unsupported(f);
@@ -599,12 +629,12 @@ int fg_download_async(fg_fluid* f, unsigned mask) {
     for (int k = 0; k < 2; ++k)
       CK(f, cudaEventCreateWithFlags(&f->async_ev[k], cudaEventDisableTiming), "copy event");
   }
+  // The copy is issued later: by the next step, once that step's
+  // projection is done (a copy beside the pressure solve slows it, whose
+  // arrays live in L2), or at once by anything else (issue_async_copy).
   CK(f, cudaEventRecord(f->async_ev[0], f->stream), "copy event");
-  CK(f, cudaStreamWaitEvent(f->copy_stream, f->async_ev[0], 0), "copy event");
-  CK(f, cudaMemcpy2DAsync(f->hm[FG_M], sizeof(float) * f->NY, f->d[FG_M], sizeof(float) * f->P,
-                          sizeof(float) * f->NY, f->NX, cudaMemcpyDeviceToHost, f->copy_stream),
-     "async download");
-  CK(f, cudaEventRecord(f->async_ev[1], f->copy_stream), "copy event");
+  f->async_src = f->d[FG_M];
+  f->async_deferred = true;
   f->async_pending = true;
   f->async_ops = 0;
   return FG_OK;
@@ -615,6 +645,7 @@ int fg_download_wait(fg_fluid* f) {
   if (!f->async_pending) return FG_OK;
   int rc = bind(f);
   if (rc) return rc;
+  if ((rc = issue_async_copy(f, f->async_ev[0]))) return rc;
   CK(f, cudaEventSynchronize(f->async_ev[1]), "async download");
   f->async_pending = false;
   // The mirror holds the copied frame; it is the device's M only if nothing
@@ -731,8 +762,23 @@ static int mg_prepare(fg_fluid* f) {
   return FG_OK;
 }
 
+static int simulate_enqueue(fg_fluid* f, float dt);
+
 int fg_simulate(fg_fluid* f, float dt) {
   if (!f) return FG_ERR_INVALID;
+  f->async_defer_ok = true;
+  int rc = simulate_enqueue(f, dt);
+  f->async_defer_ok = false;
+  // A read-back deferred to this step starts after its projection, or after
+  // the copied work when the step was not enqueued.
+  if (f->async_deferred) {
+    int rc2 = issue_async_copy(f, rc == FG_OK ? f->mid_ev : f->async_ev[0]);
+    if (!rc) rc = rc2;
+  }
+  return rc;
+}
+
+static int simulate_enqueue(fg_fluid* f, float dt) {
   int rc = flush(f);
   if (rc) return rc;
   ensure_skew(f);
@@ -1982,6 +2028,8 @@ int fg_batch_create(fg_fluid* const* scenes, int n, fg_fluid** out) {
       return bail(FG_ERR_CUDA);
     if (cudaEventCreate(&f->prof_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
   }
+  if (cudaEventCreateWithFlags(&f->mid_ev, cudaEventDisableTiming) != cudaSuccess)
+    return bail(FG_ERR_CUDA);
   for (int k = 0; k < fg_fluid::kMaxMarks; ++k)
     if (cudaEventCreate(&f->mark_ev[k]) != cudaSuccess) return bail(FG_ERR_CUDA);
   for (int k = 0; k < FG_NUM_FIELDS; ++k)

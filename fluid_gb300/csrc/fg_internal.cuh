@@ -311,8 +311,8 @@ struct fg_fluid {
   std::vector<fg::EditRec> edits;
   // Two staging slots for queued edits, used alternately; a slot is reused
   // once the event recorded after its upload has completed.
-  fg::EditRec* edit_pinned[2] = {};
-  fg::EditRec* edit_dev[2] = {};
+  fg::EditRec* edit_pinned[2] = {};   // the edit log, double-buffered (pinned)
+  fg::EditRec* edit_dev[2] = {};      // the same memory as the device addresses it
   uint32_t* edit_off_pinned[2] = {};
   uint32_t* edit_off_dev[2] = {};
   cudaEvent_t edit_ev[2] = {};
@@ -359,6 +359,13 @@ struct fg_fluid {
   cudaEvent_t async_ev[2] = {};
   bool async_pending = false;
   int async_ops = 0;
+  // A smoke read-back requested but not issued yet (fg_download_async): the
+  // buffer to copy, and whether the operation being enqueued is a step that
+  // issues it after its projection (mid_ev, recorded inside every step).
+  bool async_deferred = false;
+  const float* async_src = nullptr;
+  bool async_defer_ok = false;
+  cudaEvent_t mid_ev = nullptr;
   bool src_smoke = false;  // a persistent source writes M in place
   // Kernel launches enqueued so far (graph replays add the captured count).
   unsigned long long launches = 0;

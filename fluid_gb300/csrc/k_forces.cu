@@ -35,7 +35,8 @@ __global__ void k_build_flags(const float* __restrict__ S, uint8_t* __restrict__
 }
 
 // Queued tool edits, grouped by (field, cell) in call order: one thread per
-// group applies its set / add operations sequentially.
+// group applies its set / add operations sequentially.  recs and off are the
+// host's pinned edit log, read across the host link (no upload).
 struct FieldPtrs {
   float* p[FG_NUM_FIELDS];
 };

@@ -163,8 +163,8 @@ class Fluid:
         self._check(self._L.fg_download(self._h, mask), "fg_download")
 
     def download_async(self, mask=1 << FIELDS["M"]):
-        """Starts the smoke download beside the next step (download_wait
-        completes it)."""
+        """Copies the smoke field beside the next step, after its projection
+        (download_wait completes it)."""
         self._check(self._L.fg_download_async(self._h, mask), "fg_download_async")
 
     def download_wait(self):

@@ -151,13 +151,15 @@ int fg_field(fg_fluid* f, int field, float** host_ptr);
 int fg_mark_dirty(fg_fluid* f, unsigned mask);
 /* Copies the device fields in `mask` into their mirrors (waits). */
 int fg_download(fg_fluid* f, unsigned mask);
-/* Starts copying the smoke field (mask = FG_FIELD_BIT(FG_M); other fields:
+/* Copies the smoke field (mask = FG_FIELD_BIT(FG_M); other fields:
  * FG_ERR_UNSUPPORTED) of the work queued so far into its mirror on a second
- * stream and returns; the copy runs beside the next fg_simulate (which
- * writes the other smoke buffer).  The mirror is current after
- * fg_download_wait (fg_download and the next fg_download_async wait too);
- * do not read or write it before.  For a frame loop that reads the smoke
- * every frame: simulate, wait, read, start the next copy. */
+ * stream, and returns at once.  The copy runs beside the next fg_simulate
+ * (which writes the other smoke buffer), started once that step's pressure
+ * projection is done; any other call on the handle, and fg_download_wait,
+ * start it at once.  The mirror is current after fg_download_wait
+ * (fg_download and the next fg_download_async wait too); do not read or
+ * write it before.  For a frame loop that reads the smoke every frame:
+ * simulate, wait, read, start the next copy. */
 int fg_download_async(fg_fluid* f, unsigned mask);
 int fg_download_wait(fg_fluid* f);
 /* Waits for all queued work on the handle's stream. */
@@ -232,7 +234,8 @@ int fg_adaptive_time_step(fg_fluid* f, float basedt, float* out);               
  * fg_profile_jacobi waits and returns that span and its number of sweep
  * blocks (per-launch kernels, or phases of the one dataflow launch).
  * fg_launch_count is the number of kernels the handle has enqueued;
- * fg_edit_bytes the bytes of queued tool edits uploaded so far. */
+ * fg_edit_bytes the bytes of queued tool edits sent to the device so far
+ * (the edit kernel reads them from pinned host memory). */
 int fg_profile_enable(fg_fluid* f, int on);
 int fg_profile_jacobi(fg_fluid* f, float* ms, int* launches);
 /* Per-stage times (ms) of the last profiled step; returns the number of

@@ -691,6 +691,66 @@ def test_async_smoke_download_frames(gpu):
     assert np.array_equal(a.M.view(np.uint32), prev.view(np.uint32))
 
 
+@pytest.mark.parametrize("scheme,graphs", [(1, True), (0, True), (1, False)])
+def test_async_smoke_download_deferred_paths(gpu, scheme, graphs):
+    """fg_download_async leaves the copy to the next step, which starts it
+    once its projection is done; every other path starts it at once.  The
+    mirror must hold the smoke of the frame the call was made after: with
+    two steps before the wait (the second waits for the copy before it
+    overwrites that buffer), a stage call or a view in between, a wait right
+    away, and a synchronous download while a copy is deferred."""
+    kw = dict(scheme=scheme, UseBFECC=True, use_graphs=graphs, auto_sync=False)
+    if scheme == 1:
+        kw.update(num_iters=24, tb_depth=8, early_exit=False)
+    a = gpu.Fluid(1.0, 150, 170, 1.0, **kw)
+    b = gpu.Fluid(1.0, 150, 170, 1.0, **kw)
+    for f in (a, b):
+        scenes.fast_walls(f)
+        f.mark_dirty()
+        rows = np.array(list(scenes.jet_rows(f)), np.int32)
+        f.set_sources(np.ones_like(rows), rows, u=2.0, v=0.0, smoke=0.5,
+                      mode=f.SRC_SKIP_SOLID | f.SRC_SET_VELOCITY | f.SRC_SET_SMOKE)
+    mbit = 1 << gpu.FIELDS["M"]
+
+    def ref():
+        b.download(mbit)
+        return b.M.copy()
+
+    def same(x, y, what):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), what
+
+    for f in (a, b):
+        for _ in range(3):
+            f.Simulate(0.1)
+    for rnd in range(3):
+        want = ref()
+        # Two steps before the wait.
+        a.download_async()
+        for f in (a, b):
+            f.Simulate(0.1)
+            f.Simulate(0.1)
+        a.download_wait()
+        same(a.M, want, "two steps, round %d" % rnd)
+        # A stage call and a view before the wait.
+        want = ref()
+        a.download_async()
+        for f in (a, b):
+            f.advectSmoke(0.05)
+            f.Vorticity()
+        a.download_wait()
+        same(a.M, want, "stage and view, round %d" % rnd)
+        # The wait at once, then a synchronous download while one is deferred.
+        want = ref()
+        a.download_async()
+        a.download_wait()
+        same(a.M, want, "wait at once, round %d" % rnd)
+        a.download_async()
+        for f in (a, b):
+            f.Simulate(0.1)
+        a.download(mbit)
+        same(a.M, ref(), "synchronous download, round %d" % rnd)
+
+
 def test_jet128_against_golden_fixtures(gpu):
     """The 128x128 jet of the golden fixtures (200 steps, 40 iterations, the
     reference's early exit): the GPU's reference scheme equals the FP32
