@@ -335,14 +335,20 @@ int enqueue_step(fg_fluid* f, float dt) {
   int rc = enqueue_pressure(f, p.num_iters, dt, fuse_turb);
   if (rc) return rc;
   mark(f, "gradient+div stats");
-  // The projection is done: a deferred smoke read-back of the step before
-  // may start (an event-record node when the step is being captured).
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  CK(f, cudaStreamIsCapturing(f->stream, &cs), "capture status");
-  CK(f, cs == cudaStreamCaptureStatusActive
-            ? cudaEventRecordWithFlags(f->mid_ev, f->stream, cudaEventRecordExternal)
-            : cudaEventRecord(f->mid_ev, f->stream),
-     "mid-step event");
+  // The projection is done: a smoke read-back deferred to this step may
+  // start (an event-record node when the step is captured).  Only steps
+  // with a deferred read-back record it, and they are captured into graphs
+  // of their own: the node costs a replay about 4 us.  (Recorded on a side
+  // branch of the graph instead, it cost 2.5 us, but the copy then started
+  // later and the step with the read-back ran 7-9 us longer.)
+  if (f->step_mid) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(f, cudaStreamIsCapturing(f->stream, &cs), "capture status");
+    CK(f, cs == cudaStreamCaptureStatusActive
+              ? cudaEventRecordWithFlags(f->mid_ev, f->stream, cudaEventRecordExternal)
+              : cudaEventRecord(f->mid_ev, f->stream),
+       "mid-step event");
+  }
   if (!fuse_turb) CK(f, launch_confinement_turbulence(f, dt, conf, turb), "confinement/turbulence");
   CK(f, launch_borders(f), "borders");
   mark(f, "confinement/turbulence+borders");
@@ -769,6 +775,7 @@ int fg_simulate(fg_fluid* f, float dt) {
   f->async_defer_ok = true;
   int rc = simulate_enqueue(f, dt);
   f->async_defer_ok = false;
+  f->step_mid = false;
   // A read-back deferred to this step starts after its projection, or after
   // the copied work when the step was not enqueued.
   if (f->async_deferred) {
@@ -781,6 +788,7 @@ int fg_simulate(fg_fluid* f, float dt) {
 static int simulate_enqueue(fg_fluid* f, float dt) {
   int rc = flush(f);
   if (rc) return rc;
+  f->step_mid = f->async_deferred;
   ensure_skew(f);
   if ((rc = check_iters(f, f->prm.num_iters))) return rc;
   if ((rc = mg_prepare(f))) return rc;
@@ -793,7 +801,8 @@ static int simulate_enqueue(fg_fluid* f, float dt) {
   uint32_t dtb;
   memcpy(&dtb, &dt, 4);
   for (auto& g : f->graphs) {
-    if (g.dt_bits == dtb && g.version == f->params_version && memcmp(g.key, key, sizeof key) == 0) {
+    if (g.dt_bits == dtb && g.version == f->params_version && g.mid == f->step_mid &&
+        memcmp(g.key, key, sizeof key) == 0) {
       CK(f, cudaGraphLaunch(g.exec, f->stream), "graph launch");
       f->launches += g.launches;
       // Apply the pointer rotation the captured step performed.
@@ -813,6 +822,7 @@ static int simulate_enqueue(fg_fluid* f, float dt) {
   memcpy(ent.key, key, sizeof key);
   ent.dt_bits = dtb;
   ent.version = f->params_version;
+  ent.mid = f->step_mid;
   // The Jacobi kernels' per-context set-up cannot run inside a capture: do
   // it first (a no-op once done), so the captured step gets the TMA-fed and
   // dataflow kernels even if this thread's context changed since fg_create.

@@ -365,6 +365,7 @@ struct fg_fluid {
   bool async_deferred = false;
   const float* async_src = nullptr;
   bool async_defer_ok = false;
+  bool step_mid = false;  // the step being enqueued records mid_ev
   cudaEvent_t mid_ev = nullptr;
   bool src_smoke = false;  // a persistent source writes M in place
   // Kernel launches enqueued so far (graph replays add the captured count).
@@ -389,6 +390,7 @@ struct fg_fluid {
     unsigned long long launches;  // kernels in the graph
     uint32_t dt_bits;
     uint64_t version;
+    bool mid;  // records mid_ev after the projection (a read-back is deferred to the step)
     cudaGraphExec_t exec;
   };
   std::vector<GraphEntry> graphs;
