@@ -1801,7 +1801,7 @@ __global__ void k_grad(float* __restrict__ U, float* __restrict__ V, float* __re
 // U, V.  Reads U, V and writes the rotated buffers Uo, Vo, so the divergence
 // can recompute a neighbour's projected face from its original value.  A
 // thread handles GR consecutive cells of one column (k_grad_fused below).
-constexpr int GR = 4;
+constexpr int GR = 8;
 struct GradAcc {
   FF d2, r2;
   float dmax, rmax, n;
