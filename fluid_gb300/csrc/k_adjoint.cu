@@ -972,7 +972,6 @@ cudaError_t launch_loss_seed(fg_fluid* f, const float* target, double* dev_loss)
 cudaError_t launch_step_adjoint(fg_fluid* f, float dt, float* const* tape) {
   const fg_params& p = f->prm;
   const Grid& g = f->g;
-  dim3 gr = cell_grid(f), bl(BX, BY);
   size_t bytes = sizeof(float) * (size_t)f->NX * f->P;
   float** A = f->adj;
   using F = fg_fluid;

@@ -328,9 +328,6 @@ __device__ __forceinline__ int cl_ld(uint32_t a) {
   asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
   return v;
 }
-__device__ __forceinline__ void cl_st(uint32_t a, int v) {
-  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
-}
 __device__ __forceinline__ void cl_st8(uint32_t a, unsigned v) {
   asm volatile("st.shared::cluster.u8 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
@@ -2103,11 +2100,11 @@ unsigned long long context_key() {
   std::call_once(g_ctx_once, [] {
     cudaDriverEntryPointQueryResult q;
     void* fn = nullptr;
-    if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &fn, cudaEnableDefault, &q) == cudaSuccess &&
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       g_ctx_current = reinterpret_cast<PfnCtxGetCurrent>(fn);
     fn = nullptr;
-    if (cudaGetDriverEntryPoint("cuCtxGetId", &fn, cudaEnableDefault, &q) == cudaSuccess &&
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       g_ctx_id = reinterpret_cast<PfnCtxGetId>(fn);
     cudaGetLastError();
@@ -2160,7 +2157,7 @@ void init_jacobi_tma() {
   std::call_once(g_encode_once, [] {
     cudaDriverEntryPointQueryResult q;
     void* fn = nullptr;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) ==
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
