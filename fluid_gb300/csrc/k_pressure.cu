@@ -2386,8 +2386,10 @@ static cudaError_t jacobi_solve_batch(fg_fluid* f, PCtl* ctl, const float* bw, f
   return cudaGetLastError();
 }
 
+// kind: where to record the kernel that ran the sweeps (the main solve's).
 static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const float* bw, float* x0,
-                                float* x1, int iters, bool allow_exit, bool rinit = false) {
+                                float* x1, int iters, bool allow_exit, bool rinit = false,
+                                int* kind = nullptr) {
   if (f->batch) return jacobi_solve_batch(f, ctl, bw, x0, x1);
   int T = clamp_tb(f->prm.tb_depth);
   const long long nlaunch = ((long long)iters + T - 1) / T;
@@ -2406,7 +2408,7 @@ static cudaError_t jacobi_solve(fg_fluid* f, PCtl* ctl, const float* b, const fl
     e = enqueue_jacobi(f->stream, f->g, ctl, b, bw, f->wgt, f->flags, x0, x1, iters, T,
                        f->prm.jacobi_omega * f->prm.pressure_damping, check, f->prm.tolerance, &n,
                        nullptr, nullptr, nullptr, nullptr, nullptr, &f->dstats->timeout,
-                       f->tile_done, f->stall_tile, -1, &f->jacobi_kernel);
+                       f->tile_done, f->stall_tile, -1, kind);
   count(f, n);
   if (e != cudaSuccess) return e;
   if (prof) {
@@ -3031,7 +3033,8 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   mark(f, "pressure setup");
   if (num_iters > 0) {
     e = mgs ? mg_solve(f, num_iters, om)
-            : jacobi_solve(f, ctl, f->rhs, f->bw, f->phi, f->phi2, num_iters, true);
+            : jacobi_solve(f, ctl, f->rhs, f->bw, f->phi, f->phi2, num_iters, true, false,
+                           &f->jacobi_kernel);
     if (e != cudaSuccess) return e;
   }
   mark(f, "jacobi sweeps");
