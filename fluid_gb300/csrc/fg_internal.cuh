@@ -76,6 +76,16 @@ __device__ __forceinline__ float go_max(float a, float b) {
 }
 __device__ __forceinline__ float fbit(uint8_t f, uint8_t bit) { return (f & bit) ? 1.0f : 0.0f; }
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may be
+// scheduled while the kernel before it on the stream still runs; it calls
+// pdl_enter before touching global memory, which waits for that kernel to
+// complete (its writes visible) and lets the kernel after it be scheduled in
+// turn.  Both instructions are no-ops in a plain launch.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // The bilinear stencil of one sample: corner indices, weights and whether
 // each coordinate lies inside the clamp range.
 struct Bilin {
@@ -490,6 +500,25 @@ inline dim3 reduce_grid(const fg_fluid* f) {
 // True when a reduction with `ns` partials per block over `nb` blocks, plus
 // its two-level combine, fits the partials buffer without reaching the
 // scalar result slots at its end.
+// Launches kernel k(args...) with programmatic stream serialization: it may
+// be scheduled before the previous kernel on `st` finishes and must call
+// pdl_enter first (see above).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 inline bool partials_fit(const fg_fluid* f, int ns, int nb) {
   size_t rows = (size_t)nb + (size_t)((nb + 2047) / 2048) + 1;
   return 2 * (size_t)ns * rows + 8 <= (size_t)f->n_partials;

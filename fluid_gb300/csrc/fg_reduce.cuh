@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(1024)
     k_combine_store(const float* __restrict__ in, int n, unsigned max_mask, Store store) {
   __shared__ float sh[64 * NS];
   __shared__ float row[2 * NS];
+  pdl_enter();
   FF v[NS];
   slots_identity<NS>(v, max_mask);
   // U rows' loads are issued before their merges (in the same order), so

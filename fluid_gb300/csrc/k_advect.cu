@@ -274,6 +274,7 @@ __global__ void k_bfecc_vel_correct(const float* __restrict__ Ui, const float* _
                                     const float* __restrict__ Fu, const float* __restrict__ Fv,
                                     float* __restrict__ Cu, float* __restrict__ Cv,
                                     const uint8_t* __restrict__ flags, float dt, Grid g) {
+  pdl_enter();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
@@ -342,6 +343,7 @@ __global__ void k_sl_smoke(const float* __restrict__ Ut, const float* __restrict
                            int diffuse, float smokeDiffusion, float* __restrict__ mass_part,
                            Grid g) {
   __shared__ float sh[64];
+  pdl_enter();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   FF mass{0.0f, 0.0f};
@@ -395,6 +397,7 @@ __global__ void k_bfecc_smoke_fwd(const float* __restrict__ Ut, const float* __r
                                   float* __restrict__ Fm, const uint8_t* __restrict__ flags,
                                   float dt, float smokeAdv, int diffuse, float smokeDiffusion,
                                   Grid g) {
+  pdl_enter();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
@@ -433,6 +436,7 @@ __global__ void k_bfecc_smoke_correct(const float* __restrict__ Ut, const float*
                                       const float* __restrict__ Mi, const float* __restrict__ Fm,
                                       float* __restrict__ Cm, const uint8_t* __restrict__ flags,
                                       float dt, float smokeAdv, Grid g) {
+  pdl_enter();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
@@ -468,6 +472,7 @@ __global__ void __launch_bounds__(256, 4)
     k_vel_strip(const float* __restrict__ Ui, const float* __restrict__ Vi, float* __restrict__ Uo,
                 float* __restrict__ Vo, float* nU, float* nV, const uint8_t* __restrict__ flags,
                 float dt, Grid g) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i0 = (blockIdx.y * blockDim.y + threadIdx.y) * R;
   if (j >= g.NY || i0 >= g.NX) return;
@@ -526,9 +531,8 @@ static void sl_velocity_pass(fg_fluid* f, const float* Ui, const float* Vi, floa
                    f->d[FG_NEWU], f->d[FG_NEWV], (const uint8_t*)f->flags, dt);
     return;
   }
-  k_vel_strip<kStripRows, 1><<<strip_grid(f), dim3(BX, BY), 0, f->stream>>>(
-      Ui, Vi, f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV], f->flags, dt,
-      f->g);
+  launch_pdl(k_vel_strip<kStripRows, 1>, strip_grid(f), dim3(BX, BY), 0, f->stream, Ui, Vi,
+             f->partner[FG_U], f->partner[FG_V], f->d[FG_NEWU], f->d[FG_NEWV], f->flags, dt, f->g);
 }
 
 cudaError_t launch_advect_velocity(fg_fluid* f, float dt) {
@@ -558,9 +562,8 @@ static cudaError_t smoke_pass(fg_fluid* f, const float* Ms, float dt) {
   }
   dim3 gr = cell_grid(f);
   if (!partials_fit(f, 1, gr.x * gr.y)) return cudaErrorInvalidValue;
-  k_sl_smoke<<<gr, dim3(BX, BY), 0, f->stream>>>(f->d[FG_U], f->d[FG_V], Ms, f->partner[FG_M],
-                                                 f->d[FG_NEWM], f->flags, dt, sa, diffuse, sd,
-                                                 f->partials, f->g);
+  launch_pdl(k_sl_smoke, gr, dim3(BX, BY), 0, f->stream, f->d[FG_U], f->d[FG_V], Ms,
+             f->partner[FG_M], f->d[FG_NEWM], f->flags, dt, sa, diffuse, sd, f->partials, f->g);
   swap_state(f, FG_M);
   return launch_store_mass(f, gr.x * gr.y);
 }
@@ -574,17 +577,17 @@ cudaError_t launch_advect_velocity_bfecc(fg_fluid* f, float dt) {
                    (const float*)f->d[FG_NEWU], (const float*)f->d[FG_NEWV], f->fwdU, f->fwdV,
                    (const uint8_t*)f->flags, dt);
   else
-    k_vel_strip<kStripRows, 0><<<strip_grid(f), dim3(BX, BY), 0, f->stream>>>(
-        f->d[FG_U], f->d[FG_V], f->fwdU, f->fwdV, f->d[FG_NEWU], f->d[FG_NEWV], f->flags, dt,
-        f->g);
+    launch_pdl(k_vel_strip<kStripRows, 0>, strip_grid(f), dim3(BX, BY), 0, f->stream,
+               f->d[FG_U], f->d[FG_V], f->fwdU, f->fwdV, f->d[FG_NEWU], f->d[FG_NEWV], f->flags,
+               dt, f->g);
   count(f);
   if (f->batch)
     FG_CELLS_BATCH(f, bfecc_vel_correct_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V],
                    (const float*)f->fwdU, (const float*)f->fwdV, f->corrU, f->corrV,
                    (const uint8_t*)f->flags, dt);
   else
-    k_bfecc_vel_correct<<<cell_grid(f), dim3(BX, BY), 0, f->stream>>>(
-        f->d[FG_U], f->d[FG_V], f->fwdU, f->fwdV, f->corrU, f->corrV, f->flags, dt, f->g);
+    launch_pdl(k_bfecc_vel_correct, cell_grid(f), dim3(BX, BY), 0, f->stream, f->d[FG_U],
+               f->d[FG_V], f->fwdU, f->fwdV, f->corrU, f->corrV, f->flags, dt, f->g);
   // Pass 4 (fluid.go:991-993): advect the corrected field with itself.
   sl_velocity_pass(f, f->corrU, f->corrV, dt);
   swap_state(f, FG_U);
@@ -597,13 +600,22 @@ cudaError_t launch_advect_smoke_bfecc(fg_fluid* f, float dt) {
   float sd = smoke_diffusion(f, dt, &diffuse);
   float sa = f->prm.smoke_advection;
   count(f);
-  FG_CELLS(f, k_bfecc_smoke_fwd, bfecc_smoke_fwd_cell, (const float*)f->d[FG_U],
-           (const float*)f->d[FG_V], (const float*)f->d[FG_M], (const float*)f->d[FG_NEWM],
-           f->fwdM, (const uint8_t*)f->flags, dt, sa, diffuse, sd);
+  if (f->batch)
+    FG_CELLS_BATCH(f, bfecc_smoke_fwd_cell, (const float*)f->d[FG_U], (const float*)f->d[FG_V],
+                   (const float*)f->d[FG_M], (const float*)f->d[FG_NEWM], f->fwdM,
+                   (const uint8_t*)f->flags, dt, sa, diffuse, sd);
+  else
+    launch_pdl(k_bfecc_smoke_fwd, cell_grid(f), dim3(BX, BY), 0, f->stream, f->d[FG_U],
+               f->d[FG_V], f->d[FG_M], f->d[FG_NEWM], f->fwdM, f->flags, dt, sa, diffuse, sd,
+               f->g);
   count(f);
-  FG_CELLS(f, k_bfecc_smoke_correct, bfecc_smoke_correct_cell, (const float*)f->d[FG_U],
-           (const float*)f->d[FG_V], (const float*)f->d[FG_M], (const float*)f->fwdM, f->corrM,
-           (const uint8_t*)f->flags, dt, sa);
+  if (f->batch)
+    FG_CELLS_BATCH(f, bfecc_smoke_correct_cell, (const float*)f->d[FG_U],
+                   (const float*)f->d[FG_V], (const float*)f->d[FG_M], (const float*)f->fwdM,
+                   f->corrM, (const uint8_t*)f->flags, dt, sa);
+  else
+    launch_pdl(k_bfecc_smoke_correct, cell_grid(f), dim3(BX, BY), 0, f->stream, f->d[FG_U],
+               f->d[FG_V], f->d[FG_M], f->fwdM, f->corrM, f->flags, dt, sa, f->g);
   return smoke_pass(f, f->corrM, dt);
 }
 

@@ -184,7 +184,8 @@ cudaError_t launch_div_stats(fg_fluid* f) {
 cudaError_t launch_store_mass(fg_fluid* f, int nb) {
   if (!partials_fit(f, 1, nb)) return cudaErrorInvalidValue;
   count(f);
-  k_combine_store<1><<<1, 1024, 0, f->stream>>>(f->partials, nb, 0u, StoreMass{f->dstats});
+  launch_pdl(k_combine_store<1, StoreMass>, dim3(1), dim3(1024), 0, f->stream, f->partials, nb,
+             0u, StoreMass{f->dstats});
   return cudaGetLastError();
 }
 

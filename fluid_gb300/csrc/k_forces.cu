@@ -257,6 +257,7 @@ __device__ __forceinline__ void borders_border(int t, float* __restrict__ U, flo
 }
 __global__ void k_borders(float* __restrict__ U, float* __restrict__ V,
                           const uint8_t* __restrict__ flags, Grid g) {
+  pdl_enter();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   borders_border(t, U, V, flags, g);
 }
@@ -340,7 +341,13 @@ cudaError_t launch_confinement_turbulence(fg_fluid* f, float dt, bool conf, bool
 
 cudaError_t launch_borders(fg_fluid* f) {
   count(f);
-  FG_BORDER(f, k_borders, borders_border, f->d[FG_U], f->d[FG_V], (const uint8_t*)f->flags);
+  if (f->batch) {
+    FG_BORDER(f, k_borders, borders_border, f->d[FG_U], f->d[FG_V], (const uint8_t*)f->flags);
+  } else {
+    const int n = f->NX > f->NY ? f->NX : f->NY;
+    launch_pdl(k_borders, dim3((n + 127) / 128), dim3(128), 0, f->stream, f->d[FG_U], f->d[FG_V],
+               f->flags, f->g);
+  }
   return cudaGetLastError();
 }
 

@@ -1002,6 +1002,7 @@ __global__ void k_setup_system(const float* __restrict__ U, const float* __restr
                                float* __restrict__ W, float* __restrict__ BW,
                                const uint8_t* __restrict__ flags, float om, int zero_phi, Grid g,
                                int Ps, const float* __restrict__ Fu, const float* __restrict__ Fv) {
+  pdl_enter();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.NX || j >= g.NY) return;
@@ -1046,6 +1047,7 @@ __device__ __forceinline__ void jacobi_tile(
   __shared__ float4 xch[2][2][NWARP][32];
   __shared__ float red[NWARP];
   __shared__ int skip;
+  pdl_enter();
   if (threadIdx.x == 0) {
     int sk = ctl->stop;
     if (!sk && CHECK && k > 0 && __uint_as_float(ctl->slots[k - 1]) < tol) {
@@ -1952,6 +1954,7 @@ __global__ void __launch_bounds__(256)
                  const float* __restrict__ Fv, float* __restrict__ U2o,
                  float* __restrict__ V2o) {
   __shared__ float shr[64 * 5];
+  pdl_enter();
   const float* phi = ctl->sel ? phi1 : phi0;
   const float* e = ectl ? (ectl->sel ? e1 : e0) : nullptr;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -3027,9 +3030,9 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   // sel = 0 (phi) until a launch runs.
   if ((e = cudaMemsetAsync(ctl, 0, sizeof(PCtl), f->stream)) != cudaSuccess) return e;
   count(f);
-  k_setup_system<<<gr, bl, 0, f->stream>>>(f->d[FG_U], f->d[FG_V], f->phi, f->rhs, f->wgt, f->bw,
-                                           f->flags, om, num_iters == 0 ? 1 : 0, f->g, f->P,
-                                           f->step_fu, f->step_fv);
+  launch_pdl(k_setup_system, gr, bl, 0, f->stream, f->d[FG_U], f->d[FG_V], f->phi, f->rhs,
+             f->wgt, f->bw, f->flags, om, num_iters == 0 ? 1 : 0, f->g, f->P, f->step_fu,
+             f->step_fv);
   mark(f, "pressure setup");
   if (num_iters > 0) {
     e = mgs ? mg_solve(f, num_iters, om)
@@ -3049,16 +3052,16 @@ cudaError_t launch_pressure(fg_fluid* f, int num_iters, float dt, bool fuse_turb
   int nb = rg.x * rg.y;
   if (!partials_fit(f, 5, nb)) return cudaErrorInvalidValue;
   count(f);
-  k_grad_fused<<<rg, bl, 0, f->stream>>>(
-      f->d[FG_U], f->d[FG_V], f->partner[FG_U], f->partner[FG_V], f->d[FG_P], f->phi, f->phi2, ctl,
-      f->err, f->err2, refine ? ectl : nullptr, f->rhs, f->flags, cp, f->noise,
-      f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g, f->step_fu,
-      f->step_fv, f->step_u2, f->step_v2);
+  launch_pdl(k_grad_fused, rg, bl, 0, f->stream, f->d[FG_U], f->d[FG_V], f->partner[FG_U],
+             f->partner[FG_V], f->d[FG_P], f->phi, f->phi2, ctl, f->err, f->err2,
+             refine ? ectl : nullptr, f->rhs, f->flags, cp, f->noise,
+             f->prm.turbulence_strength * dt, fuse_turb ? 1 : 0, f->partials, f->g, f->step_fu,
+             f->step_fv, f->step_u2, f->step_v2);
   swap_state(f, FG_U);
   swap_state(f, FG_V);
   count(f);
-  k_combine_store<5><<<1, 1024, 0, f->stream>>>(f->partials, nb, 0x12u,
-                                                StoreDivP{f->dstats, num_iters > 0 ? ctl : nullptr});
+  launch_pdl(k_combine_store<5, StoreDivP>, dim3(1), dim3(1024), 0, f->stream, f->partials, nb,
+             0x12u, StoreDivP{f->dstats, num_iters > 0 ? ctl : nullptr});
   return cudaGetLastError();
 }
 
