@@ -227,10 +227,15 @@ struct BScene {
   int pad;
 };
 struct BTile {
-  int s, x, y, pad;  // scene, tile column, tile row
+  int s, x, y, pad;  // scene, tile column, tile row (per-cell and border tables)
 };
-// Cells a Jacobi thread block owns (rows x columns; k_pressure.cu).
-constexpr int kJacTileRows = 48, kJacTileCols = 112;
+// A Jacobi tile of a batch (k_pressure.cu) sweeps a region of 64 rows x 128
+// columns and writes the cells of it that are exact after its sweeps; its
+// BTile holds the region's first column and row in x and y and the owned
+// window in pad (region coordinates, one byte each: first row, end row,
+// first column, end column).  Inside the grid a region edge costs a halo of
+// 8 cells; at the grid's edge it costs none.
+constexpr int kJacRegionRows = 64, kJacRegionCols = 128, kJacHalo = 8;
 
 struct BatchGeom {
   int n = 0;

@@ -1027,7 +1027,17 @@ constexpr int RI = NWARP * RT;     // 64 region rows
 constexpr int OJ = RJ - 2 * TMAX;  // 112 owned columns
 constexpr int OI = RI - 2 * TMAX;  // 48 owned rows
 constexpr int TB_THREADS = 32 * NWARP;
-static_assert(OI == kJacTileRows && OJ == kJacTileCols, "batch Jacobi tiles");
+static_assert(RI == kJacRegionRows && RJ == kJacRegionCols && TMAX == kJacHalo,
+              "batch Jacobi tiles");
+// Owned window of a tile in region coordinates, one byte each: rows
+// [own & 255, own >> 8 & 255), columns [own >> 16 & 255, own >> 24).  A
+// region whose edge lies at or outside the grid's edge on a side needs no
+// halo there: the cells past the grid are zero and stay zero, and the
+// grid's outermost ring has w = bw = 0, so whatever a region-edge thread
+// reads beside it (a warp shuffle at lane 0 or 31 returns the thread's own
+// value) is multiplied by 0.
+constexpr uint32_t kOwnInner = (uint32_t)TMAX | (uint32_t)(RI - TMAX) << 8 |
+                               (uint32_t)TMAX << 16 | (uint32_t)(RJ - TMAX) << 24;
 
 // RINIT (first launch of the outer correction): instead of loading bw, the
 // kernel loads the main potential phi (from the buffer the main solve's
@@ -1038,7 +1048,7 @@ static_assert(OI == kJacTileRows && OJ == kJacTileCols, "batch Jacobi tiles");
 // follow, writes b_e and bw_e of the owned cells to rhs_e / bwe.
 template <bool OMEGA1, bool FULL, bool CHECK, bool RINIT>
 __device__ __forceinline__ void jacobi_tile(
-    int tbx, int tby, bool lead, const float* __restrict__ src, float* __restrict__ dst,
+    int ri0, int rj0, uint32_t own, bool lead, const float* __restrict__ src, float* __restrict__ dst,
     const float* __restrict__ W, const float* __restrict__ BW, const float* __restrict__ rhs,
     const uint8_t* __restrict__ flags, float om1, PCtl* ctl, int k, int t0, int ns, float tol,
     int out_sel, int zero_init, Grid g, const float* __restrict__ mphi0,
@@ -1059,10 +1069,12 @@ __device__ __forceinline__ void jacobi_tile(
   __syncthreads();
   if (skip) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int gi0 = tby * OI - TMAX + warp * RT;
-  const int gj = tbx * OJ - TMAX + lane * JT;
-  // gj is a multiple of 4 and the pitch a multiple of 4: a 4-column group is
-  // either wholly left of the grid or a 16-byte aligned read inside the row.
+  const int gi0 = ri0 + warp * RT;
+  const int gj = rj0 + lane * JT;
+  const int oi0 = own & 255, oi1 = own >> 8 & 255, oj0 = own >> 16 & 255, oj1 = own >> 24;
+  // gj is a multiple of 4 (rj0 is) and the pitch a multiple of 4: a 4-column
+  // group is either wholly left of the grid or a 16-byte aligned read inside
+  // the row.
   const bool colok = gj >= 0 && gj < g.P;
   float x[RT][JT], w[RT][JT], bw[RT][JT];
   uint32_t fr[RINIT ? RT : 1];
@@ -1092,7 +1104,7 @@ __device__ __forceinline__ void jacobi_tile(
         if (RINIT) fr[r] &= ~(0xffu << (8 * q));
       }
   }
-  const bool own_col = lane * JT >= TMAX && lane * JT < RJ - TMAX;
+  const bool own_col = lane * JT >= oj0 && lane * JT < oj1;
   if (RINIT) {
     // Residual of the main potential held in x, with b in bw.
     xch[1][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
@@ -1101,7 +1113,6 @@ __device__ __forceinline__ void jacobi_tile(
     float4 u4 = warp > 0 ? xch[1][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 d4 = warp < NWARP - 1 ? xch[1][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
     float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
-    const bool own_row_warp = warp >= TMAX / RT && warp < NWARP - TMAX / RT;
 #pragma unroll
     for (int r = 0; r < RT; ++r) {
       float lf = __shfl_up_sync(0xffffffffu, x[r][JT - 1], 1);
@@ -1128,7 +1139,7 @@ __device__ __forceinline__ void jacobi_tile(
         prev[q] = x[r][q];
         bw[r][q] = w[r][q] * be[q];
       }
-      if (rhs_e && own_col && own_row_warp) {
+      if (rhs_e && own_col && warp * RT + r >= oi0 && warp * RT + r < oi1) {
         int gi = gi0 + r;
         if (gi < g.NX && gj < g.NY) {
           size_t c = (size_t)gi * g.P + gj;
@@ -1188,7 +1199,7 @@ __device__ __forceinline__ void jacobi_tile(
       if (CHECK && last) {
         const int ri = warp * RT + r;
         const int gi = gi0 + r;
-        if (own_col && ri >= TMAX && ri < RI - TMAX && gi < g.NX && gj < g.NY) {
+        if (own_col && ri >= oi0 && ri < oi1 && gi < g.NX && gj < g.NY) {
           size_t c = (size_t)gi * g.P + gj;
           float4 b4 = *reinterpret_cast<const float4*>(rhs + c);
           uint32_t f4 = *reinterpret_cast<const uint32_t*>(flags + c);
@@ -1217,12 +1228,12 @@ __device__ __forceinline__ void jacobi_tile(
   } else {
     for (int sw = 0; sw < ns; ++sw) sweep(sw, sw == ns - 1);
   }
-  // Owned cells: rows TMAX..RI-TMAX-1, columns TMAX..RJ-TMAX-1.
-  if (own_col && warp >= TMAX / RT && warp < NWARP - TMAX / RT) {
+  // Owned cells: rows [oi0, oi1), columns [oj0, oj1) of the region.
+  if (own_col) {
 #pragma unroll
     for (int r = 0; r < RT; ++r) {
       int gi = gi0 + r;
-      if (gi >= g.NX || gj >= g.NY) continue;
+      if (warp * RT + r < oi0 || warp * RT + r >= oi1 || gi >= g.NX || gj >= g.NY) continue;
       size_t c = (size_t)gi * g.P + gj;
       if (gj + JT <= g.NY) {
         *reinterpret_cast<float4*>(dst + c) = make_float4(x[r][0], x[r][1], x[r][2], x[r][3]);
@@ -1263,8 +1274,9 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
                 const float* __restrict__ mphi0, const float* __restrict__ mphi1,
                 const PCtl* __restrict__ mctl, float* __restrict__ rhs_e,
                 float* __restrict__ bwe) {
-  jacobi_tile<OMEGA1, FULL, CHECK, RINIT>(blockIdx.x, blockIdx.y,
-                                          blockIdx.x == 0 && blockIdx.y == 0, src, dst, W, BW,
+  jacobi_tile<OMEGA1, FULL, CHECK, RINIT>((int)blockIdx.y * OI - TMAX, (int)blockIdx.x * OJ - TMAX,
+                                          kOwnInner, blockIdx.x == 0 && blockIdx.y == 0, src,
+                                          dst, W, BW,
                                           rhs, flags, om1, ctl, k, t0, ns, tol, out_sel,
                                           zero_init, g, mphi0, mphi1, mctl, rhs_e, bwe);
 }
@@ -1272,7 +1284,10 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
 // A batch's Jacobi launch k of L: scene s runs its nl_s = ceil(iters_s / T)
 // launches as the last nl_s of the L, the first of them with the remainder
 // sweeps, so every scene ends in the same buffer.  Blocks of scenes that
-// have not started return at once.
+// have not started return at once.  Each block's table entry gives its
+// region's origin and owned window (fg_internal.cuh): regions at a scene's
+// edges start or end there and own up to it, so a scene is cut into fewer
+// regions than whole 48 x 112 tiles with halos on every side.
 template <bool OMEGA1>
 __global__ void __launch_bounds__(TB_THREADS, 2)
     kb_jacobi(const BTile* __restrict__ tiles, const BScene* __restrict__ sc,
@@ -1287,12 +1302,12 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   const int ns = k == first ? s.iters - (nl - 1) * T : T;
   const long long o = s.off;
   if (ns == TMAX)
-    jacobi_tile<OMEGA1, true, false, false>(t.x, t.y, blockIdx.x == 0, src + o, dst + o, W + o,
+    jacobi_tile<OMEGA1, true, false, false>(t.y, t.x, (uint32_t)t.pad, blockIdx.x == 0, src + o, dst + o, W + o,
                                             BW + o, nullptr, flags + o, om1, ctl, k, 0, ns, 0.0f,
                                             out_sel, k == first, s.g, nullptr, nullptr, nullptr,
                                             nullptr, nullptr);
   else
-    jacobi_tile<OMEGA1, false, false, false>(t.x, t.y, blockIdx.x == 0, src + o, dst + o, W + o,
+    jacobi_tile<OMEGA1, false, false, false>(t.y, t.x, (uint32_t)t.pad, blockIdx.x == 0, src + o, dst + o, W + o,
                                              BW + o, nullptr, flags + o, om1, ctl, k, 0, ns, 0.0f,
                                              out_sel, k == first, s.g, nullptr, nullptr, nullptr,
                                              nullptr, nullptr);

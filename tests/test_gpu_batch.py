@@ -9,7 +9,10 @@ import scenes
 
 pytestmark = pytest.mark.gpu
 
-SIDES = [(30, 20), (64, 48), (17, 33), (100, 90), (40, 40), (128, 64), (9, 9)]
+# Grids (w + 2) x (h + 2): Jacobi regions of 64 rows x 128 columns cut them
+# into one to three regions per axis, starting and ending at scene edges.
+SIDES = [(30, 20), (64, 48), (17, 33), (100, 90), (40, 40), (128, 64), (9, 9), (150, 140),
+         (60, 250), (62, 126)]
 DT = 0.1
 
 
