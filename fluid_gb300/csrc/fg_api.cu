@@ -1920,26 +1920,6 @@ int upload_table(fg_fluid* f, T** dev, const std::vector<T>& host) {
   return FG_OK;
 }
 
-// Jacobi regions of length R along an axis of n cells: the first starts at
-// the grid's edge (no halo needed there), each next one kJacHalo before the
-// end of what the last one owns, and the one that reaches n owns up to n.
-// Starts stay multiples of 4 (the column loads are 16-byte vectors): the
-// first is 0 and every owned end before the last is a multiple of 4.
-struct JacSpan {
-  int a, o0, o1;  // region start; owned cells [a + o0, a + o1)
-};
-std::vector<JacSpan> jacobi_spans(int n, int R) {
-  std::vector<JacSpan> out;
-  int pos = 0;
-  while (pos < n) {
-    const int a = pos == 0 ? 0 : pos - kJacHalo;
-    const int end = a + R >= n ? n : a + R - kJacHalo;
-    out.push_back(JacSpan{a, pos - a, end - a});
-    pos = end;
-  }
-  return out;
-}
-
 // Block table of the per-cell kernels for a bx x by thread-block shape.
 int batch_cell_tiles(fg_fluid* f, int bx, int by) {
   fg::BatchGeom* b = f->batch;
@@ -2094,11 +2074,12 @@ int fg_batch_create(fg_fluid* const* scenes, int n, fg_fluid** out) {
   for (int s : batch_order(b)) {
     const Grid& g = b->scenes[s].g;
     for (int t = 0; t < (std::max(g.NX, g.NY) + 127) / 128; ++t) bt.push_back(BTile{s, t, 0, 0});
-    for (const JacSpan& ti : jacobi_spans(g.NX, kJacRegionRows))
-      for (const JacSpan& tj : jacobi_spans(g.NY, kJacRegionCols))
-        jt.push_back(BTile{s, tj.a, ti.a,
-                           (int)((uint32_t)ti.o0 | (uint32_t)ti.o1 << 8 | (uint32_t)tj.o0 << 16 |
-                                 (uint32_t)tj.o1 << 24)});
+    for (int ti = 0; ti < span_count(g.NX, kJacRegionRows); ++ti)
+      for (int tj = 0; tj < span_count(g.NY, kJacRegionCols); ++tj)
+        jt.push_back(BTile{s, tj * (kJacRegionCols - 2 * kJacHalo),
+                           ti * (kJacRegionRows - 2 * kJacHalo),
+                           (int)(span_own(ti, g.NX, kJacRegionRows) |
+                                 span_own(tj, g.NY, kJacRegionCols) << 16)});
   }
   if ((rc = upload_table(f, &b->border_tiles, bt)) || (rc = upload_table(f, &b->jac_tiles, jt)))
     return bail(rc);

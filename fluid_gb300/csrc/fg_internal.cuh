@@ -229,13 +229,28 @@ struct BScene {
 struct BTile {
   int s, x, y, pad;  // scene, tile column, tile row (per-cell and border tables)
 };
-// A Jacobi tile of a batch (k_pressure.cu) sweeps a region of 64 rows x 128
-// columns and writes the cells of it that are exact after its sweeps; its
-// BTile holds the region's first column and row in x and y and the owned
-// window in pad (region coordinates, one byte each: first row, end row,
-// first column, end column).  Inside the grid a region edge costs a halo of
-// 8 cells; at the grid's edge it costs none.
+// A per-launch Jacobi block (k_pressure.cu) sweeps a region of 64 rows x
+// 128 columns in registers and writes the cells of it that are exact after
+// its sweeps.  Inside the grid a region edge costs a halo of 8 cells; at the
+// grid's edge it costs none: the cells past the grid are zero and stay zero,
+// and the grid's outermost ring has w = bw = 0, so whatever a region-edge
+// thread reads beside it (a warp shuffle at lane 0 or 31 returns the
+// thread's own value) is multiplied by 0.  Along an axis of n cells, region
+// t of length R starts at t S (S = R - 2 halo); the first owns from the
+// grid's edge, the one that reaches n owns up to n, the others own [t S +
+// halo, t S + R - halo).  A batch's Jacobi BTile holds the region's first
+// column and row in x and y and the owned window in pad.
 constexpr int kJacRegionRows = 64, kJacRegionCols = 128, kJacHalo = 8;
+__host__ __device__ inline int span_count(int n, int R) {
+  const int S = R - 2 * kJacHalo;
+  return n <= R ? 1 : (n - R + S - 1) / S + 1;
+}
+// Owned window of region t in region coordinates: first | end << 8.
+__host__ __device__ inline uint32_t span_own(int t, int n, int R) {
+  const int a = t * (R - 2 * kJacHalo);
+  const uint32_t lo = t ? kJacHalo : 0, hi = a + R >= n ? n - a : R - kJacHalo;
+  return lo | hi << 8;
+}
 
 struct BatchGeom {
   int n = 0;

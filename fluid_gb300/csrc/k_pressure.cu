@@ -1014,10 +1014,13 @@ __global__ void k_setup_system(const float* __restrict__ U, const float* __restr
 // RT = 8 rows by JT = 4 consecutive columns.  Vertical neighbours come from
 // the thread's own rows, or through shared memory from the warp above/below
 // at its first/last row; horizontal neighbours from the thread's own columns
-// or a warp shuffle.  `ns` <= H sweeps run per launch; the region carries a
-// halo of H = 8 cells on each side, so the CTA owns the inner 48 x 112 cells
-// and writes only those.  Cells outside the grid or inactive have w = bw = 0
-// and stay 0.  Launch k first decides whether the solve already stopped
+// or a warp shuffle.  `ns` <= H sweeps run per launch; inside the grid the
+// region carries a halo of H = 8 cells, so the CTA owns the inner 48 x 112
+// cells, and at the grid's edges it owns up to the edge (span_count and
+// span_own, fg_internal.cuh); it writes only what it owns.  Cells outside
+// the grid or inactive have w = bw = 0 and stay 0.  The TMA-fed kernels
+// below keep regions at t S - H with the inner 48 x 112 owned.  Launch k
+// first decides whether the solve already stopped
 // (thread 0 of every CTA reads the same control words, so all CTAs agree);
 // a running launch records the max |r| of its last sweep over the active
 // cells it owns, r = fma(-s, phi, b + nb), in slots[k].
@@ -1028,16 +1031,7 @@ constexpr int OJ = RJ - 2 * TMAX;  // 112 owned columns
 constexpr int OI = RI - 2 * TMAX;  // 48 owned rows
 constexpr int TB_THREADS = 32 * NWARP;
 static_assert(RI == kJacRegionRows && RJ == kJacRegionCols && TMAX == kJacHalo,
-              "batch Jacobi tiles");
-// Owned window of a tile in region coordinates, one byte each: rows
-// [own & 255, own >> 8 & 255), columns [own >> 16 & 255, own >> 24).  A
-// region whose edge lies at or outside the grid's edge on a side needs no
-// halo there: the cells past the grid are zero and stay zero, and the
-// grid's outermost ring has w = bw = 0, so whatever a region-edge thread
-// reads beside it (a warp shuffle at lane 0 or 31 returns the thread's own
-// value) is multiplied by 0.
-constexpr uint32_t kOwnInner = (uint32_t)TMAX | (uint32_t)(RI - TMAX) << 8 |
-                               (uint32_t)TMAX << 16 | (uint32_t)(RJ - TMAX) << 24;
+              "Jacobi region geometry");
 
 // RINIT (first launch of the outer correction): instead of loading bw, the
 // kernel loads the main potential phi (from the buffer the main solve's
@@ -1274,9 +1268,10 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
                 const float* __restrict__ mphi0, const float* __restrict__ mphi1,
                 const PCtl* __restrict__ mctl, float* __restrict__ rhs_e,
                 float* __restrict__ bwe) {
-  jacobi_tile<OMEGA1, FULL, CHECK, RINIT>((int)blockIdx.y * OI - TMAX, (int)blockIdx.x * OJ - TMAX,
-                                          kOwnInner, blockIdx.x == 0 && blockIdx.y == 0, src,
-                                          dst, W, BW,
+  jacobi_tile<OMEGA1, FULL, CHECK, RINIT>((int)blockIdx.y * OI, (int)blockIdx.x * OJ,
+                                          span_own(blockIdx.y, g.NX, RI) |
+                                              span_own(blockIdx.x, g.NY, RJ) << 16,
+                                          blockIdx.x == 0 && blockIdx.y == 0, src, dst, W, BW,
                                           rhs, flags, om1, ctl, k, t0, ns, tol, out_sel,
                                           zero_init, g, mphi0, mphi1, mctl, rhs_e, bwe);
 }
@@ -2327,7 +2322,7 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
   float om1 = 1.0f - om;
   int used = FG_JACOBI_KERNEL_SWEEP;
   bool o1 = om1 == 0.0f;
-  dim3 gr((g.NY + OJ - 1) / OJ, (g.NX + OI - 1) / OI);
+  dim3 gr(span_count(g.NY, RJ), span_count(g.NX, RI));
   int nlaunch = (int)(((long long)iters + T - 1) / T);
   int k0 = 0, kernels = 0;
   // Fixed sweep counts in full launches: the leading full phases as one
@@ -2871,7 +2866,7 @@ inline dim3 level_grid(const Grid& g) { return dim3((g.NY + BX - 1) / BX, (g.NX 
 // ns (<= TMAX) damped Jacobi sweeps src -> dst on one level.
 void mg_sweeps(cudaStream_t st, const MgLevelDev& v, const float* src, float* dst, float om1,
                PCtl* ctl, int t0, int ns, int sel, int zero) {
-  dim3 gr((v.g.NY + OJ - 1) / OJ, (v.g.NX + OI - 1) / OI);
+  dim3 gr(span_count(v.g.NY, RJ), span_count(v.g.NX, RI));
   if (ns == TMAX)
     k_jacobi_rb<false, true, false, false><<<gr, TB_THREADS, 0, st>>>(
         src, dst, v.w, v.bw, nullptr, v.flags, om1, ctl, 0, t0, ns, 0.0f, sel, zero, v.g, nullptr,
