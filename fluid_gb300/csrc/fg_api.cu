@@ -1889,6 +1889,7 @@ void batch_free(fg::BatchGeom* b) {
   if (!b) return;
   cudaFree(b->scenes_dev);
   cudaFree(b->cell_tiles);
+  cudaFree(b->cell_blocks);
   cudaFree(b->cell_range);
   cudaFree(b->border_tiles);
   cudaFree(b->jac_tiles);
@@ -1924,17 +1925,23 @@ int upload_table(fg_fluid* f, T** dev, const std::vector<T>& host) {
 int batch_cell_tiles(fg_fluid* f, int bx, int by) {
   fg::BatchGeom* b = f->batch;
   std::vector<BTile> tiles;
+  std::vector<BCell> blocks;
   std::vector<int> range(2 * b->n);
   for (int s : batch_order(b)) {
     const Grid& g = b->scenes[s].g;
     range[2 * s] = (int)tiles.size();
     for (int ty = 0; ty < (g.NX + by - 1) / by; ++ty)
-      for (int tx = 0; tx < (g.NY + bx - 1) / bx; ++tx) tiles.push_back(BTile{s, tx, ty, 0});
+      for (int tx = 0; tx < (g.NY + bx - 1) / bx; ++tx) {
+        tiles.push_back(BTile{s, tx, ty, 0});
+        blocks.push_back(BCell{g, b->scenes[s].off, tx, ty, {0, 0}});
+      }
     range[2 * s + 1] = (int)tiles.size();
   }
   CK(f, cudaStreamSynchronize(f->stream), "batch sync");
   int rc = upload_table(f, &b->cell_tiles, tiles);
-  if (rc || (rc = upload_table(f, &b->cell_range, range))) return rc;
+  if (rc || (rc = upload_table(f, &b->cell_blocks, blocks)) ||
+      (rc = upload_table(f, &b->cell_range, range)))
+    return rc;
   b->bx = bx;
   b->by = by;
   b->n_cell_tiles = (int)tiles.size();

@@ -27,16 +27,25 @@ __device__ __forceinline__ const float2* bshift(const float2* p, long long o) {
   return p ? p + o : p;
 }
 
-// Body(i, j, args..., grid) over the cells of every scene.
+// Body(i, j, args..., grid) over the cells of every scene.  The block's
+// table entry (constant) is read before waiting on the previous kernel.
 template <auto Body, class... A>
-__global__ void kb_cells(const BTile* __restrict__ tiles, const BScene* __restrict__ sc, A... a) {
-  const BTile t = tiles[blockIdx.x];
-  const Grid g = sc[t.s].g;
-  const long long off = sc[t.s].off;
-  const int j = t.x * blockDim.x + threadIdx.x;
-  const int i = t.y * blockDim.y + threadIdx.y;
-  if (i >= g.NX || j >= g.NY) return;
-  Body(i, j, bshift(a, off)..., g);
+__global__ void kb_cells(const BCell* __restrict__ blocks, A... a) {
+  const BCell c = blocks[blockIdx.x];
+  pdl_enter();
+  const int j = c.x * blockDim.x + threadIdx.x;
+  const int i = c.y * blockDim.y + threadIdx.y;
+  if (i >= c.g.NX || j >= c.g.NY) return;
+  Body(i, j, bshift(a, c.off)..., c.g);
+}
+
+// kb_cells<Body> over the batch's cell blocks, with programmatic stream
+// serialization.
+template <auto Body, class... A>
+inline cudaError_t launch_cells(const fg_fluid* f, A... a) {
+  const BatchGeom* b = f->batch;
+  return launch_pdl(kb_cells<Body, A...>, dim3(b->n_cell_tiles), dim3(b->bx, b->by), 0,
+                    f->stream, b->cell_blocks, a...);
 }
 
 // Body(t, args..., grid) over the border threads (t < max(NX, NY)) of
@@ -53,9 +62,7 @@ __global__ void kb_border(const BTile* __restrict__ tiles, const BScene* __restr
 #define FG_CELLS(f, K, BODY, ...)                                                            \
   do {                                                                                       \
     if ((f)->batch) {                                                                        \
-      const BatchGeom* b_ = (f)->batch;                                                      \
-      kb_cells<BODY><<<b_->n_cell_tiles, dim3(b_->bx, b_->by), 0, (f)->stream>>>(            \
-          b_->cell_tiles, b_->scenes_dev, __VA_ARGS__);                                      \
+      launch_cells<BODY>((f), __VA_ARGS__);                                                  \
     } else {                                                                                 \
       K<<<dim3(((f)->NY + 31) / 32, ((f)->NX + 7) / 8), dim3(32, 8), 0, (f)->stream>>>(      \
           __VA_ARGS__, (f)->g);                                                              \
@@ -64,9 +71,7 @@ __global__ void kb_border(const BTile* __restrict__ tiles, const BScene* __restr
 
 // The batched wrapper of BODY only (for stages whose single-scene kernel
 // takes other arguments).
-#define FG_CELLS_BATCH(f, BODY, ...)                                                          \
-  kb_cells<BODY><<<(f)->batch->n_cell_tiles, dim3((f)->batch->bx, (f)->batch->by), 0,          \
-                   (f)->stream>>>((f)->batch->cell_tiles, (f)->batch->scenes_dev, __VA_ARGS__)
+#define FG_CELLS_BATCH(f, BODY, ...) launch_cells<BODY>((f), __VA_ARGS__)
 
 #define FG_BORDER(f, K, BODY, ...)                                                           \
   do {                                                                                       \

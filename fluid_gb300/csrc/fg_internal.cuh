@@ -229,6 +229,15 @@ struct BScene {
 struct BTile {
   int s, x, y, pad;  // scene, tile column, tile row (per-cell and border tables)
 };
+// A per-cell block of a batch with its scene's grid and offset in the same
+// entry, so the block's first read is its last table read.
+struct BCell {
+  Grid g;
+  long long off;
+  int x, y;  // tile column, tile row
+  int pad[2];
+};
+static_assert(sizeof(BCell) == 64, "one 64-byte entry per block");
 // A per-launch Jacobi block (k_pressure.cu) sweeps a region of 64 rows x
 // 128 columns in registers and writes the cells of it that are exact after
 // its sweeps.  Inside the grid a region edge costs a halo of 8 cells; at the
@@ -259,6 +268,7 @@ struct BatchGeom {
   BScene* scenes_dev = nullptr;
   int bx = 32, by = 8;  // thread-block shape of the per-cell kernels (autotuned)
   BTile* cell_tiles = nullptr;
+  BCell* cell_blocks = nullptr;  // the same tiles with their scenes (per-cell kernels)
   int n_cell_tiles = 0;
   int* cell_range = nullptr;  // device: [first, end) cell tiles of each scene (2 n entries)
   BTile* border_tiles = nullptr;
