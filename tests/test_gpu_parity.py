@@ -260,6 +260,23 @@ def test_jacobi_fixed_sweeps_bitwise(gpu, w, h):
     assert_bitwise(g, o, where="%dx%d" % (w, h))
 
 
+@pytest.mark.parametrize("w,h", [(1100, 1500), (400, 2700)])
+def test_jacobi_4_sweep_launches_bitwise(gpu, w, h):
+    """tb_depth 4 on grids large enough for the dataflow kernel: ten 4-sweep
+    launches of the per-launch kernel (the dataflow kernel runs 8-sweep
+    phases only), bit for bit against the oracle."""
+    g, o = both(gpu, w, h, scheme=1, num_iters=40, tb_depth=4, early_exit=False, UseBFECC=True)
+    for f in (g, o):
+        scenes.jet_scene(f)
+        f.SetCircularObstacle(w // 3, h // 2, max(3, min(w, h) // 8))
+    for _ in range(3):
+        for f in (g, o):
+            scenes.jet_inject(f, speed=3.0)
+            f.Simulate(0.1)
+    assert_bitwise(g, o, where="%dx%d" % (w, h))
+    assert g.stats()["jacobi_kernel"] == gpu.JACOBI_KERNEL_SWEEP
+
+
 def test_jacobi_dataflow_then_partial_launch_bitwise(gpu):
     """44 sweeps at 1100x1500: five dataflow phases, then one 4-sweep launch
     of the per-launch kernel continuing from the dataflow result."""
