@@ -1282,7 +1282,9 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
 // have not started return at once.  Each block's table entry gives its
 // region's origin and owned window (fg_internal.cuh): regions at a scene's
 // edges start or end there and own up to it, so a scene is cut into fewer
-// regions than whole 48 x 112 tiles with halos on every side.
+// regions than whole 48 x 112 tiles with halos on every side.  The tables
+// are constant and read before jacobi_tile waits on the previous launch
+// (programmatic dependent launch).
 template <bool OMEGA1>
 __global__ void __launch_bounds__(TB_THREADS, 2)
     kb_jacobi(const BTile* __restrict__ tiles, const BScene* __restrict__ sc,
@@ -2353,10 +2355,9 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
       if (used == FG_JACOBI_KERNEL_SWEEP) used = FG_JACOBI_KERNEL_TMA;
       continue;
     }
-#define FG_JAC(O, F, C, R)                                                                      \
-  k_jacobi_rb<O, F, C, R><<<gr, TB_THREADS, 0, st>>>(src, dst, W, bwk, bk, flags, om1, ctl, k, t0, \
-                                                     ns, tol, sel, zi, g, mphi0, mphi1, mctl, re, \
-                                                     bwe)
+#define FG_JAC(O, F, C, R)                                                                     \
+  launch_pdl(k_jacobi_rb<O, F, C, R>, gr, dim3(TB_THREADS), 0, st, src, dst, W, bwk, bk, flags, \
+             om1, ctl, k, t0, ns, tol, sel, zi, g, mphi0, mphi1, mctl, re, bwe)
     if (rinit) {
       if (o1) { if (full) FG_JAC(true, true, false, true); else FG_JAC(true, false, false, true); }
       else { if (full) FG_JAC(false, true, false, true); else FG_JAC(false, false, false, true); }
@@ -2388,12 +2389,9 @@ static cudaError_t jacobi_solve_batch(fg_fluid* f, PCtl* ctl, const float* bw, f
     const float* src = (k & 1) ? x1 : x0;
     float* dst = (k & 1) ? x0 : x1;
     int sel = (k & 1) ? 0 : 1;
-    if (om1 == 0.0f)
-      kb_jacobi<true><<<bt->n_jac_tiles, TB_THREADS, 0, f->stream>>>(
-          bt->jac_tiles, bt->scenes_dev, src, dst, f->wgt, bw, f->flags, om1, ctl, k, L, T, sel);
-    else
-      kb_jacobi<false><<<bt->n_jac_tiles, TB_THREADS, 0, f->stream>>>(
-          bt->jac_tiles, bt->scenes_dev, src, dst, f->wgt, bw, f->flags, om1, ctl, k, L, T, sel);
+    launch_pdl(om1 == 0.0f ? kb_jacobi<true> : kb_jacobi<false>, dim3(bt->n_jac_tiles),
+               dim3(TB_THREADS), 0, f->stream, bt->jac_tiles, bt->scenes_dev, src, dst, f->wgt, bw,
+               f->flags, om1, ctl, k, L, T, sel);
   }
   count(f, L);
   return cudaGetLastError();
