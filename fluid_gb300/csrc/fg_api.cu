@@ -2081,6 +2081,18 @@ int fg_batch_create(fg_fluid* const* scenes, int n, fg_fluid** out) {
   for (int s : batch_order(b)) {
     const Grid& g = b->scenes[s].g;
     for (int t = 0; t < (std::max(g.NX, g.NY) + 127) / 128; ++t) bt.push_back(BTile{s, t, 0, 0});
+  }
+  // Jacobi regions: scenes with more sweeps first (then larger first), so
+  // the scenes that have started by any launch are a prefix of the table.
+  std::vector<int> jord = batch_order(b);
+  b->jac_iters.clear();
+  b->jac_regions.clear();
+  std::stable_sort(jord.begin(), jord.end(),
+                   [&](int a, int c) { return b->scenes[a].iters > b->scenes[c].iters; });
+  for (int s : jord) {
+    const Grid& g = b->scenes[s].g;
+    b->jac_iters.push_back(b->scenes[s].iters);
+    b->jac_regions.push_back(span_count(g.NX, kJacRegionRows) * span_count(g.NY, kJacRegionCols));
     for (int ti = 0; ti < span_count(g.NX, kJacRegionRows); ++ti)
       for (int tj = 0; tj < span_count(g.NY, kJacRegionCols); ++tj)
         jt.push_back(BTile{s, tj * (kJacRegionCols - 2 * kJacHalo),

@@ -273,8 +273,11 @@ struct BatchGeom {
   int* cell_range = nullptr;  // device: [first, end) cell tiles of each scene (2 n entries)
   BTile* border_tiles = nullptr;
   int n_border_tiles = 0;
-  BTile* jac_tiles = nullptr;
+  BTile* jac_tiles = nullptr;  // scenes with more sweeps first (see jac_iters)
   int n_jac_tiles = 0;
+  // Per scene in the Jacobi table's order: its sweeps and its regions, so a
+  // launch runs only the table's prefix of scenes that have started.
+  std::vector<int> jac_iters, jac_regions;
   int max_iters = 0;
   int* src_scene = nullptr;  // device: scene of each source group
   double* losses = nullptr;  // device: per-scene loss of the last seed, then n floats 1 / L

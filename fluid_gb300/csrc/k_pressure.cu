@@ -1278,13 +1278,14 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
 
 // A batch's Jacobi launch k of L: scene s runs its nl_s = ceil(iters_s / T)
 // launches as the last nl_s of the L, the first of them with the remainder
-// sweeps, so every scene ends in the same buffer.  Blocks of scenes that
-// have not started return at once.  Each block's table entry gives its
-// region's origin and owned window (fg_internal.cuh): regions at a scene's
-// edges start or end there and own up to it, so a scene is cut into fewer
-// regions than whole 48 x 112 tiles with halos on every side.  The tables
-// are constant and read before jacobi_tile waits on the previous launch
-// (programmatic dependent launch).
+// sweeps, so every scene ends in the same buffer.  The table lists the
+// scenes with more sweeps first and launch k runs only the prefix of
+// scenes that have started (a block of another would return at once).
+// Each block's table entry gives its region's origin and owned window
+// (fg_internal.cuh): regions at a scene's edges start or end there and own
+// up to it, so a scene is cut into fewer regions than whole 48 x 112 tiles
+// with halos on every side.  The tables are constant and read before
+// jacobi_tile waits on the previous launch (programmatic dependent launch).
 template <bool OMEGA1>
 __global__ void __launch_bounds__(TB_THREADS, 2)
     kb_jacobi(const BTile* __restrict__ tiles, const BScene* __restrict__ sc,
@@ -2385,11 +2386,16 @@ static cudaError_t jacobi_solve_batch(fg_fluid* f, PCtl* ctl, const float* bw, f
   if (e != cudaSuccess) return e;
   float om = f->prm.jacobi_omega * f->prm.pressure_damping;
   float om1 = 1.0f - om;
+  size_t sc = 0;  // scenes (in the table's order) started by launch k
+  int n_act = 0;  // their regions: the prefix of the table launch k runs
   for (int k = 0; k < L; ++k) {
+    while (sc < bt->jac_iters.size() && L - (bt->jac_iters[sc] + T - 1) / T <= k)
+      n_act += bt->jac_regions[sc++];
     const float* src = (k & 1) ? x1 : x0;
     float* dst = (k & 1) ? x0 : x1;
     int sel = (k & 1) ? 0 : 1;
-    launch_pdl(om1 == 0.0f ? kb_jacobi<true> : kb_jacobi<false>, dim3(bt->n_jac_tiles),
+    if (n_act == 0) continue;
+    launch_pdl(om1 == 0.0f ? kb_jacobi<true> : kb_jacobi<false>, dim3(n_act),
                dim3(TB_THREADS), 0, f->stream, bt->jac_tiles, bt->scenes_dev, src, dst, f->wgt, bw,
                f->flags, om1, ctl, k, L, T, sel);
   }
