@@ -1374,9 +1374,52 @@ __device__ __forceinline__ void mbar_drain(uint64_t* bar, unsigned parity) {
     if (mbar_wait_bounded(bar, parity)) return;
 }
 
-// The TMAX sweeps of one tile in registers, with the arithmetic of
-// jacobi_tile.  hook(sw) runs before sweep sw (sw a constant after
-// unrolling), so callers can spread latency-bound side work over the sweeps.
+// One sweep of a tile in registers, with the arithmetic of jacobi_tile;
+// buf alternates between consecutive sweeps (the row exchange is double
+// buffered, one barrier per sweep).
+template <bool OMEGA1>
+__device__ __forceinline__ void tile_sweep(float (&x)[RT][JT], const float (&w)[RT][JT],
+                                           const float (&bw)[RT][JT], float om1,
+                                           float4 (&xch)[2][2][NWARP][32], int warp, int lane,
+                                           int buf) {
+  xch[buf][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
+  xch[buf][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
+  __syncthreads();
+  float4 u4 = warp > 0 ? xch[buf][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 d4 = warp < NWARP - 1 ? xch[buf][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
+#pragma unroll
+  for (int r = 0; r < RT; ++r) {
+    float lf = __shfl_up_sync(0xffffffffu, x[r][JT - 1], 1);
+    float rt = __shfl_down_sync(0xffffffffu, x[r][0], 1);
+    float nxt[JT];
+    if (r < RT - 1) {
+#pragma unroll
+      for (int q = 0; q < JT; ++q) nxt[q] = x[r + 1][q];
+    } else {
+      nxt[0] = d4.x; nxt[1] = d4.y; nxt[2] = d4.z; nxt[3] = d4.w;
+    }
+    float nw[JT];
+#pragma unroll
+    for (int q = 0; q < JT; ++q) {
+      float left = q == 0 ? lf : x[r][q - 1];
+      float right = q == JT - 1 ? rt : x[r][q + 1];
+      float nb = prev[q] + nxt[q] + left + right;  // (i-1) + (i+1) + (j-1) + (j+1)
+      float y = __fmaf_rn(w[r][q], nb, bw[r][q]);
+      if (!OMEGA1) y = __fmaf_rn(om1, x[r][q], y);
+      nw[q] = y;
+    }
+#pragma unroll
+    for (int q = 0; q < JT; ++q) {
+      prev[q] = x[r][q];
+      x[r][q] = nw[q];
+    }
+  }
+}
+
+// The TMAX sweeps of one tile.  hook(sw) runs before sweep sw (sw a
+// constant after unrolling), so callers can spread latency-bound side work
+// over the sweeps.
 struct NoHook {
   __device__ __forceinline__ void operator()(int) const {}
 };
@@ -1388,40 +1431,124 @@ __device__ __forceinline__ void tile_sweeps(float (&x)[RT][JT], const float (&w)
 #pragma unroll
   for (int sw = 0; sw < TMAX; ++sw) {
     hook(sw);
-    const int buf = sw & 1;
-    xch[buf][0][warp][lane] = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
-    xch[buf][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
-    __syncthreads();
-    float4 u4 = warp > 0 ? xch[buf][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 d4 = warp < NWARP - 1 ? xch[buf][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
+    tile_sweep<OMEGA1>(x, w, bw, om1, xch, warp, lane, sw & 1);
+  }
+}
+
+// 16 bytes from global to shared memory without passing through registers;
+// the bytes past src_bytes (0 or 16) are zero-filled.
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem),
+               "r"(src_bytes)
+               : "memory");
+}
+
+// A batch's Jacobi launch k (as kb_jacobi, same regions, same per-cell
+// arithmetic, same results) as a persistent kernel: block b runs the
+// started scenes' regions b, b + G, ... in turn, and while it sweeps one,
+// its threads' asynchronous copies bring the next region's boxes (phi, w,
+// w*b; zero outside the scene's rows and pitch) into shared memory, so the
+// loads no longer sit in front of the sweeps.  The tables are constant;
+// the copies read the previous launch's result, after the programmatic
+// wait.
+template <bool OMEGA1>
+__global__ void __launch_bounds__(TB_THREADS, 2)
+    kb_jacobi_pf(const BTile* __restrict__ tiles, const BScene* __restrict__ sc, int n,
+                 const float* __restrict__ src, float* __restrict__ dst,
+                 const float* __restrict__ W, const float* __restrict__ BW, float om1, PCtl* ctl,
+                 int k, int L, int T, int out_sel) {
+  extern __shared__ __align__(128) float4 pbuf4[];  // [3][RI][RJ] floats: phi, w, w*b
+  float* pbuf = reinterpret_cast<float*>(pbuf4);
+  __shared__ float4 xch[2][2][NWARP][32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // Thread tid copies float4 q = tid + 256 m (m < 8) of each box: region
+  // row q / 32, columns 4 (q % 32) .. + 3.
+  auto issue = [&](int i) {
+    const BTile t = tiles[i];
+    const BScene& s = sc[t.s];
+    const bool zi = k == L - (s.iters + T - 1) / T;  // the scene's first launch starts from 0
+    const float* xs = src + s.off;
+    const float* ws = W + s.off;
+    const float* bs = BW + s.off;
+#pragma unroll
+    for (int m = 0; m < TILE_FLOATS / 4 / TB_THREADS; ++m) {
+      const int q = tid + TB_THREADS * m;
+      const int row = q / (RJ / JT), col = JT * (q % (RJ / JT));
+      const int gi = t.y + row, gj = t.x + col;
+      const bool ok = gi >= 0 && gi < s.g.NX && gj >= 0 && gj < s.g.P;
+      const size_t c = ok ? (size_t)gi * s.g.P + gj : 0;
+      float* d = pbuf + row * RJ + col;
+      cp_async16(d, xs + c, ok && !zi ? 16 : 0);
+      cp_async16(d + TILE_FLOATS, ws + c, ok ? 16 : 0);
+      cp_async16(d + 2 * TILE_FLOATS, bs + c, ok ? 16 : 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int i = blockIdx.x;
+  pdl_enter();
+  if (i < n) issue(i);
+  while (i < n) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();  // every thread's copies of region i landed
+    const BTile t = tiles[i];
+    const BScene& s = sc[t.s];
+    const Grid g = s.g;
+    const int nl = (s.iters + T - 1) / T;
+    const int ns = k == L - nl ? s.iters - (nl - 1) * T : T;
+    const int gi0 = t.y + warp * RT, gj = t.x + lane * JT;
+    float x[RT][JT], w[RT][JT], bw[RT][JT];
 #pragma unroll
     for (int r = 0; r < RT; ++r) {
-      float lf = __shfl_up_sync(0xffffffffu, x[r][JT - 1], 1);
-      float rt = __shfl_down_sync(0xffffffffu, x[r][0], 1);
-      float nxt[JT];
-      if (r < RT - 1) {
+      const int o = (warp * RT + r) * RJ + lane * JT;
+      const float4 a = *reinterpret_cast<const float4*>(pbuf + o);
+      const float4 ww = *reinterpret_cast<const float4*>(pbuf + TILE_FLOATS + o);
+      const float4 bb = *reinterpret_cast<const float4*>(pbuf + 2 * TILE_FLOATS + o);
+      x[r][0] = a.x; x[r][1] = a.y; x[r][2] = a.z; x[r][3] = a.w;
+      w[r][0] = ww.x; w[r][1] = ww.y; w[r][2] = ww.z; w[r][3] = ww.w;
+      bw[r][0] = bb.x; bw[r][1] = bb.y; bw[r][2] = bb.z; bw[r][3] = bb.w;
 #pragma unroll
-        for (int q = 0; q < JT; ++q) nxt[q] = x[r + 1][q];
-      } else {
-        nxt[0] = d4.x; nxt[1] = d4.y; nxt[2] = d4.z; nxt[3] = d4.w;
-      }
-      float nw[JT];
+      for (int q = 0; q < JT; ++q)
+        if (gj + q >= g.NY) {  // the pitch padding: outside the grid
+          x[r][q] = 0.0f;
+          w[r][q] = 0.0f;
+          bw[r][q] = 0.0f;
+        }
+    }
+    __syncthreads();  // the boxes are in registers: the buffer takes the next region
+    const int nx = i + gridDim.x;
+    if (nx < n) issue(nx);
+    if (i == 0 && tid == 0) ctl->sweeps = ns;
+    // (The host launches the started scenes' regions only; a region of a
+    // scene that has not started would be left alone.)
+    const bool run = k >= L - nl;
+    if (run && ns == TMAX) {
+      tile_sweeps<OMEGA1>(x, w, bw, om1, xch, warp, lane);
+    } else if (run) {
+      for (int sw = 0; sw < ns; ++sw) tile_sweep<OMEGA1>(x, w, bw, om1, xch, warp, lane, sw & 1);
+    }
+    const uint32_t own = (uint32_t)t.pad;
+    const int oi0 = own & 255, oi1 = own >> 8 & 255, oj0 = own >> 16 & 255, oj1 = own >> 24;
+    if (run && lane * JT >= oj0 && lane * JT < oj1) {
+      float* xd = dst + s.off;
 #pragma unroll
-      for (int q = 0; q < JT; ++q) {
-        float left = q == 0 ? lf : x[r][q - 1];
-        float right = q == JT - 1 ? rt : x[r][q + 1];
-        float nb = prev[q] + nxt[q] + left + right;  // (i-1) + (i+1) + (j-1) + (j+1)
-        float y = __fmaf_rn(w[r][q], nb, bw[r][q]);
-        if (!OMEGA1) y = __fmaf_rn(om1, x[r][q], y);
-        nw[q] = y;
-      }
+      for (int r = 0; r < RT; ++r) {
+        const int gi = gi0 + r;
+        if (warp * RT + r < oi0 || warp * RT + r >= oi1 || gi >= g.NX || gj >= g.NY) continue;
+        const size_t c = (size_t)gi * g.P + gj;
+        if (gj + JT <= g.NY) {
+          *reinterpret_cast<float4*>(xd + c) = make_float4(x[r][0], x[r][1], x[r][2], x[r][3]);
+        } else {
 #pragma unroll
-      for (int q = 0; q < JT; ++q) {
-        prev[q] = x[r][q];
-        x[r][q] = nw[q];
+          for (int q = 0; q < JT; ++q)
+            if (gj + q < g.NY) xd[c + q] = x[r][q];
+        }
       }
     }
+    i = nx;
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    ctl->last_launch = k;
+    ctl->sel = out_sel;
   }
 }
 
@@ -2090,6 +2217,7 @@ struct TmaDevice {
   std::atomic<bool> ready{false};
   int sms = 0;
   int flow_per_sm = 0;
+  int batch_pf_per_sm = 0;  // blocks of kb_jacobi_pf per SM (0: the plain batch kernel runs)
 };
 static TmaDevice g_tma_dev[kMaxContexts];
 static unsigned long long g_tma_key[kMaxContexts];
@@ -2206,6 +2334,16 @@ void init_jacobi_tma() {
     int coop = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
       d->flow_per_sm = 0;
+    int p1 = 0, p2 = 0;
+    if (cudaFuncSetAttribute(kb_jacobi_pf<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) == cudaSuccess &&
+        cudaFuncSetAttribute(kb_jacobi_pf<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p1, kb_jacobi_pf<true>, TB_THREADS,
+                                                      smem) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p2, kb_jacobi_pf<false>, TB_THREADS,
+                                                      smem) == cudaSuccess)
+      d->batch_pf_per_sm = p1 < p2 ? p1 : p2;
     cudaGetLastError();
     d->ready.store(true);
   });
@@ -2386,6 +2524,8 @@ static cudaError_t jacobi_solve_batch(fg_fluid* f, PCtl* ctl, const float* bw, f
   if (e != cudaSuccess) return e;
   float om = f->prm.jacobi_omega * f->prm.pressure_damping;
   float om1 = 1.0f - om;
+  const TmaDevice* dv = tma_ready(f->stream);
+  const int pf_blocks = dv && dv->sms > 0 ? dv->batch_pf_per_sm * dv->sms : 0;
   size_t sc = 0;  // scenes (in the table's order) started by launch k
   int n_act = 0;  // their regions: the prefix of the table launch k runs
   for (int k = 0; k < L; ++k) {
@@ -2395,9 +2535,15 @@ static cudaError_t jacobi_solve_batch(fg_fluid* f, PCtl* ctl, const float* bw, f
     float* dst = (k & 1) ? x0 : x1;
     int sel = (k & 1) ? 0 : 1;
     if (n_act == 0) continue;
-    launch_pdl(om1 == 0.0f ? kb_jacobi<true> : kb_jacobi<false>, dim3(n_act),
-               dim3(TB_THREADS), 0, f->stream, bt->jac_tiles, bt->scenes_dev, src, dst, f->wgt, bw,
-               f->flags, om1, ctl, k, L, T, sel);
+    if (pf_blocks > 0)
+      launch_pdl(om1 == 0.0f ? kb_jacobi_pf<true> : kb_jacobi_pf<false>,
+                 dim3(n_act < pf_blocks ? n_act : pf_blocks), dim3(TB_THREADS),
+                 3 * (size_t)TILE_FLOATS * sizeof(float), f->stream, bt->jac_tiles,
+                 bt->scenes_dev, n_act, src, dst, f->wgt, bw, om1, ctl, k, L, T, sel);
+    else
+      launch_pdl(om1 == 0.0f ? kb_jacobi<true> : kb_jacobi<false>, dim3(n_act),
+                 dim3(TB_THREADS), 0, f->stream, bt->jac_tiles, bt->scenes_dev, src, dst, f->wgt,
+                 bw, f->flags, om1, ctl, k, L, T, sel);
   }
   count(f, L);
   return cudaGetLastError();
