@@ -65,6 +65,23 @@ def test_batch_step_bitwise_equals_single_scenes(gpu, conf):
         assert_same(a, b, "scene %d" % k)
 
 
+@pytest.mark.parametrize("omega,tb", [(0.8, 8), (1.0, 4), (0.8, 6)])
+def test_batch_damped_and_short_blocks_bitwise(gpu, omega, tb):
+    """Damped Jacobi (omega < 1: the relaxation term in every sweep) and
+    blocking depths below 8 (every launch's sweeps counted at run time),
+    each scene against its own handle, bit for bit."""
+    ref = make_scenes(gpu, seed=8, jacobi_omega=omega, tb_depth=tb)
+    mem = make_scenes(gpu, seed=8, jacobi_omega=omega, tb_depth=tb)
+    batch = gpu.Batch(mem)
+    for _ in range(6):
+        for f in ref:
+            f.Simulate(DT)
+        batch.step(DT)
+    batch.scatter()
+    for k, (a, b) in enumerate(zip(ref, mem)):
+        assert_same(a, b, "scene %d (omega %g, tb %d)" % (k, omega, tb))
+
+
 def test_autotune_keeps_results(gpu):
     ref = make_scenes(gpu, seed=4)
     mem = make_scenes(gpu, seed=4)
