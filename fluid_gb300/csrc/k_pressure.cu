@@ -1462,27 +1462,31 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
   __shared__ float4 xch[2][2][NWARP][32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // Thread tid copies float4 q = tid + 256 m (m < 8) of each box: region
-  // row q / 32, columns 4 (q % 32) .. + 3.
-  auto issue = [&](int i) {
-    const BTile t = tiles[i];
-    const BScene& s = sc[t.s];
-    const bool zi = k == L - (s.iters + T - 1) / T;  // the scene's first launch starts from 0
-    const float* xs = src + s.off;
-    const float* ws = W + s.off;
-    const float* bs = BW + s.off;
+  // row q / 32, columns 4 (q % 32) .. + 3, for a region starting at (ri0,
+  // rj0) of a scene of NX rows of pitch P at element offset off.
+  auto issue_at = [&](int ri0, int rj0, int NX, int P, long long off, bool zi) {
+    const float* xs = src + off;
+    const float* ws = W + off;
+    const float* bs = BW + off;
 #pragma unroll
     for (int m = 0; m < TILE_FLOATS / 4 / TB_THREADS; ++m) {
       const int q = tid + TB_THREADS * m;
       const int row = q / (RJ / JT), col = JT * (q % (RJ / JT));
-      const int gi = t.y + row, gj = t.x + col;
-      const bool ok = gi >= 0 && gi < s.g.NX && gj >= 0 && gj < s.g.P;
-      const size_t c = ok ? (size_t)gi * s.g.P + gj : 0;
+      const int gi = ri0 + row, gj = rj0 + col;
+      const bool ok = gi >= 0 && gi < NX && gj >= 0 && gj < P;
+      const size_t c = ok ? (size_t)gi * P + gj : 0;
       float* d = pbuf + row * RJ + col;
       cp_async16(d, xs + c, ok && !zi ? 16 : 0);
       cp_async16(d + TILE_FLOATS, ws + c, ok ? 16 : 0);
       cp_async16(d + 2 * TILE_FLOATS, bs + c, ok ? 16 : 0);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  // (A scene's first launch starts from 0: its phi box is not copied.)
+  auto issue = [&](int i) {
+    const BTile t = tiles[i];
+    const BScene& s = sc[t.s];
+    issue_at(t.y, t.x, s.g.NX, s.g.P, s.off, k == L - (s.iters + T - 1) / T);
   };
   int i = blockIdx.x;
   pdl_enter();
@@ -1514,17 +1518,40 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
           bw[r][q] = 0.0f;
         }
     }
-    __syncthreads();  // the boxes are in registers: the buffer takes the next region
     const int nx = i + gridDim.x;
-    if (nx < n) issue(nx);
     if (i == 0 && tid == 0) ctl->sweeps = ns;
     // (The host launches the started scenes' regions only; a region of a
     // scene that has not started would be left alone.)
     const bool run = k >= L - nl;
     if (run && ns == TMAX) {
-      tile_sweeps<OMEGA1>(x, w, bw, om1, xch, warp, lane);
-    } else if (run) {
-      for (int sw = 0; sw < ns; ++sw) tile_sweep<OMEGA1>(x, w, bw, om1, xch, warp, lane, sw & 1);
+      // The next region's table entry is read before sweep 0, its scene's
+      // before sweep 1, and its copies start before sweep 2 (sweep 0's
+      // barrier has ordered every thread's register fill before them), so
+      // neither the dependent table reads nor the copies sit in front of a
+      // sweep.
+      BTile tn{};
+      int nNX = 0, nP = 0, nit = 0;
+      long long noff = 0;
+      auto hook = [&](int sw) {
+        if (nx >= n) return;
+        if (sw == 0) {
+          tn = tiles[nx];
+        } else if (sw == 1) {
+          const BScene& sn = sc[tn.s];
+          nNX = sn.g.NX;
+          nP = sn.g.P;
+          noff = sn.off;
+          nit = sn.iters;
+        } else if (sw == 2) {
+          issue_at(tn.y, tn.x, nNX, nP, noff, k == L - (nit + T - 1) / T);
+        }
+      };
+      tile_sweeps<OMEGA1>(x, w, bw, om1, xch, warp, lane, hook);
+    } else {
+      __syncthreads();  // the boxes are in registers: the buffer takes the next region
+      if (nx < n) issue(nx);
+      if (run)
+        for (int sw = 0; sw < ns; ++sw) tile_sweep<OMEGA1>(x, w, bw, om1, xch, warp, lane, sw & 1);
     }
     const uint32_t own = (uint32_t)t.pad;
     const int oi0 = own & 255, oi1 = own >> 8 & 255, oj0 = own >> 16 & 255, oj1 = own >> 24;
