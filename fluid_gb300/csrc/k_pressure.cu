@@ -2443,10 +2443,9 @@ static bool launch_jacobi_flow(cudaStream_t st, const Grid& g, PCtl* ctl, float*
   if (!dv || dv->flow_per_sm <= 0 || dv->sms <= 0) return false;
   const int ntx = (g.NY + OJ - 1) / OJ, nty = (g.NX + OI - 1) / OI;
   const int ntiles = ntx * nty;
-  // Below one tile per SM the per-launch kernels are faster (with every
-  // tile in flight at once the items wait on each other's flags: 128^2
-  // jet 68.3 against 64.6 us per step, 512x256 Karman street 138.5 against
-  // 121.7 us).
+  // Below one tile per SM the per-launch kernels were measured faster
+  // (128^2 jet 68.3 against 64.6 us per step, 512x256 Karman street 138.5
+  // against 121.7 us).
   if (ntiles < dv->sms) return false;
   CUtensorMap tm0, tm1, tmw, tmb;
   if (!encode_box_map(&tm0, x0, g.NX, g.P) || !encode_box_map(&tm1, x1, g.NX, g.P) ||
