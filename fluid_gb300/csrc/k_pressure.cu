@@ -1040,7 +1040,7 @@ static_assert(RI == kJacRegionRows && RJ == kJacRegionCols && TMAX == kJacHalo,
 // (garbage only on the region's outermost ring, which the halo absorbs),
 // sets bw = w * b_e, starts the correction from 0 and, when more launches
 // follow, writes b_e and bw_e of the owned cells to rhs_e / bwe.
-template <bool OMEGA1, bool FULL, bool CHECK, bool RINIT>
+template <bool OMEGA1, bool FULL, bool CHECK, bool RINIT, int NW = NWARP>
 __device__ __forceinline__ void jacobi_tile(
     int ri0, int rj0, uint32_t own, bool lead, const float* __restrict__ src, float* __restrict__ dst,
     const float* __restrict__ W, const float* __restrict__ BW, const float* __restrict__ rhs,
@@ -1048,8 +1048,8 @@ __device__ __forceinline__ void jacobi_tile(
     int out_sel, int zero_init, Grid g, const float* __restrict__ mphi0,
     const float* __restrict__ mphi1, const PCtl* __restrict__ mctl, float* __restrict__ rhs_e,
     float* __restrict__ bwe) {
-  __shared__ float4 xch[2][2][NWARP][32];
-  __shared__ float red[NWARP];
+  __shared__ float4 xch[2][2][NW][32];
+  __shared__ float red[NW];
   __shared__ int skip;
   pdl_enter();
   if (threadIdx.x == 0) {
@@ -1105,7 +1105,7 @@ __device__ __forceinline__ void jacobi_tile(
     xch[1][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
     __syncthreads();
     float4 u4 = warp > 0 ? xch[1][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 d4 = warp < NWARP - 1 ? xch[1][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 d4 = warp < NW - 1 ? xch[1][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
     float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
 #pragma unroll
     for (int r = 0; r < RT; ++r) {
@@ -1165,7 +1165,7 @@ __device__ __forceinline__ void jacobi_tile(
     xch[buf][1][warp][lane] = make_float4(x[RT - 1][0], x[RT - 1][1], x[RT - 1][2], x[RT - 1][3]);
     __syncthreads();
     float4 u4 = warp > 0 ? xch[buf][1][warp - 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 d4 = warp < NWARP - 1 ? xch[buf][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 d4 = warp < NW - 1 ? xch[buf][0][warp + 1][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
     float prev[JT] = {u4.x, u4.y, u4.z, u4.w};
 #pragma unroll
     for (int r = 0; r < RT; ++r) {
@@ -1248,7 +1248,7 @@ __device__ __forceinline__ void jacobi_tile(
     if (CHECK) {
       float m = 0.0f;
 #pragma unroll
-      for (int q = 0; q < NWARP; ++q) m = fmaxf(m, red[q]);
+      for (int q = 0; q < NW; ++q) m = fmaxf(m, red[q]);
       if (m > 0.0f) atomicMax(&ctl->slots[k], __float_as_uint(m));
     }
     if (lead) {
@@ -1259,8 +1259,10 @@ __device__ __forceinline__ void jacobi_tile(
   }
 }
 
-template <bool OMEGA1, bool FULL, bool CHECK, bool RINIT>
-__global__ void __launch_bounds__(TB_THREADS, 2)
+// NW warps (8, or 4 on grids with fewer 8-warp regions than SMs): a region
+// of 8 NW rows x 128 columns, so a small grid spreads over more SMs.
+template <bool OMEGA1, bool FULL, bool CHECK, bool RINIT, int NW = NWARP>
+__global__ void __launch_bounds__(32 * NW, 2 * NWARP / NW)
     k_jacobi_rb(const float* __restrict__ src, float* __restrict__ dst,
                 const float* __restrict__ W, const float* __restrict__ BW,
                 const float* __restrict__ rhs, const uint8_t* __restrict__ flags, float om1,
@@ -1268,12 +1270,13 @@ __global__ void __launch_bounds__(TB_THREADS, 2)
                 const float* __restrict__ mphi0, const float* __restrict__ mphi1,
                 const PCtl* __restrict__ mctl, float* __restrict__ rhs_e,
                 float* __restrict__ bwe) {
-  jacobi_tile<OMEGA1, FULL, CHECK, RINIT>((int)blockIdx.y * OI, (int)blockIdx.x * OJ,
-                                          span_own(blockIdx.y, g.NX, RI) |
-                                              span_own(blockIdx.x, g.NY, RJ) << 16,
-                                          blockIdx.x == 0 && blockIdx.y == 0, src, dst, W, BW,
-                                          rhs, flags, om1, ctl, k, t0, ns, tol, out_sel,
-                                          zero_init, g, mphi0, mphi1, mctl, rhs_e, bwe);
+  constexpr int R = NW * RT;  // region rows
+  jacobi_tile<OMEGA1, FULL, CHECK, RINIT, NW>((int)blockIdx.y * (R - 2 * TMAX), (int)blockIdx.x * OJ,
+                                              span_own(blockIdx.y, g.NX, R) |
+                                                  span_own(blockIdx.x, g.NY, RJ) << 16,
+                                              blockIdx.x == 0 && blockIdx.y == 0, src, dst, W,
+                                              BW, rhs, flags, om1, ctl, k, t0, ns, tol, out_sel,
+                                              zero_init, g, mphi0, mphi1, mctl, rhs_e, bwe);
 }
 
 // A batch's Jacobi launch k of L: scene s runs its nl_s = ceil(iters_s / T)
@@ -2494,6 +2497,11 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
   int used = FG_JACOBI_KERNEL_SWEEP;
   bool o1 = om1 == 0.0f;
   dim3 gr(span_count(g.NY, RJ), span_count(g.NX, RI));
+  // Grids with fewer 8-warp regions than SMs run every launch on 4-warp
+  // regions (half the rows), spread over twice the SMs.
+  const TmaDevice* dv = tma_ready(st);
+  const bool narrow = dv && dv->sms > 0 && (long long)gr.x * gr.y < dv->sms;
+  const dim3 gr4(span_count(g.NY, RJ), span_count(g.NX, RI / 2));
   int nlaunch = (int)(((long long)iters + T - 1) / T);
   int k0 = 0, kernels = 0;
   // Fixed sweep counts in full launches: the leading full phases as one
@@ -2518,15 +2526,19 @@ static cudaError_t enqueue_jacobi(cudaStream_t st, const Grid& g, PCtl* ctl, con
     const float* bk = rinit ? b : (mphi0 ? rhs_e : b);
     const float* bwk = mphi0 && k > 0 ? bwe : bw;
     float* re = rinit && nlaunch > 1 ? rhs_e : nullptr;
-    if (full && !check && !rinit && !mphi0 &&
+    if (full && !check && !rinit && !mphi0 && !narrow &&
         launch_jacobi_tma(st, g, ctl, src, dst, W, bwk, om1, o1, k, t0, sel, zi, err,
                           tma_stall_tile)) {
       if (used == FG_JACOBI_KERNEL_SWEEP) used = FG_JACOBI_KERNEL_TMA;
       continue;
     }
-#define FG_JAC(O, F, C, R)                                                                     \
-  launch_pdl(k_jacobi_rb<O, F, C, R>, gr, dim3(TB_THREADS), 0, st, src, dst, W, bwk, bk, flags, \
-             om1, ctl, k, t0, ns, tol, sel, zi, g, mphi0, mphi1, mctl, re, bwe)
+#define FG_JAC(O, F, C, R)                                                                      \
+  (narrow ? launch_pdl(k_jacobi_rb<O, F, C, R, NWARP / 2>, gr4, dim3(TB_THREADS / 2), 0, st, src, \
+                       dst, W, bwk, bk, flags, om1, ctl, k, t0, ns, tol, sel, zi, g, mphi0,     \
+                       mphi1, mctl, re, bwe)                                                    \
+          : launch_pdl(k_jacobi_rb<O, F, C, R>, gr, dim3(TB_THREADS), 0, st, src, dst, W, bwk, \
+                       bk, flags, om1, ctl, k, t0, ns, tol, sel, zi, g, mphi0, mphi1, mctl, re, \
+                       bwe))
     if (rinit) {
       if (o1) { if (full) FG_JAC(true, true, false, true); else FG_JAC(true, false, false, true); }
       else { if (full) FG_JAC(false, true, false, true); else FG_JAC(false, false, false, true); }

@@ -246,9 +246,9 @@ def test_jacobi_refinement_bitwise(gpu):
 @pytest.mark.parametrize("w,h", [(70, 45), (333, 222), (1100, 1500), (9000, 100), (300, 2700)])
 def test_jacobi_fixed_sweeps_bitwise(gpu, w, h):
     """Fixed sweep counts in full 8-sweep launches against the oracle, bit for
-    bit: the persistent kernel fed by tensor-memory-accelerator copies (70x45,
-    333x222) and the dataflow kernel (1100x1500: 322 tiles; 9000x100: one
-    tile column of 188 tiles; 300x2700: 7 tile rows of 25)."""
+    bit: the per-launch kernel on 4-warp regions (70x45, 333x222: fewer 8-warp
+    regions than SMs) and the dataflow kernel (1100x1500: 322 tiles; 9000x100:
+    one tile column of 188 tiles; 300x2700: 7 tile rows of 25)."""
     g, o = both(gpu, w, h, scheme=1, num_iters=40, tb_depth=8, early_exit=False, UseBFECC=True)
     for f in (g, o):
         scenes.jet_scene(f)

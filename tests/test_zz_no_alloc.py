@@ -89,6 +89,7 @@ def test_noalloc_projection_matches_handle_path_twice(env):
         # width, height, seed, iters, tb, early_exit, tolerance, dt
         (120, 90, 11, 40, 8, False, 1e-5, 0.1),
         (77, 133, 12, 200, 4, True, 0.1, 0.05),
+        (1000, 1000, 13, 16, 8, False, 1e-5, 0.1),  # 189 regions: the TMA-fed kernel
     ]
     for width, height, seed, iters, tb, ee, tol, dt in cases:
         inputs, want, sweeps = reference_projection(fluid_gb300, width, height, seed, iters, tb, ee,
@@ -139,12 +140,13 @@ def test_noalloc_allocates_nothing_and_rejects_oversize(env):
 def test_noalloc_reports_a_wait_that_gave_up(env):
     """A copy barrier that never completes (fault injection: tile 0 expects
     16 bytes more than its copies bring; no fault, every copy lands) makes
-    the TMA-fed Jacobi kernel's bounded wait give up.  The call itself
+    the TMA-fed Jacobi kernel's bounded wait give up (a 1000x1000 grid: at
+    least one 8-warp region per SM, where that kernel runs).  The call itself
     returns FG_OK (its work is still queued); fg_project_noalloc_status
     reports FG_ERR_TIMEOUT.  Disarmed, the next call is bit for bit the
     handle path's again, whatever the stalled call left in the scratch."""
     torch, fluid_gb300, L, _lib = env
-    width, height, seed, iters, tb = 120, 90, 31, 8, 8
+    width, height, seed, iters, tb = 1000, 1000, 31, 8, 8
     inputs, want, _ = reference_projection(fluid_gb300, width, height, seed, iters, tb, False,
                                            1e-5, 0.1)
     assert L.fg_debug_stall_tile(None, 0) == 0
