@@ -3055,18 +3055,24 @@ __global__ void __launch_bounds__(kMgFuseThreads)
 
 inline dim3 level_grid(const Grid& g) { return dim3((g.NY + BX - 1) / BX, (g.NX + BY - 1) / BY); }
 
-// ns (<= TMAX) damped Jacobi sweeps src -> dst on one level.
+// ns (<= TMAX) damped Jacobi sweeps src -> dst on one level (4-warp
+// regions on levels with fewer 8-warp regions than SMs, as enqueue_jacobi).
 void mg_sweeps(cudaStream_t st, const MgLevelDev& v, const float* src, float* dst, float om1,
                PCtl* ctl, int t0, int ns, int sel, int zero) {
   dim3 gr(span_count(v.g.NY, RJ), span_count(v.g.NX, RI));
-  if (ns == TMAX)
-    k_jacobi_rb<false, true, false, false><<<gr, TB_THREADS, 0, st>>>(
-        src, dst, v.w, v.bw, nullptr, v.flags, om1, ctl, 0, t0, ns, 0.0f, sel, zero, v.g, nullptr,
-        nullptr, nullptr, nullptr, nullptr);
-  else
-    k_jacobi_rb<false, false, false, false><<<gr, TB_THREADS, 0, st>>>(
-        src, dst, v.w, v.bw, nullptr, v.flags, om1, ctl, 0, t0, ns, 0.0f, sel, zero, v.g, nullptr,
-        nullptr, nullptr, nullptr, nullptr);
+  const TmaDevice* dv = tma_ready(st);
+  const bool narrow = dv && dv->sms > 0 && (long long)gr.x * gr.y < dv->sms;
+#define FG_MGJ(F, NW)                                                                           \
+  k_jacobi_rb<false, F, false, false, NW>                                                       \
+      <<<dim3(gr.x, span_count(v.g.NX, RT * NW)), 32 * NW, 0, st>>>(                            \
+          src, dst, v.w, v.bw, nullptr, v.flags, om1, ctl, 0, t0, ns, 0.0f, sel, zero, v.g,     \
+          nullptr, nullptr, nullptr, nullptr, nullptr)
+  if (narrow) {
+    if (ns == TMAX) FG_MGJ(true, NWARP / 2); else FG_MGJ(false, NWARP / 2);
+  } else {
+    if (ns == TMAX) FG_MGJ(true, NWARP); else FG_MGJ(false, NWARP);
+  }
+#undef FG_MGJ
 }
 
 // The V-cycles of one solve.  cur[l] names the buffer of level l holding
