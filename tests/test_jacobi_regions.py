@@ -3,8 +3,8 @@ fluid_gb300/csrc/fg_internal.cuh), used by the per-launch kernel and by
 batches: along an axis of n cells the regions' owned windows cover [0, n)
 once, in order; a region edge inside the grid keeps a halo of 8 cells, one at
 the grid's edge keeps none; column regions start on a multiple of 4 (16-byte
-vector loads); and the count is the least any placement of 64- or 128-cell
-regions with such halos needs.  The header's host side is compiled by nvcc
+vector loads); and the count is the least any placement of 32-, 64- or
+128-cell regions (4-warp rows, 8-warp rows, columns) with such halos needs.  The header's host side is compiled by nvcc
 into a small CPU program; no GPU is used."""
 import os
 import subprocess
@@ -20,7 +20,7 @@ using namespace fg;
 
 int main() {
   long long checked = 0;
-  for (int R : {kJacRegionRows, kJacRegionCols}) {
+  for (int R : {kJacRegionRows / 2, kJacRegionRows, kJacRegionCols}) {
     const int S = R - 2 * kJacHalo;
     for (int n = 1; n <= 5000; ++n) {
       const int cnt = span_count(n, R);
