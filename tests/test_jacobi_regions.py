@@ -4,8 +4,9 @@ batches: along an axis of n cells the regions' owned windows cover [0, n)
 once, in order; a region edge inside the grid keeps a halo of 8 cells, one at
 the grid's edge keeps none; column regions start on a multiple of 4 (16-byte
 vector loads); and the count is the least any placement of 32-, 64- or
-128-cell regions (4-warp rows, 8-warp rows, columns) with such halos needs.  The header's host side is compiled by nvcc
-into a small CPU program; no GPU is used."""
+128-cell regions (4-warp rows, 8-warp rows, columns) with such halos needs.
+The header's host side is compiled by nvcc into a small CPU program; no GPU
+is used."""
 import os
 import subprocess
 
