@@ -1,0 +1,73 @@
+"""bench.py's reference arm (`--impl reference`): the JSON line it prints, with
+the timed host steps replaced by fixed durations so that no 2048^2 step runs
+here.  The line must carry the keys the contract names (impl, metric, value,
+unit, steps, warmup, ms_per_step, config, cpu_baseline with its kind, cores
+and sample, an e2e block without host-device bytes), and ranks other than 0
+print nothing."""
+import argparse
+import json
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _args(**kw):
+    a = dict(gpus=1, steps=20, warmup=3, cpu_steps=2, cpu_budget=30.0)
+    a.update(kw)
+    return argparse.Namespace(**a)
+
+
+def _bench(monkeypatch):
+    sys.path.insert(0, ROOT)
+    import bench
+
+    calls = []
+
+    def fake_steps(steps, threads, warmup=0, budget_s=None):
+        calls.append((steps, threads, warmup, budget_s))
+        return [4.0] * steps
+
+    monkeypatch.setattr(bench, "cpu_reference_steps", fake_steps)
+    return bench, calls
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    bench, calls = _bench(monkeypatch)
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    bench.run_reference(_args())
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    (steps, threads, warmup, budget), = calls
+    assert steps == 2 and warmup == 3 and budget == 30.0 and threads == (os.cpu_count() or 1)
+    assert line["impl"] == "reference"
+    assert line["metric"] == bench.METRIC and line["unit"] == "Mcell-steps/s"
+    assert line["steps"] == 2 and line["warmup"] == 3 and line["higher_is_better"] is True
+    assert abs(line["ms_per_step"] - 4000.0) < 1e-9
+    assert abs(line["value"] - bench.W * bench.H / 4.0 / 1e6) < 1e-12
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] == threads and cb["value"] == line["value"]
+    assert "sample" in cb and cb["unit"] == line["unit"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    assert "workload" in line["config"]
+
+
+def test_reference_arm_warmup_and_steps_are_bounded(monkeypatch, capsys):
+    bench, calls = _bench(monkeypatch)
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    bench.run_reference(_args(steps=1, warmup=50, cpu_steps=9))
+    (steps, _, warmup, _), = calls
+    assert steps == 2 and warmup == 10  # at least 2 timed steps, at most 10 warm-up steps
+    capsys.readouterr()
+
+
+def test_reference_arm_other_ranks_print_nothing(monkeypatch, capsys):
+    bench, calls = _bench(monkeypatch)
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setenv("LOCAL_RANK", "1")
+    bench.run_reference(_args(gpus=2))
+    assert calls == [] and capsys.readouterr().out == ""
