@@ -1,9 +1,10 @@
-"""bench.py's reference arm (`--impl reference`): the JSON line it prints, with
-the timed host steps replaced by fixed durations so that no 2048^2 step runs
-here.  The line must carry the keys the contract names (impl, metric, value,
-unit, steps, warmup, ms_per_step, config, cpu_baseline with its kind, cores
-and sample, an e2e block without host-device bytes), and ranks other than 0
-print nothing."""
+"""bench.py without a GPU: the reference arm (`--impl reference`) and the
+roofline arithmetic of the main arm.  The reference arm's timed host steps
+are replaced by fixed durations so that no 2048^2 step runs here; its line
+must carry the keys the contract names (impl, metric, value, unit, steps,
+warmup, ms_per_step, config, cpu_baseline with its kind, cores and sample,
+an e2e block without host-device bytes), and ranks other than 0 print
+nothing."""
 import argparse
 import json
 import os
@@ -71,3 +72,44 @@ def test_reference_arm_other_ranks_print_nothing(monkeypatch, capsys):
     monkeypatch.setenv("LOCAL_RANK", "1")
     bench.run_reference(_args(gpus=2))
     assert calls == [] and capsys.readouterr().out == ""
+
+
+def test_step_roofline_arithmetic():
+    """The step roofline sums every stage's compulsory bytes per cell (597 B at
+    200 sweeps in 8-sweep phases) over the device-timed step, and each stage's
+    over its own time; fractions are of the given peak."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    n = 2050 * 2050
+    stages = {"pressure setup": 0.024, "jacobi sweeps": 0.44, "advect velocity": 0.105,
+              "sources+viscosity": 0.01}
+    r = bench.step_roofline(stages, n, 0.75, 6759.6)
+    assert r["bytes_per_cell"] == 597 == sum(bench.STAGE_BYTES_PER_CELL.values())
+    assert abs(r["achieved"] - 597 * n / 0.75e-3 / 1e9) < 1e-6
+    assert abs(r["frac"] - r["achieved"] / 6759.6) < 1e-12
+    # (a stage of 0 compulsory bytes has no fraction)
+    assert set(r["stages"]) == {"pressure setup", "jacobi sweeps", "advect velocity"}
+    js = r["stages"]["jacobi sweeps"]
+    assert js["bytes_per_cell"] == 16 * 25 and abs(js["gbs"] - 400 * n / 0.44e-3 / 1e9) < 1e-6
+
+
+def test_jacobi_roofline_is_an_hbm_fraction_and_issue_is_bounded():
+    """The dominant kernel's `frac` counts 16 compulsory bytes per cell per
+    8-sweep phase over the phase time: at the measured 17.4 us per phase it is
+    an HBM fraction below 1, while the per-sweep model (13 B per cell-sweep)
+    is reported beside it, above the peak, and not as `frac`; the issue
+    fraction from the committed ncu instruction count stays below 1."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    n = 2050 * 2050
+    tr = bench.committed_traffic()
+    r = bench.jacobi_roofline(n, 0.0174, 6759.6, "measured", tr,
+                              {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0})
+    assert abs(r["achieved"] - 16 * n / 17.4e-6 / 1e9) < 1e-6
+    assert 0.3 < r["frac"] < 1.0
+    assert r["per_sweep_model"]["ratio_to_peak"] > 1.0
+    assert r["bytes_per_launch"] == 16 * n
+    if tr and tr.get("warp_inst_per_phase"):
+        assert 0.0 < r["issue"]["frac"] < 1.0
