@@ -113,3 +113,28 @@ def test_jacobi_roofline_is_an_hbm_fraction_and_issue_is_bounded():
     assert r["bytes_per_launch"] == 16 * n
     if tr and tr.get("warp_inst_per_phase"):
         assert 0.0 < r["issue"]["frac"] < 1.0
+
+
+def test_clock_summary_reports_active_throttle_reasons():
+    """The clocks block of the bench line: the median SM clock of the samples
+    taken during the timed region, the maximum clock, and every throttle
+    reason seen active in any sample (malformed or unavailable lines are
+    skipped)."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    s = bench.ClockSampler(0)
+    s.lines = [
+        "2070, 2070, 910.2, Not Active, Not Active, Not Active, Not Active",
+        "2055, 2070, 1380.0, Not Active, Not Active, Not Active, Active",
+        "1980, 2070, 1400.0, Not Active, Not Active, Not Active, Active",
+        "[N/A], 2070, 0, Not Active, Not Active, Not Active, Not Active",
+        "garbage",
+    ]
+    c = s.summary()
+    assert c["samples"] == 3 and c["sm_mhz"] == 2055 and c["sm_max_mhz"] == 2070
+    assert c["reasons"] == ["sw_power_cap"]
+    s.lines = ["2070, 2070, 900, Not Active, Active, Not Active, Not Active"]
+    assert s.summary()["reasons"] == ["hw_thermal_slowdown"]
+    s.lines = []
+    assert s.summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
