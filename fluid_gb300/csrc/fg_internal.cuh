@@ -238,9 +238,9 @@ struct BCell {
   int pad[2];
 };
 static_assert(sizeof(BCell) == 64, "one 64-byte entry per block");
-// A per-launch Jacobi block (k_pressure.cu) sweeps a region of 64 rows x
-// 128 columns in registers and writes the cells of it that are exact after
-// its sweeps.  Inside the grid a region edge costs a halo of 8 cells; at the
+// A per-launch Jacobi block (k_pressure.cu) sweeps a region of 64 rows (8
+// warps; 32 with 4 warps on small grids) x 128 columns in registers and
+// writes the cells of it that are exact after its sweeps.  Inside the grid a region edge costs a halo of 8 cells; at the
 // grid's edge it costs none: the cells past the grid are zero and stay zero,
 // and the grid's outermost ring has w = bw = 0, so whatever a region-edge
 // thread reads beside it (a warp shuffle at lane 0 or 31 returns the
